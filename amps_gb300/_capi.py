@@ -1,0 +1,121 @@
+"""ctypes declarations of libamps_gpu.so (include/amps_gpu.h).
+
+The shared library is the product; this module only binds it.  Importing it
+fails loudly when the library has not been built: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libamps_gpu.so")
+
+MAX_SPECIES = 8
+
+STATUS = {
+    0: "OK",
+    1: "INVALID_ARG",
+    2: "OUT_OF_DOMAIN_PARTICLES",
+    3: "GMRES_NOT_CONVERGED",
+    4: "DEVICE_TIMEOUT",
+    5: "CUDA_ERROR",
+    6: "CAPACITY_EXCEEDED",
+    7: "NO_DEVICE",
+}
+
+
+class AmpsGpuError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__("%s (%d)%s" % (STATUS.get(status, "?"), status, (": " + msg) if msg else ""))
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("nbx", C.c_int), ("nby", C.c_int), ("nbz", C.c_int),
+        ("x0", C.c_double * 3), ("dx", C.c_double * 3),
+        ("nspec", C.c_int),
+        ("charge", C.c_double * MAX_SPECIES),
+        ("mass", C.c_double * MAX_SPECIES),
+        ("weight", C.c_double * MAX_SPECIES),
+        ("dt", C.c_double), ("theta", C.c_double),
+        ("particle_capacity", C.c_longlong),
+        ("track_ids", C.c_int), ("device", C.c_int),
+    ]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("converged", C.c_int),
+                ("rel_residual", C.c_double), ("wave_energy", C.c_double)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("solve", SolveStats), ("particle_energy", C.c_double),
+                ("out_of_block", C.c_longlong), ("ulp_face", C.c_longlong)]
+
+
+P = C.c_void_p
+D = C.POINTER(C.c_double)
+F = C.POINTER(C.c_float)
+U8 = C.POINTER(C.c_uint8)
+I32 = C.POINTER(C.c_int32)
+U32 = C.POINTER(C.c_uint32)
+I64 = C.POINTER(C.c_int64)
+LL = C.POINTER(C.c_longlong)
+
+# name -> (restype, argtypes); every symbol declared in include/amps_gpu.h
+SIGNATURES = {
+    "amps_gpu_create": (C.c_int, [C.POINTER(Config), C.POINTER(P)]),
+    "amps_gpu_destroy": (C.c_int, [P]),
+    "amps_gpu_last_error": (C.c_char_p, [P]),
+    "amps_gpu_get_stream": (C.c_int, [P, C.POINTER(P)]),
+    "amps_gpu_synchronize": (C.c_int, [P]),
+    "amps_gpu_import_particles": (C.c_int, [P, C.c_longlong, D, D, U8, D]),
+    "amps_gpu_import_particles_local": (C.c_int, [P, C.c_longlong, F, F, U8, I32]),
+    "amps_gpu_export_particles": (C.c_int, [P, D, D, U8, I32, I32, U32, LL]),
+    "amps_gpu_num_particles": (C.c_int, [P, LL]),
+    "amps_gpu_import_fields": (C.c_int, [P, D, D, D, D, D]),
+    "amps_gpu_export_fields": (C.c_int, [P, D, D, D, D, D]),
+    "amps_gpu_import_moments": (C.c_int, [P, D, D]),
+    "amps_gpu_export_moments": (C.c_int, [P, D, D]),
+    "amps_gpu_move_particles": (C.c_int, [P, LL]),
+    "amps_gpu_update_j_mass_matrix": (C.c_int, [P, D]),
+    "amps_gpu_field_solve": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(SolveStats)]),
+    "amps_gpu_step": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(StepStats)]),
+    "amps_gpu_push_deposit": (C.c_int, [P, D]),
+    "amps_gpu_set_kernel_timing": (C.c_int, [P, C.c_int]),
+    "amps_gpu_get_kernel_times": (C.c_int, [P, C.POINTER(C.c_char_p), D, LL, C.c_int,
+                                            C.POINTER(C.c_int)]),
+    "amps_gpu_reset_kernel_times": (C.c_int, [P]),
+    "amps_ic_count": (C.c_longlong, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "amps_ic_maxwellian": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, D,
+                                     C.c_ulonglong, C.c_int, F, F, U8, I32]),
+    "amps_gpu_trace_dipole": (C.c_int, [C.c_int, C.c_longlong, D, D, I32, I64, C.c_double,
+                                        C.c_double, C.c_double, C.c_double, D, C.c_double,
+                                        C.c_double, C.c_longlong, C.c_double, C.c_double,
+                                        C.c_int, LL, D]),
+}
+
+_lib = None
+
+
+def load():
+    """Load and bind libamps_gpu.so (raises if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libamps_gpu.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(a, ctype):
+    """numpy array -> ctypes pointer (None passes through)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(ctype))

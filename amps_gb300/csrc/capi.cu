@@ -1,0 +1,643 @@
+// C ABI of libamps_gpu.so: context lifetime, host<->device transfers, and the
+// step sequencing of PIC::TimeStep's ECSIM track (src/pic/pic_time_step.cpp:403-551).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+
+cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
+                               const uint8_t* d_spec_in, const double* d_wc, long long n);
+cudaError_t launch_import_local(amps_gpu_ctx* c, const int32_t* d_block, long long n);
+cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, int32_t* d_blk,
+                          int32_t* d_cel);
+cudaError_t launch_add(amps_gpu_ctx* c, const double* a, const double* b, double* o, long long n);
+
+// ---------------------------------------------------------------------------
+amps_gpu_status set_err(amps_gpu_ctx* c, amps_gpu_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+amps_gpu_status cuda_check(amps_gpu_ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return AMPS_GPU_OK;
+  return set_err(c, AMPS_GPU_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+struct Pending {
+  int slot;
+  cudaEvent_t a, b;
+  int nk;
+};
+// pending timed launches per context (kept outside the struct to keep it POD-light)
+std::vector<Pending>& pending(amps_gpu_ctx* c) {
+  static std::vector<std::pair<amps_gpu_ctx*, std::vector<Pending>>> tab;
+  for (auto& e : tab)
+    if (e.first == c) return e.second;
+  tab.emplace_back(c, std::vector<Pending>());
+  return tab.back().second;
+}
+
+cudaEvent_t take_event(amps_gpu_ctx* c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+}  // namespace
+
+TimedLaunch::TimedLaunch(amps_gpu_ctx* ctx, const char* name, int kernels)
+    : c(ctx), slot(-1), nk(kernels) {
+  if (!c->timing) return;
+  for (size_t i = 0; i < c->timers.size(); i++)
+    if (std::strcmp(c->timers[i].name, name) == 0) slot = (int)i;
+  if (slot < 0) {
+    KernelTimer t;
+    t.name = name;
+    c->timers.push_back(t);
+    slot = (int)c->timers.size() - 1;
+  }
+  a = take_event(c);
+  b = take_event(c);
+  cudaEventRecord(a, c->stream);
+}
+
+TimedLaunch::~TimedLaunch() {
+  if (slot < 0) return;
+  cudaEventRecord(b, c->stream);
+  pending(c).push_back(Pending{slot, a, b, nk});
+}
+
+void flush_timers(amps_gpu_ctx* c) {
+  auto& pv = pending(c);
+  if (pv.empty()) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& p : pv) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    c->timers[p.slot].ms += ms;
+    c->timers[p.slot].launches += p.nk;
+    c->ev_pool.push_back(p.a);
+    c->ev_pool.push_back(p.b);
+  }
+  pv.clear();
+}
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+  return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+}
+
+// host layout (interleaved, global periodic numbering) <-> device layout
+// (component-major, block-owned numbering)
+long long dev_of_host(const amps_gpu_config& g, long long hc) {
+  const int NX = 8 * g.nbx, NY = 8 * g.nby;
+  const int I = (int)(hc % NX), J = (int)((hc / NX) % NY), K = (int)(hc / ((long long)NX * NY));
+  const int b = (I / 8) + g.nbx * ((J / 8) + g.nby * (K / 8));
+  return (long long)b * 512 + (I % 8) + 8 * ((J % 8) + 8 * (K % 8));
+}
+
+std::vector<long long> host_perm(const amps_gpu_config& g, long long ncor) {
+  std::vector<long long> p((size_t)ncor);
+  for (long long h = 0; h < ncor; h++) p[(size_t)h] = dev_of_host(g, h);
+  return p;
+}
+
+amps_gpu_status upload_vec3(amps_gpu_ctx* c, const double* host, double* dev) {
+  if (!host) return AMPS_GPU_OK;
+  const long long n = c->ncor;
+  auto perm = host_perm(c->cfg, n);
+  std::vector<double> tmp((size_t)(3 * n));
+  for (long long h = 0; h < n; h++)
+    for (int d = 0; d < 3; d++) tmp[(size_t)(d * n + perm[(size_t)h])] = host[3 * h + d];
+  return cuda_check(c, cudaMemcpy(dev, tmp.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice),
+                    "upload field");
+}
+
+amps_gpu_status download_vec3(amps_gpu_ctx* c, const double* dev, double* host) {
+  if (!host) return AMPS_GPU_OK;
+  const long long n = c->ncor;
+  auto perm = host_perm(c->cfg, n);
+  std::vector<double> tmp((size_t)(3 * n));
+  amps_gpu_status s = cuda_check(
+      c, cudaMemcpy(tmp.data(), dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost), "download field");
+  if (s) return s;
+  for (long long h = 0; h < n; h++)
+    for (int d = 0; d < 3; d++) host[3 * h + d] = tmp[(size_t)(d * n + perm[(size_t)h])];
+  return AMPS_GPU_OK;
+}
+
+// staging buffers for FP64 particle import/export (allocated on first use)
+struct Staging {
+  double* x = nullptr;
+  double* v = nullptr;
+  double* wc = nullptr;
+  uint8_t* sp = nullptr;
+  int32_t* i0 = nullptr;
+  int32_t* i1 = nullptr;
+  long long cap = 0;
+};
+std::vector<std::pair<amps_gpu_ctx*, Staging>>& staging_tab() {
+  static std::vector<std::pair<amps_gpu_ctx*, Staging>> t;
+  return t;
+}
+Staging* staging(amps_gpu_ctx* c, long long need) {
+  auto& t = staging_tab();
+  Staging* s = nullptr;
+  for (auto& e : t)
+    if (e.first == c) s = &e.second;
+  if (!s) {
+    t.emplace_back(c, Staging());
+    s = &t.back().second;
+  }
+  if (s->cap < need) {
+    cudaFree(s->x); cudaFree(s->v); cudaFree(s->wc); cudaFree(s->sp); cudaFree(s->i0); cudaFree(s->i1);
+    s->cap = 0;
+    if (dalloc(&s->x, 3 * need) || dalloc(&s->v, 3 * need) || dalloc(&s->wc, need) ||
+        dalloc(&s->sp, need) || dalloc(&s->i0, need) || dalloc(&s->i1, need))
+      return nullptr;
+    s->cap = need;
+  }
+  return s;
+}
+void staging_free(amps_gpu_ctx* c) {
+  auto& t = staging_tab();
+  for (size_t i = 0; i < t.size(); i++)
+    if (t[i].first == c) {
+      Staging& s = t[i].second;
+      cudaFree(s.x); cudaFree(s.v); cudaFree(s.wc); cudaFree(s.sp); cudaFree(s.i0); cudaFree(s.i1);
+      t.erase(t.begin() + i);
+      return;
+    }
+}
+
+amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long* ulp) {
+  amps_gpu_status s = cuda_check(
+      c, cudaMemcpyAsync(c->h_flags, c->d_flags, 3 * sizeof(unsigned long long),
+                         cudaMemcpyDeviceToHost, c->stream),
+      "read flags");
+  if (s) return s;
+  s = cuda_check(c, cudaStreamSynchronize(c->stream), "synchronize");
+  if (s) return s;
+  if (out_of_block) *out_of_block = (long long)c->h_flags[0];
+  if (ulp) *ulp = (long long)c->h_flags[1];
+  if (c->h_flags[2]) {
+    return set_err(c, AMPS_GPU_DEVICE_TIMEOUT,
+                   "device reported " + std::to_string(c->h_flags[2]) +
+                       " bounded-wait timeouts or invalid particle records");
+  }
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status reset_flags(amps_gpu_ctx* c) {
+  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 3 * sizeof(unsigned long long), c->stream),
+                    "reset flags");
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) {
+  if (!cfg || !out) return AMPS_GPU_INVALID_ARG;
+  *out = nullptr;
+  if (cfg->nbx <= 0 || cfg->nby <= 0 || cfg->nbz <= 0 || cfg->nspec <= 0 ||
+      cfg->nspec > AMPS_GPU_MAX_SPECIES || cfg->dt <= 0.0 || cfg->theta <= 0.0 ||
+      cfg->particle_capacity < 0 || cfg->dx[0] <= 0 || cfg->dx[1] <= 0 || cfg->dx[2] <= 0)
+    return AMPS_GPU_INVALID_ARG;
+  for (int s = 0; s < cfg->nspec; s++)
+    if (cfg->mass[s] <= 0.0) return AMPS_GPU_INVALID_ARG;
+  long long nbl = (long long)cfg->nbx * cfg->nby * cfg->nbz;
+  if (nbl * 512 > (1LL << 30) || cfg->particle_capacity > (1LL << 31) - 1)
+    return AMPS_GPU_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return AMPS_GPU_NO_DEVICE;
+  if (cfg->device < 0 || cfg->device >= ndev) return AMPS_GPU_INVALID_ARG;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return AMPS_GPU_CUDA_ERROR;
+
+  amps_gpu_ctx* c = new amps_gpu_ctx();
+  c->cfg = *cfg;
+  c->nb = (int)nbl;
+  c->ncor = nbl * 512;
+  c->cap = cfg->particle_capacity;
+  const long long nc = c->ncor;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  bool ok = e == cudaSuccess;
+  ok = ok && !dalloc(&c->d_nbr, (size_t)c->nb * 27);
+  ok = ok && !dalloc(&c->d_En, 3 * nc) && !dalloc(&c->d_Eh, 3 * nc) && !dalloc(&c->d_Bc, 3 * nc) &&
+       !dalloc(&c->d_Bc2, 3 * nc) && !dalloc(&c->d_Bcor_prev, 3 * nc) &&
+       !dalloc(&c->d_Bcor_cur, 3 * nc) && !dalloc(&c->d_J, 3 * nc) && !dalloc(&c->d_M, 243 * nc);
+  ok = ok && !dalloc(&c->d_rhs, 3 * nc) && !dalloc(&c->d_x, 3 * nc) &&
+       !dalloc(&c->d_V, (size_t)(c->restart + 1) * 3 * nc) && !dalloc(&c->d_w, 3 * nc) &&
+       !dalloc(&c->d_dinv, 3 * nc) && !dalloc(&c->d_red, 12288);
+  ok = ok && cudaMallocHost(&c->h_red, 128 * sizeof(double)) == cudaSuccess;
+  ok = ok && !dalloc(&c->d_stencil_push, (size_t)c->nb * AMPS_SC * AMPS_PUSH_STRIDE) &&
+       !dalloc(&c->d_stencil_dep, (size_t)c->nb * AMPS_SC * AMPS_DEP_STRIDE);
+  for (int bsel = 0; bsel < 2 && ok; bsel++) {
+    for (int q = 0; q < 3; q++)
+      ok = ok && !dalloc(&c->d_u[bsel][q], c->cap) && !dalloc(&c->d_v[bsel][q], c->cap);
+    ok = ok && !dalloc(&c->d_sp[bsel], c->cap) && !dalloc(&c->d_wc[bsel], c->cap);
+    if (cfg->track_ids) ok = ok && !dalloc(&c->d_id[bsel], c->cap);
+  }
+  ok = ok && !dalloc(&c->d_key, c->cap) && !dalloc(&c->d_rank, c->cap) &&
+       !dalloc(&c->d_count, nc + 1) && !dalloc(&c->d_start, nc + 1) &&
+       !dalloc(&c->d_scan_part, (nc + 1) / 1024 + 2) && !dalloc(&c->d_flags, 4);
+  ok = ok && cudaMallocHost(&c->h_flags, 4 * sizeof(unsigned long long)) == cudaSuccess;
+  ok = ok && !dalloc(&c->d_cellM, 324 * nc) && !dalloc(&c->d_cellJ, 24 * nc) &&
+       !dalloc(&c->d_energy, 4);
+  ok = ok && cudaMallocHost(&c->h_energy, 4 * sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    amps_gpu_destroy(c);
+    return AMPS_GPU_CUDA_ERROR;
+  }
+  // periodic neighbour table
+  std::vector<int> nbr((size_t)c->nb * 27);
+  for (int b = 0; b < c->nb; b++) {
+    const int bx = b % cfg->nbx, by = (b / cfg->nbx) % cfg->nby, bz = b / (cfg->nbx * cfg->nby);
+    for (int oz = -1; oz <= 1; oz++)
+      for (int oy = -1; oy <= 1; oy++)
+        for (int ox = -1; ox <= 1; ox++) {
+          const int X = (bx + ox + cfg->nbx) % cfg->nbx, Y = (by + oy + cfg->nby) % cfg->nby,
+                    Z = (bz + oz + cfg->nbz) % cfg->nbz;
+          nbr[(size_t)b * 27 + nbr_slot(ox, oy, oz)] = X + cfg->nbx * (Y + cfg->nby * Z);
+        }
+  }
+  ok = cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice) ==
+       cudaSuccess;
+  ok = ok && cudaMemset(c->d_En, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+       cudaMemset(c->d_Eh, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+       cudaMemset(c->d_Bc, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+       cudaMemset(c->d_Bcor_prev, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+       cudaMemset(c->d_Bcor_cur, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+       cudaMemset(c->d_J, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+       cudaMemset(c->d_M, 0, sizeof(double) * 243 * nc) == cudaSuccess &&
+       cudaMemset(c->d_count, 0, sizeof(int) * (nc + 1)) == cudaSuccess &&
+       cudaMemset(c->d_start, 0, sizeof(int) * (nc + 1)) == cudaSuccess &&
+       cudaMemset(c->d_flags, 0, sizeof(unsigned long long) * 4) == cudaSuccess;
+  if (!ok) {
+    amps_gpu_destroy(c);
+    return AMPS_GPU_CUDA_ERROR;
+  }
+  *out = c;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  flush_timers(c);
+  staging_free(c);
+  void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
+                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
+                  c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_count,
+                  c->d_start, c->d_scan_part, c->d_flags, c->d_cellM, c->d_cellJ, c->d_energy};
+  for (void* p : ptrs) cudaFree(p);
+  for (int b = 0; b < 2; b++) {
+    for (int q = 0; q < 3; q++) {
+      cudaFree(c->d_u[b][q]);
+      cudaFree(c->d_v[b][q]);
+    }
+    cudaFree(c->d_sp[b]);
+    cudaFree(c->d_wc[b]);
+    cudaFree(c->d_id[b]);
+  }
+  if (c->h_red) cudaFreeHost(c->h_red);
+  if (c->h_flags) cudaFreeHost(c->h_flags);
+  if (c->h_energy) cudaFreeHost(c->h_energy);
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return AMPS_GPU_OK;
+}
+
+const char* amps_gpu_last_error(const amps_gpu_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+amps_gpu_status amps_gpu_get_stream(amps_gpu_ctx* c, void** stream) {
+  if (!c || !stream) return AMPS_GPU_INVALID_ARG;
+  *stream = (void*)c->stream;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_synchronize(amps_gpu_ctx* c) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  return cuda_check(c, cudaStreamSynchronize(c->stream), "synchronize");
+}
+
+amps_gpu_status amps_gpu_import_particles(amps_gpu_ctx* c, long long n, const double* x,
+                                          const double* v, const uint8_t* spec,
+                                          const double* wcorr) {
+  if (!c || n < 0 || (n > 0 && (!x || !v || !spec)))
+    return set_err(c, AMPS_GPU_INVALID_ARG, "import_particles: bad arguments");
+  if (n > c->cap) return set_err(c, AMPS_GPU_CAPACITY_EXCEEDED, "import_particles: n > capacity");
+  cudaSetDevice(c->cfg.device);
+  Staging* s = staging(c, std::max(n, 1LL));
+  if (!s) return set_err(c, AMPS_GPU_CUDA_ERROR, "import_particles: staging allocation failed");
+  c->has_wcorr = wcorr != nullptr;
+  amps_gpu_status st = reset_flags(c);
+  if (st) return st;
+  cudaStream_t q = c->stream;
+  if (n > 0) {
+    if ((st = cuda_check(c, cudaMemcpyAsync(s->x, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, q), "H2D x")) ||
+        (st = cuda_check(c, cudaMemcpyAsync(s->v, v, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, q), "H2D v")) ||
+        (st = cuda_check(c, cudaMemcpyAsync(s->sp, spec, n, cudaMemcpyHostToDevice, q), "H2D spec")))
+      return st;
+    if (wcorr && (st = cuda_check(c, cudaMemcpyAsync(s->wc, wcorr, sizeof(double) * n, cudaMemcpyHostToDevice, q), "H2D wcorr")))
+      return st;
+  }
+  st = cuda_check(c, launch_import_fp64(c, s->x, s->v, s->sp, wcorr ? s->wc : nullptr, n), "import");
+  if (st) return st;
+  return check_flags(c, nullptr, nullptr);
+}
+
+amps_gpu_status amps_gpu_import_particles_local(amps_gpu_ctx* c, long long n, const float* u,
+                                                const float* v, const uint8_t* spec,
+                                                const int32_t* block) {
+  if (!c || n < 0 || (n > 0 && (!u || !v || !spec || !block)))
+    return set_err(c, AMPS_GPU_INVALID_ARG, "import_particles_local: bad arguments");
+  if (n > c->cap) return set_err(c, AMPS_GPU_CAPACITY_EXCEEDED, "import_particles_local: n > capacity");
+  cudaSetDevice(c->cfg.device);
+  Staging* s = staging(c, std::max(n, 1LL));
+  if (!s) return set_err(c, AMPS_GPU_CUDA_ERROR, "staging allocation failed");
+  c->has_wcorr = false;
+  amps_gpu_status st = reset_flags(c);
+  if (st) return st;
+  const int cur = c->cur;
+  cudaStream_t q = c->stream;
+  if (n > 0) {
+    // de-interleave on the host into the SoA buffers
+    std::vector<float> tmp((size_t)n);
+    for (int d = 0; d < 3; d++) {
+      for (long long p = 0; p < n; p++) tmp[(size_t)p] = u[3 * p + d];
+      if ((st = cuda_check(c, cudaMemcpy(c->d_u[cur][d], tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "H2D u")))
+        return st;
+      for (long long p = 0; p < n; p++) tmp[(size_t)p] = v[3 * p + d];
+      if ((st = cuda_check(c, cudaMemcpy(c->d_v[cur][d], tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "H2D v")))
+        return st;
+    }
+    if ((st = cuda_check(c, cudaMemcpyAsync(c->d_sp[cur], spec, n, cudaMemcpyHostToDevice, q), "H2D spec")) ||
+        (st = cuda_check(c, cudaMemcpyAsync(s->i0, block, sizeof(int32_t) * n, cudaMemcpyHostToDevice, q), "H2D block")))
+      return st;
+  }
+  st = cuda_check(c, launch_import_local(c, s->i0, n), "import_local");
+  if (st) return st;
+  return check_flags(c, nullptr, nullptr);
+}
+
+amps_gpu_status amps_gpu_num_particles(amps_gpu_ctx* c, long long* n) {
+  if (!c || !n) return AMPS_GPU_INVALID_ARG;
+  *n = c->np;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_export_particles(amps_gpu_ctx* c, double* x, double* v, uint8_t* spec,
+                                          int32_t* block, int32_t* cell, uint32_t* id,
+                                          long long* n) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  const long long np = c->np;
+  if (n) *n = np;
+  if (np == 0) return AMPS_GPU_OK;
+  Staging* s = staging(c, np);
+  if (!s) return set_err(c, AMPS_GPU_CUDA_ERROR, "staging allocation failed");
+  amps_gpu_status st = cuda_check(
+      c, launch_export(c, x ? s->x : nullptr, v ? s->v : nullptr, block ? s->i0 : nullptr,
+                       cell ? s->i1 : nullptr),
+      "export");
+  if (st) return st;
+  cudaStream_t q = c->stream;
+  const int cur = c->cur;
+  if (x && (st = cuda_check(c, cudaMemcpyAsync(x, s->x, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, q), "D2H x"))) return st;
+  if (v && (st = cuda_check(c, cudaMemcpyAsync(v, s->v, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, q), "D2H v"))) return st;
+  if (block && (st = cuda_check(c, cudaMemcpyAsync(block, s->i0, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, q), "D2H block"))) return st;
+  if (cell && (st = cuda_check(c, cudaMemcpyAsync(cell, s->i1, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, q), "D2H cell"))) return st;
+  if (spec && (st = cuda_check(c, cudaMemcpyAsync(spec, c->d_sp[cur], np, cudaMemcpyDeviceToHost, q), "D2H spec"))) return st;
+  if (id) {
+    if (!c->cfg.track_ids) return set_err(c, AMPS_GPU_INVALID_ARG, "export: ids not tracked");
+    if ((st = cuda_check(c, cudaMemcpyAsync(id, c->d_id[cur], sizeof(uint32_t) * np, cudaMemcpyDeviceToHost, q), "D2H id"))) return st;
+  }
+  return cuda_check(c, cudaStreamSynchronize(q), "export sync");
+}
+
+amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* c, const double* E_n, const double* E_half,
+                                       const double* B_center, const double* B_corner_prev,
+                                       const double* B_corner_cur) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  cudaStreamSynchronize(c->stream);
+  amps_gpu_status s;
+  if ((s = upload_vec3(c, E_n, c->d_En)) || (s = upload_vec3(c, E_half, c->d_Eh)) ||
+      (s = upload_vec3(c, B_center, c->d_Bc)) || (s = upload_vec3(c, B_corner_prev, c->d_Bcor_prev)) ||
+      (s = upload_vec3(c, B_corner_cur, c->d_Bcor_cur)))
+    return s;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* c, double* E_n, double* E_half,
+                                       double* B_center, double* B_corner_prev,
+                                       double* B_corner_cur) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  if (s) return s;
+  if ((s = download_vec3(c, c->d_En, E_n)) || (s = download_vec3(c, c->d_Eh, E_half)) ||
+      (s = download_vec3(c, c->d_Bc, B_center)) ||
+      (s = download_vec3(c, c->d_Bcor_prev, B_corner_prev)) ||
+      (s = download_vec3(c, c->d_Bcor_cur, B_corner_cur)))
+    return s;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* c, const double* J, const double* M) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  cudaStreamSynchronize(c->stream);
+  amps_gpu_status s = upload_vec3(c, J, c->d_J);
+  if (s) return s;
+  if (M) {
+    const long long n = c->ncor;
+    auto perm = host_perm(c->cfg, n);
+    std::vector<double> tmp((size_t)(243 * n));
+    for (long long h = 0; h < n; h++)
+      for (int e = 0; e < 243; e++) tmp[(size_t)(e * n + perm[(size_t)h])] = M[243 * h + e];
+    s = cuda_check(c, cudaMemcpy(c->d_M, tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice),
+                   "upload M");
+    if (s) return s;
+  }
+  c->have_moments = true;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  if (s) return s;
+  s = download_vec3(c, c->d_J, J);
+  if (s) return s;
+  if (M) {
+    const long long n = c->ncor;
+    auto perm = host_perm(c->cfg, n);
+    std::vector<double> tmp((size_t)(243 * n));
+    s = cuda_check(c, cudaMemcpy(tmp.data(), c->d_M, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost),
+                   "download M");
+    if (s) return s;
+    for (long long h = 0; h < n; h++)
+      for (int e = 0; e < 243; e++) M[243 * h + e] = tmp[(size_t)(e * n + perm[(size_t)h])];
+  }
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* c, long long* out_of_block) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s;
+  if ((s = reset_flags(c))) return s;
+  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+    return s;
+  if ((s = cuda_check(c, launch_push(c), "push"))) return s;
+  if ((s = cuda_check(c, launch_rebin(c), "rebin"))) return s;
+  return check_flags(c, out_of_block, nullptr);
+}
+
+amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* c, double* particle_energy) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s;
+  if ((s = reset_flags(c))) return s;
+  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+    return s;
+  if ((s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
+                                         cudaMemcpyDeviceToHost, c->stream), "energy")))
+    return s;
+  if ((s = check_flags(c, nullptr, nullptr))) return s;
+  if (particle_energy) *particle_energy = c->h_energy[0];
+  c->have_moments = true;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* c, double* particle_energy) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s;
+  if ((s = reset_flags(c))) return s;
+  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+    return s;
+  if ((s = cuda_check(c, launch_push(c), "push"))) return s;
+  if ((s = cuda_check(c, launch_rebin(c), "rebin"))) return s;
+  if ((s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+  if (particle_energy) {
+    if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
+                                           cudaMemcpyDeviceToHost, c->stream), "energy")))
+      return s;
+  }
+  if ((s = check_flags(c, nullptr, nullptr))) return s;
+  if (particle_energy) *particle_energy = c->h_energy[0];
+  c->have_moments = true;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
+                                     amps_gpu_solve_stats* stats) {
+  if (!c || tol <= 0.0 || maxit <= 0 || precond < 0 || precond > 1)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "field_solve: bad arguments");
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s;
+  amps_gpu_solve_stats st{};
+  if ((s = cuda_check(c, launch_rhs(c), "rhs"))) return s;
+  amps_gpu_status gs = gmres_solve(c, tol, maxit, precond, &st);
+  if (gs != AMPS_GPU_OK && gs != AMPS_GPU_GMRES_NOT_CONVERGED) return gs;
+  // ProcessFinalSolution: E^{n+theta} = E^n + dE
+  if ((s = cuda_check(c, launch_add(c, c->d_En, c->d_x, c->d_Eh, 3 * c->ncor), "E_half"))) return s;
+  if ((s = cuda_check(c, launch_update_b(c), "update_b"))) return s;
+  std::swap(c->d_Bc, c->d_Bc2);
+  std::swap(c->d_Bcor_prev, c->d_Bcor_cur);
+  if ((s = cuda_check(c, launch_c2n(c, c->d_Bc, c->d_Bcor_cur), "c2n"))) return s;
+  if ((s = cuda_check(c, launch_update_e(c), "update_e"))) return s;
+  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy + 1, c->d_energy + 1, sizeof(double),
+                                         cudaMemcpyDeviceToHost, c->stream), "wave energy")))
+    return s;
+  if ((s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync"))) return s;
+  st.wave_energy = c->h_energy[1];
+  if (stats) *stats = st;
+  if (gs == AMPS_GPU_GMRES_NOT_CONVERGED)
+    return set_err(c, gs, "GMRES did not converge: iterations " + std::to_string(st.iterations) +
+                              ", relative residual " + std::to_string(st.rel_residual));
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_step(amps_gpu_ctx* c, double tol, int maxit, int precond,
+                              amps_gpu_step_stats* stats) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  amps_gpu_status s;
+  amps_gpu_step_stats st{};
+  if (!c->have_moments) {
+    if ((s = amps_gpu_update_j_mass_matrix(c, nullptr))) return s;
+  }
+  amps_gpu_status fs = amps_gpu_field_solve(c, tol, maxit, precond, &st.solve);
+  if (fs != AMPS_GPU_OK && fs != AMPS_GPU_GMRES_NOT_CONVERGED) return fs;
+  if ((s = reset_flags(c))) return s;
+  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+    return s;
+  if ((s = cuda_check(c, launch_push(c), "push"))) return s;
+  if ((s = cuda_check(c, launch_rebin(c), "rebin"))) return s;
+  if ((s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
+                                         cudaMemcpyDeviceToHost, c->stream), "energy")))
+    return s;
+  if ((s = check_flags(c, &st.out_of_block, &st.ulp_face))) return s;
+  st.particle_energy = c->h_energy[0];
+  c->have_moments = true;
+  if (stats) *stats = st;
+  return fs;
+}
+
+amps_gpu_status amps_gpu_set_kernel_timing(amps_gpu_ctx* c, int enable) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  flush_timers(c);
+  c->timing = enable != 0;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_get_kernel_times(amps_gpu_ctx* c, const char** names, double* total_ms,
+                                          long long* launches, int cap, int* n) {
+  if (!c || !n) return AMPS_GPU_INVALID_ARG;
+  flush_timers(c);
+  int k = 0;
+  for (auto& t : c->timers) {
+    if (k >= cap) break;
+    if (names) names[k] = t.name;
+    if (total_ms) total_ms[k] = t.ms;
+    if (launches) launches[k] = t.launches;
+    k++;
+  }
+  *n = k;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_reset_kernel_times(amps_gpu_ctx* c) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  flush_timers(c);
+  for (auto& t : c->timers) {
+    t.ms = 0.0;
+    t.launches = 0;
+  }
+  return AMPS_GPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+// Shared declarations of libamps_gpu.so: device context, launch helpers,
+// block-structured index arithmetic.
+//
+// Data layout in HBM (one context = one periodic mesh of 8^3-cell blocks)
+//   blocks own their 512 low corners and 512 cells: corner id = b*512 + i + 8j + 64k
+//   FP64 vectors are component-major: v[comp*ncor + corner]
+//   mass matrix M: 243 coefficient planes, M[e*ncor + corner] (coalesced per plane)
+//   particles: FP32 SoA (u: block-local offset in cell units, v), species byte,
+//              optional 32-bit id; sorted by key = block*512 + cell
+//   per-block FP32 field stencils (9^3 corners incl. the +1 halo) for the push
+//   and deposit kernels, contiguous per block so one bulk TMA copy stages them.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/amps_gpu.h"
+
+#define AMPS_NC 8
+#define AMPS_CPB 512        // cells (and owned corners) per block
+#define AMPS_SC 729         // stencil corners per block (9^3)
+#define AMPS_PUSH_STRIDE 8  // floats per stencil corner for the push: E3 B3 pad2
+#define AMPS_DEP_STRIDE 4   // floats per stencil corner for the deposit: B3 pad1
+
+struct KernelTimer {
+  const char* name;
+  double ms = 0.0;
+  long long launches = 0;
+};
+
+struct amps_gpu_ctx {
+  amps_gpu_config cfg;
+  int nb = 0;               // blocks
+  long long ncor = 0;       // owned corners == cells
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // mesh
+  int* d_nbr = nullptr;     // [nb*27] neighbour block, slot (di+1)+3(dj+1)+9(dk+1)
+
+  // fields (FP64, component-major)
+  double* d_En = nullptr;
+  double* d_Eh = nullptr;
+  double* d_Bc = nullptr;       // centre B^n (current)
+  double* d_Bc2 = nullptr;      // scratch for B^{n+1}
+  double* d_Bcor_prev = nullptr;
+  double* d_Bcor_cur = nullptr;
+  double* d_J = nullptr;        // 3*ncor
+  double* d_M = nullptr;        // 243*ncor
+  bool have_moments = false;
+
+  // GMRES workspace
+  double* d_rhs = nullptr;
+  double* d_x = nullptr;
+  double* d_V = nullptr;        // (restart+1) * n
+  double* d_w = nullptr;
+  double* d_dinv = nullptr;
+  double* d_red = nullptr;      // partial reductions
+  double* h_red = nullptr;      // pinned
+  int restart = 30;
+
+  // per-block FP32 stencils
+  float* d_stencil_push = nullptr;  // nb * 729 * 8
+  float* d_stencil_dep = nullptr;   // nb * 729 * 4
+
+  // particles (double-buffered SoA)
+  long long cap = 0, np = 0;
+  float* d_u[2][3] = {{nullptr}};
+  float* d_v[2][3] = {{nullptr}};
+  uint8_t* d_sp[2] = {nullptr, nullptr};
+  float* d_wc[2] = {nullptr, nullptr};  // optional weight correction
+  uint32_t* d_id[2] = {nullptr, nullptr};
+  int cur = 0;
+  bool has_wcorr = false;
+  int32_t* d_key = nullptr;     // destination key per particle
+  int32_t* d_rank = nullptr;    // rank inside the destination cell
+  int32_t* d_count = nullptr;   // ncor+1
+  int32_t* d_start = nullptr;   // ncor+1 (exclusive scan)
+  int32_t* d_scan_part = nullptr;
+  unsigned long long* d_flags = nullptr;  // [0] out-of-block, [1] ulp-face, [2] bad
+  unsigned long long* h_flags = nullptr;  // pinned
+
+  // deposition scratch: per-cell partial sums
+  float* d_cellM = nullptr;     // ncor * 324
+  float* d_cellJ = nullptr;     // ncor * 24
+  double* d_energy = nullptr;   // [0] particle, [1] wave
+  double* h_energy = nullptr;   // pinned
+
+  // timing
+  bool timing = false;
+  std::vector<KernelTimer> timers;
+  std::vector<cudaEvent_t> ev_pool;
+};
+
+// ---- error helpers ----
+amps_gpu_status set_err(amps_gpu_ctx* c, amps_gpu_status s, const std::string& msg);
+amps_gpu_status cuda_check(amps_gpu_ctx* c, cudaError_t e, const char* what);
+
+// Brackets a launch with CUDA events on the context stream when timing is on.
+struct TimedLaunch {
+  amps_gpu_ctx* c;
+  int slot;
+  cudaEvent_t a = nullptr, b = nullptr;
+  int nk = 1;
+  TimedLaunch(amps_gpu_ctx* ctx, const char* name, int kernels = 1);
+  ~TimedLaunch();
+};
+void flush_timers(amps_gpu_ctx* c);
+
+// ---- kernel launchers (particles.cu) ----
+cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
+                                 const double* Bcur);
+cudaError_t launch_push(amps_gpu_ctx* c);
+cudaError_t launch_rebin(amps_gpu_ctx* c);
+cudaError_t launch_deposit(amps_gpu_ctx* c);
+
+// ---- field launchers (field.cu) ----
+cudaError_t launch_rhs(amps_gpu_ctx* c);
+cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
+cudaError_t launch_jacobi_diag(amps_gpu_ctx* c);
+cudaError_t launch_update_b(amps_gpu_ctx* c);
+cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor);
+cudaError_t launch_update_e(amps_gpu_ctx* c);
+amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
+                            amps_gpu_solve_stats* st);
+
+// ---- device helpers ----
+__host__ __device__ inline int nbr_slot(int ox, int oy, int oz) {
+  return (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
+}
+
+// Corner (or cell) id of block-local index (i,j,k) in [-8,16): follows the
+// neighbour table for indices outside [0,8).
+__device__ __forceinline__ int local_id(const int* __restrict__ nbr, int b, int i, int j, int k) {
+  int ox = (i < 0) ? -1 : ((i >= AMPS_NC) ? 1 : 0);
+  int oy = (j < 0) ? -1 : ((j >= AMPS_NC) ? 1 : 0);
+  int oz = (k < 0) ? -1 : ((k >= AMPS_NC) ? 1 : 0);
+  int bb = (ox | oy | oz) ? __ldg(nbr + b * 27 + nbr_slot(ox, oy, oz)) : b;
+  return bb * AMPS_CPB + (i - AMPS_NC * ox) + AMPS_NC * ((j - AMPS_NC * oy) + AMPS_NC * (k - AMPS_NC * oz));
+}
+
+// 27-slot index of offset (di,dj,dk): digits {0,-1,+1} -> {0,1,2}
+__host__ __device__ inline int mm_slot(int di, int dj, int dk) {
+  auto dig = [](int o) { return o == 0 ? 0 : (o < 0 ? 1 : 2); };
+  return dig(di) + 3 * dig(dj) + 9 * dig(dk);
+}

@@ -1,0 +1,607 @@
+// ECSIM field solve on sm_103a, FP64 throughout.
+//
+//   k_rhs       UpdateRhs with the supports registered by GetStencil
+//               (src/pic/ecsim/get_stencil.cpp:1260-1599, ecsim/update_rhs.cpp:285):
+//               theta c dt curl B^n - 4 pi theta dt J - (theta c dt)^2 curlcurl E^n
+//               - 4 pi theta dt M E^n
+//   k_matvec    the assembled row of GetStencil valued by UpdateMatrixElement
+//               (pic_field_solver_ecsim.cpp:6004-6019) applied matrix-free:
+//               A = I + (theta c dt)^2 (grad div - lap) + 4 pi theta dt M
+//               (replaces cLinearSystemCornerNode::MultiplyVector,
+//               srcInterface/LinearSystemCornerNode.h:3067-3205)
+//   GMRES       restarted GMRES(30), x0 = 0, right Jacobi preconditioner
+//               optional, classical Gram-Schmidt with one re-orthogonalisation;
+//               each Arnoldi step is matvec + three fused sweep/reduction
+//               kernels with FP64 warp-shuffle reductions
+//               (the external linear_solver_wrapper of LinearSystemCornerNode.h:3282)
+//   k_update_b  UpdateB (:5160-5711), k_c2n InterpolateB_C2N (:5715),
+//   k_update_e  UpdateE with the wave-energy sum (:5909-6001)
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr int kMaxV = 32;
+constexpr int kRedBlocks = 304;  // 2 x 152 SMs
+
+struct Taps {
+  double K[3][3][27];  // operator taps without the mass matrix
+  double f;            // 4 pi theta dt
+};
+
+double tap_s(int o) { return o == 0 ? 0.5 : 0.25; }
+double tap_d2(int o) { return o == 0 ? -2.0 : 1.0; }
+double tap_d1(int o) { return o == 0 ? 0.0 : (o > 0 ? 0.5 : -0.5); }
+
+// Separable form of the compact stencils built by InitDiscritizationStencil
+// (pic_field_solver_ecsim.cpp:7121): d2/dx2 = D2(x) S(y) S(z),
+// d2/dxdy = D1(x) D1(y) S(z), with S = (1/4, 1/2, 1/4), D2 = (1,-2,1), D1 = (-1/2,0,1/2).
+Taps make_taps(const amps_gpu_config& cfg, bool identity) {
+  Taps t{};
+  double coeff[3], cs[3];
+  for (int d = 0; d < 3; d++) {
+    coeff[d] = cfg.dt / cfg.dx[d] * cfg.theta;
+    cs[d] = coeff[d] * coeff[d];
+  }
+  for (int dk = -1; dk <= 1; dk++)
+    for (int dj = -1; dj <= 1; dj++)
+      for (int di = -1; di <= 1; di++) {
+        const int o[3] = {di, dj, dk};
+        const int s = mm_slot(di, dj, dk);
+        double lap[3];
+        for (int ax = 0; ax < 3; ax++) {
+          double a = 1.0;
+          for (int d = 0; d < 3; d++) a *= (d == ax) ? tap_d2(o[d]) : tap_s(o[d]);
+          lap[ax] = a;
+        }
+        for (int p = 0; p < 3; p++)
+          for (int q = 0; q < 3; q++) {
+            double gd;
+            if (p == q) {
+              gd = lap[p];
+            } else {
+              gd = 1.0;
+              for (int d = 0; d < 3; d++) gd *= (d == p || d == q) ? tap_d1(o[d]) : tap_s(o[d]);
+            }
+            double a = 0.0;
+            if (p == q) {
+              for (int d = 0; d < 3; d++) a -= lap[d] * cs[d];
+              if (s == 0 && identity) a += 1.0;
+            }
+            a += gd * coeff[p] * coeff[q];
+            t.K[p][q][s] = a;
+          }
+      }
+  t.f = 4.0 * kPi * cfg.dt * cfg.theta;
+  return t;
+}
+
+__device__ __forceinline__ void corner_ijk(long long c, int& b, int& i, int& j, int& k) {
+  b = (int)(c / AMPS_CPB);
+  const int l = (int)(c % AMPS_CPB);
+  i = l & 7;
+  j = (l >> 3) & 7;
+  k = l >> 6;
+}
+
+// y = A (dinv .* x)   (dinv may be null)
+__global__ void __launch_bounds__(256) k_matvec(long long ncor, const int* __restrict__ nbr,
+                                                const double* __restrict__ M,
+                                                const double* __restrict__ x,
+                                                const double* __restrict__ dinv,
+                                                double* __restrict__ y, Taps T) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  int b, i, j, k;
+  corner_ijk(c, b, i, j, k);
+  double y0 = 0.0, y1 = 0.0, y2 = 0.0;
+#pragma unroll 1
+  for (int s = 0; s < 27; s++) {
+    const int dig[3] = {s % 3, (s / 3) % 3, s / 9};
+    const int di = dig[0] == 0 ? 0 : (dig[0] == 1 ? -1 : 1);
+    const int dj = dig[1] == 0 ? 0 : (dig[1] == 1 ? -1 : 1);
+    const int dk = dig[2] == 0 ? 0 : (dig[2] == 1 ? -1 : 1);
+    const int nb = local_id(nbr, b, i + di, j + dj, k + dk);
+    double xv[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      xv[q] = x[q * ncor + nb];
+      if (dinv) xv[q] *= dinv[q * ncor + nb];
+    }
+    const double* Ms = M + (size_t)(9 * s) * ncor + c;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      y0 += (T.K[0][q][s] + T.f * Ms[(size_t)(0 + q) * ncor]) * xv[q];
+      y1 += (T.K[1][q][s] + T.f * Ms[(size_t)(3 + q) * ncor]) * xv[q];
+      y2 += (T.K[2][q][s] + T.f * Ms[(size_t)(6 + q) * ncor]) * xv[q];
+    }
+  }
+  y[c] = y0;
+  y[ncor + c] = y1;
+  y[2 * ncor + c] = y2;
+}
+
+__global__ void __launch_bounds__(256) k_rhs(long long ncor, const int* __restrict__ nbr,
+                                             const double* __restrict__ M,
+                                             const double* __restrict__ En,
+                                             const double* __restrict__ Bc,
+                                             const double* __restrict__ J,
+                                             double* __restrict__ rhs, Taps T, double c4x,
+                                             double c4y, double c4z) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  int b, i, j, k;
+  corner_ijk(c, b, i, j, k);
+  double r[3] = {0.0, 0.0, 0.0};
+#pragma unroll 1
+  for (int s = 0; s < 27; s++) {
+    const int dig[3] = {s % 3, (s / 3) % 3, s / 9};
+    const int di = dig[0] == 0 ? 0 : (dig[0] == 1 ? -1 : 1);
+    const int dj = dig[1] == 0 ? 0 : (dig[1] == 1 ? -1 : 1);
+    const int dk = dig[2] == 0 ? 0 : (dig[2] == 1 ? -1 : 1);
+    const int nb = local_id(nbr, b, i + di, j + dj, k + dk);
+    double ev[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) ev[q] = En[q * ncor + nb];
+    const double* Ms = M + (size_t)(9 * s) * ncor + c;
+#pragma unroll
+    for (int p = 0; p < 3; p++)
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        r[p] -= (T.K[p][q][s] + T.f * Ms[(size_t)(3 * p + q) * ncor]) * ev[q];
+  }
+#pragma unroll
+  for (int p = 0; p < 3; p++) r[p] -= T.f * J[p * ncor + c];
+  // curl B^n from the 2x2 face averages of the 8 cells around the corner
+  auto Bv = [&](int ii, int jj, int kk, int comp) {
+    return Bc[comp * ncor + local_id(nbr, b, ii, jj, kk)];
+  };
+  double cb0 = 0.0, cb1 = 0.0, cb2 = 0.0;
+  for (int a = -1; a <= 0; a++)
+    for (int q = -1; q <= 0; q++) {
+      cb0 += c4y * (Bv(i + a, j, k + q, 2) - Bv(i + a, j - 1, k + q, 2));
+      cb0 += -c4z * (Bv(i + a, j + q, k, 1) - Bv(i + a, j + q, k - 1, 1));
+      cb1 += c4z * (Bv(i + a, j + q, k, 0) - Bv(i + a, j + q, k - 1, 0));
+      cb1 += -c4x * (Bv(i, j + q, k + a, 2) - Bv(i - 1, j + q, k + a, 2));
+      cb2 += c4x * (Bv(i, j + q, k + a, 1) - Bv(i - 1, j + q, k + a, 1));
+      cb2 += -c4y * (Bv(i + q, j, k + a, 0) - Bv(i + q, j - 1, k + a, 0));
+    }
+  rhs[c] = r[0] + cb0;
+  rhs[ncor + c] = r[1] + cb1;
+  rhs[2 * ncor + c] = r[2] + cb2;
+}
+
+__global__ void __launch_bounds__(256) k_jacobi(long long ncor, const double* __restrict__ M,
+                                                double* __restrict__ dinv, double k00, double k11,
+                                                double k22, double f) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  dinv[c] = 1.0 / (k00 + f * M[(size_t)0 * ncor + c]);
+  dinv[ncor + c] = 1.0 / (k11 + f * M[(size_t)4 * ncor + c]);
+  dinv[2 * ncor + c] = 1.0 / (k22 + f * M[(size_t)8 * ncor + c]);
+}
+
+// ---- reductions ------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Reduce acc[0..nv) over the block and store partial[blockIdx.x*kMaxV + i].
+__device__ __forceinline__ void block_store_partials(double* acc, int nv, double* partial) {
+  __shared__ double s_red[8][kMaxV];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < kMaxV; i++) {
+    if (i < nv) {
+      double v = warp_sum(acc[i]);
+      if (lane == 0) s_red[wid][i] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_red[w][threadIdx.x];
+    partial[blockIdx.x * kMaxV + threadIdx.x] = t;
+  }
+}
+
+// partial dots V_i . w for i < nv
+__global__ void __launch_bounds__(256) k_dots(long long n, const double* __restrict__ V,
+                                              const double* __restrict__ w, int nv,
+                                              double* __restrict__ partial) {
+  double acc[kMaxV];
+#pragma unroll
+  for (int i = 0; i < kMaxV; i++) acc[i] = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double wt = w[t];
+#pragma unroll
+    for (int i = 0; i < kMaxV; i++)
+      if (i < nv) acc[i] += V[(size_t)i * n + t] * wt;
+  }
+  block_store_partials(acc, nv, partial);
+}
+
+// w -= sum_i h_i V_i; then partial dots of the new w with V_i (mode 0) or its
+// squared norm (mode 1)
+__global__ void __launch_bounds__(256) k_orth(long long n, const double* __restrict__ V,
+                                              double* __restrict__ w, const double* __restrict__ h,
+                                              int nv, int mode, double* __restrict__ partial) {
+  __shared__ double s_h[kMaxV];
+  if (threadIdx.x < kMaxV) s_h[threadIdx.x] = threadIdx.x < nv ? h[threadIdx.x] : 0.0;
+  __syncthreads();
+  double acc[kMaxV];
+#pragma unroll
+  for (int i = 0; i < kMaxV; i++) acc[i] = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    double wt = w[t];
+    double vv[kMaxV];
+#pragma unroll
+    for (int i = 0; i < kMaxV; i++)
+      if (i < nv) {
+        vv[i] = V[(size_t)i * n + t];
+        wt -= s_h[i] * vv[i];
+      }
+    w[t] = wt;
+    if (mode == 0) {
+#pragma unroll
+      for (int i = 0; i < kMaxV; i++)
+        if (i < nv) acc[i] += vv[i] * wt;
+    } else {
+      acc[0] += wt * wt;
+    }
+  }
+  block_store_partials(acc, mode == 0 ? nv : 1, partial);
+}
+
+// out[i] = sum of partials (+ add[i] when add != null)
+__global__ void k_reduce_partials(const double* __restrict__ partial, int nblk, int nv,
+                                  double* __restrict__ out, const double* __restrict__ add) {
+  const int i = threadIdx.x;
+  if (i >= nv) return;
+  double t = 0.0;
+  for (int bk = 0; bk < nblk; bk++) t += partial[bk * kMaxV + i];
+  if (add) t += add[i];
+  out[i] = t;
+}
+
+// dst = src * (1/sqrt(*nrm2)) or src * (1/ *scal) depending on mode
+__global__ void __launch_bounds__(256) k_scale(long long n, const double* __restrict__ src,
+                                               double* __restrict__ dst,
+                                               const double* __restrict__ nrm2) {
+  const double s = *nrm2 > 0.0 ? 1.0 / sqrt(*nrm2) : 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = src[t] * s;
+}
+
+// r = b - r (in place on r)
+__global__ void __launch_bounds__(256) k_residual(long long n, const double* __restrict__ b,
+                                                  double* __restrict__ r) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    r[t] = b[t] - r[t];
+}
+
+// x += dinv .* sum_i y_i V_i
+__global__ void __launch_bounds__(256) k_combine(long long n, const double* __restrict__ V,
+                                                 const double* __restrict__ y, int nv,
+                                                 const double* __restrict__ dinv,
+                                                 double* __restrict__ x) {
+  __shared__ double s_y[kMaxV];
+  if (threadIdx.x < kMaxV) s_y[threadIdx.x] = threadIdx.x < nv ? y[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    double a = 0.0;
+    for (int i = 0; i < nv; i++) a += s_y[i] * V[(size_t)i * n + t];
+    x[t] += (dinv ? dinv[t] : 1.0) * a;
+  }
+}
+
+// partial norms of one vector
+__global__ void __launch_bounds__(256) k_norm2(long long n, const double* __restrict__ v,
+                                               double* __restrict__ partial) {
+  double acc[kMaxV];
+#pragma unroll
+  for (int i = 0; i < kMaxV; i++) acc[i] = 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    acc[0] += v[t] * v[t];
+  block_store_partials(acc, 1, partial);
+}
+
+// ---- field updates -----------------------------------------------------------
+__global__ void __launch_bounds__(256) k_update_b(long long ncor, const int* __restrict__ nbr,
+                                                  const double* __restrict__ Eh,
+                                                  const double* __restrict__ Bn,
+                                                  double* __restrict__ Bnew, double c4x,
+                                                  double c4y, double c4z) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  int b, i, j, k;
+  corner_ijk(c, b, i, j, k);
+  double Ex[2][2][2], Ey[2][2][2], Ez[2][2][2];
+#pragma unroll
+  for (int kk = 0; kk < 2; kk++)
+#pragma unroll
+    for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+      for (int ii = 0; ii < 2; ii++) {
+        const int id = local_id(nbr, b, i + ii, j + jj, k + kk);
+        Ex[ii][jj][kk] = Eh[id];
+        Ey[ii][jj][kk] = Eh[ncor + id];
+        Ez[ii][jj][kk] = Eh[2 * ncor + id];
+      }
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+#pragma unroll
+  for (int ii = 0; ii < 2; ii++)
+#pragma unroll
+    for (int jj = 0; jj < 2; jj++) {
+      t0 += -c4y * (Ez[ii][1][jj] - Ez[ii][0][jj]) + c4z * (Ey[ii][jj][1] - Ey[ii][jj][0]);
+      t1 += -c4z * (Ex[ii][jj][1] - Ex[ii][jj][0]) + c4x * (Ez[1][ii][jj] - Ez[0][ii][jj]);
+      t2 += -c4x * (Ey[1][ii][jj] - Ey[0][ii][jj]) + c4y * (Ex[ii][1][jj] - Ex[ii][0][jj]);
+    }
+  Bnew[c] = Bn[c] + t0;
+  Bnew[ncor + c] = Bn[ncor + c] + t1;
+  Bnew[2 * ncor + c] = Bn[2 * ncor + c] + t2;
+}
+
+__global__ void __launch_bounds__(256) k_c2n(long long ncor, const int* __restrict__ nbr,
+                                             const double* __restrict__ Bc,
+                                             double* __restrict__ Bcor) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  int b, i, j, k;
+  corner_ijk(c, b, i, j, k);
+  double t[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int kk = -1; kk <= 0; kk++)
+#pragma unroll
+    for (int jj = -1; jj <= 0; jj++)
+#pragma unroll
+      for (int ii = -1; ii <= 0; ii++) {
+        const int id = local_id(nbr, b, i + ii, j + jj, k + kk);
+#pragma unroll
+        for (int d = 0; d < 3; d++) t[d] += Bc[d * ncor + id];
+      }
+#pragma unroll
+  for (int d = 0; d < 3; d++) Bcor[d * ncor + c] = t[d] / 8.0;
+}
+
+__global__ void __launch_bounds__(256) k_update_e(long long ncor, const double* __restrict__ Eh,
+                                                  double* __restrict__ En,
+                                                  const double* __restrict__ Bc, double theta,
+                                                  double vol_over_8pi, double* __restrict__ energy) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double en = 0.0;
+  if (c < ncor) {
+    double e2 = 0.0, b2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double e = (Eh[d * ncor + c] - (1.0 - theta) * En[d * ncor + c]) / theta;
+      En[d * ncor + c] = e;
+      e2 += e * e;
+      const double bb = Bc[d * ncor + c];
+      b2 += bb * bb;
+    }
+    en = (e2 + b2) * vol_over_8pi;
+  }
+  __shared__ double s[8];
+  en = warp_sum(en);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = en;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
+    atomicAdd(energy, t);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_add(long long n, const double* __restrict__ a,
+                                             const double* __restrict__ b, double* __restrict__ o) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    o[t] = a[t] + b[t];
+}
+
+unsigned grid1(long long n) { return (unsigned)((n + 255) / 256); }
+unsigned gridr(long long n) {
+  long long g = (n + 255) / 256;
+  return (unsigned)(g < kRedBlocks ? g : kRedBlocks);
+}
+
+}  // namespace
+
+// ============================================================================
+cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y) {
+  Taps T = make_taps(c->cfg, true);
+  TimedLaunch t(c, "matvec");
+  k_matvec<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, x, dinv, y, T);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(amps_gpu_ctx* c) {
+  Taps T = make_taps(c->cfg, false);
+  double c4[3];
+  for (int d = 0; d < 3; d++) c4[d] = 0.25 * (c->cfg.dt / c->cfg.dx[d] * c->cfg.theta);
+  TimedLaunch t(c, "rhs");
+  k_rhs<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, c->d_En, c->d_Bc,
+                                                c->d_J, c->d_rhs, T, c4[0], c4[1], c4[2]);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jacobi_diag(amps_gpu_ctx* c) {
+  Taps T = make_taps(c->cfg, true);
+  TimedLaunch t(c, "jacobi");
+  k_jacobi<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_M, c->d_dinv, T.K[0][0][0],
+                                                   T.K[1][1][0], T.K[2][2][0], T.f);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update_b(amps_gpu_ctx* c) {
+  double c4[3];
+  for (int d = 0; d < 3; d++) c4[d] = 0.25 * (c->cfg.dt / c->cfg.dx[d]);
+  TimedLaunch t(c, "update_b");
+  k_update_b<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_Eh, c->d_Bc,
+                                                     c->d_Bc2, c4[0], c4[1], c4[2]);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor) {
+  TimedLaunch t(c, "c2n");
+  k_c2n<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, Bcen, Bcor);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update_e(amps_gpu_ctx* c) {
+  const double vol = c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2];
+  cudaError_t e = cudaMemsetAsync(c->d_energy + 1, 0, sizeof(double), c->stream);
+  if (e != cudaSuccess) return e;
+  TimedLaunch t(c, "update_e");
+  k_update_e<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_Eh, c->d_En, c->d_Bc,
+                                                     c->cfg.theta, vol * 0.125 / kPi,
+                                                     c->d_energy + 1);
+  return cudaGetLastError();
+}
+
+// GMRES(m) with right preconditioning, CGS2 Arnoldi, Givens on the host.
+// Device scratch layout of d_red: [0, kRedBlocks*kMaxV) partials, then h1
+// (kMaxV), h2 (kMaxV), nrm2 (1).
+amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
+                            amps_gpu_solve_stats* st) {
+  const long long n = 3 * c->ncor;
+  const int m = c->restart;
+  double* partial = c->d_red;
+  double* d_h1 = c->d_red + kRedBlocks * kMaxV;
+  double* d_h2 = d_h1 + kMaxV;
+  double* d_n2 = d_h2 + kMaxV;
+  double* d_y = d_n2 + 8;
+  const unsigned gr = gridr(n);
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+#define CK(x)                                                   \
+  do {                                                          \
+    e = (x);                                                    \
+    if (e != cudaSuccess) return cuda_check(c, e, #x);          \
+  } while (0)
+
+  const double* dinv = nullptr;
+  if (precond == 1) {
+    CK(launch_jacobi_diag(c));
+    dinv = c->d_dinv;
+  }
+  CK(cudaMemsetAsync(c->d_x, 0, sizeof(double) * n, s));
+  // ||b||
+  k_norm2<<<gr, 256, 0, s>>>(n, c->d_rhs, partial);
+  k_reduce_partials<<<1, kMaxV, 0, s>>>(partial, gr, 1, d_n2, nullptr);
+  CK(cudaMemcpyAsync(c->h_red, d_n2, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const double bnorm = std::sqrt(c->h_red[0]);
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
+  int it = 0;
+  bool conv = false;
+  double rel = 0.0;
+  if (bnorm == 0.0) {
+    conv = true;
+  }
+  double* V = c->d_V;
+  double* w = c->d_w;
+  while (!conv && it < maxit) {
+    // r = b - A x ; V0 = r / ||r||
+    CK(launch_matvec(c, c->d_x, nullptr, w));
+    k_residual<<<gr, 256, 0, s>>>(n, c->d_rhs, w);
+    k_norm2<<<gr, 256, 0, s>>>(n, w, partial);
+    k_reduce_partials<<<1, kMaxV, 0, s>>>(partial, gr, 1, d_n2, nullptr);
+    CK(cudaMemcpyAsync(c->h_red, d_n2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double beta = std::sqrt(c->h_red[0]);
+    rel = beta / bnorm;
+    if (rel <= tol) {
+      conv = true;
+      break;
+    }
+    k_scale<<<gr, 256, 0, s>>>(n, w, V, d_n2);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int jj = 0;
+    for (; jj < m && it < maxit; jj++) {
+      it++;
+      const int nv = jj + 1;
+      CK(launch_matvec(c, V + (size_t)jj * n, dinv, w));
+      {
+        TimedLaunch t(c, "gmres_orth", 7);
+        k_dots<<<gr, 256, 0, s>>>(n, V, w, nv, partial);
+        k_reduce_partials<<<1, kMaxV, 0, s>>>(partial, gr, nv, d_h1, nullptr);
+        k_orth<<<gr, 256, 0, s>>>(n, V, w, d_h1, nv, 0, partial);
+        k_reduce_partials<<<1, kMaxV, 0, s>>>(partial, gr, nv, d_h2, nullptr);
+        k_orth<<<gr, 256, 0, s>>>(n, V, w, d_h2, nv, 1, partial);
+        k_reduce_partials<<<1, kMaxV, 0, s>>>(partial, gr, 1, d_n2, nullptr);
+        k_scale<<<gr, 256, 0, s>>>(n, w, V + (size_t)nv * n, d_n2);
+      }
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(c->h_red, d_h1, sizeof(double) * (2 * kMaxV + 1), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      for (int i = 0; i < nv; i++) H[(size_t)i * m + jj] = c->h_red[i] + c->h_red[kMaxV + i];
+      const double hn = std::sqrt(c->h_red[2 * kMaxV]);
+      H[(size_t)(jj + 1) * m + jj] = hn;
+      for (int i = 0; i < jj; i++) {
+        const double a = H[(size_t)i * m + jj], bb = H[(size_t)(i + 1) * m + jj];
+        H[(size_t)i * m + jj] = cs[i] * a + sn[i] * bb;
+        H[(size_t)(i + 1) * m + jj] = -sn[i] * a + cs[i] * bb;
+      }
+      const double a = H[(size_t)jj * m + jj], bb = H[(size_t)(jj + 1) * m + jj];
+      const double r = std::sqrt(a * a + bb * bb);
+      cs[jj] = r > 0.0 ? a / r : 1.0;
+      sn[jj] = r > 0.0 ? bb / r : 0.0;
+      H[(size_t)jj * m + jj] = r;
+      H[(size_t)(jj + 1) * m + jj] = 0.0;
+      g[jj + 1] = -sn[jj] * g[jj];
+      g[jj] = cs[jj] * g[jj];
+      rel = std::fabs(g[jj + 1]) / bnorm;
+      if (rel <= tol) {
+        jj++;
+        break;
+      }
+    }
+    for (int i = jj - 1; i >= 0; i--) {
+      double t = g[i];
+      for (int q = i + 1; q < jj; q++) t -= H[(size_t)i * m + q] * y[q];
+      y[i] = t / H[(size_t)i * m + i];
+    }
+    CK(cudaMemcpyAsync(d_y, y.data(), sizeof(double) * jj, cudaMemcpyHostToDevice, s));
+    k_combine<<<gr, 256, 0, s>>>(n, V, d_y, jj, dinv, c->d_x);
+    CK(cudaGetLastError());
+    if (rel <= tol) {
+      // confirm with the true residual
+      CK(launch_matvec(c, c->d_x, nullptr, w));
+      k_residual<<<gr, 256, 0, s>>>(n, c->d_rhs, w);
+      k_norm2<<<gr, 256, 0, s>>>(n, w, partial);
+      k_reduce_partials<<<1, kMaxV, 0, s>>>(partial, gr, 1, d_n2, nullptr);
+      CK(cudaMemcpyAsync(c->h_red, d_n2, sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      rel = std::sqrt(c->h_red[0]) / bnorm;
+      if (rel <= tol * 10.0) conv = true;
+    }
+  }
+#undef CK
+  if (st) {
+    st->iterations = it;
+    st->converged = conv ? 1 : 0;
+    st->rel_residual = rel;
+  }
+  return conv ? AMPS_GPU_OK : AMPS_GPU_GMRES_NOT_CONVERGED;
+}
+
+cudaError_t launch_add(amps_gpu_ctx* c, const double* a, const double* b, double* o, long long n) {
+  k_add<<<gridr(n), 256, 0, c->stream>>>(n, a, b, o);
+  return cudaGetLastError();
+}

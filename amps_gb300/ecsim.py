@@ -1,0 +1,341 @@
+"""Host-side mirror of the reference call surfaces over the C ABI.
+
+``EcsimContext`` groups the calls an AMPS run makes on this path:
+
+    ParticleBuffer   import / export of particle state  (src/pic/pic.h:2716-3846)
+    MoveParticles    PIC::Mover::MoveParticles + Lapenta2017 (src/pic/pic_mover.cpp:580)
+    UpdateJMassMatrix ECSIM::UpdateJMassMatrix         (pic_field_solver_ecsim.cpp:3244)
+    TimeStep         ECSIM::TimeStep (field solve)      (pic_field_solver_ecsim.cpp:6179)
+    PicTimeStep      PIC::TimeStep's ECSIM track        (src/pic/pic_time_step.cpp:403)
+
+Errors follow the C ABI: every failing call raises ``AmpsGpuError`` carrying the
+status (the reference aborts instead).
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _capi
+from ._capi import AmpsGpuError, ptr
+
+
+@dataclass
+class Species:
+    name: str
+    charge: float   # normalised charge (picunits::si2no_q)
+    mass: float     # normalised mass (picunits::si2no_m)
+    weight: float   # macro-particle weight
+    vth: float      # thermal speed for the Maxwellian initial condition
+
+
+@dataclass
+class PeriodicMesh:
+    """Periodic box of nbx*nby*nbz blocks of 8^3 cells."""
+    nbx: int
+    nby: int
+    nbz: int
+    dx: float = 1.0
+    x0: tuple = (0.0, 0.0, 0.0)
+
+    @property
+    def ncells(self):
+        return 512 * self.nbx * self.nby * self.nbz
+
+    @property
+    def nblocks(self):
+        return self.nbx * self.nby * self.nbz
+
+    @property
+    def shape(self):
+        return (8 * self.nbx, 8 * self.nby, 8 * self.nbz)
+
+
+@dataclass
+class Workload:
+    """One ECSIM plasma workload in the reference's normalised units
+    (c = 1, lengths in d_e = c/omega_pe, times in 1/omega_pe)."""
+    name: str
+    mesh: PeriodicMesh
+    species: List[Species]
+    ppc: int          # particles per cell per species
+    dt: float
+    theta: float = 0.5
+    b0: tuple = (0.0, 0.0, 0.0)
+    steps: int = 10
+    tol: float = 1e-8
+    seed: int = 100
+
+    @property
+    def nparticles(self):
+        return self.mesh.ncells * self.ppc * len(self.species)
+
+
+def electron_proton_plasma(name, nbx, nby, nbz, ppc, steps, mass_ratio=25.0, vth_e=0.05,
+                           wpe_over_wce=2.0, dt=0.1, dx=1.0):
+    """Two-species plasma of the ECSIM workloads: electrons and protons with
+    mass ratio 25 (the H_PLUS / 25thELECTRON pair of input/species.input),
+    omega_pe = 1 (so dx = 1 is one electron inertial length), T_i = T_e,
+    uniform B0 along z with omega_pe/omega_ce = wpe_over_wce."""
+    # omega_pe^2 = 4 pi n q^2 / m with n = ppc * w / dx^3, q = -1, m = 1
+    w = dx ** 3 / (4.0 * np.pi * ppc)
+    vth_i = vth_e / np.sqrt(mass_ratio)
+    sp = [Species("electron", -1.0, 1.0, w, vth_e),
+          Species("proton", 1.0, mass_ratio, w, vth_i)]
+    b0 = (0.0, 0.0, 1.0 / wpe_over_wce)  # omega_ce = |q| B / (m c) = B for electrons
+    return Workload(name, PeriodicMesh(nbx, nby, nbz, dx), sp, ppc, dt, 0.5, b0, steps)
+
+
+WORKLOADS = {
+    # 32^3 cells as 4^3 blocks, 64 ppc/species, 10 steps (4,194,304 particles)
+    "ecsim_32c_64ppc": lambda: electron_proton_plasma("ecsim_32c_64ppc", 4, 4, 4, 64, 10),
+    # 64^3 cells as 8^3 blocks, 128 ppc/species (67,108,864 particles)
+    "ecsim_64c_128ppc": lambda: electron_proton_plasma("ecsim_64c_128ppc", 8, 8, 8, 128, 100),
+    # small cases for tests
+    "ecsim_16c_8ppc": lambda: electron_proton_plasma("ecsim_16c_8ppc", 2, 2, 2, 8, 3),
+    "ecsim_8c_4ppc": lambda: electron_proton_plasma("ecsim_8c_4ppc", 1, 1, 1, 4, 2),
+}
+
+
+def make_initial_condition(wl: Workload, nthreads: int = 8):
+    """Maxwellian particles (FP32-representable) from the reference LCG.
+    Returns dict with u (n,3) float32 cell-unit offsets, v (n,3) float32,
+    spec (n,) uint8, block (n,) int32 and x (n,3) float64 physical."""
+    lib = _capi.load()
+    m = wl.mesh
+    ns = len(wl.species)
+    n = lib.amps_ic_count(m.nbx, m.nby, m.nbz, wl.ppc, ns)
+    u = np.empty((n, 3), np.float32)
+    v = np.empty((n, 3), np.float32)
+    spec = np.empty(n, np.uint8)
+    block = np.empty(n, np.int32)
+    vth = np.array([s.vth for s in wl.species], np.float64)
+    st = lib.amps_ic_maxwellian(m.nbx, m.nby, m.nbz, wl.ppc, ns, ptr(vth, C.c_double),
+                                wl.seed, nthreads, ptr(u, C.c_float), ptr(v, C.c_float),
+                                ptr(spec, C.c_uint8), ptr(block, C.c_int32))
+    if st != 0:
+        raise AmpsGpuError(st, "amps_ic_maxwellian")
+    return {"u": u, "v": v, "spec": spec, "block": block}
+
+
+def block_origins(mesh: PeriodicMesh, block):
+    bx = block % mesh.nbx
+    by = (block // mesh.nbx) % mesh.nby
+    bz = block // (mesh.nbx * mesh.nby)
+    L = 8.0 * mesh.dx
+    return np.stack([mesh.x0[0] + bx * L, mesh.x0[1] + by * L, mesh.x0[2] + bz * L], axis=1)
+
+
+def physical_positions(mesh: PeriodicMesh, u, block):
+    return block_origins(mesh, block) + u.astype(np.float64) * mesh.dx
+
+
+def initial_fields(wl: Workload):
+    """E = 0, uniform B0 on cells and corners (both corner slots)."""
+    nc = wl.mesh.ncells
+    z = np.zeros((nc, 3))
+    B = np.tile(np.array(wl.b0, np.float64), (nc, 1))
+    return {"E_n": z.copy(), "E_half": z.copy(), "B_center": B.copy(),
+            "B_corner_prev": B.copy(), "B_corner_cur": B.copy()}
+
+
+class EcsimContext:
+    """One device context: a periodic block mesh, its fields and particles."""
+
+    def __init__(self, wl: Workload, capacity: Optional[int] = None, track_ids: bool = True,
+                 device: int = 0):
+        self.lib = _capi.load()
+        self.wl = wl
+        cfg = _capi.Config()
+        m = wl.mesh
+        cfg.nbx, cfg.nby, cfg.nbz = m.nbx, m.nby, m.nbz
+        for d in range(3):
+            cfg.x0[d] = m.x0[d]
+            cfg.dx[d] = m.dx
+        cfg.nspec = len(wl.species)
+        for i, s in enumerate(wl.species):
+            cfg.charge[i], cfg.mass[i], cfg.weight[i] = s.charge, s.mass, s.weight
+        cfg.dt, cfg.theta = wl.dt, wl.theta
+        cfg.particle_capacity = int(capacity if capacity is not None else wl.nparticles)
+        cfg.track_ids = 1 if track_ids else 0
+        cfg.device = device
+        self.cfg = cfg
+        h = C.c_void_p()
+        st = self.lib.amps_gpu_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise AmpsGpuError(st, "amps_gpu_create")
+        self.h = h
+
+    # ---- helpers ----
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.lib.amps_gpu_last_error(self.h)
+            raise AmpsGpuError(st, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.amps_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(self.lib.amps_gpu_get_stream(self.h, C.byref(s)), "get_stream")
+        return s.value
+
+    def synchronize(self):
+        self._check(self.lib.amps_gpu_synchronize(self.h), "synchronize")
+
+    # ---- ParticleBuffer ----
+    def import_particles(self, x, v, spec, wcorr=None):
+        x = np.ascontiguousarray(x, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        spec = np.ascontiguousarray(spec, np.uint8)
+        wc = None if wcorr is None else np.ascontiguousarray(wcorr, np.float64)
+        self._check(self.lib.amps_gpu_import_particles(
+            self.h, len(spec), ptr(x, C.c_double), ptr(v, C.c_double), ptr(spec, C.c_uint8),
+            ptr(wc, C.c_double)), "import_particles")
+
+    def import_particles_local(self, u, v, spec, block):
+        u = np.ascontiguousarray(u, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        spec = np.ascontiguousarray(spec, np.uint8)
+        block = np.ascontiguousarray(block, np.int32)
+        self._check(self.lib.amps_gpu_import_particles_local(
+            self.h, len(spec), ptr(u, C.c_float), ptr(v, C.c_float), ptr(spec, C.c_uint8),
+            ptr(block, C.c_int32)), "import_particles_local")
+
+    def num_particles(self):
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_num_particles(self.h, C.byref(n)), "num_particles")
+        return n.value
+
+    def export_particles(self, ids=True):
+        n = self.num_particles()
+        x = np.empty((n, 3)); v = np.empty((n, 3))
+        spec = np.empty(n, np.uint8); block = np.empty(n, np.int32); cell = np.empty(n, np.int32)
+        idv = np.empty(n, np.uint32) if (ids and self.cfg.track_ids) else None
+        nn = C.c_longlong()
+        self._check(self.lib.amps_gpu_export_particles(
+            self.h, ptr(x, C.c_double), ptr(v, C.c_double), ptr(spec, C.c_uint8),
+            ptr(block, C.c_int32), ptr(cell, C.c_int32), ptr(idv, C.c_uint32), C.byref(nn)),
+            "export_particles")
+        out = {"x": x, "v": v, "spec": spec, "block": block, "cell": cell}
+        if idv is not None:
+            out["id"] = idv
+        return out
+
+    # ---- fields / moments ----
+    def import_fields(self, E_n=None, E_half=None, B_center=None, B_corner_prev=None,
+                      B_corner_cur=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float64)
+                for a in (E_n, E_half, B_center, B_corner_prev, B_corner_cur)]
+        self._check(self.lib.amps_gpu_import_fields(self.h, *[ptr(a, C.c_double) for a in arrs]),
+                    "import_fields")
+
+    def export_fields(self):
+        nc = self.wl.mesh.ncells
+        out = {k: np.empty((nc, 3)) for k in
+               ("E_n", "E_half", "B_center", "B_corner_prev", "B_corner_cur")}
+        self._check(self.lib.amps_gpu_export_fields(
+            self.h, *[ptr(out[k], C.c_double) for k in
+                      ("E_n", "E_half", "B_center", "B_corner_prev", "B_corner_cur")]),
+            "export_fields")
+        return out
+
+    def import_moments(self, J, M):
+        J = np.ascontiguousarray(J, np.float64)
+        M = np.ascontiguousarray(M, np.float64)
+        self._check(self.lib.amps_gpu_import_moments(self.h, ptr(J, C.c_double),
+                                                     ptr(M, C.c_double)), "import_moments")
+
+    def export_moments(self, with_m=True):
+        nc = self.wl.mesh.ncells
+        J = np.empty((nc, 3))
+        M = np.empty((nc, 243)) if with_m else None
+        self._check(self.lib.amps_gpu_export_moments(self.h, ptr(J, C.c_double),
+                                                     ptr(M, C.c_double)), "export_moments")
+        return J, M
+
+    # ---- reference call surfaces ----
+    def MoveParticles(self):
+        nout = C.c_longlong()
+        self._check(self.lib.amps_gpu_move_particles(self.h, C.byref(nout)), "MoveParticles")
+        return nout.value
+
+    def UpdateJMassMatrix(self):
+        e = C.c_double()
+        self._check(self.lib.amps_gpu_update_j_mass_matrix(self.h, C.byref(e)),
+                    "UpdateJMassMatrix")
+        return e.value
+
+    def TimeStep(self, tol=None, maxit=200, precond=0):
+        st = _capi.SolveStats()
+        tol = self.wl.tol if tol is None else tol
+        self._check(self.lib.amps_gpu_field_solve(self.h, tol, maxit, precond, C.byref(st)),
+                    "ECSIM::TimeStep")
+        return st
+
+    def PicTimeStep(self, tol=None, maxit=200, precond=0):
+        st = _capi.StepStats()
+        tol = self.wl.tol if tol is None else tol
+        self._check(self.lib.amps_gpu_step(self.h, tol, maxit, precond, C.byref(st)),
+                    "PIC::TimeStep")
+        return st
+
+    def push_deposit(self, want_energy=True):
+        e = C.c_double()
+        self._check(self.lib.amps_gpu_push_deposit(self.h, C.byref(e) if want_energy else None),
+                    "push_deposit")
+        return e.value
+
+    # ---- timing ----
+    def set_kernel_timing(self, on=True):
+        self._check(self.lib.amps_gpu_set_kernel_timing(self.h, 1 if on else 0), "timing")
+
+    def reset_kernel_times(self):
+        self._check(self.lib.amps_gpu_reset_kernel_times(self.h), "reset timing")
+
+    def kernel_times(self):
+        cap = 64
+        names = (C.c_char_p * cap)()
+        ms = np.zeros(cap)
+        cnt = np.zeros(cap, np.int64)
+        n = C.c_int()
+        self._check(self.lib.amps_gpu_get_kernel_times(self.h, names, ptr(ms, C.c_double),
+                                                       cnt.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                                       cap, C.byref(n)), "kernel times")
+        return {names[i].decode(): (float(ms[i]), int(cnt[i])) for i in range(n.value)}
+
+
+def trace_dipole(x, p, q, m0, b_eq, r_e, b_ext, r_in, r_out, max_steps, dphi_max=0.15,
+                 dt_max=1.0, precision=0, device=0):
+    """Batched relativistic Boris tracing (SI). x, p are (n,3) float64 arrays,
+    updated in place.  Returns (status, steps, total_steps, kernel_ms)."""
+    lib = _capi.load()
+    n = len(x)
+    assert x.dtype == np.float64 and p.dtype == np.float64 and x.flags.c_contiguous
+    status = np.zeros(n, np.int32)
+    steps = np.zeros(n, np.int64)
+    ext = np.ascontiguousarray(b_ext, np.float64)
+    tot = C.c_longlong()
+    ms = C.c_double()
+    st = lib.amps_gpu_trace_dipole(device, n, ptr(x, C.c_double), ptr(p, C.c_double),
+                                   ptr(status, C.c_int32), ptr(steps, C.c_int64), q, m0, b_eq,
+                                   r_e, ptr(ext, C.c_double), r_in, r_out, max_steps, dphi_max,
+                                   dt_max, precision, C.byref(tot), C.byref(ms))
+    if st != 0:
+        raise AmpsGpuError(st, "amps_gpu_trace_dipole")
+    return status, steps, tot.value, ms.value

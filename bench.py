@@ -1,0 +1,397 @@
+"""Benchmark of the AMPS particle hot path on GB300: particle-steps/s of
+push + re-bin + deposit (Lapenta2017 mover + ECSIM UpdateJMassMatrix).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload NAME]
+
+A step is one pass of push + re-bin + deposit over every particle of the
+workload (inputs resident in HBM; the particle arrays, ~1.7 GB, exceed the
+129 MB L2, so no L2 flush is needed).  The timed region is bracketed by a
+barrier and device synchronisation and timed with CUDA events on the library's
+stream; the max over ranks is reported.  N > 1 runs independent replicas (the
+path is not sharded), value = all ranks' particle-steps / max time.
+
+--impl reference times the reference CPU path on the host cores: the
+reference's ECSIM sources need its generated build headers and do not compile
+standalone, so the FP64 restatement of Lapenta2017 + ProcessCell (oracle/) is
+timed instead, one periodic single-block replica of the same plasma per host
+thread.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (push+deposit)"
+UNIT = "particle-steps/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    backend = os.environ.get("AMPS_DIST_BACKEND", "nccl")
+    dist.init_process_group(backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, val):
+    if dist is None:
+        return val
+    import torch
+    t = torch.tensor([float(val)], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, val):
+    if dist is None:
+        return val
+    import torch
+    t = torch.tensor([float(val)], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+class CudaEvents:
+    """CUDA events on an external stream through the runtime library."""
+
+    def __init__(self):
+        self.rt = C.CDLL("libcudart.so")
+
+    def event(self):
+        e = C.c_void_p()
+        assert self.rt.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def record(self, e, stream):
+        assert self.rt.cudaEventRecord(e, C.c_void_p(stream)) == 0
+
+    def elapsed_ms(self, a, b):
+        self.rt.cudaEventSynchronize(b)
+        ms = C.c_float()
+        assert self.rt.cudaEventElapsedTime(C.byref(ms), a, b) == 0
+        return ms.value
+
+    def sync(self):
+        self.rt.cudaDeviceSynchronize()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def kernel_bytes(wl, name):
+    """Algorithmic bytes per launch of each particle kernel:
+    what the kernel must read and write given the data layout."""
+    n = wl.nparticles
+    ncell = wl.mesh.ncells
+    nb = wl.mesh.nblocks
+    if name == "push":
+        # read u,v (24) + species (1); write u,v (24) + key (4) + rank (4); stencil 23.3 KB/block
+        return n * 57 + nb * 23328
+    if name == "scatter":
+        # read key, rank, start (12) + u,v,species (25); write u,v,species (25) (+ ids 8 if tracked)
+        return n * 62
+    if name == "deposit":
+        # read u,v,species (25); write per-cell partials (324+24 floats); stencil 11.7 KB/block
+        return n * 25 + ncell * 348 * 4 + nb * 11664
+    if name == "assemble":
+        # read partials (2x, each pair value reaches two corners); write M (243) + J (3) FP64
+        return ncell * (2 * 348 * 4) + ncell * 246 * 8
+    if name == "pack_stencils":
+        return ncell * 9 * 8 * 27 // 8 + nb * (23328 + 11664)
+    return None
+
+
+def cpu_replica_rate(wl_name, steps, seconds_budget, threads):
+    """FP64 oracle (Lapenta2017 + ProcessCell + re-binning) on per-thread
+    single-block periodic replicas of the workload's plasma.  Returns
+    particle-steps/s over all threads."""
+    import amps_gb300 as A
+    from tests import oracle_lib as O
+    base = A.WORKLOADS[wl_name]()
+    rep = A.electron_proton_plasma("cpu_replica", 1, 1, 1, base.ppc, steps)
+    states = []
+    for t in range(threads):
+        rep.seed = 100 + 2 * t + 1
+        ic = A.make_initial_condition(rep, nthreads=1)
+        x = A.physical_positions(rep.mesh, ic["u"], ic["block"])
+        f = A.initial_fields(rep)
+        states.append(O.OracleState(rep, x, ic["v"].astype(np.float64), ic["spec"], f))
+    counts = [0] * threads
+    deadline = [None]
+
+    def work(i):
+        st = states[i]
+        while time.time() < deadline[0]:
+            st.push()
+            st.deposit()
+            counts[i] += len(st.spec)
+
+    deadline[0] = time.time() + seconds_budget
+    t0 = time.time()
+    th = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    dt = time.time() - t0
+    n = rep.nparticles
+    return sum(counts) / dt, {"replica_particles": n, "threads": threads, "seconds": dt,
+                              "particle_steps": sum(counts)}
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import amps_gb300 as A
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    wl = A.WORKLOADS[args.workload]()
+    ev = CudaEvents()
+    t_ic = time.time()
+    ic = A.make_initial_condition(wl, nthreads=os.cpu_count() or 8)
+    t_ic = time.time() - t_ic
+    ctx = A.EcsimContext(wl, capacity=wl.nparticles, track_ids=False, device=local)
+    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
+    f = A.initial_fields(wl)
+    ctx.import_fields(**f)
+    # one field solve so the push sees a self-consistent E^{n+theta}
+    ctx.UpdateJMassMatrix()
+    solve = ctx.TimeStep(tol=wl.tol, maxit=200, precond=1)
+    stream = ctx.stream()
+    for _ in range(args.warmup):
+        ctx.push_deposit(want_energy=False)
+    ctx.synchronize()
+    ctx.set_kernel_timing(True)
+    ctx.reset_kernel_times()
+    a, b = ev.event(), ev.event()
+    clk = ClockSampler(local)
+    barrier(dist)
+    ev.sync()
+    clk.start()
+    ev.record(a, stream)
+    for _ in range(args.steps):
+        ctx.push_deposit(want_energy=False)
+    ev.record(b, stream)
+    ev.sync()
+    ms = ev.elapsed_ms(a, b)
+    clocks = clk.stop()
+    barrier(dist)
+    ktimes = ctx.kernel_times()
+    ctx.set_kernel_timing(False)
+    ms_max = max_over_ranks(dist, ms)
+    total_ps = sum_over_ranks(dist, float(wl.nparticles) * args.steps)
+    value = total_ps / (ms_max / 1e3)
+
+    # full ECSIM step (field solve + push + deposit), Jacobi GMRES
+    t_step = []
+    for _ in range(2):
+        a2, b2 = ev.event(), ev.event()
+        ev.record(a2, stream)
+        s = ctx.PicTimeStep(tol=wl.tol, maxit=200, precond=1)
+        ev.record(b2, stream)
+        t_step.append(ev.elapsed_ms(a2, b2))
+    gmres_it = s.solve.iterations
+
+    # end to end through the reference-facing C ABI with host FP64 buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        exp = ctx.export_particles(ids=False)
+        hx, hv, hs = exp["x"], exp["v"], exp["spec"]
+        nc = wl.mesh.ncells
+        hJ = np.empty((nc, 3))
+        t0 = time.time()
+        for _ in range(args.e2e_steps):
+            ctx.import_particles(hx, hv, hs)
+            ctx.push_deposit(want_energy=True)
+            out = ctx.export_particles(ids=False)
+            hx, hv = out["x"], out["v"]
+            hJ, _ = ctx.export_moments(with_m=False)
+        ctx.synchronize()
+        e2e_s = time.time() - t0
+        bi = wl.nparticles * (24 + 24 + 1)
+        bo = wl.nparticles * (24 + 24 + 1 + 4 + 4) + nc * 24
+        e2e = {"value": wl.nparticles * args.e2e_steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "steps": args.e2e_steps,
+               "api": "amps_gpu_import_particles + amps_gpu_push_deposit + "
+                      "amps_gpu_export_particles + amps_gpu_export_moments (J)"}
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    per = {k: v for k, v in ktimes.items()}
+    top = max(per, key=lambda k: per[k][0])
+    ms_top, launches = per[top]
+    nl = max(1, launches)
+    nbytes = kernel_bytes(wl, top)
+    roof = None
+    if nbytes:
+        achieved = nbytes / (ms_top / nl / 1e3) / 1e9
+        roof = {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": args.traffic, "algorithmic_bytes_per_launch": int(nbytes),
+                "avg_launch_ms": round(ms_top / nl, 4)}
+    shares = {k: round(v[0] / sum(x[0] for x in per.values()), 4) for k, v in per.items()}
+    gpu_launches = int(sum(v[1] for v in per.values()))
+
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        rate, info = cpu_replica_rate(args.workload, 1, args.cpu_seconds, 1)
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "FP64 oracle Lapenta2017+ProcessCell on a periodic 8^3-cell replica "
+                         "of the same plasma (%d particles), %.1f s" % (info["replica_particles"],
+                                                                      info["seconds"])}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 field solve)",
+            "data": "synthetic (seeded Maxwellian electron-proton plasma, LCG of rnd.h)",
+            "config": {"workload": wl.name, "particles": wl.nparticles,
+                       "cells": wl.mesh.ncells, "blocks": wl.mesh.nblocks, "ppc_per_species": wl.ppc,
+                       "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (no flush)",
+                       "ecsim_step_ms": round(min(t_step), 3), "gmres_iterations": gmres_it,
+                       "gmres_precond": "jacobi", "ic_seconds": round(t_ic, 2)},
+            "e2e": e2e, "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
+            "clocks": clocks, "gpu_launches": gpu_launches,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rates = []
+    for _ in range(args.steps):
+        r, info = cpu_replica_rate(args.workload, 1, args.ref_seconds, threads)
+        rates.append(r)
+    value = float(np.mean(rates))
+    sample = ("FP64 oracle port of Lapenta2017 + ProcessCell + re-binning, one periodic "
+              "8^3-cell replica of the same plasma per host thread (%d threads, %d particles "
+              "each), %g s per step" % (threads, info["replica_particles"], args.ref_seconds))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ecsim_64c_128ppc")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the top kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

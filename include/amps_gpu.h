@@ -1,0 +1,187 @@
+/*
+ * amps_gpu.h -- C ABI of libamps_gpu.so, the GB300 (sm_103a) implementation of
+ * the AMPS particle / ECSIM hot path.
+ *
+ * The entry points mirror the reference call surfaces they replace:
+ *   PIC::Mover::MoveParticles           src/pic/pic_mover.cpp:580
+ *   PIC::Mover::Lapenta2017             src/pic/pic_mover_boris.cpp:837-1380
+ *   ECSIM::UpdateJMassMatrix            src/pic/pic_field_solver_ecsim.cpp:3244
+ *   ECSIM::TimeStep                     src/pic/pic_field_solver_ecsim.cpp:6179
+ *   cLinearSystemCornerNode::Solve      srcInterface/LinearSystemCornerNode.h:3212
+ *   PIC::ParticleBuffer (import/export) src/pic/pic.h:2716-3846
+ *   gridless BorisStep tracing          srcEarth/gridless/GridlessParticleMovers.cpp:781
+ *
+ * Conventions
+ *   - Plain pointers to HOST memory unless a name says otherwise; sizes are
+ *     element counts.  No call aborts: every call returns amps_gpu_status and
+ *     amps_gpu_last_error() describes the last failure of a context.
+ *   - Units are the reference's normalised ECSIM units
+ *     (_PIC_FIELD_SOLVER_INPUT_UNIT_NORM_: c = E_conv = B_conv = 1); charge
+ *     and mass tables are passed already normalised (picunits::si2no_q/_m).
+ *   - Field arrays on the host side use the global periodic corner numbering
+ *     idx(I,J,K) = I + NX*(J + NY*K) with NX = 8*nbx, three interleaved
+ *     components per node (x,y,z); the mass matrix is 243 values per corner:
+ *     27 neighbour slots x row-major 3x3, slot = ii + 3*jj + 9*kk where
+ *     ii,jj,kk = 0,1,2 stand for offsets 0,-1,+1 (the reference's
+ *     MassMatrixOffsetTable, pic_field_solver_ecsim.cpp:624-640).
+ *   - Particle block ids are bx + nbx*(by + nby*bz); cell ids are block-local
+ *     i + 8*(j + 8*k) (the reference's _getCenterNodeLocalNumber order).
+ *   - A context owns one CUDA stream; it is not thread safe.
+ */
+#ifndef AMPS_GPU_H
+#define AMPS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMPS_GPU_MAX_SPECIES 8
+
+/* Replaces the reference's exit(__LINE__,__FILE__,msg) aborts
+ * (src/general/global.h:50) and the mover return codes (src/pic/pic.h:5955-5960). */
+typedef enum {
+  AMPS_GPU_OK = 0,
+  AMPS_GPU_INVALID_ARG = 1,
+  AMPS_GPU_OUT_OF_DOMAIN_PARTICLES = 2,
+  AMPS_GPU_GMRES_NOT_CONVERGED = 3,
+  AMPS_GPU_DEVICE_TIMEOUT = 4,
+  AMPS_GPU_CUDA_ERROR = 5,
+  AMPS_GPU_CAPACITY_EXCEEDED = 6,
+  AMPS_GPU_NO_DEVICE = 7
+} amps_gpu_status;
+
+typedef struct amps_gpu_ctx amps_gpu_ctx;
+
+/* Mesh, species and time-step parameters.  The mesh is a periodic box of
+ * nbx*nby*nbz uniform blocks of 8^3 cells (_BLOCK_CELLS_X_ = 8), which is the
+ * domain + ghost-block layout of Periodic::ExchangeParticles
+ * (src/pic/pic_bc_periodic.cpp:55) with the ghost layer folded away. */
+typedef struct {
+  int nbx, nby, nbz;
+  double x0[3];                 /* domain origin (xGlobalMin) */
+  double dx[3];                 /* cell size */
+  int nspec;
+  double charge[AMPS_GPU_MAX_SPECIES]; /* normalised charge (ElectricChargeTable) */
+  double mass[AMPS_GPU_MAX_SPECIES];   /* normalised mass (MolMass) */
+  double weight[AMPS_GPU_MAX_SPECIES]; /* macro-particle weight (GetLocalParticleWeight) */
+  double dt;                    /* GlobalTimeStep[0] */
+  double theta;                 /* ECSIM::theta (0.5) */
+  long long particle_capacity;  /* maximum particles held on the device */
+  int track_ids;                /* 1: carry a 32-bit particle id through re-binning */
+  int device;                   /* CUDA device ordinal */
+} amps_gpu_config;
+
+typedef struct {
+  int iterations;               /* GMRES iterations (matrix-vector products after the first) */
+  int converged;
+  double rel_residual;          /* ||b - A x|| / ||b|| (true residual at exit) */
+  double wave_energy;           /* UpdateE energy sum, pic_field_solver_ecsim.cpp:5995 */
+} amps_gpu_solve_stats;
+
+typedef struct {
+  amps_gpu_solve_stats solve;
+  double particle_energy;       /* UpdateJMassMatrix energy sum, :3972-3987 */
+  long long out_of_block;       /* particles that moved more than one block (reported, kept) */
+  long long ulp_face;           /* particles that ended within 1 FP32 ulp of a cell face */
+} amps_gpu_step_stats;
+
+/* ---- context (PIC::Init / ECSIM::Init analogue) ---- */
+amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out);
+amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* ctx);
+const char* amps_gpu_last_error(const amps_gpu_ctx* ctx);
+amps_gpu_status amps_gpu_get_stream(amps_gpu_ctx* ctx, void** stream);
+amps_gpu_status amps_gpu_synchronize(amps_gpu_ctx* ctx);
+
+/* ---- PIC::ParticleBuffer import/export (pic.h:2808-3400 accessors) ----
+ * x, v: n*3 interleaved FP64; spec: species byte; wcorr: individual weight
+ * correction (GetIndividualStatWeightCorrection) or NULL for 1.  The device
+ * locates each particle's block and cell with the reference's findTreeNode /
+ * FindCellIndex rules and stores FP32 block-local offsets. */
+amps_gpu_status amps_gpu_import_particles(amps_gpu_ctx* ctx, long long n, const double* x,
+                                          const double* v, const uint8_t* spec,
+                                          const double* wcorr);
+/* Fast path: block-local FP32 offsets in cell units (x = x0_block + u*dx). */
+amps_gpu_status amps_gpu_import_particles_local(amps_gpu_ctx* ctx, long long n, const float* u,
+                                                const float* v, const uint8_t* spec,
+                                                const int32_t* block);
+/* Exports in the device order (sorted by block, then cell).  Any pointer may
+ * be NULL.  id is the import index when track_ids is set. */
+amps_gpu_status amps_gpu_export_particles(amps_gpu_ctx* ctx, double* x, double* v, uint8_t* spec,
+                                          int32_t* block, int32_t* cell, uint32_t* id,
+                                          long long* n);
+amps_gpu_status amps_gpu_num_particles(amps_gpu_ctx* ctx, long long* n);
+
+/* ---- field state (corner E^n, E^{n+theta}; centre B^n; corner B prev/cur) ---- */
+amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* ctx, const double* E_n, const double* E_half,
+                                       const double* B_center, const double* B_corner_prev,
+                                       const double* B_corner_cur);
+amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* ctx, double* E_n, double* E_half,
+                                       double* B_center, double* B_corner_prev,
+                                       double* B_corner_cur);
+/* J: 3 per corner, M: 243 per corner (global layout above). */
+amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* ctx, const double* J, const double* M);
+amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* ctx, double* J, double* M);
+
+/* ---- hot path ---- */
+/* PIC::Mover::MoveParticles with Lapenta2017 (pic_mover.cpp:580,
+ * pic_mover_boris.cpp:876): E^{n+theta} and the corner B "prev" slot, then
+ * re-binning into destination cells (pic_mover.cpp:982-1087, periodic wrap of
+ * pic_bc_periodic.cpp:55-178). */
+amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* ctx, long long* out_of_block);
+/* ECSIM::UpdateJMassMatrix (pic_field_solver_ecsim.cpp:3244): J and the
+ * 243-term mass matrix on all corners from the corner B "cur" slot. */
+amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* ctx, double* particle_energy);
+/* ECSIM::TimeStep (pic_field_solver_ecsim.cpp:6179): RHS, GMRES solve for
+ * E^{n+theta} = E^n + dE (x0 = 0, stop when ||b-Ax|| <= tol ||b||, restart 30),
+ * UpdateB, InterpolateB_C2N, UpdateE.  precond: 0 none (the reference's
+ * PrecondParam = 0), 1 Jacobi. */
+amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* ctx, double tol, int maxit, int precond,
+                                     amps_gpu_solve_stats* stats);
+/* One PIC::TimeStep of the ECSIM track (pic_time_step.cpp:403-551): field
+ * solve, move, deposit.  Runs UpdateJMassMatrix first if no moments exist yet
+ * (the reference's first-call branch, pic_field_solver_ecsim.cpp:6209). */
+amps_gpu_status amps_gpu_step(amps_gpu_ctx* ctx, double tol, int maxit, int precond,
+                              amps_gpu_step_stats* stats);
+/* Particle push + re-bin + deposit only (the particle-steps/s hot path). */
+amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* ctx, double* particle_energy);
+
+/* ---- per-kernel device timing on the context stream (CUDA events) ---- */
+amps_gpu_status amps_gpu_set_kernel_timing(amps_gpu_ctx* ctx, int enable);
+/* Fills up to cap entries; names are static strings.  Returns the count in *n. */
+amps_gpu_status amps_gpu_get_kernel_times(amps_gpu_ctx* ctx, const char** names, double* total_ms,
+                                          long long* launches, int cap, int* n);
+amps_gpu_status amps_gpu_reset_kernel_times(amps_gpu_ctx* ctx);
+
+/* ---- host-side initial condition (test/srcFastWave/main.cpp:270-300 style) ----
+ * Uniform positions in every cell and Maxwellian velocities (Box-Muller on the
+ * reference LCG of src/general/rnd.h:56-77), one co-located particle of every
+ * species per draw.  Outputs are FP32-representable so an FP64 consumer and
+ * the FP32 device start from identical particles.  Sizes: n = ncells*ppc*nspec.
+ * u: block-local offsets in cell units (3 per particle), v: 3 per particle,
+ * block: block id.  Draws are jump-ahead seeded per block and generated with
+ * nthreads host threads (result independent of nthreads). */
+long long amps_ic_count(int nbx, int nby, int nbz, int ppc, int nspec);
+int amps_ic_maxwellian(int nbx, int nby, int nbz, int ppc, int nspec, const double* vth,
+                       unsigned long long seed, int nthreads, float* u, float* v, uint8_t* spec,
+                       int32_t* block);
+
+/* ---- batched relativistic test-particle tracing (config: dipole + uniform) ----
+ * BorisStep of srcEarth/gridless/GridlessParticleMovers.cpp:781 with the
+ * gyro-angle limiter dt = min(dt_max, dphi_max/omega) of
+ * CutoffRigidityGridless.cpp:1190-1197, one persistent kernel with warp-level
+ * compaction of finished particles.  SI units.  x, p: n*3 host arrays updated
+ * in place; status: 1 r<r_in, 2 r>r_out, 0 step cap; steps: steps taken.
+ * precision: 0 FP64, 1 FP32.  total_steps receives the sum of steps. */
+amps_gpu_status amps_gpu_trace_dipole(int device, long long n, double* x, double* p,
+                                      int32_t* status, int64_t* steps, double q, double m0,
+                                      double b_eq, double r_e, const double* b_ext, double r_in,
+                                      double r_out, long long max_steps, double dphi_max,
+                                      double dt_max, int precision, long long* total_steps,
+                                      double* kernel_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,90 @@
+/*
+ * amps_oracle.h -- FP64 CPU restatement of the AMPS particle / ECSIM hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library links, loads or
+ * calls this code: it is the checker that tests/, __graft_entry__.smoke() and
+ * the cpu_baseline leg of bench.py compare the CUDA path against.
+ *
+ * Scope: a periodic box of nbx*nby*nbz uniform blocks of 8^3 cells, two or
+ * more species, corner-based E and B (the _PIC_FIELD_SOLVER_B_CORNER_BASED_
+ * configuration), normalised units (c = E_conv = B_conv = length_conv = 1).
+ * Every function cites the reference file:line it restates.
+ *
+ * Parity: the 81-point operator coefficients are pinned against the
+ * reference's own stencil library (src/general/stencil.h) through
+ * oracle/pins/stencil_pin.cpp.  The Lapenta2017 push, ProcessCell deposition
+ * and the field update are restated line by line but cannot be compiled from
+ * the reference (they need its generated build headers), so they are pinned
+ * by the conservation law ECSIM is built on (theta = 0.5 conserves total
+ * energy to the linear-solver tolerance) rather than by golden vectors.
+ * The GMRES is absent from the reference (SWMF share/Library), so its
+ * parity is unpinned: the stop rule is stated explicitly instead.
+ */
+#ifndef AMPS_ORACLE_H
+#define AMPS_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_NC 8              /* cells per block edge (_BLOCK_CELLS_X_) */
+#define ORC_MAXSPEC 8
+
+typedef struct {
+  int nbx, nby, nbz;          /* blocks per axis */
+  double x0[3];               /* domain origin */
+  double dx[3];               /* cell size */
+  int nspec;
+  double q[ORC_MAXSPEC];      /* normalised charge per species */
+  double m[ORC_MAXSPEC];      /* normalised mass per species */
+  double w[ORC_MAXSPEC];      /* macro-particle weight per species */
+  double dt, theta;
+} orc_mesh;
+
+/* ---- stencil coefficient tables (27 taps, index ii+3jj+9kk with offsets
+ *      {0,-1,+1} for ii,jj,kk = 0,1,2 as in the reference's indexAddition) */
+void orc_laplacian_table(int axis, double out[27]);
+void orc_graddiv_table(int p, int q, double out[27]);
+
+/* ---- interpolation / push / deposition ---- */
+void orc_corner_weights(const double xloc[3], double w_table[8]);
+long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
+              int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev);
+double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
+                   const uint8_t* spec, const double* wcorr, const int32_t* block,
+                   const int32_t* cell, const double* Bc_cur, double* J, double* M);
+void orc_locate(const orc_mesh* g, long n, const double* x, int32_t* block, int32_t* cell);
+
+/* ---- field solve ---- */
+void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor);
+void orc_rhs(const orc_mesh* g, const double* E_n, const double* Bcen, const double* J,
+             const double* M, double* rhs);
+void orc_matvec(const orc_mesh* g, const double* M, const double* x, double* y);
+void orc_jacobi_diag(const orc_mesh* g, const double* M, double* diag);
+int orc_gmres(const orc_mesh* g, const double* M, const double* b, double* x, double tol,
+              int maxit, int restart, int precond, double* resid_out);
+void orc_update_b(const orc_mesh* g, const double* E_half, const double* B_n, double* B_np1);
+double orc_update_e(const orc_mesh* g, const double* E_half, double* E_n, const double* B_cen);
+
+/* ---- one full ECSIM time step in the reference order (pic_time_step.cpp:403-551) ----
+ * state arrays: E_n, E_half, Bcen (B^n on entry, B^{n+1} on exit), Bcor_prev/
+ * Bcor_cur (corner B, swapped), J, M (deposited at the end of the previous step).
+ * Returns GMRES iterations; energies are written to diag[0..2] =
+ * {particle energy, wave energy, gmres relative residual}. */
+int orc_ecsim_step(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
+                   const double* wcorr, int32_t* block, int32_t* cell, double* E_n,
+                   double* E_half, double* Bcen, double* Bcor_prev, double* Bcor_cur,
+                   double* J, double* M, double tol, int maxit, int precond, double* diag);
+
+/* ---- relativistic Boris, gridless form (srcEarth/gridless/GridlessParticleMovers.cpp:781) ---- */
+void orc_dipole_b(const double x[3], double b_eq, double r_e, const double b_ext[3], double B[3]);
+long orc_trace(long n, double* x, double* p, int32_t* status, int64_t* steps, double q, double m0,
+               double b_eq, double r_e, const double b_ext[3], double r_in, double r_out,
+               long max_steps, double dphi_max, double dt_max, int single_precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

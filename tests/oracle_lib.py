@@ -1,0 +1,156 @@
+"""ctypes binding of the FP64 oracle (oracle/liboracle.so).
+
+Test infrastructure: only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline use it, always as the checker.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+LIB = os.path.join(ORACLE_DIR, "liboracle.so")
+
+
+class Mesh(C.Structure):
+    _fields_ = [("nbx", C.c_int), ("nby", C.c_int), ("nbz", C.c_int),
+                ("x0", C.c_double * 3), ("dx", C.c_double * 3), ("nspec", C.c_int),
+                ("q", C.c_double * 8), ("m", C.c_double * 8), ("w", C.c_double * 8),
+                ("dt", C.c_double), ("theta", C.c_double)]
+
+
+D = C.POINTER(C.c_double)
+I32 = C.POINTER(C.c_int32)
+U8 = C.POINTER(C.c_uint8)
+I64 = C.POINTER(C.c_int64)
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "all"], check=True)
+    lib = C.CDLL(LIB)
+    sig = {
+        "orc_laplacian_table": (None, [C.c_int, D]),
+        "orc_graddiv_table": (None, [C.c_int, C.c_int, D]),
+        "orc_corner_weights": (None, [D, D]),
+        "orc_push": (C.c_long, [C.POINTER(Mesh), C.c_long, D, D, U8, I32, I32, D, D]),
+        "orc_deposit": (C.c_double, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D]),
+        "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
+        "orc_center_to_corner": (None, [C.POINTER(Mesh), D, D]),
+        "orc_rhs": (None, [C.POINTER(Mesh), D, D, D, D, D]),
+        "orc_matvec": (None, [C.POINTER(Mesh), D, D, D]),
+        "orc_jacobi_diag": (None, [C.POINTER(Mesh), D, D]),
+        "orc_gmres": (C.c_int, [C.POINTER(Mesh), D, D, D, C.c_double, C.c_int, C.c_int, C.c_int, D]),
+        "orc_update_b": (None, [C.POINTER(Mesh), D, D, D]),
+        "orc_update_e": (C.c_double, [C.POINTER(Mesh), D, D, D]),
+        "orc_ecsim_step": (C.c_int, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D, D,
+                                     D, D, D, C.c_double, C.c_int, C.c_int, D]),
+        "orc_dipole_b": (None, [D, C.c_double, C.c_double, D, D]),
+        "orc_trace": (C.c_long, [C.c_long, D, D, I32, I64, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, D, C.c_double, C.c_double, C.c_long, C.c_double,
+                                 C.c_double, C.c_int]),
+    }
+    for k, (r, a) in sig.items():
+        f = getattr(lib, k)
+        f.restype = r
+        f.argtypes = a
+    _lib = lib
+    return lib
+
+
+def p(a, t=C.c_double):
+    if a is None:
+        return None
+    assert a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def mesh_of(wl):
+    m = Mesh()
+    m.nbx, m.nby, m.nbz = wl.mesh.nbx, wl.mesh.nby, wl.mesh.nbz
+    for d in range(3):
+        m.x0[d] = wl.mesh.x0[d]
+        m.dx[d] = wl.mesh.dx
+    m.nspec = len(wl.species)
+    for i, s in enumerate(wl.species):
+        m.q[i], m.m[i], m.w[i] = s.charge, s.mass, s.weight
+    m.dt, m.theta = wl.dt, wl.theta
+    return m
+
+
+class OracleState:
+    """FP64 oracle state for one workload (global periodic corner layout)."""
+
+    def __init__(self, wl, x, v, spec, fields, wcorr=None):
+        self.lib = load()
+        self.wl = wl
+        self.m = mesh_of(wl)
+        n = len(spec)
+        self.x = np.ascontiguousarray(x, np.float64).copy()
+        self.v = np.ascontiguousarray(v, np.float64).copy()
+        self.spec = np.ascontiguousarray(spec, np.uint8).copy()
+        self.wcorr = None if wcorr is None else np.ascontiguousarray(wcorr, np.float64)
+        self.block = np.zeros(n, np.int32)
+        self.cell = np.zeros(n, np.int32)
+        self.lib.orc_locate(C.byref(self.m), n, p(self.x), p(self.block, C.c_int32),
+                            p(self.cell, C.c_int32))
+        nc = wl.mesh.ncells
+        self.E_n = np.ascontiguousarray(fields["E_n"], np.float64).copy()
+        self.E_half = np.ascontiguousarray(fields["E_half"], np.float64).copy()
+        self.Bcen = np.ascontiguousarray(fields["B_center"], np.float64).copy()
+        self.Bprev = np.ascontiguousarray(fields["B_corner_prev"], np.float64).copy()
+        self.Bcur = np.ascontiguousarray(fields["B_corner_cur"], np.float64).copy()
+        self.J = np.zeros((nc, 3))
+        self.M = np.zeros((nc, 243))
+
+    def push(self):
+        return self.lib.orc_push(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
+                                 p(self.spec, C.c_uint8), p(self.block, C.c_int32),
+                                 p(self.cell, C.c_int32), p(self.E_half), p(self.Bprev))
+
+    def deposit(self):
+        return self.lib.orc_deposit(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
+                                    p(self.spec, C.c_uint8), p(self.wcorr),
+                                    p(self.block, C.c_int32), p(self.cell, C.c_int32),
+                                    p(self.Bcur), p(self.J), p(self.M))
+
+    def step(self, tol=1e-8, maxit=200, precond=0):
+        diag = np.zeros(3)
+        it = self.lib.orc_ecsim_step(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
+                                     p(self.spec, C.c_uint8), p(self.wcorr),
+                                     p(self.block, C.c_int32), p(self.cell, C.c_int32),
+                                     p(self.E_n), p(self.E_half), p(self.Bcen), p(self.Bprev),
+                                     p(self.Bcur), p(self.J), p(self.M), tol, maxit, precond,
+                                     p(diag))
+        return it, diag
+
+    def rhs(self):
+        out = np.zeros_like(self.E_n)
+        self.lib.orc_rhs(C.byref(self.m), p(self.E_n), p(self.Bcen), p(self.J), p(self.M), p(out))
+        return out
+
+    def matvec(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self.lib.orc_matvec(C.byref(self.m), p(self.M), p(x), p(y))
+        return y
+
+
+def trace(x, pm, q, m0, b_eq, r_e, b_ext, r_in, r_out, max_steps, dphi, dt_max):
+    lib = load()
+    n = len(x)
+    x = np.ascontiguousarray(x, np.float64).copy()
+    pm = np.ascontiguousarray(pm, np.float64).copy()
+    st = np.zeros(n, np.int32)
+    steps = np.zeros(n, np.int64)
+    ext = np.ascontiguousarray(b_ext, np.float64)
+    tot = lib.orc_trace(n, p(x), p(pm), p(st, C.c_int32), p(steps, C.c_int64), q, m0, b_eq, r_e,
+                        p(ext), r_in, r_out, max_steps, dphi, dt_max, 0)
+    return x, pm, st, steps, tot

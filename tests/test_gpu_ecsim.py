@@ -1,0 +1,199 @@
+"""GPU parity of the ECSIM hot path against the FP64 oracle, through the C ABI.
+
+Tolerances (FP32 push/deposit against FP64):
+  positions  |dx| <= 4e-6 cell            (FP32 block-local offsets: ulp(8) = 4.8e-7)
+  velocities |dv| <= 2e-5 * max|v|
+  J, M       max|d| / max|ref| <= 1e-5    (the 1e-5 field/moment target)
+  energies   relative 1e-6
+  block / cell ids bit-exact except particles whose FP64 position lies within
+  2e-6 cell of a cell face (these are counted and reported)
+Field solve (FP64 both sides, GMRES to 1e-11): relative 1e-8.
+"""
+import numpy as np
+import pytest
+
+import amps_gb300 as A
+from tests import gpu_cases as G
+from tests import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+
+def compare_particles(ctx, st, pos_tol=4e-6, face_eps=2e-6):
+    g = G.by_id(ctx.export_particles())
+    assert len(g["id"]) == len(st.spec)
+    np.testing.assert_array_equal(g["id"], np.arange(len(st.spec)))
+    np.testing.assert_array_equal(g["spec"], st.spec)
+    dxp = np.abs(g["x"] - st.x)
+    L = np.array(st.wl.mesh.shape) * st.wl.mesh.dx  # domain length per axis
+    dxp = np.minimum(dxp, np.abs(dxp - L))   # periodic images
+    assert dxp.max() <= pos_tol, dxp.max()
+    vmax = np.abs(st.v).max()
+    assert np.abs(g["v"] - st.v).max() <= 2e-5 * vmax
+    mism = (g["block"] != st.block) | (g["cell"] != st.cell)
+    near = G.face_distance(st.x) < face_eps
+    assert not (mism & ~near).any(), np.flatnonzero(mism & ~near)[:10]
+    return int(mism.sum()), int(near.sum())
+
+
+@pytest.mark.parametrize("vscale", [1.0, 40.0])
+def test_push_matches_oracle(vscale):
+    wl, ic, x, f = G.make_case(vscale=vscale)
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    st = G.oracle_state(wl, ic, x, f)
+    # import locates particles with the reference rules
+    g0 = G.by_id(ctx.export_particles())
+    np.testing.assert_array_equal(g0["block"], st.block)
+    np.testing.assert_array_equal(g0["cell"], st.cell)
+    np.testing.assert_array_equal(g0["x"], st.x)
+    nout = ctx.MoveParticles()
+    assert nout == 0
+    assert st.push() == 0
+    mism, near = compare_particles(ctx, st)
+    print("push vscale=%g: %d id mismatches, %d particles within 2e-6 of a face" % (vscale, mism, near))
+    if vscale > 1:
+        g1 = G.by_id(ctx.export_particles())
+        # block crossings, including the periodic wrap, were exercised
+        assert (g1["block"] != g0["block"]).sum() > 1000
+
+
+def test_deposit_matches_oracle():
+    wl, ic, x, f = G.make_case()
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    st = G.oracle_state(wl, ic, x, f)
+    eg = ctx.UpdateJMassMatrix()
+    eo = st.deposit()
+    J, M = ctx.export_moments()
+    assert G.rel_err(J, st.J) <= 1e-5, G.rel_err(J, st.J)
+    assert G.rel_err(M, st.M) <= 1e-5, G.rel_err(M, st.M)
+    # diagonal 3x3 self-blocks separately (largest terms)
+    assert G.rel_err(M[:, :9], st.M[:, :9]) <= 1e-5
+    assert eg == pytest.approx(eo, rel=1e-6)
+
+
+def test_deposit_with_weight_correction():
+    wl, ic, x, f = G.make_case(nb=(1, 1, 2), ppc=4)
+    rng = np.random.default_rng(3)
+    wc = rng.uniform(0.5, 2.0, len(ic["spec"])).astype(np.float32).astype(np.float64)
+    ctx = G.gpu_ctx(wl, ic, x, f, wcorr=wc)
+    st = G.oracle_state(wl, ic, x, f, wcorr=wc)
+    eg = ctx.UpdateJMassMatrix()
+    eo = st.deposit()
+    J, M = ctx.export_moments()
+    assert G.rel_err(J, st.J) <= 1e-5
+    assert G.rel_err(M, st.M) <= 1e-5
+    assert eg == pytest.approx(eo, rel=1e-6)
+
+
+def oracle_field_solve(st, tol, precond):
+    lib = O.load()
+    b = st.rhs()
+    xs = np.zeros_like(b)
+    res = np.zeros(1)
+    it = lib.orc_gmres(O.C.byref(st.m), O.p(st.M), O.p(b), O.p(xs), tol, 500, 30, precond, O.p(res))
+    assert it > 0
+    Eh = st.E_n + xs
+    Bn = np.zeros_like(st.Bcen)
+    lib.orc_update_b(O.C.byref(st.m), O.p(Eh), O.p(st.Bcen), O.p(Bn))
+    Bc = np.zeros_like(Bn)
+    lib.orc_center_to_corner(O.C.byref(st.m), O.p(Bn), O.p(Bc))
+    En = st.E_n.copy()
+    wave = lib.orc_update_e(O.C.byref(st.m), O.p(Eh), O.p(En), O.p(Bn))
+    return {"E_half": Eh, "B_center": Bn, "B_corner_cur": Bc, "E_n": En, "wave": wave, "it": it}
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+def test_field_solve_matches_oracle(precond):
+    wl, ic, x, f = G.make_case(nb=(2, 2, 1), ppc=8)
+    st = G.oracle_state(wl, ic, x, f)
+    st.deposit()
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    ctx.import_moments(st.J, st.M)
+    s = ctx.TimeStep(tol=1e-11, maxit=400, precond=precond)
+    assert s.converged == 1 and s.rel_residual <= 1e-10
+    ref = oracle_field_solve(st, 1e-11, precond)
+    out = ctx.export_fields()
+    for k in ("E_half", "B_center", "B_corner_cur", "E_n"):
+        assert G.rel_err(out[k], ref[k]) <= 1e-8, (k, G.rel_err(out[k], ref[k]))
+    np.testing.assert_allclose(out["B_corner_prev"], f["B_corner_cur"], rtol=0, atol=0)
+    assert s.wave_energy == pytest.approx(ref["wave"], rel=1e-10)
+    print("GMRES precond=%d: gpu %d iterations, oracle %d" % (precond, s.iterations, ref["it"]))
+
+
+def test_full_steps_match_oracle_and_conserve_energy():
+    wl, ic, x, f = G.make_case(nb=(2, 2, 2), ppc=8, e_amp=0.0, b_amp=0.0)
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    st = G.oracle_state(wl, ic, x, f)
+    e0 = st.deposit()
+    wave0 = np.sum(st.Bcen ** 2 + st.E_n ** 2) / (8 * np.pi)
+    tot0 = e0 + wave0
+    for _ in range(3):
+        s = ctx.PicTimeStep(tol=1e-10, maxit=400, precond=1)
+        it, diag = st.step(tol=1e-10, maxit=400, precond=1)
+        assert s.solve.converged == 1
+        assert s.particle_energy == pytest.approx(diag[0], rel=1e-6)
+        assert s.solve.wave_energy == pytest.approx(diag[1], rel=1e-5)
+        drift = abs(s.particle_energy + s.solve.wave_energy - tot0) / tot0
+        assert drift < 1e-6, drift
+    out = ctx.export_fields()
+    J, M = ctx.export_moments()
+    # field perturbations are tiny relative to B0: compare perturbation parts
+    for k, ref in (("E_n", st.E_n), ("E_half", st.E_half)):
+        assert G.rel_err(out[k], ref) <= 1e-4, (k, G.rel_err(out[k], ref))
+    assert G.rel_err(out["B_center"] - np.array(wl.b0), st.Bcen - np.array(wl.b0)) <= 1e-4
+    assert G.rel_err(J, st.J) <= 1e-5 and G.rel_err(M, st.M) <= 1e-5
+    compare_particles(ctx, st, pos_tol=2e-5)
+
+
+def test_empty_particle_set():
+    wl, ic, x, f = G.make_case(nb=(1, 1, 1), ppc=1)
+    ctx = A.EcsimContext(wl, capacity=16, track_ids=True)
+    ctx.import_fields(**f)
+    ctx.import_particles(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0, np.uint8))
+    assert ctx.num_particles() == 0
+    e = ctx.push_deposit()
+    J, M = ctx.export_moments()
+    assert e == 0.0 and not J.any() and not M.any()
+    s = ctx.PicTimeStep(tol=1e-8, maxit=50, precond=0)
+    assert s.solve.converged == 1
+
+
+def test_capacity_and_argument_errors():
+    wl, ic, x, f = G.make_case(nb=(1, 1, 1), ppc=2)
+    ctx = A.EcsimContext(wl, capacity=10)
+    with pytest.raises(A.AmpsGpuError) as e:
+        ctx.import_particles(x, ic["v"].astype(np.float64), ic["spec"])
+    assert e.value.status == 6
+    with pytest.raises(A.AmpsGpuError) as e:
+        ctx.TimeStep(tol=-1.0)
+    assert e.value.status == 1
+    bad = A.electron_proton_plasma("bad", 0, 1, 1, 1, 1)
+    with pytest.raises(A.AmpsGpuError) as e:
+        A.EcsimContext(bad)
+    assert e.value.status == 1
+
+
+def test_gmres_not_converged_reports_status():
+    wl, ic, x, f = G.make_case(nb=(1, 1, 1), ppc=4)
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    ctx.UpdateJMassMatrix()
+    with pytest.raises(A.AmpsGpuError) as e:
+        ctx.TimeStep(tol=1e-14, maxit=1, precond=0)
+    assert e.value.status == 3
+
+
+def test_face_positions_import_and_wrap():
+    wl = A.electron_proton_plasma("faces", 2, 1, 1, 1, 1)
+    L = 16.0
+    x = np.array([[0.0, 0.5, 0.5], [8.0, 0.5, 0.5], [16.0 - 1e-12, 3.0, 7.999999999],
+                  [-1e-9, 0.25, 0.25], [16.0, 1.0, 1.0], [7.9999999999, 4.0, 4.0]])
+    v = np.zeros_like(x)
+    spec = np.zeros(len(x), np.uint8)
+    ctx = A.EcsimContext(wl, capacity=16)
+    ctx.import_fields(**A.initial_fields(wl))
+    ctx.import_particles(x, v, spec)
+    st = O.OracleState(wl, x, v, spec, A.initial_fields(wl))
+    g = G.by_id(ctx.export_particles())
+    np.testing.assert_array_equal(g["block"], st.block)
+    np.testing.assert_array_equal(g["cell"], st.cell)
+    assert np.all(g["x"] >= 0) and np.all(g["x"][:, 0] < L)

@@ -1,0 +1,160 @@
+"""The FP64 oracle against the reference's own code and known answers (CPU only).
+
+* operator taps vs the reference stencil algebra (golden stencil_taps.json)
+* corner-pair slot table vs ProcessCell's IndexMatrix (golden index_matrix.json)
+* gridless relativistic Boris vs the reference-compiled BorisStep (golden
+  gridless_boris.json)
+* ECSIM invariants the reference relies on: theta = 0.5 conserves total energy,
+  the mass matrix is symmetric in the corner pair, GMRES meets its stop rule
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests import oracle_lib as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def slot(di, dj, dk):
+    dig = lambda o: 0 if o == 0 else (1 if o < 0 else 2)
+    return dig(di) + 3 * dig(dj) + 9 * dig(dk)
+
+
+def table(name, *args):
+    lib = O.load()
+    out = np.zeros(27)
+    getattr(lib, name)(*args, O.p(out))
+    return out
+
+
+def taps_to_table(taps):
+    t = np.zeros(27)
+    for i, j, k, a in taps:
+        t[slot(i, j, k)] += a
+    return t
+
+
+def test_stencil_taps_match_reference_stencil_library():
+    g = json.load(open(os.path.join(GOLD, "stencil_taps.json")))
+    for ax, key in enumerate(("lap_x", "lap_y", "lap_z")):
+        np.testing.assert_array_equal(table("orc_laplacian_table", ax), taps_to_table(g[key]))
+        np.testing.assert_array_equal(table("orc_graddiv_table", ax, ax), taps_to_table(g[key]))
+    for (p, q), key in {(0, 1): "gd_xy", (0, 2): "gd_xz", (1, 2): "gd_yz"}.items():
+        ref = taps_to_table(g[key])
+        np.testing.assert_array_equal(table("orc_graddiv_table", p, q), ref)
+        np.testing.assert_array_equal(table("orc_graddiv_table", q, p), ref)
+
+
+def test_stencils_are_consistent_second_derivatives():
+    # applied to x^2 the Laplacian taps give 2, to x*y the mixed taps give 1
+    for ax in range(3):
+        lap = table("orc_laplacian_table", ax)
+        s = 0.0
+        for dk in (-1, 0, 1):
+            for dj in (-1, 0, 1):
+                for di in (-1, 0, 1):
+                    s += lap[slot(di, dj, dk)] * (di, dj, dk)[ax] ** 2
+        assert s == pytest.approx(2.0)
+    gd = table("orc_graddiv_table", 0, 1)
+    s = sum(gd[slot(di, dj, dk)] * di * dj for di in (-1, 0, 1) for dj in (-1, 0, 1)
+            for dk in (-1, 0, 1))
+    assert s == pytest.approx(1.0)
+
+
+def test_corner_pair_slots_match_index_matrix():
+    g = json.load(open(os.path.join(GOLD, "index_matrix.json")))["IndexMatrix"]
+    off = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    for c1 in range(8):
+        for c2 in range(8):
+            d = [off[c2][a] - off[c1][a] for a in range(3)]
+            assert slot(*d) == g[c1][c2]
+
+
+def test_corner_weights_table_order():
+    lib = O.load()
+    xl = np.array([0.25, 0.5, 0.75])
+    w = np.zeros(8)
+    lib.orc_corner_weights(O.p(xl), O.p(w))
+    off = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    for t, o in enumerate(off):
+        e = np.prod([xl[a] if o[a] else 1 - xl[a] for a in range(3)])
+        assert w[t] == pytest.approx(e, rel=1e-15)
+    assert w.sum() == pytest.approx(1.0, rel=1e-15)
+
+
+def test_gridless_boris_matches_reference_build():
+    g = json.load(open(os.path.join(GOLD, "gridless_boris.json")))
+    x, pm, st, steps, tot = O.trace(np.array(g["x0"]), np.array(g["p0"]), g["q"], g["m0"],
+                                    g["b_eq"], g["r_e"], np.array(g["b_ext"]), g["r_in"],
+                                    g["r_out"], g["max_steps"], g["dphi"], g["dt_max"])
+    np.testing.assert_array_equal(st, np.array(g["status"]))
+    np.testing.assert_array_equal(steps, np.array(g["steps"]))
+    # same operations up to the dipole factorisation; rounding differences grow
+    # over up to 3000 steps to a few 1e-9 relative
+    gx, gp = np.array(g["x"]), np.array(g["p"])
+    assert (np.linalg.norm(x - gx, axis=1) / np.linalg.norm(gx, axis=1)).max() < 1e-7
+    assert (np.linalg.norm(pm - gp, axis=1) / np.linalg.norm(gp, axis=1)).max() < 1e-7
+
+
+def small_state(nb=(1, 1, 1), ppc=4, seed=100, b0=(0.0, 0.0, 0.5), e_amp=0.0):
+    import amps_gb300 as A
+    wl = A.electron_proton_plasma("t", *nb, ppc, 3)
+    wl.seed = seed
+    ic = A.make_initial_condition(wl, nthreads=2)
+    x = A.physical_positions(wl.mesh, ic["u"], ic["block"])
+    f = A.initial_fields(wl)
+    if e_amp:
+        rng = np.random.default_rng(seed)
+        for k in ("E_n", "E_half"):
+            f[k] = e_amp * rng.standard_normal(f[k].shape)
+    return wl, ic, x, f
+
+
+def test_ecsim_energy_conserved_theta_half():
+    wl, ic, x, f = small_state(nb=(1, 1, 1), ppc=8)
+    st = O.OracleState(wl, x, ic["v"].astype(np.float64), ic["spec"], f)
+    e0 = st.deposit()
+    # wave energy of the initial state
+    wave0 = np.sum(st.Bcen ** 2 + st.E_n ** 2) / (8 * np.pi) * wl.mesh.dx ** 3
+    tot0 = e0 + wave0
+    hist = []
+    for _ in range(3):
+        it, diag = st.step(tol=1e-12, maxit=400, precond=1)
+        assert it > 0
+        hist.append(diag[0] + diag[1])
+    drift = np.abs(np.array(hist) - tot0) / tot0
+    assert drift.max() < 1e-9, (tot0, hist)
+
+
+def test_mass_matrix_pair_symmetry():
+    # M_c[slot(d)] of corner c equals M_{c+d}[slot(-d)] (ProcessCell adds the same
+    # 3x3 block to both corners of a pair)
+    wl, ic, x, f = small_state(nb=(1, 1, 1), ppc=4)
+    st = O.OracleState(wl, x, ic["v"].astype(np.float64), ic["spec"], f)
+    st.deposit()
+    M = st.M.reshape(8, 8, 8, 27, 9)  # [K][J][I][slot][ab]
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        I, J, K = rng.integers(0, 8, 3)
+        d = rng.integers(-1, 2, 3)
+        a = M[K, J, I, slot(*d)]
+        b = M[(K + d[2]) % 8, (J + d[1]) % 8, (I + d[0]) % 8, slot(*(-d))]
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-18)
+
+
+def test_gmres_meets_stop_rule():
+    wl, ic, x, f = small_state(nb=(1, 1, 1), ppc=4, e_amp=1e-3)
+    st = O.OracleState(wl, x, ic["v"].astype(np.float64), ic["spec"], f)
+    st.deposit()
+    b = st.rhs().ravel().copy()
+    for precond in (0, 1):
+        xs = np.zeros_like(b)
+        res = np.zeros(1)
+        it = O.load().orc_gmres(O.C.byref(st.m), O.p(st.M), O.p(b), O.p(xs), 1e-10, 500, 30,
+                                precond, O.p(res))
+        assert it > 0
+        r = b - st.matvec(xs.reshape(-1, 3)).ravel()
+        assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(b)
