@@ -92,6 +92,9 @@ WORKLOADS = {
     "ecsim_32c_64ppc": lambda: electron_proton_plasma("ecsim_32c_64ppc", 4, 4, 4, 64, 10),
     # 64^3 cells as 8^3 blocks, 128 ppc/species (67,108,864 particles)
     "ecsim_64c_128ppc": lambda: electron_proton_plasma("ecsim_64c_128ppc", 8, 8, 8, 128, 100),
+    # 40^3 cells, 64 ppc/species (8,192,000 particles, 205 MB of particle state:
+    # larger than the 129 MB L2, small enough for full ncu captures)
+    "ecsim_40c_64ppc": lambda: electron_proton_plasma("ecsim_40c_64ppc", 5, 5, 5, 64, 10),
     # small cases for tests
     "ecsim_16c_8ppc": lambda: electron_proton_plasma("ecsim_16c_8ppc", 2, 2, 2, 8, 3),
     "ecsim_8c_4ppc": lambda: electron_proton_plasma("ecsim_8c_4ppc", 1, 1, 1, 4, 2),
