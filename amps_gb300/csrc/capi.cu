@@ -9,11 +9,6 @@
 
 #include "common.cuh"
 
-cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
-                               const uint8_t* d_spec_in, const double* d_wc, long long n);
-cudaError_t launch_import_local(amps_gpu_ctx* c, const int32_t* d_block, long long n);
-cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, int32_t* d_blk,
-                          int32_t* d_cel);
 cudaError_t launch_add(amps_gpu_ctx* c, const double* a, const double* b, double* o, long long n);
 
 // ---------------------------------------------------------------------------
@@ -34,7 +29,7 @@ struct Pending {
   cudaEvent_t a, b;
   int nk;
 };
-// pending timed launches per context (kept outside the struct to keep it POD-light)
+// pending timed launches per context
 std::vector<Pending>& pending(amps_gpu_ctx* c) {
   static std::vector<std::pair<amps_gpu_ctx*, std::vector<Pending>>> tab;
   for (auto& e : tab)
@@ -139,15 +134,21 @@ amps_gpu_status download_vec3(amps_gpu_ctx* c, const double* dev, double* host) 
   return AMPS_GPU_OK;
 }
 
-// staging buffers for FP64 particle import/export (allocated on first use)
+// staging buffers for particle import/export (allocated on first use)
 struct Staging {
-  double* x = nullptr;
+  double* x = nullptr;   // 3n doubles (also 3n floats for the local import)
   double* v = nullptr;
   double* wc = nullptr;
   uint8_t* sp = nullptr;
   int32_t* i0 = nullptr;
   int32_t* i1 = nullptr;
+  uint32_t* id = nullptr;
   long long cap = 0;
+  void release() {
+    cudaFree(x); cudaFree(v); cudaFree(wc); cudaFree(sp); cudaFree(i0); cudaFree(i1); cudaFree(id);
+    x = v = wc = nullptr; sp = nullptr; i0 = i1 = nullptr; id = nullptr;
+    cap = 0;
+  }
 };
 std::vector<std::pair<amps_gpu_ctx*, Staging>>& staging_tab() {
   static std::vector<std::pair<amps_gpu_ctx*, Staging>> t;
@@ -163,11 +164,13 @@ Staging* staging(amps_gpu_ctx* c, long long need) {
     s = &t.back().second;
   }
   if (s->cap < need) {
-    cudaFree(s->x); cudaFree(s->v); cudaFree(s->wc); cudaFree(s->sp); cudaFree(s->i0); cudaFree(s->i1);
-    s->cap = 0;
+    s->release();
     if (dalloc(&s->x, 3 * need) || dalloc(&s->v, 3 * need) || dalloc(&s->wc, need) ||
-        dalloc(&s->sp, need) || dalloc(&s->i0, need) || dalloc(&s->i1, need))
+        dalloc(&s->sp, need) || dalloc(&s->i0, need) || dalloc(&s->i1, need) ||
+        dalloc(&s->id, need)) {
+      s->release();
       return nullptr;
+    }
     s->cap = need;
   }
   return s;
@@ -176,16 +179,17 @@ void staging_free(amps_gpu_ctx* c) {
   auto& t = staging_tab();
   for (size_t i = 0; i < t.size(); i++)
     if (t[i].first == c) {
-      Staging& s = t[i].second;
-      cudaFree(s.x); cudaFree(s.v); cudaFree(s.wc); cudaFree(s.sp); cudaFree(s.i0); cudaFree(s.i1);
+      t[i].second.release();
       t.erase(t.begin() + i);
       return;
     }
 }
 
-amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long* ulp) {
+// Reads the device flags (one synchronisation).  Overflow is returned, not an error.
+amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long* ulp,
+                            long long* overflow) {
   amps_gpu_status s = cuda_check(
-      c, cudaMemcpyAsync(c->h_flags, c->d_flags, 3 * sizeof(unsigned long long),
+      c, cudaMemcpyAsync(c->h_flags, c->d_flags, 4 * sizeof(unsigned long long),
                          cudaMemcpyDeviceToHost, c->stream),
       "read flags");
   if (s) return s;
@@ -193,6 +197,7 @@ amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long*
   if (s) return s;
   if (out_of_block) *out_of_block = (long long)c->h_flags[0];
   if (ulp) *ulp = (long long)c->h_flags[1];
+  if (overflow) *overflow = (long long)c->h_flags[3];
   if (c->h_flags[2]) {
     return set_err(c, AMPS_GPU_DEVICE_TIMEOUT,
                    "device reported " + std::to_string(c->h_flags[2]) +
@@ -202,8 +207,29 @@ amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long*
 }
 
 amps_gpu_status reset_flags(amps_gpu_ctx* c) {
-  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 3 * sizeof(unsigned long long), c->stream),
+  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 5 * sizeof(unsigned long long), c->stream),
                     "reset flags");
+}
+
+// One particle step (push, optionally fused with the deposit), with recovery
+// when the slack of some destination cell overflowed.
+amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_block,
+                              long long* near_face) {
+  amps_gpu_status s;
+  if ((s = reset_flags(c))) return s;
+  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+    return s;
+  if ((s = cuda_check(c, launch_push_step(c, deposit), "push step"))) return s;
+  long long ovf = 0;
+  if ((s = check_flags(c, out_of_block, near_face, &ovf))) return s;
+  if (ovf > 0) {
+    // rare: some cell ran out of slack.  Re-sort everything (new slack) and
+    // redo the deposition from the rebuilt layout.
+    if ((s = cuda_check(c, particles_recover(c, ovf), "overflow recovery"))) return s;
+    if (deposit && (s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+    if ((s = check_flags(c, nullptr, nullptr, nullptr))) return s;
+  }
+  return AMPS_GPU_OK;
 }
 
 }  // namespace
@@ -220,9 +246,11 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
     return AMPS_GPU_INVALID_ARG;
   for (int s = 0; s < cfg->nspec; s++)
     if (cfg->mass[s] <= 0.0) return AMPS_GPU_INVALID_ARG;
-  long long nbl = (long long)cfg->nbx * cfg->nby * cfg->nbz;
-  if (nbl * 512 > (1LL << 30) || cfg->particle_capacity > (1LL << 31) - 1)
-    return AMPS_GPU_INVALID_ARG;
+  const long long nbl = (long long)cfg->nbx * cfg->nby * cfg->nbz;
+  const long long nc = nbl * 512;
+  // slot capacity: particles + 1/4 slack + 8 slack slots per cell
+  const long long slots = cfg->particle_capacity + cfg->particle_capacity / 4 + 8 * nc + 1024;
+  if (nc > (1LL << 28) || slots > (1LL << 31) - 1) return AMPS_GPU_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return AMPS_GPU_NO_DEVICE;
   if (cfg->device < 0 || cfg->device >= ndev) return AMPS_GPU_INVALID_ARG;
@@ -231,9 +259,9 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
   amps_gpu_ctx* c = new amps_gpu_ctx();
   c->cfg = *cfg;
   c->nb = (int)nbl;
-  c->ncor = nbl * 512;
+  c->ncor = nc;
   c->cap = cfg->particle_capacity;
-  const long long nc = c->ncor;
+  c->slots = slots;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   bool ok = e == cudaSuccess;
   ok = ok && !dalloc(&c->d_nbr, (size_t)c->nb * 27);
@@ -248,14 +276,15 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
        !dalloc(&c->d_stencil_dep, (size_t)c->nb * AMPS_SC * AMPS_DEP_STRIDE);
   for (int bsel = 0; bsel < 2 && ok; bsel++) {
     for (int q = 0; q < 3; q++)
-      ok = ok && !dalloc(&c->d_u[bsel][q], c->cap) && !dalloc(&c->d_v[bsel][q], c->cap);
-    ok = ok && !dalloc(&c->d_sp[bsel], c->cap) && !dalloc(&c->d_wc[bsel], c->cap);
-    if (cfg->track_ids) ok = ok && !dalloc(&c->d_id[bsel], c->cap);
+      ok = ok && !dalloc(&c->d_u[bsel][q], slots) && !dalloc(&c->d_v[bsel][q], slots);
+    ok = ok && !dalloc(&c->d_sp[bsel], slots) && !dalloc(&c->d_wc[bsel], slots);
+    if (cfg->track_ids) ok = ok && !dalloc(&c->d_id[bsel], slots);
   }
-  ok = ok && !dalloc(&c->d_key, c->cap) && !dalloc(&c->d_rank, c->cap) &&
-       !dalloc(&c->d_count, nc + 1) && !dalloc(&c->d_start, nc + 1) &&
-       !dalloc(&c->d_scan_part, (nc + 1) / 1024 + 2) && !dalloc(&c->d_flags, 4);
-  ok = ok && cudaMallocHost(&c->h_flags, 4 * sizeof(unsigned long long)) == cudaSuccess;
+  ok = ok && !dalloc(&c->d_key, slots) && !dalloc(&c->d_rank, slots) &&
+       !dalloc(&c->d_base, nc + 1) && !dalloc(&c->d_cnt, nc) && !dalloc(&c->d_arr, nc) &&
+       !dalloc(&c->d_stay, nc) && !dalloc(&c->d_tmp, nc + 1) && !dalloc(&c->d_count, nc + 1) &&
+       !dalloc(&c->d_scan_part, (nc + 1) / 1024 + 2) && !dalloc(&c->d_flags, 8);
+  ok = ok && cudaMallocHost(&c->h_flags, 8 * sizeof(unsigned long long)) == cudaSuccess;
   ok = ok && !dalloc(&c->d_cellM, 324 * nc) && !dalloc(&c->d_cellJ, 24 * nc) &&
        !dalloc(&c->d_energy, 4);
   ok = ok && cudaMallocHost(&c->h_energy, 4 * sizeof(double)) == cudaSuccess;
@@ -278,16 +307,22 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
   }
   ok = cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice) ==
        cudaSuccess;
-  ok = ok && cudaMemset(c->d_En, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-       cudaMemset(c->d_Eh, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-       cudaMemset(c->d_Bc, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-       cudaMemset(c->d_Bcor_prev, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-       cudaMemset(c->d_Bcor_cur, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-       cudaMemset(c->d_J, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-       cudaMemset(c->d_M, 0, sizeof(double) * 243 * nc) == cudaSuccess &&
-       cudaMemset(c->d_count, 0, sizeof(int) * (nc + 1)) == cudaSuccess &&
-       cudaMemset(c->d_start, 0, sizeof(int) * (nc + 1)) == cudaSuccess &&
-       cudaMemset(c->d_flags, 0, sizeof(unsigned long long) * 4) == cudaSuccess;
+  double* zero_d[] = {c->d_En, c->d_Eh, c->d_Bc, c->d_Bcor_prev, c->d_Bcor_cur, c->d_J};
+  for (double* p : zero_d) ok = ok && cudaMemset(p, 0, sizeof(double) * 3 * nc) == cudaSuccess;
+  ok = ok && cudaMemset(c->d_M, 0, sizeof(double) * 243 * nc) == cudaSuccess;
+  // empty layout: every cell has 8 slack slots
+  {
+    std::vector<int> base((size_t)nc + 1);
+    for (long long i = 0; i <= nc; i++) base[(size_t)i] = (int)(8 * i);
+    ok = ok && cudaMemcpy(c->d_base, base.data(), sizeof(int) * (nc + 1), cudaMemcpyHostToDevice) ==
+                   cudaSuccess;
+  }
+  ok = ok && cudaMemset(c->d_cnt, 0, sizeof(int) * nc) == cudaSuccess &&
+       cudaMemset(c->d_arr, 0, sizeof(int) * nc) == cudaSuccess &&
+       cudaMemset(c->d_stay, 0, sizeof(int) * nc) == cudaSuccess &&
+       cudaMemset(c->d_sp[0], 0xFF, (size_t)slots) == cudaSuccess &&
+       cudaMemset(c->d_sp[1], 0xFF, (size_t)slots) == cudaSuccess &&
+       cudaMemset(c->d_flags, 0, sizeof(unsigned long long) * 8) == cudaSuccess;
   if (!ok) {
     amps_gpu_destroy(c);
     return AMPS_GPU_CUDA_ERROR;
@@ -304,8 +339,9 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   staging_free(c);
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
                   c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
-                  c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_count,
-                  c->d_start, c->d_scan_part, c->d_flags, c->d_cellM, c->d_cellJ, c->d_energy};
+                  c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
+                  c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
+                  c->d_cellM, c->d_cellJ, c->d_energy};
   for (void* p : ptrs) cudaFree(p);
   for (int b = 0; b < 2; b++) {
     for (int q = 0; q < 3; q++) {
@@ -361,7 +397,8 @@ amps_gpu_status amps_gpu_import_particles(amps_gpu_ctx* c, long long n, const do
   }
   st = cuda_check(c, launch_import_fp64(c, s->x, s->v, s->sp, wcorr ? s->wc : nullptr, n), "import");
   if (st) return st;
-  return check_flags(c, nullptr, nullptr);
+  c->have_moments = false;
+  return check_flags(c, nullptr, nullptr, nullptr);
 }
 
 amps_gpu_status amps_gpu_import_particles_local(amps_gpu_ctx* c, long long n, const float* u,
@@ -376,26 +413,20 @@ amps_gpu_status amps_gpu_import_particles_local(amps_gpu_ctx* c, long long n, co
   c->has_wcorr = false;
   amps_gpu_status st = reset_flags(c);
   if (st) return st;
-  const int cur = c->cur;
   cudaStream_t q = c->stream;
+  float* du = reinterpret_cast<float*>(s->x);
+  float* dv = reinterpret_cast<float*>(s->v);
   if (n > 0) {
-    // de-interleave on the host into the SoA buffers
-    std::vector<float> tmp((size_t)n);
-    for (int d = 0; d < 3; d++) {
-      for (long long p = 0; p < n; p++) tmp[(size_t)p] = u[3 * p + d];
-      if ((st = cuda_check(c, cudaMemcpy(c->d_u[cur][d], tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "H2D u")))
-        return st;
-      for (long long p = 0; p < n; p++) tmp[(size_t)p] = v[3 * p + d];
-      if ((st = cuda_check(c, cudaMemcpy(c->d_v[cur][d], tmp.data(), sizeof(float) * n, cudaMemcpyHostToDevice), "H2D v")))
-        return st;
-    }
-    if ((st = cuda_check(c, cudaMemcpyAsync(c->d_sp[cur], spec, n, cudaMemcpyHostToDevice, q), "H2D spec")) ||
+    if ((st = cuda_check(c, cudaMemcpyAsync(du, u, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, q), "H2D u")) ||
+        (st = cuda_check(c, cudaMemcpyAsync(dv, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, q), "H2D v")) ||
+        (st = cuda_check(c, cudaMemcpyAsync(s->sp, spec, n, cudaMemcpyHostToDevice, q), "H2D spec")) ||
         (st = cuda_check(c, cudaMemcpyAsync(s->i0, block, sizeof(int32_t) * n, cudaMemcpyHostToDevice, q), "H2D block")))
       return st;
   }
-  st = cuda_check(c, launch_import_local(c, s->i0, n), "import_local");
+  st = cuda_check(c, launch_import_local(c, du, dv, s->sp, s->i0, n), "import_local");
   if (st) return st;
-  return check_flags(c, nullptr, nullptr);
+  c->have_moments = false;
+  return check_flags(c, nullptr, nullptr, nullptr);
 }
 
 amps_gpu_status amps_gpu_num_particles(amps_gpu_ctx* c, long long* n) {
@@ -408,6 +439,7 @@ amps_gpu_status amps_gpu_export_particles(amps_gpu_ctx* c, double* x, double* v,
                                           int32_t* block, int32_t* cell, uint32_t* id,
                                           long long* n) {
   if (!c) return AMPS_GPU_INVALID_ARG;
+  if (id && !c->cfg.track_ids) return set_err(c, AMPS_GPU_INVALID_ARG, "export: ids not tracked");
   cudaSetDevice(c->cfg.device);
   const long long np = c->np;
   if (n) *n = np;
@@ -415,21 +447,17 @@ amps_gpu_status amps_gpu_export_particles(amps_gpu_ctx* c, double* x, double* v,
   Staging* s = staging(c, np);
   if (!s) return set_err(c, AMPS_GPU_CUDA_ERROR, "staging allocation failed");
   amps_gpu_status st = cuda_check(
-      c, launch_export(c, x ? s->x : nullptr, v ? s->v : nullptr, block ? s->i0 : nullptr,
-                       cell ? s->i1 : nullptr),
+      c, launch_export(c, x ? s->x : nullptr, v ? s->v : nullptr, spec ? s->sp : nullptr,
+                       block ? s->i0 : nullptr, cell ? s->i1 : nullptr, id ? s->id : nullptr),
       "export");
   if (st) return st;
   cudaStream_t q = c->stream;
-  const int cur = c->cur;
   if (x && (st = cuda_check(c, cudaMemcpyAsync(x, s->x, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, q), "D2H x"))) return st;
   if (v && (st = cuda_check(c, cudaMemcpyAsync(v, s->v, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost, q), "D2H v"))) return st;
   if (block && (st = cuda_check(c, cudaMemcpyAsync(block, s->i0, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, q), "D2H block"))) return st;
   if (cell && (st = cuda_check(c, cudaMemcpyAsync(cell, s->i1, sizeof(int32_t) * np, cudaMemcpyDeviceToHost, q), "D2H cell"))) return st;
-  if (spec && (st = cuda_check(c, cudaMemcpyAsync(spec, c->d_sp[cur], np, cudaMemcpyDeviceToHost, q), "D2H spec"))) return st;
-  if (id) {
-    if (!c->cfg.track_ids) return set_err(c, AMPS_GPU_INVALID_ARG, "export: ids not tracked");
-    if ((st = cuda_check(c, cudaMemcpyAsync(id, c->d_id[cur], sizeof(uint32_t) * np, cudaMemcpyDeviceToHost, q), "D2H id"))) return st;
-  }
+  if (spec && (st = cuda_check(c, cudaMemcpyAsync(spec, s->sp, np, cudaMemcpyDeviceToHost, q), "D2H spec"))) return st;
+  if (id && (st = cuda_check(c, cudaMemcpyAsync(id, s->id, sizeof(uint32_t) * np, cudaMemcpyDeviceToHost, q), "D2H id"))) return st;
   return cuda_check(c, cudaStreamSynchronize(q), "export sync");
 }
 
@@ -505,13 +533,7 @@ amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
 amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* c, long long* out_of_block) {
   if (!c) return AMPS_GPU_INVALID_ARG;
   cudaSetDevice(c->cfg.device);
-  amps_gpu_status s;
-  if ((s = reset_flags(c))) return s;
-  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
-    return s;
-  if ((s = cuda_check(c, launch_push(c), "push"))) return s;
-  if ((s = cuda_check(c, launch_rebin(c), "rebin"))) return s;
-  return check_flags(c, out_of_block, nullptr);
+  return particle_step(c, false, out_of_block, nullptr);
 }
 
 amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* c, double* particle_energy) {
@@ -525,7 +547,7 @@ amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* c, double* particle_
   if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
                                          cudaMemcpyDeviceToHost, c->stream), "energy")))
     return s;
-  if ((s = check_flags(c, nullptr, nullptr))) return s;
+  if ((s = check_flags(c, nullptr, nullptr, nullptr))) return s;
   if (particle_energy) *particle_energy = c->h_energy[0];
   c->have_moments = true;
   return AMPS_GPU_OK;
@@ -534,20 +556,14 @@ amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* c, double* particle_
 amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* c, double* particle_energy) {
   if (!c) return AMPS_GPU_INVALID_ARG;
   cudaSetDevice(c->cfg.device);
-  amps_gpu_status s;
-  if ((s = reset_flags(c))) return s;
-  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
-    return s;
-  if ((s = cuda_check(c, launch_push(c), "push"))) return s;
-  if ((s = cuda_check(c, launch_rebin(c), "rebin"))) return s;
-  if ((s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+  amps_gpu_status s = particle_step(c, true, nullptr, nullptr);
+  if (s) return s;
   if (particle_energy) {
-    if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
-                                           cudaMemcpyDeviceToHost, c->stream), "energy")))
+    if ((s = cuda_check(c, cudaMemcpy(c->h_energy, c->d_energy, sizeof(double),
+                                      cudaMemcpyDeviceToHost), "energy")))
       return s;
+    *particle_energy = c->h_energy[0];
   }
-  if ((s = check_flags(c, nullptr, nullptr))) return s;
-  if (particle_energy) *particle_energy = c->h_energy[0];
   c->have_moments = true;
   return AMPS_GPU_OK;
 }
@@ -591,16 +607,10 @@ amps_gpu_status amps_gpu_step(amps_gpu_ctx* c, double tol, int maxit, int precon
   }
   amps_gpu_status fs = amps_gpu_field_solve(c, tol, maxit, precond, &st.solve);
   if (fs != AMPS_GPU_OK && fs != AMPS_GPU_GMRES_NOT_CONVERGED) return fs;
-  if ((s = reset_flags(c))) return s;
-  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+  if ((s = particle_step(c, true, &st.out_of_block, &st.ulp_face))) return s;
+  if ((s = cuda_check(c, cudaMemcpy(c->h_energy, c->d_energy, sizeof(double),
+                                    cudaMemcpyDeviceToHost), "energy")))
     return s;
-  if ((s = cuda_check(c, launch_push(c), "push"))) return s;
-  if ((s = cuda_check(c, launch_rebin(c), "rebin"))) return s;
-  if ((s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
-  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
-                                         cudaMemcpyDeviceToHost, c->stream), "energy")))
-    return s;
-  if ((s = check_flags(c, &st.out_of_block, &st.ulp_face))) return s;
   st.particle_energy = c->h_energy[0];
   c->have_moments = true;
   if (stats) *stats = st;

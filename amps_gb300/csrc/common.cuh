@@ -6,7 +6,7 @@
 //   FP64 vectors are component-major: v[comp*ncor + corner]
 //   mass matrix M: 243 coefficient planes, M[e*ncor + corner] (coalesced per plane)
 //   particles: FP32 SoA (u: block-local offset in cell units, v), species byte,
-//              optional 32-bit id; sorted by key = block*512 + cell
+//              optional 32-bit id; every cell owns a slot range with slack
 //   per-block FP32 field stencils (9^3 corners incl. the +1 halo) for the push
 //   and deposit kernels, contiguous per block so one bulk TMA copy stages them.
 #pragma once
@@ -66,8 +66,10 @@ struct amps_gpu_ctx {
   float* d_stencil_push = nullptr;  // nb * 729 * 8
   float* d_stencil_dep = nullptr;   // nb * 729 * 4
 
-  // particles (double-buffered SoA)
-  long long cap = 0, np = 0;
+  // particles: two FP32 SoA buffers of `slots` entries.  Buffer `cur` holds the
+  // slotted cell layout (cell c owns [base[c], base[c+1]), occupancy cnt[c]);
+  // the other one is the unsorted list used by import and overflow recovery.
+  long long cap = 0, np = 0, slots = 0;
   float* d_u[2][3] = {{nullptr}};
   float* d_v[2][3] = {{nullptr}};
   uint8_t* d_sp[2] = {nullptr, nullptr};
@@ -75,12 +77,17 @@ struct amps_gpu_ctx {
   uint32_t* d_id[2] = {nullptr, nullptr};
   int cur = 0;
   bool has_wcorr = false;
-  int32_t* d_key = nullptr;     // destination key per particle
-  int32_t* d_rank = nullptr;    // rank inside the destination cell
-  int32_t* d_count = nullptr;   // ncor+1
-  int32_t* d_start = nullptr;   // ncor+1 (exclusive scan)
+  int32_t* d_base = nullptr;    // ncor+1 slot offsets
+  int32_t* d_cnt = nullptr;     // ncor occupancy
+  int32_t* d_arr = nullptr;     // ncor arrivals in the current step
+  int32_t* d_stay = nullptr;    // ncor stayers in the current step
+  int32_t* d_tmp = nullptr;     // ncor+1 scratch for scans
+  int32_t* d_key = nullptr;     // slots: list keys (import / overflow)
+  int32_t* d_rank = nullptr;    // slots: rank inside the destination cell (rebuild)
+  int32_t* d_count = nullptr;   // ncor+1 histogram (rebuild)
   int32_t* d_scan_part = nullptr;
-  unsigned long long* d_flags = nullptr;  // [0] out-of-block, [1] ulp-face, [2] bad
+  // [0] moved > 1 block, [1] near a cell face, [2] device error, [3] overflow, [4] list tail
+  unsigned long long* d_flags = nullptr;
   unsigned long long* h_flags = nullptr;  // pinned
 
   // deposition scratch: per-cell partial sums
@@ -113,9 +120,15 @@ void flush_timers(amps_gpu_ctx* c);
 // ---- kernel launchers (particles.cu) ----
 cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
                                  const double* Bcur);
-cudaError_t launch_push(amps_gpu_ctx* c);
-cudaError_t launch_rebin(amps_gpu_ctx* c);
+cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit);
 cudaError_t launch_deposit(amps_gpu_ctx* c);
+cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
+cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
+                               const uint8_t* d_spec_in, const double* d_wc, long long n);
+cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* d_v,
+                                const uint8_t* d_sp, const int32_t* d_block, long long n);
+cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, uint8_t* d_sp,
+                          int32_t* d_blk, int32_t* d_cel, uint32_t* d_id);
 
 // ---- field launchers (field.cu) ----
 cudaError_t launch_rhs(amps_gpu_ctx* c);

@@ -1,23 +1,38 @@
 // Particle kernels of the ECSIM hot path on sm_103a.
 //
-//   k_pack_stencils  per-block FP32 copies of E^{n+theta}, corner B^n, corner
-//                    B^{n+1} on the block's 9^3 corners (the SetBlock_E/SetBlock_B
-//                    scratch of src/pic/pic_mover.cpp:86-167)
-//   k_push           Lapenta2017 (src/pic/pic_mover_boris.cpp:876-1120) +
-//                    destination block/cell (findTreeNode/FindCellIndex,
-//                    meshAMRgeneric.h:2256-2320,2852-2883) with periodic wrap
-//                    (pic_bc_periodic.cpp:86-178); warp-aggregated cell counts
-//   k_scan_*         exclusive scan of the per-cell counts
-//   k_scatter        stable-by-warp scatter into the destination cell ranges
-//                    (the temp-list commit of pic_mover.cpp:982-1087)
-//   k_deposit        ProcessCell (pic_field_solver_ecsim.cpp:1882-2438): one warp
-//                    per cell, FP32 per-particle terms, register tiles, Kahan-
-//                    compensated chunk sums, per-cell partials
-//   k_assemble       flush of the per-cell partials into the 243-term corner
-//                    mass matrix and corner J (:2362-2426 and the shared-corner
-//                    sum of :3931-3968), FP64
+// Particle layout: every cell owns a slot range [base[c], base[c+1]) of the
+// FP32 SoA arrays; its cnt[c] particles sit at the front, the rest is slack
+// (species byte 0xFF marks an empty slot).  Almost every particle stays in its
+// cell during a step, so the step never re-sorts the whole population:
+//
+//   k_push_deposit<DEP>  one warp per cell: Lapenta2017 push of the cell's
+//                        particles (src/pic/pic_mover_boris.cpp:876-1120) with
+//                        E^{n+theta} and corner B^n gathered from a per-block
+//                        stencil staged by one bulk (TMA) copy; particles that
+//                        stay are compacted in place and, when DEP, deposited
+//                        right away with ProcessCell's terms
+//                        (pic_field_solver_ecsim.cpp:1882-2438); particles that
+//                        leave are written into the slack of their destination
+//                        cell (findTreeNode/FindCellIndex rules,
+//                        meshAMRgeneric.h:2256-2320,2852-2883, periodic wrap of
+//                        pic_bc_periodic.cpp:86-178), or to an overflow list
+//   k_arrivals<DEP>      one warp per cell: deposits the particles that arrived,
+//                        moves them behind the stayers, updates cnt
+//   k_deposit            full ProcessCell pass over the compact layout
+//                        (UpdateJMassMatrix without a preceding push)
+//   k_assemble           per-cell partial sums -> 243-term corner mass matrix
+//                        and corner J in FP64 (:2362-2426, shared corners summed)
+//   rebuild              counting sort of an unsorted list into the slotted
+//                        layout: import, and recovery when slack overflows
+//
+// Deposition arithmetic: per particle the 36 corner-pair weight products,
+// k*alpha (9), the 8 weights and q*alpha*v are staged in shared memory; each
+// lane then owns a 4 x 3 tile of the 36x9 mass-matrix block (27 lanes) or of
+// the 8x3 current block (2 lanes) and accumulates it in registers over chunks
+// of 32 particles, adding chunk sums with Kahan compensation.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 
 #include "common.cuh"
@@ -26,6 +41,9 @@
 namespace {
 
 constexpr uint32_t kWaitLimit = 1u << 24;
+constexpr int kRec = 60;      // floats per staged particle record
+constexpr int kWarps = 8;     // warps per CTA (one row of 8 cells each)
+constexpr uint8_t kHole = 0xFF;
 
 struct SpeciesTab {
   float qdt2m[AMPS_GPU_MAX_SPECIES];  // 0.5*q*dt/m (weight independent)
@@ -43,16 +61,68 @@ SpeciesTab make_species(const amps_gpu_config& c) {
   return t;
 }
 
+// SoA view of one particle buffer
+struct PBuf {
+  float* u[3];
+  float* v[3];
+  uint8_t* sp;
+  float* wc;    // may be null
+  uint32_t* id; // may be null
+};
+
+PBuf pbuf(amps_gpu_ctx* c, int which) {
+  PBuf b;
+  for (int q = 0; q < 3; q++) {
+    b.u[q] = c->d_u[which][q];
+    b.v[q] = c->d_v[which][q];
+  }
+  b.sp = c->d_sp[which];
+  b.wc = c->has_wcorr ? c->d_wc[which] : nullptr;
+  b.id = c->cfg.track_ids ? c->d_id[which] : nullptr;
+  return b;
+}
+
+__device__ __forceinline__ void copy_particle(const PBuf& s, long long ps, const PBuf& d,
+                                              long long pd) {
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    d.u[q][pd] = s.u[q][ps];
+    d.v[q][pd] = s.v[q][ps];
+  }
+  d.sp[pd] = s.sp[ps];
+  if (d.wc) d.wc[pd] = s.wc[ps];
+  if (d.id) d.id[pd] = s.id[ps];
+}
+
+__device__ __forceinline__ float clamp_below8(float u) {
+  return u < 8.0f ? u : 7.99999952316284180f;  // nextafterf(8, 0)
+}
+
+// Warp-aggregated reservation: one atomic per distinct key among active lanes;
+// ranks inside the warp follow lane order.  Returns the reserved index.
+__device__ __forceinline__ int warp_reserve(bool active, int key, int* __restrict__ counter) {
+  const unsigned act = __ballot_sync(0xffffffffu, active);
+  int r = -1;
+  if (active) {
+    const unsigned peers = __match_any_sync(act, key);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(counter + key, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    r = base + __popc(peers & lanemask_lt());
+  }
+  return r;
+}
+
 // ---------------------------------------------------------------------------
-// stencil packing
 __global__ void k_pack_stencils(int nb, long long ncor, const int* __restrict__ nbr,
                                 const double* __restrict__ Eh, const double* __restrict__ Bprev,
                                 const double* __restrict__ Bcur, float* __restrict__ sp,
                                 float* __restrict__ sd) {
   const int b = blockIdx.x;
   for (int s = threadIdx.x; s < AMPS_SC; s += blockDim.x) {
-    int i = s % 9, j = (s / 9) % 9, k = s / 81;
-    int cid = local_id(nbr, b, i, j, k);
+    const int i = s % 9, j = (s / 9) % 9, k = s / 81;
+    const int cid = local_id(nbr, b, i, j, k);
     float4* op = reinterpret_cast<float4*>(sp + ((size_t)b * AMPS_SC + s) * AMPS_PUSH_STRIDE);
     op[0] = make_float4((float)Eh[cid], (float)Eh[ncor + cid], (float)Eh[2 * ncor + cid],
                         (float)Bprev[cid]);
@@ -62,141 +132,522 @@ __global__ void k_pack_stencils(int nb, long long ncor, const int* __restrict__ 
   }
 }
 
-// Warp-aggregated slot reservation in the destination cell: one atomic per
-// distinct key in the warp, ranks inside the warp follow lane order.
-__device__ __forceinline__ void reserve_slot(bool active, int key, int* __restrict__ count,
-                                             int* __restrict__ rank_out, long long p) {
-  unsigned act = __ballot_sync(0xffffffffu, active);
-  if (!active) return;
-  unsigned peers = __match_any_sync(act, key);
-  int leader = __ffs(peers) - 1;
-  int lane = threadIdx.x & 31;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(count + key, __popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  rank_out[p] = base + __popc(peers & lanemask_lt());
-}
-
-__device__ __forceinline__ float clamp_below8(float u) {
-  return u < 8.0f ? u : 7.99999952316284180f;  // nextafterf(8, 0)
-}
-
-// ---------------------------------------------------------------------------
-// Lapenta2017 push + destination key
-struct PushArgs {
-  const int* nbr;
-  const int* start;
-  const float* stencil;
-  float* ux; float* uy; float* uz;
-  float* vx; float* vy; float* vz;
-  const uint8_t* sp;
-  int* key;
-  int* rank;
-  int* count;
-  unsigned long long* flags;
-  float dtdx[3];
-  float dt;
-  SpeciesTab st;
-};
-
-__global__ void __launch_bounds__(256) k_push(PushArgs a) {
-  extern __shared__ __align__(16) float4 s_st[];  // 729 corners x 2 float4
-  __shared__ __align__(8) uint64_t bar;
-  const int b = blockIdx.x;
-  const int p0 = a.start[b * AMPS_CPB], p1 = a.start[(b + 1) * AMPS_CPB];
-  const long long n = p1 - p0;
-  const int lo = p0 + (int)(n * blockIdx.y / gridDim.y);
-  const int hi = p0 + (int)(n * (blockIdx.y + 1) / gridDim.y);
-  if (lo >= hi) return;
-  const uint32_t bytes = AMPS_SC * AMPS_PUSH_STRIDE * sizeof(float);
+// Stage one bulk copy per stencil into shared memory; returns false on timeout.
+__device__ bool stage_stencils(uint64_t* bar, void* dst0, const void* src0, uint32_t bytes0,
+                               void* dst1, const void* src1, uint32_t bytes1,
+                               unsigned long long* flags) {
   if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
+    mbar_init(bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(&bar, bytes);
-    bulk_copy_g2s(s_st, a.stencil + (size_t)b * AMPS_SC * AMPS_PUSH_STRIDE, bytes, &bar);
+    mbar_arrive_expect_tx(bar, bytes0 + bytes1);
+    if (bytes0) bulk_copy_g2s(dst0, src0, bytes0, bar);
+    if (bytes1) bulk_copy_g2s(dst1, src1, bytes1, bar);
   }
-  if (!mbar_wait_bounded(&bar, 0, kWaitLimit)) {
-    if (threadIdx.x == 0) atomicAdd(a.flags + 2, 1ull);
-    mbar_wait_bounded(&bar, 0, kWaitLimit);
-    return;
+  if (!mbar_wait_bounded(bar, 0, kWaitLimit)) {
+    if (threadIdx.x == 0) atomicAdd(flags + 2, 1ull);
+    mbar_wait_bounded(bar, 0, kWaitLimit);  // let the copies land before exiting
+    return false;
   }
-  unsigned long long n_out = 0, n_ulp = 0;
-  for (int base = lo; base < hi; base += blockDim.x) {
-    const int p = base + threadIdx.x;
-    const bool act = p < hi;
-    int key = 0;
-    if (act) {
-      float u[3] = {a.ux[p], a.uy[p], a.uz[p]};
-      float v[3] = {a.vx[p], a.vy[p], a.vz[p]};
-      const int s = a.sp[p];
-      int ic[3];
-      float f[3];
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Deposition pieces shared by k_push_deposit, k_arrivals and k_deposit.
+
+// Record of one particle at block-local offset u inside cell (i,j,k).
+__device__ __forceinline__ double stage_record(float* __restrict__ r, const float4* __restrict__ sB,
+                                               float u0, float u1, float u2, float v0, float v1,
+                                               float v2, int s, float wcorr, int i, int j, int k,
+                                               const SpeciesTab& st, float inv_vol) {
+  const float fx = fminf(fmaxf(u0 - (float)i, 0.f), 1.f);
+  const float fy = fminf(fmaxf(u1 - (float)j, 0.f), 1.f);
+  const float fz = fminf(fmaxf(u2 - (float)k, 0.f), 1.f);
+  const float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
+  float w[8];
+  w[0] = gx * gy * gz; w[1] = fx * gy * gz; w[2] = fx * fy * gz; w[3] = gx * fy * gz;
+  w[4] = gx * gy * fz; w[5] = fx * gy * fz; w[6] = fx * fy * fz; w[7] = gx * fy * fz;
+  const int sb = i + 9 * (j + 9 * k);
+  const int coff[8] = {0, 1, 10, 9, 81, 82, 91, 90};
+  float B0 = 0.f, B1 = 0.f, B2 = 0.f;
 #pragma unroll
-      for (int d = 0; d < 3; d++) {
-        ic[d] = min(max((int)u[d], 0), AMPS_NC - 1);
-        f[d] = u[d] - (float)ic[d];
+  for (int c = 0; c < 8; c++) {
+    const float4 q = sB[sb + coff[c]];
+    B0 = fmaf(w[c], q.x, B0);
+    B1 = fmaf(w[c], q.y, B1);
+    B2 = fmaf(w[c], q.z, B2);
+  }
+  const float h = st.qdt2m[s];
+  const float h2 = h * h;
+  const float c0 = 1.0f / (1.0f + h2 * (B0 * B0 + B1 * B1 + B2 * B2));
+  const float P0 = -h * B0, P1 = -h * B1, P2 = -h * B2;
+  float al[9];
+  al[0] = c0 * (1.f + h2 * B0 * B0);
+  al[1] = c0 * (-P2 + h2 * B0 * B1);
+  al[2] = c0 * (P1 + h2 * B0 * B2);
+  al[3] = c0 * (P2 + h2 * B1 * B0);
+  al[4] = c0 * (1.f + h2 * B1 * B1);
+  al[5] = c0 * (-P0 + h2 * B1 * B2);
+  al[6] = c0 * (-P1 + h2 * B2 * B0);
+  al[7] = c0 * (P0 + h2 * B2 * B1);
+  al[8] = c0 * (1.f + h2 * B2 * B2);
+  const float qW = st.qw[s] * wcorr;
+  const float mW = st.mw[s] * wcorr;
+  const float kc = qW * h * inv_vol;
+  float4* r4 = reinterpret_cast<float4*>(r);
+  {
+    float ww[36];
+    int pr = 0;
+#pragma unroll
+    for (int c1 = 0; c1 < 8; c1++)
+#pragma unroll
+      for (int c2 = 0; c2 <= c1; c2++, pr++) ww[pr] = w[c1] * w[c2];
+#pragma unroll
+    for (int t = 0; t < 9; t++) r4[t] = make_float4(ww[4 * t], ww[4 * t + 1], ww[4 * t + 2], ww[4 * t + 3]);
+  }
+  r4[9] = make_float4(kc * al[0], kc * al[1], kc * al[2], 0.f);
+  r4[10] = make_float4(kc * al[3], kc * al[4], kc * al[5], 0.f);
+  r4[11] = make_float4(kc * al[6], kc * al[7], kc * al[8], 0.f);
+  r4[12] = make_float4(w[0], w[1], w[2], w[3]);
+  r4[13] = make_float4(w[4], w[5], w[6], w[7]);
+  const float vr0 = al[0] * v0 + al[1] * v1 + al[2] * v2;
+  const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
+  const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
+  r4[14] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
+  return 0.5 * (double)mW * ((double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2);
+}
+
+struct Tile {
+  float sum[12], cmp[12];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int e = 0; e < 12; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
+  }
+  // accumulate the cnt staged records of the warp, then compensated add
+  __device__ __forceinline__ void accumulate(const float* __restrict__ rec, int cnt, int offA,
+                                             int offB) {
+    float acc[12];
+#pragma unroll
+    for (int e = 0; e < 12; e++) acc[e] = 0.f;
+#pragma unroll 2
+    for (int r = 0; r < cnt; r++) {
+      const float4 A = *reinterpret_cast<const float4*>(rec + r * kRec + offA);
+      const float4 B = *reinterpret_cast<const float4*>(rec + r * kRec + offB);
+      const float av[4] = {A.x, A.y, A.z, A.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        acc[3 * q + 0] = fmaf(av[q], B.x, acc[3 * q + 0]);
+        acc[3 * q + 1] = fmaf(av[q], B.y, acc[3 * q + 1]);
+        acc[3 * q + 2] = fmaf(av[q], B.z, acc[3 * q + 2]);
       }
-      float E[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-      for (int cc = 0; cc < 2; cc++)
-#pragma unroll
-        for (int bb = 0; bb < 2; bb++)
-#pragma unroll
-          for (int aa = 0; aa < 2; aa++) {
-            const float w = (aa ? f[0] : 1.f - f[0]) * (bb ? f[1] : 1.f - f[1]) *
-                            (cc ? f[2] : 1.f - f[2]);
-            const int sidx = (ic[0] + aa) + 9 * (ic[1] + bb) + 81 * (ic[2] + cc);
-            const float4 q0 = s_st[2 * sidx], q1 = s_st[2 * sidx + 1];
-            E[0] = fmaf(w, q0.x, E[0]);
-            E[1] = fmaf(w, q0.y, E[1]);
-            E[2] = fmaf(w, q0.z, E[2]);
-            B[0] = fmaf(w, q0.w, B[0]);
-            B[1] = fmaf(w, q1.x, B[1]);
-            B[2] = fmaf(w, q1.y, B[2]);
-          }
-      // alpha (Eq. D.3) and v' = 2 alpha (v + qdt/2m E) - v (Eq. D.8)
-      const float h = a.st.qdt2m[s];
-      const float h2 = h * h;
-      const float c0 = 1.0f / (1.0f + h2 * (B[0] * B[0] + B[1] * B[1] + B[2] * B[2]));
-      const float P0 = -h * B[0], P1 = -h * B[1], P2 = -h * B[2];
-      const float t0 = fmaf(h, E[0], v[0]), t1 = fmaf(h, E[1], v[1]), t2 = fmaf(h, E[2], v[2]);
-      const float bt = h2 * (B[0] * t0 + B[1] * t1 + B[2] * t2);
-      // alpha t = c0 * (t + h2 B (B.t) - P x t ... ) written out row by row
-      const float a0 = c0 * (t0 + B[0] * bt + (-P2 * t1 + P1 * t2));
-      const float a1 = c0 * (t1 + B[1] * bt + (P2 * t0 - P0 * t2));
-      const float a2 = c0 * (t2 + B[2] * bt + (-P1 * t0 + P0 * t1));
-      float vn[3] = {2.f * a0 - v[0], 2.f * a1 - v[1], 2.f * a2 - v[2]};
-      int o[3];
-      bool far = false, nearf = false;
-#pragma unroll
-      for (int d = 0; d < 3; d++) {
-        float un = fmaf(vn[d], a.dtdx[d], u[d]);
-        int od = (int)floorf(un * 0.125f);
-        if (od > 1 || od < -1) far = true;
-        od = max(-1, min(1, od));
-        un -= 8.0f * (float)od;
-        un = clamp_below8(fmaxf(un, 0.0f));
-        o[d] = od;
-        u[d] = un;
-        ic[d] = min((int)un, AMPS_NC - 1);
-        float fr = un - rintf(un);
-        if (fabsf(fr) < 4.76837158203125e-7f) nearf = true;
-      }
-      if (far) n_out++;
-      if (nearf) n_ulp++;
-      const int nbk = (o[0] | o[1] | o[2]) ? __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2])) : b;
-      key = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
-      a.ux[p] = u[0]; a.uy[p] = u[1]; a.uz[p] = u[2];
-      a.vx[p] = vn[0]; a.vy[p] = vn[1]; a.vz[p] = vn[2];
-      a.key[p] = key;
     }
-    reserve_slot(act, key, a.count, a.rank, p);
+#pragma unroll
+    for (int e = 0; e < 12; e++) {
+      const float y = acc[e] - cmp[e];
+      const float t = sum[e] + y;
+      cmp[e] = (t - sum[e]) - y;
+      sum[e] = t;
+    }
   }
-  if (n_out) atomicAdd(a.flags + 0, n_out);
-  if (n_ulp) atomicAdd(a.flags + 1, n_ulp);
+  // write (or add to) the cell partials
+  __device__ __forceinline__ void flush(int lane, float* __restrict__ cellM,
+                                        float* __restrict__ cellJ, long long cid, bool add) {
+    if (lane < 27) {
+      const int g = lane / 3, hh = lane % 3;
+      float* dst = cellM + cid * 324;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+          const int o = (4 * g + q) * 9 + 3 * hh + e;
+          const float v = sum[3 * q + e] - cmp[3 * q + e];
+          dst[o] = add ? dst[o] + v : v;
+        }
+    } else if (lane < 29) {
+      const int g = lane - 27;
+      float* dst = cellJ + cid * 24;
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+          const int o = (4 * g + q) * 3 + e;
+          const float v = sum[3 * q + e] - cmp[3 * q + e];
+          dst[o] = add ? dst[o] + v : v;
+        }
+    }
+  }
+};
+
+__device__ __forceinline__ void lane_offsets(int lane, int& offA, int& offB) {
+  offA = lane < 27 ? 4 * (lane / 3) : 48 + 4 * (lane - 27);
+  offB = lane < 27 ? 36 + 4 * (lane % 3) : 56;
+}
+
+__device__ __forceinline__ void reduce_energy(double en, double* s_en, double* energy) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
+  if ((threadIdx.x & 31) == 0) s_en[threadIdx.x >> 5] = en;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_en[w];
+    if (t != 0.0) atomicAdd(energy, t);
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct StepArgs {
+  const int* nbr;
+  const int* base;
+  int* cnt;
+  int* arr;
+  int* stay;
+  const float* st_push;
+  const float* st_dep;
+  PBuf p;         // current slots
+  PBuf ovf;       // overflow list (the other buffer)
+  int* ovf_key;
+  float* cellM; float* cellJ;
+  double* energy;
+  unsigned long long* flags;  // [0] far, [1] near-face, [2] device error, [3] overflow count
+  float dtdx[3];
+  float inv_vol;
+  long long ovf_cap;
+  SpeciesTab st;
+};
+
+// Lapenta2017 velocity update v' = 2 alpha (v + h E) - v (Eqs. D.3, D.8)
+__device__ __forceinline__ void lapenta(float h, const float E[3], const float B[3], float v[3]) {
+  const float h2 = h * h;
+  const float c0 = 1.0f / (1.0f + h2 * (B[0] * B[0] + B[1] * B[1] + B[2] * B[2]));
+  const float P0 = -h * B[0], P1 = -h * B[1], P2 = -h * B[2];
+  const float t0 = fmaf(h, E[0], v[0]), t1 = fmaf(h, E[1], v[1]), t2 = fmaf(h, E[2], v[2]);
+  const float bt = h2 * (B[0] * t0 + B[1] * t1 + B[2] * t2);
+  const float a0 = c0 * (t0 + B[0] * bt + (-P2 * t1 + P1 * t2));
+  const float a1 = c0 * (t1 + B[1] * bt + (P2 * t0 - P0 * t2));
+  const float a2 = c0 * (t2 + B[2] * bt + (-P1 * t0 + P0 * t1));
+  v[0] = 2.f * a0 - v[0];
+  v[1] = 2.f * a1 - v[1];
+  v[2] = 2.f * a2 - v[2];
+}
+
+template <bool DEP>
+__global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  float4* s_push = s_dyn;                         // 729 x 2 float4
+  float4* s_dep = s_dyn + 2 * AMPS_SC;            // 729 float4
+  float* s_rec = reinterpret_cast<float*>(s_dyn + 3 * AMPS_SC);  // kWarps x 32 x kRec
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double s_en[kWarps];
+  const int b = blockIdx.x, k = blockIdx.y;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t bp = AMPS_SC * AMPS_PUSH_STRIDE * sizeof(float);
+  const uint32_t bd = DEP ? AMPS_SC * AMPS_DEP_STRIDE * sizeof(float) : 0;
+  if (!stage_stencils(&bar, s_push, a.st_push + (size_t)b * AMPS_SC * AMPS_PUSH_STRIDE, bp, s_dep,
+                      a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE, bd, a.flags))
+    return;
+  float* rec = s_rec + wid * 32 * kRec;
+  int offA, offB;
+  lane_offsets(lane, offA, offB);
+  double en = 0.0;
+  unsigned long long n_far = 0, n_near = 0;
+  const int j = wid;
+  for (int i = 0; i < AMPS_NC; i++) {
+    const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
+    const int b0 = a.base[cid], n0 = a.cnt[cid];
+    Tile tile;
+    tile.zero();
+    int nst = 0;
+    for (int q0 = 0; q0 < n0; q0 += 32) {
+      const int p = b0 + q0 + lane;
+      const bool act = q0 + lane < n0;
+      float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+      int s = 0, key = -1;
+      float wcv = 1.0f;
+      uint32_t idv = 0;
+      if (act) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) { u[d] = a.p.u[d][p]; v[d] = a.p.v[d][p]; }
+        s = a.p.sp[p];
+        if (a.p.wc) wcv = a.p.wc[p];
+        if (a.p.id) idv = a.p.id[p];
+        // gather E^{n+theta}, B^n at the old position
+        int ic[3];
+        float f[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          ic[d] = min(max((int)u[d], 0), AMPS_NC - 1);
+          f[d] = u[d] - (float)ic[d];
+        }
+        float E[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int cc = 0; cc < 2; cc++)
+#pragma unroll
+          for (int bb = 0; bb < 2; bb++)
+#pragma unroll
+            for (int aa = 0; aa < 2; aa++) {
+              const float w = (aa ? f[0] : 1.f - f[0]) * (bb ? f[1] : 1.f - f[1]) *
+                              (cc ? f[2] : 1.f - f[2]);
+              const int sidx = (ic[0] + aa) + 9 * (ic[1] + bb) + 81 * (ic[2] + cc);
+              const float4 q0v = s_push[2 * sidx], q1v = s_push[2 * sidx + 1];
+              E[0] = fmaf(w, q0v.x, E[0]);
+              E[1] = fmaf(w, q0v.y, E[1]);
+              E[2] = fmaf(w, q0v.z, E[2]);
+              B[0] = fmaf(w, q0v.w, B[0]);
+              B[1] = fmaf(w, q1v.x, B[1]);
+              B[2] = fmaf(w, q1v.y, B[2]);
+            }
+        lapenta(a.st.qdt2m[s], E, B, v);
+        int o[3];
+        bool far = false, nearf = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          float un = fmaf(v[d], a.dtdx[d], u[d]);
+          int od = (int)floorf(un * 0.125f);
+          if (od > 1 || od < -1) far = true;
+          od = max(-1, min(1, od));
+          un -= 8.0f * (float)od;
+          un = clamp_below8(fmaxf(un, 0.0f));
+          o[d] = od;
+          u[d] = un;
+          ic[d] = min((int)un, AMPS_NC - 1);
+          if (fabsf(un - rintf(un)) < 4.76837158203125e-7f) nearf = true;
+        }
+        if (far) n_far++;
+        if (nearf) n_near++;
+        const int nbk = (o[0] | o[1] | o[2]) ? __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2])) : b;
+        key = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+      }
+      const bool stays = act && key == (int)cid;
+      const unsigned smask = __ballot_sync(0xffffffffu, stays);
+      const int spos = __popc(smask & lanemask_lt());
+      __syncwarp();
+      if (stays) {
+        const long long d = b0 + nst + spos;
+#pragma unroll
+        for (int dd = 0; dd < 3; dd++) { a.p.u[dd][d] = u[dd]; a.p.v[dd][d] = v[dd]; }
+        if (d != p) {
+          a.p.sp[d] = (uint8_t)s;
+          if (a.p.wc) a.p.wc[d] = wcv;
+          if (a.p.id) a.p.id[d] = idv;
+        }
+        if (DEP)
+          en += stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv,
+                             i, j, k, a.st, a.inv_vol);
+      }
+      // movers: slack of the destination cell, else the overflow list
+      const bool mover = act && !stays;
+      const int slot = warp_reserve(mover, mover ? key : 0, a.arr);
+      if (mover) {
+        const int cb = a.base[key], ccap = a.base[key + 1] - cb, cn = a.cnt[key];
+        if (slot < ccap - cn) {
+          const long long d = (long long)cb + ccap - 1 - slot;
+#pragma unroll
+          for (int dd = 0; dd < 3; dd++) { a.p.u[dd][d] = u[dd]; a.p.v[dd][d] = v[dd]; }
+          a.p.sp[d] = (uint8_t)s;
+          if (a.p.wc) a.p.wc[d] = wcv;
+          if (a.p.id) a.p.id[d] = idv;
+        } else {
+          const unsigned long long o = atomicAdd(a.flags + 3, 1ull);
+          if ((long long)o < a.ovf_cap) {
+#pragma unroll
+            for (int dd = 0; dd < 3; dd++) { a.ovf.u[dd][o] = u[dd]; a.ovf.v[dd][o] = v[dd]; }
+            a.ovf.sp[o] = (uint8_t)s;
+            if (a.ovf.wc) a.ovf.wc[o] = wcv;
+            if (a.ovf.id) a.ovf.id[o] = idv;
+            a.ovf_key[o] = key;
+          } else {
+            atomicAdd(a.flags + 2, 1ull);
+          }
+        }
+      }
+      const int cst = __popc(smask);
+      if (DEP) {
+        __syncwarp();
+        if (lane < 29 && cst > 0) tile.accumulate(rec, cst, offA, offB);
+        __syncwarp();
+      }
+      nst += cst;
+    }
+    // vacated slots become holes
+    for (int t = nst + lane; t < n0; t += 32) a.p.sp[b0 + t] = kHole;
+    if (lane == 0) a.stay[cid] = nst;
+    if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid, false);
+  }
+  if (n_far) atomicAdd(a.flags + 0, n_far);
+  if (n_near) atomicAdd(a.flags + 1, n_near);
+  if (DEP) reduce_energy(en, s_en, a.energy);
+}
+
+// Arrivals: deposit (DEP), move behind the stayers, update the occupancy.
+template <bool DEP>
+__global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  float4* s_dep = s_dyn;
+  float* s_rec = reinterpret_cast<float*>(s_dyn + AMPS_SC);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double s_en[kWarps];
+  const int b = blockIdx.x, k = blockIdx.y;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (DEP) {
+    if (!stage_stencils(&bar, s_dep, a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE,
+                        AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0, a.flags))
+      return;
+  }
+  float* rec = s_rec + wid * 32 * kRec;
+  int offA, offB;
+  lane_offsets(lane, offA, offB);
+  double en = 0.0;
+  const int j = wid;
+  for (int i = 0; i < AMPS_NC; i++) {
+    const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
+    const int b0 = a.base[cid], cap = a.base[cid + 1] - b0, n0 = a.cnt[cid];
+    const int nst = a.stay[cid];
+    const int na = min(a.arr[cid], cap - n0);
+    if (na > 0) {
+      Tile tile;
+      tile.zero();
+      const int src0 = b0 + cap - na, dst0 = b0 + nst;
+      for (int q0 = 0; q0 < na; q0 += 32) {
+        const bool act = q0 + lane < na;
+        const long long ps = src0 + q0 + lane, pd = dst0 + q0 + lane;
+        float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+        int s = 0;
+        float wcv = 1.0f;
+        uint32_t idv = 0;
+        if (act) {
+#pragma unroll
+          for (int d = 0; d < 3; d++) { u[d] = a.p.u[d][ps]; v[d] = a.p.v[d][ps]; }
+          s = a.p.sp[ps];
+          if (a.p.wc) wcv = a.p.wc[ps];
+          if (a.p.id) idv = a.p.id[ps];
+        }
+        __syncwarp();
+        if (act) {
+#pragma unroll
+          for (int d = 0; d < 3; d++) { a.p.u[d][pd] = u[d]; a.p.v[d][pd] = v[d]; }
+          a.p.sp[pd] = (uint8_t)s;
+          if (a.p.wc) a.p.wc[pd] = wcv;
+          if (a.p.id) a.p.id[pd] = idv;
+          if (DEP)
+            en += stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+                               wcv, i, j, k, a.st, a.inv_vol);
+        }
+        if (DEP) {
+          __syncwarp();
+          const int cnt = min(32, na - q0);
+          if (lane < 29) tile.accumulate(rec, cnt, offA, offB);
+          __syncwarp();
+        }
+      }
+      __syncwarp();
+      // slots that held arrivals and are now beyond the new occupancy
+      for (int t = lane; t < na; t += 32) {
+        const int slot = src0 + t;
+        if (slot >= dst0 + na) a.p.sp[slot] = kHole;
+      }
+      if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid, true);
+    }
+    if (lane == 0) {
+      a.cnt[cid] = nst + na;
+      a.arr[cid] = 0;
+    }
+  }
+  if (DEP) reduce_energy(en, s_en, a.energy);
+}
+
+// Full deposition over the compact layout.
+__global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  float4* s_dep = s_dyn;
+  float* s_rec = reinterpret_cast<float*>(s_dyn + AMPS_SC);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double s_en[kWarps];
+  const int b = blockIdx.x, k = blockIdx.y;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (!stage_stencils(&bar, s_dep, a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE,
+                      AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0, a.flags))
+    return;
+  float* rec = s_rec + wid * 32 * kRec;
+  int offA, offB;
+  lane_offsets(lane, offA, offB);
+  double en = 0.0;
+  const int j = wid;
+  for (int i = 0; i < AMPS_NC; i++) {
+    const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
+    const int b0 = a.base[cid], n0 = a.cnt[cid];
+    Tile tile;
+    tile.zero();
+    for (int q0 = 0; q0 < n0; q0 += 32) {
+      const long long p = b0 + q0 + lane;
+      if (q0 + lane < n0)
+        en += stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p],
+                           a.p.v[0][p], a.p.v[1][p], a.p.v[2][p], a.p.sp[p],
+                           a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, a.inv_vol);
+      __syncwarp();
+      if (lane < 29) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
+      __syncwarp();
+    }
+    tile.flush(lane, a.cellM, a.cellJ, cid, false);
+  }
+  reduce_energy(en, s_en, a.energy);
+}
+
+// ---------------------------------------------------------------------------
+// Corner assembly.  For corner c and each of its 8 cells, the pair (c, c2) of
+// that cell lands in slot(c2 - c) of M_c.  The 64 (slot, cell, pair) entries are
+// grouped by slot so each output slot is written once.
+struct AsmEntry {
+  unsigned char slot, cell, pair, pad;
+};
+__constant__ AsmEntry c_asm[64];
+__constant__ unsigned char c_asm_corner[8];
+
+__global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __restrict__ nbr,
+                                                  const float* __restrict__ cellM,
+                                                  const float* __restrict__ cellJ, double inv_vol,
+                                                  double* __restrict__ M, double* __restrict__ J) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  const int b = (int)(c / AMPS_CPB), l = (int)(c % AMPS_CPB);
+  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+  int cell[8];
+#pragma unroll
+  for (int co = 0; co < 8; co++)
+    cell[co] = local_id(nbr, b, i - (co & 1), j - ((co >> 1) & 1), k - ((co >> 2) & 1));
+  double acc[9];
+  int cur = c_asm[0].slot;
+#pragma unroll
+  for (int e = 0; e < 9; e++) acc[e] = 0.0;
+  for (int t = 0; t < 64; t++) {
+    const AsmEntry en = c_asm[t];
+    if (en.slot != cur) {
+#pragma unroll
+      for (int e = 0; e < 9; e++) {
+        M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
+        acc[e] = 0.0;
+      }
+      cur = en.slot;
+    }
+    const float* src = cellM + (size_t)cell[en.cell] * 324 + en.pair * 9;
+#pragma unroll
+    for (int e = 0; e < 9; e++) acc[e] += (double)src[e];
+  }
+#pragma unroll
+  for (int e = 0; e < 9; e++) M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
+  double jj[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int co = 0; co < 8; co++) {
+    const float* src = cellJ + (size_t)cell[co] * 24 + c_asm_corner[co] * 3;
+    jj[0] += (double)src[0];
+    jj[1] += (double)src[1];
+    jj[2] += (double)src[2];
+  }
+  J[c] = jj[0] * inv_vol;
+  J[ncor + c] = jj[1] * inv_vol;
+  J[2 * ncor + c] = jj[2] * inv_vol;
 }
 
 // ---------------------------------------------------------------------------
@@ -256,9 +707,9 @@ __global__ void __launch_bounds__(1024) k_scan_parts(int* part, int nparts) {
   }
 }
 
-__global__ void __launch_bounds__(256) k_scan_final(const int* __restrict__ in, long long n,
-                                                    const int* __restrict__ part,
-                                                    int* __restrict__ out) {
+// in and out may alias (each element is read before it is written by the same thread)
+__global__ void __launch_bounds__(256) k_scan_final(const int* in, long long n,
+                                                    const int* __restrict__ part, int* out) {
   __shared__ int s_warp[32];
   long long base = (long long)blockIdx.x * kScanTile + threadIdx.x * 4;
   int v[4], s = 0;
@@ -277,270 +728,69 @@ __global__ void __launch_bounds__(256) k_scan_final(const int* __restrict__ in, 
 }
 
 // ---------------------------------------------------------------------------
-struct ScatterArgs {
-  const int* key; const int* rank; const int* start;
-  const float* su[3]; const float* sv[3]; const uint8_t* ssp; const float* swc; const uint32_t* sid;
-  float* du[3]; float* dv[3]; uint8_t* dsp; float* dwc; uint32_t* did;
-  long long n;
-};
-
-__global__ void __launch_bounds__(256) k_scatter(ScatterArgs a) {
-  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
-       p += (long long)gridDim.x * blockDim.x) {
-    const long long d = (long long)a.start[a.key[p]] + a.rank[p];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      a.du[c][d] = a.su[c][p];
-      a.dv[c][d] = a.sv[c][p];
-    }
-    a.dsp[d] = a.ssp[p];
-    if (a.swc) a.dwc[d] = a.swc[p];
-    if (a.sid) a.did[d] = a.sid[p];
+// Rebuild: unsorted particles (list buffer, keys) -> slotted layout.
+__global__ void __launch_bounds__(256) k_rb_rank(long long n, const int* __restrict__ key,
+                                                 int* __restrict__ rank, int* __restrict__ count) {
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long p = base + threadIdx.x;
+    const bool act = p < n;
+    const int r = warp_reserve(act, act ? key[p] : 0, count);
+    if (act) rank[p] = r;
   }
 }
 
-// ---------------------------------------------------------------------------
-// Deposition.  Record of one particle staged in shared memory (floats):
-//   [0,36)  w_c1*w_c2 for the 36 pairs c2<=c1 (pair = c1(c1+1)/2 + c2)
-//   [36,48) k*alpha in three groups of 4 (k = qW * qdt/2m / V; pad in slot 3)
-//   [48,56) w_c (InterpolationCoefficientTable order)
-//   [56,60) qW * alpha v (pad in slot 3)
-constexpr int kRec = 60;
-constexpr int kDepWarps = 8;
-
-struct DepositArgs {
-  const int* start;
-  const float* stencil;
-  const float* ux; const float* uy; const float* uz;
-  const float* vx; const float* vy; const float* vz;
-  const uint8_t* sp; const float* wc;
-  float* cellM; float* cellJ;
-  double* energy;
-  unsigned long long* flags;
-  float inv_vol;
-  SpeciesTab st;
-};
-
-__global__ void __launch_bounds__(256) k_deposit(DepositArgs a) {
-  extern __shared__ __align__(16) float4 s_dyn[];
-  float4* s_B = s_dyn;                                  // 729 float4
-  float* s_rec = reinterpret_cast<float*>(s_dyn + AMPS_SC);  // kDepWarps * 32 * kRec
-  __shared__ __align__(8) uint64_t bar;
-  __shared__ double s_en[kDepWarps];
-  const int b = blockIdx.x, k = blockIdx.y;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const uint32_t bytes = AMPS_SC * AMPS_DEP_STRIDE * sizeof(float);
-  if (threadIdx.x == 0) {
-    mbar_init(&bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(&bar, bytes);
-    bulk_copy_g2s(s_B, a.stencil + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE, bytes, &bar);
-  }
-  if (!mbar_wait_bounded(&bar, 0, kWaitLimit)) {
-    if (threadIdx.x == 0) atomicAdd(a.flags + 2, 1ull);
-    mbar_wait_bounded(&bar, 0, kWaitLimit);
-    return;
-  }
-  float* rec = s_rec + wid * 32 * kRec;
-  double en = 0.0;
-  const int j = wid;
-  // lane roles in the accumulation phase
-  const bool tile = lane < 29;
-  const int offA = lane < 27 ? 4 * (lane / 3) : 48 + 4 * (lane - 27);
-  const int offB = lane < 27 ? 36 + 4 * (lane % 3) : 56;
-  for (int i = 0; i < AMPS_NC; i++) {
-    const int cl = i + AMPS_NC * (j + AMPS_NC * k);
-    const long long cid = (long long)b * AMPS_CPB + cl;
-    const int p0 = a.start[cid], p1 = a.start[cid + 1];
-    float sum[12], cmp[12];
-#pragma unroll
-    for (int e = 0; e < 12; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
-    for (int base = p0; base < p1; base += 32) {
-      const int p = base + lane;
-      if (p < p1) {
-        const float u0 = a.ux[p], u1 = a.uy[p], u2 = a.uz[p];
-        const float v0 = a.vx[p], v1 = a.vy[p], v2 = a.vz[p];
-        const int s = a.sp[p];
-        const float wcorr = a.wc ? a.wc[p] : 1.0f;
-        const float fx = fminf(fmaxf(u0 - (float)i, 0.f), 1.f);
-        const float fy = fminf(fmaxf(u1 - (float)j, 0.f), 1.f);
-        const float fz = fminf(fmaxf(u2 - (float)k, 0.f), 1.f);
-        const float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
-        float w[8];
-        w[0] = gx * gy * gz; w[1] = fx * gy * gz; w[2] = fx * fy * gz; w[3] = gx * fy * gz;
-        w[4] = gx * gy * fz; w[5] = fx * gy * fz; w[6] = fx * fy * fz; w[7] = gx * fy * fz;
-        const int sb = i + 9 * (j + 9 * k);
-        const int coff[8] = {0, 1, 10, 9, 81, 82, 91, 90};
-        float B0 = 0.f, B1 = 0.f, B2 = 0.f;
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-          const float4 q = s_B[sb + coff[c]];
-          B0 = fmaf(w[c], q.x, B0);
-          B1 = fmaf(w[c], q.y, B1);
-          B2 = fmaf(w[c], q.z, B2);
-        }
-        const float h = a.st.qdt2m[s];
-        const float h2 = h * h;
-        const float c0 = 1.0f / (1.0f + h2 * (B0 * B0 + B1 * B1 + B2 * B2));
-        const float P0 = -h * B0, P1 = -h * B1, P2 = -h * B2;
-        float al[9];
-        al[0] = c0 * (1.f + h2 * B0 * B0);
-        al[1] = c0 * (-P2 + h2 * B0 * B1);
-        al[2] = c0 * (P1 + h2 * B0 * B2);
-        al[3] = c0 * (P2 + h2 * B1 * B0);
-        al[4] = c0 * (1.f + h2 * B1 * B1);
-        al[5] = c0 * (-P0 + h2 * B1 * B2);
-        al[6] = c0 * (-P1 + h2 * B2 * B0);
-        al[7] = c0 * (P0 + h2 * B2 * B1);
-        al[8] = c0 * (1.f + h2 * B2 * B2);
-        const float qW = a.st.qw[s] * wcorr;
-        const float mW = a.st.mw[s] * wcorr;
-        const float kc = qW * h * a.inv_vol;
-        en += 0.5 * (double)mW * ((double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2);
-        float* r = rec + lane * kRec;
-        float4* r4 = reinterpret_cast<float4*>(r);
-        float ww[36];
-        {
-          int pr = 0;
-#pragma unroll
-          for (int c1 = 0; c1 < 8; c1++)
-#pragma unroll
-            for (int c2 = 0; c2 <= c1; c2++, pr++) ww[pr] = w[c1] * w[c2];
-        }
-#pragma unroll
-        for (int t = 0; t < 9; t++) r4[t] = make_float4(ww[4 * t], ww[4 * t + 1], ww[4 * t + 2], ww[4 * t + 3]);
-        r4[9] = make_float4(kc * al[0], kc * al[1], kc * al[2], 0.f);
-        r4[10] = make_float4(kc * al[3], kc * al[4], kc * al[5], 0.f);
-        r4[11] = make_float4(kc * al[6], kc * al[7], kc * al[8], 0.f);
-        r4[12] = make_float4(w[0], w[1], w[2], w[3]);
-        r4[13] = make_float4(w[4], w[5], w[6], w[7]);
-        const float vr0 = al[0] * v0 + al[1] * v1 + al[2] * v2;
-        const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
-        const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
-        r4[14] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
-      }
-      __syncwarp();
-      const int cnt = min(32, p1 - base);
-      if (tile) {
-        float acc[12];
-#pragma unroll
-        for (int e = 0; e < 12; e++) acc[e] = 0.f;
-        for (int r = 0; r < cnt; r++) {
-          const float4 A = *reinterpret_cast<const float4*>(rec + r * kRec + offA);
-          const float4 Bv = *reinterpret_cast<const float4*>(rec + r * kRec + offB);
-          const float av[4] = {A.x, A.y, A.z, A.w};
-#pragma unroll
-          for (int q = 0; q < 4; q++) {
-            acc[3 * q + 0] = fmaf(av[q], Bv.x, acc[3 * q + 0]);
-            acc[3 * q + 1] = fmaf(av[q], Bv.y, acc[3 * q + 1]);
-            acc[3 * q + 2] = fmaf(av[q], Bv.z, acc[3 * q + 2]);
-          }
-        }
-        // compensated (Kahan) add of the chunk sum
-#pragma unroll
-        for (int e = 0; e < 12; e++) {
-          const float y = acc[e] - cmp[e];
-          const float t = sum[e] + y;
-          cmp[e] = (t - sum[e]) - y;
-          sum[e] = t;
-        }
-      }
-      __syncwarp();
-    }
-    // flush the cell partials
-    if (lane < 27) {
-      const int g = lane / 3, hh = lane % 3;
-      float* dst = a.cellM + cid * 324;
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++) dst[(4 * g + q) * 9 + 3 * hh + e] = sum[3 * q + e] - cmp[3 * q + e];
-    } else if (lane < 29) {
-      const int g = lane - 27;
-      float* dst = a.cellJ + cid * 24;
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++) dst[(4 * g + q) * 3 + e] = sum[3 * q + e] - cmp[3 * q + e];
-    }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
-  if (lane == 0) s_en[wid] = en;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < kDepWarps; w++) t += s_en[w];
-    atomicAdd(a.energy, t);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Corner assembly.  For corner c and each of its 8 cells, the pair (c, c2) of
-// that cell lands in slot(c2 - c) of M_c.  The 64 (slot, cell, pair) entries are
-// grouped by slot so each output slot is written once.
-struct AsmEntry {
-  unsigned char slot, cell, pair, pad;
-};
-__constant__ AsmEntry c_asm[64];
-__constant__ unsigned char c_asm_corner[8];  // table index of the corner inside cell co
-
-__global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __restrict__ nbr,
-                                                  const float* __restrict__ cellM,
-                                                  const float* __restrict__ cellJ, double inv_vol,
-                                                  double* __restrict__ M, double* __restrict__ J) {
+// cap[c] = count + slack, slack = max(8, count/4) scaled by num/den so that
+// the total fits the slot capacity; cap[ncell] = 0 (scan terminator)
+__global__ void __launch_bounds__(256) k_rb_caps(long long ncell, const int* __restrict__ count,
+                                                 int* __restrict__ cap, int num, int den) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncor) return;
-  const int b = (int)(c / AMPS_CPB), l = (int)(c % AMPS_CPB);
-  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
-  int cell[8];
-#pragma unroll
-  for (int co = 0; co < 8; co++)
-    cell[co] = local_id(nbr, b, i - (co & 1), j - ((co >> 1) & 1), k - ((co >> 2) & 1));
-  double acc[9];
-  int cur = c_asm[0].slot;
-#pragma unroll
-  for (int e = 0; e < 9; e++) acc[e] = 0.0;
-  for (int t = 0; t < 64; t++) {
-    const AsmEntry en = c_asm[t];
-    if (en.slot != cur) {
-#pragma unroll
-      for (int e = 0; e < 9; e++) {
-        M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
-        acc[e] = 0.0;
-      }
-      cur = en.slot;
+  if (c > ncell) return;
+  if (c == ncell) { cap[c] = 0; return; }
+  const int n = count[c];
+  const int slack = max(8, n >> 2);
+  cap[c] = n + (int)(((long long)slack * num) / den);
+}
+
+__global__ void __launch_bounds__(256) k_rb_scatter(long long n, const int* __restrict__ key,
+                                                    const int* __restrict__ rank,
+                                                    const int* __restrict__ base, PBuf s, PBuf d) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long q = (long long)base[key[p]] + rank[p];
+    copy_particle(s, p, d, q);
+  }
+}
+
+// Append every particle of the compact layout to the list buffer (overflow
+// recovery): one warp per cell, one atomic per chunk.
+__global__ void __launch_bounds__(256) k_gather_valid(long long ncell, const int* __restrict__ base,
+                                                      const int* __restrict__ cnt, PBuf s, PBuf d,
+                                                      int* __restrict__ key,
+                                                      unsigned long long* __restrict__ tail) {
+  const long long cid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (cid >= ncell) return;
+  const int b0 = base[cid], n0 = cnt[cid];
+  for (int q0 = 0; q0 < n0; q0 += 32) {
+    const int m = min(32, n0 - q0);
+    unsigned long long o = 0;
+    if (lane == 0) o = atomicAdd(tail, (unsigned long long)m);
+    o = __shfl_sync(0xffffffffu, o, 0);
+    if (lane < m) {
+      copy_particle(s, b0 + q0 + lane, d, (long long)o + lane);
+      key[o + lane] = (int)cid;
     }
-    const float* src = cellM + (size_t)cell[en.cell] * 324 + en.pair * 9;
-#pragma unroll
-    for (int e = 0; e < 9; e++) acc[e] += (double)src[e];
   }
-#pragma unroll
-  for (int e = 0; e < 9; e++) M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
-  double jj[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-  for (int co = 0; co < 8; co++) {
-    const float* src = cellJ + (size_t)cell[co] * 24 + c_asm_corner[co] * 3;
-    jj[0] += (double)src[0];
-    jj[1] += (double)src[1];
-    jj[2] += (double)src[2];
-  }
-  J[c] = jj[0] * inv_vol;
-  J[ncor + c] = jj[1] * inv_vol;
-  J[2 * ncor + c] = jj[2] * inv_vol;
 }
 
 // ---------------------------------------------------------------------------
 // Import: FP64 physical position -> block, cell, FP32 offset (findTreeNode +
-// FindCellIndex + periodic exchange rules), then the same slot reservation.
+// FindCellIndex + periodic exchange rules) into the unsorted list buffer.
 struct ImportArgs {
   const double* x; const double* v; const uint8_t* sp; const double* wc;
-  float* ux; float* uy; float* uz; float* vx; float* vy; float* vz;
-  uint8_t* dsp; float* dwc; uint32_t* did;
-  int* key; int* rank; int* count;
+  PBuf d;
+  int* key;
   unsigned long long* flags;
   long long n;
   int nbk[3];
@@ -549,84 +799,112 @@ struct ImportArgs {
 };
 
 __global__ void __launch_bounds__(256) k_import(ImportArgs a) {
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < a.n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long p = base + threadIdx.x;
-    const bool act = p < a.n;
-    int key = 0;
-    if (act) {
-      int bx[3], ic[3];
-      float uf[3];
-      for (int d = 0; d < 3; d++) {
-        double x = a.x[3 * p + d];
-        const double L = AMPS_NC * a.dx[d];
-        int bb = (int)floor((x - a.x0[d]) / L);
-        double xmin = a.x0[d] + bb * L;
-        if (x < xmin) { bb--; xmin = a.x0[d] + bb * L; }
-        if (x >= xmin + L) { bb++; xmin = a.x0[d] + bb * L; }
-        int ci = (int)((x - xmin) / a.dx[d]);
-        if (ci >= AMPS_NC) ci = AMPS_NC - 1;
-        if (ci < 0) ci = 0;
-        if (bb < 0 || bb >= a.nbk[d]) {
-          int br = ((bb % a.nbk[d]) + a.nbk[d]) % a.nbk[d];
-          double xr = a.x0[d] + br * L;
-          x += xr - xmin;
-          if (x < xr) x = xr;
-          if (x >= xr + L) x = (xr + L) - 1.0E-10 * L;
-          bb = br;
-          xmin = xr;
-          if (bb < 0 || bb >= a.nbk[d]) atomicAdd(a.flags + 2, 1ull);
-        }
-        float u = (float)((x - xmin) / a.dx[d]);
-        // keep the FP32 offset inside the FP64 cell
-        if (u < (float)ci) u = (float)ci;
-        if (u >= (float)(ci + 1)) u = nextafterf((float)(ci + 1), 0.0f);
-        uf[d] = u;
-        bx[d] = bb;
-        ic[d] = ci;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int bx[3], ic[3];
+    float uf[3];
+    for (int d = 0; d < 3; d++) {
+      double x = a.x[3 * p + d];
+      const double L = AMPS_NC * a.dx[d];
+      int bb = (int)floor((x - a.x0[d]) / L);
+      double xmin = a.x0[d] + bb * L;
+      if (x < xmin) { bb--; xmin = a.x0[d] + bb * L; }
+      if (x >= xmin + L) { bb++; xmin = a.x0[d] + bb * L; }
+      int ci = (int)((x - xmin) / a.dx[d]);
+      if (ci >= AMPS_NC) ci = AMPS_NC - 1;
+      if (ci < 0) ci = 0;
+      if (bb < 0 || bb >= a.nbk[d]) {
+        const int br = ((bb % a.nbk[d]) + a.nbk[d]) % a.nbk[d];
+        const double xr = a.x0[d] + br * L;
+        x += xr - xmin;
+        if (x < xr) x = xr;
+        if (x >= xr + L) x = (xr + L) - 1.0E-10 * L;
+        bb = br;
+        xmin = xr;
       }
-      const int blk = bx[0] + a.nbk[0] * (bx[1] + a.nbk[1] * bx[2]);
-      key = blk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
-      a.ux[p] = uf[0]; a.uy[p] = uf[1]; a.uz[p] = uf[2];
-      a.vx[p] = (float)a.v[3 * p]; a.vy[p] = (float)a.v[3 * p + 1]; a.vz[p] = (float)a.v[3 * p + 2];
-      int s = a.sp[p];
-      if (s >= a.nspec) atomicAdd(a.flags + 2, 1ull);
-      a.dsp[p] = (uint8_t)s;
-      if (a.dwc) a.dwc[p] = a.wc ? (float)a.wc[p] : 1.0f;
-      if (a.did) a.did[p] = (uint32_t)p;
-      a.key[p] = key;
+      float u = (float)((x - xmin) / a.dx[d]);
+      // keep the FP32 offset inside the FP64 cell
+      if (u < (float)ci) u = (float)ci;
+      if (u >= (float)(ci + 1)) u = nextafterf((float)(ci + 1), 0.0f);
+      uf[d] = u;
+      bx[d] = bb;
+      ic[d] = ci;
     }
-    reserve_slot(act, key, a.count, a.rank, p);
+    const int blk = bx[0] + a.nbk[0] * (bx[1] + a.nbk[1] * bx[2]);
+    a.key[p] = blk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+    for (int d = 0; d < 3; d++) {
+      a.d.u[d][p] = uf[d];
+      a.d.v[d][p] = (float)a.v[3 * p + d];
+    }
+    const int s = a.sp[p];
+    if (s >= a.nspec) atomicAdd(a.flags + 2, 1ull);
+    a.d.sp[p] = (uint8_t)s;
+    if (a.d.wc) a.d.wc[p] = a.wc ? (float)a.wc[p] : 1.0f;
+    if (a.d.id) a.d.id[p] = (uint32_t)p;
   }
 }
 
-// Local import: block id + FP32 offsets already given.
-__global__ void __launch_bounds__(256) k_import_local(long long n, const int* __restrict__ blk,
-                                                      float* ux, float* uy, float* uz,
-                                                      uint32_t* did, int* key, int* rank,
-                                                      int* count, int nb,
+// Local import: interleaved FP32 offsets/velocities and block ids.
+__global__ void __launch_bounds__(256) k_import_local(long long n, const float* __restrict__ u,
+                                                      const float* __restrict__ v,
+                                                      const uint8_t* __restrict__ sp,
+                                                      const int* __restrict__ blk, int nb,
+                                                      int nspec, PBuf d, int* key,
                                                       unsigned long long* flags) {
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long p = base + threadIdx.x;
-    const bool act = p < n;
-    int kk = 0;
-    if (act) {
-      float u[3] = {ux[p], uy[p], uz[p]};
-      int ic[3];
-      for (int d = 0; d < 3; d++) {
-        if (!(u[d] >= 0.f && u[d] < 8.f)) atomicAdd(flags + 2, 1ull);
-        u[d] = clamp_below8(fmaxf(u[d], 0.f));
-        ic[d] = min((int)u[d], AMPS_NC - 1);
-      }
-      ux[p] = u[0]; uy[p] = u[1]; uz[p] = u[2];
-      int b = blk[p];
-      if (b < 0 || b >= nb) { atomicAdd(flags + 2, 1ull); b = 0; }
-      kk = b * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
-      key[p] = kk;
-      if (did) did[p] = (uint32_t)p;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int ic[3];
+    for (int q = 0; q < 3; q++) {
+      float uu = u[3 * p + q];
+      if (!(uu >= 0.f && uu < 8.f)) atomicAdd(flags + 2, 1ull);
+      uu = clamp_below8(fmaxf(uu, 0.f));
+      ic[q] = min((int)uu, AMPS_NC - 1);
+      d.u[q][p] = uu;
+      d.v[q][p] = v[3 * p + q];
     }
-    reserve_slot(act, kk, count, rank, p);
+    int b = blk[p];
+    if (b < 0 || b >= nb) { atomicAdd(flags + 2, 1ull); b = 0; }
+    const int s = sp[p];
+    if (s >= nspec) atomicAdd(flags + 2, 1ull);
+    d.sp[p] = (uint8_t)s;
+    if (d.wc) d.wc[p] = 1.0f;
+    if (d.id) d.id[p] = (uint32_t)p;
+    key[p] = b * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+  }
+}
+
+// Export: compact arrays in cell order (out offsets = exclusive scan of cnt).
+__global__ void __launch_bounds__(256) k_export(long long ncells, const int* __restrict__ base,
+                                                const int* __restrict__ cnt,
+                                                const int* __restrict__ out0, PBuf s, int nbx,
+                                                int nby, double x00, double x01, double x02,
+                                                double dx0, double dx1, double dx2, double* x,
+                                                double* v, uint8_t* sp, int32_t* blk,
+                                                int32_t* cel, uint32_t* id) {
+  const long long cid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cid >= ncells) return;
+  const int b = (int)(cid / AMPS_CPB), l = (int)(cid % AMPS_CPB);
+  const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+  const double o0 = x00 + bx * (AMPS_NC * dx0), o1 = x01 + by * (AMPS_NC * dx1),
+               o2 = x02 + bz * (AMPS_NC * dx2);
+  const int b0 = base[cid], n0 = cnt[cid];
+  long long q = out0[cid];
+  for (int t = 0; t < n0; t++, q++) {
+    const long long p = b0 + t;
+    if (x) {
+      x[3 * q] = o0 + (double)s.u[0][p] * dx0;
+      x[3 * q + 1] = o1 + (double)s.u[1][p] * dx1;
+      x[3 * q + 2] = o2 + (double)s.u[2][p] * dx2;
+    }
+    if (v) {
+      v[3 * q] = s.v[0][p];
+      v[3 * q + 1] = s.v[1][p];
+      v[3 * q + 2] = s.v[2][p];
+    }
+    if (sp) sp[q] = s.sp[p];
+    if (blk) blk[q] = b;
+    if (cel) cel[q] = l;
+    if (id && s.id) id[q] = s.id[p];
   }
 }
 
@@ -653,15 +931,15 @@ void init_asm_table() {
   int n = 0;
   for (int slot = 0; slot < 27; slot++)
     for (int co = 0; co < 8; co++) {
-      // cell = corner + (-(co&1), -((co>>1)&1), -((co>>2)&1)); the corner sits at
-      // local offset ((co&1), (co>>1)&1, (co>>2)&1) inside that cell
-      int lx = co & 1, ly = (co >> 1) & 1, lz = (co >> 2) & 1;
-      int c1 = tidx(lx, ly, lz);
+      // cell = corner - (co&1, (co>>1)&1, (co>>2)&1): the corner sits at local
+      // offset (co&1, (co>>1)&1, (co>>2)&1) of that cell
+      const int lx = co & 1, ly = (co >> 1) & 1, lz = (co >> 2) & 1;
+      const int c1 = tidx(lx, ly, lz);
       corner_of[co] = (unsigned char)c1;
       for (int c2 = 0; c2 < 8; c2++) {
-        int dx = off[c2][0] - lx, dy = off[c2][1] - ly, dz = off[c2][2] - lz;
-        if (mm_slot(dx, dy, dz) != slot) continue;
-        int hi = c1 > c2 ? c1 : c2, lo = c1 > c2 ? c2 : c1;
+        const int ddx = off[c2][0] - lx, ddy = off[c2][1] - ly, ddz = off[c2][2] - lz;
+        if (mm_slot(ddx, ddy, ddz) != slot) continue;
+        const int hi = c1 > c2 ? c1 : c2, lo = c1 > c2 ? c2 : c1;
         e[n].slot = (unsigned char)slot;
         e[n].cell = (unsigned char)co;
         e[n].pair = (unsigned char)(hi * (hi + 1) / 2 + lo);
@@ -672,6 +950,90 @@ void init_asm_table() {
   cudaMemcpyToSymbol(c_asm, e, sizeof(e));
   cudaMemcpyToSymbol(c_asm_corner, corner_of, sizeof(corner_of));
   g_asm_ready = true;
+}
+
+StepArgs step_args(amps_gpu_ctx* c) {
+  StepArgs a;
+  a.nbr = c->d_nbr;
+  a.base = c->d_base;
+  a.cnt = c->d_cnt;
+  a.arr = c->d_arr;
+  a.stay = c->d_stay;
+  a.st_push = c->d_stencil_push;
+  a.st_dep = c->d_stencil_dep;
+  a.p = pbuf(c, c->cur);
+  a.ovf = pbuf(c, c->cur ^ 1);
+  a.ovf_key = c->d_key;
+  a.cellM = c->d_cellM;
+  a.cellJ = c->d_cellJ;
+  a.energy = c->d_energy;
+  a.flags = c->d_flags;
+  for (int d = 0; d < 3; d++) a.dtdx[d] = (float)(c->cfg.dt / c->cfg.dx[d]);
+  a.inv_vol = (float)(1.0 / (c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2]));
+  a.ovf_cap = c->slots;
+  a.st = make_species(c->cfg);
+  return a;
+}
+
+size_t smem_push(bool dep) {
+  return (size_t)AMPS_SC * (2 + 1) * sizeof(float4) + (dep ? kWarps * 32 * kRec * sizeof(float) : 0);
+}
+size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * 32 * kRec * sizeof(float); }
+
+void set_smem_attrs() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_push_deposit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(true));
+  cudaFuncSetAttribute(k_push_deposit<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
+  cudaFuncSetAttribute(k_arrivals<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
+  cudaFuncSetAttribute(k_arrivals<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
+  cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
+  done = true;
+}
+
+cudaError_t scan_ints(amps_gpu_ctx* c, const int* in, int* out, long long n) {
+  const int tiles = (int)((n + kScanTile - 1) / kScanTile);
+  TimedLaunch t(c, "scan", 3);
+  k_scan_reduce<<<tiles, 256, 0, c->stream>>>(in, n, c->d_scan_part);
+  k_scan_parts<<<1, 1024, 0, c->stream>>>(c->d_scan_part, tiles);
+  k_scan_final<<<tiles, 256, 0, c->stream>>>(in, n, c->d_scan_part, out);
+  return cudaGetLastError();
+}
+
+// Counting sort of the list buffer (cur^1, keys in d_key) with n particles into
+// the slotted layout of buffer cur.
+cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
+  cudaStream_t s = c->stream;
+  const long long nc = c->ncor;
+  cudaError_t e = cudaMemsetAsync(c->d_count, 0, sizeof(int) * (nc + 1), s);
+  if (e != cudaSuccess) return e;
+  {
+    TimedLaunch t(c, "rebuild");
+    k_rb_rank<<<grid_for(n, 256), 256, 0, s>>>(n, c->d_key, c->d_rank, c->d_count);
+  }
+  // slack scaled so that sum(cap) <= slots: sum(cap) <= n + max(8 nc, n/4 + 8 nc)
+  const long long worst = n + std::max(8LL * nc, n / 4 + 8LL * nc);
+  int num = 1, den = 1;
+  if (worst > c->slots) {
+    num = (int)std::max(0LL, (c->slots - n) / 1024);
+    den = (int)std::max(1LL, (worst - n) / 1024 + 1);
+  }
+  {
+    TimedLaunch t(c, "rebuild");
+    k_rb_caps<<<(unsigned)((nc + 1 + 255) / 256), 256, 0, s>>>(nc, c->d_count, c->d_tmp, num, den);
+  }
+  e = scan_ints(c, c->d_tmp, c->d_base, nc + 1);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(c->d_sp[c->cur], 0xFF, (size_t)c->slots, s);
+  if (e != cudaSuccess) return e;
+  {
+    TimedLaunch t(c, "rebuild");
+    k_rb_scatter<<<grid_for(n, 256), 256, 0, s>>>(n, c->d_key, c->d_rank, c->d_base,
+                                                   pbuf(c, c->cur ^ 1), pbuf(c, c->cur));
+  }
+  e = cudaMemcpyAsync(c->d_cnt, c->d_count, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return e;
+  return cudaMemsetAsync(c->d_arr, 0, sizeof(int) * nc, s);
 }
 
 }  // namespace
@@ -686,128 +1048,88 @@ cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double
   return cudaGetLastError();
 }
 
-static int push_splits(const amps_gpu_ctx* c) {
-  long long per = c->np / (c->nb > 0 ? c->nb : 1);
-  long long s = per / 4096;
-  if (s < 1) s = 1;
-  if (s > 256) s = 256;
-  return (int)s;
-}
-
-cudaError_t launch_push(amps_gpu_ctx* c) {
-  const int cur = c->cur;
-  cudaError_t e = cudaMemsetAsync(c->d_count, 0, sizeof(int) * (c->ncor + 1), c->stream);
-  if (e != cudaSuccess) return e;
-  PushArgs a;
-  a.nbr = c->d_nbr;
-  a.start = c->d_start;
-  a.stencil = c->d_stencil_push;
-  a.ux = c->d_u[cur][0]; a.uy = c->d_u[cur][1]; a.uz = c->d_u[cur][2];
-  a.vx = c->d_v[cur][0]; a.vy = c->d_v[cur][1]; a.vz = c->d_v[cur][2];
-  a.sp = c->d_sp[cur];
-  a.key = c->d_key; a.rank = c->d_rank; a.count = c->d_count;
-  a.flags = c->d_flags;
-  for (int d = 0; d < 3; d++) a.dtdx[d] = (float)(c->cfg.dt / c->cfg.dx[d]);
-  a.dt = (float)c->cfg.dt;
-  a.st = make_species(c->cfg);
-  const size_t smem = AMPS_SC * AMPS_PUSH_STRIDE * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_push, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
-  TimedLaunch t(c, "push");
-  dim3 grid(c->nb, push_splits(c));
-  k_push<<<grid, 256, smem, c->stream>>>(a);
-  return cudaGetLastError();
-}
-
-static cudaError_t scan_counts(amps_gpu_ctx* c) {
-  const long long n = c->ncor + 1;
-  const int tiles = (int)((n + kScanTile - 1) / kScanTile);
-  TimedLaunch t(c, "scan", 3);
-  k_scan_reduce<<<tiles, 256, 0, c->stream>>>(c->d_count, n, c->d_scan_part);
-  k_scan_parts<<<1, 1024, 0, c->stream>>>(c->d_scan_part, tiles);
-  k_scan_final<<<tiles, 256, 0, c->stream>>>(c->d_count, n, c->d_scan_part, c->d_start);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_rebin(amps_gpu_ctx* c) {
-  cudaError_t e = scan_counts(c);
-  if (e != cudaSuccess) return e;
-  const int s = c->cur, d = s ^ 1;
-  ScatterArgs a;
-  a.key = c->d_key; a.rank = c->d_rank; a.start = c->d_start;
-  for (int q = 0; q < 3; q++) {
-    a.su[q] = c->d_u[s][q]; a.sv[q] = c->d_v[s][q];
-    a.du[q] = c->d_u[d][q]; a.dv[q] = c->d_v[d][q];
-  }
-  a.ssp = c->d_sp[s]; a.dsp = c->d_sp[d];
-  a.swc = c->has_wcorr ? c->d_wc[s] : nullptr;
-  a.dwc = c->has_wcorr ? c->d_wc[d] : nullptr;
-  a.sid = c->cfg.track_ids ? c->d_id[s] : nullptr;
-  a.did = c->cfg.track_ids ? c->d_id[d] : nullptr;
-  a.n = c->np;
-  {
-    TimedLaunch t(c, "scatter");
-    k_scatter<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
-  }
-  c->cur = d;
-  return cudaGetLastError();
-}
-
-cudaError_t launch_deposit(amps_gpu_ctx* c) {
+static cudaError_t launch_assemble(amps_gpu_ctx* c) {
   init_asm_table();
-  const int cur = c->cur;
-  DepositArgs a;
-  a.start = c->d_start;
-  a.stencil = c->d_stencil_dep;
-  a.ux = c->d_u[cur][0]; a.uy = c->d_u[cur][1]; a.uz = c->d_u[cur][2];
-  a.vx = c->d_v[cur][0]; a.vy = c->d_v[cur][1]; a.vz = c->d_v[cur][2];
-  a.sp = c->d_sp[cur];
-  a.wc = c->has_wcorr ? c->d_wc[cur] : nullptr;
-  a.cellM = c->d_cellM; a.cellJ = c->d_cellJ;
-  a.energy = c->d_energy;
-  a.flags = c->d_flags;
-  a.inv_vol = (float)(1.0 / (c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2]));
-  a.st = make_species(c->cfg);
-  const size_t smem = AMPS_SC * sizeof(float4) + kDepWarps * 32 * kRec * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  TimedLaunch t(c, "assemble");
+  const double inv_vol = 1.0 / (c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2]);
+  k_assemble<<<(unsigned)((c->ncor + 255) / 256), 256, 0, c->stream>>>(
+      c->ncor, c->d_nbr, c->d_cellM, c->d_cellJ, inv_vol, c->d_M, c->d_J);
+  return cudaGetLastError();
+}
+
+// Full deposit (UpdateJMassMatrix on the current layout).
+cudaError_t launch_deposit(amps_gpu_ctx* c) {
+  set_smem_attrs();
   cudaError_t e = cudaMemsetAsync(c->d_energy, 0, sizeof(double), c->stream);
   if (e != cudaSuccess) return e;
+  StepArgs a = step_args(c);
   {
     TimedLaunch t(c, "deposit");
-    k_deposit<<<dim3(c->nb, AMPS_NC), kDepWarps * 32, smem, c->stream>>>(a);
+    k_deposit<<<dim3(c->nb, AMPS_NC), kWarps * 32, smem_dep(), c->stream>>>(a);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_assemble(c);
+}
+
+// Push (+ deposit) of one step: k_push_deposit, k_arrivals (+ assemble).
+// Overflow recovery is done by the caller (particles_recover).
+cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
+  set_smem_attrs();
+  cudaError_t e;
+  if (deposit) {
+    e = cudaMemsetAsync(c->d_energy, 0, sizeof(double), c->stream);
+    if (e != cudaSuccess) return e;
+  }
+  StepArgs a = step_args(c);
+  const dim3 grid(c->nb, AMPS_NC);
+  {
+    TimedLaunch t(c, deposit ? "push_deposit" : "push");
+    if (deposit)
+      k_push_deposit<true><<<grid, kWarps * 32, smem_push(true), c->stream>>>(a);
+    else
+      k_push_deposit<false><<<grid, kWarps * 32, smem_push(false), c->stream>>>(a);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   {
-    TimedLaunch t(c, "assemble");
-    const double inv_vol = 1.0 / (c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2]);
-    k_assemble<<<(unsigned)((c->ncor + 255) / 256), 256, 0, c->stream>>>(
-        c->ncor, c->d_nbr, c->d_cellM, c->d_cellJ, inv_vol, c->d_M, c->d_J);
+    TimedLaunch t(c, "arrivals");
+    if (deposit)
+      k_arrivals<true><<<grid, kWarps * 32, smem_dep(), c->stream>>>(a);
+    else
+      k_arrivals<false><<<grid, kWarps * 32, smem_dep(), c->stream>>>(a);
   }
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (deposit) return launch_assemble(c);
+  return cudaSuccess;
 }
 
-// Import helpers used by the C ABI (capi.cu)
+// After an overflow (n_overflow particles already in the list buffer with
+// their keys): append the compact layout behind them and rebuild.
+cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow) {
+  c->h_flags[3] = (unsigned long long)n_overflow;
+  cudaError_t e = cudaMemcpyAsync(c->d_flags + 4, c->h_flags + 3, sizeof(unsigned long long),
+                                  cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return e;
+  {
+    TimedLaunch t(c, "recover");
+    const long long threads = c->ncor * 32;
+    k_gather_valid<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        c->ncor, c->d_base, c->d_cnt, pbuf(c, c->cur), pbuf(c, c->cur ^ 1), c->d_key,
+        c->d_flags + 4);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return rebuild_from_list(c, c->np);
+}
+
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
                                const uint8_t* d_spec_in, const double* d_wc, long long n) {
-  cudaError_t e = cudaMemsetAsync(c->d_count, 0, sizeof(int) * (c->ncor + 1), c->stream);
-  if (e != cudaSuccess) return e;
-  const int cur = c->cur;
   ImportArgs a;
   a.x = d_x; a.v = d_v; a.sp = d_spec_in; a.wc = d_wc;
-  a.ux = c->d_u[cur][0]; a.uy = c->d_u[cur][1]; a.uz = c->d_u[cur][2];
-  a.vx = c->d_v[cur][0]; a.vy = c->d_v[cur][1]; a.vz = c->d_v[cur][2];
-  a.dsp = c->d_sp[cur];
-  a.dwc = c->has_wcorr ? c->d_wc[cur] : nullptr;
-  a.did = c->cfg.track_ids ? c->d_id[cur] : nullptr;
-  a.key = c->d_key; a.rank = c->d_rank; a.count = c->d_count;
+  a.d = pbuf(c, c->cur ^ 1);
+  a.key = c->d_key;
   a.flags = c->d_flags;
   a.n = n;
   a.nbk[0] = c->cfg.nbx; a.nbk[1] = c->cfg.nby; a.nbk[2] = c->cfg.nbz;
@@ -817,66 +1139,39 @@ cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double*
     TimedLaunch t(c, "import");
     k_import<<<grid_for(n, 256), 256, 0, c->stream>>>(a);
   }
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   c->np = n;
-  return launch_rebin(c);
+  return rebuild_from_list(c, n);
 }
 
-cudaError_t launch_import_local(amps_gpu_ctx* c, const int32_t* d_block, long long n) {
-  cudaError_t e = cudaMemsetAsync(c->d_count, 0, sizeof(int) * (c->ncor + 1), c->stream);
-  if (e != cudaSuccess) return e;
-  const int cur = c->cur;
+cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* d_v,
+                                const uint8_t* d_sp, const int32_t* d_block, long long n) {
   {
     TimedLaunch t(c, "import");
-    k_import_local<<<grid_for(n, 256), 256, 0, c->stream>>>(
-        n, d_block, c->d_u[cur][0], c->d_u[cur][1], c->d_u[cur][2],
-        c->cfg.track_ids ? c->d_id[cur] : nullptr, c->d_key, c->d_rank, c->d_count, c->nb,
-        c->d_flags);
+    k_import_local<<<grid_for(n, 256), 256, 0, c->stream>>>(n, d_u, d_v, d_sp, d_block, c->nb,
+                                                             c->cfg.nspec, pbuf(c, c->cur ^ 1),
+                                                             c->d_key, c->d_flags);
   }
-  e = cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   c->np = n;
-  return launch_rebin(c);
+  return rebuild_from_list(c, n);
 }
 
-// Export: physical FP64 positions, velocities, block and cell per particle in
-// device order.
-__global__ void __launch_bounds__(256) k_export(long long ncells, const int* __restrict__ start,
-                                                const float* ux, const float* uy, const float* uz,
-                                                const float* vx, const float* vy, const float* vz,
-                                                int nbx, int nby, double x00, double x01,
-                                                double x02, double dx0, double dx1, double dx2,
-                                                double* x, double* v, int32_t* blk, int32_t* cel) {
-  const long long cid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cid >= ncells) return;
-  const int b = (int)(cid / AMPS_CPB), l = (int)(cid % AMPS_CPB);
-  const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
-  const double o0 = x00 + bx * (AMPS_NC * dx0), o1 = x01 + by * (AMPS_NC * dx1),
-               o2 = x02 + bz * (AMPS_NC * dx2);
-  for (int p = start[cid]; p < start[cid + 1]; p++) {
-    if (x) {
-      x[3LL * p] = o0 + (double)ux[p] * dx0;
-      x[3LL * p + 1] = o1 + (double)uy[p] * dx1;
-      x[3LL * p + 2] = o2 + (double)uz[p] * dx2;
-    }
-    if (v) {
-      v[3LL * p] = vx[p];
-      v[3LL * p + 1] = vy[p];
-      v[3LL * p + 2] = vz[p];
-    }
-    if (blk) blk[p] = b;
-    if (cel) cel[p] = l;
-  }
-}
-
-cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, int32_t* d_blk,
-                          int32_t* d_cel) {
-  const int cur = c->cur;
+cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, uint8_t* d_sp,
+                          int32_t* d_blk, int32_t* d_cel, uint32_t* d_id) {
+  cudaError_t e = cudaMemcpyAsync(c->d_tmp, c->d_cnt, sizeof(int) * c->ncor,
+                                  cudaMemcpyDeviceToDevice, c->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(c->d_tmp + c->ncor, 0, sizeof(int), c->stream);
+  if (e != cudaSuccess) return e;
+  e = scan_ints(c, c->d_tmp, c->d_tmp, c->ncor + 1);
+  if (e != cudaSuccess) return e;
   TimedLaunch t(c, "export");
   k_export<<<(unsigned)((c->ncor + 255) / 256), 256, 0, c->stream>>>(
-      c->ncor, c->d_start, c->d_u[cur][0], c->d_u[cur][1], c->d_u[cur][2], c->d_v[cur][0],
-      c->d_v[cur][1], c->d_v[cur][2], c->cfg.nbx, c->cfg.nby, c->cfg.x0[0], c->cfg.x0[1],
-      c->cfg.x0[2], c->cfg.dx[0], c->cfg.dx[1], c->cfg.dx[2], d_x, d_v, d_blk, d_cel);
+      c->ncor, c->d_base, c->d_cnt, c->d_tmp, pbuf(c, c->cur), c->cfg.nbx, c->cfg.nby,
+      c->cfg.x0[0], c->cfg.x0[1], c->cfg.x0[2], c->cfg.dx[0], c->cfg.dx[1], c->cfg.dx[2], d_x, d_v,
+      d_sp, d_blk, d_cel, d_id);
   return cudaGetLastError();
 }

@@ -168,22 +168,22 @@ def measured_peaks():
 
 # ---------------------------------------------------------------------------
 def kernel_bytes(wl, name):
-    """Algorithmic bytes per launch of each particle kernel:
-    what the kernel must read and write given the data layout."""
+    """Algorithmic bytes per launch of each particle-step kernel: what the
+    kernel must read and write given the slotted cell layout."""
     n = wl.nparticles
     ncell = wl.mesh.ncells
     nb = wl.mesh.nblocks
-    if name == "push":
-        # read u,v (24) + species (1); write u,v (24) + key (4) + rank (4); stencil 23.3 KB/block
-        return n * 57 + nb * 23328
-    if name == "scatter":
-        # read key, rank, start (12) + u,v,species (25); write u,v,species (25) (+ ids 8 if tracked)
-        return n * 62
-    if name == "deposit":
-        # read u,v,species (25); write per-cell partials (324+24 floats); stencil 11.7 KB/block
-        return n * 25 + ncell * 348 * 4 + nb * 11664
+    ctas = nb * 8
+    if name == "push_deposit":
+        # particles: read u,v (24) + species (1), write u,v (24); per cell: base, cnt
+        # (8), stay (4), partials 348 floats; stencils 23.3 + 11.7 KB per CTA
+        return n * 49 + ncell * (12 + 348 * 4) + ctas * (23328 + 11664)
+    if name == "arrivals":
+        # per cell: base, base+1, cnt, stay, arr (20) and cnt/arr writes (8); the
+        # ~1% arrivals and their partial read-modify-write; stencil per CTA
+        return ncell * 28 + ctas * 11664
     if name == "assemble":
-        # read partials (2x, each pair value reaches two corners); write M (243) + J (3) FP64
+        # read partials (each pair value reaches two corners); write M (243) + J (3) FP64
         return ncell * (2 * 348 * 4) + ncell * 246 * 8
     if name == "pack_stencils":
         return ncell * 9 * 8 * 27 // 8 + nb * (23328 + 11664)
