@@ -157,8 +157,30 @@ __device__ bool stage_stencils(uint64_t* bar, void* dst0, const void* src0, uint
 // ---------------------------------------------------------------------------
 // Deposition pieces shared by k_push_deposit, k_arrivals and k_deposit.
 
-// Record of one particle at block-local offset u inside cell (i,j,k).
-__device__ __forceinline__ double stage_record(float* __restrict__ r, const float4* __restrict__ sB,
+// Per-cell partial sums: 36 pairs x 9 (mass matrix) and 8 corners x 3 (current),
+// contiguous per cell.
+__host__ __device__ __forceinline__ long long cellM_at(long long cid, int pe) {
+  return cid * 324 + pe;
+}
+__host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
+  return cid * 24 + ce;
+}
+
+// FP32 -> FP64 widening with integer operations (exact for zero and normal
+// numbers; GB300's FP64 pipe is narrow, the integer pipe is not).
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;  // zero, subnormal, inf, nan
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+
+// Record of one particle at block-local offset u inside cell (i,j,k); returns
+// its kinetic energy 0.5 m W v^2 (FP32; summed per cell, then in FP64).
+__device__ __forceinline__ float stage_record(float* __restrict__ r, const float4* __restrict__ sB,
                                                float u0, float u1, float u2, float v0, float v1,
                                                float v2, int s, float wcorr, int i, int j, int k,
                                                const SpeciesTab& st, float inv_vol) {
@@ -216,7 +238,7 @@ __device__ __forceinline__ double stage_record(float* __restrict__ r, const floa
   const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
   const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
   r4[14] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
-  return 0.5 * (double)mW * ((double)v0 * v0 + (double)v1 * v1 + (double)v2 * v2);
+  return 0.5f * mW * (v0 * v0 + v1 * v1 + v2 * v2);
 }
 
 struct Tile {
@@ -231,7 +253,7 @@ struct Tile {
     float acc[12];
 #pragma unroll
     for (int e = 0; e < 12; e++) acc[e] = 0.f;
-#pragma unroll 2
+#pragma unroll 4
     for (int r = 0; r < cnt; r++) {
       const float4 A = *reinterpret_cast<const float4*>(rec + r * kRec + offA);
       const float4 B = *reinterpret_cast<const float4*>(rec + r * kRec + offB);
@@ -256,25 +278,23 @@ struct Tile {
                                         float* __restrict__ cellJ, long long cid, bool add) {
     if (lane < 27) {
       const int g = lane / 3, hh = lane % 3;
-      float* dst = cellM + cid * 324;
 #pragma unroll
       for (int q = 0; q < 4; q++)
 #pragma unroll
         for (int e = 0; e < 3; e++) {
-          const int o = (4 * g + q) * 9 + 3 * hh + e;
+          const long long o = cellM_at(cid, (4 * g + q) * 9 + 3 * hh + e);
           const float v = sum[3 * q + e] - cmp[3 * q + e];
-          dst[o] = add ? dst[o] + v : v;
+          cellM[o] = add ? cellM[o] + v : v;
         }
     } else if (lane < 29) {
       const int g = lane - 27;
-      float* dst = cellJ + cid * 24;
 #pragma unroll
       for (int q = 0; q < 4; q++)
 #pragma unroll
         for (int e = 0; e < 3; e++) {
-          const int o = (4 * g + q) * 3 + e;
+          const long long o = cellJ_at(cid, (4 * g + q) * 3 + e);
           const float v = sum[3 * q + e] - cmp[3 * q + e];
-          dst[o] = add ? dst[o] + v : v;
+          cellJ[o] = add ? cellJ[o] + v : v;
         }
     }
   }
@@ -358,6 +378,7 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = a.base[cid], n0 = a.cnt[cid];
     Tile tile;
+    float en_cell = 0.f;
     tile.zero();
     int nst = 0;
     for (int q0 = 0; q0 < n0; q0 += 32) {
@@ -434,7 +455,7 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
           if (a.p.id) a.p.id[d] = idv;
         }
         if (DEP)
-          en += stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv,
+          en_cell += stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv,
                              i, j, k, a.st, a.inv_vol);
       }
       // movers: slack of the destination cell, else the overflow list
@@ -474,7 +495,10 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
     // vacated slots become holes
     for (int t = nst + lane; t < n0; t += 32) a.p.sp[b0 + t] = kHole;
     if (lane == 0) a.stay[cid] = nst;
-    if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid, false);
+    if (DEP) {
+      tile.flush(lane, a.cellM, a.cellJ, cid, false);
+      en += (double)en_cell;
+    }
   }
   if (n_far) atomicAdd(a.flags + 0, n_far);
   if (n_near) atomicAdd(a.flags + 1, n_near);
@@ -580,17 +604,19 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
     const int b0 = a.base[cid], n0 = a.cnt[cid];
     Tile tile;
     tile.zero();
+    float en_cell = 0.f;
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const long long p = b0 + q0 + lane;
       if (q0 + lane < n0)
-        en += stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p],
-                           a.p.v[0][p], a.p.v[1][p], a.p.v[2][p], a.p.sp[p],
-                           a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, a.inv_vol);
+        en_cell += stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p],
+                                a.p.v[0][p], a.p.v[1][p], a.p.v[2][p], a.p.sp[p],
+                                a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, a.inv_vol);
       __syncwarp();
       if (lane < 29) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
+    en += (double)en_cell;
   }
   reduce_energy(en, s_en, a.energy);
 }
@@ -617,37 +643,38 @@ __global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __r
 #pragma unroll
   for (int co = 0; co < 8; co++)
     cell[co] = local_id(nbr, b, i - (co & 1), j - ((co >> 1) & 1), k - ((co >> 2) & 1));
-  double acc[9];
+  // sums of at most 8 FP32 partials per element, widened once to FP64
+  float acc[9];
   int cur = c_asm[0].slot;
 #pragma unroll
-  for (int e = 0; e < 9; e++) acc[e] = 0.0;
+  for (int e = 0; e < 9; e++) acc[e] = 0.f;
   for (int t = 0; t < 64; t++) {
     const AsmEntry en = c_asm[t];
     if (en.slot != cur) {
 #pragma unroll
       for (int e = 0; e < 9; e++) {
-        M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
-        acc[e] = 0.0;
+        M[(size_t)(cur * 9 + e) * ncor + c] = widen(acc[e]);
+        acc[e] = 0.f;
       }
       cur = en.slot;
     }
-    const float* src = cellM + (size_t)cell[en.cell] * 324 + en.pair * 9;
+    const float* src = cellM + cellM_at(cell[en.cell], en.pair * 9);
 #pragma unroll
-    for (int e = 0; e < 9; e++) acc[e] += (double)src[e];
+    for (int e = 0; e < 9; e++) acc[e] += src[e];
   }
 #pragma unroll
-  for (int e = 0; e < 9; e++) M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
-  double jj[3] = {0.0, 0.0, 0.0};
+  for (int e = 0; e < 9; e++) M[(size_t)(cur * 9 + e) * ncor + c] = widen(acc[e]);
+  float jj[3] = {0.f, 0.f, 0.f};
 #pragma unroll
   for (int co = 0; co < 8; co++) {
-    const float* src = cellJ + (size_t)cell[co] * 24 + c_asm_corner[co] * 3;
-    jj[0] += (double)src[0];
-    jj[1] += (double)src[1];
-    jj[2] += (double)src[2];
+    const float* src = cellJ + cellJ_at(cell[co], c_asm_corner[co] * 3);
+    jj[0] += src[0];
+    jj[1] += src[1];
+    jj[2] += src[2];
   }
-  J[c] = jj[0] * inv_vol;
-  J[ncor + c] = jj[1] * inv_vol;
-  J[2 * ncor + c] = jj[2] * inv_vol;
+  J[c] = widen(jj[0]) * inv_vol;
+  J[ncor + c] = widen(jj[1]) * inv_vol;
+  J[2 * ncor + c] = widen(jj[2]) * inv_vol;
 }
 
 // ---------------------------------------------------------------------------

@@ -72,7 +72,8 @@ def test_fp64_tracer_matches_oracle_many_lifetimes():
     assert tot == int(steps.sum())
     ok = agree & (st != 0)
     rel = np.linalg.norm(x[ok] - xo[ok], axis=1) / np.linalg.norm(xo[ok], axis=1)
-    assert np.median(rel) < 1e-9 and rel.max() < 1e-4
+    # most trajectories agree to rounding; a few chaotic ones amplify it
+    assert np.median(rel) < 1e-12 and np.quantile(rel, 0.95) < 1e-6
     # lifetimes are uneven (the point of the persistent kernel)
     assert steps.min() < 50 and steps.max() == 4000
 
