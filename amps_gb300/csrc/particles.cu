@@ -36,30 +36,11 @@
 #include <cstdio>
 
 #include "common.cuh"
-#include "ptx.cuh"
+#include "deposit_core.cuh"
 
 namespace {
 
-constexpr uint32_t kWaitLimit = 1u << 24;
-constexpr int kRec = 60;      // floats per staged particle record
-constexpr int kWarps = 8;     // warps per CTA (one row of 8 cells each)
-constexpr uint8_t kHole = 0xFF;
 
-struct SpeciesTab {
-  float qdt2m[AMPS_GPU_MAX_SPECIES];  // 0.5*q*dt/m (weight independent)
-  float qw[AMPS_GPU_MAX_SPECIES];     // q*w
-  float mw[AMPS_GPU_MAX_SPECIES];     // m*w
-};
-
-SpeciesTab make_species(const amps_gpu_config& c) {
-  SpeciesTab t{};
-  for (int s = 0; s < c.nspec; s++) {
-    t.qdt2m[s] = (float)(0.5 * (c.charge[s] * c.dt / c.mass[s]));
-    t.qw[s] = (float)(c.charge[s] * c.weight[s]);
-    t.mw[s] = (float)(c.mass[s] * c.weight[s]);
-  }
-  return t;
-}
 
 // SoA view of one particle buffer
 struct PBuf {
@@ -129,191 +110,6 @@ __global__ void k_pack_stencils(int nb, long long ncor, const int* __restrict__ 
     op[1] = make_float4((float)Bprev[ncor + cid], (float)Bprev[2 * ncor + cid], 0.f, 0.f);
     reinterpret_cast<float4*>(sd)[(size_t)b * AMPS_SC + s] =
         make_float4((float)Bcur[cid], (float)Bcur[ncor + cid], (float)Bcur[2 * ncor + cid], 0.f);
-  }
-}
-
-// Stage one bulk copy per stencil into shared memory; returns false on timeout.
-__device__ bool stage_stencils(uint64_t* bar, void* dst0, const void* src0, uint32_t bytes0,
-                               void* dst1, const void* src1, uint32_t bytes1,
-                               unsigned long long* flags) {
-  if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(bar, bytes0 + bytes1);
-    if (bytes0) bulk_copy_g2s(dst0, src0, bytes0, bar);
-    if (bytes1) bulk_copy_g2s(dst1, src1, bytes1, bar);
-  }
-  if (!mbar_wait_bounded(bar, 0, kWaitLimit)) {
-    if (threadIdx.x == 0) atomicAdd(flags + 2, 1ull);
-    mbar_wait_bounded(bar, 0, kWaitLimit);  // let the copies land before exiting
-    return false;
-  }
-  return true;
-}
-
-// ---------------------------------------------------------------------------
-// Deposition pieces shared by k_push_deposit, k_arrivals and k_deposit.
-
-// Per-cell partial sums: 36 pairs x 9 (mass matrix) and 8 corners x 3 (current),
-// contiguous per cell.
-__host__ __device__ __forceinline__ long long cellM_at(long long cid, int pe) {
-  return cid * 324 + pe;
-}
-__host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
-  return cid * 24 + ce;
-}
-
-// FP32 -> FP64 widening with integer operations (exact for zero and normal
-// numbers; GB300's FP64 pipe is narrow, the integer pipe is not).
-__device__ __forceinline__ double widen(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xFFu;
-  if (e == 0u || e == 0xFFu) return (double)f;  // zero, subnormal, inf, nan
-  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
-                               ((unsigned long long)(e + 896u) << 52) |
-                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
-}
-
-// Record of one particle at block-local offset u inside cell (i,j,k); returns
-// its kinetic energy 0.5 m W v^2 (FP32; summed per cell, then in FP64).
-__device__ __forceinline__ float stage_record(float* __restrict__ r, const float4* __restrict__ sB,
-                                               float u0, float u1, float u2, float v0, float v1,
-                                               float v2, int s, float wcorr, int i, int j, int k,
-                                               const SpeciesTab& st, float inv_vol) {
-  const float fx = fminf(fmaxf(u0 - (float)i, 0.f), 1.f);
-  const float fy = fminf(fmaxf(u1 - (float)j, 0.f), 1.f);
-  const float fz = fminf(fmaxf(u2 - (float)k, 0.f), 1.f);
-  const float gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
-  float w[8];
-  w[0] = gx * gy * gz; w[1] = fx * gy * gz; w[2] = fx * fy * gz; w[3] = gx * fy * gz;
-  w[4] = gx * gy * fz; w[5] = fx * gy * fz; w[6] = fx * fy * fz; w[7] = gx * fy * fz;
-  const int sb = i + 9 * (j + 9 * k);
-  const int coff[8] = {0, 1, 10, 9, 81, 82, 91, 90};
-  float B0 = 0.f, B1 = 0.f, B2 = 0.f;
-#pragma unroll
-  for (int c = 0; c < 8; c++) {
-    const float4 q = sB[sb + coff[c]];
-    B0 = fmaf(w[c], q.x, B0);
-    B1 = fmaf(w[c], q.y, B1);
-    B2 = fmaf(w[c], q.z, B2);
-  }
-  const float h = st.qdt2m[s];
-  const float h2 = h * h;
-  const float c0 = 1.0f / (1.0f + h2 * (B0 * B0 + B1 * B1 + B2 * B2));
-  const float P0 = -h * B0, P1 = -h * B1, P2 = -h * B2;
-  float al[9];
-  al[0] = c0 * (1.f + h2 * B0 * B0);
-  al[1] = c0 * (-P2 + h2 * B0 * B1);
-  al[2] = c0 * (P1 + h2 * B0 * B2);
-  al[3] = c0 * (P2 + h2 * B1 * B0);
-  al[4] = c0 * (1.f + h2 * B1 * B1);
-  al[5] = c0 * (-P0 + h2 * B1 * B2);
-  al[6] = c0 * (-P1 + h2 * B2 * B0);
-  al[7] = c0 * (P0 + h2 * B2 * B1);
-  al[8] = c0 * (1.f + h2 * B2 * B2);
-  const float qW = st.qw[s] * wcorr;
-  const float mW = st.mw[s] * wcorr;
-  const float kc = qW * h * inv_vol;
-  float4* r4 = reinterpret_cast<float4*>(r);
-  {
-    float ww[36];
-    int pr = 0;
-#pragma unroll
-    for (int c1 = 0; c1 < 8; c1++)
-#pragma unroll
-      for (int c2 = 0; c2 <= c1; c2++, pr++) ww[pr] = w[c1] * w[c2];
-#pragma unroll
-    for (int t = 0; t < 9; t++) r4[t] = make_float4(ww[4 * t], ww[4 * t + 1], ww[4 * t + 2], ww[4 * t + 3]);
-  }
-  r4[9] = make_float4(kc * al[0], kc * al[1], kc * al[2], 0.f);
-  r4[10] = make_float4(kc * al[3], kc * al[4], kc * al[5], 0.f);
-  r4[11] = make_float4(kc * al[6], kc * al[7], kc * al[8], 0.f);
-  r4[12] = make_float4(w[0], w[1], w[2], w[3]);
-  r4[13] = make_float4(w[4], w[5], w[6], w[7]);
-  const float vr0 = al[0] * v0 + al[1] * v1 + al[2] * v2;
-  const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
-  const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
-  r4[14] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
-  return 0.5f * mW * (v0 * v0 + v1 * v1 + v2 * v2);
-}
-
-struct Tile {
-  float sum[12], cmp[12];
-  __device__ __forceinline__ void zero() {
-#pragma unroll
-    for (int e = 0; e < 12; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
-  }
-  // accumulate the cnt staged records of the warp, then compensated add
-  __device__ __forceinline__ void accumulate(const float* __restrict__ rec, int cnt, int offA,
-                                             int offB) {
-    float acc[12];
-#pragma unroll
-    for (int e = 0; e < 12; e++) acc[e] = 0.f;
-#pragma unroll 4
-    for (int r = 0; r < cnt; r++) {
-      const float4 A = *reinterpret_cast<const float4*>(rec + r * kRec + offA);
-      const float4 B = *reinterpret_cast<const float4*>(rec + r * kRec + offB);
-      const float av[4] = {A.x, A.y, A.z, A.w};
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        acc[3 * q + 0] = fmaf(av[q], B.x, acc[3 * q + 0]);
-        acc[3 * q + 1] = fmaf(av[q], B.y, acc[3 * q + 1]);
-        acc[3 * q + 2] = fmaf(av[q], B.z, acc[3 * q + 2]);
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < 12; e++) {
-      const float y = acc[e] - cmp[e];
-      const float t = sum[e] + y;
-      cmp[e] = (t - sum[e]) - y;
-      sum[e] = t;
-    }
-  }
-  // write (or add to) the cell partials
-  __device__ __forceinline__ void flush(int lane, float* __restrict__ cellM,
-                                        float* __restrict__ cellJ, long long cid, bool add) {
-    if (lane < 27) {
-      const int g = lane / 3, hh = lane % 3;
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++) {
-          const long long o = cellM_at(cid, (4 * g + q) * 9 + 3 * hh + e);
-          const float v = sum[3 * q + e] - cmp[3 * q + e];
-          cellM[o] = add ? cellM[o] + v : v;
-        }
-    } else if (lane < 29) {
-      const int g = lane - 27;
-#pragma unroll
-      for (int q = 0; q < 4; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++) {
-          const long long o = cellJ_at(cid, (4 * g + q) * 3 + e);
-          const float v = sum[3 * q + e] - cmp[3 * q + e];
-          cellJ[o] = add ? cellJ[o] + v : v;
-        }
-    }
-  }
-};
-
-__device__ __forceinline__ void lane_offsets(int lane, int& offA, int& offB) {
-  offA = lane < 27 ? 4 * (lane / 3) : 48 + 4 * (lane - 27);
-  offB = lane < 27 ? 36 + 4 * (lane % 3) : 56;
-}
-
-__device__ __forceinline__ void reduce_energy(double en, double* s_en, double* energy) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
-  if ((threadIdx.x & 31) == 0) s_en[threadIdx.x >> 5] = en;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_en[w];
-    if (t != 0.0) atomicAdd(energy, t);
   }
 }
 
