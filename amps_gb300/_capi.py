@@ -82,6 +82,8 @@ SIGNATURES = {
     "amps_gpu_field_solve": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(SolveStats)]),
     "amps_gpu_step": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(StepStats)]),
     "amps_gpu_push_deposit": (C.c_int, [P, D]),
+    "amps_gpu_update_j_mass_matrix_noalloc": (C.c_int, [C.POINTER(Config), C.c_longlong, P, P,
+                                                        P, P, P, P, P, P, P]),
     "amps_gpu_set_kernel_timing": (C.c_int, [P, C.c_int]),
     "amps_gpu_get_kernel_times": (C.c_int, [P, C.POINTER(C.c_char_p), D, LL, C.c_int,
                                             C.POINTER(C.c_int)]),

@@ -1,0 +1,276 @@
+// ECSIM current / mass-matrix deposition that allocates no device memory.
+//
+// Who needs it: callers that own every device allocation themselves and may
+// not let a library call cudaMalloc/cudaFree -- a host code that runs inside
+// a memory-pool-managed framework, or one that records its step into a CUDA
+// graph and cannot have allocations happen inside the recorded region.  They
+// pass their own device buffers for the inputs and outputs; the per-block
+// field stencils and per-cell partial sums that the deposition needs in
+// between live in one file-scope __device__ array instead.
+//
+// Limits and sharing:
+//   * the scratch array holds a mesh of at most kMaxBlocks = 16 blocks of 8^3
+//     cells (8192 cells); larger meshes are rejected with AMPS_GPU_INVALID_ARG;
+//   * the array (11.1 MiB) stays resident on every GPU that loads the library
+//     until the process exits;
+//   * every call uses the same array: two calls that overlap on the GPU (on
+//     different streams, or from different host threads without ordering)
+//     race on it.  Each call overwrites all scratch it reads, so no state
+//     leaks from one call into the next;
+//   * the first call on a device resolves the array's device address with
+//     cudaGetSymbolAddress; make that first call before any stream capture.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "deposit_core.cuh"
+
+namespace {
+
+constexpr int kMaxBlocks = 16;
+constexpr long long kMaxCells = (long long)kMaxBlocks * AMPS_CPB;
+constexpr size_t kStencilBytes = (size_t)kMaxBlocks * AMPS_SC * AMPS_DEP_STRIDE * sizeof(float);
+constexpr size_t kCellMBytes = (size_t)kMaxCells * 324 * sizeof(float);
+constexpr size_t kCellJBytes = (size_t)kMaxCells * 24 * sizeof(float);
+constexpr size_t kScratchBytes = kStencilBytes + kCellMBytes + kCellJBytes;
+static_assert(kStencilBytes % 256 == 0 && kCellMBytes % 256 == 0, "scratch sub-array alignment");
+
+// The scratch.  In host code this name is only a handle: its device address
+// comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_deposit_scratch[kScratchBytes];
+// bounded-wait bookkeeping of the stencil staging (device code names it directly)
+static __device__ unsigned long long g_na_flags[4];
+
+constexpr int kMaxDevices = 64;
+unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
+std::mutex g_setup_mu;
+
+// (slot, cell, pair) entries of the corner assembly grouped by slot, and the
+// table index of the corner inside each of its 8 cells (the same tables the
+// context path builds at run time).
+struct NaEntry {
+  unsigned char slot, cell, pair, pad;
+};
+__constant__ NaEntry c_na_asm[64] = {
+    {0, 0, 0, 0},   {0, 1, 2, 0},   {0, 2, 9, 0},   {0, 3, 5, 0},   {0, 4, 14, 0},  {0, 5, 20, 0},
+    {0, 6, 35, 0},  {0, 7, 27, 0},  {1, 1, 1, 0},   {1, 3, 8, 0},   {1, 5, 19, 0},  {1, 7, 34, 0},
+    {2, 0, 1, 0},   {2, 2, 8, 0},   {2, 4, 19, 0},  {2, 6, 34, 0},  {3, 2, 6, 0},   {3, 3, 4, 0},
+    {3, 6, 32, 0},  {3, 7, 26, 0},  {4, 3, 3, 0},   {4, 7, 25, 0},  {5, 2, 7, 0},   {5, 6, 33, 0},
+    {6, 0, 6, 0},   {6, 1, 4, 0},   {6, 4, 32, 0},  {6, 5, 26, 0},  {7, 1, 7, 0},   {7, 5, 33, 0},
+    {8, 0, 3, 0},   {8, 4, 25, 0},  {9, 4, 10, 0},  {9, 5, 16, 0},  {9, 6, 31, 0},  {9, 7, 23, 0},
+    {10, 5, 15, 0}, {10, 7, 24, 0}, {11, 4, 11, 0}, {11, 6, 30, 0}, {12, 6, 28, 0}, {12, 7, 22, 0},
+    {13, 7, 21, 0}, {14, 6, 29, 0}, {15, 4, 13, 0}, {15, 5, 17, 0}, {16, 5, 18, 0}, {17, 4, 12, 0},
+    {18, 0, 10, 0}, {18, 1, 16, 0}, {18, 2, 31, 0}, {18, 3, 23, 0}, {19, 1, 11, 0}, {19, 3, 30, 0},
+    {20, 0, 15, 0}, {20, 2, 24, 0}, {21, 2, 13, 0}, {21, 3, 17, 0}, {22, 3, 12, 0}, {23, 2, 18, 0},
+    {24, 0, 28, 0}, {24, 1, 22, 0}, {25, 1, 29, 0}, {26, 0, 21, 0}};
+__constant__ unsigned char c_na_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+
+struct NaMesh {
+  int nbx, nby, nbz;
+  __device__ __forceinline__ int nx() const { return 8 * nbx; }
+  __device__ __forceinline__ int ny() const { return 8 * nby; }
+  __device__ __forceinline__ int nz() const { return 8 * nbz; }
+  // global periodic corner index of block-local (i,j,k), i,j,k in [-8,16)
+  __device__ __forceinline__ long long global(int b, int i, int j, int k) const {
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int I = ((bx * 8 + i) % nx() + nx()) % nx();
+    const int J = ((by * 8 + j) % ny() + ny()) % ny();
+    const int K = ((bz * 8 + k) % nz() + nz()) % nz();
+    return (long long)I + (long long)nx() * (J + (long long)ny() * K);
+  }
+  // block-owned id of the same corner / cell
+  __device__ __forceinline__ long long owned(int b, int i, int j, int k) const {
+    const long long g = global(b, i, j, k);
+    const int I = (int)(g % nx()), J = (int)((g / nx()) % ny()), K = (int)(g / ((long long)nx() * ny()));
+    const int bb = (I >> 3) + nbx * ((J >> 3) + nby * (K >> 3));
+    return (long long)bb * AMPS_CPB + (I & 7) + 8 * ((J & 7) + 8 * (K & 7));
+  }
+};
+
+__global__ void k_na_pack(NaMesh m, const double* __restrict__ Bg, float* __restrict__ st) {
+  const int b = blockIdx.x;
+  for (int s = threadIdx.x; s < AMPS_SC; s += blockDim.x) {
+    const int i = s % 9, j = (s / 9) % 9, k = s / 81;
+    const long long g = m.global(b, i, j, k);
+    reinterpret_cast<float4*>(st)[(size_t)b * AMPS_SC + s] =
+        make_float4((float)Bg[3 * g], (float)Bg[3 * g + 1], (float)Bg[3 * g + 2], 0.f);
+  }
+}
+
+struct NaArgs {
+  const int* start;
+  const float* u;
+  const float* v;
+  const uint8_t* sp;
+  long long n;
+  const float* stencil;
+  float* cellM;
+  float* cellJ;
+  double* energy;
+  float inv_vol;
+  SpeciesTab st;
+};
+
+constexpr int kNaWarps = 8;
+
+__global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  float4* s_dep = s_dyn;
+  float* s_rec = reinterpret_cast<float*>(s_dyn + AMPS_SC);
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ double s_en[kNaWarps];
+  const int b = blockIdx.x, k = blockIdx.y;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (!stage_stencils(&bar, s_dep, a.stencil + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE,
+                      AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0,
+                      g_na_flags)) {
+    // the staging copy never completed: mark the energy output NaN
+    if (threadIdx.x == 0) *a.energy = __longlong_as_double(0x7ff8000000000000LL);
+    return;
+  }
+  float* rec = s_rec + wid * 32 * kRec;
+  int offA, offB;
+  lane_offsets(lane, offA, offB);
+  double en = 0.0;
+  const int j = wid;
+  for (int i = 0; i < AMPS_NC; i++) {
+    const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
+    const int b0 = a.start[cid], n0 = a.start[cid + 1] - b0;
+    Tile tile;
+    tile.zero();
+    float en_cell = 0.f;
+    for (int q0 = 0; q0 < n0; q0 += 32) {
+      const long long p = b0 + q0 + lane;
+      if (q0 + lane < n0)
+        en_cell += stage_record(rec + lane * kRec, s_dep, a.u[p], a.u[a.n + p], a.u[2 * a.n + p],
+                                a.v[p], a.v[a.n + p], a.v[2 * a.n + p], a.sp[p], 1.0f, i, j, k,
+                                a.st, a.inv_vol);
+      __syncwarp();
+      if (lane < 29) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
+      __syncwarp();
+    }
+    tile.flush(lane, a.cellM, a.cellJ, cid, false);
+    en += (double)en_cell;
+  }
+  reduce_energy(en, s_en, a.energy);
+}
+
+__global__ void __launch_bounds__(256) k_na_assemble(NaMesh m, long long ncor,
+                                                     const float* __restrict__ cellM,
+                                                     const float* __restrict__ cellJ,
+                                                     double inv_vol, double* __restrict__ M,
+                                                     double* __restrict__ J) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncor) return;
+  const int b = (int)(c / AMPS_CPB), l = (int)(c % AMPS_CPB);
+  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+  const long long g = m.global(b, i, j, k);
+  long long cell[8];
+#pragma unroll
+  for (int co = 0; co < 8; co++)
+    cell[co] = m.owned(b, i - (co & 1), j - ((co >> 1) & 1), k - ((co >> 2) & 1));
+  float acc[9];
+  int cur = c_na_asm[0].slot;
+#pragma unroll
+  for (int e = 0; e < 9; e++) acc[e] = 0.f;
+  for (int t = 0; t < 64; t++) {
+    const NaEntry en = c_na_asm[t];
+    if (en.slot != cur) {
+#pragma unroll
+      for (int e = 0; e < 9; e++) {
+        M[243 * g + cur * 9 + e] = widen(acc[e]);
+        acc[e] = 0.f;
+      }
+      cur = en.slot;
+    }
+    const float* src = cellM + cellM_at(cell[en.cell], en.pair * 9);
+#pragma unroll
+    for (int e = 0; e < 9; e++) acc[e] += src[e];
+  }
+#pragma unroll
+  for (int e = 0; e < 9; e++) M[243 * g + cur * 9 + e] = widen(acc[e]);
+  float jj[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int co = 0; co < 8; co++) {
+    const float* src = cellJ + cellJ_at(cell[co], c_na_corner[co] * 3);
+    jj[0] += src[0];
+    jj[1] += src[1];
+    jj[2] += src[2];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; d++) J[3 * g + d] = widen(jj[d]) * inv_vol;
+}
+
+// Resolves the scratch address on `dev` (current) once; 0 on success.
+cudaError_t setup_device(int dev, unsigned char** out) {
+  std::lock_guard<std::mutex> lk(g_setup_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_deposit_scratch);
+    if (e != cudaSuccess) return e;
+    const int smem = (int)(AMPS_SC * sizeof(float4) + kNaWarps * 32 * kRec * sizeof(float));
+    e = cudaFuncSetAttribute(k_na_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(
+    const amps_gpu_config* cfg, long long n, const int32_t* d_cell_start, const float* d_u,
+    const float* d_v, const uint8_t* d_spec, const double* d_B_corner, double* d_J, double* d_M,
+    double* d_energy, void* stream) {
+  if (!cfg || n < 0 || !d_cell_start || !d_B_corner || !d_J || !d_M || !d_energy ||
+      (n > 0 && (!d_u || !d_v || !d_spec)))
+    return AMPS_GPU_INVALID_ARG;
+  if (cfg->nbx <= 0 || cfg->nby <= 0 || cfg->nbz <= 0 || cfg->nspec <= 0 ||
+      cfg->nspec > AMPS_GPU_MAX_SPECIES || cfg->dt <= 0.0 || cfg->dx[0] <= 0 || cfg->dx[1] <= 0 ||
+      cfg->dx[2] <= 0)
+    return AMPS_GPU_INVALID_ARG;
+  for (int s = 0; s < cfg->nspec; s++)
+    if (cfg->mass[s] <= 0.0) return AMPS_GPU_INVALID_ARG;
+  const long long nb = (long long)cfg->nbx * cfg->nby * cfg->nbz;
+  if (nb > kMaxBlocks) return AMPS_GPU_INVALID_ARG;  // larger than the static scratch
+  if (n > (1LL << 31) - 1) return AMPS_GPU_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return AMPS_GPU_NO_DEVICE;
+  if (cfg->device < 0 || cfg->device >= ndev || cfg->device >= kMaxDevices)
+    return AMPS_GPU_INVALID_ARG;
+  if (cudaSetDevice(cfg->device) != cudaSuccess) return AMPS_GPU_CUDA_ERROR;
+  unsigned char* base = nullptr;
+  if (setup_device(cfg->device, &base) != cudaSuccess) return AMPS_GPU_CUDA_ERROR;
+  float* stencil = reinterpret_cast<float*>(base);
+  float* cellM = reinterpret_cast<float*>(base + kStencilBytes);
+  float* cellJ = reinterpret_cast<float*>(base + kStencilBytes + kCellMBytes);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const NaMesh m{cfg->nbx, cfg->nby, cfg->nbz};
+  const long long ncor = nb * AMPS_CPB;
+  if (cudaMemsetAsync(d_energy, 0, sizeof(double), s) != cudaSuccess) return AMPS_GPU_CUDA_ERROR;
+  k_na_pack<<<(unsigned)nb, 256, 0, s>>>(m, d_B_corner, stencil);
+  NaArgs a;
+  a.start = d_cell_start;
+  a.u = d_u;
+  a.v = d_v;
+  a.sp = d_spec;
+  a.n = n;
+  a.stencil = stencil;
+  a.cellM = cellM;
+  a.cellJ = cellJ;
+  a.energy = d_energy;
+  a.inv_vol = (float)(1.0 / (cfg->dx[0] * cfg->dx[1] * cfg->dx[2]));
+  for (int q = 0; q < cfg->nspec; q++) {
+    a.st.qdt2m[q] = (float)(0.5 * (cfg->charge[q] * cfg->dt / cfg->mass[q]));
+    a.st.qw[q] = (float)(cfg->charge[q] * cfg->weight[q]);
+    a.st.mw[q] = (float)(cfg->mass[q] * cfg->weight[q]);
+  }
+  const size_t smem = AMPS_SC * sizeof(float4) + kNaWarps * 32 * kRec * sizeof(float);
+  k_na_deposit<<<dim3((unsigned)nb, AMPS_NC), kNaWarps * 32, smem, s>>>(a);
+  const double inv_vol = 1.0 / (cfg->dx[0] * cfg->dx[1] * cfg->dx[2]);
+  k_na_assemble<<<(unsigned)((ncor + 255) / 256), 256, 0, s>>>(m, ncor, cellM, cellJ, inv_vol,
+                                                               d_M, d_J);
+  return cudaGetLastError() == cudaSuccess ? AMPS_GPU_OK : AMPS_GPU_CUDA_ERROR;
+}
