@@ -64,6 +64,14 @@ LL = C.POINTER(C.c_longlong)
 
 # name -> (restype, argtypes); every symbol declared in include/amps_gpu.h
 SIGNATURES = {
+    "amps_amr_build": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, D, C.c_double, P, C.c_int,
+                                 C.POINTER(P)]),
+    "amps_amr_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "amps_amr_tables": (C.c_int, [P, I32, I32, I32, I32, D, I32]),
+    "amps_amr_destroy": (C.c_int, [P]),
+    "amps_amr_nested_leaves": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_double, P, C.c_int]),
     "amps_gpu_create": (C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     "amps_gpu_destroy": (C.c_int, [P]),
     "amps_gpu_last_error": (C.c_char_p, [P]),

@@ -1,0 +1,138 @@
+"""Block-structured AMR meshes (host side, over the C ABI's amps_amr_* builder).
+
+A mesh is a list of leaf blocks of 8^3 cells; a leaf at level L has cell size
+dx0 / 2^L and an origin on the finest lattice.  AmrMesh holds the tables the
+builder derives: block -> unique corner maps, hanging-corner constraints and
+the finest-block -> leaf map (the reference's findTreeNode,
+src/meshAMR/meshAMRgeneric.h:2793-2885).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import AmpsGpuError, ptr
+
+
+class BlockDesc(C.Structure):
+    _fields_ = [("level", C.c_int), ("ix", C.c_int), ("iy", C.c_int), ("iz", C.c_int)]
+
+
+def nested_leaves(nb0, lmax, mode, frac):
+    """Leaves of a nested refinement (mode 0: central box of relative half-width
+    frac/2, mode 1: central sphere of relative radius frac; halved per level)."""
+    lib = _capi.load()
+    n = lib.amps_amr_nested_leaves(nb0[0], nb0[1], nb0[2], lmax, mode, frac, None, 0)
+    if n < 0:
+        raise AmpsGpuError(-n, "amps_amr_nested_leaves")
+    arr = (BlockDesc * n)()
+    lib.amps_amr_nested_leaves(nb0[0], nb0[1], nb0[2], lmax, mode, frac, C.cast(arr, C.c_void_p), n)
+    return np.array([(b.level, b.ix, b.iy, b.iz) for b in arr], np.int32).reshape(-1, 4)
+
+
+class AmrMesh:
+    def __init__(self, nb0, lmax, leaves, dx0=1.0, x0=(0.0, 0.0, 0.0)):
+        self.lib = _capi.load()
+        self.nb0 = tuple(int(v) for v in nb0)
+        self.lmax = int(lmax)
+        self.dx0 = float(dx0)
+        self.x0 = tuple(float(v) for v in x0)
+        leaves = np.ascontiguousarray(leaves, np.int32).reshape(-1, 4)
+        self.leaves = leaves
+        descs = (BlockDesc * len(leaves))(*[BlockDesc(*map(int, r)) for r in leaves])
+        h = C.c_void_p()
+        x0a = np.array(self.x0, np.float64)
+        st = self.lib.amps_amr_build(self.nb0[0], self.nb0[1], self.nb0[2], self.lmax,
+                                     ptr(x0a, C.c_double), self.dx0, C.cast(descs, C.c_void_p), len(leaves),
+                                     C.byref(h))
+        if st != 0:
+            raise AmpsGpuError(st, "amps_amr_build")
+        self.h = h
+        nb, nc, nh, npar = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        nf = (C.c_int * 3)()
+        self.lib.amps_amr_info(h, C.byref(nb), C.byref(nc), C.byref(nh), C.byref(npar), nf)
+        self.nblocks, self.ncorners, self.nhanging = nb.value, nc.value, nh.value
+        self.nfine = tuple(nf)
+        self.corner_tab = np.zeros(self.nblocks * 729, np.int32)
+        self.corner_xyz = np.zeros(self.ncorners * 3, np.int32)
+        self.hang_start = np.zeros(self.ncorners + 1, np.int32)
+        self.hang_parent = np.zeros(max(npar.value, 1), np.int32)
+        self.hang_weight = np.zeros(max(npar.value, 1), np.float64)
+        nfb = (self.nfine[0] // 8) * (self.nfine[1] // 8) * (self.nfine[2] // 8)
+        self.fine_map = np.zeros(nfb, np.int32)
+        self.lib.amps_amr_tables(h, ptr(self.corner_tab, C.c_int32), ptr(self.corner_xyz, C.c_int32),
+                                 ptr(self.hang_start, C.c_int32), ptr(self.hang_parent, C.c_int32),
+                                 ptr(self.hang_weight, C.c_double), ptr(self.fine_map, C.c_int32))
+        self.level = np.ascontiguousarray(leaves[:, 0])
+        self.origin = np.ascontiguousarray(leaves[:, 1:4])
+
+    @property
+    def ncells(self):
+        return self.nblocks * 512
+
+    @property
+    def dxf(self):
+        return self.dx0 / (1 << self.lmax)
+
+    def block_dx(self):
+        return self.dx0 / (2.0 ** self.level)
+
+    def block_origins(self):
+        return np.array(self.x0) + self.origin * self.dxf
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.amps_amr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def uniform_mesh(nb0, dx0=1.0):
+    """Single-level mesh of nb0 blocks per axis."""
+    leaves = [(0, 8 * i, 8 * j, 8 * k) for k in range(nb0[2]) for j in range(nb0[1])
+              for i in range(nb0[0])]
+    return AmrMesh(nb0, 0, np.array(leaves, np.int32), dx0)
+
+
+def central_refined_mesh(nb0, lmax=1, frac=0.5, dx0=1.0):
+    """Base blocks with the central box (relative half-width frac/2) refined,
+    the mesh of the AMR plasma workload."""
+    return AmrMesh(nb0, lmax, nested_leaves(nb0, lmax, 0, frac), dx0)
+
+
+def sphere_refined_mesh(nb0, lmax, radius=0.2, dx0=1.0):
+    return AmrMesh(nb0, lmax, nested_leaves(nb0, lmax, 1, radius), dx0)
+
+
+def amr_initial_condition(mesh, species, ppc_base, seed=100):
+    """Uniform-density Maxwellian plasma on an AMR mesh: ppc_base particles per
+    species per level-0 cell volume (so a cell at level L holds ppc_base/8^L),
+    positions uniform within each cell, co-located species, reference LCG
+    stream split per block.  Returns u (FP32 block-local cell units), v, spec,
+    block, all FP32-representable."""
+    ns = len(species)
+    vth = np.array([s.vth for s in species], np.float64)
+    lib = _capi.load()
+    us, vs, ss, bs = [], [], [], []
+    for b in range(mesh.nblocks):
+        L = int(mesh.level[b])
+        ppc = max(1, ppc_base // (8 ** L))
+        n = lib.amps_ic_count(1, 1, 1, ppc, ns)
+        u = np.empty((n, 3), np.float32)
+        v = np.empty((n, 3), np.float32)
+        sp = np.empty(n, np.uint8)
+        bl = np.empty(n, np.int32)
+        st = lib.amps_ic_maxwellian(1, 1, 1, ppc, ns, ptr(vth, C.c_double),
+                                    (seed * 7919 + 104729 * (b + 1)) & 0x7FFFFFFF or 1, 1,
+                                    ptr(u, C.c_float), ptr(v, C.c_float), ptr(sp, C.c_uint8),
+                                    ptr(bl, C.c_int32))
+        if st != 0:
+            raise AmpsGpuError(st, "amps_ic_maxwellian")
+        us.append(u); vs.append(v); ss.append(sp); bs.append(np.full(n, b, np.int32))
+    return {"u": np.concatenate(us), "v": np.concatenate(vs), "spec": np.concatenate(ss),
+            "block": np.concatenate(bs)}

@@ -87,6 +87,40 @@ typedef struct {
   long long ulp_face;           /* particles that ended within 1 FP32 ulp of a cell face */
 } amps_gpu_step_stats;
 
+/* ---- block-structured AMR meshes (leaf blocks of the reference octree,
+ *      src/meshAMR/meshAMRgeneric.h) ----
+ * A leaf block has 8^3 cells, a refinement level (cell size dx0 / 2^level) and
+ * its origin on the finest lattice in finest-cell units.  amps_amr_build checks
+ * coverage, non-overlap and 2:1 balance (faces, edges, vertices), numbers the
+ * unique corners, and derives the hanging-corner constraints (interpolation
+ * from the coarser block's corners) that the reference's same-level stencils
+ * (src/pic/ecsim/get_stencil.cpp:1100-1160) leave undefined. */
+typedef struct {
+  int level;
+  int ix, iy, iz;  /* origin, finest-cell units */
+} amps_block_desc;
+
+typedef struct amps_amr_mesh amps_amr_mesh;
+
+amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax, const double* x0,
+                               double dx0, const amps_block_desc* blocks, int nblocks,
+                               amps_amr_mesh** out);
+amps_gpu_status amps_amr_info(const amps_amr_mesh* m, int* nblocks, int* ncorners, int* nhanging,
+                              int* nparents, int* nfine);
+/* corner_tab[nblocks*729] (block-local corner i+9(j+9k) -> unique corner),
+ * corner_xyz[3*ncorners], hang_start[ncorners+1], hang_parent[nparents],
+ * hang_weight[nparents], fine_map[finest blocks]; any pointer may be NULL */
+amps_gpu_status amps_amr_tables(const amps_amr_mesh* m, int32_t* corner_tab, int32_t* corner_xyz,
+                                int32_t* hang_start, int32_t* hang_parent, double* hang_weight,
+                                int32_t* fine_map);
+amps_gpu_status amps_amr_destroy(amps_amr_mesh* m);
+/* Leaves of a nested refinement: mode 0 refines a central box of relative
+ * half-width frac/2 (halved per level), mode 1 a central sphere of relative
+ * radius frac (halved per level); 2:1 balance enforced.  Returns the leaf
+ * count (negative status on error) and fills up to cap leaves. */
+int amps_amr_nested_leaves(int nbx0, int nby0, int nbz0, int lmax, int mode, double frac,
+                           amps_block_desc* out, int cap);
+
 /* ---- context (PIC::Init / ECSIM::Init analogue) ---- */
 amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out);
 amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* ctx);

@@ -1,0 +1,522 @@
+/*
+ * amps_oracle_amr.c -- FP64 CPU restatement of the ECSIM particle / field path
+ * on block-structured AMR meshes.  TEST INFRASTRUCTURE ONLY.
+ *
+ * The reference's ECSIM discretisation is written corner by corner for a
+ * uniform mesh; per cell it is
+ *   curl E (cell) = C E_corners     UpdateB, pic_field_solver_ecsim.cpp:5160-5711
+ *   curl B (corner) = C^T B_cells   GetStencil's curl B supports, get_stencil.cpp:1500-1599
+ *   curl curl = C^T C assembled     the compact stencils of InitDiscritizationStencil :7121
+ *   M = per-cell pair sums          ProcessCell, :1882-2438
+ * (C: 3 x 24 face-average differences, coefficient 1/(4 dx)).  On an AMR mesh
+ * the same per-cell pieces are assembled with each cell's own dx in weak form
+ * (every cell term times its volume), and the corners of fine blocks that lie
+ * on a coarser block's face or edge without being its corners ("hanging")
+ * take the multilinear interpolation of the coarse corners: the operator is
+ * P^T A P on the free corners, and hanging rows read x_h - (P x)_h = 0.  On a
+ * uniform mesh this is the reference's operator times the cell volume.
+ * The reference itself defines no coarse/fine interface (its stencils assume
+ * same-level neighbours, get_stencil.cpp:1100-1160): parity across levels is
+ * pinned by energy conservation, not by reference output.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PI_D 3.14159265358979323846264338327950288
+#define NSPEC_MAX 8
+
+typedef struct {
+  int nblocks, ncorners, lmax;
+  int nfine[3];
+  double x0[3], dx0;
+  const int32_t* level;       /* nblocks */
+  const int32_t* origin;      /* nblocks*3, finest-cell units */
+  const int32_t* corner_tab;  /* nblocks*729 */
+  const int32_t* hang_start;  /* ncorners+1 */
+  const int32_t* hang_parent;
+  const double* hang_weight;
+  const int32_t* fine_map;    /* finest blocks */
+  int nspec;
+  double q[NSPEC_MAX], m[NSPEC_MAX], w[NSPEC_MAX];
+  double dt, theta;
+} orc_amr;
+
+static const int kOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                               {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+static int wrapi(int v, int n) { v %= n; return v < 0 ? v + n : v; }
+
+static double bdx(const orc_amr* g, int b) { return g->dx0 / (double)(1 << g->level[b]); }
+
+static void borigin(const orc_amr* g, int b, double o[3]) {
+  const double dxf = g->dx0 / (double)(1 << g->lmax);
+  for (int d = 0; d < 3; d++) o[d] = g->x0[d] + g->origin[3 * b + d] * dxf;
+}
+
+/* value of a corner field (3 comps) with the hanging constraint applied */
+static void corner_val(const orc_amr* g, const double* F, int c, double out[3]) {
+  const int s = g->hang_start[c], e = g->hang_start[c + 1];
+  if (s == e) {
+    for (int d = 0; d < 3; d++) out[d] = F[3 * c + d];
+    return;
+  }
+  out[0] = out[1] = out[2] = 0.0;
+  for (int t = s; t < e; t++)
+    for (int d = 0; d < 3; d++) out[d] += g->hang_weight[t] * F[3 * g->hang_parent[t] + d];
+}
+
+static int cell_corner(const orc_amr* g, int b, int i, int j, int k) {
+  return g->corner_tab[b * 729 + i + 9 * (j + 9 * k)];
+}
+
+/* block containing x (finest-block map), block-local cell (FindCellIndex) */
+static void locate_one(const orc_amr* g, double x[3], int32_t* blk, int32_t* cel) {
+  const double dxf = g->dx0 / (double)(1 << g->lmax);
+  int F[3];
+  for (int d = 0; d < 3; d++) {
+    const double L = g->nfine[d] * dxf;
+    /* periodic wrap of the position itself */
+    if (x[d] < g->x0[d]) x[d] += L;
+    if (x[d] >= g->x0[d] + L) x[d] -= L;
+    if (x[d] >= g->x0[d] + L) x[d] = g->x0[d] + L - 1e-10 * dxf;
+    if (x[d] < g->x0[d]) x[d] = g->x0[d];
+    F[d] = (int)floor((x[d] - g->x0[d]) / dxf);
+    if (F[d] >= g->nfine[d]) F[d] = g->nfine[d] - 1;
+    if (F[d] < 0) F[d] = 0;
+  }
+  const int nfb0 = g->nfine[0] / 8, nfb1 = g->nfine[1] / 8;
+  const int b = g->fine_map[F[0] / 8 + nfb0 * (F[1] / 8 + nfb1 * (F[2] / 8))];
+  double o[3];
+  borigin(g, b, o);
+  const double dx = bdx(g, b);
+  int ic[3];
+  for (int d = 0; d < 3; d++) {
+    int i = (int)((x[d] - o[d]) / dx);
+    if (i >= 8) i = 7;
+    if (i < 0) i = 0;
+    ic[d] = i;
+  }
+  *blk = b;
+  *cel = ic[0] + 8 * (ic[1] + 8 * ic[2]);
+}
+
+void orc_amr_locate(const orc_amr* g, long n, double* x, int32_t* block, int32_t* cell) {
+  for (long p = 0; p < n; p++) locate_one(g, x + 3 * p, block + p, cell + p);
+}
+
+static void alpha_matrix(double h, const double B[3], double al[9]) {
+  double sq = h * h, P[3], BB[3][3];
+  for (int i = 0; i < 3; i++) {
+    P[i] = -h * B[i];
+    for (int j = 0; j < 3; j++) BB[i][j] = sq * B[i] * B[j];
+  }
+  double c0 = 1.0 / (1.0 + sq * (B[0] * B[0] + B[1] * B[1] + B[2] * B[2]));
+  al[0] = c0 * (1.0 + BB[0][0]); al[1] = c0 * (-P[2] + BB[0][1]); al[2] = c0 * (P[1] + BB[0][2]);
+  al[3] = c0 * (P[2] + BB[1][0]); al[4] = c0 * (1.0 + BB[1][1]); al[5] = c0 * (-P[0] + BB[1][2]);
+  al[6] = c0 * (-P[1] + BB[2][0]); al[7] = c0 * (P[0] + BB[2][1]); al[8] = c0 * (1.0 + BB[2][2]);
+}
+
+/* trilinear weights in table order and the corresponding unique corners */
+static void stencil(const orc_amr* g, int b, const double x[3], double w[8], int cid[8]) {
+  double o[3], f[3];
+  int ic[3];
+  borigin(g, b, o);
+  const double dx = bdx(g, b);
+  for (int d = 0; d < 3; d++) {
+    double u = (x[d] - o[d]) / dx;
+    int i = (int)u;
+    if (i > 7) i = 7;
+    if (i < 0) i = 0;
+    ic[d] = i;
+    f[d] = u - i;
+  }
+  for (int c = 0; c < 8; c++) {
+    double ww = 1.0;
+    for (int d = 0; d < 3; d++) ww *= kOff[c][d] ? f[d] : 1.0 - f[d];
+    w[c] = ww;
+    cid[c] = cell_corner(g, b, ic[0] + kOff[c][0], ic[1] + kOff[c][1], ic[2] + kOff[c][2]);
+  }
+}
+
+long orc_amr_push(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
+                  int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev) {
+  for (long p = 0; p < n; p++) {
+    double w[8], E[3] = {0, 0, 0}, B[3] = {0, 0, 0}, val[3];
+    int cid[8];
+    stencil(g, block[p], x + 3 * p, w, cid);
+    for (int c = 0; c < 8; c++) {
+      corner_val(g, E_half, cid[c], val);
+      for (int d = 0; d < 3; d++) E[d] += w[c] * val[d];
+      corner_val(g, Bc_prev, cid[c], val);
+      for (int d = 0; d < 3; d++) B[d] += w[c] * val[d];
+    }
+    const int s = spec[p];
+    const double h = 0.5 * g->q[s] * g->dt / g->m[s];
+    double al[9], vn[3];
+    alpha_matrix(h, B, al);
+    for (int i = 0; i < 3; i++) {
+      double vp = 0.0;
+      for (int j = 0; j < 3; j++) vp += al[3 * i + j] * (v[3 * p + j] + h * E[j]);
+      vn[i] = 2.0 * vp - v[3 * p + i];
+    }
+    for (int d = 0; d < 3; d++) {
+      v[3 * p + d] = vn[d];
+      x[3 * p + d] += g->dt * vn[d];
+    }
+    locate_one(g, x + 3 * p, block + p, cell + p);
+  }
+  return 0;
+}
+
+/* per-cell partials (cellJ[ncell*24] = sum q W w_c alpha v; cellM[ncell*324] =
+ * sum (q W qdt/2m / V) w_c1 w_c2 alpha over pairs c2<=c1).  Returns energy. */
+double orc_amr_deposit(const orc_amr* g, long n, const double* x, const double* v,
+                       const uint8_t* spec, const double* wcorr, const int32_t* block,
+                       const int32_t* cell, const double* Bc_cur, double* cellJ, double* cellM) {
+  const long ncell = (long)g->nblocks * 512;
+  memset(cellJ, 0, sizeof(double) * ncell * 24);
+  memset(cellM, 0, sizeof(double) * ncell * 324);
+  double energy = 0.0;
+  for (long p = 0; p < n; p++) {
+    double w[8], B[3] = {0, 0, 0}, val[3];
+    int cid[8];
+    const int b = block[p];
+    stencil(g, b, x + 3 * p, w, cid);
+    for (int c = 0; c < 8; c++) {
+      corner_val(g, Bc_cur, cid[c], val);
+      for (int d = 0; d < 3; d++) B[d] += w[c] * val[d];
+    }
+    const double dx = bdx(g, b), V = dx * dx * dx;
+    const int s = spec[p];
+    const double W = g->w[s] * (wcorr ? wcorr[p] : 1.0);
+    const double qW = g->q[s] * W, mW = g->m[s] * W;
+    const double h = 0.5 * qW * g->dt / mW;
+    double al[9], vr[3] = {0, 0, 0};
+    alpha_matrix(h, B, al);
+    const double* vv = v + 3 * p;
+    energy += 0.5 * mW * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) vr[i] += al[3 * i + j] * vv[j];
+    const long cl = (long)b * 512 + cell[p];
+    for (int c = 0; c < 8; c++)
+      for (int d = 0; d < 3; d++) cellJ[cl * 24 + 3 * c + d] += qW * w[c] * vr[d];
+    const double mc = qW * h / V;
+    int pr = 0;
+    for (int c1 = 0; c1 < 8; c1++)
+      for (int c2 = 0; c2 <= c1; c2++, pr++)
+        for (int ab = 0; ab < 9; ab++) cellM[cl * 324 + pr * 9 + ab] += mc * w[c1] * w[c2] * al[ab];
+  }
+  return energy;
+}
+
+/* curl of the cell from its 8 corner values (table order): C x */
+static void cell_curl(const double e[8][3], double dx, double out[3]) {
+  double dEz_dy = 0, dEy_dz = 0, dEx_dz = 0, dEz_dx = 0, dEy_dx = 0, dEx_dy = 0;
+  for (int c = 0; c < 8; c++) {
+    const double sx = kOff[c][0] ? 1.0 : -1.0, sy = kOff[c][1] ? 1.0 : -1.0,
+                 sz = kOff[c][2] ? 1.0 : -1.0;
+    dEz_dy += sy * e[c][2]; dEy_dz += sz * e[c][1];
+    dEx_dz += sz * e[c][0]; dEz_dx += sx * e[c][2];
+    dEy_dx += sx * e[c][1]; dEx_dy += sy * e[c][0];
+  }
+  const double f = 0.25 / dx;
+  out[0] = f * (dEz_dy - dEy_dz);
+  out[1] = f * (dEx_dz - dEz_dx);
+  out[2] = f * (dEy_dx - dEx_dy);
+}
+
+/* C^T y scattered onto the 8 corners (adds s * C^T y) */
+static void cell_curl_t(const double y[3], double dx, double s, double out[8][3]) {
+  const double f = 0.25 / dx * s;
+  for (int c = 0; c < 8; c++) {
+    const double sx = kOff[c][0] ? 1.0 : -1.0, sy = kOff[c][1] ? 1.0 : -1.0,
+                 sz = kOff[c][2] ? 1.0 : -1.0;
+    out[c][0] += f * (sz * y[1] - sy * y[2]);
+    out[c][1] += f * (sx * y[2] - sz * y[0]);
+    out[c][2] += f * (sy * y[0] - sx * y[1]);
+  }
+}
+
+static int pair_index(int a, int b) {
+  const int hi = a > b ? a : b, lo = a > b ? b : a;
+  return hi * (hi + 1) / 2 + lo;
+}
+
+/* y = A x on the full corner vector (free rows: P^T A P x; hanging rows: x_h - (P x)_h).
+ * with_identity/with_curl/with_mass select the operator pieces (all on for the solve). */
+void orc_amr_apply(const orc_amr* g, const double* cellM, const double* x, double* y,
+                   int with_identity, int with_curl, int with_mass) {
+  const int nc = g->ncorners;
+  memset(y, 0, sizeof(double) * 3 * nc);
+  const double f = 4.0 * PI_D * g->dt * g->theta, th2 = g->theta * g->theta * g->dt * g->dt;
+  for (int b = 0; b < g->nblocks; b++) {
+    const double dx = bdx(g, b), V = dx * dx * dx;
+    for (int l = 0; l < 512; l++) {
+      const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+      int cid[8];
+      double e[8][3], out[8][3];
+      memset(out, 0, sizeof(out));
+      for (int c = 0; c < 8; c++) {
+        cid[c] = cell_corner(g, b, i + kOff[c][0], j + kOff[c][1], k + kOff[c][2]);
+        corner_val(g, x, cid[c], e[c]);
+      }
+      if (with_identity)
+        for (int c = 0; c < 8; c++)
+          for (int d = 0; d < 3; d++) out[c][d] += 0.125 * V * e[c][d];
+      if (with_curl) {
+        double cu[3];
+        cell_curl(e, dx, cu);
+        cell_curl_t(cu, dx, th2 * V, out);
+      }
+      if (with_mass) {
+        const double* mm = cellM + ((long)b * 512 + l) * 324;
+        for (int a = 0; a < 8; a++)
+          for (int c2 = 0; c2 < 8; c2++) {
+            const double* blk = mm + pair_index(a, c2) * 9;
+            for (int p = 0; p < 3; p++)
+              for (int q = 0; q < 3; q++) out[a][p] += f * V * blk[3 * p + q] * e[c2][q];
+          }
+      }
+      /* scatter with P^T */
+      for (int c = 0; c < 8; c++) {
+        const int cc = cid[c], s = g->hang_start[cc], en = g->hang_start[cc + 1];
+        if (s == en) {
+          for (int d = 0; d < 3; d++) y[3 * cc + d] += out[c][d];
+        } else {
+          for (int t = s; t < en; t++)
+            for (int d = 0; d < 3; d++) y[3 * g->hang_parent[t] + d] += g->hang_weight[t] * out[c][d];
+        }
+      }
+    }
+  }
+  /* hanging rows: constraint */
+  for (int c = 0; c < nc; c++) {
+    const int s = g->hang_start[c], en = g->hang_start[c + 1];
+    if (s == en) continue;
+    double pv[3];
+    corner_val(g, x, c, pv);
+    for (int d = 0; d < 3; d++) y[3 * c + d] = x[3 * c + d] - pv[d];
+  }
+}
+
+/* RHS in weak form: sum_cells V [theta c dt C^T B - (theta c dt)^2 C^T C E^n - f M E^n] - f J_weak,
+ * with J_weak = sum_cells cellJ (no 1/V); hanging rows 0. */
+void orc_amr_rhs(const orc_amr* g, const double* E_n, const double* Bcen, const double* cellJ,
+                 const double* cellM, double* rhs) {
+  const int nc = g->ncorners;
+  double* tmp = (double*)malloc(sizeof(double) * 3 * nc);
+  orc_amr_apply(g, cellM, E_n, tmp, 0, 1, 1);
+  const double f = 4.0 * PI_D * g->dt * g->theta;
+  for (long i = 0; i < 3L * nc; i++) rhs[i] = -tmp[i];
+  for (int b = 0; b < g->nblocks; b++) {
+    const double dx = bdx(g, b), V = dx * dx * dx;
+    for (int l = 0; l < 512; l++) {
+      const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+      const long cl = (long)b * 512 + l;
+      double out[8][3];
+      memset(out, 0, sizeof(out));
+      cell_curl_t(Bcen + 3 * cl, dx, g->theta * g->dt * V, out);
+      for (int c = 0; c < 8; c++)
+        for (int d = 0; d < 3; d++) out[c][d] -= f * cellJ[cl * 24 + 3 * c + d];
+      for (int c = 0; c < 8; c++) {
+        const int cc = cell_corner(g, b, i + kOff[c][0], j + kOff[c][1], k + kOff[c][2]);
+        const int s = g->hang_start[cc], en = g->hang_start[cc + 1];
+        if (s == en) {
+          for (int d = 0; d < 3; d++) rhs[3 * cc + d] += out[c][d];
+        } else {
+          for (int t = s; t < en; t++)
+            for (int d = 0; d < 3; d++) rhs[3 * g->hang_parent[t] + d] += g->hang_weight[t] * out[c][d];
+        }
+      }
+    }
+  }
+  for (int c = 0; c < nc; c++)
+    if (g->hang_start[c + 1] > g->hang_start[c])
+      for (int d = 0; d < 3; d++) rhs[3 * c + d] = 0.0;
+  free(tmp);
+}
+
+static double dotv(long n, const double* a, const double* b) {
+  double s = 0.0;
+  for (long i = 0; i < n; i++) s += a[i] * b[i];
+  return s;
+}
+
+/* restarted GMRES(m), x0 = 0, no preconditioner; stop on ||b-Ax|| <= tol ||b|| */
+int orc_amr_gmres(const orc_amr* g, const double* cellM, const double* b, double* x, double tol,
+                  int maxit, int restart, double* resid_out) {
+  const long n = 3L * g->ncorners;
+  const int m = restart;
+  double* V = (double*)malloc(sizeof(double) * n * (m + 1));
+  double* w = (double*)malloc(sizeof(double) * n);
+  double* H = (double*)calloc((size_t)(m + 1) * m, sizeof(double));
+  double *cs = (double*)malloc(sizeof(double) * m), *sn = (double*)malloc(sizeof(double) * m);
+  double* s = (double*)malloc(sizeof(double) * (m + 1));
+  double* yv = (double*)malloc(sizeof(double) * m);
+  for (long i = 0; i < n; i++) x[i] = 0.0;
+  const double bn = sqrt(dotv(n, b, b));
+  int it = 0, conv = 0;
+  double rel = 0.0;
+  if (bn == 0.0) { conv = 1; goto done; }
+  while (it < maxit) {
+    orc_amr_apply(g, cellM, x, w, 1, 1, 1);
+    for (long i = 0; i < n; i++) V[i] = b[i] - w[i];
+    double beta = sqrt(dotv(n, V, V));
+    rel = beta / bn;
+    if (rel <= tol) { conv = 1; break; }
+    for (long i = 0; i < n; i++) V[i] /= beta;
+    for (int i = 0; i <= m; i++) s[i] = 0.0;
+    s[0] = beta;
+    int j;
+    for (j = 0; j < m && it < maxit; j++) {
+      it++;
+      orc_amr_apply(g, cellM, V + (long)j * n, w, 1, 1, 1);
+      for (int i = 0; i <= j; i++) {
+        double hh = dotv(n, w, V + (long)i * n);
+        H[i * m + j] = hh;
+        for (long t = 0; t < n; t++) w[t] -= hh * V[(long)i * n + t];
+      }
+      double hn = sqrt(dotv(n, w, w));
+      H[(j + 1) * m + j] = hn;
+      for (long t = 0; t < n; t++) V[(long)(j + 1) * n + t] = hn > 0 ? w[t] / hn : 0.0;
+      for (int i = 0; i < j; i++) {
+        double a = H[i * m + j], c = H[(i + 1) * m + j];
+        H[i * m + j] = cs[i] * a + sn[i] * c;
+        H[(i + 1) * m + j] = -sn[i] * a + cs[i] * c;
+      }
+      double a = H[j * m + j], c = H[(j + 1) * m + j], r = sqrt(a * a + c * c);
+      cs[j] = r > 0 ? a / r : 1.0;
+      sn[j] = r > 0 ? c / r : 0.0;
+      H[j * m + j] = r;
+      H[(j + 1) * m + j] = 0.0;
+      s[j + 1] = -sn[j] * s[j];
+      s[j] = cs[j] * s[j];
+      rel = fabs(s[j + 1]) / bn;
+      if (rel <= tol) { j++; break; }
+    }
+    for (int i = j - 1; i >= 0; i--) {
+      double t = s[i];
+      for (int k = i + 1; k < j; k++) t -= H[i * m + k] * yv[k];
+      yv[i] = t / H[i * m + i];
+    }
+    for (long t = 0; t < n; t++) {
+      double acc = 0.0;
+      for (int i = 0; i < j; i++) acc += yv[i] * V[(long)i * n + t];
+      x[t] += acc;
+    }
+    if (rel <= tol) {
+      orc_amr_apply(g, cellM, x, w, 1, 1, 1);
+      for (long i = 0; i < n; i++) w[i] = b[i] - w[i];
+      rel = sqrt(dotv(n, w, w)) / bn;
+      if (rel <= 10 * tol) { conv = 1; break; }
+    }
+  }
+done:
+  if (resid_out) *resid_out = rel;
+  free(V); free(w); free(H); free(cs); free(sn); free(s); free(yv);
+  return conv ? it : -it;
+}
+
+/* B^{n+1} = B^n - c dt C E^{n+theta} per cell */
+void orc_amr_update_b(const orc_amr* g, const double* E_half, const double* Bn, double* Bnp1) {
+  for (int b = 0; b < g->nblocks; b++) {
+    const double dx = bdx(g, b);
+    for (int l = 0; l < 512; l++) {
+      const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+      double e[8][3], cu[3];
+      for (int c = 0; c < 8; c++)
+        corner_val(g, E_half, cell_corner(g, b, i + kOff[c][0], j + kOff[c][1], k + kOff[c][2]), e[c]);
+      cell_curl(e, dx, cu);
+      const long cl = (long)b * 512 + l;
+      for (int d = 0; d < 3; d++) Bnp1[3 * cl + d] = Bn[3 * cl + d] - g->dt * cu[d];
+    }
+  }
+}
+
+/* corner B: volume-weighted mean of the touching cells; hanging corners interpolated */
+void orc_amr_c2n(const orc_amr* g, const double* Bcen, double* Bcor) {
+  const int nc = g->ncorners;
+  double* wsum = (double*)calloc((size_t)nc, sizeof(double));
+  memset(Bcor, 0, sizeof(double) * 3 * nc);
+  for (int b = 0; b < g->nblocks; b++) {
+    const double dx = bdx(g, b), V = dx * dx * dx;
+    for (int l = 0; l < 512; l++) {
+      const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+      const long cl = (long)b * 512 + l;
+      for (int c = 0; c < 8; c++) {
+        const int cc = cell_corner(g, b, i + kOff[c][0], j + kOff[c][1], k + kOff[c][2]);
+        wsum[cc] += V;
+        for (int d = 0; d < 3; d++) Bcor[3 * cc + d] += V * Bcen[3 * cl + d];
+      }
+    }
+  }
+  for (int c = 0; c < nc; c++)
+    if (wsum[c] > 0)
+      for (int d = 0; d < 3; d++) Bcor[3 * c + d] /= wsum[c];
+  for (int c = 0; c < nc; c++) {
+    if (g->hang_start[c + 1] == g->hang_start[c]) continue;
+    double v[3];
+    corner_val(g, Bcor, c, v);
+    for (int d = 0; d < 3; d++) Bcor[3 * c + d] = v[d];
+  }
+  free(wsum);
+}
+
+/* E^{n+1} in place; hanging corners re-interpolated.  Returns the wave energy
+ * sum_cells V (sum_corners |E|^2 / 8 + |B|^2) / (8 pi). */
+double orc_amr_update_e(const orc_amr* g, const double* E_half, double* E_n, const double* Bcen) {
+  const int nc = g->ncorners;
+  const double th = g->theta;
+  for (long i = 0; i < 3L * nc; i++) E_n[i] = (E_half[i] - (1.0 - th) * E_n[i]) / th;
+  for (int c = 0; c < nc; c++) {
+    if (g->hang_start[c + 1] == g->hang_start[c]) continue;
+    double v[3];
+    corner_val(g, E_n, c, v);
+    for (int d = 0; d < 3; d++) E_n[3 * c + d] = v[d];
+  }
+  double sum = 0.0;
+  for (int b = 0; b < g->nblocks; b++) {
+    const double dx = bdx(g, b), V = dx * dx * dx;
+    for (int l = 0; l < 512; l++) {
+      const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+      const long cl = (long)b * 512 + l;
+      double e2 = 0.0;
+      for (int c = 0; c < 8; c++) {
+        double v[3];
+        corner_val(g, E_n, cell_corner(g, b, i + kOff[c][0], j + kOff[c][1], k + kOff[c][2]), v);
+        e2 += v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+      }
+      const double* B = Bcen + 3 * cl;
+      sum += (0.125 * e2 + B[0] * B[0] + B[1] * B[1] + B[2] * B[2]) * V * 0.125 / PI_D;
+    }
+  }
+  return sum;
+}
+
+/* one ECSIM step on the AMR mesh (reference order of pic_time_step.cpp:403-551) */
+int orc_amr_step(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
+                 const double* wcorr, int32_t* block, int32_t* cell, double* E_n, double* E_half,
+                 double* Bcen, double* Bcor_prev, double* Bcor_cur, double* cellJ, double* cellM,
+                 double tol, int maxit, double* diag) {
+  const int nc = g->ncorners;
+  const long ncell = (long)g->nblocks * 512;
+  double* rhs = (double*)malloc(sizeof(double) * 3 * nc);
+  double* dE = (double*)malloc(sizeof(double) * 3 * nc);
+  double* Bnew = (double*)malloc(sizeof(double) * 3 * ncell);
+  double resid = 0.0;
+  orc_amr_rhs(g, E_n, Bcen, cellJ, cellM, rhs);
+  int it = orc_amr_gmres(g, cellM, rhs, dE, tol, maxit, 30, &resid);
+  for (long i = 0; i < 3L * nc; i++) E_half[i] = E_n[i] + dE[i];
+  orc_amr_update_b(g, E_half, Bcen, Bnew);
+  memcpy(Bcen, Bnew, sizeof(double) * 3 * ncell);
+  memcpy(Bcor_prev, Bcor_cur, sizeof(double) * 3 * nc);
+  orc_amr_c2n(g, Bcen, Bcor_cur);
+  double wave = orc_amr_update_e(g, E_half, E_n, Bcen);
+  orc_amr_push(g, n, x, v, spec, block, cell, E_half, Bcor_prev);
+  double pe = orc_amr_deposit(g, n, x, v, spec, wcorr, block, cell, Bcor_cur, cellJ, cellM);
+  if (diag) { diag[0] = pe; diag[1] = wave; diag[2] = resid; }
+  free(rhs); free(dE); free(Bnew);
+  return it;
+}

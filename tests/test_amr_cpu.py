@@ -1,0 +1,130 @@
+"""AMR mesh builder and the cell-assembled ECSIM operator (CPU only).
+
+* builder invariants: coverage, hanging-corner constraints (weights sum to 1,
+  parents free), 2:1 balance rejected when violated;
+* on a single-level mesh the cell-assembled operator and RHS of the AMR oracle
+  equal the uniform oracle's (itself pinned to the reference stencil taps)
+  times the cell volume -- so the AMR extension reduces to the reference;
+* on a two-level mesh with hanging corners the ECSIM step conserves total
+  energy (theta = 0.5), the property the reference's discretisation is built on.
+"""
+import numpy as np
+import pytest
+
+import amps_gb300 as A
+from amps_gb300 import amr
+from tests import oracle_amr as OA
+from tests import oracle_lib as O
+
+
+def test_uniform_mesh_has_no_hanging_corners():
+    m = amr.uniform_mesh((2, 1, 2))
+    assert m.nblocks == 4 and m.ncorners == m.ncells and m.nhanging == 0
+    assert (m.fine_map >= 0).all()
+
+
+def test_central_refined_mesh_tables():
+    m = amr.central_refined_mesh((4, 4, 4), lmax=1, frac=0.5)
+    assert m.nblocks == 56 + 64
+    assert m.nhanging > 0
+    vol = np.sum((8 * m.block_dx()) ** 3)
+    assert vol == pytest.approx(32.0 ** 3)
+    hs = m.hang_start
+    for c in np.flatnonzero(hs[1:] > hs[:-1]):
+        w = m.hang_weight[hs[c]:hs[c + 1]]
+        par = m.hang_parent[hs[c]:hs[c + 1]]
+        assert w.sum() == pytest.approx(1.0)
+        assert np.all(hs[par + 1] == hs[par])          # parents are free corners
+        # the hanging corner is the weighted mean of its parents' positions
+        xyz = m.corner_xyz.reshape(-1, 3).astype(float)
+        mid = (w[:, None] * xyz[par]).sum(0)
+        d = np.abs(mid - xyz[c])
+        d = np.minimum(d, np.array(m.nfine) - d)
+        assert d.max() < 1e-9
+    # config 2 mesh: 448 coarse + 512 fine blocks
+    m2 = amr.central_refined_mesh((8, 8, 8), lmax=1, frac=0.5)
+    assert m2.nblocks == 960 and np.sum(m2.level == 1) == 512
+
+
+def test_unbalanced_mesh_rejected():
+    # a level-2 block next to a level-0 block violates 2:1 balance
+    leaves = [(2, 0, 0, 0)]
+    leaves += [(2, x, y, z) for z in (0, 8) for y in (0, 8) for x in (0, 8) if (x, y, z) != (0, 0, 0)]
+    leaves += [(1, x, y, z) for z in (0, 16) for y in (0, 16) for x in (0, 16) if (x, y, z) != (0, 0, 0)]
+    leaves += [(0, 32, 0, 0)]  # level-0 neighbour of the level-1 block is fine, of level-2 is not
+    with pytest.raises(A.AmpsGpuError):
+        amr.AmrMesh((2, 1, 1), 2, np.array(leaves, np.int32)).close()
+
+
+def uniform_pair(nb, ppc=4, seed=5):
+    wl = A.electron_proton_plasma("t", *nb, ppc, 2)
+    wl.seed = seed
+    ic = A.make_initial_condition(wl, nthreads=2)
+    x = A.physical_positions(wl.mesh, ic["u"], ic["block"])
+    v = ic["v"].astype(np.float64)
+    rng = np.random.default_rng(seed)
+    f = A.initial_fields(wl)
+    for k in ("B_corner_cur", "B_corner_prev", "B_center"):
+        f[k] = f[k] + 0.05 * rng.standard_normal(f[k].shape)
+    st = O.OracleState(wl, x, v, ic["spec"], f)
+    st.deposit()
+    m = amr.uniform_mesh(nb)
+    ao = OA.AmrOracle(m, wl.species, wl.dt, wl.theta, x, v, ic["spec"])
+    xyz = m.corner_xyz.reshape(-1, 3)
+    NX, NY, _ = wl.mesh.shape
+    gidx = xyz[:, 0] + NX * (xyz[:, 1] + NY * xyz[:, 2])   # AMR corner -> uniform corner
+    ao.Bcur[:] = f["B_corner_cur"][gidx]
+    # cells: both use block*512 + local numbering
+    ao.Bcen[:] = f["B_center"][cell_map(wl)]
+    ao.deposit()
+    return wl, st, ao, gidx, rng
+
+
+def cell_map(wl):
+    """uniform global cell index of every AMR cell (block*512 + local)"""
+    nb = wl.mesh.nblocks
+    b = np.repeat(np.arange(nb), 512)
+    l = np.tile(np.arange(512), nb)
+    bx = b % wl.mesh.nbx; by = (b // wl.mesh.nbx) % wl.mesh.nby; bz = b // (wl.mesh.nbx * wl.mesh.nby)
+    I = bx * 8 + (l & 7); J = by * 8 + ((l >> 3) & 7); K = bz * 8 + (l >> 6)
+    NX, NY, _ = wl.mesh.shape
+    return I + NX * (J + NY * K)
+
+
+def test_amr_operator_equals_uniform_reference_operator():
+    wl, st, ao, gidx, rng = uniform_pair((1, 2, 1))
+    x_u = rng.standard_normal((wl.mesh.ncells, 3))
+    y_u = st.matvec(x_u)
+    y_a = ao.apply(x_u[gidx])
+    V = wl.mesh.dx ** 3
+    np.testing.assert_allclose(y_a, V * y_u[gidx], rtol=1e-11, atol=1e-13)
+
+
+def test_amr_rhs_equals_uniform_reference_rhs():
+    wl, st, ao, gidx, rng = uniform_pair((2, 1, 1))
+    st.E_n[:] = 1e-2 * rng.standard_normal(st.E_n.shape)
+    ao.E_n[:] = st.E_n[gidx]
+    st.Bcen[:] = ao.Bcen[np.argsort(cell_map(wl))]
+    r_u = st.rhs()
+    r_a = np.zeros_like(ao.E_n)
+    OA.lib().orc_amr_rhs(OA.C.byref(ao.g), OA.p(ao.E_n), OA.p(ao.Bcen), OA.p(ao.cellJ),
+                         OA.p(ao.cellM), OA.p(r_a))
+    np.testing.assert_allclose(r_a, wl.mesh.dx ** 3 * r_u[gidx], rtol=1e-10, atol=1e-14)
+
+
+def test_amr_energy_conserved_two_levels():
+    m = amr.central_refined_mesh((4, 4, 4), lmax=1, frac=0.5)
+    wl = A.electron_proton_plasma("amr", 1, 1, 1, 8, 3)
+    ic = amr.amr_initial_condition(m, wl.species, 8, seed=3)
+    x = m.block_origins()[ic["block"]] + ic["u"].astype(np.float64) * m.block_dx()[ic["block"]][:, None]
+    ao = OA.AmrOracle(m, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64), ic["spec"])
+    np.testing.assert_array_equal(ao.block, ic["block"])
+    ao.Bcen[:] = np.array(wl.b0)
+    ao.c2n()
+    e0 = ao.deposit()
+    tot0 = e0 + ao.wave_energy()
+    for _ in range(3):
+        it, diag = ao.step(tol=1e-12, maxit=600)
+        assert it > 0
+        drift = abs(diag[0] + diag[1] - tot0) / tot0
+        assert drift < 1e-8, drift
