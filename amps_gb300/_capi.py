@@ -73,6 +73,9 @@ SIGNATURES = {
     "amps_amr_nested_leaves": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_double, P, C.c_int]),
     "amps_gpu_create": (C.c_int, [C.POINTER(Config), C.POINTER(P)]),
+    "amps_gpu_create_amr": (C.c_int, [C.POINTER(Config), P, C.POINTER(P)]),
+    "amps_gpu_mesh_sizes": (C.c_int, [P, LL, LL, LL]),
+    "amps_gpu_export_cell_moments": (C.c_int, [P, D, D]),
     "amps_gpu_destroy": (C.c_int, [P]),
     "amps_gpu_last_error": (C.c_char_p, [P]),
     "amps_gpu_get_stream": (C.c_int, [P, C.POINTER(P)]),

@@ -109,30 +109,80 @@ def sphere_refined_mesh(nb0, lmax, radius=0.2, dx0=1.0):
     return AmrMesh(nb0, lmax, nested_leaves(nb0, lmax, 1, radius), dx0)
 
 
-def amr_initial_condition(mesh, species, ppc_base, seed=100):
+def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1):
     """Uniform-density Maxwellian plasma on an AMR mesh: ppc_base particles per
     species per level-0 cell volume (so a cell at level L holds ppc_base/8^L),
     positions uniform within each cell, co-located species, reference LCG
     stream split per block.  Returns u (FP32 block-local cell units), v, spec,
-    block, all FP32-representable."""
+    block, all FP32-representable.  Blocks are generated on nthreads host
+    threads (the result does not depend on it)."""
     ns = len(species)
     vth = np.array([s.vth for s in species], np.float64)
     lib = _capi.load()
-    us, vs, ss, bs = [], [], [], []
-    for b in range(mesh.nblocks):
+    counts = [lib.amps_ic_count(1, 1, 1, max(1, ppc_base // (8 ** int(mesh.level[b]))), ns)
+              for b in range(mesh.nblocks)]
+    off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    n = int(off[-1])
+    u = np.empty((n, 3), np.float32)
+    v = np.empty((n, 3), np.float32)
+    sp = np.empty(n, np.uint8)
+    bl = np.empty(n, np.int32)
+    scratch = np.empty(n, np.int32)
+
+    def one(b):
         L = int(mesh.level[b])
         ppc = max(1, ppc_base // (8 ** L))
-        n = lib.amps_ic_count(1, 1, 1, ppc, ns)
-        u = np.empty((n, 3), np.float32)
-        v = np.empty((n, 3), np.float32)
-        sp = np.empty(n, np.uint8)
-        bl = np.empty(n, np.int32)
+        a, e = int(off[b]), int(off[b + 1])
         st = lib.amps_ic_maxwellian(1, 1, 1, ppc, ns, ptr(vth, C.c_double),
                                     (seed * 7919 + 104729 * (b + 1)) & 0x7FFFFFFF or 1, 1,
-                                    ptr(u, C.c_float), ptr(v, C.c_float), ptr(sp, C.c_uint8),
-                                    ptr(bl, C.c_int32))
+                                    ptr(u[a:e], C.c_float), ptr(v[a:e], C.c_float),
+                                    ptr(sp[a:e], C.c_uint8), ptr(scratch[a:e], C.c_int32))
         if st != 0:
             raise AmpsGpuError(st, "amps_ic_maxwellian")
-        us.append(u); vs.append(v); ss.append(sp); bs.append(np.full(n, b, np.int32))
-    return {"u": np.concatenate(us), "v": np.concatenate(vs), "spec": np.concatenate(ss),
-            "block": np.concatenate(bs)}
+        bl[a:e] = b
+
+    if nthreads > 1:
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=nthreads) as ex:
+            list(ex.map(one, range(mesh.nblocks)))
+    else:
+        for b in range(mesh.nblocks):
+            one(b)
+    return {"u": u, "v": v, "spec": sp, "block": bl}
+
+
+def amr_initial_fields(mesh, b0):
+    """E = 0, B = b0 on every cell and corner (mesh numbering)."""
+    nc, ncell = mesh.ncorners, mesh.ncells
+    bc = np.tile(np.asarray(b0, np.float64), (nc, 1))
+    return {"E_n": np.zeros((nc, 3)), "E_half": np.zeros((nc, 3)),
+            "B_center": np.tile(np.asarray(b0, np.float64), (ncell, 1)),
+            "B_corner_prev": bc, "B_corner_cur": bc.copy()}
+
+
+class AmrWorkload:
+    """Electron-proton plasma of the uniform workloads on an AMR mesh: the mesh
+    recipe (level-0 blocks, levels, refined region) and ppc_base particles per
+    species per level-0 cell volume."""
+
+    def __init__(self, name, nb0, lmax, mode, frac, ppc_base, steps=10):
+        from .ecsim import electron_proton_plasma
+        self.name = name
+        self.nb0, self.lmax, self.mode, self.frac = tuple(nb0), lmax, mode, frac
+        self.ppc = ppc_base
+        # species, dt, theta, b0 and tolerance: the uniform plasma (dx0 = 1)
+        self.plasma = electron_proton_plasma(name, 1, 1, 1, ppc_base, steps)
+        self.species, self.dt, self.theta = self.plasma.species, self.plasma.dt, self.plasma.theta
+        self.b0, self.tol = self.plasma.b0, self.plasma.tol
+
+    def mesh(self):
+        return AmrMesh(self.nb0, self.lmax, nested_leaves(self.nb0, self.lmax, self.mode, self.frac))
+
+
+AMR_WORKLOADS = {
+    # 64^3 base cells in 8^3 blocks, central 1/8 of the volume refined 2x,
+    # 128 particles per species per base cell (67,108,864 particles)
+    "amr_64c_128ppc": lambda: AmrWorkload("amr_64c_128ppc", (8, 8, 8), 1, 0, 0.5, 128),
+    # the same recipe at 32^3 base cells and 16 ppc (small case: tests, profiles)
+    "amr_32c_16ppc": lambda: AmrWorkload("amr_32c_16ppc", (4, 4, 4), 1, 0, 0.5, 16),
+}

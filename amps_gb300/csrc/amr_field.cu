@@ -1,0 +1,464 @@
+// ECSIM field kernels on block-structured AMR meshes (FP64), and the AMR
+// variants of the particle import/export and stencil packing.
+//
+// The operator is assembled per cell in weak form (each term times the cell
+// volume V): identity/8, (theta c dt)^2 C^T C with C the face-average curl of
+// UpdateB (pic_field_solver_ecsim.cpp:5160-5711) whose transpose is the curl B
+// of the RHS supports (src/pic/ecsim/get_stencil.cpp:1500-1599), and
+// 4 pi theta dt M from the per-cell mass-matrix partials of ProcessCell
+// (:1882-2438).  Corners of fine blocks that lie on a coarser block's face or
+// edge off its corner lattice are hanging: they take the interpolation of the
+// coarse corners (P), contributions to them are scattered to the parents (P^T),
+// and their rows read x_h - (P x)_h = 0.  On a uniform mesh this is the
+// reference operator times V.  One thread per cell, FP64 atomics for the
+// scatter to the (up to 8) cells sharing a corner.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "deposit_core.cuh"
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+__constant__ int c_off[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+struct Hang {
+  const int* hs;
+  const int* hp;
+  const double* hw;
+};
+
+// value of corner c of a component-major field (component d), P applied,
+// optionally scaled by a diagonal (right preconditioner)
+__device__ __forceinline__ double cval(const double* __restrict__ F, const double* __restrict__ dinv,
+                                       long long nvc, int c, int d, const Hang& h) {
+  const int s = h.hs[c], e = h.hs[c + 1];
+  if (s == e) return dinv ? dinv[d * nvc + c] * F[d * nvc + c] : F[d * nvc + c];
+  double v = 0.0;
+  for (int t = s; t < e; t++) {
+    const int p = h.hp[t];
+    v += h.hw[t] * (dinv ? dinv[d * nvc + p] * F[d * nvc + p] : F[d * nvc + p]);
+  }
+  return v;
+}
+
+// scatter out[8][3] to the cell's corners with P^T
+__device__ __forceinline__ void scatter(double* __restrict__ y, long long nvc, const int cid[8],
+                                        const double out[8][3], const Hang& h) {
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int cc = cid[c], s = h.hs[cc], e = h.hs[cc + 1];
+    if (s == e) {
+#pragma unroll
+      for (int d = 0; d < 3; d++) atomicAdd(y + d * nvc + cc, out[c][d]);
+    } else {
+      for (int t = s; t < e; t++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) atomicAdd(y + d * nvc + h.hp[t], h.hw[t] * out[c][d]);
+    }
+  }
+}
+
+__device__ __forceinline__ void cell_curl(const double e[8][3], double dx, double cu[3]) {
+  double a = 0, b = 0, c = 0, d = 0, f = 0, g = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const double sx = c_off[k][0] ? 1.0 : -1.0, sy = c_off[k][1] ? 1.0 : -1.0,
+                 sz = c_off[k][2] ? 1.0 : -1.0;
+    a += sy * e[k][2]; b += sz * e[k][1];
+    c += sz * e[k][0]; d += sx * e[k][2];
+    f += sx * e[k][1]; g += sy * e[k][0];
+  }
+  const double q = 0.25 / dx;
+  cu[0] = q * (a - b);
+  cu[1] = q * (c - d);
+  cu[2] = q * (f - g);
+}
+
+__device__ __forceinline__ void cell_curl_t(const double y[3], double s, double out[8][3]) {
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const double sx = c_off[k][0] ? 1.0 : -1.0, sy = c_off[k][1] ? 1.0 : -1.0,
+                 sz = c_off[k][2] ? 1.0 : -1.0;
+    out[k][0] += s * (sz * y[1] - sy * y[2]);
+    out[k][1] += s * (sx * y[2] - sz * y[0]);
+    out[k][2] += s * (sy * y[0] - sx * y[1]);
+  }
+}
+
+struct ApplyArgs {
+  long long ncell, nvc;
+  const int* ctab;
+  Hang h;
+  const double* bdx;
+  const float* cellM;
+  const float* cellJ;
+  const double* x;     // input field (component-major)
+  const double* dinv;  // optional right preconditioner
+  const double* Bcen;  // RHS: centre B (component-major over cells)
+  double* y;
+  double th2dt2, f, thdt;
+  int with_identity, with_curl, with_mass, rhs_mode;
+};
+
+// y += cell contributions.  rhs_mode: y = -(curl-curl + M) x + theta dt C^T B - f J
+__global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= a.ncell) return;
+  const int b = (int)(cell >> 9), l = (int)(cell & 511);
+  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+  const double dx = a.bdx[b], V = dx * dx * dx;
+  int cid[8];
+  double e[8][3], out[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    cid[c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      e[c][d] = cval(a.x, a.dinv, a.nvc, cid[c], d, a.h);
+      out[c][d] = 0.0;
+    }
+  }
+  const double sg = a.rhs_mode ? -1.0 : 1.0;
+  if (a.with_identity)
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) out[c][d] += 0.125 * V * e[c][d];
+  if (a.with_curl) {
+    double cu[3];
+    cell_curl(e, dx, cu);
+    cell_curl_t(cu, sg * a.th2dt2 * V * 0.25 / dx, out);
+  }
+  if (a.with_mass) {
+    const float* mm = a.cellM + cell * 324;
+    const double fv = sg * a.f * V;
+#pragma unroll 1
+    for (int c1 = 0; c1 < 8; c1++)
+#pragma unroll 1
+      for (int c2 = 0; c2 <= c1; c2++) {
+        const float* blk = mm + (c1 * (c1 + 1) / 2 + c2) * 9;
+        double m9[9];
+#pragma unroll
+        for (int t = 0; t < 9; t++) m9[t] = fv * widen(blk[t]);
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+          out[c1][p] += m9[3 * p] * e[c2][0] + m9[3 * p + 1] * e[c2][1] + m9[3 * p + 2] * e[c2][2];
+          if (c1 != c2)
+            out[c2][p] += m9[3 * p] * e[c1][0] + m9[3 * p + 1] * e[c1][1] + m9[3 * p + 2] * e[c1][2];
+        }
+      }
+  }
+  if (a.rhs_mode) {
+    const double B[3] = {a.Bcen[cell], a.Bcen[a.ncell + cell], a.Bcen[2 * a.ncell + cell]};
+    cell_curl_t(B, a.thdt * V * 0.25 / dx, out);
+    const float* jj = a.cellJ + cell * 24;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) out[c][d] -= a.f * widen(jj[3 * c + d]);
+  }
+  scatter(a.y, a.nvc, cid, out, a.h);
+}
+
+// hanging rows: y_h = x_h - (P x)_h (operator) or 0 (rhs)
+__global__ void __launch_bounds__(256) k_amr_constraint(long long nvc, Hang h,
+                                                        const double* __restrict__ x,
+                                                        const double* __restrict__ dinv,
+                                                        double* __restrict__ y, int rhs_mode) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+  const int s = h.hs[c], e = h.hs[c + 1];
+  if (s == e) return;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (rhs_mode) {
+      y[d * nvc + c] = 0.0;
+    } else {
+      double pv = 0.0;
+      for (int t = s; t < e; t++) {
+        const int p = h.hp[t];
+        pv += h.hw[t] * (dinv ? dinv[d * nvc + p] : 1.0) * x[d * nvc + p];
+      }
+      y[d * nvc + c] = (dinv ? dinv[d * nvc + c] : 1.0) * x[d * nvc + c] - pv;
+    }
+  }
+}
+
+// Jacobi diagonal (free corners: sum over their cells of the cell diagonal)
+__global__ void __launch_bounds__(256) k_amr_diag(long long ncell, long long nvc, const int* ctab,
+                                                  Hang h, const double* bdx, const float* cellM,
+                                                  double th2dt2, double f, double* diag) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncell) return;
+  const int b = (int)(cell >> 9), l = (int)(cell & 511);
+  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+  const double dx = bdx[b], V = dx * dx * dx;
+  const float* mm = cellM + cell * 324;
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int cc = ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+    if (h.hs[cc + 1] > h.hs[cc]) continue;
+    const float* blk = mm + (c * (c + 1) / 2 + c) * 9;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      atomicAdd(diag + d * nvc + cc,
+                V * (0.125 + th2dt2 / (8.0 * dx * dx) + f * widen(blk[4 * d])));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_amr_invert_diag(long long nvc, Hang h, double* diag) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+  const bool hang = h.hs[c + 1] > h.hs[c];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double v = diag[d * nvc + c];
+    diag[d * nvc + c] = (hang || v == 0.0) ? 1.0 : 1.0 / v;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_amr_update_b(long long ncell, long long nvc,
+                                                      const int* ctab, Hang h, const double* bdx,
+                                                      const double* Eh, const double* Bn,
+                                                      double* Bnew, double dt) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncell) return;
+  const int b = (int)(cell >> 9), l = (int)(cell & 511);
+  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+  double e[8][3];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int cc = ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+#pragma unroll
+    for (int d = 0; d < 3; d++) e[c][d] = cval(Eh, nullptr, nvc, cc, d, h);
+  }
+  double cu[3];
+  cell_curl(e, bdx[b], cu);
+#pragma unroll
+  for (int d = 0; d < 3; d++) Bnew[d * ncell + cell] = Bn[d * ncell + cell] - dt * cu[d];
+}
+
+// C2N: accumulate V*B and V on the corners (P^T for hanging is not used: their
+// value is re-interpolated afterwards)
+__global__ void __launch_bounds__(256) k_amr_c2n_acc(long long ncell, long long nvc,
+                                                     const int* ctab, const double* bdx,
+                                                     const double* Bcen, double* acc,
+                                                     double* wsum) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncell) return;
+  const int b = (int)(cell >> 9), l = (int)(cell & 511);
+  const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+  const double dx = bdx[b], V = dx * dx * dx;
+  const double B[3] = {Bcen[cell], Bcen[ncell + cell], Bcen[2 * ncell + cell]};
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int cc = ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+    atomicAdd(wsum + cc, V);
+#pragma unroll
+    for (int d = 0; d < 3; d++) atomicAdd(acc + d * nvc + cc, V * B[d]);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_amr_c2n_div(long long nvc, const double* wsum,
+                                                     double* acc) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+  const double w = wsum[c];
+#pragma unroll
+  for (int d = 0; d < 3; d++) acc[d * nvc + c] = w > 0.0 ? acc[d * nvc + c] / w : 0.0;
+}
+
+// hanging corners of a field take the interpolation of their (free) parents
+__global__ void __launch_bounds__(256) k_amr_fix_hanging(long long nvc, Hang h, double* F) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+  const int s = h.hs[c], e = h.hs[c + 1];
+  if (s == e) return;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    double v = 0.0;
+    for (int t = s; t < e; t++) v += h.hw[t] * F[d * nvc + h.hp[t]];
+    F[d * nvc + c] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_amr_update_e(long long nvc, const double* Eh, double* En,
+                                                      double theta) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    En[d * nvc + c] = (Eh[d * nvc + c] - (1.0 - theta) * En[d * nvc + c]) / theta;
+}
+
+// wave energy sum_cells V (sum_corners |E|^2/8 + |B|^2) / (8 pi)
+__global__ void __launch_bounds__(256) k_amr_wave_energy(long long ncell, long long nvc,
+                                                         const int* ctab, const double* bdx,
+                                                         const double* En, const double* Bcen,
+                                                         double* energy) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double en = 0.0;
+  if (cell < ncell) {
+    const int b = (int)(cell >> 9), l = (int)(cell & 511);
+    const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+    const double dx = bdx[b], V = dx * dx * dx;
+    double e2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int cc = ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const double v = En[d * nvc + cc];
+        e2 += v * v;
+      }
+    }
+    double b2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const double v = Bcen[d * ncell + cell];
+      b2 += v * v;
+    }
+    en = (0.125 * e2 + b2) * V * 0.125 / kPi;
+  }
+  __shared__ double s[8];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) en += __shfl_xor_sync(0xffffffffu, en, o);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = en;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s[w];
+    atomicAdd(energy, t);
+  }
+}
+
+__global__ void k_amr_pack(long long nvc, const int* ctab, Hang h, const double* Eh,
+                           const double* Bprev, const double* Bcur, float* sp, float* sd) {
+  const int b = blockIdx.x;
+  for (int s = threadIdx.x; s < AMPS_SC; s += blockDim.x) {
+    const int cc = ctab[b * 729 + s];
+    float4* op = reinterpret_cast<float4*>(sp + ((size_t)b * AMPS_SC + s) * AMPS_PUSH_STRIDE);
+    op[0] = make_float4((float)cval(Eh, nullptr, nvc, cc, 0, h), (float)cval(Eh, nullptr, nvc, cc, 1, h),
+                        (float)cval(Eh, nullptr, nvc, cc, 2, h), (float)cval(Bprev, nullptr, nvc, cc, 0, h));
+    op[1] = make_float4((float)cval(Bprev, nullptr, nvc, cc, 1, h),
+                        (float)cval(Bprev, nullptr, nvc, cc, 2, h), 0.f, 0.f);
+    reinterpret_cast<float4*>(sd)[(size_t)b * AMPS_SC + s] =
+        make_float4((float)cval(Bcur, nullptr, nvc, cc, 0, h), (float)cval(Bcur, nullptr, nvc, cc, 1, h),
+                    (float)cval(Bcur, nullptr, nvc, cc, 2, h), 0.f);
+  }
+}
+
+Hang hang_of(const amps_gpu_ctx* c) { return Hang{c->d_hs, c->d_hp, c->d_hw}; }
+unsigned g1(long long n) { return (unsigned)((n + 255) / 256); }
+
+}  // namespace
+
+// ============================================================================
+cudaError_t launch_amr_pack(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
+                            const double* Bcur) {
+  TimedLaunch t(c, "pack_stencils");
+  k_amr_pack<<<c->nb, 256, 0, c->stream>>>(c->nvc, c->d_ctab, hang_of(c), Eh, Bprev, Bcur,
+                                            c->d_stencil_push, c->d_stencil_dep);
+  return cudaGetLastError();
+}
+
+static ApplyArgs apply_args(amps_gpu_ctx* c) {
+  ApplyArgs a{};
+  a.ncell = c->ncor;
+  a.nvc = c->nvc;
+  a.ctab = c->d_ctab;
+  a.h = hang_of(c);
+  a.bdx = c->d_bdx;
+  a.cellM = c->d_cellM;
+  a.cellJ = c->d_cellJ;
+  const double th = c->cfg.theta, dt = c->cfg.dt;
+  a.th2dt2 = th * th * dt * dt;
+  a.f = 4.0 * kPi * dt * th;
+  a.thdt = th * dt;
+  return a;
+}
+
+cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y) {
+  cudaError_t e = cudaMemsetAsync(y, 0, sizeof(double) * 3 * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  ApplyArgs a = apply_args(c);
+  a.x = x;
+  a.dinv = dinv;
+  a.y = y;
+  a.with_identity = a.with_curl = a.with_mass = 1;
+  a.rhs_mode = 0;
+  TimedLaunch t(c, "matvec", 2);
+  k_amr_cell_op<<<g1(c->ncor), 256, 0, c->stream>>>(a);
+  k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, x, dinv, y, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_rhs(amps_gpu_ctx* c) {
+  cudaError_t e = cudaMemsetAsync(c->d_rhs, 0, sizeof(double) * 3 * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  ApplyArgs a = apply_args(c);
+  a.x = c->d_En;
+  a.dinv = nullptr;
+  a.Bcen = c->d_Bc;
+  a.y = c->d_rhs;
+  a.with_identity = 0;
+  a.with_curl = a.with_mass = 1;
+  a.rhs_mode = 1;
+  TimedLaunch t(c, "rhs", 2);
+  k_amr_cell_op<<<g1(c->ncor), 256, 0, c->stream>>>(a);
+  k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, nullptr, nullptr, c->d_rhs, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_jacobi(amps_gpu_ctx* c) {
+  cudaError_t e = cudaMemsetAsync(c->d_dinv, 0, sizeof(double) * 3 * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  ApplyArgs a = apply_args(c);
+  TimedLaunch t(c, "jacobi", 2);
+  k_amr_diag<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, a.h, c->d_bdx,
+                                                  c->d_cellM, a.th2dt2, a.f, c->d_dinv);
+  k_amr_invert_diag<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_dinv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_update_b(amps_gpu_ctx* c) {
+  TimedLaunch t(c, "update_b");
+  k_amr_update_b<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, hang_of(c),
+                                                      c->d_bdx, c->d_Eh, c->d_Bc, c->d_Bc2,
+                                                      c->cfg.dt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor) {
+  // the GMRES work vector holds the weights (3*nvc >= nvc doubles)
+  double* wsum = c->d_w;
+  cudaError_t e = cudaMemsetAsync(Bcor, 0, sizeof(double) * 3 * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(wsum, 0, sizeof(double) * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  TimedLaunch t(c, "c2n", 3);
+  k_amr_c2n_acc<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, c->d_bdx, Bcen,
+                                                     Bcor, wsum);
+  k_amr_c2n_div<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, wsum, Bcor);
+  k_amr_fix_hanging<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, hang_of(c), Bcor);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_update_e(amps_gpu_ctx* c) {
+  cudaError_t e = cudaMemsetAsync(c->d_energy + 1, 0, sizeof(double), c->stream);
+  if (e != cudaSuccess) return e;
+  TimedLaunch t(c, "update_e", 3);
+  k_amr_update_e<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, c->d_Eh, c->d_En, c->cfg.theta);
+  k_amr_fix_hanging<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, hang_of(c), c->d_En);
+  k_amr_wave_energy<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, c->d_bdx,
+                                                         c->d_En, c->d_Bc, c->d_energy + 1);
+  return cudaGetLastError();
+}
+
+// E^{n+theta} = E^n + dE with hanging corners re-interpolated
+cudaError_t launch_amr_fix_hanging(amps_gpu_ctx* c, double* F) {
+  k_amr_fix_hanging<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, hang_of(c), F);
+  return cudaGetLastError();
+}

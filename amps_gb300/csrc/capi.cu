@@ -7,6 +7,7 @@
 #include <cstring>
 #include <string>
 
+#include "amr_mesh.h"
 #include "common.cuh"
 
 cudaError_t launch_add(amps_gpu_ctx* c, const double* a, const double* b, double* o, long long n);
@@ -110,10 +111,19 @@ std::vector<long long> host_perm(const amps_gpu_config& g, long long ncor) {
   return p;
 }
 
-amps_gpu_status upload_vec3(amps_gpu_ctx* c, const double* host, double* dev) {
+// Host order: uniform meshes use the global periodic numbering I + NX (J + NY K)
+// for corners and cells; AMR meshes use the unique-corner numbering of the mesh
+// builder for corners and block*512 + i + 8j + 64k for cells.
+std::vector<long long> field_perm(amps_gpu_ctx* c, long long n) {
+  if (!c->amr) return host_perm(c->cfg, n);
+  std::vector<long long> p((size_t)n);
+  for (long long h = 0; h < n; h++) p[(size_t)h] = h;
+  return p;
+}
+
+amps_gpu_status upload_vec3(amps_gpu_ctx* c, const double* host, double* dev, long long n) {
   if (!host) return AMPS_GPU_OK;
-  const long long n = c->ncor;
-  auto perm = host_perm(c->cfg, n);
+  auto perm = field_perm(c, n);
   std::vector<double> tmp((size_t)(3 * n));
   for (long long h = 0; h < n; h++)
     for (int d = 0; d < 3; d++) tmp[(size_t)(d * n + perm[(size_t)h])] = host[3 * h + d];
@@ -121,10 +131,9 @@ amps_gpu_status upload_vec3(amps_gpu_ctx* c, const double* host, double* dev) {
                     "upload field");
 }
 
-amps_gpu_status download_vec3(amps_gpu_ctx* c, const double* dev, double* host) {
+amps_gpu_status download_vec3(amps_gpu_ctx* c, const double* dev, double* host, long long n) {
   if (!host) return AMPS_GPU_OK;
-  const long long n = c->ncor;
-  auto perm = host_perm(c->cfg, n);
+  auto perm = field_perm(c, n);
   std::vector<double> tmp((size_t)(3 * n));
   amps_gpu_status s = cuda_check(
       c, cudaMemcpy(tmp.data(), dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost), "download field");
@@ -235,42 +244,36 @@ amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_b
 }  // namespace
 
 // ===========================================================================
-extern "C" {
+namespace {
 
-amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) {
-  if (!cfg || !out) return AMPS_GPU_INVALID_ARG;
-  *out = nullptr;
-  if (cfg->nbx <= 0 || cfg->nby <= 0 || cfg->nbz <= 0 || cfg->nspec <= 0 ||
-      cfg->nspec > AMPS_GPU_MAX_SPECIES || cfg->dt <= 0.0 || cfg->theta <= 0.0 ||
-      cfg->particle_capacity < 0 || cfg->dx[0] <= 0 || cfg->dx[1] <= 0 || cfg->dx[2] <= 0)
+amps_gpu_status check_config(const amps_gpu_config* cfg) {
+  if (cfg->nspec <= 0 || cfg->nspec > AMPS_GPU_MAX_SPECIES || cfg->dt <= 0.0 ||
+      cfg->theta <= 0.0 || cfg->particle_capacity < 0)
     return AMPS_GPU_INVALID_ARG;
   for (int s = 0; s < cfg->nspec; s++)
     if (cfg->mass[s] <= 0.0) return AMPS_GPU_INVALID_ARG;
-  const long long nbl = (long long)cfg->nbx * cfg->nby * cfg->nbz;
-  const long long nc = nbl * 512;
-  // slot capacity: particles + 1/4 slack + 8 slack slots per cell
-  const long long slots = cfg->particle_capacity + cfg->particle_capacity / 4 + 8 * nc + 1024;
-  if (nc > (1LL << 28) || slots > (1LL << 31) - 1) return AMPS_GPU_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return AMPS_GPU_NO_DEVICE;
   if (cfg->device < 0 || cfg->device >= ndev) return AMPS_GPU_INVALID_ARG;
   if (cudaSetDevice(cfg->device) != cudaSuccess) return AMPS_GPU_CUDA_ERROR;
+  return AMPS_GPU_OK;
+}
 
-  amps_gpu_ctx* c = new amps_gpu_ctx();
-  c->cfg = *cfg;
-  c->nb = (int)nbl;
-  c->ncor = nc;
-  c->cap = cfg->particle_capacity;
-  c->slots = slots;
+// Allocations and initial state shared by uniform and AMR contexts (c->nb,
+// c->ncor, c->nvc, c->amr set by the caller).  Corner vectors hold 3*nvc
+// doubles, cell vectors 3*ncor; the 243-term corner mass matrix exists on
+// uniform meshes only (AMR solves read the per-cell partials).
+bool alloc_context(amps_gpu_ctx* c) {
+  const long long nc = c->ncor, nv = c->nvc, slots = c->slots;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   bool ok = e == cudaSuccess;
-  ok = ok && !dalloc(&c->d_nbr, (size_t)c->nb * 27);
-  ok = ok && !dalloc(&c->d_En, 3 * nc) && !dalloc(&c->d_Eh, 3 * nc) && !dalloc(&c->d_Bc, 3 * nc) &&
-       !dalloc(&c->d_Bc2, 3 * nc) && !dalloc(&c->d_Bcor_prev, 3 * nc) &&
-       !dalloc(&c->d_Bcor_cur, 3 * nc) && !dalloc(&c->d_J, 3 * nc) && !dalloc(&c->d_M, 243 * nc);
-  ok = ok && !dalloc(&c->d_rhs, 3 * nc) && !dalloc(&c->d_x, 3 * nc) &&
-       !dalloc(&c->d_V, (size_t)(c->restart + 1) * 3 * nc) && !dalloc(&c->d_w, 3 * nc) &&
-       !dalloc(&c->d_dinv, 3 * nc) && !dalloc(&c->d_red, 12288);
+  ok = ok && !dalloc(&c->d_En, 3 * nv) && !dalloc(&c->d_Eh, 3 * nv) && !dalloc(&c->d_Bc, 3 * nc) &&
+       !dalloc(&c->d_Bc2, 3 * nc) && !dalloc(&c->d_Bcor_prev, 3 * nv) &&
+       !dalloc(&c->d_Bcor_cur, 3 * nv);
+  if (!c->amr) ok = ok && !dalloc(&c->d_J, 3 * nc) && !dalloc(&c->d_M, 243 * nc);
+  ok = ok && !dalloc(&c->d_rhs, 3 * nv) && !dalloc(&c->d_x, 3 * nv) &&
+       !dalloc(&c->d_V, (size_t)(c->restart + 1) * 3 * nv) && !dalloc(&c->d_w, 3 * nv) &&
+       !dalloc(&c->d_dinv, 3 * nv) && !dalloc(&c->d_red, 12288);
   ok = ok && cudaMallocHost(&c->h_red, 128 * sizeof(double)) == cudaSuccess;
   ok = ok && !dalloc(&c->d_stencil_push, (size_t)c->nb * AMPS_SC * AMPS_PUSH_STRIDE) &&
        !dalloc(&c->d_stencil_dep, (size_t)c->nb * AMPS_SC * AMPS_DEP_STRIDE);
@@ -278,7 +281,7 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
     for (int q = 0; q < 3; q++)
       ok = ok && !dalloc(&c->d_u[bsel][q], slots) && !dalloc(&c->d_v[bsel][q], slots);
     ok = ok && !dalloc(&c->d_sp[bsel], slots) && !dalloc(&c->d_wc[bsel], slots);
-    if (cfg->track_ids) ok = ok && !dalloc(&c->d_id[bsel], slots);
+    if (c->cfg.track_ids) ok = ok && !dalloc(&c->d_id[bsel], slots);
   }
   ok = ok && !dalloc(&c->d_key, slots) && !dalloc(&c->d_rank, slots) &&
        !dalloc(&c->d_base, nc + 1) && !dalloc(&c->d_cnt, nc) && !dalloc(&c->d_arr, nc) &&
@@ -290,6 +293,68 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
   ok = ok && cudaMallocHost(&c->h_energy, 4 * sizeof(double)) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
+    return false;
+  }
+  double* zero_v[] = {c->d_En, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur};
+  for (double* p : zero_v) ok = ok && cudaMemset(p, 0, sizeof(double) * 3 * nv) == cudaSuccess;
+  ok = ok && cudaMemset(c->d_Bc, 0, sizeof(double) * 3 * nc) == cudaSuccess;
+  if (!c->amr)
+    ok = ok && cudaMemset(c->d_J, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
+         cudaMemset(c->d_M, 0, sizeof(double) * 243 * nc) == cudaSuccess;
+  // cell partials start at zero so an AMR solve before any deposit is defined
+  ok = ok && cudaMemset(c->d_cellM, 0, sizeof(float) * 324 * nc) == cudaSuccess &&
+       cudaMemset(c->d_cellJ, 0, sizeof(float) * 24 * nc) == cudaSuccess;
+  // empty layout: every cell has 8 slack slots
+  {
+    std::vector<int> base((size_t)nc + 1);
+    for (long long i = 0; i <= nc; i++) base[(size_t)i] = (int)(8 * i);
+    ok = ok && cudaMemcpy(c->d_base, base.data(), sizeof(int) * (nc + 1), cudaMemcpyHostToDevice) ==
+                   cudaSuccess;
+  }
+  ok = ok && cudaMemset(c->d_cnt, 0, sizeof(int) * nc) == cudaSuccess &&
+       cudaMemset(c->d_arr, 0, sizeof(int) * nc) == cudaSuccess &&
+       cudaMemset(c->d_stay, 0, sizeof(int) * nc) == cudaSuccess &&
+       cudaMemset(c->d_sp[0], 0xFF, (size_t)slots) == cudaSuccess &&
+       cudaMemset(c->d_sp[1], 0xFF, (size_t)slots) == cudaSuccess &&
+       cudaMemset(c->d_flags, 0, sizeof(unsigned long long) * 8) == cudaSuccess;
+  return ok;
+}
+
+// slot capacity: particles + 1/4 slack + 8 slack slots per cell
+long long slot_count(long long cap, long long ncell) { return cap + cap / 4 + 8 * ncell + 1024; }
+
+template <class T>
+bool upload(T** d, const std::vector<T>& h) {
+  if (dalloc(d, h.size())) return false;
+  return h.empty() ||
+         cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" {
+
+amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) {
+  if (!cfg || !out) return AMPS_GPU_INVALID_ARG;
+  *out = nullptr;
+  if (cfg->nbx <= 0 || cfg->nby <= 0 || cfg->nbz <= 0 || cfg->dx[0] <= 0 || cfg->dx[1] <= 0 ||
+      cfg->dx[2] <= 0)
+    return AMPS_GPU_INVALID_ARG;
+  const long long nbl = (long long)cfg->nbx * cfg->nby * cfg->nbz;
+  const long long nc = nbl * 512;
+  const long long slots = slot_count(cfg->particle_capacity, nc);
+  if (nc > (1LL << 28) || slots > (1LL << 31) - 1) return AMPS_GPU_INVALID_ARG;
+  amps_gpu_status cs = check_config(cfg);
+  if (cs) return cs;
+
+  amps_gpu_ctx* c = new amps_gpu_ctx();
+  c->cfg = *cfg;
+  c->nb = (int)nbl;
+  c->ncor = nc;
+  c->nvc = nc;
+  c->cap = cfg->particle_capacity;
+  c->slots = slots;
+  if (!alloc_context(c)) {
     amps_gpu_destroy(c);
     return AMPS_GPU_CUDA_ERROR;
   }
@@ -305,29 +370,88 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
           nbr[(size_t)b * 27 + nbr_slot(ox, oy, oz)] = X + cfg->nbx * (Y + cfg->nby * Z);
         }
   }
-  ok = cudaMemcpy(c->d_nbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice) ==
-       cudaSuccess;
-  double* zero_d[] = {c->d_En, c->d_Eh, c->d_Bc, c->d_Bcor_prev, c->d_Bcor_cur, c->d_J};
-  for (double* p : zero_d) ok = ok && cudaMemset(p, 0, sizeof(double) * 3 * nc) == cudaSuccess;
-  ok = ok && cudaMemset(c->d_M, 0, sizeof(double) * 243 * nc) == cudaSuccess;
-  // empty layout: every cell has 8 slack slots
-  {
-    std::vector<int> base((size_t)nc + 1);
-    for (long long i = 0; i <= nc; i++) base[(size_t)i] = (int)(8 * i);
-    ok = ok && cudaMemcpy(c->d_base, base.data(), sizeof(int) * (nc + 1), cudaMemcpyHostToDevice) ==
-                   cudaSuccess;
-  }
-  ok = ok && cudaMemset(c->d_cnt, 0, sizeof(int) * nc) == cudaSuccess &&
-       cudaMemset(c->d_arr, 0, sizeof(int) * nc) == cudaSuccess &&
-       cudaMemset(c->d_stay, 0, sizeof(int) * nc) == cudaSuccess &&
-       cudaMemset(c->d_sp[0], 0xFF, (size_t)slots) == cudaSuccess &&
-       cudaMemset(c->d_sp[1], 0xFF, (size_t)slots) == cudaSuccess &&
-       cudaMemset(c->d_flags, 0, sizeof(unsigned long long) * 8) == cudaSuccess;
-  if (!ok) {
+  if (!upload(&c->d_nbr, nbr)) {
     amps_gpu_destroy(c);
     return AMPS_GPU_CUDA_ERROR;
   }
   *out = c;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_mesh* m,
+                                    amps_gpu_ctx** out) {
+  if (!cfg || !m || !out) return AMPS_GPU_INVALID_ARG;
+  *out = nullptr;
+  const long long nbl = (long long)m->blocks.size();
+  const long long nc = nbl * 512;
+  const long long nv = (long long)m->hang_start.size() - 1;
+  const long long slots = slot_count(cfg->particle_capacity, nc);
+  if (nbl <= 0 || nv <= 0 || nc > (1LL << 28) || slots > (1LL << 31) - 1 ||
+      m->corner_tab.size() != (size_t)nbl * 729)
+    return AMPS_GPU_INVALID_ARG;
+  for (int d = 0; d < 3; d++)
+    if (m->nfine[d] <= 0 || m->nfine[d] % 8) return AMPS_GPU_INVALID_ARG;
+  amps_gpu_status cs = check_config(cfg);
+  if (cs) return cs;
+
+  amps_gpu_ctx* c = new amps_gpu_ctx();
+  c->cfg = *cfg;
+  // geometry comes from the mesh: level-0 blocks and cell size
+  c->cfg.nbx = m->nb0[0];
+  c->cfg.nby = m->nb0[1];
+  c->cfg.nbz = m->nb0[2];
+  for (int d = 0; d < 3; d++) {
+    c->cfg.x0[d] = m->x0[d];
+    c->cfg.dx[d] = m->dx0;
+  }
+  c->amr = true;
+  c->lmax = m->lmax;
+  c->dxf = m->dx0 / (double)(1 << m->lmax);
+  c->nb = (int)nbl;
+  c->ncor = nc;
+  c->nvc = nv;
+  c->cap = cfg->particle_capacity;
+  c->slots = slots;
+  bool ok = alloc_context(c);
+  std::vector<int> borg((size_t)nbl * 3), bscale((size_t)nbl);
+  std::vector<double> bdx((size_t)nbl);
+  std::vector<float> bdtdx((size_t)nbl), binvvol((size_t)nbl);
+  for (long long b = 0; b < nbl; b++) {
+    const amps_block_desc& d = m->blocks[(size_t)b];
+    borg[(size_t)(3 * b)] = d.ix;
+    borg[(size_t)(3 * b + 1)] = d.iy;
+    borg[(size_t)(3 * b + 2)] = d.iz;
+    bscale[(size_t)b] = 1 << (m->lmax - d.level);
+    bdx[(size_t)b] = m->dx0 / (double)(1 << d.level);
+    bdtdx[(size_t)b] = (float)(cfg->dt / bdx[(size_t)b]);
+    binvvol[(size_t)b] = (float)(1.0 / (bdx[(size_t)b] * bdx[(size_t)b] * bdx[(size_t)b]));
+  }
+  ok = ok && upload(&c->d_ctab, m->corner_tab) && upload(&c->d_hs, m->hang_start) &&
+       upload(&c->d_hp, m->hang_parent) && upload(&c->d_hw, m->hang_weight) &&
+       upload(&c->d_fine_map, m->fine_map) && upload(&c->d_borg, borg) &&
+       upload(&c->d_bscale, bscale) && upload(&c->d_bdx, bdx) && upload(&c->d_bdtdx, bdtdx) &&
+       upload(&c->d_binvvol, binvvol);
+  if (!ok) {
+    cudaGetLastError();
+    amps_gpu_destroy(c);
+    return AMPS_GPU_CUDA_ERROR;
+  }
+  for (int d = 0; d < 3; d++) c->amrdev.nfine[d] = m->nfine[d];
+  c->amrdev.fine_map = c->d_fine_map;
+  c->amrdev.borg = c->d_borg;
+  c->amrdev.bscale = c->d_bscale;
+  c->amrdev.bdtdx = c->d_bdtdx;
+  c->amrdev.binvvol = c->d_binvvol;
+  *out = c;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_mesh_sizes(const amps_gpu_ctx* c, long long* nblocks, long long* ncells,
+                                    long long* ncorners) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  if (nblocks) *nblocks = c->nb;
+  if (ncells) *ncells = c->ncor;
+  if (ncorners) *ncorners = c->nvc;
   return AMPS_GPU_OK;
 }
 
@@ -341,7 +465,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
-                  c->d_cellM, c->d_cellJ, c->d_energy};
+                  c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw,
+                  c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol};
   for (void* p : ptrs) cudaFree(p);
   for (int b = 0; b < 2; b++) {
     for (int q = 0; q < 3; q++) {
@@ -468,9 +593,11 @@ amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* c, const double* E_n, const
   cudaSetDevice(c->cfg.device);
   cudaStreamSynchronize(c->stream);
   amps_gpu_status s;
-  if ((s = upload_vec3(c, E_n, c->d_En)) || (s = upload_vec3(c, E_half, c->d_Eh)) ||
-      (s = upload_vec3(c, B_center, c->d_Bc)) || (s = upload_vec3(c, B_corner_prev, c->d_Bcor_prev)) ||
-      (s = upload_vec3(c, B_corner_cur, c->d_Bcor_cur)))
+  const long long nv = c->nvc, nc = c->ncor;
+  if ((s = upload_vec3(c, E_n, c->d_En, nv)) || (s = upload_vec3(c, E_half, c->d_Eh, nv)) ||
+      (s = upload_vec3(c, B_center, c->d_Bc, nc)) ||
+      (s = upload_vec3(c, B_corner_prev, c->d_Bcor_prev, nv)) ||
+      (s = upload_vec3(c, B_corner_cur, c->d_Bcor_cur, nv)))
     return s;
   return AMPS_GPU_OK;
 }
@@ -482,19 +609,23 @@ amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* c, double* E_n, double* E_h
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   if (s) return s;
-  if ((s = download_vec3(c, c->d_En, E_n)) || (s = download_vec3(c, c->d_Eh, E_half)) ||
-      (s = download_vec3(c, c->d_Bc, B_center)) ||
-      (s = download_vec3(c, c->d_Bcor_prev, B_corner_prev)) ||
-      (s = download_vec3(c, c->d_Bcor_cur, B_corner_cur)))
+  const long long nv = c->nvc, nc = c->ncor;
+  if ((s = download_vec3(c, c->d_En, E_n, nv)) || (s = download_vec3(c, c->d_Eh, E_half, nv)) ||
+      (s = download_vec3(c, c->d_Bc, B_center, nc)) ||
+      (s = download_vec3(c, c->d_Bcor_prev, B_corner_prev, nv)) ||
+      (s = download_vec3(c, c->d_Bcor_cur, B_corner_cur, nv)))
     return s;
   return AMPS_GPU_OK;
 }
 
 amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* c, const double* J, const double* M) {
   if (!c) return AMPS_GPU_INVALID_ARG;
+  if (c->amr)
+    return set_err(c, AMPS_GPU_INVALID_ARG,
+                   "import_moments: AMR contexts keep per-cell moments only");
   cudaSetDevice(c->cfg.device);
   cudaStreamSynchronize(c->stream);
-  amps_gpu_status s = upload_vec3(c, J, c->d_J);
+  amps_gpu_status s = upload_vec3(c, J, c->d_J, c->ncor);
   if (s) return s;
   if (M) {
     const long long n = c->ncor;
@@ -512,10 +643,13 @@ amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* c, const double* J, const 
 
 amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
   if (!c) return AMPS_GPU_INVALID_ARG;
+  if (c->amr)
+    return set_err(c, AMPS_GPU_INVALID_ARG,
+                   "export_moments: AMR contexts keep per-cell moments (export_cell_moments)");
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   if (s) return s;
-  s = download_vec3(c, c->d_J, J);
+  s = download_vec3(c, c->d_J, J, c->ncor);
   if (s) return s;
   if (M) {
     const long long n = c->ncor;
@@ -526,6 +660,29 @@ amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
     if (s) return s;
     for (long long h = 0; h < n; h++)
       for (int e = 0; e < 243; e++) M[243 * h + e] = tmp[(size_t)(e * n + perm[(size_t)h])];
+  }
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_export_cell_moments(amps_gpu_ctx* c, double* cellJ, double* cellM) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  if (s) return s;
+  const long long nc = c->ncor;
+  if (cellJ) {
+    std::vector<float> t((size_t)(24 * nc));
+    s = cuda_check(c, cudaMemcpy(t.data(), c->d_cellJ, sizeof(float) * t.size(), cudaMemcpyDeviceToHost),
+                   "download cellJ");
+    if (s) return s;
+    for (size_t i = 0; i < t.size(); i++) cellJ[i] = (double)t[i];
+  }
+  if (cellM) {
+    std::vector<float> t((size_t)(324 * nc));
+    s = cuda_check(c, cudaMemcpy(t.data(), c->d_cellM, sizeof(float) * t.size(), cudaMemcpyDeviceToHost),
+                   "download cellM");
+    if (s) return s;
+    for (size_t i = 0; i < t.size(); i++) cellM[i] = (double)t[i];
   }
   return AMPS_GPU_OK;
 }
@@ -579,7 +736,7 @@ amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* c, double tol, int maxit, int
   amps_gpu_status gs = gmres_solve(c, tol, maxit, precond, &st);
   if (gs != AMPS_GPU_OK && gs != AMPS_GPU_GMRES_NOT_CONVERGED) return gs;
   // ProcessFinalSolution: E^{n+theta} = E^n + dE
-  if ((s = cuda_check(c, launch_add(c, c->d_En, c->d_x, c->d_Eh, 3 * c->ncor), "E_half"))) return s;
+  if ((s = cuda_check(c, launch_add(c, c->d_En, c->d_x, c->d_Eh, 3 * c->nvc), "E_half"))) return s;
   if ((s = cuda_check(c, launch_update_b(c), "update_b"))) return s;
   std::swap(c->d_Bc, c->d_Bc2);
   std::swap(c->d_Bcor_prev, c->d_Bcor_cur);

@@ -31,15 +31,43 @@ struct KernelTimer {
   long long launches = 0;
 };
 
+// Device view of a block-structured AMR mesh for the particle kernels (null
+// pointers on uniform meshes).  Block origins are integers on the finest
+// lattice and cell sizes powers of two of the finest one, so a particle's
+// block-local FP32 offset converts between blocks with one rounding.
+struct AmrDev {
+  int nfine[3];            // finest cells per axis
+  const int* fine_map;     // finest block -> leaf block
+  const int* borg;         // nb*3 origins, finest-cell units
+  const int* bscale;       // nb: finest cells per cell (2^(lmax-level))
+  const float* bdtdx;      // nb: dt / dx
+  const float* binvvol;    // nb: 1 / dx^3
+};
+
 struct amps_gpu_ctx {
   amps_gpu_config cfg;
   int nb = 0;               // blocks
-  long long ncor = 0;       // owned corners == cells
+  long long ncor = 0;       // cells (= owned corners on a uniform mesh)
+  long long nvc = 0;        // corners carrying unknowns (= ncor uniform, unique corners on AMR)
   cudaStream_t stream = nullptr;
   std::string err;
 
   // mesh
-  int* d_nbr = nullptr;     // [nb*27] neighbour block, slot (di+1)+3(dj+1)+9(dk+1)
+  int* d_nbr = nullptr;     // [nb*27] neighbour block, slot (di+1)+3(dj+1)+9(dk+1) (uniform)
+  bool amr = false;
+  AmrDev amrdev{};          // particle-kernel view (AMR)
+  int lmax = 0;
+  double dxf = 0.0;         // finest cell size (AMR)
+  int* d_ctab = nullptr;    // [nb*729] block-local corner -> unique corner (AMR)
+  int* d_hs = nullptr;      // [nvc+1] hanging CSR start (AMR)
+  int* d_hp = nullptr;      // hanging parents
+  double* d_hw = nullptr;   // hanging weights
+  int* d_fine_map = nullptr;
+  int* d_borg = nullptr;      // nb*3 origins, finest-cell units
+  int* d_bscale = nullptr;    // nb finest cells per cell
+  double* d_bdx = nullptr;    // nb cell sizes
+  float* d_bdtdx = nullptr;   // dt/dx per block
+  float* d_binvvol = nullptr; // 1/dx^3 per block
 
   // fields (FP64, component-major)
   double* d_En = nullptr;
@@ -139,6 +167,18 @@ cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor);
 cudaError_t launch_update_e(amps_gpu_ctx* c);
 amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
                             amps_gpu_solve_stats* st);
+
+// ---- AMR field launchers (amr_field.cu); the launchers above dispatch to
+//      them when the context holds an AMR mesh ----
+cudaError_t launch_amr_pack(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
+                            const double* Bcur);
+cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
+cudaError_t launch_amr_rhs(amps_gpu_ctx* c);
+cudaError_t launch_amr_jacobi(amps_gpu_ctx* c);
+cudaError_t launch_amr_update_b(amps_gpu_ctx* c);
+cudaError_t launch_amr_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor);
+cudaError_t launch_amr_update_e(amps_gpu_ctx* c);
+cudaError_t launch_amr_fix_hanging(amps_gpu_ctx* c, double* F);
 
 // ---- device helpers ----
 __host__ __device__ inline int nbr_slot(int ox, int oy, int oz) {

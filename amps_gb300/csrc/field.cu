@@ -423,6 +423,7 @@ unsigned gridr(long long n) {
 
 // ============================================================================
 cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y) {
+  if (c->amr) return launch_amr_matvec(c, x, dinv, y);
   Taps T = make_taps(c->cfg, true);
   TimedLaunch t(c, "matvec");
   k_matvec<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, x, dinv, y, T);
@@ -430,6 +431,7 @@ cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, 
 }
 
 cudaError_t launch_rhs(amps_gpu_ctx* c) {
+  if (c->amr) return launch_amr_rhs(c);
   Taps T = make_taps(c->cfg, false);
   double c4[3];
   for (int d = 0; d < 3; d++) c4[d] = 0.25 * (c->cfg.dt / c->cfg.dx[d] * c->cfg.theta);
@@ -440,6 +442,7 @@ cudaError_t launch_rhs(amps_gpu_ctx* c) {
 }
 
 cudaError_t launch_jacobi_diag(amps_gpu_ctx* c) {
+  if (c->amr) return launch_amr_jacobi(c);
   Taps T = make_taps(c->cfg, true);
   TimedLaunch t(c, "jacobi");
   k_jacobi<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_M, c->d_dinv, T.K[0][0][0],
@@ -448,6 +451,7 @@ cudaError_t launch_jacobi_diag(amps_gpu_ctx* c) {
 }
 
 cudaError_t launch_update_b(amps_gpu_ctx* c) {
+  if (c->amr) return launch_amr_update_b(c);
   double c4[3];
   for (int d = 0; d < 3; d++) c4[d] = 0.25 * (c->cfg.dt / c->cfg.dx[d]);
   TimedLaunch t(c, "update_b");
@@ -457,12 +461,14 @@ cudaError_t launch_update_b(amps_gpu_ctx* c) {
 }
 
 cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor) {
+  if (c->amr) return launch_amr_c2n(c, Bcen, Bcor);
   TimedLaunch t(c, "c2n");
   k_c2n<<<grid1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, Bcen, Bcor);
   return cudaGetLastError();
 }
 
 cudaError_t launch_update_e(amps_gpu_ctx* c) {
+  if (c->amr) return launch_amr_update_e(c);
   const double vol = c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2];
   cudaError_t e = cudaMemsetAsync(c->d_energy + 1, 0, sizeof(double), c->stream);
   if (e != cudaSuccess) return e;
@@ -478,7 +484,7 @@ cudaError_t launch_update_e(amps_gpu_ctx* c) {
 // (kMaxV), h2 (kMaxV), nrm2 (1).
 amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
                             amps_gpu_solve_stats* st) {
-  const long long n = 3 * c->ncor;
+  const long long n = 3 * c->nvc;
   const int m = c->restart;
   double* partial = c->d_red;
   double* d_h1 = c->d_red + kRedBlocks * kMaxV;

@@ -79,6 +79,36 @@ __device__ __forceinline__ float clamp_below8(float u) {
   return u < 8.0f ? u : 7.99999952316284180f;  // nextafterf(8, 0)
 }
 
+// AMR destination of a particle that left block b: unwrapped block-local
+// offset un (cell units of b) -> position on the finest lattice (exact: the
+// scale is a power of two), leaf block from the fine map, offset in that
+// block's cell units (one rounding).  Periodic wrap moves the lattice position
+// by whole domain lengths, which enter as integers.
+__device__ __forceinline__ int amr_dest(const AmrDev& m, int b, float un[3], int ic[3]) {
+  const float fs = (float)__ldg(m.bscale + b);
+  int F[3], shift[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int g = __ldg(m.borg + 3 * b + d) + (int)floorf(un[d] * fs);
+    const int n = m.nfine[d];
+    int w = g % n;
+    if (w < 0) w += n;
+    F[d] = w;
+    shift[d] = g - w;
+  }
+  const int nb0 = m.nfine[0] >> 3, nb1 = m.nfine[1] >> 3;
+  const int bn = __ldg(m.fine_map + (F[0] >> 3) + nb0 * ((F[1] >> 3) + nb1 * (F[2] >> 3)));
+  const float inv = 1.0f / (float)__ldg(m.bscale + bn);  // exact: power of two
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int delta = __ldg(m.borg + 3 * bn + d) + shift[d] - __ldg(m.borg + 3 * b + d);
+    const float u = clamp_below8(fmaxf((un[d] * fs - (float)delta) * inv, 0.0f));
+    un[d] = u;
+    ic[d] = min((int)u, AMPS_NC - 1);
+  }
+  return bn;
+}
+
 // Warp-aggregated reservation: one atomic per distinct key among active lanes;
 // ranks inside the warp follow lane order.  Returns the reserved index.
 __device__ __forceinline__ int warp_reserve(bool active, int key, int* __restrict__ counter) {
@@ -132,7 +162,13 @@ struct StepArgs {
   float inv_vol;
   long long ovf_cap;
   SpeciesTab st;
+  AmrDev amr;     // fine_map == nullptr on uniform meshes
 };
+
+// 1/dx^3 of block b
+__device__ __forceinline__ float block_inv_vol(const StepArgs& a, int b) {
+  return a.amr.binvvol ? __ldg(a.amr.binvvol + b) : a.inv_vol;
+}
 
 // Lapenta2017 velocity update v' = 2 alpha (v + h E) - v (Eqs. D.3, D.8)
 __device__ __forceinline__ void lapenta(float h, const float E[3], const float B[3], float v[3]) {
@@ -149,7 +185,7 @@ __device__ __forceinline__ void lapenta(float h, const float E[3], const float B
   v[2] = 2.f * a2 - v[2];
 }
 
-template <bool DEP>
+template <bool DEP, bool AMR>
 __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
   float4* s_push = s_dyn;                         // 729 x 2 float4
@@ -170,6 +206,8 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
   double en = 0.0;
   unsigned long long n_far = 0, n_near = 0;
   const int j = wid;
+  const float inv_vol = block_inv_vol(a, b);
+  const float bdtdx = AMR ? __ldg(a.amr.bdtdx + b) : 0.0f;
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = a.base[cid], n0 = a.cnt[cid];
@@ -217,24 +255,41 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
               B[2] = fmaf(w, q1v.y, B[2]);
             }
         lapenta(a.st.qdt2m[s], E, B, v);
-        int o[3];
         bool far = false, nearf = false;
+        int nbk = b;
+        if (AMR) {
+          bool out = false;
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          float un = fmaf(v[d], a.dtdx[d], u[d]);
-          int od = (int)floorf(un * 0.125f);
-          if (od > 1 || od < -1) far = true;
-          od = max(-1, min(1, od));
-          un -= 8.0f * (float)od;
-          un = clamp_below8(fmaxf(un, 0.0f));
-          o[d] = od;
-          u[d] = un;
-          ic[d] = min((int)un, AMPS_NC - 1);
-          if (fabsf(un - rintf(un)) < 4.76837158203125e-7f) nearf = true;
+          for (int d = 0; d < 3; d++) {
+            u[d] = fmaf(v[d], bdtdx, u[d]);
+            const int od = (int)floorf(u[d] * 0.125f);
+            if (od > 1 || od < -1) far = true;
+            if (!(u[d] >= 0.0f && u[d] < 8.0f)) out = true;
+            ic[d] = min((int)u[d], AMPS_NC - 1);
+          }
+          if (out) nbk = amr_dest(a.amr, b, u, ic);
+#pragma unroll
+          for (int d = 0; d < 3; d++)
+            if (fabsf(u[d] - rintf(u[d])) < 4.76837158203125e-7f) nearf = true;
+        } else {
+          int o[3];
+#pragma unroll
+          for (int d = 0; d < 3; d++) {
+            float un = fmaf(v[d], a.dtdx[d], u[d]);
+            int od = (int)floorf(un * 0.125f);
+            if (od > 1 || od < -1) far = true;
+            od = max(-1, min(1, od));
+            un -= 8.0f * (float)od;
+            un = clamp_below8(fmaxf(un, 0.0f));
+            o[d] = od;
+            u[d] = un;
+            ic[d] = min((int)un, AMPS_NC - 1);
+            if (fabsf(un - rintf(un)) < 4.76837158203125e-7f) nearf = true;
+          }
+          if (o[0] | o[1] | o[2]) nbk = __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2]));
         }
         if (far) n_far++;
         if (nearf) n_near++;
-        const int nbk = (o[0] | o[1] | o[2]) ? __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2])) : b;
         key = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
       }
       const bool stays = act && key == (int)cid;
@@ -252,7 +307,7 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
         }
         if (DEP)
           en_cell += stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv,
-                             i, j, k, a.st, a.inv_vol);
+                             i, j, k, a.st, inv_vol);
       }
       // movers: slack of the destination cell, else the overflow list
       const bool mover = act && !stays;
@@ -321,6 +376,7 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
   lane_offsets(lane, offA, offB);
   double en = 0.0;
   const int j = wid;
+  const float inv_vol = block_inv_vol(a, b);
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = a.base[cid], cap = a.base[cid + 1] - b0, n0 = a.cnt[cid];
@@ -353,7 +409,7 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
           if (a.p.id) a.p.id[pd] = idv;
           if (DEP)
             en += stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
-                               wcv, i, j, k, a.st, a.inv_vol);
+                               wcv, i, j, k, a.st, inv_vol);
         }
         if (DEP) {
           __syncwarp();
@@ -395,6 +451,7 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
   lane_offsets(lane, offA, offB);
   double en = 0.0;
   const int j = wid;
+  const float inv_vol = block_inv_vol(a, b);
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = a.base[cid], n0 = a.cnt[cid];
@@ -406,7 +463,7 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
       if (q0 + lane < n0)
         en_cell += stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p],
                                 a.p.v[0][p], a.p.v[1][p], a.p.v[2][p], a.p.sp[p],
-                                a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, a.inv_vol);
+                                a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, inv_vol);
       __syncwarp();
       if (lane < 29) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
       __syncwarp();
@@ -667,6 +724,61 @@ __global__ void __launch_bounds__(256) k_import(ImportArgs a) {
   }
 }
 
+// AMR import: FP64 position -> leaf block through the finest-block map, cell
+// and FP32 offset in that block's cell units (same periodic rules).
+struct ImportAmrArgs {
+  const double* x; const double* v; const uint8_t* sp; const double* wc;
+  PBuf d;
+  int* key;
+  unsigned long long* flags;
+  long long n;
+  AmrDev m;
+  double x0[3], dxf;
+  int nspec;
+};
+
+__global__ void __launch_bounds__(256) k_import_amr(ImportAmrArgs a) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    double x[3];
+    int F[3];
+    for (int d = 0; d < 3; d++) {
+      const double L = a.m.nfine[d] * a.dxf;
+      double xx = a.x[3 * p + d];
+      if (xx < a.x0[d]) xx += L;
+      if (xx >= a.x0[d] + L) xx -= L;
+      if (xx >= a.x0[d] + L) xx = a.x0[d] + L - 1e-10 * a.dxf;
+      if (xx < a.x0[d]) xx = a.x0[d];
+      int f = (int)floor((xx - a.x0[d]) / a.dxf);
+      F[d] = min(max(f, 0), a.m.nfine[d] - 1);
+      x[d] = xx;
+    }
+    const int nb0 = a.m.nfine[0] >> 3, nb1 = a.m.nfine[1] >> 3;
+    const int blk = a.m.fine_map[(F[0] >> 3) + nb0 * ((F[1] >> 3) + nb1 * (F[2] >> 3))];
+    const double dx = a.m.bscale[blk] * a.dxf;
+    int ic[3];
+    for (int d = 0; d < 3; d++) {
+      const double o = a.x0[d] + a.m.borg[3 * blk + d] * a.dxf;
+      const double ud = (x[d] - o) / dx;
+      int ci = (int)ud;
+      if (ci >= AMPS_NC) ci = AMPS_NC - 1;
+      if (ci < 0) ci = 0;
+      float u = (float)ud;
+      if (u < (float)ci) u = (float)ci;
+      if (u >= (float)(ci + 1)) u = nextafterf((float)(ci + 1), 0.0f);
+      ic[d] = ci;
+      a.d.u[d][p] = u;
+      a.d.v[d][p] = (float)a.v[3 * p + d];
+    }
+    a.key[p] = blk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+    const int s = a.sp[p];
+    if (s >= a.nspec) atomicAdd(a.flags + 2, 1ull);
+    a.d.sp[p] = (uint8_t)s;
+    if (a.d.wc) a.d.wc[p] = a.wc ? (float)a.wc[p] : 1.0f;
+    if (a.d.id) a.d.id[p] = (uint32_t)p;
+  }
+}
+
 // Local import: interleaved FP32 offsets/velocities and block ids.
 __global__ void __launch_bounds__(256) k_import_local(long long n, const float* __restrict__ u,
                                                       const float* __restrict__ v,
@@ -703,13 +815,23 @@ __global__ void __launch_bounds__(256) k_export(long long ncells, const int* __r
                                                 int nby, double x00, double x01, double x02,
                                                 double dx0, double dx1, double dx2, double* x,
                                                 double* v, uint8_t* sp, int32_t* blk,
-                                                int32_t* cel, uint32_t* id) {
+                                                int32_t* cel, uint32_t* id, AmrDev m, double dxf) {
   const long long cid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (cid >= ncells) return;
   const int b = (int)(cid / AMPS_CPB), l = (int)(cid % AMPS_CPB);
-  const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
-  const double o0 = x00 + bx * (AMPS_NC * dx0), o1 = x01 + by * (AMPS_NC * dx1),
-               o2 = x02 + bz * (AMPS_NC * dx2);
+  double o0, o1, o2;
+  if (m.borg) {
+    // AMR: origin on the finest lattice, cell size a power of two of the finest
+    o0 = x00 + m.borg[3 * b] * dxf;
+    o1 = x01 + m.borg[3 * b + 1] * dxf;
+    o2 = x02 + m.borg[3 * b + 2] * dxf;
+    dx0 = dx1 = dx2 = m.bscale[b] * dxf;
+  } else {
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    o0 = x00 + bx * (AMPS_NC * dx0);
+    o1 = x01 + by * (AMPS_NC * dx1);
+    o2 = x02 + bz * (AMPS_NC * dx2);
+  }
   const int b0 = base[cid], n0 = cnt[cid];
   long long q = out0[cid];
   for (int t = 0; t < n0; t++, q++) {
@@ -795,6 +917,7 @@ StepArgs step_args(amps_gpu_ctx* c) {
   a.inv_vol = (float)(1.0 / (c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2]));
   a.ovf_cap = c->slots;
   a.st = make_species(c->cfg);
+  a.amr = c->amrdev;
   return a;
 }
 
@@ -806,8 +929,10 @@ size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * 32 * kRec
 void set_smem_attrs() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_push_deposit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(true));
-  cudaFuncSetAttribute(k_push_deposit<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
+  cudaFuncSetAttribute(k_push_deposit<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(true));
+  cudaFuncSetAttribute(k_push_deposit<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
+  cudaFuncSetAttribute(k_push_deposit<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(true));
+  cudaFuncSetAttribute(k_push_deposit<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
   cudaFuncSetAttribute(k_arrivals<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
   cudaFuncSetAttribute(k_arrivals<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
   cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
@@ -865,13 +990,16 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
 // launchers
 cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
                                  const double* Bcur) {
+  if (c->amr) return launch_amr_pack(c, Eh, Bprev, Bcur);
   TimedLaunch t(c, "pack_stencils");
   k_pack_stencils<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, Eh, Bprev, Bcur,
                                                  c->d_stencil_push, c->d_stencil_dep);
   return cudaGetLastError();
 }
 
+// On AMR meshes the field operator reads the per-cell partials directly.
 static cudaError_t launch_assemble(amps_gpu_ctx* c) {
+  if (c->amr) return cudaSuccess;
   init_asm_table();
   TimedLaunch t(c, "assemble");
   const double inv_vol = 1.0 / (c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2]);
@@ -908,10 +1036,17 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
   const dim3 grid(c->nb, AMPS_NC);
   {
     TimedLaunch t(c, deposit ? "push_deposit" : "push");
-    if (deposit)
-      k_push_deposit<true><<<grid, kWarps * 32, smem_push(true), c->stream>>>(a);
-    else
-      k_push_deposit<false><<<grid, kWarps * 32, smem_push(false), c->stream>>>(a);
+    if (c->amr) {
+      if (deposit)
+        k_push_deposit<true, true><<<grid, kWarps * 32, smem_push(true), c->stream>>>(a);
+      else
+        k_push_deposit<false, true><<<grid, kWarps * 32, smem_push(false), c->stream>>>(a);
+    } else {
+      if (deposit)
+        k_push_deposit<true, false><<<grid, kWarps * 32, smem_push(true), c->stream>>>(a);
+      else
+        k_push_deposit<false, false><<<grid, kWarps * 32, smem_push(false), c->stream>>>(a);
+    }
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -949,6 +1084,26 @@ cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow) {
 
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
                                const uint8_t* d_spec_in, const double* d_wc, long long n) {
+  if (c->amr) {
+    ImportAmrArgs a;
+    a.x = d_x; a.v = d_v; a.sp = d_spec_in; a.wc = d_wc;
+    a.d = pbuf(c, c->cur ^ 1);
+    a.key = c->d_key;
+    a.flags = c->d_flags;
+    a.n = n;
+    a.m = c->amrdev;
+    for (int d = 0; d < 3; d++) a.x0[d] = c->cfg.x0[d];
+    a.dxf = c->dxf;
+    a.nspec = c->cfg.nspec;
+    {
+      TimedLaunch t(c, "import");
+      k_import_amr<<<grid_for(n, 256), 256, 0, c->stream>>>(a);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    c->np = n;
+    return rebuild_from_list(c, n);
+  }
   ImportArgs a;
   a.x = d_x; a.v = d_v; a.sp = d_spec_in; a.wc = d_wc;
   a.d = pbuf(c, c->cur ^ 1);
@@ -995,6 +1150,6 @@ cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, uint8_t* d_
   k_export<<<(unsigned)((c->ncor + 255) / 256), 256, 0, c->stream>>>(
       c->ncor, c->d_base, c->d_cnt, c->d_tmp, pbuf(c, c->cur), c->cfg.nbx, c->cfg.nby,
       c->cfg.x0[0], c->cfg.x0[1], c->cfg.x0[2], c->cfg.dx[0], c->cfg.dx[1], c->cfg.dx[2], d_x, d_v,
-      d_sp, d_blk, d_cel, d_id);
+      d_sp, d_blk, d_cel, d_id, c->amrdev, c->dxf);
   return cudaGetLastError();
 }

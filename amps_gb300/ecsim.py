@@ -144,12 +144,14 @@ def initial_fields(wl: Workload):
 
 
 class EcsimContext:
-    """One device context: a periodic block mesh, its fields and particles."""
+    """One device context: a periodic block mesh (uniform, or the AMR mesh
+    `amr_mesh` with wl's species and time step), its fields and particles."""
 
     def __init__(self, wl: Workload, capacity: Optional[int] = None, track_ids: bool = True,
-                 device: int = 0):
+                 device: int = 0, amr_mesh=None):
         self.lib = _capi.load()
         self.wl = wl
+        self.amr_mesh = amr_mesh
         cfg = _capi.Config()
         m = wl.mesh
         cfg.nbx, cfg.nby, cfg.nbz = m.nbx, m.nby, m.nbz
@@ -165,10 +167,16 @@ class EcsimContext:
         cfg.device = device
         self.cfg = cfg
         h = C.c_void_p()
-        st = self.lib.amps_gpu_create(C.byref(cfg), C.byref(h))
+        if amr_mesh is None:
+            st = self.lib.amps_gpu_create(C.byref(cfg), C.byref(h))
+        else:
+            st = self.lib.amps_gpu_create_amr(C.byref(cfg), amr_mesh.h, C.byref(h))
         if st != 0:
             raise AmpsGpuError(st, "amps_gpu_create")
         self.h = h
+        nb, ncell, ncor = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self.lib.amps_gpu_mesh_sizes(h, C.byref(nb), C.byref(ncell), C.byref(ncor))
+        self.nblocks, self.ncells, self.ncorners = nb.value, ncell.value, ncor.value
 
     # ---- helpers ----
     def _check(self, st, what):
@@ -249,9 +257,9 @@ class EcsimContext:
                     "import_fields")
 
     def export_fields(self):
-        nc = self.wl.mesh.ncells
-        out = {k: np.empty((nc, 3)) for k in
-               ("E_n", "E_half", "B_center", "B_corner_prev", "B_corner_cur")}
+        out = {k: np.empty((self.ncorners, 3)) for k in
+               ("E_n", "E_half", "B_corner_prev", "B_corner_cur")}
+        out["B_center"] = np.empty((self.ncells, 3))
         self._check(self.lib.amps_gpu_export_fields(
             self.h, *[ptr(out[k], C.c_double) for k in
                       ("E_n", "E_half", "B_center", "B_corner_prev", "B_corner_cur")]),
@@ -270,6 +278,16 @@ class EcsimContext:
         M = np.empty((nc, 243)) if with_m else None
         self._check(self.lib.amps_gpu_export_moments(self.h, ptr(J, C.c_double),
                                                      ptr(M, C.c_double)), "export_moments")
+        return J, M
+
+    def export_cell_moments(self, with_m=True):
+        """per-cell ProcessCell partials (cells in block order): cellJ (ncells, 24),
+        cellM (ncells, 324) or None"""
+        J = np.empty((self.ncells, 24))
+        M = np.empty((self.ncells, 324)) if with_m else None
+        self._check(self.lib.amps_gpu_export_cell_moments(self.h, ptr(J, C.c_double),
+                                                          ptr(M, C.c_double)),
+                    "export_cell_moments")
         return J, M
 
     # ---- reference call surfaces ----

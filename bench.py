@@ -4,6 +4,12 @@ push + re-bin + deposit (Lapenta2017 mover + ECSIM UpdateJMassMatrix).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--workload NAME]
 
+Default workload: the two-level AMR plasma (64^3 base cells in 8^3-cell
+blocks, central 1/8 of the volume refined 2x, electrons + protons at 128
+particles per species per base cell: 67,108,864 particles, 960 blocks).
+Uniform periodic workloads (WORKLOADS in amps_gb300.ecsim) run with the same
+command.
+
 A step is one pass of push + re-bin + deposit over every particle of the
 workload (inputs resident in HBM; the particle arrays, ~1.7 GB, exceed the
 129 MB L2, so no L2 flush is needed).  The timed region is bracketed by a
@@ -14,8 +20,8 @@ path is not sharded), value = all ranks' particle-steps / max time.
 --impl reference times the reference CPU path on the host cores: the
 reference's ECSIM sources need its generated build headers and do not compile
 standalone, so the FP64 restatement of Lapenta2017 + ProcessCell (oracle/) is
-timed instead, one periodic single-block replica of the same plasma per host
-thread.
+timed instead, one replica of the same plasma per host thread (AMR workloads:
+the same mesh recipe at 32^3 base cells).
 """
 import argparse
 import ctypes as C
@@ -167,12 +173,10 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def kernel_bytes(wl, name):
+def kernel_bytes(n, ncell, nb, name):
     """Algorithmic bytes per launch of each particle-step kernel: what the
-    kernel must read and write given the slotted cell layout."""
-    n = wl.nparticles
-    ncell = wl.mesh.ncells
-    nb = wl.mesh.nblocks
+    kernel must read and write given the slotted cell layout (n particles,
+    ncell cells, nb blocks)."""
     ctas = nb * 8
     if name == "push_deposit":
         # particles: read u,v (24) + species (1), write u,v (24); per cell: base, cnt
@@ -228,23 +232,100 @@ def cpu_replica_rate(wl_name, steps, seconds_budget, threads):
                               "particle_steps": sum(counts)}
 
 
+def cpu_amr_replica_rate(seconds_budget, threads, ppc_base=32):
+    """FP64 AMR oracle (push with re-binning across levels + ProcessCell per
+    cell) on per-thread replicas of the AMR plasma: the same mesh recipe at
+    32^3 base cells (120 blocks).  Returns particle-steps/s over all threads."""
+    import amps_gb300 as A  # noqa: F401
+    from amps_gb300 import amr
+    from tests import oracle_amr as OA
+    wl = amr.AmrWorkload("cpu_replica", (4, 4, 4), 1, 0, 0.5, ppc_base)
+    mesh = wl.mesh()
+    f = amr.amr_initial_fields(mesh, wl.b0)
+    states = []
+    for t in range(threads):
+        ic = amr.amr_initial_condition(mesh, wl.species, ppc_base, seed=100 + 2 * t + 1)
+        bo, bd = mesh.block_origins(), mesh.block_dx()
+        x = bo[ic["block"]] + ic["u"].astype(np.float64) * bd[ic["block"]][:, None]
+        ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64),
+                          ic["spec"])
+        ao.E_half[:] = f["E_half"]
+        ao.Bprev[:] = f["B_corner_prev"]
+        ao.Bcur[:] = f["B_corner_cur"]
+        states.append(ao)
+    counts = [0] * threads
+    deadline = [None]
+
+    def work(i):
+        st = states[i]
+        while time.time() < deadline[0]:
+            st.push()
+            st.deposit()
+            counts[i] += len(st.spec)
+
+    deadline[0] = time.time() + seconds_budget
+    t0 = time.time()
+    th = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    dt = time.time() - t0
+    n = len(states[0].spec)
+    return sum(counts) / dt, {"replica_particles": n, "threads": threads, "seconds": dt,
+                              "particle_steps": sum(counts),
+                              "replica": "AMR mesh, 4^3 level-0 blocks, central 1/8 refined 2x, "
+                                         "%d ppc per species per base cell" % ppc_base}
+
+
+def setup_workload(name, device, track_ids=False):
+    """Context with the workload's particles and initial fields imported.
+    Returns (ctx, info)."""
+    import amps_gb300 as A
+    from amps_gb300 import amr
+    t_ic = time.time()
+    if name in amr.AMR_WORKLOADS:
+        wl = amr.AMR_WORKLOADS[name]()
+        mesh = wl.mesh()
+        ic = amr.amr_initial_condition(mesh, wl.species, wl.ppc, seed=100,
+                                       nthreads=os.cpu_count() or 8)
+        t_ic = time.time() - t_ic
+        n = len(ic["spec"])
+        ctx = A.EcsimContext(wl.plasma, capacity=n, track_ids=track_ids, device=device,
+                             amr_mesh=mesh)
+        f = amr.amr_initial_fields(mesh, wl.b0)
+        info = {"workload": name, "particles": n, "cells": mesh.ncells, "blocks": mesh.nblocks,
+                "corners": mesh.ncorners, "hanging_corners": mesh.nhanging,
+                "levels": wl.lmax + 1, "fine_blocks": int(np.sum(mesh.level > 0)),
+                "ppc_per_species_base_cell": wl.ppc, "amr": True, "tol": wl.tol}
+    else:
+        wl = A.WORKLOADS[name]()
+        ic = A.make_initial_condition(wl, nthreads=os.cpu_count() or 8)
+        t_ic = time.time() - t_ic
+        n = wl.nparticles
+        ctx = A.EcsimContext(wl, capacity=n, track_ids=track_ids, device=device)
+        f = A.initial_fields(wl)
+        info = {"workload": name, "particles": n, "cells": wl.mesh.ncells,
+                "blocks": wl.mesh.nblocks, "ppc_per_species": wl.ppc, "amr": False,
+                "tol": wl.tol}
+    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
+    ctx.import_fields(**f)
+    info["ic_seconds"] = round(t_ic, 2)
+    return ctx, info
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import amps_gb300 as A
     ws, rank, local = dist_env()
     dist = init_dist(ws)
-    wl = A.WORKLOADS[args.workload]()
     ev = CudaEvents()
-    t_ic = time.time()
-    ic = A.make_initial_condition(wl, nthreads=os.cpu_count() or 8)
-    t_ic = time.time() - t_ic
-    ctx = A.EcsimContext(wl, capacity=wl.nparticles, track_ids=False, device=local)
-    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
-    f = A.initial_fields(wl)
-    ctx.import_fields(**f)
+    ctx, info = setup_workload(args.workload, local)
+    npart, ncell, nblk = info["particles"], info["cells"], info["blocks"]
+    tol = info["tol"]
     # one field solve so the push sees a self-consistent E^{n+theta}
     ctx.UpdateJMassMatrix()
-    solve = ctx.TimeStep(tol=wl.tol, maxit=200, precond=1)
+    solve = ctx.TimeStep(tol=tol, maxit=200, precond=1)
     stream = ctx.stream()
     for _ in range(args.warmup):
         ctx.push_deposit(want_energy=False)
@@ -267,7 +348,7 @@ def run_gpu(args):
     ktimes = ctx.kernel_times()
     ctx.set_kernel_timing(False)
     ms_max = max_over_ranks(dist, ms)
-    total_ps = sum_over_ranks(dist, float(wl.nparticles) * args.steps)
+    total_ps = sum_over_ranks(dist, float(npart) * args.steps)
     value = total_ps / (ms_max / 1e3)
 
     # full ECSIM step (field solve + push + deposit), Jacobi GMRES
@@ -275,7 +356,7 @@ def run_gpu(args):
     for _ in range(2):
         a2, b2 = ev.event(), ev.event()
         ev.record(a2, stream)
-        s = ctx.PicTimeStep(tol=wl.tol, maxit=200, precond=1)
+        s = ctx.PicTimeStep(tol=tol, maxit=200, precond=1)
         ev.record(b2, stream)
         t_step.append(ev.elapsed_ms(a2, b2))
     gmres_it = s.solve.iterations
@@ -285,23 +366,26 @@ def run_gpu(args):
     if args.e2e_steps > 0:
         exp = ctx.export_particles(ids=False)
         hx, hv, hs = exp["x"], exp["v"], exp["spec"]
-        nc = wl.mesh.ncells
-        hJ = np.empty((nc, 3))
         t0 = time.time()
         for _ in range(args.e2e_steps):
             ctx.import_particles(hx, hv, hs)
             ctx.push_deposit(want_energy=True)
             out = ctx.export_particles(ids=False)
             hx, hv = out["x"], out["v"]
-            hJ, _ = ctx.export_moments(with_m=False)
+            if info["amr"]:
+                hJ, _ = ctx.export_cell_moments(with_m=False)
+            else:
+                hJ, _ = ctx.export_moments(with_m=False)
         ctx.synchronize()
         e2e_s = time.time() - t0
-        bi = wl.nparticles * (24 + 24 + 1)
-        bo = wl.nparticles * (24 + 24 + 1 + 4 + 4) + nc * 24
-        e2e = {"value": wl.nparticles * args.e2e_steps / e2e_s, "unit": UNIT,
+        bi = npart * (24 + 24 + 1)
+        bo = npart * (24 + 24 + 1 + 4 + 4) + hJ.nbytes
+        e2e = {"value": npart * args.e2e_steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "steps": args.e2e_steps,
                "api": "amps_gpu_import_particles + amps_gpu_push_deposit + "
-                      "amps_gpu_export_particles + amps_gpu_export_moments (J)"}
+                      "amps_gpu_export_particles + " +
+                      ("amps_gpu_export_cell_moments (J)" if info["amr"]
+                       else "amps_gpu_export_moments (J)")}
 
     # roofline of the dominant kernel
     peak, peak_kind = measured_peaks()
@@ -309,7 +393,7 @@ def run_gpu(args):
     top = max(per, key=lambda k: per[k][0])
     ms_top, launches = per[top]
     nl = max(1, launches)
-    nbytes = kernel_bytes(wl, top)
+    nbytes = kernel_bytes(npart, ncell, nblk, top)
     roof = None
     if nbytes:
         achieved = nbytes / (ms_top / nl / 1e3) / 1e9
@@ -322,23 +406,26 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
-        rate, info = cpu_replica_rate(args.workload, 1, args.cpu_seconds, 1)
-        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "FP64 oracle Lapenta2017+ProcessCell on a periodic 8^3-cell replica "
-                         "of the same plasma (%d particles), %.1f s" % (info["replica_particles"],
-                                                                      info["seconds"])}
+        if info["amr"]:
+            rate, ci = cpu_amr_replica_rate(args.cpu_seconds, 1)
+            smp = "FP64 AMR oracle push+re-bin+ProcessCell on one replica (%s; %d particles), " \
+                  "%.1f s" % (ci["replica"], ci["replica_particles"], ci["seconds"])
+        else:
+            rate, ci = cpu_replica_rate(args.workload, 1, args.cpu_seconds, 1)
+            smp = "FP64 oracle Lapenta2017+ProcessCell on a periodic 8^3-cell replica of the " \
+                  "same plasma (%d particles), %.1f s" % (ci["replica_particles"], ci["seconds"])
+        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 field solve)",
             "data": "synthetic (seeded Maxwellian electron-proton plasma, LCG of rnd.h)",
-            "config": {"workload": wl.name, "particles": wl.nparticles,
-                       "cells": wl.mesh.ncells, "blocks": wl.mesh.nblocks, "ppc_per_species": wl.ppc,
-                       "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (no flush)",
-                       "ecsim_step_ms": round(min(t_step), 3), "gmres_iterations": gmres_it,
-                       "gmres_precond": "jacobi", "ic_seconds": round(t_ic, 2)},
+            "config": dict(info, **{
+                "parallelism": "replicas" if ws > 1 else "single GPU",
+                "l2": "inputs larger than L2 (no flush)",
+                "ecsim_step_ms": round(min(t_step), 3), "gmres_iterations": gmres_it,
+                "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations}),
             "e2e": e2e, "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
             "clocks": clocks, "gpu_launches": gpu_launches,
         }
@@ -352,15 +439,25 @@ def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
+    from amps_gb300 import amr
     threads = os.cpu_count() or 1
     rates = []
+    is_amr = args.workload in amr.AMR_WORKLOADS
     for _ in range(args.steps):
-        r, info = cpu_replica_rate(args.workload, 1, args.ref_seconds, threads)
+        if is_amr:
+            r, info = cpu_amr_replica_rate(args.ref_seconds, threads)
+        else:
+            r, info = cpu_replica_rate(args.workload, 1, args.ref_seconds, threads)
         rates.append(r)
     value = float(np.mean(rates))
-    sample = ("FP64 oracle port of Lapenta2017 + ProcessCell + re-binning, one periodic "
-              "8^3-cell replica of the same plasma per host thread (%d threads, %d particles "
-              "each), %g s per step" % (threads, info["replica_particles"], args.ref_seconds))
+    if is_amr:
+        sample = ("FP64 AMR oracle port of Lapenta2017 + re-binning across levels + ProcessCell, "
+                  "one replica per host thread (%s; %d threads, %d particles each), %g s per "
+                  "step" % (info["replica"], threads, info["replica_particles"], args.ref_seconds))
+    else:
+        sample = ("FP64 oracle port of Lapenta2017 + ProcessCell + re-binning, one periodic "
+                  "8^3-cell replica of the same plasma per host thread (%d threads, %d particles "
+                  "each), %g s per step" % (threads, info["replica_particles"], args.ref_seconds))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -378,7 +475,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="ecsim_64c_128ppc")
+    ap.add_argument("--workload", default="amr_64c_128ppc")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=8.0)

@@ -123,6 +123,17 @@ int amps_amr_nested_leaves(int nbx0, int nby0, int nbz0, int lmax, int mode, dou
 
 /* ---- context (PIC::Init / ECSIM::Init analogue) ---- */
 amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out);
+/* Context on a block-structured AMR mesh (the leaf blocks of the reference's
+ * octree, meshAMRgeneric.h): geometry (x0, level-0 dx, level-0 block counts)
+ * is taken from the mesh, species/dt/theta/capacity/device from cfg.  Corner
+ * fields use the mesh's unique-corner numbering (amps_amr_tables), cell fields
+ * block*512 + i + 8j + 64k; a particle's block-local offset is in its block's
+ * cell units.  The mesh may be destroyed after this call. */
+amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_mesh* mesh,
+                                    amps_gpu_ctx** out);
+/* blocks, cells (block*512 + local) and corners carrying unknowns */
+amps_gpu_status amps_gpu_mesh_sizes(const amps_gpu_ctx* ctx, long long* nblocks,
+                                    long long* ncells, long long* ncorners);
 amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* ctx);
 const char* amps_gpu_last_error(const amps_gpu_ctx* ctx);
 amps_gpu_status amps_gpu_get_stream(amps_gpu_ctx* ctx, void** stream);
@@ -154,9 +165,16 @@ amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* ctx, const double* E_n, con
 amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* ctx, double* E_n, double* E_half,
                                        double* B_center, double* B_corner_prev,
                                        double* B_corner_cur);
-/* J: 3 per corner, M: 243 per corner (global layout above). */
+/* J: 3 per corner, M: 243 per corner (global layout above).  Uniform meshes
+ * only: AMR contexts return AMPS_GPU_INVALID_ARG. */
 amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* ctx, const double* J, const double* M);
 amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* ctx, double* J, double* M);
+/* Per-cell pieces of ProcessCell (pic_field_solver_ecsim.cpp:1882-2438) before
+ * the corner assembly, cells in block order: cellJ[24] = sum q W w_c (alpha v)
+ * for the 8 corners (order (0,0,0),(1,0,0),(1,1,0),(0,1,0), then z+1), and
+ * cellM[324] = sum (q W h / V) w_c1 w_c2 alpha (row-major 3x3) for the 36 pairs
+ * c2 <= c1.  Accumulated in FP32, returned widened to FP64. */
+amps_gpu_status amps_gpu_export_cell_moments(amps_gpu_ctx* ctx, double* cellJ, double* cellM);
 
 /* ---- hot path ---- */
 /* PIC::Mover::MoveParticles with Lapenta2017 (pic_mover.cpp:580,

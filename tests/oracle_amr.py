@@ -128,6 +128,24 @@ class AmrOracle:
                                  p(self.cellM), tol, maxit, p(diag))
         return it, diag
 
+    def field_solve(self, tol=1e-10, maxit=400):
+        """ECSIM field solve from the current cellJ/cellM (rhs, GMRES, E^{n+theta},
+        UpdateB, corner B prev <- cur, C2N, UpdateE).  Returns (iterations, wave energy)."""
+        g = C.byref(self.g)
+        rhs = np.zeros_like(self.E_n)
+        self.L.orc_amr_rhs(g, p(self.E_n), p(self.Bcen), p(self.cellJ), p(self.cellM), p(rhs))
+        dE = np.zeros_like(self.E_n)
+        res = np.zeros(1)
+        it = self.L.orc_amr_gmres(g, p(self.cellM), p(rhs), p(dE), tol, maxit, 30, p(res))
+        self.E_half[:] = self.E_n + dE
+        bnew = np.zeros_like(self.Bcen)
+        self.L.orc_amr_update_b(g, p(self.E_half), p(self.Bcen), p(bnew))
+        self.Bcen[:] = bnew
+        self.Bprev[:] = self.Bcur
+        self.L.orc_amr_c2n(g, p(self.Bcen), p(self.Bcur))
+        wave = self.L.orc_amr_update_e(g, p(self.E_half), p(self.E_n), p(self.Bcen))
+        return it, wave
+
     def wave_energy(self):
         """sum_cells V (sum_corners |E|^2/8 + |B|^2)/(8 pi) of the current state"""
         tmp = self.E_n.copy()
