@@ -7,12 +7,14 @@ surfaces (PIC::Mover, PIC::ParticleBuffer, ECSIM) for Python callers.
 from ._capi import AmpsGpuError, load  # noqa: F401
 from .ecsim import (  # noqa: F401
     WORKLOADS,
+    PRECOND_SHAPES,
     EcsimContext,
     PeriodicMesh,
     Species,
     Workload,
     block_origins,
     electron_proton_plasma,
+    init_precond_weights,
     initial_fields,
     make_initial_condition,
     physical_positions,
@@ -22,5 +24,6 @@ from .ecsim import (  # noqa: F401
 __all__ = [
     "AmpsGpuError", "load", "WORKLOADS", "EcsimContext", "PeriodicMesh", "Species", "Workload",
     "block_origins", "electron_proton_plasma", "initial_fields", "make_initial_condition",
+    "PRECOND_SHAPES", "init_precond_weights",
     "physical_positions", "trace_dipole",
 ]

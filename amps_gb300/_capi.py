@@ -95,6 +95,16 @@ SIGNATURES = {
     "amps_gpu_push_deposit": (C.c_int, [P, D]),
     "amps_gpu_update_j_mass_matrix_noalloc": (C.c_int, [C.POINTER(Config), C.c_longlong, P, P,
                                                         P, P, P, P, P, P, P]),
+    "amps_gpu_set_inner_fp64": (C.c_int, [P, C.c_int]),
+    "amps_gpu_precond_load": (C.c_int, [P, F, F, F]),
+    "amps_gpu_precond_get": (C.c_int, [P, F, F, F]),
+    "amps_gpu_precond_use_tensor_cores": (C.c_int, [P, C.c_int]),
+    "amps_gpu_precond_harvest": (C.c_int, [P, C.c_longlong]),
+    "amps_gpu_precond_num_samples": (C.c_int, [P, LL]),
+    "amps_gpu_precond_get_samples": (C.c_int, [P, C.c_longlong, C.c_longlong, F, F]),
+    "amps_gpu_precond_train": (C.c_int, [P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, F]),
+    "amps_gpu_precond_loss_grad": (C.c_int, [P, C.c_longlong, F, F, F, F, F, F]),
+    "amps_gpu_precond_forward": (C.c_int, [P, C.c_longlong, F, C.c_int, F]),
     "amps_gpu_set_kernel_timing": (C.c_int, [P, C.c_int]),
     "amps_gpu_get_kernel_times": (C.c_int, [P, C.POINTER(C.c_char_p), D, LL, C.c_int,
                                             C.POINTER(C.c_int)]),

@@ -44,8 +44,9 @@ __device__ __forceinline__ double cval(const double* __restrict__ F, const doubl
 }
 
 // scatter out[8][3] to the cell's corners with P^T
-__device__ __forceinline__ void scatter(double* __restrict__ y, long long nvc, const int cid[8],
-                                        const double out[8][3], const Hang& h) {
+template <typename T>
+__device__ __forceinline__ void scatter(T* __restrict__ y, long long nvc, const int cid[8],
+                                        const T out[8][3], const Hang& h) {
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     const int cc = cid[c], s = h.hs[cc], e = h.hs[cc + 1];
@@ -53,39 +54,56 @@ __device__ __forceinline__ void scatter(double* __restrict__ y, long long nvc, c
 #pragma unroll
       for (int d = 0; d < 3; d++) atomicAdd(y + d * nvc + cc, out[c][d]);
     } else {
-      for (int t = s; t < e; t++)
+      for (int t = s; t < e; t++) {
+        const T w = (T)h.hw[t];
 #pragma unroll
-        for (int d = 0; d < 3; d++) atomicAdd(y + d * nvc + h.hp[t], h.hw[t] * out[c][d]);
+        for (int d = 0; d < 3; d++) atomicAdd(y + d * nvc + h.hp[t], w * out[c][d]);
+      }
     }
   }
 }
 
-__device__ __forceinline__ void cell_curl(const double e[8][3], double dx, double cu[3]) {
-  double a = 0, b = 0, c = 0, d = 0, f = 0, g = 0;
+template <typename T>
+__device__ __forceinline__ void cell_curl(const T e[8][3], T q, T cu[3]) {
+  T a = 0, b = 0, c = 0, d = 0, f = 0, g = 0;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    const double sx = c_off[k][0] ? 1.0 : -1.0, sy = c_off[k][1] ? 1.0 : -1.0,
-                 sz = c_off[k][2] ? 1.0 : -1.0;
-    a += sy * e[k][2]; b += sz * e[k][1];
-    c += sz * e[k][0]; d += sx * e[k][2];
-    f += sx * e[k][1]; g += sy * e[k][0];
+    const bool px = k == 1 || k == 2 || k == 5 || k == 6;
+    const bool py = k == 2 || k == 3 || k == 6 || k == 7;
+    const bool pz = k >= 4;
+    a += py ? e[k][2] : -e[k][2];
+    b += pz ? e[k][1] : -e[k][1];
+    c += pz ? e[k][0] : -e[k][0];
+    d += px ? e[k][2] : -e[k][2];
+    f += px ? e[k][1] : -e[k][1];
+    g += py ? e[k][0] : -e[k][0];
   }
-  const double q = 0.25 / dx;
   cu[0] = q * (a - b);
   cu[1] = q * (c - d);
   cu[2] = q * (f - g);
 }
 
-__device__ __forceinline__ void cell_curl_t(const double y[3], double s, double out[8][3]) {
+// out += s C^T y  (C with the 1/(4 dx) factor folded into s)
+template <typename T>
+__device__ __forceinline__ void cell_curl_t(const T y[3], T s, T out[8][3]) {
+  const T a0 = s * y[0], a1 = s * y[1], a2 = s * y[2];
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    const double sx = c_off[k][0] ? 1.0 : -1.0, sy = c_off[k][1] ? 1.0 : -1.0,
-                 sz = c_off[k][2] ? 1.0 : -1.0;
-    out[k][0] += s * (sz * y[1] - sy * y[2]);
-    out[k][1] += s * (sx * y[2] - sz * y[0]);
-    out[k][2] += s * (sy * y[0] - sx * y[1]);
+    const bool px = k == 1 || k == 2 || k == 5 || k == 6;
+    const bool py = k == 2 || k == 3 || k == 6 || k == 7;
+    const bool pz = k >= 4;
+    out[k][0] += (pz ? a1 : -a1) - (py ? a2 : -a2);
+    out[k][1] += (px ? a2 : -a2) - (pz ? a0 : -a0);
+    out[k][2] += (py ? a0 : -a0) - (px ? a1 : -a1);
   }
 }
+
+template <typename T>
+__device__ __forceinline__ T from_f32(float v);
+template <>
+__device__ __forceinline__ double from_f32<double>(float v) { return widen(v); }
+template <>
+__device__ __forceinline__ float from_f32<float>(float v) { return v; }
 
 struct ApplyArgs {
   long long ncell, nvc;
@@ -97,51 +115,56 @@ struct ApplyArgs {
   const double* x;     // input field (component-major)
   const double* dinv;  // optional right preconditioner
   const double* Bcen;  // RHS: centre B (component-major over cells)
-  double* y;
   double th2dt2, f, thdt;
   int with_identity, with_curl, with_mass, rhs_mode;
 };
 
-// y += cell contributions.  rhs_mode: y = -(curl-curl + M) x + theta dt C^T B - f J
-__global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a) {
+// y += cell contributions in precision T (FP64: outer residuals and RHS;
+// FP32: inner GMRES operator).  rhs_mode: y = -(curl-curl + M) x
+// + theta dt C^T B - f J.
+template <typename T>
+__global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a, T* __restrict__ y) {
   const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= a.ncell) return;
   const int b = (int)(cell >> 9), l = (int)(cell & 511);
   const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
-  const double dx = a.bdx[b], V = dx * dx * dx;
+  const double dxd = a.bdx[b];
+  const T dx = (T)dxd, V = (T)(dxd * dxd * dxd);
   int cid[8];
-  double e[8][3], out[8][3];
+  T e[8][3], out[8][3];
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     cid[c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      e[c][d] = cval(a.x, a.dinv, a.nvc, cid[c], d, a.h);
-      out[c][d] = 0.0;
+      e[c][d] = (T)cval(a.x, a.dinv, a.nvc, cid[c], d, a.h);
+      out[c][d] = (T)0;
     }
   }
-  const double sg = a.rhs_mode ? -1.0 : 1.0;
-  if (a.with_identity)
+  const T sg = a.rhs_mode ? (T)-1 : (T)1;
+  if (a.with_identity) {
+    const T v8 = (T)0.125 * V;
 #pragma unroll
     for (int c = 0; c < 8; c++)
 #pragma unroll
-      for (int d = 0; d < 3; d++) out[c][d] += 0.125 * V * e[c][d];
+      for (int d = 0; d < 3; d++) out[c][d] += v8 * e[c][d];
+  }
   if (a.with_curl) {
-    double cu[3];
-    cell_curl(e, dx, cu);
-    cell_curl_t(cu, sg * a.th2dt2 * V * 0.25 / dx, out);
+    T cu[3];
+    cell_curl<T>(e, (T)0.25 / dx, cu);
+    cell_curl_t<T>(cu, sg * (T)a.th2dt2 * V * (T)0.25 / dx, out);
   }
   if (a.with_mass) {
     const float* mm = a.cellM + cell * 324;
-    const double fv = sg * a.f * V;
-#pragma unroll 1
-    for (int c1 = 0; c1 < 8; c1++)
-#pragma unroll 1
-      for (int c2 = 0; c2 <= c1; c2++) {
-        const float* blk = mm + (c1 * (c1 + 1) / 2 + c2) * 9;
-        double m9[9];
+    const T fv = sg * (T)a.f * V;
+    int pr = 0;
 #pragma unroll
-        for (int t = 0; t < 9; t++) m9[t] = fv * widen(blk[t]);
+    for (int c1 = 0; c1 < 8; c1++)
+#pragma unroll
+      for (int c2 = 0; c2 <= c1; c2++, pr++) {
+        T m9[9];
+#pragma unroll
+        for (int t = 0; t < 9; t++) m9[t] = fv * from_f32<T>(mm[pr * 9 + t]);
 #pragma unroll
         for (int p = 0; p < 3; p++) {
           out[c1][p] += m9[3 * p] * e[c2][0] + m9[3 * p + 1] * e[c2][1] + m9[3 * p + 2] * e[c2][2];
@@ -151,15 +174,40 @@ __global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a) {
       }
   }
   if (a.rhs_mode) {
-    const double B[3] = {a.Bcen[cell], a.Bcen[a.ncell + cell], a.Bcen[2 * a.ncell + cell]};
-    cell_curl_t(B, a.thdt * V * 0.25 / dx, out);
+    const T B[3] = {(T)a.Bcen[cell], (T)a.Bcen[a.ncell + cell], (T)a.Bcen[2 * a.ncell + cell]};
+    cell_curl_t<T>(B, (T)a.thdt * V * (T)0.25 / dx, out);
     const float* jj = a.cellJ + cell * 24;
 #pragma unroll
     for (int c = 0; c < 8; c++)
 #pragma unroll
-      for (int d = 0; d < 3; d++) out[c][d] -= a.f * widen(jj[3 * c + d]);
+      for (int d = 0; d < 3; d++) out[c][d] -= (T)a.f * from_f32<T>(jj[3 * c + d]);
   }
-  scatter(a.y, a.nvc, cid, out, a.h);
+  scatter<T>(y, a.nvc, cid, out, a.h);
+}
+
+// FP32 accumulation -> FP64 operator output (free rows); hanging rows get the
+// constraint x_h - (P x)_h in FP64
+__global__ void __launch_bounds__(256) k_amr_finish32(long long nvc, Hang h,
+                                                      const float* __restrict__ y32,
+                                                      const double* __restrict__ x,
+                                                      const double* __restrict__ dinv,
+                                                      double* __restrict__ y) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+  const int s = h.hs[c], e = h.hs[c + 1];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (s == e) {
+      y[d * nvc + c] = (double)y32[d * nvc + c];
+    } else {
+      double pv = 0.0;
+      for (int t = s; t < e; t++) {
+        const int p = h.hp[t];
+        pv += h.hw[t] * (dinv ? dinv[d * nvc + p] : 1.0) * x[d * nvc + p];
+      }
+      y[d * nvc + c] = (dinv ? dinv[d * nvc + c] : 1.0) * x[d * nvc + c] - pv;
+    }
+  }
 }
 
 // hanging rows: y_h = x_h - (P x)_h (operator) or 0 (rhs)
@@ -235,7 +283,7 @@ __global__ void __launch_bounds__(256) k_amr_update_b(long long ncell, long long
     for (int d = 0; d < 3; d++) e[c][d] = cval(Eh, nullptr, nvc, cc, d, h);
   }
   double cu[3];
-  cell_curl(e, bdx[b], cu);
+  cell_curl<double>(e, 0.25 / bdx[b], cu);
 #pragma unroll
   for (int d = 0; d < 3; d++) Bnew[d * ncell + cell] = Bn[d * ncell + cell] - dt * cu[d];
 }
@@ -386,12 +434,26 @@ cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* di
   ApplyArgs a = apply_args(c);
   a.x = x;
   a.dinv = dinv;
-  a.y = y;
   a.with_identity = a.with_curl = a.with_mass = 1;
   a.rhs_mode = 0;
   TimedLaunch t(c, "matvec", 2);
-  k_amr_cell_op<<<g1(c->ncor), 256, 0, c->stream>>>(a);
+  k_amr_cell_op<double><<<g1(c->ncor), 256, 0, c->stream>>>(a, y);
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, x, dinv, y, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv,
+                                double* y) {
+  cudaError_t e = cudaMemsetAsync(c->d_y32, 0, sizeof(float) * 3 * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  ApplyArgs a = apply_args(c);
+  a.x = x;
+  a.dinv = dinv;
+  a.with_identity = a.with_curl = a.with_mass = 1;
+  a.rhs_mode = 0;
+  TimedLaunch t(c, "matvec32", 2);
+  k_amr_cell_op<float><<<g1(c->ncor), 256, 0, c->stream>>>(a, c->d_y32);
+  k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_y32, x, dinv, y);
   return cudaGetLastError();
 }
 
@@ -402,12 +464,11 @@ cudaError_t launch_amr_rhs(amps_gpu_ctx* c) {
   a.x = c->d_En;
   a.dinv = nullptr;
   a.Bcen = c->d_Bc;
-  a.y = c->d_rhs;
   a.with_identity = 0;
   a.with_curl = a.with_mass = 1;
   a.rhs_mode = 1;
   TimedLaunch t(c, "rhs", 2);
-  k_amr_cell_op<<<g1(c->ncor), 256, 0, c->stream>>>(a);
+  k_amr_cell_op<double><<<g1(c->ncor), 256, 0, c->stream>>>(a, c->d_rhs);
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, nullptr, nullptr, c->d_rhs, 1);
   return cudaGetLastError();
 }

@@ -9,6 +9,7 @@
 
 #include "amr_mesh.h"
 #include "common.cuh"
+#include "precond.cuh"
 
 cudaError_t launch_add(amps_gpu_ctx* c, const double* a, const double* b, double* o, long long n);
 
@@ -271,6 +272,7 @@ bool alloc_context(amps_gpu_ctx* c) {
        !dalloc(&c->d_Bc2, 3 * nc) && !dalloc(&c->d_Bcor_prev, 3 * nv) &&
        !dalloc(&c->d_Bcor_cur, 3 * nv);
   if (!c->amr) ok = ok && !dalloc(&c->d_J, 3 * nc) && !dalloc(&c->d_M, 243 * nc);
+  if (c->amr) ok = ok && !dalloc(&c->d_y32, 3 * nv);
   ok = ok && !dalloc(&c->d_rhs, 3 * nv) && !dalloc(&c->d_x, 3 * nv) &&
        !dalloc(&c->d_V, (size_t)(c->restart + 1) * 3 * nv) && !dalloc(&c->d_w, 3 * nv) &&
        !dalloc(&c->d_dinv, 3 * nv) && !dalloc(&c->d_red, 12288);
@@ -300,7 +302,7 @@ bool alloc_context(amps_gpu_ctx* c) {
   ok = ok && cudaMemset(c->d_Bc, 0, sizeof(double) * 3 * nc) == cudaSuccess;
   if (!c->amr)
     ok = ok && cudaMemset(c->d_J, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
-         cudaMemset(c->d_M, 0, sizeof(double) * 243 * nc) == cudaSuccess;
+         cudaMemset(c->d_M, 0, sizeof(float) * 243 * nc) == cudaSuccess;
   // cell partials start at zero so an AMR solve before any deposit is defined
   ok = ok && cudaMemset(c->d_cellM, 0, sizeof(float) * 324 * nc) == cudaSuccess &&
        cudaMemset(c->d_cellJ, 0, sizeof(float) * 24 * nc) == cudaSuccess;
@@ -320,8 +322,10 @@ bool alloc_context(amps_gpu_ctx* c) {
   return ok;
 }
 
-// slot capacity: particles + 1/4 slack + 8 slack slots per cell
-long long slot_count(long long cap, long long ncell) { return cap + cap / 4 + 8 * ncell + 1024; }
+// slot capacity: particles + 1/4 slack + AMPS_SLACK_MIN slack slots per cell
+long long slot_count(long long cap, long long ncell) {
+  return cap + cap / 4 + (long long)AMPS_SLACK_MIN * ncell + 1024;
+}
 
 template <class T>
 bool upload(T** d, const std::vector<T>& h) {
@@ -461,8 +465,11 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   flush_timers(c);
   staging_free(c);
+  precond_free(c->pn);
+  c->pn = nullptr;
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
                   c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
+                  c->d_Z, c->d_y32,
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw,
@@ -630,10 +637,10 @@ amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* c, const double* J, const 
   if (M) {
     const long long n = c->ncor;
     auto perm = host_perm(c->cfg, n);
-    std::vector<double> tmp((size_t)(243 * n));
+    std::vector<float> tmp((size_t)(243 * n));
     for (long long h = 0; h < n; h++)
-      for (int e = 0; e < 243; e++) tmp[(size_t)(e * n + perm[(size_t)h])] = M[243 * h + e];
-    s = cuda_check(c, cudaMemcpy(c->d_M, tmp.data(), sizeof(double) * tmp.size(), cudaMemcpyHostToDevice),
+      for (int e = 0; e < 243; e++) tmp[(size_t)(e * n + perm[(size_t)h])] = (float)M[243 * h + e];
+    s = cuda_check(c, cudaMemcpy(c->d_M, tmp.data(), sizeof(float) * tmp.size(), cudaMemcpyHostToDevice),
                    "upload M");
     if (s) return s;
   }
@@ -654,8 +661,8 @@ amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
   if (M) {
     const long long n = c->ncor;
     auto perm = host_perm(c->cfg, n);
-    std::vector<double> tmp((size_t)(243 * n));
-    s = cuda_check(c, cudaMemcpy(tmp.data(), c->d_M, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost),
+    std::vector<float> tmp((size_t)(243 * n));
+    s = cuda_check(c, cudaMemcpy(tmp.data(), c->d_M, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost),
                    "download M");
     if (s) return s;
     for (long long h = 0; h < n; h++)
@@ -727,14 +734,17 @@ amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* c, double* particle_energy) 
 
 amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
                                      amps_gpu_solve_stats* stats) {
-  if (!c || tol <= 0.0 || maxit <= 0 || precond < 0 || precond > 1)
+  if (!c || tol <= 0.0 || maxit <= 0 || precond < 0 || precond > 2)
     return set_err(c, AMPS_GPU_INVALID_ARG, "field_solve: bad arguments");
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s;
   amps_gpu_solve_stats st{};
+  if (precond == 2 && (s = reset_flags(c))) return s;
   if ((s = cuda_check(c, launch_rhs(c), "rhs"))) return s;
   amps_gpu_status gs = gmres_solve(c, tol, maxit, precond, &st);
   if (gs != AMPS_GPU_OK && gs != AMPS_GPU_GMRES_NOT_CONVERGED) return gs;
+  // the tensor-core preconditioner reports bounded-wait timeouts in the flags
+  if (precond == 2 && (s = check_flags(c, nullptr, nullptr, nullptr))) return s;
   // ProcessFinalSolution: E^{n+theta} = E^n + dE
   if ((s = cuda_check(c, launch_add(c, c->d_En, c->d_x, c->d_Eh, 3 * c->nvc), "E_half"))) return s;
   if ((s = cuda_check(c, launch_update_b(c), "update_b"))) return s;

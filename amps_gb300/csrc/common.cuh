@@ -4,7 +4,8 @@
 // Data layout in HBM (one context = one periodic mesh of 8^3-cell blocks)
 //   blocks own their 512 low corners and 512 cells: corner id = b*512 + i + 8j + 64k
 //   FP64 vectors are component-major: v[comp*ncor + corner]
-//   mass matrix M: 243 coefficient planes, M[e*ncor + corner] (coalesced per plane)
+//   mass matrix M: 243 FP32 coefficient planes, M[e*ncor + corner] (coalesced per
+//              plane; the deposited values are FP32 sums, widened where FP64 is needed)
 //   particles: FP32 SoA (u: block-local offset in cell units, v), species byte,
 //              optional 32-bit id; every cell owns a slot range with slack
 //   per-block FP32 field stencils (9^3 corners incl. the +1 halo) for the push
@@ -24,6 +25,7 @@
 #define AMPS_SC 729         // stencil corners per block (9^3)
 #define AMPS_PUSH_STRIDE 8  // floats per stencil corner for the push: E3 B3 pad2
 #define AMPS_DEP_STRIDE 4   // floats per stencil corner for the deposit: B3 pad1
+#define AMPS_SLACK_MIN 32   // slack slots per cell on top of count/4 (rebuild)
 
 struct KernelTimer {
   const char* name;
@@ -43,6 +45,8 @@ struct AmrDev {
   const float* bdtdx;      // nb: dt / dx
   const float* binvvol;    // nb: 1 / dx^3
 };
+
+struct PrecondState;
 
 struct amps_gpu_ctx {
   amps_gpu_config cfg;
@@ -77,7 +81,7 @@ struct amps_gpu_ctx {
   double* d_Bcor_prev = nullptr;
   double* d_Bcor_cur = nullptr;
   double* d_J = nullptr;        // 3*ncor
-  double* d_M = nullptr;        // 243*ncor
+  float* d_M = nullptr;         // 243*ncor (uniform meshes)
   bool have_moments = false;
 
   // GMRES workspace
@@ -86,6 +90,10 @@ struct amps_gpu_ctx {
   double* d_V = nullptr;        // (restart+1) * n
   double* d_w = nullptr;
   double* d_dinv = nullptr;
+  double* d_Z = nullptr;        // (restart+1) * n preconditioned directions (learned)
+  float* d_y32 = nullptr;       // 3*nvc FP32 accumulation of the inner AMR operator
+  bool inner_fp32 = true;       // GMRES inner operator in FP32 (iterative refinement)
+  PrecondState* pn = nullptr;   // learned preconditioner (precond.cu)
   double* d_red = nullptr;      // partial reductions
   double* h_red = nullptr;      // pinned
   int restart = 30;
@@ -161,6 +169,8 @@ cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, uint8_t* d_
 // ---- field launchers (field.cu) ----
 cudaError_t launch_rhs(amps_gpu_ctx* c);
 cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
+// the same operator evaluated in FP32 arithmetic (inner GMRES iterations)
+cudaError_t launch_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
 cudaError_t launch_jacobi_diag(amps_gpu_ctx* c);
 cudaError_t launch_update_b(amps_gpu_ctx* c);
 cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor);
@@ -173,6 +183,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
 cudaError_t launch_amr_pack(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
                             const double* Bcur);
 cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
+cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
 cudaError_t launch_amr_rhs(amps_gpu_ctx* c);
 cudaError_t launch_amr_jacobi(amps_gpu_ctx* c);
 cudaError_t launch_amr_update_b(amps_gpu_ctx* c);
@@ -193,6 +204,18 @@ __device__ __forceinline__ int local_id(const int* __restrict__ nbr, int b, int 
   int oz = (k < 0) ? -1 : ((k >= AMPS_NC) ? 1 : 0);
   int bb = (ox | oy | oz) ? __ldg(nbr + b * 27 + nbr_slot(ox, oy, oz)) : b;
   return bb * AMPS_CPB + (i - AMPS_NC * ox) + AMPS_NC * ((j - AMPS_NC * oy) + AMPS_NC * (k - AMPS_NC * oz));
+}
+
+// FP32 -> FP64 widening with integer operations (exact for zero and normal
+// numbers; GB300's FP64 pipe is narrow, the integer pipe is not).
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;  // zero, subnormal, inf, nan
+  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e + 896u) << 52) |
+                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
 }
 
 // 27-slot index of offset (di,dj,dk): digits {0,-1,+1} -> {0,1,2}

@@ -67,18 +67,6 @@ __host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
   return cid * 24 + ce;
 }
 
-// FP32 -> FP64 widening with integer operations (exact for zero and normal
-// numbers; GB300's FP64 pipe is narrow, the integer pipe is not).
-__device__ __forceinline__ double widen(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xFFu;
-  if (e == 0u || e == 0xFFu) return (double)f;  // zero, subnormal, inf, nan
-  const unsigned long long d = ((unsigned long long)(u & 0x80000000u) << 32) |
-                               ((unsigned long long)(e + 896u) << 52) |
-                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
-  return __longlong_as_double((long long)d);
-}
-
 // Record of one particle at block-local offset u inside cell (i,j,k); returns
 // its kinetic energy 0.5 m W v^2 (FP32; summed per cell, then in FP64).
 __device__ __forceinline__ float stage_record(float* __restrict__ r, const float4* __restrict__ sB,

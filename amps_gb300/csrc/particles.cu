@@ -487,7 +487,7 @@ __constant__ unsigned char c_asm_corner[8];
 __global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __restrict__ nbr,
                                                   const float* __restrict__ cellM,
                                                   const float* __restrict__ cellJ, double inv_vol,
-                                                  double* __restrict__ M, double* __restrict__ J) {
+                                                  float* __restrict__ M, double* __restrict__ J) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncor) return;
   const int b = (int)(c / AMPS_CPB), l = (int)(c % AMPS_CPB);
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __r
 #pragma unroll
   for (int co = 0; co < 8; co++)
     cell[co] = local_id(nbr, b, i - (co & 1), j - ((co >> 1) & 1), k - ((co >> 2) & 1));
-  // sums of at most 8 FP32 partials per element, widened once to FP64
+  // sums of at most 8 FP32 partials per element (stored FP32)
   float acc[9];
   int cur = c_asm[0].slot;
 #pragma unroll
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __r
     if (en.slot != cur) {
 #pragma unroll
       for (int e = 0; e < 9; e++) {
-        M[(size_t)(cur * 9 + e) * ncor + c] = widen(acc[e]);
+        M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
         acc[e] = 0.f;
       }
       cur = en.slot;
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __r
     for (int e = 0; e < 9; e++) acc[e] += src[e];
   }
 #pragma unroll
-  for (int e = 0; e < 9; e++) M[(size_t)(cur * 9 + e) * ncor + c] = widen(acc[e]);
+  for (int e = 0; e < 9; e++) M[(size_t)(cur * 9 + e) * ncor + c] = acc[e];
   float jj[3] = {0.f, 0.f, 0.f};
 #pragma unroll
   for (int co = 0; co < 8; co++) {
@@ -620,15 +620,18 @@ __global__ void __launch_bounds__(256) k_rb_rank(long long n, const int* __restr
   }
 }
 
-// cap[c] = count + slack, slack = max(8, count/4) scaled by num/den so that
-// the total fits the slot capacity; cap[ncell] = 0 (scan terminator)
+// cap[c] = count + slack, slack = count/4 + AMPS_SLACK_MIN scaled by num/den so
+// that the total fits the slot capacity; cap[ncell] = 0 (scan terminator).
+// The constant term keeps sparsely filled cells (fine AMR levels) from
+// overflowing: a cell's occupancy random-walks by ~sqrt(2 x crossings) per
+// step, and over 10^5 cells the largest excursion reaches ~4.5 of those.
 __global__ void __launch_bounds__(256) k_rb_caps(long long ncell, const int* __restrict__ count,
                                                  int* __restrict__ cap, int num, int den) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c > ncell) return;
   if (c == ncell) { cap[c] = 0; return; }
   const int n = count[c];
-  const int slack = max(8, n >> 2);
+  const int slack = (n >> 2) + AMPS_SLACK_MIN;
   cap[c] = n + (int)(((long long)slack * num) / den);
 }
 
@@ -959,8 +962,8 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
     TimedLaunch t(c, "rebuild");
     k_rb_rank<<<grid_for(n, 256), 256, 0, s>>>(n, c->d_key, c->d_rank, c->d_count);
   }
-  // slack scaled so that sum(cap) <= slots: sum(cap) <= n + max(8 nc, n/4 + 8 nc)
-  const long long worst = n + std::max(8LL * nc, n / 4 + 8LL * nc);
+  // slack scaled so that sum(cap) <= slots: sum(cap) <= n + n/4 + AMPS_SLACK_MIN nc
+  const long long worst = n + n / 4 + (long long)AMPS_SLACK_MIN * nc;
   int num = 1, den = 1;
   if (worst > c->slots) {
     num = (int)std::max(0LL, (c->slots - n) / 1024);

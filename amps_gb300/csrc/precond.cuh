@@ -1,0 +1,49 @@
+// State of the learned preconditioner (precond.cu, precond_tc.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+struct amps_gpu_ctx;
+
+extern const int kWSize[3];  // weights per layer: 27*3*32, 27*32*32, 27*32*3
+
+struct PrecondState {
+  float* w[3] = {nullptr, nullptr, nullptr};  // FP32 masters [27][cin][cout]
+  float* g[3] = {nullptr, nullptr, nullptr};  // gradients
+  float* m[3] = {nullptr, nullptr, nullptr};  // Adam moments
+  float* v[3] = {nullptr, nullptr, nullptr};
+  long long adam_t = 0;
+  // BF16 operand images of the weights for the tensor-core kernel (one
+  // contiguous buffer, bulk-copied into shared memory per CTA)
+  uint16_t* wtc = nullptr;
+  bool tc_ready = false;
+  bool use_tc = false;
+  // harvested samples: sx[cap][1000][3], se[cap][512][3]
+  float* sx = nullptr;
+  float* se = nullptr;
+  long long cap = 0, n = 0;
+  // work buffers for S samples
+  int work_S = 0;
+  float *wx = nullptr, *we = nullptr, *h1 = nullptr, *h2 = nullptr, *y = nullptr;
+  float *dy = nullptr, *dh1 = nullptr, *dh2 = nullptr, *wt = nullptr;
+  int* perm = nullptr;
+  long long perm_n = 0;
+  double* dloss = nullptr;  // device loss accumulator
+  unsigned long long* flags = nullptr;  // the context's device flags ([2]: timeouts)
+};
+
+cudaError_t precond_work(PrecondState* P, int S);
+void precond_free(PrecondState* P);
+cudaError_t precond_forward32(PrecondState* P, cudaStream_t st, int S);
+cudaError_t precond_backward32(PrecondState* P, cudaStream_t st, int S, double* d_loss);
+cudaError_t precond_zero_grads(PrecondState* P, cudaStream_t st);
+cudaError_t precond_adam(PrecondState* P, cudaStream_t st, float lr);
+cudaError_t precond_gather_batch(PrecondState* P, cudaStream_t st, int S, long long first);
+cudaError_t precond_owned_out(PrecondState* P, cudaStream_t st, int S, float* out);
+// BF16 tcgen05 inference: x[S][1000][3] -> y[S][1000][3] (owned voxels)
+cudaError_t precond_prepare_tc(PrecondState* P, cudaStream_t st);
+cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const float* x, float* y);
+// GMRES hooks (field.cu)
+cudaError_t launch_precond_net(amps_gpu_ctx* c, const double* v, double* z);
+cudaError_t precond_harvest_pairs(amps_gpu_ctx* c, const double* r, const double* e, int e_scaled);

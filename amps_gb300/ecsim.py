@@ -322,6 +322,70 @@ class EcsimContext:
                     "push_deposit")
         return e.value
 
+    # ---- field-solve options and the learned preconditioner ----
+    def set_inner_fp64(self, on=True):
+        """GMRES inner operator in FP64 (True) or FP32 with FP64 refinement (False)."""
+        self._check(self.lib.amps_gpu_set_inner_fp64(self.h, 1 if on else 0), "set_inner_fp64")
+
+    def precond_load(self, w1, w2, w3):
+        ws = [np.ascontiguousarray(w, np.float32) for w in (w1, w2, w3)]
+        for w, shp in zip(ws, PRECOND_SHAPES):
+            if w.shape != shp:
+                raise ValueError("weight shape %s, expected %s" % (w.shape, shp))
+        self._check(self.lib.amps_gpu_precond_load(self.h, *[ptr(w, C.c_float) for w in ws]),
+                    "precond_load")
+
+    def precond_weights(self):
+        ws = [np.empty(shp, np.float32) for shp in PRECOND_SHAPES]
+        self._check(self.lib.amps_gpu_precond_get(self.h, *[ptr(w, C.c_float) for w in ws]),
+                    "precond_get")
+        return ws
+
+    def precond_use_tensor_cores(self, on=True):
+        self._check(self.lib.amps_gpu_precond_use_tensor_cores(self.h, 1 if on else 0),
+                    "precond_use_tensor_cores")
+
+    def precond_harvest(self, capacity):
+        self._check(self.lib.amps_gpu_precond_harvest(self.h, int(capacity)), "precond_harvest")
+
+    def precond_num_samples(self):
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_precond_num_samples(self.h, C.byref(n)), "num_samples")
+        return n.value
+
+    def precond_samples(self, first=0, count=None):
+        if count is None:
+            count = self.precond_num_samples() - first
+        x = np.empty((count, 1000, 3), np.float32)
+        e = np.empty((count, 512, 3), np.float32)
+        self._check(self.lib.amps_gpu_precond_get_samples(self.h, first, count, ptr(x, C.c_float),
+                                                          ptr(e, C.c_float)), "get_samples")
+        return x, e
+
+    def precond_train(self, epochs, batch=64, lr=1e-3, seed=1):
+        loss = np.zeros(epochs, np.float32)
+        self._check(self.lib.amps_gpu_precond_train(self.h, epochs, batch, lr, seed,
+                                                    ptr(loss, C.c_float)), "precond_train")
+        return loss
+
+    def precond_loss_grad(self, x, e):
+        x = np.ascontiguousarray(x, np.float32)
+        e = np.ascontiguousarray(e, np.float32)
+        g = [np.empty(shp, np.float32) for shp in PRECOND_SHAPES]
+        loss = C.c_float()
+        self._check(self.lib.amps_gpu_precond_loss_grad(
+            self.h, len(x), ptr(x, C.c_float), ptr(e, C.c_float), C.byref(loss),
+            *[ptr(q, C.c_float) for q in g]), "precond_loss_grad")
+        return loss.value, g
+
+    def precond_forward(self, x, tensor_cores=False):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.empty((len(x), 512, 3), np.float32)
+        self._check(self.lib.amps_gpu_precond_forward(self.h, len(x), ptr(x, C.c_float),
+                                                      1 if tensor_cores else 0, ptr(y, C.c_float)),
+                    "precond_forward")
+        return y
+
     # ---- timing ----
     def set_kernel_timing(self, on=True):
         self._check(self.lib.amps_gpu_set_kernel_timing(self.h, 1 if on else 0), "timing")
@@ -339,6 +403,22 @@ class EcsimContext:
                                                        cnt.ctypes.data_as(C.POINTER(C.c_longlong)),
                                                        cap, C.byref(n)), "kernel times")
         return {names[i].decode(): (float(ms[i]), int(cnt[i])) for i in range(n.value)}
+
+
+PRECOND_SHAPES = ((27, 3, 32), (27, 32, 32), (27, 32, 3))
+
+
+def init_precond_weights(seed=0, out_scale=1e-3):
+    """Seeded initial weights of the block network: layers 1-2 scaled by
+    1/sqrt(fan-in), the output layer by out_scale/sqrt(fan-in) so that the
+    untrained preconditioner is Jacobi plus a small correction."""
+    rng = np.random.default_rng(seed)
+    ws = []
+    for l, shp in enumerate(PRECOND_SHAPES):
+        fan = shp[0] * shp[1]
+        sc = (out_scale if l == 2 else 1.0) / np.sqrt(fan)
+        ws.append((sc * rng.standard_normal(shp)).astype(np.float32))
+    return ws
 
 
 def trace_dipole(x, p, q, m0, b_eq, r_e, b_ext, r_in, r_out, max_steps, dphi_max=0.15,

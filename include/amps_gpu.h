@@ -188,7 +188,10 @@ amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* ctx, double* particl
 /* ECSIM::TimeStep (pic_field_solver_ecsim.cpp:6179): RHS, GMRES solve for
  * E^{n+theta} = E^n + dE (x0 = 0, stop when ||b-Ax|| <= tol ||b||, restart 30),
  * UpdateB, InterpolateB_C2N, UpdateE.  precond: 0 none (the reference's
- * PrecondParam = 0), 1 Jacobi. */
+ * PrecondParam = 0), 1 Jacobi, 2 the learned block network loaded with
+ * amps_gpu_precond_load (uniform meshes; Jacobi-scaled input, flexible GMRES).
+ * Each restart cycle begins from the FP64 residual b - A x; the Arnoldi steps
+ * apply the operator in FP32 unless amps_gpu_set_inner_fp64 switched that off. */
 amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* ctx, double tol, int maxit, int precond,
                                      amps_gpu_solve_stats* stats);
 /* One PIC::TimeStep of the ECSIM track (pic_time_step.cpp:403-551): field
@@ -198,6 +201,49 @@ amps_gpu_status amps_gpu_step(amps_gpu_ctx* ctx, double tol, int maxit, int prec
                               amps_gpu_step_stats* stats);
 /* Particle push + re-bin + deposit only (the particle-steps/s hot path). */
 amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* ctx, double* particle_energy);
+/* GMRES inner operator precision: 0 FP32 arithmetic with FP64 refinement at
+ * each restart (default), 1 FP64 throughout.  No reference counterpart (the
+ * reference's solve is FP64). */
+amps_gpu_status amps_gpu_set_inner_fp64(amps_gpu_ctx* ctx, int fp64);
+
+/* ---- learned right preconditioner for the field solve (no reference
+ *      counterpart: the reference's GMRES takes PrecondParam 0/1 only) ----
+ * Network, per mesh block: input x = D r (Jacobi-scaled residual) on the
+ * block's 8^3 owned corners plus a 1-corner halo (10^3 corners, 3 channels),
+ * three 3x3x3 convolutions 3 -> 32 -> 32 -> 3 with zero padding at the halo
+ * edge and no activation, output on the owned corners; z = x + N(x).
+ * Weights: w1[27][3][32], w2[27][32][32], w3[27][32][3] (tap t = (dx+1) +
+ * 3(dy+1) + 9(dz+1), then input channel, then output channel), FP32 masters,
+ * BF16 copies for inference.  Training pairs come from the Jacobi field solves
+ * themselves (harvest on): each Arnoldi step's (r = A e, e) and the final
+ * (b, x), cut into blocks and normalised by the RMS of D r over the block. */
+amps_gpu_status amps_gpu_precond_load(amps_gpu_ctx* ctx, const float* w1, const float* w2,
+                                      const float* w3);
+amps_gpu_status amps_gpu_precond_get(amps_gpu_ctx* ctx, float* w1, float* w2, float* w3);
+/* inference path used inside the field solve: 1 BF16 tcgen05 kernel, 0 FP32
+ * training forward (default after load: 0) */
+amps_gpu_status amps_gpu_precond_use_tensor_cores(amps_gpu_ctx* ctx, int on);
+/* enable (capacity > 0: keep up to capacity block samples) or stop harvesting */
+amps_gpu_status amps_gpu_precond_harvest(amps_gpu_ctx* ctx, long long capacity);
+amps_gpu_status amps_gpu_precond_num_samples(amps_gpu_ctx* ctx, long long* n);
+/* read samples [first, first+count): x[count][1000][3] (halo region, z-major:
+ * index (k*10 + j)*10 + i for block corner (i-1, j-1, k-1)), e[count][512][3] */
+amps_gpu_status amps_gpu_precond_get_samples(amps_gpu_ctx* ctx, long long first, long long count,
+                                             float* x, float* e);
+/* Adam on the harvested samples (mini-batches of `batch` blocks, shuffled with
+ * `seed`); loss = mean over owned corners and channels of (x + N(x) - e)^2.
+ * loss_out[epochs] receives the mean loss of every epoch. */
+amps_gpu_status amps_gpu_precond_train(amps_gpu_ctx* ctx, int epochs, int batch, float lr,
+                                       unsigned long long seed, float* loss_out);
+/* Loss and weight gradients of the current weights on given samples (host
+ * arrays in the get_samples layout), computed by the training kernels. */
+amps_gpu_status amps_gpu_precond_loss_grad(amps_gpu_ctx* ctx, long long count, const float* x,
+                                           const float* e, float* loss, float* g1, float* g2,
+                                           float* g3);
+/* N(x) on given samples by the inference path (tensor_cores 1: BF16 tcgen05
+ * kernel; 0: the FP32 training forward).  y[count][512][3]. */
+amps_gpu_status amps_gpu_precond_forward(amps_gpu_ctx* ctx, long long count, const float* x,
+                                         int tensor_cores, float* y);
 
 /* ---- deposition for callers that may not allocate device memory ----
  * No counterpart in the reference: a variant of UpdateJMassMatrix for a host
