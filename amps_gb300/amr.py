@@ -183,6 +183,13 @@ AMR_WORKLOADS = {
     # 64^3 base cells in 8^3 blocks, central 1/8 of the volume refined 2x,
     # 128 particles per species per base cell (67,108,864 particles)
     "amr_64c_128ppc": lambda: AmrWorkload("amr_64c_128ppc", (8, 8, 8), 1, 0, 0.5, 128),
-    # the same recipe at 32^3 base cells and 16 ppc (small case: tests, profiles)
+    # the same recipe at 32^3 base cells and 16 ppc (small case: tests)
     "amr_32c_16ppc": lambda: AmrWorkload("amr_32c_16ppc", (4, 4, 4), 1, 0, 0.5, 16),
+    # the 64^3 mesh at 32 ppc (16.8M particles, 0.8 GB of particle state: larger
+    # than L2, small enough for full profiler captures)
+    "amr_64c_32ppc": lambda: AmrWorkload("amr_64c_32ppc", (8, 8, 8), 1, 0, 0.5, 32),
+    # three levels, 256^3 effective cells: level 2 inside a central sphere of
+    # radius 0.2 box lengths, level 1 inside radius 0.4; 64 particles per
+    # species per base-cell volume (8 per level-1 cell, 1 per level-2 cell)
+    "amr_256e_3lvl": lambda: AmrWorkload("amr_256e_3lvl", (8, 8, 8), 2, 1, 0.4, 64),
 }

@@ -185,9 +185,13 @@ __global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a, T* __restrict_
   scatter<T>(y, a.nvc, cid, out, a.h);
 }
 
-// FP32 accumulation -> FP64 operator output (free rows); hanging rows get the
-// constraint x_h - (P x)_h in FP64
+// Free rows: the identity part S (D x) in FP64 (S = P^T diag(sum of V/8) P,
+// mostly diagonal, CSR) plus the FP32 accumulation of the other terms.
+// Hanging rows: the constraint x_h - (P x)_h in FP64.
 __global__ void __launch_bounds__(256) k_amr_finish32(long long nvc, Hang h,
+                                                      const int* __restrict__ ss,
+                                                      const int* __restrict__ sc,
+                                                      const double* __restrict__ sv,
                                                       const float* __restrict__ y32,
                                                       const double* __restrict__ x,
                                                       const double* __restrict__ dinv,
@@ -198,7 +202,12 @@ __global__ void __launch_bounds__(256) k_amr_finish32(long long nvc, Hang h,
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (s == e) {
-      y[d * nvc + c] = (double)y32[d * nvc + c];
+      double acc = (double)y32[d * nvc + c];
+      for (int q = ss[c]; q < ss[c + 1]; q++) {
+        const int col = sc[q];
+        acc += sv[q] * (dinv ? dinv[d * nvc + col] : 1.0) * x[d * nvc + col];
+      }
+      y[d * nvc + c] = acc;
     } else {
       double pv = 0.0;
       for (int t = s; t < e; t++) {
@@ -449,11 +458,13 @@ cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* 
   ApplyArgs a = apply_args(c);
   a.x = x;
   a.dinv = dinv;
-  a.with_identity = a.with_curl = a.with_mass = 1;
+  a.with_identity = 0;  // the identity part is applied in FP64 by k_amr_finish32
+  a.with_curl = a.with_mass = 1;
   a.rhs_mode = 0;
   TimedLaunch t(c, "matvec32", 2);
   k_amr_cell_op<float><<<g1(c->ncor), 256, 0, c->stream>>>(a, c->d_y32);
-  k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_y32, x, dinv, y);
+  k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_sv,
+                                                     c->d_y32, x, dinv, y);
   return cudaGetLastError();
 }
 

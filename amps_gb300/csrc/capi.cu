@@ -435,6 +435,54 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
        upload(&c->d_fine_map, m->fine_map) && upload(&c->d_borg, borg) &&
        upload(&c->d_bscale, bscale) && upload(&c->d_bdx, bdx) && upload(&c->d_bdtdx, bdtdx) &&
        upload(&c->d_binvvol, binvvol);
+  // identity part of the operator, S = P^T diag(D) P with D(corner) = sum over
+  // its cells of V/8: rows of free corners (hanging rows are constraints)
+  {
+    std::vector<double> D((size_t)nv, 0.0);
+    for (long long b = 0; b < nbl; b++) {
+      const double v8 = 0.125 * bdx[(size_t)b] * bdx[(size_t)b] * bdx[(size_t)b];
+      for (int l = 0; l < 512; l++) {
+        const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
+        for (int q = 0; q < 8; q++) {
+          const int ci = i + (q & 1), cj = j + ((q >> 1) & 1), ck = k + (q >> 2);
+          D[(size_t)m->corner_tab[(size_t)b * 729 + ci + 9 * (cj + 9 * ck)]] += v8;
+        }
+      }
+    }
+    std::vector<std::vector<std::pair<int, double>>> rows((size_t)nv);
+    auto add = [&](int r, int col, double v) {
+      for (auto& e : rows[(size_t)r])
+        if (e.first == col) {
+          e.second += v;
+          return;
+        }
+      rows[(size_t)r].emplace_back(col, v);
+    };
+    const auto& hs = m->hang_start;
+    for (long long cc = 0; cc < nv; cc++) {
+      const int s0 = hs[(size_t)cc], s1 = hs[(size_t)cc + 1];
+      if (s0 == s1) {
+        add((int)cc, (int)cc, D[(size_t)cc]);
+      } else {
+        for (int a = s0; a < s1; a++)
+          for (int b2 = s0; b2 < s1; b2++)
+            add(m->hang_parent[(size_t)a], m->hang_parent[(size_t)b2],
+                D[(size_t)cc] * m->hang_weight[(size_t)a] * m->hang_weight[(size_t)b2]);
+      }
+    }
+    std::vector<int> ss((size_t)nv + 1, 0), sc;
+    std::vector<double> sv;
+    for (long long r = 0; r < nv; r++) {
+      ss[(size_t)r] = (int)sc.size();
+      if (hs[(size_t)r + 1] > hs[(size_t)r]) continue;  // constraint row
+      for (auto& e : rows[(size_t)r]) {
+        sc.push_back(e.first);
+        sv.push_back(e.second);
+      }
+    }
+    ss[(size_t)nv] = (int)sc.size();
+    ok = ok && upload(&c->d_ss, ss) && upload(&c->d_sc, sc) && upload(&c->d_sv, sv);
+  }
   if (!ok) {
     cudaGetLastError();
     amps_gpu_destroy(c);
@@ -473,7 +521,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw,
-                  c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol};
+                  c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol,
+                  c->d_ss, c->d_sc, c->d_sv};
   for (void* p : ptrs) cudaFree(p);
   for (int b = 0; b < 2; b++) {
     for (int q = 0; q < 3; q++) {

@@ -72,6 +72,9 @@ struct amps_gpu_ctx {
   double* d_bdx = nullptr;    // nb cell sizes
   float* d_bdtdx = nullptr;   // dt/dx per block
   float* d_binvvol = nullptr; // 1/dx^3 per block
+  int* d_ss = nullptr;        // identity part of the AMR operator, CSR rows (nvc+1)
+  int* d_sc = nullptr;        //   columns
+  double* d_sv = nullptr;     //   values
 
   // fields (FP64, component-major)
   double* d_En = nullptr;

@@ -316,7 +316,13 @@ template <int CIN, int COUT>
 cudaError_t conv(PrecondState* P, cudaStream_t st, int S, const float* in, const float* W,
                  float* out, int owned_only) {
   const size_t sm = conv_smem<CIN, COUT>();
-  cudaFuncSetAttribute(k_conv<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  static unsigned long long attr_set = 0;  // per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!((attr_set >> dev) & 1ull)) {
+    cudaFuncSetAttribute(k_conv<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr_set |= 1ull << dev;
+  }
   k_conv<CIN, COUT><<<dim3(kR, S), 256, sm, st>>>(in, W, out, owned_only);
   return cudaGetLastError();
 }
@@ -437,14 +443,21 @@ cudaError_t launch_precond_net(amps_gpu_ctx* c, const double* v, double* z) {
   if (!P) return cudaErrorInvalidValue;
   cudaError_t e = precond_work(P, c->nb);
   if (e != cudaSuccess) return e;
-  TimedLaunch t(c, "precond_net", 5);
-  k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, v, c->d_dinv, P->wx);
+  {
+    TimedLaunch t(c, "precond_gather");
+    k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, v, c->d_dinv, P->wx);
+  }
   if (P->use_tc) {
+    TimedLaunch t(c, "precond_net_tc");
     if ((e = precond_forward_tc(P, c->stream, c->nb, P->wx, P->y)) != cudaSuccess) return e;
   } else {
+    TimedLaunch t(c, "precond_net_fp32", 3);
     if ((e = precond_forward32(P, c->stream, c->nb)) != cudaSuccess) return e;
   }
-  k_scatter_z<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, P->wx, P->y, z);
+  {
+    TimedLaunch t(c, "precond_scatter");
+    k_scatter_z<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, P->wx, P->y, z);
+  }
   return cudaGetLastError();
 }
 
@@ -612,6 +625,8 @@ amps_gpu_status amps_gpu_precond_train(amps_gpu_ctx* c, int epochs, int batch, f
   std::vector<int> perm((size_t)P->n);
   std::iota(perm.begin(), perm.end(), 0);
   const long long nbatch = P->n / S;
+  const double total = (double)epochs * (double)nbatch;
+  long long step = 0;
   for (int ep = 0; ep < epochs; ep++) {
     std::shuffle(perm.begin(), perm.end(), rng);
     er = cudaMemcpyAsync(P->perm, perm.data(), sizeof(int) * P->n, cudaMemcpyHostToDevice, st);
@@ -621,7 +636,9 @@ amps_gpu_status amps_gpu_precond_train(amps_gpu_ctx* c, int epochs, int batch, f
       if ((er = precond_gather_batch(P, st, S, bi * S)) != cudaSuccess) break;
       if ((er = precond_zero_grads(P, st)) != cudaSuccess) break;
       if ((er = precond_backward32(P, st, S, P->dloss)) != cudaSuccess) break;
-      er = precond_adam(P, st, lr);
+      // cosine decay of the learning rate to 1% over the run
+      const double ph = (double)(step++) / total;
+      er = precond_adam(P, st, (float)(lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(3.14159265358979 * ph)))));
     }
     double lsum = 0.0;
     if (er == cudaSuccess)
@@ -672,8 +689,10 @@ amps_gpu_status amps_gpu_precond_forward(amps_gpu_ctx* c, long long count, const
   cudaError_t er;
   if (tensor_cores) {
     if (!P->tc_ready) return set_err(c, AMPS_GPU_INVALID_ARG, "precond_forward: tensor-core path not ready");
+    TimedLaunch t(c, "precond_forward_tc");
     er = precond_forward_tc(P, st, (int)count, P->wx, P->y);
   } else {
+    TimedLaunch t(c, "precond_forward_fp32", 3);
     er = precond_forward32(P, st, (int)count);
   }
   if (er == cudaSuccess) er = precond_owned_out(P, st, (int)count, P->dh1);

@@ -165,19 +165,27 @@ __global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__
     const int NG = N / 8;
     const uint32_t wbase = w_s + (L == 0 ? 0 : (L == 1 ? kW1 : kW1 + kW2));
     if (tid == 0) {
+      // taps outer, tiles inner: consecutive MMAs write different accumulators
       const uint32_t id = idesc_bf16(N);
-      for (int tile = 0; tile < kTiles; tile++) {
-        const uint32_t d = tmem + (uint32_t)(tile * N);
-        for (int t = 0; t < 27; t++) {
-          const int off = (t % 3 - 1) + 12 * ((t / 3) % 3 - 1) + 144 * (t / 9 - 1);
-          const uint32_t row0 = (uint32_t)(kMBegin + tile * 128 + off);
-          for (int ks = 0; ks < NQ / 2; ks++) {
-            const uint64_t ad = sdesc(act_s + (uint32_t)(2 * ks) * kPlane + row0 * 16u, kPlane, 128);
-            const uint64_t bd =
-                sdesc(wbase + (uint32_t)((t * NQ + 2 * ks) * NG) * 128u, (uint32_t)NG * 128u, 128);
-            mma_bf16(d, ad, bd, id, (t | ks) != 0 ? 1u : 0u);
+      const uint64_t adesc0 = sdesc(0, kPlane, 128);
+      const uint64_t bdesc0 = sdesc(0, (uint32_t)NG * 128u, 128);
+      int off = -157;  // tap (-1,-1,-1)
+      for (int t = 0; t < 27; t++) {
+        for (int ks = 0; ks < NQ / 2; ks++) {
+          const uint64_t bd = bdesc0 | (uint64_t)(((wbase + (uint32_t)((t * NQ + 2 * ks) * NG) * 128u) >> 4) & 0x3FFFu);
+          uint32_t a_addr = act_s + (uint32_t)(2 * ks) * kPlane + (uint32_t)(kMBegin + off) * 16u;
+          const uint32_t acc = (t | ks) != 0 ? 1u : 0u;
+#pragma unroll 4
+          for (int tile = 0; tile < kTiles; tile++) {
+            const uint64_t ad = adesc0 | (uint64_t)((a_addr >> 4) & 0x3FFFu);
+            mma_bf16(tmem + (uint32_t)(tile * N), ad, bd, id, acc);
+            a_addr += 128u * 16u;
           }
         }
+        // next tap: x fastest, then y, then z
+        off += 1;
+        if (t % 3 == 2) off += 12 - 3;
+        if (t % 9 == 8) off += 144 - 36;
       }
       mma_commit(&bar[0]);
     }
@@ -281,8 +289,14 @@ cudaError_t precond_prepare_tc(PrecondState* P, cudaStream_t st) {
 
 cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const float* x, float* y) {
   if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_precond_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-  if (e != cudaSuccess) return e;
+  static unsigned long long attr_set = 0;  // per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!((attr_set >> dev) & 1ull)) {
+    cudaError_t e = cudaFuncSetAttribute(k_precond_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    if (e != cudaSuccess) return e;
+    attr_set |= 1ull << dev;
+  }
   k_precond_tc<<<S, 128, kSmem, st>>>(x, y, P->wtc, P->flags);
   return cudaGetLastError();
 }

@@ -314,6 +314,101 @@ def setup_workload(name, device, track_ids=False):
     return ctx, info
 
 
+def precond_ab(workload, device, nsamples=20000, epochs=20, lr=2e-3, dt=None, reps=3):
+    """Learned vs plain vs Jacobi GMRES on one uniform workload: train the block
+    network on nsamples pairs harvested from Jacobi solves of seeded plasma
+    states, then time the field solve and the full ECSIM step from identical
+    held-out states (host wall clock around calls that synchronise)."""
+    import amps_gb300 as A
+    from amps_gb300 import precond as PC
+    wl = A.WORKLOADS[workload]()
+    if dt is not None:
+        wl.dt = dt
+    ctx, info = PC.build_trained_context(wl, nsamples=nsamples, epochs=epochs, batch=64, lr=lr,
+                                         device=device, e_amp=1e-3, b_amp=0.02)
+    ctx.precond_use_tensor_cores(True)
+    names = {0: "plain", 1: "jacobi", 2: "learned"}
+    solve = {k: [] for k in names.values()}
+    step = {k: [] for k in names.values()}
+    iters = {k: [] for k in names.values()}
+    for seed in (5001, 5002, 5003):
+        PC.random_state(ctx, wl, seed, e_amp=1e-3, b_amp=0.02)
+        ctx.PicTimeStep(tol=wl.tol, maxit=400, precond=1)   # evolve once from the seeded state
+        f0 = ctx.export_fields()
+        p0 = ctx.export_particles(ids=False)
+        for pc, nm in names.items():
+            ts, tp = [], []
+            for _ in range(reps):
+                ctx.import_fields(**f0)
+                ctx.synchronize()
+                t = time.perf_counter()
+                st = ctx.TimeStep(tol=wl.tol, maxit=400, precond=pc)
+                ctx.synchronize()
+                ts.append((time.perf_counter() - t) * 1e3)
+                if not st.converged:
+                    raise RuntimeError("%s solve did not converge" % nm)
+            iters[nm].append(st.iterations)
+            for _ in range(reps):
+                ctx.import_particles(p0["x"], p0["v"], p0["spec"])
+                ctx.import_fields(**f0)
+                ctx.UpdateJMassMatrix()
+                ctx.synchronize()
+                t = time.perf_counter()
+                ctx.PicTimeStep(tol=wl.tol, maxit=400, precond=pc)
+                ctx.synchronize()
+                tp.append((time.perf_counter() - t) * 1e3)
+            solve[nm].append(min(ts))
+            step[nm].append(min(tp))
+    ctx.close()
+    med = lambda v: float(np.median(v))
+    out = {"workload": workload, "dt": wl.dt, "tol": wl.tol, "pairs": info["samples"],
+           "solves_harvested": info["solves"], "train_seconds": round(info["train_seconds"], 2),
+           "loss_first_last": [info["loss"][0], info["loss"][-1]],
+           "gmres_iterations": {k: iters[k] for k in iters},
+           "field_solve_ms": {k: round(med(v), 3) for k, v in solve.items()},
+           "ecsim_step_ms": {k: round(med(v), 3) for k, v in step.items()},
+           "inference": "BF16 tcgen05 kernel, FP32 accumulate; flexible GMRES"}
+    out["step_speedup_learned_vs_plain"] = round(out["ecsim_step_ms"]["plain"] /
+                                                 out["ecsim_step_ms"]["learned"], 3)
+    out["step_speedup_learned_vs_jacobi"] = round(out["ecsim_step_ms"]["jacobi"] /
+                                                  out["ecsim_step_ms"]["learned"], 3)
+    return out
+
+
+def run_precond_kernel(args):
+    """Inference of the block network alone (BF16 tcgen05 kernel) on
+    args.precond_kernel random blocks: FLOP rate against the dense bf16 peak."""
+    import amps_gb300 as A
+    ws, rank, local = dist_env()
+    wl = A.electron_proton_plasma("precond_kernel", 1, 1, 1, 1, 1)
+    ctx = A.EcsimContext(wl, capacity=16, track_ids=False, device=local)
+    ctx.precond_load(*A.init_precond_weights(seed=3, out_scale=1.0))
+    rng = np.random.default_rng(1)
+    S = args.precond_kernel
+    x = rng.standard_normal((S, 1000, 3)).astype(np.float32)
+    ctx.set_kernel_timing(True)
+    for _ in range(args.warmup):
+        ctx.precond_forward(x, tensor_cores=True)
+    ctx.reset_kernel_times()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.precond_forward(x, tensor_cores=True)
+    wall = time.perf_counter() - t0
+    kt = ctx.kernel_times()
+    ms, n = kt.get("precond_forward_tc", (float("nan"), 1))
+    # useful FLOP per block (padded GEMM rows not counted): 2 x voxels x taps x cin x cout
+    flop = 2 * 27 * (1000 * 3 * 32 + 1000 * 32 * 32 + 512 * 32 * 3)
+    tflops = S * flop / (ms / n / 1e3) / 1e12
+    d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = d.get("bf16_tflops", 1900.0)
+    print(json.dumps({"metric": "precond inference (BF16 tcgen05)", "blocks": S, "steps": args.steps,
+                      "kernel_ms_per_launch": ms / n, "useful_tflops": tflops,
+                      "bf16_peak_tflops": peak, "frac": tflops / peak,
+                      "wall_ms_per_call": wall * 1e3 / args.steps}), flush=True)
+    ctx.close()
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import amps_gb300 as A
@@ -415,6 +510,11 @@ def run_gpu(args):
             smp = "FP64 oracle Lapenta2017+ProcessCell on a periodic 8^3-cell replica of the " \
                   "same plasma (%d particles), %.1f s" % (ci["replica_particles"], ci["seconds"])
         cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp}
+    pab = None
+    if rank == 0 and args.precond_ab:
+        pab = {"config": precond_ab("ecsim_32c_64ppc", local)}
+        if args.precond_stiff:
+            pab["stiff_dt_1_over_wpe"] = precond_ab("ecsim_32c_64ppc", local, dt=1.0)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -427,6 +527,7 @@ def run_gpu(args):
                 "ecsim_step_ms": round(min(t_step), 3), "gmres_iterations": gmres_it,
                 "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations}),
             "e2e": e2e, "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
+            "precond_ab": pab,
             "clocks": clocks, "gpu_launches": gpu_launches,
         }
         print(json.dumps(line), flush=True)
@@ -479,6 +580,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--precond-ab", type=int, default=1,
+                    help="learned vs plain vs Jacobi GMRES on the 32^3 plasma (1 = on)")
+    ap.add_argument("--precond-stiff", type=int, default=1,
+                    help="also the same A/B at dt = 1/omega_pe")
+    ap.add_argument("--precond-kernel", type=int, default=0,
+                    help="time only the tensor-core inference kernel on this many blocks")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the top kernel from an ncu capture")
     args = ap.parse_args()
@@ -486,6 +593,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.precond_kernel > 0:
+        run_precond_kernel(args)
     else:
         run_gpu(args)
 
