@@ -186,7 +186,7 @@ __device__ __forceinline__ void lapenta(float h, const float E[3], const float B
 }
 
 template <bool DEP, bool AMR>
-__global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
+__global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
   float4* s_push = s_dyn;                         // 729 x 2 float4
   float4* s_dep = s_dyn + 2 * AMPS_SC;            // 729 float4
@@ -215,19 +215,32 @@ __global__ void __launch_bounds__(256) k_push_deposit(StepArgs a) {
     float en_cell = 0.f;
     tile.zero();
     int nst = 0;
+    // software pipeline: the next chunk's particles are loaded while this one
+    // is processed (its slots lie above every slot this chunk writes)
+    float pu[3] = {0.f, 0.f, 0.f}, pv[3] = {0.f, 0.f, 0.f};
+    int ps = 0;
+    float pwc = 1.0f;
+    uint32_t pid = 0;
+    auto prefetch = [&](int q) {
+      if (q < n0) {
+        const int pn = b0 + q;
+#pragma unroll
+        for (int d = 0; d < 3; d++) { pu[d] = a.p.u[d][pn]; pv[d] = a.p.v[d][pn]; }
+        ps = a.p.sp[pn];
+        pwc = a.p.wc ? a.p.wc[pn] : 1.0f;
+        pid = a.p.id ? a.p.id[pn] : 0u;
+      }
+    };
+    prefetch(lane);
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const int p = b0 + q0 + lane;
       const bool act = q0 + lane < n0;
-      float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
-      int s = 0, key = -1;
-      float wcv = 1.0f;
-      uint32_t idv = 0;
+      float u[3] = {pu[0], pu[1], pu[2]}, v[3] = {pv[0], pv[1], pv[2]};
+      int s = ps, key = -1;
+      float wcv = pwc;
+      uint32_t idv = pid;
+      prefetch(q0 + 32 + lane);
       if (act) {
-#pragma unroll
-        for (int d = 0; d < 3; d++) { u[d] = a.p.u[d][p]; v[d] = a.p.v[d][p]; }
-        s = a.p.sp[p];
-        if (a.p.wc) wcv = a.p.wc[p];
-        if (a.p.id) idv = a.p.id[p];
         // gather E^{n+theta}, B^n at the old position
         int ic[3];
         float f[3];

@@ -12,14 +12,18 @@
 // offset = plane size).  Rows 157 .. 1692 (12 tiles of 128) cover every voxel
 // of R; rows outside R are computed and dropped.
 //
-// Per layer one thread issues 12 tiles x 27 taps x (K/16) MMAs of 128 x N x 16
-// into tensor memory (N = 32, or 16 for the 3-channel output layer), commits
-// them to an mbarrier, and the four warps read their 32 accumulator lanes back
-// (tcgen05.ld), convert to BF16 and overwrite the activation planes in place
-// (zero on the ring), or write the owned voxels' FP32 output.
-// Shared memory: 4 activation planes (110,592 B) + the three layers' BF16
-// weight images (110,592 B, one bulk copy); tensor memory: 512 columns.
-// Every wait is bounded; a timeout is counted in flags[2].
+// A cluster of two CTAs serves one mesh block; each keeps the whole activation
+// buffer and computes 6 of the 12 tiles.  Per layer one thread of each CTA
+// issues 6 tiles x 27 taps x (K/16) MMAs of 128 x N x 16 into tensor memory
+// (N = 32, or 16 for the 3-channel output layer), commits them to an mbarrier,
+// and the four warps read their 32 accumulator lanes back (tcgen05.ld),
+// convert to BF16 and write the rows into both CTAs' activation planes
+// (distributed shared memory; zero on the ring), or write the owned voxels'
+// FP32 output.  A cluster barrier separates the layers.
+// Shared memory per CTA: 4 activation planes (110,592 B) + the three layers'
+// BF16 weight images (110,592 B, one bulk copy); tensor memory: 256 columns.
+// Every mbarrier wait is bounded; a timeout is counted in flags[2] and the CTA
+// still takes part in every cluster barrier, so its peer never waits on it.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -34,12 +38,14 @@ constexpr int kPlane = kPadV * 16;          // bytes per 8-channel BF16 plane
 constexpr int kActBytes = 4 * kPlane;       // 110,592
 constexpr int kMBegin = 157;                // padded voxel (1,1,1)
 constexpr int kTiles = 12;                  // rows kMBegin .. kMBegin + 1535
+constexpr int kSplit = 2;                   // CTAs (cluster) per mesh block
+constexpr int kMyTiles = kTiles / kSplit;
 constexpr int kW1 = 27 * 2 * 4 * 128;       // K 16 (3 used), N 32
 constexpr int kW2 = 27 * 4 * 4 * 128;       // K 32, N 32
 constexpr int kW3 = 27 * 4 * 2 * 128;       // K 32, N 16 (3 used)
 constexpr int kWBytes = kW1 + kW2 + kW3;    // 110,592
 constexpr int kSmem = kActBytes + kWBytes + 64;
-constexpr int kTmemCols = 512;
+constexpr int kTmemCols = 256;             // kMyTiles x 32 columns
 constexpr uint32_t kWait = 1u << 24;
 
 // shared-memory matrix descriptor: no swizzle, K-major
@@ -82,17 +88,46 @@ __device__ __forceinline__ void fence_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
-  uint32_t r[16];
+// 16 consecutive accumulator columns of this warp's 32 lanes; the registers are
+// valid only after tmem_wait() and reg_fence16()
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t r[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
         "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+// orders every use of r after the preceding tmem_wait()
+__device__ __forceinline__ void reg_fence16(uint32_t r[16]) {
+  asm volatile(""
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]));
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// shared::cluster address of the same offset in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t peer_addr(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, uint4 v) {
+  asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y),
+               "r"(v.z), "r"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
@@ -108,7 +143,8 @@ __device__ __forceinline__ bool interior(int p, int& i, int& j, int& k) {
   return px >= 1 && px <= 10 && py >= 1 && py <= 10 && pz >= 1 && pz <= 10;
 }
 
-__global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__ x,
+__global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
+    k_precond_tc(const float* __restrict__ x,
                                                        float* __restrict__ y,
                                                        const uint16_t* __restrict__ wimg,
                                                        unsigned long long* __restrict__ flags) {
@@ -117,7 +153,9 @@ __global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__
   uint8_t* wsm = smem + kActBytes;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kActBytes + kWBytes);  // [0] mma, [1] weights
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
-  const int s = blockIdx.x;
+  const int s = blockIdx.x / kSplit;
+  const uint32_t rank = cluster_rank(), peer = rank ^ 1u;
+  const int tile0 = (int)rank * kMyTiles;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
@@ -142,29 +180,49 @@ __global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__
   }
   // layer-1 input: channels 0..2 of plane 0
   const float* xs = x + (size_t)s * 1000 * 3;
-  for (int v = tid; v < 1000; v += blockDim.x) {
-    const int i = v % 10, j = (v / 10) % 10, k = v / 100;
-    const int p = (k + 1) * 144 + (j + 1) * 12 + (i + 1);
-    uint4 q;
-    q.x = pack_bf16(xs[3 * v], xs[3 * v + 1]);
-    q.y = pack_bf16(xs[3 * v + 2], 0.f);
-    q.z = 0u;
-    q.w = 0u;
-    *reinterpret_cast<uint4*>(act + (size_t)p * 16) = q;
+  {
+    constexpr int kPer = (1000 + 127) / 128;
+    float xv[kPer][3];
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+      const int v = tid + q * 128;
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) xv[q][ch] = v < 1000 ? __ldg(xs + 3 * v + ch) : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < kPer; q++) {
+      const int v = tid + q * 128;
+      if (v < 1000) {
+        const int i = v % 10, j = (v / 10) % 10, k = v / 100;
+        const int p = (k + 1) * 144 + (j + 1) * 12 + (i + 1);
+        uint4 w4;
+        w4.x = pack_bf16(xv[q][0], xv[q][1]);
+        w4.y = pack_bf16(xv[q][2], 0.f);
+        w4.z = 0u;
+        w4.w = 0u;
+        *reinterpret_cast<uint4*>(act + (size_t)p * 16) = w4;
+      }
+    }
   }
+  // both CTAs' buffers are initialised before either writes into the other's
+  cluster_sync();
   fence_async_smem();
   __syncthreads();
-  bool ok = mbar_wait_bounded(&bar[1], 0, kWait);
+  // CTA-uniform status: the warp-collective tcgen05.ld below needs it
+  bool ok = __syncthreads_and(mbar_wait_bounded(&bar[1], 0, kWait)) != 0;
   tc_fence_after();
   const uint32_t tmem = *tslot;
   const uint32_t act_s = smem_u32(act), w_s = smem_u32(wsm);
+  const uint32_t act_peer = peer_addr(act_s, peer);
+  uint32_t mma_phase = 0;
+  bool mma_pending = false;
 
-  for (int L = 0; L < 3 && ok; L++) {
+  for (int L = 0; L < 3; L++) {
     const int N = L < 2 ? 32 : 16;
     const int NQ = L == 0 ? 2 : 4;  // 8-channel K chunks
     const int NG = N / 8;
     const uint32_t wbase = w_s + (L == 0 ? 0 : (L == 1 ? kW1 : kW1 + kW2));
-    if (tid == 0) {
+    if (ok && tid == 0) {
       // taps outer, tiles inner: consecutive MMAs write different accumulators
       const uint32_t id = idesc_bf16(N);
       const uint64_t adesc0 = sdesc(0, kPlane, 128);
@@ -173,10 +231,11 @@ __global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__
       for (int t = 0; t < 27; t++) {
         for (int ks = 0; ks < NQ / 2; ks++) {
           const uint64_t bd = bdesc0 | (uint64_t)(((wbase + (uint32_t)((t * NQ + 2 * ks) * NG) * 128u) >> 4) & 0x3FFFu);
-          uint32_t a_addr = act_s + (uint32_t)(2 * ks) * kPlane + (uint32_t)(kMBegin + off) * 16u;
+          uint32_t a_addr =
+              act_s + (uint32_t)(2 * ks) * kPlane + (uint32_t)(kMBegin + tile0 * 128 + off) * 16u;
           const uint32_t acc = (t | ks) != 0 ? 1u : 0u;
-#pragma unroll 4
-          for (int tile = 0; tile < kTiles; tile++) {
+#pragma unroll 3
+          for (int tile = 0; tile < kMyTiles; tile++) {
             const uint64_t ad = adesc0 | (uint64_t)((a_addr >> 4) & 0x3FFFu);
             mma_bf16(tmem + (uint32_t)(tile * N), ad, bd, id, acc);
             a_addr += 128u * 16u;
@@ -189,45 +248,62 @@ __global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__
       }
       mma_commit(&bar[0]);
     }
+    mma_pending = ok;
     __syncwarp();
-    ok = mbar_wait_bounded(&bar[0], (uint32_t)(L & 1), kWait);
-    if (!ok) break;
+    if (mma_pending) {
+      ok = __syncthreads_and(mbar_wait_bounded(&bar[0], mma_phase, kWait)) != 0;
+      if (ok) {
+        mma_phase ^= 1u;
+        mma_pending = false;
+      }
+    }
     tc_fence_after();
-    for (int tile = 0; tile < kTiles; tile++) {
-      const int m = kMBegin + tile * 128 + warp * 32 + lane;
-      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(tile * N);
-      int i, j, k;
-      const bool in = m < kPadV && interior(m, i, j, k);
-      if (L < 2) {
-        float v0[16], v1[16];
-        tmem_ld16(ta, v0);
-        tmem_ld16(ta + 16, v1);
-        if (m < kPadV) {
+    // epilogue: groups of tiles whose accumulator loads share one wait
+    constexpr int kGroup = 3;
+    for (int t0 = 0; t0 < kMyTiles && ok; t0 += kGroup) {
+      uint32_t r[kGroup][2][16];
 #pragma unroll
-          for (int q = 0; q < 4; q++) {
-            const float* src = q < 2 ? v0 + 8 * q : v1 + 8 * (q - 2);
-            uint4 w4 = make_uint4(0u, 0u, 0u, 0u);
-            if (in) {
-              w4.x = pack_bf16(src[0], src[1]);
-              w4.y = pack_bf16(src[2], src[3]);
-              w4.z = pack_bf16(src[4], src[5]);
-              w4.w = pack_bf16(src[6], src[7]);
+      for (int g = 0; g < kGroup; g++) {
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((t0 + g) * N);
+        tmem_ld16(ta, r[g][0]);
+        if (L < 2) tmem_ld16(ta + 16, r[g][1]);
+      }
+      tmem_wait();
+#pragma unroll
+      for (int g = 0; g < kGroup; g++) {
+        reg_fence16(r[g][0]);
+        if (L < 2) reg_fence16(r[g][1]);
+        const int m = kMBegin + (tile0 + t0 + g) * 128 + warp * 32 + lane;
+        int i, j, k;
+        const bool in = m < kPadV && interior(m, i, j, k);
+        if (L < 2) {
+          if (m < kPadV) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+              const uint32_t* src = r[g][q >> 1] + 8 * (q & 1);
+              uint4 w4 = make_uint4(0u, 0u, 0u, 0u);
+              if (in) {
+                w4.x = pack_bf16(__uint_as_float(src[0]), __uint_as_float(src[1]));
+                w4.y = pack_bf16(__uint_as_float(src[2]), __uint_as_float(src[3]));
+                w4.z = pack_bf16(__uint_as_float(src[4]), __uint_as_float(src[5]));
+                w4.w = pack_bf16(__uint_as_float(src[6]), __uint_as_float(src[7]));
+              }
+              const uint32_t off_b = (uint32_t)q * kPlane + (uint32_t)m * 16u;
+              *reinterpret_cast<uint4*>(act + off_b) = w4;
+              st_cluster_v4(act_peer + off_b, w4);
             }
-            *reinterpret_cast<uint4*>(act + (size_t)q * kPlane + (size_t)m * 16) = w4;
           }
-        }
-      } else {
-        float v0[16];
-        tmem_ld16(ta, v0);
-        if (in && i >= 1 && i <= 8 && j >= 1 && j <= 8 && k >= 1 && k <= 8) {
+        } else if (in && i >= 1 && i <= 8 && j >= 1 && j <= 8 && k >= 1 && k <= 8) {
           float* dst = y + ((size_t)s * 1000 + (k * 10 + j) * 10 + i) * 3;
-          dst[0] = v0[0];
-          dst[1] = v0[1];
-          dst[2] = v0[2];
+          dst[0] = __uint_as_float(r[g][0][0]);
+          dst[1] = __uint_as_float(r[g][0][1]);
+          dst[2] = __uint_as_float(r[g][0][2]);
         }
       }
     }
     tc_fence_before();
+    // the peer's rows of this layer have landed in this CTA's buffer
+    cluster_sync();
     fence_async_smem();
     __syncthreads();
     tc_fence_after();
@@ -235,7 +311,7 @@ __global__ void __launch_bounds__(128, 1) k_precond_tc(const float* __restrict__
   if (!ok) {
     if (tid == 0) atomicAdd(flags + 2, 1ull);
     // let outstanding MMAs and the weight copy finish before releasing memory
-    mbar_wait_bounded(&bar[0], 0, kWait);
+    if (mma_pending) mbar_wait_bounded(&bar[0], mma_phase, kWait);
     mbar_wait_bounded(&bar[1], 0, kWait);
   }
   tc_fence_before();
@@ -297,6 +373,6 @@ cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const fl
     if (e != cudaSuccess) return e;
     attr_set |= 1ull << dev;
   }
-  k_precond_tc<<<S, 128, kSmem, st>>>(x, y, P->wtc, P->flags);
+  k_precond_tc<<<S * kSplit, 128, kSmem, st>>>(x, y, P->wtc, P->flags);
   return cudaGetLastError();
 }
