@@ -441,16 +441,17 @@ cudaError_t precond_harvest_pairs(amps_gpu_ctx* c, const double* r, const double
 cudaError_t launch_precond_net(amps_gpu_ctx* c, const double* v, double* z) {
   PrecondState* P = c->pn;
   if (!P) return cudaErrorInvalidValue;
-  cudaError_t e = precond_work(P, c->nb);
-  if (e != cudaSuccess) return e;
+  cudaError_t e;
+  if (P->use_tc) {
+    TimedLaunch t(c, "precond_net_tc");
+    return precond_apply_tc_mesh(P, c->stream, c->nb, c->d_nbr, c->ncor, v, c->d_dinv, z);
+  }
+  if ((e = precond_work(P, c->nb)) != cudaSuccess) return e;
   {
     TimedLaunch t(c, "precond_gather");
     k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, v, c->d_dinv, P->wx);
   }
-  if (P->use_tc) {
-    TimedLaunch t(c, "precond_net_tc");
-    if ((e = precond_forward_tc(P, c->stream, c->nb, P->wx, P->y)) != cudaSuccess) return e;
-  } else {
+  {
     TimedLaunch t(c, "precond_net_fp32", 3);
     if ((e = precond_forward32(P, c->stream, c->nb)) != cudaSuccess) return e;
   }

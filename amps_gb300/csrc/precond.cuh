@@ -44,6 +44,9 @@ cudaError_t precond_owned_out(PrecondState* P, cudaStream_t st, int S, float* ou
 // BF16 tcgen05 inference: x[S][1000][3] -> y[S][1000][3] (owned voxels)
 cudaError_t precond_prepare_tc(PrecondState* P, cudaStream_t st);
 cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const float* x, float* y);
+// z = D v + N(D v) on a uniform mesh in one launch (gather, network, scatter)
+cudaError_t precond_apply_tc_mesh(PrecondState* P, cudaStream_t st, int nb, const int* nbr,
+                                  long long ncor, const double* v, const double* dinv, double* z);
 // GMRES hooks (field.cu)
 cudaError_t launch_precond_net(amps_gpu_ctx* c, const double* v, double* z);
 cudaError_t precond_harvest_pairs(amps_gpu_ctx* c, const double* r, const double* e, int e_scaled);

@@ -143,11 +143,21 @@ __device__ __forceinline__ bool interior(int p, int& i, int& j, int& k) {
   return px >= 1 && px <= 10 && py >= 1 && py <= 10 && pz >= 1 && pz <= 10;
 }
 
+// Inputs/outputs: samples mode (x[S][1000][3] -> y[S][1000][3], owned voxels)
+// or mesh mode (mesh.v != null: x = dinv .* v gathered around mesh block s
+// through the neighbour table, z = x + y written to the FP64 corners).
+struct MeshIO {
+  const double* v;
+  const double* dinv;
+  const int* nbr;
+  long long ncor;
+  double* z;
+};
+
 __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
-    k_precond_tc(const float* __restrict__ x,
-                                                       float* __restrict__ y,
-                                                       const uint16_t* __restrict__ wimg,
-                                                       unsigned long long* __restrict__ flags) {
+    k_precond_tc(const float* __restrict__ x, float* __restrict__ y,
+                 const uint16_t* __restrict__ wimg, unsigned long long* __restrict__ flags,
+                 MeshIO mesh) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* act = smem;
   uint8_t* wsm = smem + kActBytes;
@@ -187,7 +197,19 @@ __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
     for (int q = 0; q < kPer; q++) {
       const int v = tid + q * 128;
 #pragma unroll
-      for (int ch = 0; ch < 3; ch++) xv[q][ch] = v < 1000 ? __ldg(xs + 3 * v + ch) : 0.f;
+      for (int ch = 0; ch < 3; ch++) xv[q][ch] = 0.f;
+      if (v < 1000) {
+        if (mesh.v) {
+          const int i = v % 10, j = (v / 10) % 10, k = v / 100;
+          const long long id = local_id(mesh.nbr, s, i - 1, j - 1, k - 1);
+#pragma unroll
+          for (int ch = 0; ch < 3; ch++)
+            xv[q][ch] = (float)(mesh.dinv[ch * mesh.ncor + id] * mesh.v[ch * mesh.ncor + id]);
+        } else {
+#pragma unroll
+          for (int ch = 0; ch < 3; ch++) xv[q][ch] = __ldg(xs + 3 * v + ch);
+        }
+      }
     }
 #pragma unroll
     for (int q = 0; q < kPer; q++) {
@@ -294,10 +316,19 @@ __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
             }
           }
         } else if (in && i >= 1 && i <= 8 && j >= 1 && j <= 8 && k >= 1 && k <= 8) {
-          float* dst = y + ((size_t)s * 1000 + (k * 10 + j) * 10 + i) * 3;
-          dst[0] = __uint_as_float(r[g][0][0]);
-          dst[1] = __uint_as_float(r[g][0][1]);
-          dst[2] = __uint_as_float(r[g][0][2]);
+          if (mesh.v) {
+            // z = D v (FP64) + N(D v) on the owned corner (i-1, j-1, k-1)
+            const long long id = (long long)s * AMPS_CPB + (i - 1) + 8 * ((j - 1) + 8 * (k - 1));
+#pragma unroll
+            for (int ch = 0; ch < 3; ch++)
+              mesh.z[ch * mesh.ncor + id] = mesh.dinv[ch * mesh.ncor + id] * mesh.v[ch * mesh.ncor + id] +
+                                            (double)__uint_as_float(r[g][0][ch]);
+          } else {
+            float* dst = y + ((size_t)s * 1000 + (k * 10 + j) * 10 + i) * 3;
+            dst[0] = __uint_as_float(r[g][0][0]);
+            dst[1] = __uint_as_float(r[g][0][1]);
+            dst[2] = __uint_as_float(r[g][0][2]);
+          }
         }
       }
     }
@@ -363,8 +394,7 @@ cudaError_t precond_prepare_tc(PrecondState* P, cudaStream_t st) {
   return e;
 }
 
-cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const float* x, float* y) {
-  if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
+static cudaError_t set_tc_attr() {
   static unsigned long long attr_set = 0;  // per device
   int dev = 0;
   cudaGetDevice(&dev);
@@ -373,6 +403,24 @@ cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const fl
     if (e != cudaSuccess) return e;
     attr_set |= 1ull << dev;
   }
-  k_precond_tc<<<S * kSplit, 128, kSmem, st>>>(x, y, P->wtc, P->flags);
+  return cudaSuccess;
+}
+
+cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const float* x, float* y) {
+  if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
+  cudaError_t e = set_tc_attr();
+  if (e != cudaSuccess) return e;
+  MeshIO none{nullptr, nullptr, nullptr, 0, nullptr};
+  k_precond_tc<<<S * kSplit, 128, kSmem, st>>>(x, y, P->wtc, P->flags, none);
+  return cudaGetLastError();
+}
+
+cudaError_t precond_apply_tc_mesh(PrecondState* P, cudaStream_t st, int nb, const int* nbr,
+                                  long long ncor, const double* v, const double* dinv, double* z) {
+  if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
+  cudaError_t e = set_tc_attr();
+  if (e != cudaSuccess) return e;
+  MeshIO io{v, dinv, nbr, ncor, z};
+  k_precond_tc<<<nb * kSplit, 128, kSmem, st>>>(nullptr, nullptr, P->wtc, P->flags, io);
   return cudaGetLastError();
 }

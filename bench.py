@@ -409,6 +409,23 @@ def run_precond_kernel(args):
     ctx.close()
 
 
+def tracer_line(n32, n64, device):
+    """Batched relativistic test-particle tracing (cutoff workload): particle-steps/s
+    in FP32 on n32 particles and FP64 on the first n64 of them; status agreement."""
+    from amps_gb300 import tracer as T
+    x32, p32, st32, s32, tot32, ms32 = T.trace_cutoff(n32, seed=7, precision=1, device=device)
+    x64, p64, st64, s64, tot64, ms64 = T.trace_cutoff(n64, seed=7, precision=0, device=device)
+    same = float(np.mean(st32[:n64] == st64))
+    return {"workload": "cutoff tracing: protons on r=1.1 R_E, isotropic, 0.1-20 GV log-uniform, "
+                        "dipole B_eq=3.1e-5 T + 5 nT southward, stop r<1, r>10 R_E or 1e5 steps",
+            "fp32": {"particles": n32, "particle_steps": int(tot32), "kernel_ms": ms32,
+                     "particle_steps_per_s": tot32 / (ms32 / 1e3)},
+            "fp64": {"particles": n64, "particle_steps": int(tot64), "kernel_ms": ms64,
+                     "particle_steps_per_s": tot64 / (ms64 / 1e3)},
+            "status_agreement_fp32_vs_fp64": same,
+            "status_counts_fp32": {str(k): int(np.sum(st32 == k)) for k in np.unique(st32)}}
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import amps_gb300 as A
@@ -510,6 +527,9 @@ def run_gpu(args):
             smp = "FP64 oracle Lapenta2017+ProcessCell on a periodic 8^3-cell replica of the " \
                   "same plasma (%d particles), %.1f s" % (ci["replica_particles"], ci["seconds"])
         cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp}
+    trc = None
+    if rank == 0 and args.tracer > 0:
+        trc = tracer_line(args.tracer, max(1, args.tracer // 16), local)
     pab = None
     if rank == 0 and args.precond_ab:
         pab = {"config": precond_ab("ecsim_32c_64ppc", local)}
@@ -527,7 +547,7 @@ def run_gpu(args):
                 "ecsim_step_ms": round(min(t_step), 3), "gmres_iterations": gmres_it,
                 "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations}),
             "e2e": e2e, "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
-            "precond_ab": pab,
+            "precond_ab": pab, "tracer": trc,
             "clocks": clocks, "gpu_launches": gpu_launches,
         }
         print(json.dumps(line), flush=True)
@@ -584,6 +604,9 @@ def main():
                     help="learned vs plain vs Jacobi GMRES on the 32^3 plasma (1 = on)")
     ap.add_argument("--precond-stiff", type=int, default=1,
                     help="also the same A/B at dt = 1/omega_pe")
+    ap.add_argument("--tracer", type=int, default=0,
+                    help="also run the cutoff tracing workload with this many particles (FP32; "
+                         "FP64 on 1/16 of them)")
     ap.add_argument("--precond-kernel", type=int, default=0,
                     help="time only the tensor-core inference kernel on this many blocks")
     ap.add_argument("--traffic", type=float, default=None,
