@@ -105,6 +105,9 @@ SIGNATURES = {
     "amps_gpu_precond_train": (C.c_int, [P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, F]),
     "amps_gpu_precond_loss_grad": (C.c_int, [P, C.c_longlong, F, F, F, F, F, F]),
     "amps_gpu_precond_forward": (C.c_int, [P, C.c_longlong, F, C.c_int, F]),
+    "amps_gpu_set_graphs": (C.c_int, [P, C.c_int]),
+    "amps_gpu_autotune": (C.c_int, [P, D]),
+    "amps_gpu_get_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "amps_gpu_set_kernel_timing": (C.c_int, [P, C.c_int]),
     "amps_gpu_get_kernel_times": (C.c_int, [P, C.POINTER(C.c_char_p), D, LL, C.c_int,
                                             C.POINTER(C.c_int)]),

@@ -446,7 +446,8 @@ cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* di
   a.with_identity = a.with_curl = a.with_mass = 1;
   a.rhs_mode = 0;
   TimedLaunch t(c, "matvec", 2);
-  k_amr_cell_op<double><<<g1(c->ncor), 256, 0, c->stream>>>(a, y);
+  k_amr_cell_op<double><<<(unsigned)((c->ncor + c->tune_tb - 1) / c->tune_tb), c->tune_tb, 0,
+                          c->stream>>>(a, y);
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, x, dinv, y, 0);
   return cudaGetLastError();
 }
@@ -462,7 +463,8 @@ cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* 
   a.with_curl = a.with_mass = 1;
   a.rhs_mode = 0;
   TimedLaunch t(c, "matvec32", 2);
-  k_amr_cell_op<float><<<g1(c->ncor), 256, 0, c->stream>>>(a, c->d_y32);
+  k_amr_cell_op<float><<<(unsigned)((c->ncor + c->tune_tb - 1) / c->tune_tb), c->tune_tb, 0,
+                         c->stream>>>(a, c->d_y32);
   k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_sv,
                                                      c->d_y32, x, dinv, y);
   return cudaGetLastError();

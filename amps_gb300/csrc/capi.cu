@@ -221,17 +221,75 @@ amps_gpu_status reset_flags(amps_gpu_ctx* c) {
                     "reset flags");
 }
 
+// The launch sequence of one particle step: flag reset, stencil pack, push
+// (+ deposit), arrivals (+ assembly), flag read-back.
+cudaError_t enqueue_particle_step(amps_gpu_ctx* c, bool deposit) {
+  cudaError_t e = cudaMemsetAsync(c->d_flags, 0, 5 * sizeof(unsigned long long), c->stream);
+  if (e == cudaSuccess) e = launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur);
+  if (e == cudaSuccess) e = launch_push_step(c, deposit);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->h_flags, c->d_flags, 4 * sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, c->stream);
+  return e;
+}
+
+// The same sequence as a CUDA graph, captured once per set of buffers it reads
+// (the corner-B slots swap every field solve, so two graphs alternate).
+cudaError_t launch_particle_step_graph(amps_gpu_ctx* c, bool deposit) {
+  const void* key[4] = {c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur,
+                        (const void*)((uintptr_t)c->d_u[c->cur][0] ^ (c->has_wcorr ? 1u : 0u))};
+  for (auto& g : c->graphs)
+    if (g.deposit == deposit && std::memcmp(g.key, key, sizeof(key)) == 0)
+      return cudaGraphLaunch(g.exec, c->stream);
+  particles_prepare();
+  cudaGraph_t graph;
+  cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t e1 = enqueue_particle_step(c, deposit);
+  e = cudaStreamEndCapture(c->stream, &graph);
+  if (e1 != cudaSuccess) return e1;
+  if (e != cudaSuccess) return e;
+  amps_gpu_ctx::StepGraph g;
+  g.deposit = deposit;
+  std::memcpy(g.key, key, sizeof(key));
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return e;
+  if (c->graphs.size() >= 8) {
+    cudaGraphExecDestroy(c->graphs.front().exec);
+    c->graphs.erase(c->graphs.begin());
+  }
+  c->graphs.push_back(g);
+  return cudaGraphLaunch(g.exec, c->stream);
+}
+
+// flags already copied to h_flags by the step: interpret them after a sync
+amps_gpu_status read_step_flags(amps_gpu_ctx* c, long long* out_of_block, long long* ulp,
+                                long long* overflow) {
+  amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "synchronize");
+  if (s) return s;
+  if (out_of_block) *out_of_block = (long long)c->h_flags[0];
+  if (ulp) *ulp = (long long)c->h_flags[1];
+  if (overflow) *overflow = (long long)c->h_flags[3];
+  if (c->h_flags[2])
+    return set_err(c, AMPS_GPU_DEVICE_TIMEOUT,
+                   "device reported " + std::to_string(c->h_flags[2]) +
+                       " bounded-wait timeouts or invalid particle records");
+  return AMPS_GPU_OK;
+}
+
 // One particle step (push, optionally fused with the deposit), with recovery
 // when the slack of some destination cell overflowed.
 amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_block,
                               long long* near_face) {
   amps_gpu_status s;
-  if ((s = reset_flags(c))) return s;
-  if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
+  const bool graph = c->use_graphs && !c->timing;
+  if ((s = cuda_check(c, graph ? launch_particle_step_graph(c, deposit)
+                               : enqueue_particle_step(c, deposit),
+                      "particle step")))
     return s;
-  if ((s = cuda_check(c, launch_push_step(c, deposit), "push step"))) return s;
   long long ovf = 0;
-  if ((s = check_flags(c, out_of_block, near_face, &ovf))) return s;
+  if ((s = read_step_flags(c, out_of_block, near_face, &ovf))) return s;
   if (ovf > 0) {
     // rare: some cell ran out of slack.  Re-sort everything (new slack) and
     // redo the deposition from the rebuilt layout.
@@ -515,6 +573,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   staging_free(c);
   precond_free(c->pn);
   c->pn = nullptr;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
                   c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
                   c->d_Z, c->d_y32,
@@ -831,6 +891,26 @@ amps_gpu_status amps_gpu_step(amps_gpu_ctx* c, double tol, int maxit, int precon
   c->have_moments = true;
   if (stats) *stats = st;
   return fs;
+}
+
+amps_gpu_status amps_gpu_set_graphs(amps_gpu_ctx* c, int on) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  c->use_graphs = on != 0;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_autotune(amps_gpu_ctx* c, double* ms) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  return field_autotune(c, ms);
+}
+
+amps_gpu_status amps_gpu_get_tuning(amps_gpu_ctx* c, int* threads_per_cta, int* reduction_ctas) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  if (threads_per_cta) *threads_per_cta = c->tune_tb;
+  if (reduction_ctas) *reduction_ctas = c->tune_red;
+  return AMPS_GPU_OK;
 }
 
 amps_gpu_status amps_gpu_set_kernel_timing(amps_gpu_ctx* c, int enable) {

@@ -97,6 +97,20 @@ struct amps_gpu_ctx {
   float* d_y32 = nullptr;       // 3*nvc FP32 accumulation of the inner AMR operator
   bool inner_fp32 = true;       // GMRES inner operator in FP32 (iterative refinement)
   PrecondState* pn = nullptr;   // learned preconditioner (precond.cu)
+
+  // launch parameters chosen by the autotuner (field.cu: field_autotune)
+  int tune_tb = 256;            // threads per CTA of the operator kernels
+  int tune_red = 304;           // maximum CTAs of the reduction sweeps
+  int tune_ept = 4;             // minimum elements per thread of the sweeps
+
+  // CUDA graphs of the particle step (capi.cu), keyed by the pointers they bake in
+  bool use_graphs = false;
+  struct StepGraph {
+    bool deposit;
+    const void* key[4];
+    cudaGraphExec_t exec;
+  };
+  std::vector<StepGraph> graphs;
   double* d_red = nullptr;      // partial reductions
   double* h_red = nullptr;      // pinned
   int restart = 30;
@@ -160,6 +174,7 @@ void flush_timers(amps_gpu_ctx* c);
 cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
                                  const double* Bcur);
 cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit);
+void particles_prepare();
 cudaError_t launch_deposit(amps_gpu_ctx* c);
 cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
@@ -180,6 +195,9 @@ cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor);
 cudaError_t launch_update_e(amps_gpu_ctx* c);
 amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
                             amps_gpu_solve_stats* st);
+// times candidate launch shapes of the operator and reduction kernels on the
+// context's own data and keeps the fastest; ms[6] receives the timings
+amps_gpu_status field_autotune(amps_gpu_ctx* c, double* ms);
 
 // ---- AMR field launchers (amr_field.cu); the launchers above dispatch to
 //      them when the context holds an AMR mesh ----

@@ -1,4 +1,5 @@
-// ECSIM field solve on sm_103a, FP64 throughout.
+// ECSIM field solve on sm_103a on uniform meshes (FP64 vectors; the inner
+// GMRES operator in FP32 arithmetic around an FP64 identity part).
 //
 //   k_rhs       UpdateRhs with the supports registered by GetStencil
 //               (src/pic/ecsim/get_stencil.cpp:1260-1599, ecsim/update_rhs.cpp:285):
@@ -9,19 +10,18 @@
 //               A = I + (theta c dt)^2 (grad div - lap) + 4 pi theta dt M
 //               (replaces cLinearSystemCornerNode::MultiplyVector,
 //               srcInterface/LinearSystemCornerNode.h:3067-3205)
-//   GMRES       restarted GMRES(30), x0 = 0, right Jacobi preconditioner
-//               optional, classical Gram-Schmidt with one re-orthogonalisation;
-//               each Arnoldi step is matvec + three fused sweep/reduction
-//               kernels with FP64 warp-shuffle reductions
+//   GMRES       restarted GMRES(30), x0 = 0, right preconditioner (none,
+//               Jacobi, learned), classical Gram-Schmidt with one
+//               re-orthogonalisation; each Arnoldi step is matvec + three fused
+//               sweep/reduction kernels with FP64 warp-shuffle reductions
 //               (the external linear_solver_wrapper of LinearSystemCornerNode.h:3282)
 //   k_update_b  UpdateB (:5160-5711), k_c2n InterpolateB_C2N (:5715),
 //   k_update_e  UpdateE with the wave-energy sum (:5909-6001)
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
-
-#include <algorithm>
 
 #include "common.cuh"
 #include "precond.cuh"
@@ -475,10 +475,12 @@ __global__ void __launch_bounds__(256) k_add(long long n, const double* __restri
 }
 
 unsigned grid1(long long n) { return (unsigned)((n + 255) / 256); }
-// sweep/reduction grid: at least 4 elements per thread, at most kRedBlocks CTAs
-unsigned gridr(long long n) {
-  long long g = (n + 1023) / 1024;
-  return (unsigned)(g < kRedBlocks ? g : kRedBlocks);
+unsigned gridt(long long n, int tb) { return (unsigned)((n + tb - 1) / tb); }
+// sweep/reduction grid: at least ept elements per thread, at most cap CTAs
+unsigned gridr(long long n, int cap = kRedBlocks, int ept = 4) {
+  long long g = (n + 256LL * ept - 1) / (256LL * ept);
+  if (g > cap) g = cap;
+  return (unsigned)(g < 1 ? 1 : g);
 }
 
 }  // namespace
@@ -488,7 +490,8 @@ cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, 
   if (c->amr) return launch_amr_matvec(c, x, dinv, y);
   Taps T = make_taps(c->cfg, true);
   TimedLaunch t(c, "matvec");
-  k_matvec<<<grid1(3 * c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, x, dinv, y, T);
+  k_matvec<<<gridt(3 * c->ncor, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M,
+                                                                          x, dinv, y, T);
   return cudaGetLastError();
 }
 
@@ -496,7 +499,8 @@ cudaError_t launch_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv
   if (c->amr) return launch_amr_matvec32(c, x, dinv, y);
   const TapsF T = taps_f32(make_taps(c->cfg, false));
   TimedLaunch t(c, "matvec32");
-  k_matvec32<<<grid1(3 * c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, x, dinv, y, T);
+  k_matvec32<<<gridt(3 * c->ncor, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr,
+                                                                            c->d_M, x, dinv, y, T);
   return cudaGetLastError();
 }
 
@@ -567,7 +571,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   double* d_h2 = d_h1 + kMaxV;
   double* d_n2 = d_h2 + kMaxV;
   double* d_y = d_n2 + 8;
-  const unsigned gr = gridr(n);
+  const unsigned gr = gridr(n, c->tune_red, c->tune_ept);
   cudaStream_t s = c->stream;
   cudaError_t e;
 #define CK(x)                                                   \
@@ -701,6 +705,75 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     st->rel_residual = rel;
   }
   return conv ? AMPS_GPU_OK : AMPS_GPU_GMRES_NOT_CONVERGED;
+}
+
+// Autotuner: candidate launch shapes timed with CUDA events on the context
+// stream, on scratch vectors (the operator and the sweeps have no side effects
+// outside them).  ms[0..2]: operator with 64/128/256 threads per CTA;
+// ms[3..5]: one 8-vector CGS2 sweep with 76/152/304 CTAs (4 elements per thread).
+amps_gpu_status field_autotune(amps_gpu_ctx* c, double* ms) {
+  const long long n = 3 * c->nvc;
+  cudaStream_t s = c->stream;
+  cudaError_t e;
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+    return set_err(c, AMPS_GPU_CUDA_ERROR, "autotune: events");
+  const bool timing = c->timing;
+  c->timing = false;
+  amps_gpu_status st = AMPS_GPU_OK;
+  auto fail = [&](cudaError_t err, const char* what) {
+    st = cuda_check(c, err, what);
+    return st;
+  };
+  double* x = c->d_x;
+  double* y = c->d_w;
+  if ((e = cudaMemsetAsync(x, 0, sizeof(double) * n, s)) != cudaSuccess) fail(e, "autotune");
+  if ((e = cudaMemsetAsync(c->d_V, 0, sizeof(double) * n * 10, s)) != cudaSuccess) fail(e, "autotune");
+  const int tbs[3] = {64, 128, 256};
+  double best = 1e30;
+  int best_tb = c->tune_tb;
+  for (int q = 0; q < 3 && !st; q++) {
+    c->tune_tb = tbs[q];
+    for (int w = 0; w < 2 && !st; w++)
+      if ((e = launch_matvec32(c, x, nullptr, y)) != cudaSuccess) fail(e, "autotune matvec");
+    cudaEventRecord(a, s);
+    for (int r = 0; r < 5 && !st; r++)
+      if ((e = launch_matvec32(c, x, nullptr, y)) != cudaSuccess) fail(e, "autotune matvec");
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    if (ms) ms[q] = t / 5.0;
+    if (t < best) { best = t; best_tb = tbs[q]; }
+  }
+  c->tune_tb = best_tb;
+  const int caps[3] = {76, 152, 304};
+  double* partial = c->d_red;
+  double* d_h1 = c->d_red + kRedBlocks * kMaxV;
+  double* d_h2 = d_h1 + kMaxV;
+  double* d_n2 = d_h2 + kMaxV;
+  best = 1e30;
+  int best_cap = c->tune_red;
+  for (int q = 0; q < 3 && !st; q++) {
+    const unsigned gr = gridr(n, caps[q], 4);
+    arnoldi_orth<8>(s, gr, n, c->d_V, y, 8, partial, d_h1, d_h2, d_n2, c->d_V + 8 * n);
+    cudaEventRecord(a, s);
+    for (int r = 0; r < 5; r++)
+      arnoldi_orth<8>(s, gr, n, c->d_V, y, 8, partial, d_h1, d_h2, d_n2, c->d_V + 8 * n);
+    cudaEventRecord(b, s);
+    if ((e = cudaEventSynchronize(b)) != cudaSuccess) fail(e, "autotune sweep");
+    float t = 0.f;
+    cudaEventElapsedTime(&t, a, b);
+    if (ms) ms[3 + q] = t / 5.0;
+    if (t < best) { best = t; best_cap = caps[q]; }
+  }
+  c->tune_red = best_cap;
+  c->tune_ept = 4;
+  c->timing = timing;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!st) st = cuda_check(c, cudaGetLastError(), "autotune");
+  return st;
 }
 
 cudaError_t launch_add(amps_gpu_ctx* c, const double* a, const double* b, double* o, long long n) {

@@ -1004,6 +1004,14 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
 
 // ===========================================================================
 // launchers
+
+// one-time host-side setup of the particle kernels (kernel attributes, the
+// constant assembly table); must precede any stream capture
+void particles_prepare() {
+  set_smem_attrs();
+  init_asm_table();
+}
+
 cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double* Bprev,
                                  const double* Bcur) {
   if (c->amr) return launch_amr_pack(c, Eh, Bprev, Bcur);

@@ -386,6 +386,21 @@ class EcsimContext:
                     "precond_forward")
         return y
 
+    # ---- launch configuration ----
+    def set_graphs(self, on=True):
+        self._check(self.lib.amps_gpu_set_graphs(self.h, 1 if on else 0), "set_graphs")
+
+    def autotune(self):
+        """Times candidate launch shapes of the field kernels; returns the
+        candidates' times and the chosen (threads per CTA, reduction CTAs)."""
+        ms = np.zeros(6)
+        self._check(self.lib.amps_gpu_autotune(self.h, ptr(ms, C.c_double)), "autotune")
+        tb, red = C.c_int(), C.c_int()
+        self._check(self.lib.amps_gpu_get_tuning(self.h, C.byref(tb), C.byref(red)), "get_tuning")
+        return {"operator_ms_tb64_128_256": ms[:3].round(4).tolist(),
+                "sweep_ms_cta76_152_304": ms[3:].round(4).tolist(),
+                "threads_per_cta": tb.value, "reduction_ctas": red.value}
+
     # ---- timing ----
     def set_kernel_timing(self, on=True):
         self._check(self.lib.amps_gpu_set_kernel_timing(self.h, 1 if on else 0), "timing")

@@ -437,13 +437,13 @@ def run_gpu(args):
     tol = info["tol"]
     # one field solve so the push sees a self-consistent E^{n+theta}
     ctx.UpdateJMassMatrix()
+    tuning = ctx.autotune()
     solve = ctx.TimeStep(tol=tol, maxit=200, precond=1)
     stream = ctx.stream()
+    ctx.set_graphs(args.graphs > 0)
     for _ in range(args.warmup):
         ctx.push_deposit(want_energy=False)
     ctx.synchronize()
-    ctx.set_kernel_timing(True)
-    ctx.reset_kernel_times()
     a, b = ev.event(), ev.event()
     clk = ClockSampler(local)
     barrier(dist)
@@ -457,6 +457,12 @@ def run_gpu(args):
     ms = ev.elapsed_ms(a, b)
     clocks = clk.stop()
     barrier(dist)
+    # per-kernel breakdown (roofline): the same steps again with event timing
+    ctx.set_kernel_timing(True)
+    ctx.reset_kernel_times()
+    n_kt = max(3, args.steps // 4)
+    for _ in range(n_kt):
+        ctx.push_deposit(want_energy=False)
     ktimes = ctx.kernel_times()
     ctx.set_kernel_timing(False)
     ms_max = max_over_ranks(dist, ms)
@@ -514,7 +520,8 @@ def run_gpu(args):
                 "traffic": args.traffic, "algorithmic_bytes_per_launch": int(nbytes),
                 "avg_launch_ms": round(ms_top / nl, 4)}
     shares = {k: round(v[0] / sum(x[0] for x in per.values()), 4) for k, v in per.items()}
-    gpu_launches = int(sum(v[1] for v in per.values()))
+    # kernels per step (from the event-timed pass) x timed steps
+    gpu_launches = int(round(sum(v[1] for v in per.values()) / n_kt * args.steps))
 
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
@@ -545,7 +552,8 @@ def run_gpu(args):
                 "parallelism": "replicas" if ws > 1 else "single GPU",
                 "l2": "inputs larger than L2 (no flush)",
                 "ecsim_step_ms": round(min(t_step), 3), "gmres_iterations": gmres_it,
-                "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations}),
+                "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations,
+                "cuda_graphs": args.graphs > 0, "autotune": tuning}),
             "e2e": e2e, "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
             "precond_ab": pab, "tracer": trc,
             "clocks": clocks, "gpu_launches": gpu_launches,
@@ -604,6 +612,7 @@ def main():
                     help="learned vs plain vs Jacobi GMRES on the 32^3 plasma (1 = on)")
     ap.add_argument("--precond-stiff", type=int, default=1,
                     help="also the same A/B at dt = 1/omega_pe")
+    ap.add_argument("--graphs", type=int, default=1, help="particle step as a CUDA graph")
     ap.add_argument("--tracer", type=int, default=0,
                     help="also run the cutoff tracing workload with this many particles (FP32; "
                          "FP64 on 1/16 of them)")

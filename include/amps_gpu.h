@@ -273,6 +273,17 @@ amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(const amps_gpu_config* cfg
                                                       double* d_M, double* d_energy,
                                                       void* stream);
 
+/* ---- launch configuration (no reference counterpart) ----
+ * set_graphs: run the particle step (flag reset, stencil pack, push/deposit,
+ * arrivals, assembly, flag read-back) as a captured CUDA graph, one per set of
+ * field buffers it reads; graphs are not used while kernel timing is on.
+ * autotune: times 3 CTA sizes of the field operator kernels and 3 grid sizes of
+ * the GMRES sweeps on this context's data and keeps the fastest; ms[6]
+ * (optional) receives the candidates' times. get_tuning reads the choice. */
+amps_gpu_status amps_gpu_set_graphs(amps_gpu_ctx* ctx, int on);
+amps_gpu_status amps_gpu_autotune(amps_gpu_ctx* ctx, double* ms);
+amps_gpu_status amps_gpu_get_tuning(amps_gpu_ctx* ctx, int* threads_per_cta, int* reduction_ctas);
+
 /* ---- per-kernel device timing on the context stream (CUDA events) ---- */
 amps_gpu_status amps_gpu_set_kernel_timing(amps_gpu_ctx* ctx, int enable);
 /* Fills up to cap entries; names are static strings.  Returns the count in *n. */
