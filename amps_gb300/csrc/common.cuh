@@ -175,6 +175,8 @@ cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double
                                  const double* Bcur);
 cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit);
 void particles_prepare();
+cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
+                            double c_light, long long max_sub);
 cudaError_t launch_deposit(amps_gpu_ctx* c);
 cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,

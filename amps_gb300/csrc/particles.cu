@@ -869,6 +869,153 @@ __global__ void __launch_bounds__(256) k_export(long long ncells, const int* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mover::Relativistic::Boris (src/pic/pic_mover_relativistic_boris.cpp:16-583,
+// scalar path :119-175) on the mesh: FP64 sub-steps of dt = min(1/f_g,
+// remaining), f_g = |q||B|/(2 pi m gamma) (specfunc.h:1290), fields E, B
+// interpolated from the FP64 corner arrays at each sub-step's start position
+// (CornerBased::InitStencil weights, normalised), periodic re-location after
+// every sub-step (findTreeNode rules).  One thread per particle of the list
+// buffer; writes the new block-local offset, velocity and key.
+struct RelBorisArgs {
+  PBuf d;
+  int* key;
+  long long n;
+  const int* nbr;
+  long long ncor;
+  const double* E;
+  const double* B;
+  int nbk[3];
+  double x0[3], dx[3];
+  double qm[AMPS_GPU_MAX_SPECIES];  // q/m per species
+  double qabs_over_m[AMPS_GPU_MAX_SPECIES];
+  double dt_total, c_light;
+  long long max_sub;
+  unsigned long long* flags;   // [2] sub-step cap reached
+  unsigned long long* nsub;    // total sub-steps
+};
+
+// block and in-block coordinate of x (periodic; same rules as k_import)
+__device__ __forceinline__ void rb_locate(const RelBorisArgs& a, double x[3], int bx[3],
+                                          double xmin[3]) {
+  for (int d = 0; d < 3; d++) {
+    const double L = AMPS_NC * a.dx[d];
+    int bb = (int)floor((x[d] - a.x0[d]) / L);
+    double xm = a.x0[d] + bb * L;
+    if (x[d] < xm) { bb--; xm = a.x0[d] + bb * L; }
+    if (x[d] >= xm + L) { bb++; xm = a.x0[d] + bb * L; }
+    if (bb < 0 || bb >= a.nbk[d]) {
+      const int br = ((bb % a.nbk[d]) + a.nbk[d]) % a.nbk[d];
+      const double xr = a.x0[d] + br * L;
+      x[d] += xr - xm;
+      if (x[d] < xr) x[d] = xr;
+      if (x[d] >= xr + L) x[d] = (xr + L) - 1.0E-10 * L;
+      bb = br;
+      xm = xr;
+    }
+    bx[d] = bb;
+    xmin[d] = xm;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_relboris(RelBorisArgs a) {
+  unsigned long long my_sub = 0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int key = a.key[p];
+    const int b0 = key / AMPS_CPB;
+    const int sp = a.d.sp[p];
+    int bx[3] = {b0 % a.nbk[0], (b0 / a.nbk[0]) % a.nbk[1], b0 / (a.nbk[0] * a.nbk[1])};
+    double x[3], v[3];
+    for (int d = 0; d < 3; d++) {
+      x[d] = a.x0[d] + bx[d] * (AMPS_NC * a.dx[d]) + (double)a.d.u[d][p] * a.dx[d];
+      v[d] = a.d.v[d][p];
+    }
+    double rem = a.dt_total;
+    long long ns = 0;
+    double xmin[3];
+    while (rem > 0.0) {
+      if (ns >= a.max_sub) {
+        atomicAdd(a.flags + 2, 1ull);
+        break;
+      }
+      rb_locate(a, x, bx, xmin);
+      const int b = bx[0] + a.nbk[0] * (bx[1] + a.nbk[1] * bx[2]);
+      int iX[3];
+      double xl[3];
+      for (int d = 0; d < 3; d++) {
+        const double xmax = xmin[d] + AMPS_NC * a.dx[d];
+        double xx = x[d];
+        if (fabs(xx - xmax) < 1e-10 * a.dx[d]) xx = xmax - 1e-10 * a.dx[d];
+        xl[d] = (xx - xmin[d]) / a.dx[d];
+        iX[d] = min(max((int)xl[d], 0), AMPS_NC - 1);
+        xl[d] -= iX[d];
+      }
+      double w[8], norm = 0.0;
+      for (int q = 0; q < 8; q++) {
+        const int aa = q & 1, bb = (q >> 1) & 1, cc = q >> 2;
+        w[q] = (aa ? xl[0] : 1.0 - xl[0]) * (bb ? xl[1] : 1.0 - xl[1]) * (cc ? xl[2] : 1.0 - xl[2]);
+        norm += w[q];
+      }
+      double Ef[3] = {0, 0, 0}, Bf[3] = {0, 0, 0};
+      for (int q = 0; q < 8; q++) {
+        const int id = local_id(a.nbr, b, iX[0] + (q & 1), iX[1] + ((q >> 1) & 1), iX[2] + (q >> 2));
+        const double wq = w[q] / norm;
+        for (int d = 0; d < 3; d++) {
+          Ef[d] += wq * a.E[d * a.ncor + id];
+          Bf[d] += wq * a.B[d * a.ncor + id];
+        }
+      }
+      const double cc2 = a.c_light * a.c_light;
+      double gam = 1.0 / sqrt(1.0 - (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / cc2);
+      const double bmag = sqrt(Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
+      double dt = rem;
+      if (bmag > 1.0e-25) {
+        const double fg = a.qabs_over_m[sp] * bmag / (2.0 * 3.14159265358979323846 * gam);
+        const double dtmax = 1.0 / fg;
+        if (dtmax < rem) dt = dtmax;
+      }
+      rem -= dt;
+      const double h = 0.5 * a.qm[sp] * dt;
+      double um[3], t[3], up[3], sv[3], upl[3], uf[3], l = 0.0;
+      for (int d = 0; d < 3; d++) um[d] = gam * v[d] + h * Ef[d];
+      gam = sqrt(1.0 + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]) / cc2);
+      for (int d = 0; d < 3; d++) { t[d] = h / gam * Bf[d]; l += t[d] * t[d]; }
+      up[0] = um[0] + (um[1] * t[2] - um[2] * t[1]);
+      up[1] = um[1] + (um[2] * t[0] - um[0] * t[2]);
+      up[2] = um[2] + (um[0] * t[1] - um[1] * t[0]);
+      for (int d = 0; d < 3; d++) sv[d] = 2.0 * t[d] / (1.0 + l);
+      upl[0] = um[0] + (up[1] * sv[2] - up[2] * sv[1]);
+      upl[1] = um[1] + (up[2] * sv[0] - up[0] * sv[2]);
+      upl[2] = um[2] + (up[0] * sv[1] - up[1] * sv[0]);
+      for (int d = 0; d < 3; d++) uf[d] = upl[d] + h * Ef[d];
+      gam = sqrt(1.0 + (uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2]) / cc2);
+      for (int d = 0; d < 3; d++) {
+        v[d] = uf[d] / gam;
+        x[d] += v[d] * dt;
+      }
+      ns++;
+    }
+    my_sub += (unsigned long long)ns;
+    // final block, cell and FP32 offset
+    rb_locate(a, x, bx, xmin);
+    int ic[3];
+    for (int d = 0; d < 3; d++) {
+      int ci = (int)((x[d] - xmin[d]) / a.dx[d]);
+      ci = min(max(ci, 0), AMPS_NC - 1);
+      float u = (float)((x[d] - xmin[d]) / a.dx[d]);
+      if (u < (float)ci) u = (float)ci;
+      if (u >= (float)(ci + 1)) u = nextafterf((float)(ci + 1), 0.0f);
+      ic[d] = ci;
+      a.d.u[d][p] = u;
+      a.d.v[d][p] = (float)v[d];
+    }
+    const int blk = bx[0] + a.nbk[0] * (bx[1] + a.nbk[1] * bx[2]);
+    a.key[p] = blk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+  }
+  if (my_sub) atomicAdd(a.nsub, my_sub);
+}
+
 int grid_for(long long n, int threads) {
   long long g = (n + threads - 1) / threads;
   if (g > 152LL * 64) g = 152LL * 64;
@@ -1100,6 +1247,48 @@ cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow) {
     k_gather_valid<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
         c->ncor, c->d_base, c->d_cnt, pbuf(c, c->cur), pbuf(c, c->cur ^ 1), c->d_key,
         c->d_flags + 4);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return rebuild_from_list(c, c->np);
+}
+
+// Relativistic Boris move of every particle: compact layout -> list buffer,
+// sub-stepped move with new keys, counting-sort rebuild.  Sub-step total in
+// flags[4] (read back by the caller).
+cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
+                            double c_light, long long max_sub) {
+  cudaError_t e = cudaMemsetAsync(c->d_flags + 4, 0, 2 * sizeof(unsigned long long), c->stream);
+  if (e != cudaSuccess) return e;
+  {
+    TimedLaunch t(c, "relboris_gather");
+    const long long threads = c->ncor * 32;
+    k_gather_valid<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+        c->ncor, c->d_base, c->d_cnt, pbuf(c, c->cur), pbuf(c, c->cur ^ 1), c->d_key,
+        c->d_flags + 4);
+  }
+  RelBorisArgs a;
+  a.d = pbuf(c, c->cur ^ 1);
+  a.key = c->d_key;
+  a.n = c->np;
+  a.nbr = c->d_nbr;
+  a.ncor = c->ncor;
+  a.E = E;
+  a.B = B;
+  a.nbk[0] = c->cfg.nbx; a.nbk[1] = c->cfg.nby; a.nbk[2] = c->cfg.nbz;
+  for (int d = 0; d < 3; d++) { a.x0[d] = c->cfg.x0[d]; a.dx[d] = c->cfg.dx[d]; }
+  for (int sp = 0; sp < AMPS_GPU_MAX_SPECIES; sp++) {
+    a.qm[sp] = sp < c->cfg.nspec ? c->cfg.charge[sp] / c->cfg.mass[sp] : 0.0;
+    a.qabs_over_m[sp] = sp < c->cfg.nspec ? fabs(c->cfg.charge[sp]) / c->cfg.mass[sp] : 0.0;
+  }
+  a.dt_total = dt_total;
+  a.c_light = c_light;
+  a.max_sub = max_sub;
+  a.flags = c->d_flags;
+  a.nsub = c->d_flags + 5;
+  {
+    TimedLaunch t(c, "relboris");
+    k_relboris<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

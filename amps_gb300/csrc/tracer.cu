@@ -11,7 +11,9 @@
 // warp refills them from a global queue with one atomic per warp (warp-level
 // compaction), so uneven lifetimes do not idle lanes.  State is carried in
 // normalised units (x / R_E, p / (m c), t c / R_E, B / B_eq) so the FP32
-// variant keeps full range; the host converts SI at the boundary.
+// variant keeps full range; the host converts SI at the boundary.  The FP32
+// variant accumulates positions with compensated (Kahan) sums: a half drift is
+// ~1e-2 of |x|, so plain FP32 sums would lose ~1e-5 of every displacement.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -63,11 +65,25 @@ __device__ __forceinline__ void field(const TraceArgs<T>& a, T x, T y, T z, T& b
   bz = T(3) * z * mdotr * ir5 - ir3 + a.ext[2];
 }
 
+// x += d with a running compensation c (FP32 only; FP64 sums are plain)
+template <class T>
+__device__ __forceinline__ void comp_add(T& x, T& c, T d) {
+  if constexpr (sizeof(T) == 4) {
+    const T yv = d - c;
+    const T t = x + yv;
+    c = (t - x) - yv;
+    x = t;
+  } else {
+    x += d;
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(256) k_trace(TraceArgs<T> a) {
   const int lane = threadIdx.x & 31;
   long long idx = -1;
   T x = 0, y = 0, z = 0, px = 0, py = 0, pz = 0;
+  T cx = 0, cy = 0, cz = 0;  // position compensation (FP32)
   long long st = 0;
   unsigned long long my_total = 0;
   bool queue_done = false;
@@ -90,6 +106,7 @@ __global__ void __launch_bounds__(256) k_trace(TraceArgs<T> a) {
           idx = (long long)mine;
           x = a.x[idx]; y = a.y[idx]; z = a.z[idx];
           px = a.px[idx]; py = a.py[idx]; pz = a.pz[idx];
+          cx = cy = cz = T(0);
           st = 0;
         }
       }
@@ -107,9 +124,9 @@ __global__ void __launch_bounds__(256) k_trace(TraceArgs<T> a) {
         const T om = fabs(a.kq) * bm / g;
         if (om > T(0) && a.dphi / om < dt) dt = a.dphi / om;
         const T ig = T(1) / g;
-        x += T(0.5) * dt * px * ig;
-        y += T(0.5) * dt * py * ig;
-        z += T(0.5) * dt * pz * ig;
+        comp_add(x, cx, T(0.5) * dt * px * ig);
+        comp_add(y, cy, T(0.5) * dt * py * ig);
+        comp_add(z, cz, T(0.5) * dt * pz * ig);
         const T f = a.kq * dt * T(0.5) * ig;
         const T tx = f * bx, ty = f * by, tz = f * bz;
         const T sfac = T(2) / (T(1) + tx * tx + ty * ty + tz * tz);
@@ -120,9 +137,9 @@ __global__ void __launch_bounds__(256) k_trace(TraceArgs<T> a) {
         py += sfac * (qz * tx - qx * tz);
         pz += sfac * (qx * ty - qy * tx);
         const T ig2 = T(1) / sqrt(T(1) + px * px + py * py + pz * pz);
-        x += T(0.5) * dt * px * ig2;
-        y += T(0.5) * dt * py * ig2;
-        z += T(0.5) * dt * pz * ig2;
+        comp_add(x, cx, T(0.5) * dt * px * ig2);
+        comp_add(y, cy, T(0.5) * dt * py * ig2);
+        comp_add(z, cz, T(0.5) * dt * pz * ig2);
         st++;
         const T r2 = x * x + y * y + z * z;
         if (r2 < a.r_in2) { status = 1; break; }

@@ -296,6 +296,15 @@ class EcsimContext:
         self._check(self.lib.amps_gpu_move_particles(self.h, C.byref(nout)), "MoveParticles")
         return nout.value
 
+    def MoveParticlesRelativistic(self, dt_total, light_speed=1.0):
+        """Mover::Relativistic::Boris on the mesh fields (E^n, corner B cur);
+        returns the number of sub-steps taken."""
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_move_particles_relativistic(self.h, dt_total, light_speed,
+                                                                  C.byref(n)),
+                    "Mover::Relativistic::Boris")
+        return n.value
+
     def UpdateJMassMatrix(self):
         e = C.c_double()
         self._check(self.lib.amps_gpu_update_j_mass_matrix(self.h, C.byref(e)),

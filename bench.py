@@ -416,6 +416,8 @@ def tracer_line(n32, n64, device):
     x32, p32, st32, s32, tot32, ms32 = T.trace_cutoff(n32, seed=7, precision=1, device=device)
     x64, p64, st64, s64, tot64, ms64 = T.trace_cutoff(n64, seed=7, precision=0, device=device)
     same = float(np.mean(st32[:n64] == st64))
+    short = s64 < 10000
+    same_short = float(np.mean(st32[:n64][short] == st64[short])) if short.any() else None
     return {"workload": "cutoff tracing: protons on r=1.1 R_E, isotropic, 0.1-20 GV log-uniform, "
                         "dipole B_eq=3.1e-5 T + 5 nT southward, stop r<1, r>10 R_E or 1e5 steps",
             "fp32": {"particles": n32, "particle_steps": int(tot32), "kernel_ms": ms32,
@@ -423,7 +425,10 @@ def tracer_line(n32, n64, device):
             "fp64": {"particles": n64, "particle_steps": int(tot64), "kernel_ms": ms64,
                      "particle_steps_per_s": tot64 / (ms64 / 1e3)},
             "status_agreement_fp32_vs_fp64": same,
-            "status_counts_fp32": {str(k): int(np.sum(st32 == k)) for k in np.unique(st32)}}
+            "status_agreement_lifetime_below_1e4_steps": same_short,
+            "status_fraction_fp32": {str(k): float(np.mean(st32[:n64] == k)) for k in (0, 1, 2)},
+            "status_fraction_fp64": {str(k): float(np.mean(st64 == k)) for k in (0, 1, 2)},
+            "status": "0 step budget, 1 r < 1 R_E, 2 r > 10 R_E"}
 
 
 # ---------------------------------------------------------------------------
@@ -536,7 +541,7 @@ def run_gpu(args):
         cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp}
     trc = None
     if rank == 0 and args.tracer > 0:
-        trc = tracer_line(args.tracer, max(1, args.tracer // 16), local)
+        trc = tracer_line(args.tracer, max(1, args.tracer // 256), local)
     pab = None
     if rank == 0 and args.precond_ab:
         pab = {"config": precond_ab("ecsim_32c_64ppc", local)}
@@ -615,7 +620,7 @@ def main():
     ap.add_argument("--graphs", type=int, default=1, help="particle step as a CUDA graph")
     ap.add_argument("--tracer", type=int, default=0,
                     help="also run the cutoff tracing workload with this many particles (FP32; "
-                         "FP64 on 1/16 of them)")
+                         "FP64 on 1/256 of them)")
     ap.add_argument("--precond-kernel", type=int, default=0,
                     help="time only the tensor-core inference kernel on this many blocks")
     ap.add_argument("--traffic", type=float, default=None,

@@ -182,6 +182,14 @@ amps_gpu_status amps_gpu_export_cell_moments(amps_gpu_ctx* ctx, double* cellJ, d
  * re-binning into destination cells (pic_mover.cpp:982-1087, periodic wrap of
  * pic_bc_periodic.cpp:55-178). */
 amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* ctx, long long* out_of_block);
+/* Mover::Relativistic::Boris (src/pic/pic_mover_relativistic_boris.cpp:16-583)
+ * on the mesh fields: every particle advances by dt_total in FP64 sub-steps of
+ * at most one gyro period (1/f_g, f_g = |q||B|/(2 pi m gamma)), with E = the
+ * corner E^n slot and B = the corner B "cur" slot interpolated at each
+ * sub-step's start, then re-binned.  light_speed in the context's units.
+ * Uniform meshes only.  substeps (optional) receives the total sub-steps. */
+amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* ctx, double dt_total,
+                                                     double light_speed, long long* substeps);
 /* ECSIM::UpdateJMassMatrix (pic_field_solver_ecsim.cpp:3244): J and the
  * 243-term mass matrix on all corners from the corner B "cur" slot. */
 amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* ctx, double* particle_energy);

@@ -261,6 +261,76 @@ long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* sp
   return nbad;
 }
 
+/* Mover::Relativistic::Boris (src/pic/pic_mover_relativistic_boris.cpp:16-583,
+ * scalar path :119-175) on the mesh fields: sub-steps of dt = min(1/f_g,
+ * remaining) with f_g = |q||B|/(2 pi m gamma) (specfunc.h:1290), fields at the
+ * sub-step's start position (corner-interpolated E and B), u = gamma v,
+ * u- = u + (q dt/2m) E, t = (q dt/2m / gamma(u-)) B, u' = u- + u- x t,
+ * s = 2t/(1+|t|^2), u+ = u- + u' x s, u = u+ + (q dt/2m) E, x += v dt;
+ * periodic re-location after every sub-step (findTreeNode).  c = light speed in
+ * the mesh's units.  Returns the number of sub-steps. */
+long orc_relboris(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
+                  int32_t* block, int32_t* cell, const double* E, const double* B, double dt_total,
+                  double c_light) {
+  long nsub = 0;
+  for (long p = 0; p < n; p++) {
+    double xI[3], vI[3];
+    for (int d = 0; d < 3; d++) { xI[d] = x[3 * p + d]; vI[d] = v[3 * p + d]; }
+    const int sp = spec[p];
+    const double q = g->q[sp], m = g->m[sp];
+    double rem = dt_total;
+    while (rem > 0.0) {
+      int bxyz[3], iX[3], nd[8][3];
+      double xmin[3], wt[8], wn[8], xs[3] = {xI[0], xI[1], xI[2]};
+      locate_one(g, xs, block + p, cell + p);
+      for (int d = 0; d < 3; d++) xI[d] = xs[d];
+      block_geom(g, block[p], bxyz, xmin);
+      corner_stencil(xmin, g->dx, xs, wt, wn, nd, iX);
+      double Ef[3] = {0, 0, 0}, Bf[3] = {0, 0, 0};
+      for (int s2 = 0; s2 < 8; s2++) {
+        long c = cidx(g, bxyz[0] * NC + iX[0] + nd[s2][0], bxyz[1] * NC + iX[1] + nd[s2][1],
+                      bxyz[2] * NC + iX[2] + nd[s2][2]);
+        for (int d = 0; d < 3; d++) {
+          Ef[d] += wn[s2] * E[3 * c + d];
+          Bf[d] += wn[s2] * B[3 * c + d];
+        }
+      }
+      const double v2 = vI[0] * vI[0] + vI[1] * vI[1] + vI[2] * vI[2];
+      double gam = 1.0 / sqrt(1.0 - v2 / (c_light * c_light));
+      const double bmag = sqrt(Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
+      double dt = rem;
+      if (bmag > 1.0e-25) {
+        const double fg = fabs(q) * bmag / (2.0 * PI_D * m * gam);
+        const double dtmax = 1.0 / fg;
+        if (dtmax < rem) dt = dtmax;
+      }
+      rem -= dt;
+      const double h = q * dt / (2.0 * m);
+      double um[3], t[3], up[3], s[3], upl[3], uf[3], l = 0.0;
+      for (int d = 0; d < 3; d++) um[d] = gam * vI[d] + h * Ef[d];
+      gam = sqrt(1.0 + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]) / (c_light * c_light));
+      for (int d = 0; d < 3; d++) { t[d] = h / gam * Bf[d]; l += t[d] * t[d]; }
+      up[0] = um[0] + (um[1] * t[2] - um[2] * t[1]);
+      up[1] = um[1] + (um[2] * t[0] - um[0] * t[2]);
+      up[2] = um[2] + (um[0] * t[1] - um[1] * t[0]);
+      for (int d = 0; d < 3; d++) s[d] = 2.0 * t[d] / (1.0 + l);
+      upl[0] = um[0] + (up[1] * s[2] - up[2] * s[1]);
+      upl[1] = um[1] + (up[2] * s[0] - up[0] * s[2]);
+      upl[2] = um[2] + (up[0] * s[1] - up[1] * s[0]);
+      for (int d = 0; d < 3; d++) uf[d] = upl[d] + h * Ef[d];
+      gam = sqrt(1.0 + (uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2]) / (c_light * c_light));
+      for (int d = 0; d < 3; d++) {
+        vI[d] = uf[d] / gam;
+        xI[d] += vI[d] * dt;
+      }
+      nsub++;
+    }
+    locate_one(g, xI, block + p, cell + p);
+    for (int d = 0; d < 3; d++) { x[3 * p + d] = xI[d]; v[3 * p + d] = vI[d]; }
+  }
+  return nsub;
+}
+
 /* IndexMatrix[c1][c2] of ProcessCell (pic_field_solver_ecsim.cpp:1889-1891):
  * neighbour slot of corner c2 as seen from corner c1. */
 static int index_matrix(int c1, int c2) {

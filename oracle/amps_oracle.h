@@ -52,6 +52,11 @@ void orc_graddiv_table(int p, int q, double out[27]);
 void orc_corner_weights(const double xloc[3], double w_table[8]);
 long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
               int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev);
+/* Mover::Relativistic::Boris on the mesh corner fields E, B (sub-stepped by the
+ * gyro period); returns the number of sub-steps */
+long orc_relboris(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
+                  int32_t* block, int32_t* cell, const double* E, const double* B, double dt_total,
+                  double c_light);
 double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
                    const uint8_t* spec, const double* wcorr, const int32_t* block,
                    const int32_t* cell, const double* Bc_cur, double* J, double* M);

@@ -46,7 +46,7 @@ typedef struct {
 static const int kOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
                                {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
 
-static int wrapi(int v, int n) { v %= n; return v < 0 ? v + n : v; }
+
 
 static double bdx(const orc_amr* g, int b) { return g->dx0 / (double)(1 << g->level[b]); }
 

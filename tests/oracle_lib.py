@@ -41,6 +41,8 @@ def load():
         "orc_graddiv_table": (None, [C.c_int, C.c_int, D]),
         "orc_corner_weights": (None, [D, D]),
         "orc_push": (C.c_long, [C.POINTER(Mesh), C.c_long, D, D, U8, I32, I32, D, D]),
+        "orc_relboris": (C.c_long, [C.POINTER(Mesh), C.c_long, D, D, U8, I32, I32, D, D,
+                                    C.c_double, C.c_double]),
         "orc_deposit": (C.c_double, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D]),
         "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
         "orc_center_to_corner": (None, [C.POINTER(Mesh), D, D]),
@@ -109,6 +111,13 @@ class OracleState:
         self.Bcur = np.ascontiguousarray(fields["B_corner_cur"], np.float64).copy()
         self.J = np.zeros((nc, 3))
         self.M = np.zeros((nc, 243))
+
+    def relboris(self, dt_total, c_light=1.0):
+        """Mover::Relativistic::Boris on E^n and the corner B cur slot"""
+        return self.lib.orc_relboris(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
+                                     p(self.spec, C.c_uint8), p(self.block, C.c_int32),
+                                     p(self.cell, C.c_int32), p(self.E_n), p(self.Bcur),
+                                     dt_total, c_light)
 
     def push(self):
         return self.lib.orc_push(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
