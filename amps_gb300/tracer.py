@@ -29,9 +29,13 @@ def sphere_starts(n, seed, r0=1.1, rig_gv=(0.1, 20.0)):
 
 
 def trace_cutoff(n, seed=7, precision=0, max_steps=100000, b_eq=3.1e-5, b_south=5e-9,
-                 device=0):
-    """Runs the workload; returns (x, p, status, steps, total_steps, kernel_ms)."""
-    x, p = sphere_starts(n, seed)
+                 device=0, starts=None):
+    """Runs the workload (on `starts` = (x, p) when given, else n seeded starts);
+    returns (x, p, status, steps, total_steps, kernel_ms)."""
+    if starts is None:
+        x, p = sphere_starts(n, seed)
+    else:
+        x, p = (np.ascontiguousarray(a[:n], np.float64).copy() for a in starts)
     st, steps, tot, ms = trace_dipole(x, p, Q_P, M_P, b_eq, R_E,
                                       np.array([0.0, 0.0, -b_south]), R_E, 10.0 * R_E, max_steps,
                                       0.15, 10.0, precision, device)

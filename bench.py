@@ -413,8 +413,10 @@ def tracer_line(n32, n64, device):
     """Batched relativistic test-particle tracing (cutoff workload): particle-steps/s
     in FP32 on n32 particles and FP64 on the first n64 of them; status agreement."""
     from amps_gb300 import tracer as T
-    x32, p32, st32, s32, tot32, ms32 = T.trace_cutoff(n32, seed=7, precision=1, device=device)
-    x64, p64, st64, s64, tot64, ms64 = T.trace_cutoff(n64, seed=7, precision=0, device=device)
+    starts = T.sphere_starts(n32, 7)
+    x32, p32, st32, s32, tot32, ms32 = T.trace_cutoff(n32, precision=1, device=device, starts=starts)
+    # FP64 on the first n64 of the same particles
+    x64, p64, st64, s64, tot64, ms64 = T.trace_cutoff(n64, precision=0, device=device, starts=starts)
     same = float(np.mean(st32[:n64] == st64))
     short = s64 < 10000
     same_short = float(np.mean(st32[:n64][short] == st64[short])) if short.any() else None
@@ -483,6 +485,24 @@ def run_gpu(args):
         ev.record(b2, stream)
         t_step.append(ev.elapsed_ms(a2, b2))
     gmres_it = s.solve.iterations
+
+    # energy conservation over many full ECSIM steps (theta = 0.5)
+    energy = None
+    if args.energy_steps > 0:
+        tot = []
+        its = []
+        t0 = time.perf_counter()
+        for _ in range(args.energy_steps):
+            s = ctx.PicTimeStep(tol=tol, maxit=400, precond=1)
+            tot.append(s.particle_energy + s.solve.wave_energy)
+            its.append(s.solve.iterations)
+        wall = time.perf_counter() - t0
+        tot = np.array(tot)
+        energy = {"steps": args.energy_steps, "total_energy_first": float(tot[0]),
+                  "total_energy_last": float(tot[-1]),
+                  "max_relative_drift": float(np.max(np.abs(tot - tot[0])) / abs(tot[0])),
+                  "gmres_iterations_mean": float(np.mean(its)),
+                  "wall_ms_per_step": wall * 1e3 / args.energy_steps}
 
     # end to end through the reference-facing C ABI with host FP64 buffers
     e2e = None
@@ -560,7 +580,7 @@ def run_gpu(args):
                 "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations,
                 "cuda_graphs": args.graphs > 0, "autotune": tuning}),
             "e2e": e2e, "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
-            "precond_ab": pab, "tracer": trc,
+            "precond_ab": pab, "tracer": trc, "energy": energy,
             "clocks": clocks, "gpu_launches": gpu_launches,
         }
         print(json.dumps(line), flush=True)
@@ -618,6 +638,8 @@ def main():
     ap.add_argument("--precond-stiff", type=int, default=1,
                     help="also the same A/B at dt = 1/omega_pe")
     ap.add_argument("--graphs", type=int, default=1, help="particle step as a CUDA graph")
+    ap.add_argument("--energy-steps", type=int, default=0,
+                    help="also run this many full ECSIM steps and report the energy drift")
     ap.add_argument("--tracer", type=int, default=0,
                     help="also run the cutoff tracing workload with this many particles (FP32; "
                          "FP64 on 1/256 of them)")

@@ -18,18 +18,21 @@ def test_relboris_matches_oracle(dt_total, vscale):
     v = ic["v"].astype(np.float64)
     sp = np.linalg.norm(v, axis=1)
     v = np.where(sp[:, None] >= 0.95, v * (0.95 / sp)[:, None], v)   # keep |v| < c
-    st = O.OracleState(wl, x, v, ic["spec"], f)
     with A.EcsimContext(wl, capacity=len(x) + 1024, track_ids=True) as ctx:
         ctx.import_particles(x, v, ic["spec"])
         ctx.import_fields(**f)
+        # the oracle starts from the device's FP32-stored state
+        e0 = by_id(ctx.export_particles())
         nsub = ctx.MoveParticlesRelativistic(dt_total, 1.0)
         e = by_id(ctx.export_particles())
+    st = O.OracleState(wl, e0["x"], e0["v"], e0["spec"], f)
     nsub_ref = st.relboris(dt_total, 1.0)
     assert nsub > len(x) and abs(nsub - nsub_ref) <= max(2, nsub_ref // 10000)
-    assert rel_err(e["v"], st.v) < 2e-5
+    # the device stores the result in FP32 (offsets and velocities)
+    assert rel_err(e["v"], st.v) < 2e-6
     L = np.array(wl.mesh.shape, float) * wl.mesh.dx
     d = e["x"] - st.x
     d -= L * np.rint(d / L)
-    assert np.max(np.abs(d)) < 2e-5 * dt_total
+    assert np.max(np.abs(d)) < 2e-6 * wl.mesh.dx * max(1.0, dt_total / 10.0)
     mism = (e["block"] != st.block) | (e["cell"] != st.cell)
     assert np.all(face_distance(st.x[mism]) < 1e-4), mism.sum()
