@@ -155,16 +155,17 @@ __global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a, T* __restrict_
     cell_curl_t<T>(cu, sg * (T)a.th2dt2 * V * (T)0.25 / dx, out);
   }
   if (a.with_mass) {
-    const float* mm = a.cellM + cell * 324;
+    // pair (c1, c2) uses the cell's partial of its weight monomial
+    const float* mm = a.cellM + cell * AMPS_CELLM;
     const T fv = sg * (T)a.f * V;
-    int pr = 0;
 #pragma unroll
     for (int c1 = 0; c1 < 8; c1++)
 #pragma unroll
-      for (int c2 = 0; c2 <= c1; c2++, pr++) {
+      for (int c2 = 0; c2 <= c1; c2++) {
+        const int mo = pair_monomial(c1, c2);
         T m9[9];
 #pragma unroll
-        for (int t = 0; t < 9; t++) m9[t] = fv * from_f32<T>(mm[pr * 9 + t]);
+        for (int t = 0; t < 9; t++) m9[t] = fv * from_f32<T>(mm[mo * 9 + t]);
 #pragma unroll
         for (int p = 0; p < 3; p++) {
           out[c1][p] += m9[3 * p] * e[c2][0] + m9[3 * p + 1] * e[c2][1] + m9[3 * p + 2] * e[c2][2];
@@ -252,12 +253,12 @@ __global__ void __launch_bounds__(256) k_amr_diag(long long ncell, long long nvc
   const int b = (int)(cell >> 9), l = (int)(cell & 511);
   const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
   const double dx = bdx[b], V = dx * dx * dx;
-  const float* mm = cellM + cell * 324;
+  const float* mm = cellM + cell * AMPS_CELLM;
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     const int cc = ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
     if (h.hs[cc + 1] > h.hs[cc]) continue;
-    const float* blk = mm + (c * (c + 1) / 2 + c) * 9;
+    const float* blk = mm + pair_monomial(c, c) * 9;
 #pragma unroll
     for (int d = 0; d < 3; d++)
       atomicAdd(diag + d * nvc + cc,

@@ -348,7 +348,7 @@ bool alloc_context(amps_gpu_ctx* c) {
        !dalloc(&c->d_stay, nc) && !dalloc(&c->d_tmp, nc + 1) && !dalloc(&c->d_count, nc + 1) &&
        !dalloc(&c->d_scan_part, (nc + 1) / 1024 + 2) && !dalloc(&c->d_flags, 8);
   ok = ok && cudaMallocHost(&c->h_flags, 8 * sizeof(unsigned long long)) == cudaSuccess;
-  ok = ok && !dalloc(&c->d_cellM, 324 * nc) && !dalloc(&c->d_cellJ, 24 * nc) &&
+  ok = ok && !dalloc(&c->d_cellM, (size_t)AMPS_CELLM * nc) && !dalloc(&c->d_cellJ, 24 * nc) &&
        !dalloc(&c->d_energy, 4);
   ok = ok && cudaMallocHost(&c->h_energy, 4 * sizeof(double)) == cudaSuccess;
   if (!ok) {
@@ -362,7 +362,7 @@ bool alloc_context(amps_gpu_ctx* c) {
     ok = ok && cudaMemset(c->d_J, 0, sizeof(double) * 3 * nc) == cudaSuccess &&
          cudaMemset(c->d_M, 0, sizeof(float) * 243 * nc) == cudaSuccess;
   // cell partials start at zero so an AMR solve before any deposit is defined
-  ok = ok && cudaMemset(c->d_cellM, 0, sizeof(float) * 324 * nc) == cudaSuccess &&
+  ok = ok && cudaMemset(c->d_cellM, 0, sizeof(float) * AMPS_CELLM * nc) == cudaSuccess &&
        cudaMemset(c->d_cellJ, 0, sizeof(float) * 24 * nc) == cudaSuccess;
   // empty layout: every cell has 8 slack slots
   {
@@ -794,11 +794,22 @@ amps_gpu_status amps_gpu_export_cell_moments(amps_gpu_ctx* c, double* cellJ, dou
     for (size_t i = 0; i < t.size(); i++) cellJ[i] = (double)t[i];
   }
   if (cellM) {
-    std::vector<float> t((size_t)(324 * nc));
+    // device: 27 weight-monomial sums per cell; host: ProcessCell's 36 pairs
+    std::vector<float> t((size_t)(AMPS_CELLM * nc));
     s = cuda_check(c, cudaMemcpy(t.data(), c->d_cellM, sizeof(float) * t.size(), cudaMemcpyDeviceToHost),
                    "download cellM");
     if (s) return s;
-    for (size_t i = 0; i < t.size(); i++) cellM[i] = (double)t[i];
+    static const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1},
+                     oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    for (long long cl = 0; cl < nc; cl++) {
+      int pr = 0;
+      for (int c1 = 0; c1 < 8; c1++)
+        for (int c2 = 0; c2 <= c1; c2++, pr++) {
+          const int mo = (ox[c1] + ox[c2]) + 3 * (oy[c1] + oy[c2]) + 9 * (oz[c1] + oz[c2]);
+          for (int e = 0; e < 9; e++)
+            cellM[(size_t)cl * 324 + pr * 9 + e] = (double)t[(size_t)cl * AMPS_CELLM + mo * 9 + e];
+        }
+    }
   }
   return AMPS_GPU_OK;
 }

@@ -26,6 +26,7 @@
 #define AMPS_PUSH_STRIDE 8  // floats per stencil corner for the push: E3 B3 pad2
 #define AMPS_DEP_STRIDE 4   // floats per stencil corner for the deposit: B3 pad1
 #define AMPS_SLACK_MIN 32   // slack slots per cell on top of count/4 (rebuild)
+#define AMPS_CELLM 243      // per-cell mass-matrix partials: 27 weight monomials x 9
 
 struct KernelTimer {
   const char* name;
@@ -144,7 +145,7 @@ struct amps_gpu_ctx {
   unsigned long long* h_flags = nullptr;  // pinned
 
   // deposition scratch: per-cell partial sums
-  float* d_cellM = nullptr;     // ncor * 324
+  float* d_cellM = nullptr;     // ncor * AMPS_CELLM
   float* d_cellJ = nullptr;     // ncor * 24
   double* d_energy = nullptr;   // [0] particle, [1] wave
   double* h_energy = nullptr;   // pinned

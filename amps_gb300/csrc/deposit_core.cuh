@@ -13,7 +13,11 @@
 
 namespace {
 constexpr uint32_t kWaitLimit = 1u << 24;
-constexpr int kRec = 60;      // floats per staged particle record
+// floats per staged particle record: 64 used; the stride of 68 (272 B) puts the
+// records of 8 consecutive lanes in distinct 16-byte bank groups, so a warp's
+// 16-byte record stores run without bank conflicts
+constexpr int kRec = 68;
+constexpr int kTileLanes = 30;  // lanes owning a 3 x 3 output tile
 constexpr int kWarps = 8;     // warps per CTA (one row of 8 cells each)
 constexpr uint8_t kHole = 0xFF;
 
@@ -58,10 +62,20 @@ __device__ bool stage_stencils(uint64_t* bar, void* dst0, const void* src0, uint
 // ---------------------------------------------------------------------------
 // Deposition pieces shared by k_push_deposit, k_arrivals and k_deposit.
 
-// Per-cell partial sums: 36 pairs x 9 (mass matrix) and 8 corners x 3 (current),
-// contiguous per cell.
+// Per-cell partial sums, contiguous per cell.  Mass matrix: the product of two
+// trilinear corner weights depends only on the per-axis sums a_d = o1_d + o2_d
+// of the corners' offsets, w_c1 w_c2 = X_x[a_x] X_y[a_y] X_z[a_z] with
+// X[0] = (1-f)^2, X[1] = f(1-f), X[2] = f^2, so ProcessCell's 36 corner-pair
+// blocks are 27 distinct monomial sums x 9 (index (a_x + 3 a_y + 9 a_z) * 9 +
+// row * 3 + col).  Current: 8 corners x 3.
 __host__ __device__ __forceinline__ long long cellM_at(long long cid, int pe) {
-  return cid * 324 + pe;
+  return cid * AMPS_CELLM + pe;
+}
+// monomial index of the corner pair (c1, c2) in the table order of the corners
+__host__ __device__ __forceinline__ int pair_monomial(int c1, int c2) {
+  const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1},
+            oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  return (ox[c1] + ox[c2]) + 3 * (oy[c1] + oy[c2]) + 9 * (oz[c1] + oz[c2]);
 }
 __host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
   return cid * 24 + ce;
@@ -109,53 +123,66 @@ __device__ __forceinline__ float stage_record(float* __restrict__ r, const float
   const float kc = qW * h * inv_vol;
   float4* r4 = reinterpret_cast<float4*>(r);
   {
-    float ww[36];
-    int pr = 0;
+    // 27 weight monomials in groups of 3 (+1 pad): record floats 0..35
+    const float X[3] = {gx * gx, gx * fx, fx * fx};
+    const float Y[3] = {gy * gy, gy * fy, fy * fy};
+    const float Z[3] = {gz * gz, gz * fz, fz * fz};
+    float m[27];
 #pragma unroll
-    for (int c1 = 0; c1 < 8; c1++)
+    for (int c = 0; c < 3; c++)
 #pragma unroll
-      for (int c2 = 0; c2 <= c1; c2++, pr++) ww[pr] = w[c1] * w[c2];
+      for (int b = 0; b < 3; b++) {
+        const float yz = Y[b] * Z[c];
 #pragma unroll
-    for (int t = 0; t < 9; t++) r4[t] = make_float4(ww[4 * t], ww[4 * t + 1], ww[4 * t + 2], ww[4 * t + 3]);
+        for (int a = 0; a < 3; a++) m[a + 3 * b + 9 * c] = X[a] * yz;
+      }
+#pragma unroll
+    for (int g = 0; g < 9; g++) r4[g] = make_float4(m[3 * g], m[3 * g + 1], m[3 * g + 2], 0.f);
   }
+  // k alpha rows (36..47), corner weights in groups of 3 (48..59), q W alpha v (60..63)
   r4[9] = make_float4(kc * al[0], kc * al[1], kc * al[2], 0.f);
   r4[10] = make_float4(kc * al[3], kc * al[4], kc * al[5], 0.f);
   r4[11] = make_float4(kc * al[6], kc * al[7], kc * al[8], 0.f);
-  r4[12] = make_float4(w[0], w[1], w[2], w[3]);
-  r4[13] = make_float4(w[4], w[5], w[6], w[7]);
+  r4[12] = make_float4(w[0], w[1], w[2], 0.f);
+  r4[13] = make_float4(w[3], w[4], w[5], 0.f);
+  r4[14] = make_float4(w[6], w[7], 0.f, 0.f);
   const float vr0 = al[0] * v0 + al[1] * v1 + al[2] * v2;
   const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
   const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
-  r4[14] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
+  r4[15] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
   return 0.5f * mW * (v0 * v0 + v1 * v1 + v2 * v2);
 }
 
+// Each of the first kTileLanes lanes owns a 3 x 3 tile: lanes 0..26 the
+// products (monomials 3g..3g+2) x (k alpha row hh), lanes 27..29 the products
+// (corner weights 3g'..3g'+2) x (q W alpha v).  A record costs every lane two
+// 16-byte shared loads and 9 FMAs.
 struct Tile {
-  float sum[12], cmp[12];
+  float sum[9], cmp[9];
   __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int e = 0; e < 12; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
+    for (int e = 0; e < 9; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
   }
   // accumulate the cnt staged records of the warp, then compensated add
   __device__ __forceinline__ void accumulate(const float* __restrict__ rec, int cnt, int offA,
                                              int offB) {
-    float acc[12];
+    float acc[9];
 #pragma unroll
-    for (int e = 0; e < 12; e++) acc[e] = 0.f;
+    for (int e = 0; e < 9; e++) acc[e] = 0.f;
 #pragma unroll 4
     for (int r = 0; r < cnt; r++) {
       const float4 A = *reinterpret_cast<const float4*>(rec + r * kRec + offA);
       const float4 B = *reinterpret_cast<const float4*>(rec + r * kRec + offB);
-      const float av[4] = {A.x, A.y, A.z, A.w};
+      const float av[3] = {A.x, A.y, A.z};
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
+      for (int q = 0; q < 3; q++) {
         acc[3 * q + 0] = fmaf(av[q], B.x, acc[3 * q + 0]);
         acc[3 * q + 1] = fmaf(av[q], B.y, acc[3 * q + 1]);
         acc[3 * q + 2] = fmaf(av[q], B.z, acc[3 * q + 2]);
       }
     }
 #pragma unroll
-    for (int e = 0; e < 12; e++) {
+    for (int e = 0; e < 9; e++) {
       const float y = acc[e] - cmp[e];
       const float t = sum[e] + y;
       cmp[e] = (t - sum[e]) - y;
@@ -168,30 +195,39 @@ struct Tile {
     if (lane < 27) {
       const int g = lane / 3, hh = lane % 3;
 #pragma unroll
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < 3; q++)
 #pragma unroll
         for (int e = 0; e < 3; e++) {
-          const long long o = cellM_at(cid, (4 * g + q) * 9 + 3 * hh + e);
+          const long long o = cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e);
           const float v = sum[3 * q + e] - cmp[3 * q + e];
           cellM[o] = add ? cellM[o] + v : v;
         }
-    } else if (lane < 29) {
+    } else if (lane < kTileLanes) {
       const int g = lane - 27;
 #pragma unroll
-      for (int q = 0; q < 4; q++)
+      for (int q = 0; q < 3; q++) {
+        const int corner = 3 * g + q;
+        if (corner < 8) {
 #pragma unroll
-        for (int e = 0; e < 3; e++) {
-          const long long o = cellJ_at(cid, (4 * g + q) * 3 + e);
-          const float v = sum[3 * q + e] - cmp[3 * q + e];
-          cellJ[o] = add ? cellJ[o] + v : v;
+          for (int e = 0; e < 3; e++) {
+            const long long o = cellJ_at(cid, corner * 3 + e);
+            const float v = sum[3 * q + e] - cmp[3 * q + e];
+            cellJ[o] = add ? cellJ[o] + v : v;
+          }
         }
+      }
     }
   }
 };
 
 __device__ __forceinline__ void lane_offsets(int lane, int& offA, int& offB) {
-  offA = lane < 27 ? 4 * (lane / 3) : 48 + 4 * (lane - 27);
-  offB = lane < 27 ? 36 + 4 * (lane % 3) : 56;
+  if (lane < 27) {
+    offA = 4 * (lane / 3);
+    offB = 36 + 4 * (lane % 3);
+  } else {
+    offA = lane < kTileLanes ? 48 + 4 * (lane - 27) : 0;
+    offB = 60;
+  }
 }
 
 __device__ __forceinline__ void reduce_energy(double en, double* s_en, double* energy) {

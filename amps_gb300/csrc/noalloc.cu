@@ -31,7 +31,7 @@ namespace {
 constexpr int kMaxBlocks = 16;
 constexpr long long kMaxCells = (long long)kMaxBlocks * AMPS_CPB;
 constexpr size_t kStencilBytes = (size_t)kMaxBlocks * AMPS_SC * AMPS_DEP_STRIDE * sizeof(float);
-constexpr size_t kCellMBytes = (size_t)kMaxCells * 324 * sizeof(float);
+constexpr size_t kCellMBytes = (size_t)kMaxCells * AMPS_CELLM * sizeof(float);
 constexpr size_t kCellJBytes = (size_t)kMaxCells * 24 * sizeof(float);
 constexpr size_t kScratchBytes = kStencilBytes + kCellMBytes + kCellJBytes;
 static_assert(kStencilBytes % 256 == 0 && kCellMBytes % 256 == 0, "scratch sub-array alignment");
@@ -46,24 +46,24 @@ constexpr int kMaxDevices = 64;
 unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
 std::mutex g_setup_mu;
 
-// (slot, cell, pair) entries of the corner assembly grouped by slot, and the
-// table index of the corner inside each of its 8 cells (the same tables the
-// context path builds at run time).
+// (slot, cell, weight monomial) entries of the corner assembly grouped by slot,
+// and the table index of the corner inside each of its 8 cells (the same tables
+// the context path builds at run time).
 struct NaEntry {
-  unsigned char slot, cell, pair, pad;
+  unsigned char slot, cell, mono, pad;
 };
 __constant__ NaEntry c_na_asm[64] = {
-    {0, 0, 0, 0},   {0, 1, 2, 0},   {0, 2, 9, 0},   {0, 3, 5, 0},   {0, 4, 14, 0},  {0, 5, 20, 0},
-    {0, 6, 35, 0},  {0, 7, 27, 0},  {1, 1, 1, 0},   {1, 3, 8, 0},   {1, 5, 19, 0},  {1, 7, 34, 0},
-    {2, 0, 1, 0},   {2, 2, 8, 0},   {2, 4, 19, 0},  {2, 6, 34, 0},  {3, 2, 6, 0},   {3, 3, 4, 0},
-    {3, 6, 32, 0},  {3, 7, 26, 0},  {4, 3, 3, 0},   {4, 7, 25, 0},  {5, 2, 7, 0},   {5, 6, 33, 0},
-    {6, 0, 6, 0},   {6, 1, 4, 0},   {6, 4, 32, 0},  {6, 5, 26, 0},  {7, 1, 7, 0},   {7, 5, 33, 0},
-    {8, 0, 3, 0},   {8, 4, 25, 0},  {9, 4, 10, 0},  {9, 5, 16, 0},  {9, 6, 31, 0},  {9, 7, 23, 0},
-    {10, 5, 15, 0}, {10, 7, 24, 0}, {11, 4, 11, 0}, {11, 6, 30, 0}, {12, 6, 28, 0}, {12, 7, 22, 0},
-    {13, 7, 21, 0}, {14, 6, 29, 0}, {15, 4, 13, 0}, {15, 5, 17, 0}, {16, 5, 18, 0}, {17, 4, 12, 0},
-    {18, 0, 10, 0}, {18, 1, 16, 0}, {18, 2, 31, 0}, {18, 3, 23, 0}, {19, 1, 11, 0}, {19, 3, 30, 0},
-    {20, 0, 15, 0}, {20, 2, 24, 0}, {21, 2, 13, 0}, {21, 3, 17, 0}, {22, 3, 12, 0}, {23, 2, 18, 0},
-    {24, 0, 28, 0}, {24, 1, 22, 0}, {25, 1, 29, 0}, {26, 0, 21, 0}};
+    {0, 0, 0, 0}, {0, 1, 2, 0}, {0, 2, 6, 0}, {0, 3, 8, 0}, {0, 4, 18, 0}, {0, 5, 20, 0},
+    {0, 6, 24, 0}, {0, 7, 26, 0}, {1, 1, 1, 0}, {1, 3, 7, 0}, {1, 5, 19, 0}, {1, 7, 25, 0},
+    {2, 0, 1, 0}, {2, 2, 7, 0}, {2, 4, 19, 0}, {2, 6, 25, 0}, {3, 2, 3, 0}, {3, 3, 5, 0},
+    {3, 6, 21, 0}, {3, 7, 23, 0}, {4, 3, 4, 0}, {4, 7, 22, 0}, {5, 2, 4, 0}, {5, 6, 22, 0},
+    {6, 0, 3, 0}, {6, 1, 5, 0}, {6, 4, 21, 0}, {6, 5, 23, 0}, {7, 1, 4, 0}, {7, 5, 22, 0},
+    {8, 0, 4, 0}, {8, 4, 22, 0}, {9, 4, 9, 0}, {9, 5, 11, 0}, {9, 6, 15, 0}, {9, 7, 17, 0},
+    {10, 5, 10, 0}, {10, 7, 16, 0}, {11, 4, 10, 0}, {11, 6, 16, 0}, {12, 6, 12, 0}, {12, 7, 14, 0},
+    {13, 7, 13, 0}, {14, 6, 13, 0}, {15, 4, 12, 0}, {15, 5, 14, 0}, {16, 5, 13, 0}, {17, 4, 13, 0},
+    {18, 0, 9, 0}, {18, 1, 11, 0}, {18, 2, 15, 0}, {18, 3, 17, 0}, {19, 1, 10, 0}, {19, 3, 16, 0},
+    {20, 0, 10, 0}, {20, 2, 16, 0}, {21, 2, 12, 0}, {21, 3, 14, 0}, {22, 3, 13, 0}, {23, 2, 13, 0},
+    {24, 0, 12, 0}, {24, 1, 14, 0}, {25, 1, 13, 0}, {26, 0, 13, 0}};
 __constant__ unsigned char c_na_corner[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 
 struct NaMesh {
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
                                 a.v[p], a.v[a.n + p], a.v[2 * a.n + p], a.sp[p], 1.0f, i, j, k,
                                 a.st, a.inv_vol);
       __syncwarp();
-      if (lane < 29) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
+      if (lane < kTileLanes) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(256) k_na_assemble(NaMesh m, long long ncor,
       }
       cur = en.slot;
     }
-    const float* src = cellM + cellM_at(cell[en.cell], en.pair * 9);
+    const float* src = cellM + cellM_at(cell[en.cell], en.mono * 9);
 #pragma unroll
     for (int e = 0; e < 9; e++) acc[e] += src[e];
   }

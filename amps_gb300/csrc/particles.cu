@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
       const int cst = __popc(smask);
       if (DEP) {
         __syncwarp();
-        if (lane < 29 && cst > 0) tile.accumulate(rec, cst, offA, offB);
+        if (lane < kTileLanes && cst > 0) tile.accumulate(rec, cst, offA, offB);
         __syncwarp();
       }
       nst += cst;
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
         if (DEP) {
           __syncwarp();
           const int cnt = min(32, na - q0);
-          if (lane < 29) tile.accumulate(rec, cnt, offA, offB);
+          if (lane < kTileLanes) tile.accumulate(rec, cnt, offA, offB);
           __syncwarp();
         }
       }
@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
                                 a.p.v[0][p], a.p.v[1][p], a.p.v[2][p], a.p.sp[p],
                                 a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, inv_vol);
       __syncwarp();
-      if (lane < 29) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
+      if (lane < kTileLanes) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
@@ -489,10 +489,11 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
 
 // ---------------------------------------------------------------------------
 // Corner assembly.  For corner c and each of its 8 cells, the pair (c, c2) of
-// that cell lands in slot(c2 - c) of M_c.  The 64 (slot, cell, pair) entries are
+// that cell lands in slot(c2 - c) of M_c; its block is the cell's partial of
+// the pair's weight monomial.  The 64 (slot, cell, monomial) entries are
 // grouped by slot so each output slot is written once.
 struct AsmEntry {
-  unsigned char slot, cell, pair, pad;
+  unsigned char slot, cell, mono, pad;
 };
 __constant__ AsmEntry c_asm[64];
 __constant__ unsigned char c_asm_corner[8];
@@ -524,7 +525,7 @@ __global__ void __launch_bounds__(256) k_assemble(long long ncor, const int* __r
       }
       cur = en.slot;
     }
-    const float* src = cellM + cellM_at(cell[en.cell], en.pair * 9);
+    const float* src = cellM + cellM_at(cell[en.cell], en.mono * 9);
 #pragma unroll
     for (int e = 0; e < 9; e++) acc[e] += src[e];
   }
@@ -1047,10 +1048,9 @@ void init_asm_table() {
       for (int c2 = 0; c2 < 8; c2++) {
         const int ddx = off[c2][0] - lx, ddy = off[c2][1] - ly, ddz = off[c2][2] - lz;
         if (mm_slot(ddx, ddy, ddz) != slot) continue;
-        const int hi = c1 > c2 ? c1 : c2, lo = c1 > c2 ? c2 : c1;
         e[n].slot = (unsigned char)slot;
         e[n].cell = (unsigned char)co;
-        e[n].pair = (unsigned char)(hi * (hi + 1) / 2 + lo);
+        e[n].mono = (unsigned char)pair_monomial(c1, c2);
         e[n].pad = 0;
         n++;
       }

@@ -180,15 +180,18 @@ def kernel_bytes(n, ncell, nb, name):
     ctas = nb * 8
     if name == "push_deposit":
         # particles: read u,v (24) + species (1), write u,v (24); per cell: base, cnt
-        # (8), stay (4), partials 348 floats; stencils 23.3 + 11.7 KB per CTA
-        return n * 49 + ncell * (12 + 348 * 4) + ctas * (23328 + 11664)
+        # (8), stay (4), partials 267 floats (27 monomials x 9 + 8 corners x 3);
+        # stencils 23.3 + 11.7 KB per CTA
+        return n * 49 + ncell * (12 + 267 * 4) + ctas * (23328 + 11664)
     if name == "arrivals":
         # per cell: base, base+1, cnt, stay, arr (20) and cnt/arr writes (8); the
         # ~1% arrivals and their partial read-modify-write; stencil per CTA
         return ncell * 28 + ctas * 11664
     if name == "assemble":
-        # read partials (each pair value reaches two corners); write M (243) + J (3) FP64
-        return ncell * (2 * 348 * 4) + ncell * 246 * 8
+        # read the partials (64 monomial blocks + 8 current rows per corner, from
+        # 8 cells: each cell's 267 floats are read by its 8 corners, mostly from
+        # L2); write M (243 FP32) + J (3 FP64)
+        return ncell * 267 * 4 + ncell * (243 * 4 + 3 * 8)
     if name == "pack_stencils":
         return ncell * 9 * 8 * 27 // 8 + nb * (23328 + 11664)
     return None
