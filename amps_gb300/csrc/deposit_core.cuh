@@ -189,6 +189,49 @@ struct Tile {
       sum[e] = t;
     }
   }
+  // the cell's current partials of this lane's tile, loaded ahead of an add-flush
+  __device__ __forceinline__ void preload(int lane, const float* __restrict__ cellM,
+                                          const float* __restrict__ cellJ, long long cid,
+                                          float old[9]) const {
+#pragma unroll
+    for (int e = 0; e < 9; e++) old[e] = 0.f;
+    if (lane < 27) {
+      const int g = lane / 3, hh = lane % 3;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++) old[3 * q + e] = cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)];
+    } else if (lane < kTileLanes) {
+      const int g = lane - 27;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        if (3 * g + q < 8)
+#pragma unroll
+          for (int e = 0; e < 3; e++) old[3 * q + e] = cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)];
+    }
+  }
+  // write old + this tile's sums
+  __device__ __forceinline__ void flush_onto(int lane, float* __restrict__ cellM,
+                                             float* __restrict__ cellJ, long long cid,
+                                             const float old[9]) {
+    if (lane < 27) {
+      const int g = lane / 3, hh = lane % 3;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++)
+          cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)] =
+              old[3 * q + e] + (sum[3 * q + e] - cmp[3 * q + e]);
+    } else if (lane < kTileLanes) {
+      const int g = lane - 27;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        if (3 * g + q < 8)
+#pragma unroll
+          for (int e = 0; e < 3; e++)
+            cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)] = old[3 * q + e] + (sum[3 * q + e] - cmp[3 * q + e]);
+    }
+  }
   // write (or add to) the cell partials
   __device__ __forceinline__ void flush(int lane, float* __restrict__ cellM,
                                         float* __restrict__ cellJ, long long cid, bool add) {

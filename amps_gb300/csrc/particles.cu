@@ -208,9 +208,16 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
   const float bdtdx = AMR ? __ldg(a.amr.bdtdx + b) : 0.0f;
+  // slot range and occupancy of the row's 8 cells, one lane per cell
+  int mb0 = 0, mn0 = 0;
+  if (lane < AMPS_NC) {
+    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
+    mb0 = a.base[cl];
+    mn0 = a.cnt[cl];
+  }
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
-    const int b0 = a.base[cid], n0 = a.cnt[cid];
+    const int b0 = __shfl_sync(0xffffffffu, mb0, i), n0 = __shfl_sync(0xffffffffu, mn0, i);
     Tile tile;
     float en_cell = 0.f;
     tile.zero();
@@ -390,14 +397,27 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
   double en = 0.0;
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
+  // the row's 8 cells: lane i < 8 loads cell i's slot range, occupancy, stayers
+  // and arrivals at once (one round of loads instead of eight dependent ones)
+  int mb0 = 0, mcap = 0, mn0 = 0, mst = 0, marr = 0;
+  if (lane < AMPS_NC) {
+    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
+    mb0 = a.base[cl];
+    mcap = a.base[cl + 1] - mb0;
+    mn0 = a.cnt[cl];
+    mst = a.stay[cl];
+    marr = a.arr[cl];
+  }
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
-    const int b0 = a.base[cid], cap = a.base[cid + 1] - b0, n0 = a.cnt[cid];
-    const int nst = a.stay[cid];
-    const int na = min(a.arr[cid], cap - n0);
+    const int b0 = __shfl_sync(0xffffffffu, mb0, i), cap = __shfl_sync(0xffffffffu, mcap, i);
+    const int n0 = __shfl_sync(0xffffffffu, mn0, i), nst = __shfl_sync(0xffffffffu, mst, i);
+    const int na = min(__shfl_sync(0xffffffffu, marr, i), cap - n0);
     if (na > 0) {
       Tile tile;
       tile.zero();
+      float old[9];
+      if (DEP) tile.preload(lane, a.cellM, a.cellJ, cid, old);
       const int src0 = b0 + cap - na, dst0 = b0 + nst;
       for (int q0 = 0; q0 < na; q0 += 32) {
         const bool act = q0 + lane < na;
@@ -437,12 +457,13 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
         const int slot = src0 + t;
         if (slot >= dst0 + na) a.p.sp[slot] = kHole;
       }
-      if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid, true);
+      if (DEP) tile.flush_onto(lane, a.cellM, a.cellJ, cid, old);
     }
-    if (lane == 0) {
-      a.cnt[cid] = nst + na;
-      a.arr[cid] = 0;
-    }
+  }
+  if (lane < AMPS_NC) {
+    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
+    a.cnt[cl] = mst + max(0, min(marr, mcap - mn0));
+    a.arr[cl] = 0;
   }
   if (DEP) reduce_energy(en, s_en, a.energy);
 }
