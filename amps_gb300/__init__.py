@@ -9,6 +9,7 @@ from .ecsim import (  # noqa: F401
     WORKLOADS,
     PRECOND_SHAPES,
     EcsimContext,
+    PinnedArrays,
     PeriodicMesh,
     Species,
     Workload,
@@ -24,6 +25,6 @@ from .ecsim import (  # noqa: F401
 __all__ = [
     "AmpsGpuError", "load", "WORKLOADS", "EcsimContext", "PeriodicMesh", "Species", "Workload",
     "block_origins", "electron_proton_plasma", "initial_fields", "make_initial_condition",
-    "PRECOND_SHAPES", "init_precond_weights",
+    "PRECOND_SHAPES", "init_precond_weights", "PinnedArrays",
     "physical_positions", "trace_dipole",
 ]

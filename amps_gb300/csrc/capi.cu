@@ -97,51 +97,13 @@ cudaError_t dalloc(T** p, size_t count) {
   return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
 }
 
-// host layout (interleaved, global periodic numbering) <-> device layout
-// (component-major, block-owned numbering)
-long long dev_of_host(const amps_gpu_config& g, long long hc) {
-  const int NX = 8 * g.nbx, NY = 8 * g.nby;
-  const int I = (int)(hc % NX), J = (int)((hc / NX) % NY), K = (int)(hc / ((long long)NX * NY));
-  const int b = (I / 8) + g.nbx * ((J / 8) + g.nby * (K / 8));
-  return (long long)b * 512 + (I % 8) + 8 * ((J % 8) + 8 * (K % 8));
-}
-
-std::vector<long long> host_perm(const amps_gpu_config& g, long long ncor) {
-  std::vector<long long> p((size_t)ncor);
-  for (long long h = 0; h < ncor; h++) p[(size_t)h] = dev_of_host(g, h);
-  return p;
-}
-
-// Host order: uniform meshes use the global periodic numbering I + NX (J + NY K)
-// for corners and cells; AMR meshes use the unique-corner numbering of the mesh
-// builder for corners and block*512 + i + 8j + 64k for cells.
-std::vector<long long> field_perm(amps_gpu_ctx* c, long long n) {
-  if (!c->amr) return host_perm(c->cfg, n);
-  std::vector<long long> p((size_t)n);
-  for (long long h = 0; h < n; h++) p[(size_t)h] = h;
-  return p;
-}
-
+// fields: host layout (interleaved) <-> device layout (component-major), on the GPU
 amps_gpu_status upload_vec3(amps_gpu_ctx* c, const double* host, double* dev, long long n) {
-  if (!host) return AMPS_GPU_OK;
-  auto perm = field_perm(c, n);
-  std::vector<double> tmp((size_t)(3 * n));
-  for (long long h = 0; h < n; h++)
-    for (int d = 0; d < 3; d++) tmp[(size_t)(d * n + perm[(size_t)h])] = host[3 * h + d];
-  return cuda_check(c, cudaMemcpy(dev, tmp.data(), sizeof(double) * 3 * n, cudaMemcpyHostToDevice),
-                    "upload field");
+  return layout_upload(c, host, dev, n, 3, false);
 }
 
 amps_gpu_status download_vec3(amps_gpu_ctx* c, const double* dev, double* host, long long n) {
-  if (!host) return AMPS_GPU_OK;
-  auto perm = field_perm(c, n);
-  std::vector<double> tmp((size_t)(3 * n));
-  amps_gpu_status s = cuda_check(
-      c, cudaMemcpy(tmp.data(), dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost), "download field");
-  if (s) return s;
-  for (long long h = 0; h < n; h++)
-    for (int d = 0; d < 3; d++) host[3 * h + d] = tmp[(size_t)(d * n + perm[(size_t)h])];
-  return AMPS_GPU_OK;
+  return layout_download(c, dev, host, n, 3, false);
 }
 
 // staging buffers for particle import/export (allocated on first use)
@@ -575,6 +537,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   c->pn = nullptr;
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   c->graphs.clear();
+  cudaFree(c->d_hstage);
+  c->d_hstage = nullptr;
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
                   c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
                   c->d_Z, c->d_y32,
@@ -743,16 +707,7 @@ amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* c, const double* J, const 
   cudaStreamSynchronize(c->stream);
   amps_gpu_status s = upload_vec3(c, J, c->d_J, c->ncor);
   if (s) return s;
-  if (M) {
-    const long long n = c->ncor;
-    auto perm = host_perm(c->cfg, n);
-    std::vector<float> tmp((size_t)(243 * n));
-    for (long long h = 0; h < n; h++)
-      for (int e = 0; e < 243; e++) tmp[(size_t)(e * n + perm[(size_t)h])] = (float)M[243 * h + e];
-    s = cuda_check(c, cudaMemcpy(c->d_M, tmp.data(), sizeof(float) * tmp.size(), cudaMemcpyHostToDevice),
-                   "upload M");
-    if (s) return s;
-  }
+  if ((s = layout_upload(c, M, c->d_M, c->ncor, 243, true))) return s;
   c->have_moments = true;
   return AMPS_GPU_OK;
 }
@@ -767,16 +722,7 @@ amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
   if (s) return s;
   s = download_vec3(c, c->d_J, J, c->ncor);
   if (s) return s;
-  if (M) {
-    const long long n = c->ncor;
-    auto perm = host_perm(c->cfg, n);
-    std::vector<float> tmp((size_t)(243 * n));
-    s = cuda_check(c, cudaMemcpy(tmp.data(), c->d_M, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost),
-                   "download M");
-    if (s) return s;
-    for (long long h = 0; h < n; h++)
-      for (int e = 0; e < 243; e++) M[243 * h + e] = tmp[(size_t)(e * n + perm[(size_t)h])];
-  }
+  if ((s = layout_download(c, c->d_M, M, c->ncor, 243, true))) return s;
   return AMPS_GPU_OK;
 }
 
@@ -785,32 +731,8 @@ amps_gpu_status amps_gpu_export_cell_moments(amps_gpu_ctx* c, double* cellJ, dou
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   if (s) return s;
-  const long long nc = c->ncor;
-  if (cellJ) {
-    std::vector<float> t((size_t)(24 * nc));
-    s = cuda_check(c, cudaMemcpy(t.data(), c->d_cellJ, sizeof(float) * t.size(), cudaMemcpyDeviceToHost),
-                   "download cellJ");
-    if (s) return s;
-    for (size_t i = 0; i < t.size(); i++) cellJ[i] = (double)t[i];
-  }
-  if (cellM) {
-    // device: 27 weight-monomial sums per cell; host: ProcessCell's 36 pairs
-    std::vector<float> t((size_t)(AMPS_CELLM * nc));
-    s = cuda_check(c, cudaMemcpy(t.data(), c->d_cellM, sizeof(float) * t.size(), cudaMemcpyDeviceToHost),
-                   "download cellM");
-    if (s) return s;
-    static const int ox[8] = {0, 1, 1, 0, 0, 1, 1, 0}, oy[8] = {0, 0, 1, 1, 0, 0, 1, 1},
-                     oz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
-    for (long long cl = 0; cl < nc; cl++) {
-      int pr = 0;
-      for (int c1 = 0; c1 < 8; c1++)
-        for (int c2 = 0; c2 <= c1; c2++, pr++) {
-          const int mo = (ox[c1] + ox[c2]) + 3 * (oy[c1] + oy[c2]) + 9 * (oz[c1] + oz[c2]);
-          for (int e = 0; e < 9; e++)
-            cellM[(size_t)cl * 324 + pr * 9 + e] = (double)t[(size_t)cl * AMPS_CELLM + mo * 9 + e];
-        }
-    }
-  }
+  if (!cellJ && !cellM) return AMPS_GPU_OK;
+  if ((s = layout_cell_moments(c, cellJ, cellM))) return s;
   return AMPS_GPU_OK;
 }
 

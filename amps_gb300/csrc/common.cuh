@@ -150,6 +150,10 @@ struct amps_gpu_ctx {
   double* d_energy = nullptr;   // [0] particle, [1] wave
   double* h_energy = nullptr;   // pinned
 
+  // device staging of host <-> device layout conversions (layout.cu)
+  double* d_hstage = nullptr;
+  size_t hstage_bytes = 0;
+
   // timing
   bool timing = false;
   std::vector<KernelTimer> timers;
@@ -176,6 +180,13 @@ cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double
                                  const double* Bcur);
 cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit);
 void particles_prepare();
+
+// ---- host <-> device layout conversion (layout.cu) ----
+amps_gpu_status layout_upload(amps_gpu_ctx* c, const double* host, void* dev, long long n,
+                              int ncomp, bool dev_f32);
+amps_gpu_status layout_download(amps_gpu_ctx* c, const void* dev, double* host, long long n,
+                                int ncomp, bool dev_f32);
+amps_gpu_status layout_cell_moments(amps_gpu_ctx* c, double* hJ, double* hM);
 cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
                             double c_light, long long max_sub);
 cudaError_t launch_deposit(amps_gpu_ctx* c);

@@ -272,19 +272,26 @@ class EcsimContext:
         self._check(self.lib.amps_gpu_import_moments(self.h, ptr(J, C.c_double),
                                                      ptr(M, C.c_double)), "import_moments")
 
-    def export_moments(self, with_m=True):
+    def export_moments(self, with_m=True, out=None):
+        """corner J (ncells, 3) and M (ncells, 243); out=(J, M) reuses arrays"""
         nc = self.wl.mesh.ncells
-        J = np.empty((nc, 3))
-        M = np.empty((nc, 243)) if with_m else None
+        if out is not None:
+            J, M = out
+        else:
+            J = np.empty((nc, 3))
+            M = np.empty((nc, 243)) if with_m else None
         self._check(self.lib.amps_gpu_export_moments(self.h, ptr(J, C.c_double),
                                                      ptr(M, C.c_double)), "export_moments")
         return J, M
 
-    def export_cell_moments(self, with_m=True):
+    def export_cell_moments(self, with_m=True, out=None):
         """per-cell ProcessCell partials (cells in block order): cellJ (ncells, 24),
-        cellM (ncells, 324) or None"""
-        J = np.empty((self.ncells, 24))
-        M = np.empty((self.ncells, 324)) if with_m else None
+        cellM (ncells, 324) or None; out=(J, M) reuses arrays"""
+        if out is not None:
+            J, M = out
+        else:
+            J = np.empty((self.ncells, 24))
+            M = np.empty((self.ncells, 324)) if with_m else None
         self._check(self.lib.amps_gpu_export_cell_moments(self.h, ptr(J, C.c_double),
                                                           ptr(M, C.c_double)),
                     "export_cell_moments")
@@ -430,6 +437,30 @@ class EcsimContext:
 
 
 PRECOND_SHAPES = ((27, 3, 32), (27, 32, 32), (27, 32, 3))
+
+
+class PinnedArrays:
+    """Page-locked host arrays (cudaHostAlloc) viewed as numpy arrays, for
+    host <-> device copies at full link bandwidth."""
+
+    def __init__(self):
+        self.rt = C.CDLL("libcudart.so")
+        self.ptrs = []
+
+    def empty(self, shape, dtype=np.float64):
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        p = C.c_void_p()
+        if self.rt.cudaHostAlloc(C.byref(p), C.c_size_t(max(nbytes, 1)), 0) != 0:
+            raise MemoryError("cudaHostAlloc of %d bytes failed" % nbytes)
+        self.ptrs.append(p)
+        buf = (C.c_byte * max(nbytes, 1)).from_address(p.value)
+        return np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        for p in self.ptrs:
+            self.rt.cudaFreeHost(p)
+        self.ptrs = []
 
 
 def init_precond_weights(seed=0, out_scale=1e-3):
