@@ -436,6 +436,63 @@ def tracer_line(n32, n64, device):
             "status": "0 step budget, 1 r < 1 R_E, 2 r > 10 R_E"}
 
 
+def oracle_check(workload, device):
+    """One full ECSIM step of the workload on the GPU and on the FP64 AMR oracle
+    from the same initial state (the oracle starts from the device's FP32 particle
+    offsets): relative errors of fields, per-cell moments and particles."""
+    import amps_gb300 as A
+    from amps_gb300 import amr
+    from tests import oracle_amr as OA
+    wl = amr.AMR_WORKLOADS[workload]()
+    mesh = wl.mesh()
+    ic = amr.amr_initial_condition(mesh, wl.species, wl.ppc, seed=100, nthreads=os.cpu_count() or 8)
+    n = len(ic["spec"])
+    f = amr.amr_initial_fields(mesh, wl.b0)
+    ctx = A.EcsimContext(wl.plasma, capacity=n, track_ids=True, device=device, amr_mesh=mesh)
+    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
+    ctx.import_fields(**f)
+    e0 = ctx.export_particles()
+    order = np.argsort(e0["id"])
+    x0 = e0["x"][order]
+    t0 = time.perf_counter()
+    ctx.UpdateJMassMatrix()
+    st = ctx.PicTimeStep(tol=wl.tol, maxit=400, precond=1)
+    ctx.synchronize()
+    t_gpu = time.perf_counter() - t0
+    g = ctx.export_fields()
+    gJ, gM = ctx.export_cell_moments()
+    e1 = ctx.export_particles()
+    o1 = np.argsort(e1["id"])
+    ctx.close()
+    ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x0, ic["v"].astype(np.float64), ic["spec"])
+    ao.Bcen[:] = f["B_center"]
+    ao.Bprev[:] = f["B_corner_prev"]
+    ao.Bcur[:] = f["B_corner_cur"]
+    t0 = time.perf_counter()
+    ao.deposit()
+    it, diag = ao.step(tol=wl.tol, maxit=400)
+    t_cpu = time.perf_counter() - t0
+
+    def rel(a, b):
+        den = np.max(np.abs(b))
+        return float(np.max(np.abs(a - b)) / (den if den > 0 else 1.0))
+    L = np.array(mesh.nfine, float) * mesh.dxf
+    d = e1["x"][o1] - ao.x
+    d -= L * np.rint(d / L)
+    same = (e1["block"][o1] == ao.block) & (e1["cell"][o1] == ao.cell)
+    return {"workload": workload, "particles": n, "gpu_seconds": round(t_gpu, 3),
+            "oracle_seconds": round(t_cpu, 1),
+            "rel_err_E_n": rel(g["E_n"], ao.E_n), "rel_err_E_half": rel(g["E_half"], ao.E_half),
+            "rel_err_B_center": rel(g["B_center"] - np.array(wl.b0), ao.Bcen - np.array(wl.b0)),
+            "rel_err_cell_J": rel(gJ.ravel(), ao.cellJ), "rel_err_cell_M": rel(gM.ravel(), ao.cellM),
+            "max_position_err_dx0": float(np.max(np.abs(d)) / mesh.dx0),
+            "rel_err_v": rel(e1["v"][o1], ao.v),
+            "block_cell_identical": float(np.mean(same)),
+            "particle_energy_rel": abs(st.particle_energy - diag[0]) / diag[0],
+            "wave_energy_rel": abs(st.solve.wave_energy - diag[1]) / diag[1],
+            "gmres_iterations_gpu_oracle": [st.solve.iterations, int(it)]}
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import amps_gb300 as A
@@ -672,6 +729,8 @@ def main():
     ap.add_argument("--precond-stiff", type=int, default=1,
                     help="also the same A/B at dt = 1/omega_pe")
     ap.add_argument("--graphs", type=int, default=1, help="particle step as a CUDA graph")
+    ap.add_argument("--oracle-check", action="store_true",
+                    help="one full ECSIM step on the GPU and the FP64 oracle (AMR workloads)")
     ap.add_argument("--energy-steps", type=int, default=0,
                     help="also run this many full ECSIM steps and report the energy drift")
     ap.add_argument("--tracer", type=int, default=0,
@@ -684,6 +743,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
+    if args.oracle_check:
+        print(json.dumps({"oracle_check": oracle_check(args.workload, 0)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     elif args.precond_kernel > 0:
