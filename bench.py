@@ -38,6 +38,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (push+deposit)"
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
+# one-pass ncu capture summarised in profiles/dram_traffic_amr_64c_128ppc.md
+MEASURED_TRAFFIC = {"amr_64c_128ppc": {"push_deposit": 4.66e9, "arrivals": 1.09e9}}
 UNIT = "particle-steps/s"
 
 
@@ -637,12 +640,15 @@ def run_gpu(args):
     ms_top, launches = per[top]
     nl = max(1, launches)
     nbytes = kernel_bytes(npart, ncell, nblk, top)
+    traffic = args.traffic
+    if traffic is None and top in MEASURED_TRAFFIC.get(args.workload, {}):
+        traffic = MEASURED_TRAFFIC[args.workload][top]
     roof = None
     if nbytes:
         achieved = nbytes / (ms_top / nl / 1e3) / 1e9
         roof = {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": args.traffic, "algorithmic_bytes_per_launch": int(nbytes),
+                "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
                 "avg_launch_ms": round(ms_top / nl, 4)}
     shares = {k: round(v[0] / sum(x[0] for x in per.values()), 4) for k, v in per.items()}
     # kernels per step (from the event-timed pass) x timed steps
@@ -749,7 +755,8 @@ def main():
     ap.add_argument("--precond-kernel", type=int, default=0,
                     help="time only the tensor-core inference kernel on this many blocks")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="DRAM bytes per launch of the top kernel from an ncu capture")
+                    help="DRAM bytes per launch of the top kernel from an ncu capture "
+                         "(default: the capture in profiles/ for the default workload)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
