@@ -82,6 +82,7 @@ SIGNATURES = {
     "amps_gpu_synchronize": (C.c_int, [P]),
     "amps_gpu_import_particles": (C.c_int, [P, C.c_longlong, D, D, U8, D]),
     "amps_gpu_import_particles_local": (C.c_int, [P, C.c_longlong, F, F, U8, I32]),
+    "amps_gpu_import_particles_local_weighted": (C.c_int, [P, C.c_longlong, F, F, U8, I32, F]),
     "amps_gpu_export_particles": (C.c_int, [P, D, D, U8, I32, I32, U32, LL]),
     "amps_gpu_num_particles": (C.c_int, [P, LL]),
     "amps_gpu_import_fields": (C.c_int, [P, D, D, D, D, D]),
@@ -103,6 +104,9 @@ SIGNATURES = {
     "amps_gpu_precond_harvest": (C.c_int, [P, C.c_longlong]),
     "amps_gpu_precond_num_samples": (C.c_int, [P, LL]),
     "amps_gpu_precond_get_samples": (C.c_int, [P, C.c_longlong, C.c_longlong, F, F]),
+    "amps_gpu_precond_sample_sets": (C.c_int, [P, C.c_longlong, C.c_longlong, I32]),
+    "amps_gpu_precond_num_sets": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "amps_gpu_precond_select": (C.c_int, [P, C.c_int]),
     "amps_gpu_precond_train": (C.c_int, [P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, F]),
     "amps_gpu_precond_loss_grad": (C.c_int, [P, C.c_longlong, F, F, F, F, F, F]),
     "amps_gpu_precond_forward": (C.c_int, [P, C.c_longlong, F, C.c_int, F]),

@@ -109,18 +109,25 @@ def sphere_refined_mesh(nb0, lmax, radius=0.2, dx0=1.0):
     return AmrMesh(nb0, lmax, nested_leaves(nb0, lmax, 1, radius), dx0)
 
 
-def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1):
-    """Uniform-density Maxwellian plasma on an AMR mesh: ppc_base particles per
-    species per level-0 cell volume (so a cell at level L holds ppc_base/8^L),
-    positions uniform within each cell, co-located species, reference LCG
-    stream split per block.  Returns u (FP32 block-local cell units), v, spec,
-    block, all FP32-representable.  Blocks are generated on nthreads host
-    threads (the result does not depend on it)."""
+def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1, per_cell=False):
+    """Uniform-density Maxwellian plasma on an AMR mesh, positions uniform within
+    each cell, co-located species, reference LCG stream split per block.
+
+    per_cell False: ppc_base particles per species per level-0 cell volume (a
+    cell at level L holds ppc_base/8^L), all of weight 1.  per_cell True:
+    ppc_base particles per species in every cell, a level-L particle carrying
+    the weight correction 8^-L (the same density with equal statistics per
+    cell).  Returns u (FP32 block-local cell units), v, spec, block, all
+    FP32-representable, and wcorr (FP32, or None for per_cell False).  Blocks
+    are generated on nthreads host threads (the result does not depend on it)."""
     ns = len(species)
     vth = np.array([s.vth for s in species], np.float64)
     lib = _capi.load()
-    counts = [lib.amps_ic_count(1, 1, 1, max(1, ppc_base // (8 ** int(mesh.level[b]))), ns)
-              for b in range(mesh.nblocks)]
+
+    def block_ppc(b):
+        return ppc_base if per_cell else max(1, ppc_base // (8 ** int(mesh.level[b])))
+
+    counts = [lib.amps_ic_count(1, 1, 1, block_ppc(b), ns) for b in range(mesh.nblocks)]
     off = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
     n = int(off[-1])
     u = np.empty((n, 3), np.float32)
@@ -129,9 +136,10 @@ def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1):
     bl = np.empty(n, np.int32)
     scratch = np.empty(n, np.int32)
 
+    wc = np.empty(n, np.float32) if per_cell else None
+
     def one(b):
-        L = int(mesh.level[b])
-        ppc = max(1, ppc_base // (8 ** L))
+        ppc = block_ppc(b)
         a, e = int(off[b]), int(off[b + 1])
         st = lib.amps_ic_maxwellian(1, 1, 1, ppc, ns, ptr(vth, C.c_double),
                                     (seed * 7919 + 104729 * (b + 1)) & 0x7FFFFFFF or 1, 1,
@@ -140,6 +148,8 @@ def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1):
         if st != 0:
             raise AmpsGpuError(st, "amps_ic_maxwellian")
         bl[a:e] = b
+        if per_cell:
+            wc[a:e] = 0.125 ** int(mesh.level[b])
 
     if nthreads > 1:
         from concurrent.futures import ThreadPoolExecutor
@@ -148,7 +158,7 @@ def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1):
     else:
         for b in range(mesh.nblocks):
             one(b)
-    return {"u": u, "v": v, "spec": sp, "block": bl}
+    return {"u": u, "v": v, "spec": sp, "block": bl, "wcorr": wc}
 
 
 def amr_initial_fields(mesh, b0):
@@ -163,13 +173,15 @@ def amr_initial_fields(mesh, b0):
 class AmrWorkload:
     """Electron-proton plasma of the uniform workloads on an AMR mesh: the mesh
     recipe (level-0 blocks, levels, refined region) and ppc_base particles per
-    species per level-0 cell volume."""
+    species per level-0 cell volume (per_cell False) or in every cell with
+    weight corrections 8^-L (per_cell True)."""
 
-    def __init__(self, name, nb0, lmax, mode, frac, ppc_base, steps=10):
+    def __init__(self, name, nb0, lmax, mode, frac, ppc_base, steps=10, per_cell=False):
         from .ecsim import electron_proton_plasma
         self.name = name
         self.nb0, self.lmax, self.mode, self.frac = tuple(nb0), lmax, mode, frac
         self.ppc = ppc_base
+        self.per_cell = per_cell
         # species, dt, theta, b0 and tolerance: the uniform plasma (dx0 = 1)
         self.plasma = electron_proton_plasma(name, 1, 1, 1, ppc_base, steps)
         self.species, self.dt, self.theta = self.plasma.species, self.plasma.dt, self.plasma.theta
@@ -177,6 +189,10 @@ class AmrWorkload:
 
     def mesh(self):
         return AmrMesh(self.nb0, self.lmax, nested_leaves(self.nb0, self.lmax, self.mode, self.frac))
+
+    def initial_condition(self, mesh, seed=100, nthreads=1):
+        return amr_initial_condition(mesh, self.species, self.ppc, seed=seed, nthreads=nthreads,
+                                     per_cell=self.per_cell)
 
 
 AMR_WORKLOADS = {
@@ -189,7 +205,11 @@ AMR_WORKLOADS = {
     # than L2, small enough for full profiler captures)
     "amr_64c_32ppc": lambda: AmrWorkload("amr_64c_32ppc", (8, 8, 8), 1, 0, 0.5, 32),
     # three levels, 256^3 effective cells: level 2 inside a central sphere of
-    # radius 0.2 box lengths, level 1 inside radius 0.4; 64 particles per
-    # species per base-cell volume (8 per level-1 cell, 1 per level-2 cell)
-    "amr_256e_3lvl": lambda: AmrWorkload("amr_256e_3lvl", (8, 8, 8), 2, 1, 0.4, 64),
+    # radius 0.2 box lengths, level 1 inside radius 0.4 (4432 blocks, 2.27M
+    # cells); 64 particles per species in every cell, weight corrections 8^-L
+    # (290,455,168 particles)
+    "amr_256e_3lvl": lambda: AmrWorkload("amr_256e_3lvl", (8, 8, 8), 2, 1, 0.4, 64, per_cell=True),
+    # the same mesh at 64 particles per species per base-cell volume (8 per
+    # level-1 cell, 1 per level-2 cell; 33.5M particles)
+    "amr_256e_3lvl_sparse": lambda: AmrWorkload("amr_256e_3lvl_sparse", (8, 8, 8), 2, 1, 0.4, 64),
 }

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 
 #include "amr_mesh.h"
 #include "common.cuh"
@@ -354,6 +355,79 @@ bool upload(T** d, const std::vector<T>& h) {
          cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
+// The learned preconditioner's mesh maps (see amps_gpu_ctx::d_pc_in).
+bool upload_pc_maps(amps_gpu_ctx* c, const std::vector<int>& in, const std::vector<int>& out,
+                    const std::vector<int>& set, const std::vector<int>& jac, int nsets) {
+  c->pc_nsets = nsets;
+  c->pc_njac = (long long)jac.size();
+  c->h_pc_set = set;
+  return upload(&c->d_pc_in, in) && upload(&c->d_pc_out, out) && upload(&c->d_pc_jac, jac) &&
+         (nsets == 1 || upload(&c->d_pc_set, set));
+}
+
+// Uniform periodic mesh: region corner (i, j, k) in -1..8 of block b is the
+// corner of the periodic lattice there; every block writes its 512 corners.
+bool build_pc_maps_uniform(amps_gpu_ctx* c) {
+  const int nbx = c->cfg.nbx, nby = c->cfg.nby, nbz = c->cfg.nbz;
+  const int NX = 8 * nbx, NY = 8 * nby, NZ = 8 * nbz;
+  std::vector<int> in((size_t)c->nb * 1000), out((size_t)c->nb * 512), set((size_t)c->nb, 0), jac;
+  for (int b = 0; b < c->nb; b++) {
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    for (int v = 0; v < 1000; v++) {
+      const int I = (8 * bx + v % 10 - 1 + NX) % NX, J = (8 * by + (v / 10) % 10 - 1 + NY) % NY,
+                K = (8 * bz + v / 100 - 1 + NZ) % NZ;
+      const int ob = (I >> 3) + nbx * ((J >> 3) + nby * (K >> 3));
+      in[(size_t)b * 1000 + v] = ob * AMPS_CPB + (I & 7) + 8 * ((J & 7) + 8 * (K & 7));
+    }
+    for (int q = 0; q < 512; q++) out[(size_t)b * 512 + q] = b * AMPS_CPB + q;
+  }
+  return upload_pc_maps(c, in, out, set, jac, 1);
+}
+
+// AMR mesh: region corner (i, j, k) of block b sits at origin + (i, j, k) *
+// scale on the finest lattice (periodic); it is the unique corner there, or -1
+// where none exists (inside a coarser neighbour's cell) or it is hanging.  A
+// free corner is written by the block whose cell has it as low corner (the
+// leaf containing the corner + (eps, eps, eps)); hanging corners keep z = D v.
+bool build_pc_maps_amr(amps_gpu_ctx* c, const amps_amr_mesh* m) {
+  const long long nbl = (long long)m->blocks.size(), nv = c->nvc;
+  const long long FX = m->nfine[0], FY = m->nfine[1], FZ = m->nfine[2];
+  auto key = [&](long long x, long long y, long long z) {
+    x = ((x % FX) + FX) % FX;
+    y = ((y % FY) + FY) % FY;
+    z = ((z % FZ) + FZ) % FZ;
+    return x + FX * (y + FY * z);
+  };
+  std::unordered_map<long long, int> at;
+  at.reserve((size_t)nv * 2);
+  for (long long q = 0; q < nv; q++)
+    at[key(m->corner_xyz[(size_t)(3 * q)], m->corner_xyz[(size_t)(3 * q + 1)],
+           m->corner_xyz[(size_t)(3 * q + 2)])] = (int)q;
+  auto hanging = [&](int id) { return m->hang_start[(size_t)id + 1] > m->hang_start[(size_t)id]; };
+  std::vector<int> in((size_t)nbl * 1000), out((size_t)nbl * 512), set((size_t)nbl);
+  std::vector<char> written((size_t)nv, 0);
+  for (long long b = 0; b < nbl; b++) {
+    const amps_block_desc& d = m->blocks[(size_t)b];
+    const int sc = 1 << (m->lmax - d.level);
+    set[(size_t)b] = d.level;
+    for (int v = 0; v < 1000; v++) {
+      const auto it = at.find(key(d.ix + (long long)(v % 10 - 1) * sc, d.iy + (long long)((v / 10) % 10 - 1) * sc,
+                                  d.iz + (long long)(v / 100 - 1) * sc));
+      in[(size_t)b * 1000 + v] = (it == at.end() || hanging(it->second)) ? -1 : it->second;
+    }
+    for (int q = 0; q < 512; q++) {
+      const int id = m->corner_tab[(size_t)b * 729 + (q & 7) + 9 * (((q >> 3) & 7) + 9 * (q >> 6))];
+      const bool mine = !hanging(id) && !written[(size_t)id];
+      if (mine) written[(size_t)id] = 1;
+      out[(size_t)b * 512 + q] = mine ? id : -1;
+    }
+  }
+  std::vector<int> jac;
+  for (long long q = 0; q < nv; q++)
+    if (!written[(size_t)q]) jac.push_back((int)q);
+  return upload_pc_maps(c, in, out, set, jac, m->lmax + 1);
+}
+
 }  // namespace
 
 extern "C" {
@@ -394,7 +468,7 @@ amps_gpu_status amps_gpu_create(const amps_gpu_config* cfg, amps_gpu_ctx** out) 
           nbr[(size_t)b * 27 + nbr_slot(ox, oy, oz)] = X + cfg->nbx * (Y + cfg->nby * Z);
         }
   }
-  if (!upload(&c->d_nbr, nbr)) {
+  if (!upload(&c->d_nbr, nbr) || !build_pc_maps_uniform(c)) {
     amps_gpu_destroy(c);
     return AMPS_GPU_CUDA_ERROR;
   }
@@ -454,7 +528,7 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
        upload(&c->d_hp, m->hang_parent) && upload(&c->d_hw, m->hang_weight) &&
        upload(&c->d_fine_map, m->fine_map) && upload(&c->d_borg, borg) &&
        upload(&c->d_bscale, bscale) && upload(&c->d_bdx, bdx) && upload(&c->d_bdtdx, bdtdx) &&
-       upload(&c->d_binvvol, binvvol);
+       upload(&c->d_binvvol, binvvol) && build_pc_maps_amr(c, m);
   // identity part of the operator, S = P^T diag(D) P with D(corner) = sum over
   // its cells of V/8: rows of free corners (hanging rows are constraints)
   {
@@ -546,7 +620,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw,
                   c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol,
-                  c->d_ss, c->d_sc, c->d_sv};
+                  c->d_ss, c->d_sc, c->d_sv, c->d_pc_in, c->d_pc_out, c->d_pc_set, c->d_pc_jac};
   for (void* p : ptrs) cudaFree(p);
   for (int b = 0; b < 2; b++) {
     for (int q = 0; q < 3; q++) {
@@ -609,26 +683,36 @@ amps_gpu_status amps_gpu_import_particles(amps_gpu_ctx* c, long long n, const do
 amps_gpu_status amps_gpu_import_particles_local(amps_gpu_ctx* c, long long n, const float* u,
                                                 const float* v, const uint8_t* spec,
                                                 const int32_t* block) {
+  return amps_gpu_import_particles_local_weighted(c, n, u, v, spec, block, nullptr);
+}
+
+amps_gpu_status amps_gpu_import_particles_local_weighted(amps_gpu_ctx* c, long long n,
+                                                         const float* u, const float* v,
+                                                         const uint8_t* spec, const int32_t* block,
+                                                         const float* wcorr) {
   if (!c || n < 0 || (n > 0 && (!u || !v || !spec || !block)))
     return set_err(c, AMPS_GPU_INVALID_ARG, "import_particles_local: bad arguments");
   if (n > c->cap) return set_err(c, AMPS_GPU_CAPACITY_EXCEEDED, "import_particles_local: n > capacity");
   cudaSetDevice(c->cfg.device);
   Staging* s = staging(c, std::max(n, 1LL));
   if (!s) return set_err(c, AMPS_GPU_CUDA_ERROR, "staging allocation failed");
-  c->has_wcorr = false;
+  c->has_wcorr = wcorr != nullptr;
   amps_gpu_status st = reset_flags(c);
   if (st) return st;
   cudaStream_t q = c->stream;
   float* du = reinterpret_cast<float*>(s->x);
   float* dv = reinterpret_cast<float*>(s->v);
+  float* dw = wcorr ? reinterpret_cast<float*>(s->wc) : nullptr;
   if (n > 0) {
     if ((st = cuda_check(c, cudaMemcpyAsync(du, u, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, q), "H2D u")) ||
         (st = cuda_check(c, cudaMemcpyAsync(dv, v, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, q), "H2D v")) ||
         (st = cuda_check(c, cudaMemcpyAsync(s->sp, spec, n, cudaMemcpyHostToDevice, q), "H2D spec")) ||
         (st = cuda_check(c, cudaMemcpyAsync(s->i0, block, sizeof(int32_t) * n, cudaMemcpyHostToDevice, q), "H2D block")))
       return st;
+    if (dw && (st = cuda_check(c, cudaMemcpyAsync(dw, wcorr, sizeof(float) * n, cudaMemcpyHostToDevice, q), "H2D wcorr")))
+      return st;
   }
-  st = cuda_check(c, launch_import_local(c, du, dv, s->sp, s->i0, n), "import_local");
+  st = cuda_check(c, launch_import_local(c, du, dv, s->sp, s->i0, dw, n), "import_local");
   if (st) return st;
   c->have_moments = false;
   return check_flags(c, nullptr, nullptr, nullptr);

@@ -98,6 +98,18 @@ struct amps_gpu_ctx {
   float* d_y32 = nullptr;       // 3*nvc FP32 accumulation of the inner AMR operator
   bool inner_fp32 = true;       // GMRES inner operator in FP32 (iterative refinement)
   PrecondState* pn = nullptr;   // learned preconditioner (precond.cu)
+  // the network's view of the mesh: per block the 10^3 corner region (block
+  // corners -1..8) and the 8^3 corners it writes, as indices into the corner
+  // vectors (-1: no input there / not written by this block), the weight set
+  // of the block (its refinement level; null on a uniform mesh) and the
+  // corners no block writes (hanging corners: z = D v there)
+  int* d_pc_in = nullptr;       // [nb*1000]
+  int* d_pc_out = nullptr;      // [nb*512]
+  int* d_pc_set = nullptr;      // [nb]
+  int* d_pc_jac = nullptr;      // [pc_njac]
+  long long pc_njac = 0;
+  int pc_nsets = 1;
+  std::vector<int> h_pc_set;    // [nb]
 
   // launch parameters chosen by the autotuner (field.cu: field_autotune)
   int tune_tb = 256;            // threads per CTA of the operator kernels
@@ -194,7 +206,8 @@ cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
                                const uint8_t* d_spec_in, const double* d_wc, long long n);
 cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* d_v,
-                                const uint8_t* d_sp, const int32_t* d_block, long long n);
+                                const uint8_t* d_sp, const int32_t* d_block, const float* d_wc,
+                                long long n);
 cudaError_t launch_export(amps_gpu_ctx* c, double* d_x, double* d_v, uint8_t* d_sp,
                           int32_t* d_blk, int32_t* d_cel, uint32_t* d_id);
 

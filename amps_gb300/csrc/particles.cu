@@ -821,7 +821,8 @@ __global__ void __launch_bounds__(256) k_import_amr(ImportAmrArgs a) {
 __global__ void __launch_bounds__(256) k_import_local(long long n, const float* __restrict__ u,
                                                       const float* __restrict__ v,
                                                       const uint8_t* __restrict__ sp,
-                                                      const int* __restrict__ blk, int nb,
+                                                      const int* __restrict__ blk,
+                                                      const float* __restrict__ wc, int nb,
                                                       int nspec, PBuf d, int* key,
                                                       unsigned long long* flags) {
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
@@ -840,7 +841,7 @@ __global__ void __launch_bounds__(256) k_import_local(long long n, const float* 
     const int s = sp[p];
     if (s >= nspec) atomicAdd(flags + 2, 1ull);
     d.sp[p] = (uint8_t)s;
-    if (d.wc) d.wc[p] = 1.0f;
+    if (d.wc) d.wc[p] = wc ? wc[p] : 1.0f;
     if (d.id) d.id[p] = (uint32_t)p;
     key[p] = b * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
   }
@@ -1358,11 +1359,12 @@ cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double*
 }
 
 cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* d_v,
-                                const uint8_t* d_sp, const int32_t* d_block, long long n) {
+                                const uint8_t* d_sp, const int32_t* d_block, const float* d_wc,
+                                long long n) {
   {
     TimedLaunch t(c, "import");
-    k_import_local<<<grid_for(n, 256), 256, 0, c->stream>>>(n, d_u, d_v, d_sp, d_block, c->nb,
-                                                             c->cfg.nspec, pbuf(c, c->cur ^ 1),
+    k_import_local<<<grid_for(n, 256), 256, 0, c->stream>>>(n, d_u, d_v, d_sp, d_block, d_wc,
+                                                             c->nb, c->cfg.nspec, pbuf(c, c->cur ^ 1),
                                                              c->d_key, c->d_flags);
   }
   cudaError_t e = cudaGetLastError();

@@ -219,9 +219,12 @@ __global__ void k_gather_batch(int S, const int* __restrict__ perm, long long fi
     we[(size_t)s * kOwn * 3 + q] = se[src * kOwn * 3 + q];
 }
 
-// One block per mesh block: x = dinv .* r on R (FP32) and e (owned corners,
-// optionally scaled by dinv), both divided by the RMS of x over R.
-__global__ void __launch_bounds__(256) k_harvest(int nb, long long ncor, const int* __restrict__ nbr,
+// One block per mesh block: x = dinv .* r on R (FP32, zero where the region
+// map has no corner) and e on the corners the block writes (optionally scaled
+// by dinv; where it writes none, e = x so that the target correction is 0),
+// both divided by the RMS of x over R.
+__global__ void __launch_bounds__(256) k_harvest(int nb, long long nvc, const int* __restrict__ in_map,
+                                                 const int* __restrict__ out_map,
                                                  const double* __restrict__ r,
                                                  const double* __restrict__ e,
                                                  const double* __restrict__ dinv, int e_scaled,
@@ -234,11 +237,10 @@ __global__ void __launch_bounds__(256) k_harvest(int nb, long long ncor, const i
   __shared__ double sh[8];
   double ss = 0.0;
   for (int q = threadIdx.x; q < kRV; q += blockDim.x) {
-    const int i = q % 10, j = (q / 10) % 10, k = q / 100;
-    const int id = local_id(nbr, b, i - 1, j - 1, k - 1);
+    const int id = in_map[(size_t)b * kRV + q];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) {
-      const double v = dinv[ch * ncor + id] * r[ch * ncor + id];
+      const double v = id >= 0 ? dinv[ch * nvc + id] * r[ch * nvc + id] : 0.0;
       sxv[q * 3 + ch] = (float)v;
       ss += v * v;
     }
@@ -253,45 +255,69 @@ __global__ void __launch_bounds__(256) k_harvest(int nb, long long ncor, const i
   const float inv = rms > 0.0 ? (float)(1.0 / rms) : 0.f;
   for (int q = threadIdx.x; q < kRV * 3; q += blockDim.x) sx[s * kRV * 3 + q] = sxv[q] * inv;
   for (int q = threadIdx.x; q < kOwn; q += blockDim.x) {
-    const long long id = (long long)b * AMPS_CPB + q;  // owned corner q = i + 8j + 64k
+    const int id = out_map[(size_t)b * kOwn + q];  // corner q = i + 8j + 64k of the block
+    const int vox = (((q >> 6) + 1) * 10 + ((q >> 3) & 7) + 1) * 10 + (q & 7) + 1;
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) {
-      double v = e[ch * ncor + id];
-      if (e_scaled) v *= dinv[ch * ncor + id];
-      se[(s * kOwn + q) * 3 + ch] = (float)(v * (rms > 0.0 ? 1.0 / rms : 0.0));
+      float t;
+      if (id >= 0) {
+        double v = e[ch * nvc + id];
+        if (e_scaled) v *= dinv[ch * nvc + id];
+        t = (float)(v * (rms > 0.0 ? 1.0 / rms : 0.0));
+      } else {
+        t = sxv[vox * 3 + ch] * inv;
+      }
+      se[(s * kOwn + q) * 3 + ch] = t;
     }
   }
 }
 
 // inference input: wx[b][v][ch] = dinv .* v on R around mesh block b
-__global__ void __launch_bounds__(256) k_gather_region(int nb, long long ncor,
-                                                       const int* __restrict__ nbr,
+__global__ void __launch_bounds__(256) k_gather_region(int nb, long long nvc,
+                                                       const int* __restrict__ in_map,
                                                        const double* __restrict__ vin,
                                                        const double* __restrict__ dinv,
                                                        float* __restrict__ wx) {
   const int b = blockIdx.x;
   for (int q = threadIdx.x; q < kRV; q += blockDim.x) {
-    const int i = q % 10, j = (q / 10) % 10, k = q / 100;
-    const int id = local_id(nbr, b, i - 1, j - 1, k - 1);
+    const int id = in_map[(size_t)b * kRV + q];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++)
-      wx[((size_t)b * kRV + q) * 3 + ch] = (float)(dinv[ch * ncor + id] * vin[ch * ncor + id]);
+      wx[((size_t)b * kRV + q) * 3 + ch] = id >= 0 ? (float)(dinv[ch * nvc + id] * vin[ch * nvc + id]) : 0.f;
   }
 }
 
-// z (owned corners, FP64) = x + y
-__global__ void __launch_bounds__(256) k_scatter_z(int nb, long long ncor,
+// z (FP64) = x + y on the corners block b writes, for the blocks of weight set
+// `want` (all blocks when set is null)
+__global__ void __launch_bounds__(256) k_scatter_z(int nb, long long nvc,
+                                                   const int* __restrict__ out_map,
+                                                   const int* __restrict__ set, int want,
                                                    const float* __restrict__ wx,
                                                    const float* __restrict__ y,
                                                    double* __restrict__ z) {
   const int b = blockIdx.x;
+  if (set && set[b] != want) return;
   for (int q = threadIdx.x; q < kOwn; q += blockDim.x) {
+    const int id = out_map[(size_t)b * kOwn + q];
+    if (id < 0) continue;
     const int i = q & 7, j = (q >> 3) & 7, k = q >> 6;
     const int v = ((k + 1) * 10 + (j + 1)) * 10 + (i + 1);
 #pragma unroll
     for (int ch = 0; ch < 3; ch++)
-      z[ch * ncor + (long long)b * AMPS_CPB + q] =
-          (double)(wx[((size_t)b * kRV + v) * 3 + ch] + y[((size_t)b * kRV + v) * 3 + ch]);
+      z[ch * nvc + id] = (double)(wx[((size_t)b * kRV + v) * 3 + ch] + y[((size_t)b * kRV + v) * 3 + ch]);
+  }
+}
+
+// z = dinv .* v on the corners no block writes (hanging corners)
+__global__ void __launch_bounds__(256) k_pc_jacobi(long long n, const int* __restrict__ ids,
+                                                   long long nvc, const double* __restrict__ vin,
+                                                   const double* __restrict__ dinv,
+                                                   double* __restrict__ z) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long id = ids[q];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) z[ch * nvc + id] = dinv[ch * nvc + id] * vin[ch * nvc + id];
   }
 }
 
@@ -368,11 +394,24 @@ cudaError_t precond_work(PrecondState* P, int S) {
   return e;
 }
 
+void precond_select(PrecondState* P, int set) {
+  P->adam_saved[(size_t)P->active] = P->adam_t;
+  P->active = set;
+  for (int l = 0; l < 3; l++) {
+    const size_t o = (size_t)set * kWSize[l];
+    P->w[l] = P->wb[l] + o;
+    P->g[l] = P->gb[l] + o;
+    P->m[l] = P->mb[l] + o;
+    P->v[l] = P->vb[l] + o;
+  }
+  P->adam_t = P->adam_saved[(size_t)set];
+}
+
 void precond_free(PrecondState* P) {
   if (!P) return;
   free_work(P);
   for (int l = 0; l < 3; l++) {
-    cudaFree(P->w[l]); cudaFree(P->g[l]); cudaFree(P->m[l]); cudaFree(P->v[l]);
+    cudaFree(P->wb[l]); cudaFree(P->gb[l]); cudaFree(P->mb[l]); cudaFree(P->vb[l]);
   }
   cudaFree(P->wtc);
   cudaFree(P->dloss);
@@ -429,11 +468,13 @@ cudaError_t precond_gather_batch(PrecondState* P, cudaStream_t st, int S, long l
 
 cudaError_t precond_harvest_pairs(amps_gpu_ctx* c, const double* r, const double* e, int e_scaled) {
   PrecondState* P = c->pn;
-  if (!P || P->cap <= 0 || P->n >= P->cap || c->amr || !c->d_dinv) return cudaSuccess;
+  if (!P || P->cap <= 0 || P->n >= P->cap || !c->d_dinv) return cudaSuccess;
   TimedLaunch t(c, "precond_harvest");
-  k_harvest<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, r, e, c->d_dinv, e_scaled,
-                                          P->sx, P->se, P->n, P->cap);
-  P->n = std::min(P->cap, P->n + c->nb);
+  k_harvest<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_in, c->d_pc_out, r, e, c->d_dinv,
+                                          e_scaled, P->sx, P->se, P->n, P->cap);
+  const long long add = std::min<long long>(P->cap - P->n, c->nb);
+  P->sample_set.insert(P->sample_set.end(), c->h_pc_set.begin(), c->h_pc_set.begin() + add);
+  P->n += add;
   return cudaGetLastError();
 }
 
@@ -442,23 +483,37 @@ cudaError_t launch_precond_net(amps_gpu_ctx* c, const double* v, double* z) {
   PrecondState* P = c->pn;
   if (!P) return cudaErrorInvalidValue;
   cudaError_t e;
+  if (c->pc_njac > 0) {
+    TimedLaunch t(c, "precond_jacobi_hanging");
+    k_pc_jacobi<<<(unsigned)std::min<long long>((c->pc_njac + 255) / 256, 1216), 256, 0, c->stream>>>(
+        c->pc_njac, c->d_pc_jac, c->nvc, v, c->d_dinv, z);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   if (P->use_tc) {
     TimedLaunch t(c, "precond_net_tc");
-    return precond_apply_tc_mesh(P, c->stream, c->nb, c->d_nbr, c->ncor, v, c->d_dinv, z);
+    return precond_apply_tc_mesh(P, c->stream, c->nb, c->d_pc_in, c->d_pc_out, c->d_pc_set, c->nvc,
+                                 v, c->d_dinv, z);
   }
   if ((e = precond_work(P, c->nb)) != cudaSuccess) return e;
   {
     TimedLaunch t(c, "precond_gather");
-    k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, v, c->d_dinv, P->wx);
+    k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_in, v, c->d_dinv, P->wx);
   }
-  {
-    TimedLaunch t(c, "precond_net_fp32", 3);
-    if ((e = precond_forward32(P, c->stream, c->nb)) != cudaSuccess) return e;
-  }
-  {
+  // the FP32 path runs every set's network over all blocks and keeps each
+  // block's own
+  const int active = P->active;
+  for (int s = 0; s < P->nsets; s++) {
+    precond_select(P, s);
+    {
+      TimedLaunch t(c, "precond_net_fp32", 3);
+      if ((e = precond_forward32(P, c->stream, c->nb)) != cudaSuccess) break;
+    }
     TimedLaunch t(c, "precond_scatter");
-    k_scatter_z<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, P->wx, P->y, z);
+    k_scatter_z<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_out, c->d_pc_set, s, P->wx,
+                                              P->y, z);
   }
+  precond_select(P, active);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
@@ -472,18 +527,19 @@ cudaError_t precond_owned_out(PrecondState* P, cudaStream_t st, int S, float* ou
 namespace {
 
 amps_gpu_status ensure_state(amps_gpu_ctx* c) {
-  if (c->amr)
-    return set_err(c, AMPS_GPU_INVALID_ARG,
-                   "learned preconditioner: uniform meshes only (AMR contexts use Jacobi)");
   if (c->pn) return AMPS_GPU_OK;
   PrecondState* P = new PrecondState();
+  P->nsets = c->pc_nsets;
+  P->adam_saved.assign((size_t)P->nsets, 0);
   bool ok = true;
   for (int l = 0; l < 3 && ok; l++) {
-    for (float** p : {&P->w[l], &P->g[l], &P->m[l], &P->v[l]}) {
-      ok = ok && cudaMalloc(reinterpret_cast<void**>(p), sizeof(float) * kWSize[l]) == cudaSuccess;
-      ok = ok && cudaMemset(*p, 0, sizeof(float) * kWSize[l]) == cudaSuccess;
+    const size_t bytes = sizeof(float) * kWSize[l] * (size_t)P->nsets;
+    for (float** p : {&P->wb[l], &P->gb[l], &P->mb[l], &P->vb[l]}) {
+      ok = ok && cudaMalloc(reinterpret_cast<void**>(p), bytes) == cudaSuccess;
+      ok = ok && cudaMemset(*p, 0, bytes) == cudaSuccess;
     }
   }
+  if (ok) precond_select(P, 0);
   ok = ok && cudaMalloc(reinterpret_cast<void**>(&P->dloss), sizeof(double) * 4) == cudaSuccess;
   if (!c->d_Z)
     ok = ok && cudaMalloc(reinterpret_cast<void**>(&c->d_Z),
@@ -494,6 +550,18 @@ amps_gpu_status ensure_state(amps_gpu_ctx* c) {
     return set_err(c, AMPS_GPU_CUDA_ERROR, "learned preconditioner: allocation failed");
   }
   P->flags = c->d_flags;
+  // BF16 images of every set (zero weights: the network adds nothing)
+  for (int s = 0; s < P->nsets && ok; s++) {
+    precond_select(P, s);
+    ok = precond_prepare_tc(P, c->stream) == cudaSuccess;
+  }
+  if (ok) precond_select(P, 0);
+  ok = ok && cudaStreamSynchronize(c->stream) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    precond_free(P);
+    return set_err(c, AMPS_GPU_CUDA_ERROR, "learned preconditioner: weight images");
+  }
   c->pn = P;
   return AMPS_GPU_OK;
 }
@@ -573,6 +641,7 @@ amps_gpu_status amps_gpu_precond_harvest(amps_gpu_ctx* c, long long capacity) {
   cudaFree(P->se);
   P->sx = P->se = nullptr;
   P->cap = P->n = 0;
+  P->sample_set.clear();
   if (capacity == 0) return AMPS_GPU_OK;
   if (cudaMalloc(reinterpret_cast<void**>(&P->sx), sizeof(float) * capacity * 1000 * 3) != cudaSuccess ||
       cudaMalloc(reinterpret_cast<void**>(&P->se), sizeof(float) * capacity * 512 * 3) != cudaSuccess) {
@@ -582,6 +651,30 @@ amps_gpu_status amps_gpu_precond_harvest(amps_gpu_ctx* c, long long capacity) {
     return set_err(c, AMPS_GPU_CUDA_ERROR, "precond_harvest: allocation failed");
   }
   P->cap = capacity;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_precond_num_sets(amps_gpu_ctx* c, int* n) {
+  if (!c || !n) return AMPS_GPU_INVALID_ARG;
+  *n = c->pc_nsets;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_precond_select(amps_gpu_ctx* c, int set) {
+  if (!c || set < 0 || set >= c->pc_nsets)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "precond_select: no such weight set");
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s = ensure_state(c);
+  if (s) return s;
+  precond_select(c->pn, set);
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_precond_sample_sets(amps_gpu_ctx* c, long long first, long long count,
+                                             int32_t* sets) {
+  if (!c || !c->pn || !sets || first < 0 || count < 0 || first + count > c->pn->n)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "precond_sample_sets: range");
+  for (long long q = 0; q < count; q++) sets[q] = c->pn->sample_set[(size_t)(first + q)];
   return AMPS_GPU_OK;
 }
 
@@ -610,27 +703,30 @@ amps_gpu_status amps_gpu_precond_train(amps_gpu_ctx* c, int epochs, int batch, f
   if (!c || !c->pn || epochs <= 0 || batch <= 0 || !(lr > 0.f))
     return set_err(c, AMPS_GPU_INVALID_ARG, "precond_train: bad arguments");
   PrecondState* P = c->pn;
-  if (P->n < 1) return set_err(c, AMPS_GPU_INVALID_ARG, "precond_train: no samples");
+  // the active set's samples
+  std::vector<int> perm;
+  for (long long q = 0; q < P->n; q++)
+    if (P->sample_set[(size_t)q] == P->active) perm.push_back((int)q);
+  const long long ns = (long long)perm.size();
+  if (ns < 1) return set_err(c, AMPS_GPU_INVALID_ARG, "precond_train: no samples of this weight set");
   cudaSetDevice(c->cfg.device);
   cudaStream_t st = c->stream;
-  const int S = (int)std::min<long long>(batch, P->n);
+  const int S = (int)std::min<long long>(batch, ns);
   cudaError_t er = precond_work(P, S);
   if (er != cudaSuccess) return cuda_check(c, er, "precond work buffers");
-  if (P->perm_n < P->n) {
+  if (P->perm_n < ns) {
     cudaFree(P->perm);
-    if (cudaMalloc(reinterpret_cast<void**>(&P->perm), sizeof(int) * P->n) != cudaSuccess)
+    if (cudaMalloc(reinterpret_cast<void**>(&P->perm), sizeof(int) * ns) != cudaSuccess)
       return set_err(c, AMPS_GPU_CUDA_ERROR, "precond_train: allocation failed");
-    P->perm_n = P->n;
+    P->perm_n = ns;
   }
   std::mt19937_64 rng(seed);
-  std::vector<int> perm((size_t)P->n);
-  std::iota(perm.begin(), perm.end(), 0);
-  const long long nbatch = P->n / S;
+  const long long nbatch = ns / S;
   const double total = (double)epochs * (double)nbatch;
   long long step = 0;
   for (int ep = 0; ep < epochs; ep++) {
     std::shuffle(perm.begin(), perm.end(), rng);
-    er = cudaMemcpyAsync(P->perm, perm.data(), sizeof(int) * P->n, cudaMemcpyHostToDevice, st);
+    er = cudaMemcpyAsync(P->perm, perm.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, st);
     if (er == cudaSuccess) er = cudaMemsetAsync(P->dloss, 0, sizeof(double), st);
     for (long long bi = 0; bi < nbatch && er == cudaSuccess; bi++) {
       TimedLaunch t(c, "precond_train", 12);

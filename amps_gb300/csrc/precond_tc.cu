@@ -145,12 +145,15 @@ __device__ __forceinline__ bool interior(int p, int& i, int& j, int& k) {
 
 // Inputs/outputs: samples mode (x[S][1000][3] -> y[S][1000][3], owned voxels)
 // or mesh mode (mesh.v != null: x = dinv .* v gathered around mesh block s
-// through the neighbour table, z = x + y written to the FP64 corners).
+// through in_map, z = x + y written to the FP64 corners of out_map, with the
+// weight set set[s] of the block, or set 0 when set is null).
 struct MeshIO {
   const double* v;
   const double* dinv;
-  const int* nbr;
-  long long ncor;
+  const int* in_map;
+  const int* out_map;
+  const int* set;
+  long long nvc;
   double* z;
 };
 
@@ -185,8 +188,9 @@ __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
   }
   __syncthreads();
   if (tid == 0) {
+    const int wset = (mesh.v && mesh.set) ? mesh.set[s] : 0;
     mbar_arrive_expect_tx(&bar[1], kWBytes);
-    bulk_copy_g2s(wsm, wimg, kWBytes, &bar[1]);
+    bulk_copy_g2s(wsm, wimg + (size_t)wset * (kWBytes / 2), kWBytes, &bar[1]);
   }
   // layer-1 input: channels 0..2 of plane 0
   const float* xs = x + (size_t)s * 1000 * 3;
@@ -200,11 +204,12 @@ __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
       for (int ch = 0; ch < 3; ch++) xv[q][ch] = 0.f;
       if (v < 1000) {
         if (mesh.v) {
-          const int i = v % 10, j = (v / 10) % 10, k = v / 100;
-          const long long id = local_id(mesh.nbr, s, i - 1, j - 1, k - 1);
+          const long long id = mesh.in_map[(size_t)s * 1000 + v];
+          if (id >= 0) {
 #pragma unroll
-          for (int ch = 0; ch < 3; ch++)
-            xv[q][ch] = (float)(mesh.dinv[ch * mesh.ncor + id] * mesh.v[ch * mesh.ncor + id]);
+            for (int ch = 0; ch < 3; ch++)
+              xv[q][ch] = (float)(mesh.dinv[ch * mesh.nvc + id] * mesh.v[ch * mesh.nvc + id]);
+          }
         } else {
 #pragma unroll
           for (int ch = 0; ch < 3; ch++) xv[q][ch] = __ldg(xs + 3 * v + ch);
@@ -317,12 +322,14 @@ __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
           }
         } else if (in && i >= 1 && i <= 8 && j >= 1 && j <= 8 && k >= 1 && k <= 8) {
           if (mesh.v) {
-            // z = D v (FP64) + N(D v) on the owned corner (i-1, j-1, k-1)
-            const long long id = (long long)s * AMPS_CPB + (i - 1) + 8 * ((j - 1) + 8 * (k - 1));
+            // z = D v (FP64) + N(D v) on the block's corner (i-1, j-1, k-1)
+            const long long id = mesh.out_map[(size_t)s * 512 + (i - 1) + 8 * ((j - 1) + 8 * (k - 1))];
+            if (id >= 0) {
 #pragma unroll
-            for (int ch = 0; ch < 3; ch++)
-              mesh.z[ch * mesh.ncor + id] = mesh.dinv[ch * mesh.ncor + id] * mesh.v[ch * mesh.ncor + id] +
-                                            (double)__uint_as_float(r[g][0][ch]);
+              for (int ch = 0; ch < 3; ch++)
+                mesh.z[ch * mesh.nvc + id] = mesh.dinv[ch * mesh.nvc + id] * mesh.v[ch * mesh.nvc + id] +
+                                             (double)__uint_as_float(r[g][0][ch]);
+            }
           } else {
             float* dst = y + ((size_t)s * 1000 + (k * 10 + j) * 10 + i) * 3;
             dst[0] = __uint_as_float(r[g][0][0]);
@@ -385,10 +392,11 @@ __global__ void k_pack_wtc(const float* __restrict__ w1, const float* __restrict
 cudaError_t precond_prepare_tc(PrecondState* P, cudaStream_t st) {
   P->tc_ready = false;
   if (!P->wtc) {
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&P->wtc), kWBytes);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&P->wtc), (size_t)kWBytes * P->nsets);
     if (e != cudaSuccess) return e;
   }
-  k_pack_wtc<<<108, 256, 0, st>>>(P->w[0], P->w[1], P->w[2], P->wtc);
+  k_pack_wtc<<<108, 256, 0, st>>>(P->w[0], P->w[1], P->w[2],
+                                  P->wtc + (size_t)P->active * (kWBytes / 2));
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) P->tc_ready = true;
   return e;
@@ -410,17 +418,19 @@ cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const fl
   if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
   cudaError_t e = set_tc_attr();
   if (e != cudaSuccess) return e;
-  MeshIO none{nullptr, nullptr, nullptr, 0, nullptr};
-  k_precond_tc<<<S * kSplit, 128, kSmem, st>>>(x, y, P->wtc, P->flags, none);
+  MeshIO none{nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr};
+  k_precond_tc<<<S * kSplit, 128, kSmem, st>>>(x, y, P->wtc + (size_t)P->active * (kWBytes / 2),
+                                               P->flags, none);
   return cudaGetLastError();
 }
 
-cudaError_t precond_apply_tc_mesh(PrecondState* P, cudaStream_t st, int nb, const int* nbr,
-                                  long long ncor, const double* v, const double* dinv, double* z) {
+cudaError_t precond_apply_tc_mesh(PrecondState* P, cudaStream_t st, int nb, const int* in_map,
+                                  const int* out_map, const int* set, long long nvc,
+                                  const double* v, const double* dinv, double* z) {
   if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
   cudaError_t e = set_tc_attr();
   if (e != cudaSuccess) return e;
-  MeshIO io{v, dinv, nbr, ncor, z};
+  MeshIO io{v, dinv, in_map, out_map, set, nvc, z};
   k_precond_tc<<<nb * kSplit, 128, kSmem, st>>>(nullptr, nullptr, P->wtc, P->flags, io);
   return cudaGetLastError();
 }

@@ -219,14 +219,15 @@ class EcsimContext:
             self.h, len(spec), ptr(x, C.c_double), ptr(v, C.c_double), ptr(spec, C.c_uint8),
             ptr(wc, C.c_double)), "import_particles")
 
-    def import_particles_local(self, u, v, spec, block):
+    def import_particles_local(self, u, v, spec, block, wcorr=None):
         u = np.ascontiguousarray(u, np.float32)
         v = np.ascontiguousarray(v, np.float32)
         spec = np.ascontiguousarray(spec, np.uint8)
         block = np.ascontiguousarray(block, np.int32)
-        self._check(self.lib.amps_gpu_import_particles_local(
+        wc = None if wcorr is None else np.ascontiguousarray(wcorr, np.float32)
+        self._check(self.lib.amps_gpu_import_particles_local_weighted(
             self.h, len(spec), ptr(u, C.c_float), ptr(v, C.c_float), ptr(spec, C.c_uint8),
-            ptr(block, C.c_int32)), "import_particles_local")
+            ptr(block, C.c_int32), ptr(wc, C.c_float)), "import_particles_local")
 
     def num_particles(self):
         n = C.c_longlong()
@@ -342,6 +343,24 @@ class EcsimContext:
     def set_inner_fp64(self, on=True):
         """GMRES inner operator in FP64 (True) or FP32 with FP64 refinement (False)."""
         self._check(self.lib.amps_gpu_set_inner_fp64(self.h, 1 if on else 0), "set_inner_fp64")
+
+    def precond_num_sets(self):
+        """Weight sets of the network: 1 on a uniform mesh, one per level on AMR."""
+        n = C.c_int()
+        self._check(self.lib.amps_gpu_precond_num_sets(self.h, C.byref(n)), "precond_num_sets")
+        return n.value
+
+    def precond_select(self, wset):
+        """Weight set that load / weights / train / loss_grad / forward act on."""
+        self._check(self.lib.amps_gpu_precond_select(self.h, int(wset)), "precond_select")
+
+    def precond_sample_sets(self, first=0, count=None):
+        if count is None:
+            count = self.precond_num_samples() - first
+        out = np.empty(count, np.int32)
+        self._check(self.lib.amps_gpu_precond_sample_sets(self.h, first, count, ptr(out, C.c_int32)),
+                    "precond_sample_sets")
+        return out
 
     def precond_load(self, w1, w2, w3):
         ws = [np.ascontiguousarray(w, np.float32) for w in (w1, w2, w3)]

@@ -293,8 +293,7 @@ def setup_workload(name, device, track_ids=False):
     if name in amr.AMR_WORKLOADS:
         wl = amr.AMR_WORKLOADS[name]()
         mesh = wl.mesh()
-        ic = amr.amr_initial_condition(mesh, wl.species, wl.ppc, seed=100,
-                                       nthreads=os.cpu_count() or 8)
+        ic = wl.initial_condition(mesh, seed=100, nthreads=os.cpu_count() or 8)
         t_ic = time.time() - t_ic
         n = len(ic["spec"])
         ctx = A.EcsimContext(wl.plasma, capacity=n, track_ids=track_ids, device=device,
@@ -303,7 +302,10 @@ def setup_workload(name, device, track_ids=False):
         info = {"workload": name, "particles": n, "cells": mesh.ncells, "blocks": mesh.nblocks,
                 "corners": mesh.ncorners, "hanging_corners": mesh.nhanging,
                 "levels": wl.lmax + 1, "fine_blocks": int(np.sum(mesh.level > 0)),
-                "ppc_per_species_base_cell": wl.ppc, "amr": True, "tol": wl.tol}
+                ("ppc_per_species_per_cell" if wl.per_cell else "ppc_per_species_base_cell"): wl.ppc,
+                "amr": True, "tol": wl.tol}
+        if wl.per_cell:
+            info["weights"] = "weight correction 8^-level per particle (uniform density)"
     else:
         wl = A.WORKLOADS[name]()
         ic = A.make_initial_condition(wl, nthreads=os.cpu_count() or 8)
@@ -314,7 +316,7 @@ def setup_workload(name, device, track_ids=False):
         info = {"workload": name, "particles": n, "cells": wl.mesh.ncells,
                 "blocks": wl.mesh.nblocks, "ppc_per_species": wl.ppc, "amr": False,
                 "tol": wl.tol}
-    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
+    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"], ic.get("wcorr"))
     ctx.import_fields(**f)
     info["ic_seconds"] = round(t_ic, 2)
     return ctx, info
@@ -448,11 +450,11 @@ def oracle_check(workload, device):
     from tests import oracle_amr as OA
     wl = amr.AMR_WORKLOADS[workload]()
     mesh = wl.mesh()
-    ic = amr.amr_initial_condition(mesh, wl.species, wl.ppc, seed=100, nthreads=os.cpu_count() or 8)
+    ic = wl.initial_condition(mesh, seed=100, nthreads=os.cpu_count() or 8)
     n = len(ic["spec"])
     f = amr.amr_initial_fields(mesh, wl.b0)
     ctx = A.EcsimContext(wl.plasma, capacity=n, track_ids=True, device=device, amr_mesh=mesh)
-    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
+    ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"], ic.get("wcorr"))
     ctx.import_fields(**f)
     e0 = ctx.export_particles()
     order = np.argsort(e0["id"])
@@ -467,7 +469,9 @@ def oracle_check(workload, device):
     e1 = ctx.export_particles()
     o1 = np.argsort(e1["id"])
     ctx.close()
-    ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x0, ic["v"].astype(np.float64), ic["spec"])
+    wc = None if ic["wcorr"] is None else ic["wcorr"].astype(np.float64)
+    ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x0, ic["v"].astype(np.float64), ic["spec"],
+                      wcorr=wc)
     ao.Bcen[:] = f["B_center"]
     ao.Bprev[:] = f["B_corner_prev"]
     ao.Bcur[:] = f["B_corner_cur"]

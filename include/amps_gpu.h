@@ -151,6 +151,13 @@ amps_gpu_status amps_gpu_import_particles(amps_gpu_ctx* ctx, long long n, const 
 amps_gpu_status amps_gpu_import_particles_local(amps_gpu_ctx* ctx, long long n, const float* u,
                                                 const float* v, const uint8_t* spec,
                                                 const int32_t* block);
+/* The same with a per-particle weight correction factor (the reference's
+ * individual statistical weight correction, GetIndividualStatWeightCorrection
+ * pic.h:3438); wcorr may be NULL (all 1). */
+amps_gpu_status amps_gpu_import_particles_local_weighted(amps_gpu_ctx* ctx, long long n,
+                                                         const float* u, const float* v,
+                                                         const uint8_t* spec, const int32_t* block,
+                                                         const float* wcorr);
 /* Exports in the device order (sorted by block, then cell).  Any pointer may
  * be NULL.  id is the import index when track_ids is set. */
 amps_gpu_status amps_gpu_export_particles(amps_gpu_ctx* ctx, double* x, double* v, uint8_t* spec,
@@ -197,7 +204,7 @@ amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* ctx, double* particl
  * E^{n+theta} = E^n + dE (x0 = 0, stop when ||b-Ax|| <= tol ||b||, restart 30),
  * UpdateB, InterpolateB_C2N, UpdateE.  precond: 0 none (the reference's
  * PrecondParam = 0), 1 Jacobi, 2 the learned block network loaded with
- * amps_gpu_precond_load (uniform meshes; Jacobi-scaled input, flexible GMRES).
+ * amps_gpu_precond_load or trained (Jacobi-scaled input, flexible GMRES).
  * Each restart cycle begins from the FP64 residual b - A x; the Arnoldi steps
  * apply the operator in FP32 unless amps_gpu_set_inner_fp64 switched that off. */
 amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* ctx, double tol, int maxit, int precond,
@@ -224,7 +231,16 @@ amps_gpu_status amps_gpu_set_inner_fp64(amps_gpu_ctx* ctx, int fp64);
  * 3(dy+1) + 9(dz+1), then input channel, then output channel), FP32 masters,
  * BF16 copies for inference.  Training pairs come from the Jacobi field solves
  * themselves (harvest on): each Arnoldi step's (r = A e, e) and the final
- * (b, x), cut into blocks and normalised by the RMS of D r over the block. */
+ * (b, x), cut into blocks and normalised by the RMS of D r over the block.
+ * On AMR meshes the halo corners are those of the block's own lattice (zero
+ * where a coarser neighbour has none, and at hanging corners), a free corner
+ * is written by the block whose cell has it as low corner, hanging corners
+ * get z = D r, and every refinement level has its own weight set. */
+/* weight sets: 1 on a uniform mesh, lmax + 1 on an AMR mesh (set = level).
+ * load, get, train, loss_grad and forward act on the selected set (0 at
+ * creation); inference inside the field solve uses each block's own set. */
+amps_gpu_status amps_gpu_precond_num_sets(amps_gpu_ctx* ctx, int* n);
+amps_gpu_status amps_gpu_precond_select(amps_gpu_ctx* ctx, int set);
 amps_gpu_status amps_gpu_precond_load(amps_gpu_ctx* ctx, const float* w1, const float* w2,
                                       const float* w3);
 amps_gpu_status amps_gpu_precond_get(amps_gpu_ctx* ctx, float* w1, float* w2, float* w3);
@@ -238,8 +254,12 @@ amps_gpu_status amps_gpu_precond_num_samples(amps_gpu_ctx* ctx, long long* n);
  * index (k*10 + j)*10 + i for block corner (i-1, j-1, k-1)), e[count][512][3] */
 amps_gpu_status amps_gpu_precond_get_samples(amps_gpu_ctx* ctx, long long first, long long count,
                                              float* x, float* e);
-/* Adam on the harvested samples (mini-batches of `batch` blocks, shuffled with
- * `seed`); loss = mean over owned corners and channels of (x + N(x) - e)^2.
+/* weight set (block level) of samples [first, first+count) */
+amps_gpu_status amps_gpu_precond_sample_sets(amps_gpu_ctx* ctx, long long first, long long count,
+                                             int32_t* sets);
+/* Adam on the harvested samples of the selected weight set (mini-batches of
+ * `batch` blocks, shuffled with `seed`); loss = mean over owned corners and
+ * channels of (x + N(x) - e)^2.
  * loss_out[epochs] receives the mean loss of every epoch. */
 amps_gpu_status amps_gpu_precond_train(amps_gpu_ctx* ctx, int epochs, int batch, float lr,
                                        unsigned long long seed, float* loss_out);

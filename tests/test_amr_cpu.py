@@ -128,3 +128,20 @@ def test_amr_energy_conserved_two_levels():
         assert it > 0
         drift = abs(diag[0] + diag[1] - tot0) / tot0
         assert drift < 1e-8, drift
+
+
+@pytest.mark.parametrize("recipe", ["box2", "sphere3"])
+def test_every_free_corner_is_one_cells_low_corner(recipe):
+    """The learned preconditioner writes each free (non-hanging) corner from the
+    block whose cell has it as low corner: on nested meshes that cell exists
+    and is unique for every free corner."""
+    if recipe == "box2":
+        m = amr.central_refined_mesh((4, 4, 4), lmax=1, frac=0.5)
+    else:
+        m = amr.sphere_refined_mesh((4, 4, 4), lmax=2, radius=0.2)
+    tab = m.corner_tab.reshape(m.nblocks, 9, 9, 9)      # [b][k][j][i]
+    low = tab[:, :8, :8, :8].reshape(-1)
+    hanging = m.hang_start[1:] > m.hang_start[:-1]
+    count = np.bincount(low[~hanging[low]], minlength=m.ncorners)
+    free = ~hanging
+    assert np.all(count[free] == 1), (np.sum(count[free] == 0), np.sum(count[free] > 1))

@@ -1,0 +1,116 @@
+"""Learned GMRES preconditioner on block-structured AMR meshes (and the mesh
+maps it shares with uniform meshes).
+
+* coverage of the mesh maps: with all weights zero the network adds nothing,
+  so the flexible solve with the learned preconditioner must reproduce the
+  Jacobi solve (same iterations, same fields): a corner written by no block,
+  or by two, would change z = D v and the Krylov space;
+* weight sets: one per refinement level, harvested samples tagged with their
+  block's level;
+* in-situ training from the run's own Jacobi solves: every set's loss falls,
+  and on a later state the trained network converges to the same solution in
+  no more iterations than Jacobi, on the tensor-core and the FP32 path.
+"""
+import numpy as np
+import pytest
+
+import amps_gb300 as A
+from amps_gb300 import precond as PC
+from tests.gpu_cases import rel_err
+from tests.test_gpu_amr import amr_case, gpu_for
+
+pytestmark = pytest.mark.gpu
+
+
+def solve_from(ctx, f0, precond, tc=None):
+    ctx.import_fields(**f0)
+    if tc is not None:
+        ctx.precond_use_tensor_cores(tc)
+    st = ctx.TimeStep(tol=1e-8, maxit=400, precond=precond)
+    assert st.converged and st.rel_residual <= 1e-8
+    return st.iterations, ctx.export_fields()
+
+
+@pytest.mark.parametrize("kind", ["amr", "uniform"])
+def test_zero_network_reproduces_jacobi(kind):
+    if kind == "amr":
+        mesh, wl, ic, x, f = amr_case(ppc=8)
+        ctx = gpu_for(mesh, wl, ic, x, f)
+        nsets = mesh.lmax + 1
+    else:
+        wl = A.electron_proton_plasma("u", 2, 2, 2, 8, 2)
+        ctx = A.EcsimContext(wl, capacity=wl.nparticles + 1024)
+        ic = A.make_initial_condition(wl)
+        ctx.import_particles_local(ic["u"], ic["v"], ic["spec"], ic["block"])
+        ctx.import_fields(**A.initial_fields(wl))
+        nsets = 1
+    with ctx:
+        assert ctx.precond_num_sets() == nsets
+        ctx.UpdateJMassMatrix()
+        f0 = ctx.export_fields()
+        it_j, fj = solve_from(ctx, f0, 1)
+        ctx.precond_select(0)   # creates the network: every set's weights are zero
+        it_tc, ftc = solve_from(ctx, f0, 2, tc=True)
+        it_32, f32 = solve_from(ctx, f0, 2, tc=False)
+    # the inner operator's FP32 rounding differs between the two forms, so
+    # the iterates agree to about the tolerance, not bit for bit
+    assert abs(it_tc - it_j) <= 1 and abs(it_32 - it_j) <= 1, (it_j, it_tc, it_32)
+    for k in ("E_n", "E_half", "B_center"):
+        assert rel_err(ftc[k], fj[k]) < 1e-7, k
+        assert rel_err(f32[k], fj[k]) < 1e-7, k
+
+
+def test_weight_sets_and_sample_levels():
+    mesh, wl, ic, x, f = amr_case(ppc=8)
+    ctx = gpu_for(mesh, wl, ic, x, f)
+    with ctx:
+        ctx.UpdateJMassMatrix()
+        ctx.precond_harvest(3 * mesh.nblocks)
+        ctx.TimeStep(tol=1e-8, maxit=400, precond=1)
+        n = ctx.precond_num_samples()
+        assert n >= mesh.nblocks
+        sets = ctx.precond_sample_sets(0, n)
+        # samples come in whole sweeps over the blocks, in block order
+        lev = np.asarray(mesh.level)
+        for s0 in range(0, n - mesh.nblocks + 1, mesh.nblocks):
+            assert np.array_equal(sets[s0:s0 + mesh.nblocks], lev)
+        with pytest.raises(A.AmpsGpuError):
+            ctx.precond_select(mesh.lmax + 1)
+        # set 1 holds its own weights
+        w0 = A.init_precond_weights(seed=1)
+        w1 = A.init_precond_weights(seed=2)
+        ctx.precond_select(0)
+        ctx.precond_load(*w0)
+        ctx.precond_select(1)
+        ctx.precond_load(*w1)
+        got1 = ctx.precond_weights()
+        ctx.precond_select(0)
+        got0 = ctx.precond_weights()
+    for a, b in zip(got0, w0):
+        assert np.array_equal(a, b)
+    for a, b in zip(got1, w1):
+        assert np.array_equal(a, b)
+
+
+def test_trained_amr_preconditioner():
+    mesh, wl, ic, x, f = amr_case(ppc=16, seed=21)
+    ctx = gpu_for(mesh, wl, ic, x, f)
+    with ctx:
+        ctx.UpdateJMassMatrix()
+        info = PC.train_in_situ(ctx, 40 * mesh.nblocks, epochs=30, batch=32, lr=2e-3, seed=3)
+        assert info["samples"] == 40 * mesh.nblocks
+        for e in info["sets"]:
+            assert e["samples"] > 0
+            first, last = e["loss_first_last"]
+            assert last < 0.5 * first, e
+        # a later state of the same run
+        for _ in range(2):
+            ctx.PicTimeStep(tol=1e-8, maxit=400, precond=1)
+        f0 = ctx.export_fields()
+        it_j, fj = solve_from(ctx, f0, 1)
+        it_tc, ftc = solve_from(ctx, f0, 2, tc=True)
+        it_32, f32 = solve_from(ctx, f0, 2, tc=False)
+    assert it_tc <= it_j and it_32 <= it_j, (it_j, it_tc, it_32)
+    for k in ("E_n", "B_center"):
+        assert rel_err(ftc[k], fj[k]) < 1e-6, k
+        assert rel_err(f32[k], fj[k]) < 1e-6, k
