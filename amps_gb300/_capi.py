@@ -107,6 +107,7 @@ SIGNATURES = {
     "amps_gpu_precond_sample_sets": (C.c_int, [P, C.c_longlong, C.c_longlong, I32]),
     "amps_gpu_precond_num_sets": (C.c_int, [P, C.POINTER(C.c_int)]),
     "amps_gpu_precond_select": (C.c_int, [P, C.c_int]),
+    "amps_gpu_precond_interface_jacobi": (C.c_int, [P, C.c_int, C.POINTER(C.c_int)]),
     "amps_gpu_precond_train": (C.c_int, [P, C.c_int, C.c_int, C.c_float, C.c_ulonglong, F]),
     "amps_gpu_precond_loss_grad": (C.c_int, [P, C.c_longlong, F, F, F, F, F, F]),
     "amps_gpu_precond_forward": (C.c_int, [P, C.c_longlong, F, C.c_int, F]),

@@ -355,14 +355,38 @@ bool upload(T** d, const std::vector<T>& h) {
          cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
-// The learned preconditioner's mesh maps (see amps_gpu_ctx::d_pc_in).
+// The learned preconditioner's mesh maps (see amps_gpu_ctx::d_pc_in).  The
+// interface variant of the output maps hands the corners of every block whose
+// region holds a non-free entry to the Jacobi list.
 bool upload_pc_maps(amps_gpu_ctx* c, const std::vector<int>& in, const std::vector<int>& out,
                     const std::vector<int>& set, const std::vector<int>& jac, int nsets) {
   c->pc_nsets = nsets;
-  c->pc_njac = (long long)jac.size();
   c->h_pc_set = set;
-  return upload(&c->d_pc_in, in) && upload(&c->d_pc_out, out) && upload(&c->d_pc_jac, jac) &&
-         (nsets == 1 || upload(&c->d_pc_set, set));
+  std::vector<int> out1(out), jac1(jac);
+  int niface = 0;
+  c->h_pc_iface.assign((size_t)c->nb, 0);
+  for (int b = 0; b < c->nb; b++) {
+    bool iface = false;
+    for (int v = 0; v < 1000 && !iface; v++) iface = in[(size_t)b * 1000 + v] < 0;
+    if (!iface) continue;
+    niface++;
+    c->h_pc_iface[(size_t)b] = 1;
+    for (int q = 0; q < 512; q++) {
+      int& o = out1[(size_t)b * 512 + q];
+      if (o >= 0) jac1.push_back(o);
+      o = -1;
+    }
+  }
+  c->pc_iface_blocks = niface;
+  c->pc_njac_v[0] = (long long)jac.size();
+  c->pc_njac_v[1] = (long long)jac1.size();
+  const bool ok = upload(&c->d_pc_in, in) && upload(&c->d_pc_out_v[0], out) &&
+                  upload(&c->d_pc_jac_v[0], jac) && upload(&c->d_pc_out_v[1], out1) &&
+                  upload(&c->d_pc_jac_v[1], jac1) && (nsets == 1 || upload(&c->d_pc_set, set));
+  c->d_pc_out = c->d_pc_out_v[0];
+  c->d_pc_jac = c->d_pc_jac_v[0];
+  c->pc_njac = c->pc_njac_v[0];
+  return ok;
 }
 
 // Uniform periodic mesh: region corner (i, j, k) in -1..8 of block b is the
@@ -385,10 +409,11 @@ bool build_pc_maps_uniform(amps_gpu_ctx* c) {
 }
 
 // AMR mesh: region corner (i, j, k) of block b sits at origin + (i, j, k) *
-// scale on the finest lattice (periodic); it is the unique corner there, or -1
-// where none exists (inside a coarser neighbour's cell) or it is hanging.  A
-// free corner is written by the block whose cell has it as low corner (the
-// leaf containing the corner + (eps, eps, eps)); hanging corners keep z = D v.
+// scale on the finest lattice (periodic); its entry is the unique corner
+// there, -2 - h for a hanging corner h (input interpolated from its parents),
+// or -1 where none exists (inside a coarser neighbour's cell).  A free corner
+// is written by the block whose cell has it as low corner (the leaf containing
+// the corner + (eps, eps, eps)); hanging corners keep z = D v.
 bool build_pc_maps_amr(amps_gpu_ctx* c, const amps_amr_mesh* m) {
   const long long nbl = (long long)m->blocks.size(), nv = c->nvc;
   const long long FX = m->nfine[0], FY = m->nfine[1], FZ = m->nfine[2];
@@ -413,7 +438,8 @@ bool build_pc_maps_amr(amps_gpu_ctx* c, const amps_amr_mesh* m) {
     for (int v = 0; v < 1000; v++) {
       const auto it = at.find(key(d.ix + (long long)(v % 10 - 1) * sc, d.iy + (long long)((v / 10) % 10 - 1) * sc,
                                   d.iz + (long long)(v / 100 - 1) * sc));
-      in[(size_t)b * 1000 + v] = (it == at.end() || hanging(it->second)) ? -1 : it->second;
+      in[(size_t)b * 1000 + v] =
+          it == at.end() ? -1 : (hanging(it->second) ? -2 - it->second : it->second);
     }
     for (int q = 0; q < 512; q++) {
       const int id = m->corner_tab[(size_t)b * 729 + (q & 7) + 9 * (((q >> 3) & 7) + 9 * (q >> 6))];
@@ -620,7 +646,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw,
                   c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol,
-                  c->d_ss, c->d_sc, c->d_sv, c->d_pc_in, c->d_pc_out, c->d_pc_set, c->d_pc_jac};
+                  c->d_ss, c->d_sc, c->d_sv, c->d_pc_in, c->d_pc_out_v[0], c->d_pc_out_v[1],
+                  c->d_pc_set, c->d_pc_jac_v[0], c->d_pc_jac_v[1]};
   for (void* p : ptrs) cudaFree(p);
   for (int b = 0; b < 2; b++) {
     for (int q = 0; q < 3; q++) {

@@ -99,17 +99,25 @@ struct amps_gpu_ctx {
   bool inner_fp32 = true;       // GMRES inner operator in FP32 (iterative refinement)
   PrecondState* pn = nullptr;   // learned preconditioner (precond.cu)
   // the network's view of the mesh: per block the 10^3 corner region (block
-  // corners -1..8) and the 8^3 corners it writes, as indices into the corner
-  // vectors (-1: no input there / not written by this block), the weight set
-  // of the block (its refinement level; null on a uniform mesh) and the
-  // corners no block writes (hanging corners: z = D v there)
+  // corners -1..8) as entries of pc_input(), the 8^3 corners it writes as
+  // indices into the corner vectors (-1: not written by this block), the
+  // weight set of the block (its refinement level; null on a uniform mesh) and
+  // the corners no block writes (z = D v there).  Two variants of the output
+  // maps: [0] the network on every block, [1] Jacobi on the blocks whose region
+  // reaches a refinement interface (a hanging or missing corner).
   int* d_pc_in = nullptr;       // [nb*1000]
-  int* d_pc_out = nullptr;      // [nb*512]
+  int* d_pc_out = nullptr;      // active variant [nb*512]
   int* d_pc_set = nullptr;      // [nb]
-  int* d_pc_jac = nullptr;      // [pc_njac]
+  int* d_pc_jac = nullptr;      // active variant [pc_njac]
   long long pc_njac = 0;
+  int* d_pc_out_v[2] = {nullptr, nullptr};
+  int* d_pc_jac_v[2] = {nullptr, nullptr};
+  long long pc_njac_v[2] = {0, 0};
   int pc_nsets = 1;
+  int pc_iface_blocks = 0;      // blocks that reach a refinement interface
+  bool pc_iface_jacobi = false; // variant [1] active
   std::vector<int> h_pc_set;    // [nb]
+  std::vector<char> h_pc_iface; // [nb] block reaches a refinement interface
 
   // launch parameters chosen by the autotuner (field.cu: field_autotune)
   int tune_tb = 256;            // threads per CTA of the operator kernels
@@ -127,6 +135,8 @@ struct amps_gpu_ctx {
   double* d_red = nullptr;      // partial reductions
   double* h_red = nullptr;      // pinned
   int restart = 30;
+  int gm_guess[3] = {0, 0, 0};  // per preconditioner: Arnoldi steps of the last first cycle
+                                // (steps queued before the host first waits)
 
   // per-block FP32 stencils
   float* d_stencil_push = nullptr;  // nb * 729 * 8
@@ -242,6 +252,24 @@ cudaError_t launch_amr_fix_hanging(amps_gpu_ctx* c, double* F);
 // ---- device helpers ----
 __host__ __device__ inline int nbr_slot(int ox, int oy, int oz) {
   return (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
+}
+
+// Input of the learned preconditioner at one entry e of its region map: D v at
+// a free corner (e >= 0), nothing (e == -1: no corner of the block's lattice
+// there), or at a hanging corner h (e = -2 - h) D v interpolated from its
+// parents (hs/hp/hw: the hanging-corner CSR of the mesh).
+__device__ __forceinline__ double pc_input(int e, int ch, long long nvc, const double* __restrict__ v,
+                                           const double* __restrict__ dinv, const int* __restrict__ hs,
+                                           const int* __restrict__ hp, const double* __restrict__ hw) {
+  if (e >= 0) return dinv[ch * nvc + e] * v[ch * nvc + e];
+  if (e == -1) return 0.0;
+  const int h = -2 - e;
+  double s = 0.0;
+  for (int q = hs[h]; q < hs[h + 1]; q++) {
+    const long long p = hp[q];
+    s += hw[q] * dinv[ch * nvc + p] * v[ch * nvc + p];
+  }
+  return s;
 }
 
 // Corner (or cell) id of block-local index (i,j,k) in [-8,16): follows the

@@ -31,6 +31,7 @@ namespace {
 constexpr double kPi = 3.14159265358979323846264338327950288;
 constexpr int kMaxV = 32;
 constexpr int kRedBlocks = 304;  // 2 x 152 SMs
+constexpr int kGmOffset = 10240;  // doubles into d_red (12288 doubles)
 
 struct Taps {
   double K[3][3][27];  // operator taps without the mass matrix
@@ -341,12 +342,14 @@ __global__ void __launch_bounds__(256) k_residual(long long n, const double* __r
     r[t] = b[t] - r[t];
 }
 
-// x += dinv .* sum_i y_i V_i
+// x += dinv .* sum_i y_i V_i  (nv from *d_nv when given)
 __global__ void __launch_bounds__(256) k_combine(long long n, const double* __restrict__ V,
                                                  const double* __restrict__ y, int nv,
+                                                 const int* __restrict__ d_nv,
                                                  const double* __restrict__ dinv,
                                                  double* __restrict__ x) {
   __shared__ double s_y[kMaxV];
+  if (d_nv) nv = *d_nv;
   if (threadIdx.x < kMaxV) s_y[threadIdx.x] = threadIdx.x < nv ? y[threadIdx.x] : 0.0;
   __syncthreads();
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
@@ -365,6 +368,73 @@ __global__ void __launch_bounds__(256) k_norm2(long long n, const double* __rest
        t += (long long)gridDim.x * blockDim.x)
     acc[0] += v[t] * v[t];
   block_store_partials<1>(acc, 1, partial);
+}
+
+// GMRES least-squares state on the device: the Hessenberg columns after the
+// Givens rotations (row stride kMaxV), the rotations, the rotated right-hand
+// side g (|g[j]| = residual norm after j steps), the solution y, and the
+// step count jj / converged flag that the host polls.
+struct GmState {
+  double H[(kMaxV + 1) * kMaxV];
+  double cs[kMaxV], sn[kMaxV];
+  double g[kMaxV + 1];
+  double y[kMaxV];
+  double target;
+  int jj;    // columns processed in this cycle
+  int done;  // |g[jj]| <= target, or breakdown
+};
+static_assert(kGmOffset * sizeof(double) + sizeof(GmState) <= 12288 * sizeof(double),
+              "GmState must fit in d_red");
+static_assert(kRedBlocks * kMaxV + 2 * kMaxV + 8 + kMaxV <= kGmOffset, "d_red layout");
+
+// start of a cycle: g = (||r||, 0, ...); *n2 = ||r||^2
+__global__ void k_gm_start(GmState* __restrict__ S, const double* __restrict__ n2, double target) {
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i <= kMaxV; i++) S->g[i] = 0.0;
+  S->g[0] = sqrt(*n2);
+  S->target = target;
+  S->jj = 0;
+  S->done = 0;
+}
+
+// Arnoldi column jj: h = h1 + h2 (the two CGS passes), h[jj+1] = ||w||; apply
+// the previous rotations, form rotation jj, update g.  Frozen once done, so
+// steps launched past convergence change nothing the solution uses.
+__global__ void k_gm_step(GmState* __restrict__ S, int jj, const double* __restrict__ h1,
+                          const double* __restrict__ h2, const double* __restrict__ n2) {
+  if (threadIdx.x != 0 || S->done) return;
+  double* H = S->H;
+  for (int i = 0; i <= jj; i++) H[i * kMaxV + jj] = h1[i] + h2[i];
+  const double hn = sqrt(*n2);
+  H[(jj + 1) * kMaxV + jj] = hn;
+  for (int i = 0; i < jj; i++) {
+    const double a = H[i * kMaxV + jj], b = H[(i + 1) * kMaxV + jj];
+    H[i * kMaxV + jj] = S->cs[i] * a + S->sn[i] * b;
+    H[(i + 1) * kMaxV + jj] = -S->sn[i] * a + S->cs[i] * b;
+  }
+  const double a = H[jj * kMaxV + jj], b = H[(jj + 1) * kMaxV + jj];
+  const double r = sqrt(a * a + b * b);
+  const double c = r > 0.0 ? a / r : 1.0, s = r > 0.0 ? b / r : 0.0;
+  S->cs[jj] = c;
+  S->sn[jj] = s;
+  H[jj * kMaxV + jj] = r;
+  H[(jj + 1) * kMaxV + jj] = 0.0;
+  S->g[jj + 1] = -s * S->g[jj];
+  S->g[jj] = c * S->g[jj];
+  S->jj = jj + 1;
+  if (fabs(S->g[jj + 1]) <= S->target || hn == 0.0) S->done = 1;
+}
+
+// y = R^-1 g on the processed columns (back substitution)
+__global__ void k_gm_solve(GmState* __restrict__ S) {
+  if (threadIdx.x != 0) return;
+  const int j = S->jj;
+  for (int i = j - 1; i >= 0; i--) {
+    double t = S->g[i];
+    for (int q = i + 1; q < j; q++) t -= S->H[i * kMaxV + q] * S->y[q];
+    const double d = S->H[i * kMaxV + i];
+    S->y[i] = d != 0.0 ? t / d : 0.0;
+  }
 }
 
 // one CGS2 Arnoldi orthogonalisation with a register budget fitted to nv
@@ -553,24 +623,28 @@ cudaError_t launch_update_e(amps_gpu_ctx* c) {
   return cudaGetLastError();
 }
 
-// GMRES(m) with right preconditioning, CGS2 Arnoldi, Givens on the host, and
-// iterative refinement across restarts: every cycle starts from the true FP64
-// residual r = b - A x, its Arnoldi steps apply the operator with its identity
-// part in FP64 and the rest in FP32 (c->inner_fp32), and the solve ends when the
-// FP64 residual satisfies ||b - A x|| <= tol ||b||.  The preconditioner is
-// none (precond 0), Jacobi (1, z = D v) or the learned block network (2,
-// z = D v + N(D v); flexible form: the directions z_j are kept).
+// GMRES(m) with right preconditioning, CGS2 Arnoldi, Givens rotations on the
+// device, and iterative refinement across restarts: every cycle starts from
+// the true FP64 residual r = b - A x, its Arnoldi steps apply the operator with
+// its identity part in FP64 and the rest in FP32 (c->inner_fp32), and the solve
+// ends when the FP64 residual satisfies ||b - A x|| <= tol ||b||.  The
+// preconditioner is none (precond 0), Jacobi (1, z = D v) or the learned block
+// network (2, z = D v + N(D v); flexible form: the directions z_j are kept).
+// The host does not wait for each step: it queues as many Arnoldi steps as the
+// last cycle took before it first reads the device's convergence flag, then
+// one step per read; steps queued past convergence leave the least-squares
+// state untouched (k_gm_step is frozen), so they cost time but not accuracy.
 // Device scratch layout of d_red: [0, kRedBlocks*kMaxV) partials, then h1
-// (kMaxV), h2 (kMaxV), nrm2 (1), y.
+// (kMaxV), h2 (kMaxV), nrm2 (8), y (kMaxV); GmState at kGmOffset.
 amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
                             amps_gpu_solve_stats* st) {
   const long long n = 3 * c->nvc;
-  const int m = c->restart;
+  const int m = std::min(c->restart, kMaxV);
   double* partial = c->d_red;
   double* d_h1 = c->d_red + kRedBlocks * kMaxV;
   double* d_h2 = d_h1 + kMaxV;
   double* d_n2 = d_h2 + kMaxV;
-  double* d_y = d_n2 + 8;
+  GmState* gs = reinterpret_cast<GmState*>(c->d_red + kGmOffset);
   const unsigned gr = gridr(n, c->tune_red, c->tune_ept);
   cudaStream_t s = c->stream;
   cudaError_t e;
@@ -603,7 +677,6 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   CK(cudaMemsetAsync(c->d_x, 0, sizeof(double) * n, s));
   double bnorm = 0.0;
   CK(read_norm(c->d_rhs, &bnorm));
-  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1), y(m);
   int it = 0, cycles = 0;
   bool conv = false;
   double rel = 0.0;
@@ -624,15 +697,14 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     // of the off-identity terms), so a cycle runs to the tolerance; a later
     // cycle only corrects what that noise left
     const double target = tol * bnorm;
-    // V0 = r / ||r||
-    c->h_red[0] = beta * beta;
-    CK(cudaMemcpyAsync(d_n2, c->h_red, sizeof(double), cudaMemcpyHostToDevice, s));
+    // V0 = r / ||r|| (d_n2 holds ||r||^2 from read_norm)
+    k_gm_start<<<1, 32, 0, s>>>(gs, d_n2, target);
     k_scale<<<gr, 256, 0, s>>>(n, w, V, d_n2);
-    std::fill(g.begin(), g.end(), 0.0);
-    g[0] = beta;
-    int jj = 0;
-    for (; jj < m && it < maxit; jj++) {
-      it++;
+    int launched = 0, used = 0;
+    bool done = false;
+    const int first_read = cycles == 1 ? std::max(1, std::min(c->gm_guess[precond], m)) : 1;
+    while (!done && launched < m && it + launched < maxit) {
+      const int jj = launched++;
       const int nv = jj + 1;
       double* vj = V + (size_t)jj * n;
       if (flexible) {
@@ -656,40 +728,23 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
         else
           arnoldi_orth<32>(s, gr, n, V, w, nv, partial, d_h1, d_h2, d_n2, vnext);
       }
+      k_gm_step<<<1, 32, 0, s>>>(gs, jj, d_h1, d_h2, d_n2);
       CK(cudaGetLastError());
-      CK(cudaMemcpyAsync(c->h_red, d_h1, sizeof(double) * (2 * kMaxV + 1), cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      for (int i = 0; i < nv; i++) H[(size_t)i * m + jj] = c->h_red[i] + c->h_red[kMaxV + i];
-      const double hn = std::sqrt(c->h_red[2 * kMaxV]);
-      H[(size_t)(jj + 1) * m + jj] = hn;
-      for (int i = 0; i < jj; i++) {
-        const double a = H[(size_t)i * m + jj], bb = H[(size_t)(i + 1) * m + jj];
-        H[(size_t)i * m + jj] = cs[i] * a + sn[i] * bb;
-        H[(size_t)(i + 1) * m + jj] = -sn[i] * a + cs[i] * bb;
-      }
-      const double a = H[(size_t)jj * m + jj], bb = H[(size_t)(jj + 1) * m + jj];
-      const double r = std::sqrt(a * a + bb * bb);
-      cs[jj] = r > 0.0 ? a / r : 1.0;
-      sn[jj] = r > 0.0 ? bb / r : 0.0;
-      H[(size_t)jj * m + jj] = r;
-      H[(size_t)(jj + 1) * m + jj] = 0.0;
-      g[jj + 1] = -sn[jj] * g[jj];
-      g[jj] = cs[jj] * g[jj];
-      if (std::fabs(g[jj + 1]) <= target || hn == 0.0) {
-        jj++;
-        break;
+      if (launched >= first_read || launched == m || it + launched >= maxit) {
+        CK(cudaMemcpyAsync(c->h_red, &gs->jj, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        const int* stat = reinterpret_cast<const int*>(c->h_red);
+        used = stat[0];
+        done = stat[1] != 0;
       }
     }
-    for (int i = jj - 1; i >= 0; i--) {
-      double t = g[i];
-      for (int q = i + 1; q < jj; q++) t -= H[(size_t)i * m + q] * y[q];
-      y[i] = H[(size_t)i * m + i] != 0.0 ? t / H[(size_t)i * m + i] : 0.0;
-    }
-    CK(cudaMemcpyAsync(d_y, y.data(), sizeof(double) * jj, cudaMemcpyHostToDevice, s));
+    it += used;
+    if (cycles == 1) c->gm_guess[precond] = used;
+    k_gm_solve<<<1, 32, 0, s>>>(gs);
     if (flexible)
-      k_combine<<<gr, 256, 0, s>>>(n, c->d_Z, d_y, jj, nullptr, c->d_x);
+      k_combine<<<gr, 256, 0, s>>>(n, c->d_Z, gs->y, kMaxV, &gs->jj, nullptr, c->d_x);
     else
-      k_combine<<<gr, 256, 0, s>>>(n, V, d_y, jj, dinv, c->d_x);
+      k_combine<<<gr, 256, 0, s>>>(n, V, gs->y, kMaxV, &gs->jj, dinv, c->d_x);
     CK(cudaGetLastError());
     // true residual in FP64
     CK(launch_matvec(c, c->d_x, nullptr, w));

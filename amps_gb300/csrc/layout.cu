@@ -1,6 +1,7 @@
-// Host <-> device layout conversion of fields and moments, done on the GPU:
-// the host array crosses the bus in one bulk copy through a device staging
-// buffer, and a kernel permutes it.
+// Host <-> device layout conversion of fields and moments, done on the GPU.
+// A page-locked host array is read or written by the permuting kernel itself
+// across the host link (no staging copy in HBM); a pageable one crosses the
+// bus in one bulk copy through a device staging buffer.
 //
 // Host layout: interleaved per point (point*ncomp + comp); points numbered
 // I + NX (J + NY K) on uniform meshes (the reference's global corner order),
@@ -84,6 +85,17 @@ unsigned grid_of(long long n) {
 
 Perm perm_of(const amps_gpu_ctx* c) { return Perm{c->cfg.nbx, c->cfg.nby, c->amr}; }
 
+// device address of a page-locked host array, or null for pageable memory
+template <class T>
+T* mapped(T* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? static_cast<T*>(at.devicePointer) : nullptr;
+}
+
 // device staging of `bytes` (grows on demand, kept with the context)
 double* host_stage(amps_gpu_ctx* c, size_t bytes) {
   if (c->hstage_bytes >= bytes) return c->d_hstage;
@@ -104,9 +116,14 @@ amps_gpu_status layout_upload(amps_gpu_ctx* c, const double* host, void* dev, lo
                               int ncomp, bool dev_f32) {
   if (!host) return AMPS_GPU_OK;
   const size_t bytes = sizeof(double) * (size_t)n * ncomp;
-  double* st = host_stage(c, bytes);
-  if (!st) return set_err(c, AMPS_GPU_CUDA_ERROR, "layout staging allocation failed");
-  cudaError_t e = cudaMemcpyAsync(st, host, bytes, cudaMemcpyHostToDevice, c->stream);
+  const double* st = mapped(host);
+  cudaError_t e = cudaSuccess;
+  if (!st) {
+    double* buf = host_stage(c, bytes);
+    if (!buf) return set_err(c, AMPS_GPU_CUDA_ERROR, "layout staging allocation failed");
+    e = cudaMemcpyAsync(buf, host, bytes, cudaMemcpyHostToDevice, c->stream);
+    st = buf;
+  }
   if (e == cudaSuccess) {
     if (dev_f32)
       k_to_device<float><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c), st,
@@ -124,7 +141,8 @@ amps_gpu_status layout_download(amps_gpu_ctx* c, const void* dev, double* host, 
                                 int ncomp, bool dev_f32) {
   if (!host) return AMPS_GPU_OK;
   const size_t bytes = sizeof(double) * (size_t)n * ncomp;
-  double* st = host_stage(c, bytes);
+  double* direct = mapped(host);
+  double* st = direct ? direct : host_stage(c, bytes);
   if (!st) return set_err(c, AMPS_GPU_CUDA_ERROR, "layout staging allocation failed");
   if (dev_f32)
     k_to_host<float><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c),
@@ -133,7 +151,7 @@ amps_gpu_status layout_download(amps_gpu_ctx* c, const void* dev, double* host, 
     k_to_host<double><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c),
                                                         static_cast<const double*>(dev), st);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(host, st, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && !direct) e = cudaMemcpyAsync(host, st, bytes, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_check(c, e, "download");
 }
@@ -142,15 +160,19 @@ amps_gpu_status layout_cell_moments(amps_gpu_ctx* c, double* hJ, double* hM) {
   const long long nc = c->ncor;
   const size_t bj = hJ ? sizeof(double) * (size_t)nc * 24 : 0;
   const size_t bm = hM ? sizeof(double) * (size_t)nc * 324 : 0;
-  double* st = host_stage(c, bj + bm);
-  if (!st) return set_err(c, AMPS_GPU_CUDA_ERROR, "layout staging allocation failed");
-  double* sJ = hJ ? st : nullptr;
-  double* sM = hM ? st + (bj / sizeof(double)) : nullptr;
+  // page-locked destinations are written by the kernel directly
+  double* mJ = hJ ? mapped(hJ) : nullptr;
+  double* mM = hM ? mapped(hM) : nullptr;
+  const size_t stage = (hJ && !mJ ? bj : 0) + (hM && !mM ? bm : 0);
+  double* st = stage ? host_stage(c, stage) : nullptr;
+  if (stage && !st) return set_err(c, AMPS_GPU_CUDA_ERROR, "layout staging allocation failed");
+  double* sJ = hJ ? (mJ ? mJ : st) : nullptr;
+  double* sM = hM ? (mM ? mM : st + (hJ && !mJ ? bj / sizeof(double) : 0)) : nullptr;
   k_cell_moments_to_host<<<grid_of(nc * 324), 256, 0, c->stream>>>(nc, c->d_cellJ, c->d_cellM, sJ,
                                                                     sM);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess && hJ) e = cudaMemcpyAsync(hJ, sJ, bj, cudaMemcpyDeviceToHost, c->stream);
-  if (e == cudaSuccess && hM) e = cudaMemcpyAsync(hM, sM, bm, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && hJ && !mJ) e = cudaMemcpyAsync(hJ, sJ, bj, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && hM && !mM) e = cudaMemcpyAsync(hM, sM, bm, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   return cuda_check(c, e, "download cell moments");
 }

@@ -224,6 +224,8 @@ __global__ void k_gather_batch(int S, const int* __restrict__ perm, long long fi
 // by dinv; where it writes none, e = x so that the target correction is 0),
 // both divided by the RMS of x over R.
 __global__ void __launch_bounds__(256) k_harvest(int nb, long long nvc, const int* __restrict__ in_map,
+                                                 const int* __restrict__ hs, const int* __restrict__ hp,
+                                                 const double* __restrict__ hw,
                                                  const int* __restrict__ out_map,
                                                  const double* __restrict__ r,
                                                  const double* __restrict__ e,
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(256) k_harvest(int nb, long long nvc, const in
     const int id = in_map[(size_t)b * kRV + q];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++) {
-      const double v = id >= 0 ? dinv[ch * nvc + id] * r[ch * nvc + id] : 0.0;
+      const double v = pc_input(id, ch, nvc, r, dinv, hs, hp, hw);
       sxv[q * 3 + ch] = (float)v;
       ss += v * v;
     }
@@ -275,6 +277,9 @@ __global__ void __launch_bounds__(256) k_harvest(int nb, long long nvc, const in
 // inference input: wx[b][v][ch] = dinv .* v on R around mesh block b
 __global__ void __launch_bounds__(256) k_gather_region(int nb, long long nvc,
                                                        const int* __restrict__ in_map,
+                                                       const int* __restrict__ hs,
+                                                       const int* __restrict__ hp,
+                                                       const double* __restrict__ hw,
                                                        const double* __restrict__ vin,
                                                        const double* __restrict__ dinv,
                                                        float* __restrict__ wx) {
@@ -283,7 +288,7 @@ __global__ void __launch_bounds__(256) k_gather_region(int nb, long long nvc,
     const int id = in_map[(size_t)b * kRV + q];
 #pragma unroll
     for (int ch = 0; ch < 3; ch++)
-      wx[((size_t)b * kRV + q) * 3 + ch] = id >= 0 ? (float)(dinv[ch * nvc + id] * vin[ch * nvc + id]) : 0.f;
+      wx[((size_t)b * kRV + q) * 3 + ch] = (float)pc_input(id, ch, nvc, vin, dinv, hs, hp, hw);
   }
 }
 
@@ -470,10 +475,12 @@ cudaError_t precond_harvest_pairs(amps_gpu_ctx* c, const double* r, const double
   PrecondState* P = c->pn;
   if (!P || P->cap <= 0 || P->n >= P->cap || !c->d_dinv) return cudaSuccess;
   TimedLaunch t(c, "precond_harvest");
-  k_harvest<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_in, c->d_pc_out, r, e, c->d_dinv,
+  k_harvest<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_in, c->d_hs, c->d_hp, c->d_hw,
+                                          c->d_pc_out_v[0], r, e, c->d_dinv,
                                           e_scaled, P->sx, P->se, P->n, P->cap);
   const long long add = std::min<long long>(P->cap - P->n, c->nb);
   P->sample_set.insert(P->sample_set.end(), c->h_pc_set.begin(), c->h_pc_set.begin() + add);
+  P->sample_iface.insert(P->sample_iface.end(), c->h_pc_iface.begin(), c->h_pc_iface.begin() + add);
   P->n += add;
   return cudaGetLastError();
 }
@@ -491,13 +498,14 @@ cudaError_t launch_precond_net(amps_gpu_ctx* c, const double* v, double* z) {
   }
   if (P->use_tc) {
     TimedLaunch t(c, "precond_net_tc");
-    return precond_apply_tc_mesh(P, c->stream, c->nb, c->d_pc_in, c->d_pc_out, c->d_pc_set, c->nvc,
-                                 v, c->d_dinv, z);
+    return precond_apply_tc_mesh(P, c->stream, c->nb, c->d_pc_in, c->d_hs, c->d_hp, c->d_hw,
+                                 c->d_pc_out, c->d_pc_set, c->nvc, v, c->d_dinv, z);
   }
   if ((e = precond_work(P, c->nb)) != cudaSuccess) return e;
   {
     TimedLaunch t(c, "precond_gather");
-    k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_in, v, c->d_dinv, P->wx);
+    k_gather_region<<<c->nb, 256, 0, c->stream>>>(c->nb, c->nvc, c->d_pc_in, c->d_hs, c->d_hp,
+                                                  c->d_hw, v, c->d_dinv, P->wx);
   }
   // the FP32 path runs every set's network over all blocks and keeps each
   // block's own
@@ -642,6 +650,7 @@ amps_gpu_status amps_gpu_precond_harvest(amps_gpu_ctx* c, long long capacity) {
   P->sx = P->se = nullptr;
   P->cap = P->n = 0;
   P->sample_set.clear();
+  P->sample_iface.clear();
   if (capacity == 0) return AMPS_GPU_OK;
   if (cudaMalloc(reinterpret_cast<void**>(&P->sx), sizeof(float) * capacity * 1000 * 3) != cudaSuccess ||
       cudaMalloc(reinterpret_cast<void**>(&P->se), sizeof(float) * capacity * 512 * 3) != cudaSuccess) {
@@ -667,6 +676,17 @@ amps_gpu_status amps_gpu_precond_select(amps_gpu_ctx* c, int set) {
   amps_gpu_status s = ensure_state(c);
   if (s) return s;
   precond_select(c->pn, set);
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_precond_interface_jacobi(amps_gpu_ctx* c, int on, int* nblocks) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  const int q = on ? 1 : 0;
+  c->pc_iface_jacobi = on != 0;
+  c->d_pc_out = c->d_pc_out_v[q];
+  c->d_pc_jac = c->d_pc_jac_v[q];
+  c->pc_njac = c->pc_njac_v[q];
+  if (nblocks) *nblocks = c->pc_iface_blocks;
   return AMPS_GPU_OK;
 }
 
@@ -703,10 +723,12 @@ amps_gpu_status amps_gpu_precond_train(amps_gpu_ctx* c, int epochs, int batch, f
   if (!c || !c->pn || epochs <= 0 || batch <= 0 || !(lr > 0.f))
     return set_err(c, AMPS_GPU_INVALID_ARG, "precond_train: bad arguments");
   PrecondState* P = c->pn;
-  // the active set's samples
+  // the active set's samples (without those of interface blocks when these
+  // use Jacobi)
   std::vector<int> perm;
   for (long long q = 0; q < P->n; q++)
-    if (P->sample_set[(size_t)q] == P->active) perm.push_back((int)q);
+    if (P->sample_set[(size_t)q] == P->active && !(c->pc_iface_jacobi && P->sample_iface[(size_t)q]))
+      perm.push_back((int)q);
   const long long ns = (long long)perm.size();
   if (ns < 1) return set_err(c, AMPS_GPU_INVALID_ARG, "precond_train: no samples of this weight set");
   cudaSetDevice(c->cfg.device);

@@ -38,6 +38,7 @@ struct PrecondState {
   float* se = nullptr;
   long long cap = 0, n = 0;
   std::vector<int> sample_set;
+  std::vector<char> sample_iface;  // sample's block reaches a refinement interface
   // work buffers for S samples
   int work_S = 0;
   float *wx = nullptr, *we = nullptr, *h1 = nullptr, *h2 = nullptr, *y = nullptr;
@@ -63,6 +64,7 @@ cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const fl
 // z = D v + N(D v) on the corners the blocks write, in one launch (gather
 // through in_map, network with the block's weight set, scatter through out_map)
 cudaError_t precond_apply_tc_mesh(PrecondState* P, cudaStream_t st, int nb, const int* in_map,
+                                  const int* hs, const int* hp, const double* hw,
                                   const int* out_map, const int* set, long long nvc,
                                   const double* v, const double* dinv, double* z);
 // GMRES hooks (field.cu)

@@ -151,6 +151,9 @@ struct MeshIO {
   const double* v;
   const double* dinv;
   const int* in_map;
+  const int* hs;  // hanging-corner CSR (AMR), for pc_input
+  const int* hp;
+  const double* hw;
   const int* out_map;
   const int* set;
   long long nvc;
@@ -204,12 +207,10 @@ __global__ void __cluster_dims__(kSplit, 1, 1) __launch_bounds__(128, 1)
       for (int ch = 0; ch < 3; ch++) xv[q][ch] = 0.f;
       if (v < 1000) {
         if (mesh.v) {
-          const long long id = mesh.in_map[(size_t)s * 1000 + v];
-          if (id >= 0) {
+          const int id = mesh.in_map[(size_t)s * 1000 + v];
 #pragma unroll
-            for (int ch = 0; ch < 3; ch++)
-              xv[q][ch] = (float)(mesh.dinv[ch * mesh.nvc + id] * mesh.v[ch * mesh.nvc + id]);
-          }
+          for (int ch = 0; ch < 3; ch++)
+            xv[q][ch] = (float)pc_input(id, ch, mesh.nvc, mesh.v, mesh.dinv, mesh.hs, mesh.hp, mesh.hw);
         } else {
 #pragma unroll
           for (int ch = 0; ch < 3; ch++) xv[q][ch] = __ldg(xs + 3 * v + ch);
@@ -418,19 +419,20 @@ cudaError_t precond_forward_tc(PrecondState* P, cudaStream_t st, int S, const fl
   if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
   cudaError_t e = set_tc_attr();
   if (e != cudaSuccess) return e;
-  MeshIO none{nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr};
+  MeshIO none{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0, nullptr};
   k_precond_tc<<<S * kSplit, 128, kSmem, st>>>(x, y, P->wtc + (size_t)P->active * (kWBytes / 2),
                                                P->flags, none);
   return cudaGetLastError();
 }
 
 cudaError_t precond_apply_tc_mesh(PrecondState* P, cudaStream_t st, int nb, const int* in_map,
+                                  const int* hs, const int* hp, const double* hw,
                                   const int* out_map, const int* set, long long nvc,
                                   const double* v, const double* dinv, double* z) {
   if (!P->tc_ready || !P->flags) return cudaErrorInvalidValue;
   cudaError_t e = set_tc_attr();
   if (e != cudaSuccess) return e;
-  MeshIO io{v, dinv, in_map, out_map, set, nvc, z};
+  MeshIO io{v, dinv, in_map, hs, hp, hw, out_map, set, nvc, z};
   k_precond_tc<<<nb * kSplit, 128, kSmem, st>>>(nullptr, nullptr, P->wtc, P->flags, io);
   return cudaGetLastError();
 }

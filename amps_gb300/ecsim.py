@@ -257,10 +257,13 @@ class EcsimContext:
         self._check(self.lib.amps_gpu_import_fields(self.h, *[ptr(a, C.c_double) for a in arrs]),
                     "import_fields")
 
-    def export_fields(self):
-        out = {k: np.empty((self.ncorners, 3)) for k in
-               ("E_n", "E_half", "B_corner_prev", "B_corner_cur")}
-        out["B_center"] = np.empty((self.ncells, 3))
+    def export_fields(self, out=None):
+        """corner E^n, E^{n+theta}, B prev/cur and centre B; out: dict of
+        arrays to fill (e.g. page-locked ones)"""
+        if out is None:
+            out = {k: np.empty((self.ncorners, 3)) for k in
+                   ("E_n", "E_half", "B_corner_prev", "B_corner_cur")}
+            out["B_center"] = np.empty((self.ncells, 3))
         self._check(self.lib.amps_gpu_export_fields(
             self.h, *[ptr(out[k], C.c_double) for k in
                       ("E_n", "E_half", "B_center", "B_corner_prev", "B_corner_cur")]),
@@ -353,6 +356,14 @@ class EcsimContext:
     def precond_select(self, wset):
         """Weight set that load / weights / train / loss_grad / forward act on."""
         self._check(self.lib.amps_gpu_precond_select(self.h, int(wset)), "precond_select")
+
+    def precond_interface_jacobi(self, on=True):
+        """Jacobi instead of the network on blocks at refinement interfaces;
+        returns the number of such blocks."""
+        n = C.c_int()
+        self._check(self.lib.amps_gpu_precond_interface_jacobi(self.h, 1 if on else 0, C.byref(n)),
+                    "precond_interface_jacobi")
+        return n.value
 
     def precond_sample_sets(self, first=0, count=None):
         if count is None:

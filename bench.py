@@ -510,6 +510,28 @@ def oracle_check(workload, device):
             "gmres_iterations_gpu_oracle": [st.solve.iterations, int(it)]}
 
 
+def field_solve_ab(ctx, tol, ev, stream, reps=3):
+    """Jacobi vs learned field solve from the same state (fields restored
+    between solves; the moments do not change): iterations and CUDA-event
+    times."""
+    f0 = ctx.export_fields()
+    out = {}
+    for pc, nm in ((1, "jacobi"), (2, "learned")):
+        ms, its = [], []
+        for _ in range(reps):
+            ctx.import_fields(**f0)
+            a, b = ev.event(), ev.event()
+            ev.record(a, stream)
+            st = ctx.TimeStep(tol=tol, maxit=400, precond=pc)
+            ev.record(b, stream)
+            ms.append(ev.elapsed_ms(a, b))
+            its.append(st.iterations)
+        out[nm] = {"iterations": its[-1], "ms": round(float(np.median(ms)), 3)}
+    ctx.import_fields(**f0)
+    out["speedup"] = round(out["jacobi"]["ms"] / out["learned"]["ms"], 3)
+    return out
+
+
 # ---------------------------------------------------------------------------
 def run_gpu(args):
     import amps_gb300 as A
@@ -566,20 +588,35 @@ def run_gpu(args):
     # energy conservation over many full ECSIM steps (theta = 0.5)
     energy = None
     if args.energy_steps > 0:
+        pc = args.energy_precond
+        training = solve_ab = None
+        if pc == 2:
+            # the network learns from this run's own Jacobi solves (one weight
+            # set per refinement level), then replaces Jacobi
+            from amps_gb300 import precond as PC
+            training = PC.train_in_situ(ctx, args.train_samples, tol=tol, epochs=20, batch=64,
+                                        lr=2e-3, seed=0)
+            ctx.precond_use_tensor_cores(True)
+            solve_ab = field_solve_ab(ctx, tol, ev, stream)
         tot = []
         its = []
         t0 = time.perf_counter()
         for _ in range(args.energy_steps):
-            s = ctx.PicTimeStep(tol=tol, maxit=400, precond=1)
+            s = ctx.PicTimeStep(tol=tol, maxit=400, precond=pc)
             tot.append(s.particle_energy + s.solve.wave_energy)
             its.append(s.solve.iterations)
         wall = time.perf_counter() - t0
         tot = np.array(tot)
-        energy = {"steps": args.energy_steps, "total_energy_first": float(tot[0]),
+        energy = {"steps": args.energy_steps, "precond": {1: "jacobi", 2: "learned"}[pc],
+                  "total_energy_first": float(tot[0]),
                   "total_energy_last": float(tot[-1]),
                   "max_relative_drift": float(np.max(np.abs(tot - tot[0])) / abs(tot[0])),
                   "gmres_iterations_mean": float(np.mean(its)),
-                  "wall_ms_per_step": wall * 1e3 / args.energy_steps}
+                  "wall_ms_per_step": wall * 1e3 / args.energy_steps,
+                  "cuda_graphs": args.graphs > 0}
+        if training is not None:
+            energy["precond_training"] = training
+            energy["field_solve_jacobi_vs_learned"] = solve_ab
 
     # end to end through the reference-facing C ABI with host FP64 buffers in
     # page-locked memory: per step the host hands in the fields the push and
@@ -753,6 +790,11 @@ def main():
                     help="one full ECSIM step on the GPU and the FP64 oracle (AMR workloads)")
     ap.add_argument("--energy-steps", type=int, default=0,
                     help="also run this many full ECSIM steps and report the energy drift")
+    ap.add_argument("--energy-precond", type=int, default=1, choices=(1, 2),
+                    help="preconditioner of those steps: 1 Jacobi, 2 the learned network "
+                         "(trained first on the run's own Jacobi solves)")
+    ap.add_argument("--train-samples", type=int, default=20000,
+                    help="block pairs harvested for the in-run training (--energy-precond 2)")
     ap.add_argument("--tracer", type=int, default=0,
                     help="also run the cutoff tracing workload with this many particles (FP32; "
                          "FP64 on 1/256 of them)")

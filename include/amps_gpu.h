@@ -241,6 +241,11 @@ amps_gpu_status amps_gpu_set_inner_fp64(amps_gpu_ctx* ctx, int fp64);
  * creation); inference inside the field solve uses each block's own set. */
 amps_gpu_status amps_gpu_precond_num_sets(amps_gpu_ctx* ctx, int* n);
 amps_gpu_status amps_gpu_precond_select(amps_gpu_ctx* ctx, int set);
+/* on != 0: blocks whose halo region reaches a refinement interface (a hanging
+ * corner, or a position with no corner of the block's lattice) use Jacobi
+ * instead of the network, and training skips their samples; *nblocks (may be
+ * NULL) receives their number. */
+amps_gpu_status amps_gpu_precond_interface_jacobi(amps_gpu_ctx* ctx, int on, int* nblocks);
 amps_gpu_status amps_gpu_precond_load(amps_gpu_ctx* ctx, const float* w1, const float* w2,
                                       const float* w3);
 amps_gpu_status amps_gpu_precond_get(amps_gpu_ctx* ctx, float* w1, float* w2, float* w3);
