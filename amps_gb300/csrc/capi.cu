@@ -260,6 +260,7 @@ amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_b
     if (deposit && (s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
     if ((s = check_flags(c, nullptr, nullptr, nullptr))) return s;
   }
+  if (deposit && (s = cuda_check(c, launch_species_moments(c), "species moments"))) return s;
   return AMPS_GPU_OK;
 }
 
@@ -635,12 +636,13 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   staging_free(c);
   precond_free(c->pn);
   c->pn = nullptr;
+  species_free(c);
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   c->graphs.clear();
   cudaFree(c->d_hstage);
   c->d_hstage = nullptr;
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
-                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red,
+                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red, c->d_arn,
                   c->d_Z, c->d_y32,
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
@@ -884,6 +886,7 @@ amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* c, double* particle_
   if ((s = cuda_check(c, launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur), "pack")))
     return s;
   if ((s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+  if ((s = cuda_check(c, launch_species_moments(c), "species moments"))) return s;
   if ((s = cuda_check(c, cudaMemcpyAsync(c->h_energy, c->d_energy, sizeof(double),
                                          cudaMemcpyDeviceToHost, c->stream), "energy")))
     return s;

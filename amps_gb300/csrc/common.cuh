@@ -133,6 +133,7 @@ struct amps_gpu_ctx {
   };
   std::vector<StepGraph> graphs;
   double* d_red = nullptr;      // partial reductions
+  double* d_arn = nullptr;      // per-CTA partial sums of the cooperative Arnoldi step
   double* h_red = nullptr;      // pinned
   int restart = 30;
   int gm_guess[3] = {0, 0, 0};  // per preconditioner: Arnoldi steps of the last first cycle
@@ -171,6 +172,13 @@ struct amps_gpu_ctx {
   float* d_cellJ = nullptr;     // ncor * 24
   double* d_energy = nullptr;   // [0] particle, [1] wave
   double* h_energy = nullptr;   // pinned
+
+  // species moments on corners (species.cu), when sampling is on
+  bool spec_on = false;
+  float* d_cellS = nullptr;     // [ncor][nspec][10][8] per-cell partials
+  double* d_specC = nullptr;    // [10*nspec][nvc] corner values
+  int* d_spec_start = nullptr;  // corner -> (cell*8 + corner-of-cell) CSR
+  int* d_spec_ent = nullptr;
 
   // device staging of host <-> device layout conversions (layout.cu)
   double* d_hstage = nullptr;
@@ -212,6 +220,10 @@ amps_gpu_status layout_cell_moments(amps_gpu_ctx* c, double* hJ, double* hM);
 cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
                             double c_light, long long max_sub);
 cudaError_t launch_deposit(amps_gpu_ctx* c);
+// species moments on corners (species.cu)
+amps_gpu_status species_setup(amps_gpu_ctx* c, bool on);
+void species_free(amps_gpu_ctx* c);
+cudaError_t launch_species_moments(amps_gpu_ctx* c);
 cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
                                const uint8_t* d_spec_in, const double* d_wc, long long n);

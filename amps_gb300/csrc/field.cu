@@ -17,6 +17,7 @@
 //               (the external linear_solver_wrapper of LinearSystemCornerNode.h:3282)
 //   k_update_b  UpdateB (:5160-5711), k_c2n InterpolateB_C2N (:5715),
 //   k_update_e  UpdateE with the wave-energy sum (:5909-6001)
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,12 +27,15 @@
 #include "common.cuh"
 #include "precond.cuh"
 
+namespace cg = cooperative_groups;
+
 namespace {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
 constexpr int kMaxV = 32;
 constexpr int kRedBlocks = 304;  // 2 x 152 SMs
 constexpr int kGmOffset = 10240;  // doubles into d_red (12288 doubles)
+constexpr int kArnMaxGrid = 160;  // CTAs of the cooperative Arnoldi step (>= SMs)
 
 struct Taps {
   double K[3][3][27];  // operator taps without the mass matrix
@@ -399,13 +403,13 @@ __global__ void k_gm_start(GmState* __restrict__ S, const double* __restrict__ n
 
 // Arnoldi column jj: h = h1 + h2 (the two CGS passes), h[jj+1] = ||w||; apply
 // the previous rotations, form rotation jj, update g.  Frozen once done, so
-// steps launched past convergence change nothing the solution uses.
-__global__ void k_gm_step(GmState* __restrict__ S, int jj, const double* __restrict__ h1,
-                          const double* __restrict__ h2, const double* __restrict__ n2) {
-  if (threadIdx.x != 0 || S->done) return;
+// steps launched past convergence change nothing the solution uses.  One thread.
+__device__ void gm_update(GmState* __restrict__ S, int jj, const double* h1, const double* h2,
+                          double n2) {
+  if (S->done) return;
   double* H = S->H;
   for (int i = 0; i <= jj; i++) H[i * kMaxV + jj] = h1[i] + h2[i];
-  const double hn = sqrt(*n2);
+  const double hn = sqrt(n2);
   H[(jj + 1) * kMaxV + jj] = hn;
   for (int i = 0; i < jj; i++) {
     const double a = H[i * kMaxV + jj], b = H[(i + 1) * kMaxV + jj];
@@ -448,6 +452,135 @@ void arnoldi_orth(cudaStream_t s, unsigned gr, long long n, const double* V, dou
   k_orth<NVM, 1><<<gr, 256, 0, s>>>(n, V, w, d_h2, nv, partial);
   k_reduce_partials<<<1, 32, 0, s>>>(partial, gr, 1, d_n2, nullptr);
   k_scale<<<gr, 256, 0, s>>>(n, w, vnext, d_n2);
+}
+
+// One whole Arnoldi step after the operator, in one cooperative launch (one
+// CTA per SM, grid-wide barriers between the phases): CGS2 against V_0..V_nv-1
+// (h1 = V^T w, w -= V h1, h2 = V^T w, w -= V h2), ||w||, V_nv = w / ||w||,
+// and the Givens update of the least-squares state.  Every CTA reduces the
+// per-CTA partial sums of a phase itself (152 rows), so the phases need no
+// further launches; each phase writes its own partial buffer.
+constexpr int kArnThreads = 256;
+
+__device__ __forceinline__ void arn_grid_reduce(const double* __restrict__ part, int nblk, int nv,
+                                                double* __restrict__ s_out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = wid; i < nv; i += kArnThreads / 32) {
+    double t = 0.0;
+    for (int b = lane; b < nblk; b += 32) t += __ldcg(part + (size_t)b * kMaxV + i);
+    t = warp_sum(t);
+    if (lane == 0) s_out[i] = t;
+  }
+  __syncthreads();
+}
+
+template <int NVM>
+__device__ __forceinline__ void arn_block_store(const double (&acc)[NVM], int nv, double* __restrict__ row,
+                                                double* __restrict__ s_red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NVM; i++) {
+    if (i < nv) {
+      const double v = warp_sum(acc[i]);
+      if (lane == 0) s_red[wid * kMaxV + i] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0.0;
+    for (int w = 0; w < kArnThreads / 32; w++) t += s_red[w * kMaxV + threadIdx.x];
+    row[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+template <int NVM>
+__global__ void __launch_bounds__(kArnThreads, 1) k_arnoldi(long long n, const double* __restrict__ V,
+                                                          double* __restrict__ w, int nv,
+                                                          double* __restrict__ vnext,
+                                                          double* __restrict__ part, GmState* gs,
+                                                          int jj) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double s_red[(kArnThreads / 32) * kMaxV];
+  __shared__ double s_h1[kMaxV], s_h2[kMaxV], s_n2[1];
+  const int nblk = gridDim.x;
+  double* pA = part;
+  double* pB = part + (size_t)nblk * kMaxV;
+  double* pC = pB + (size_t)nblk * kMaxV;
+  const long long stride = (long long)nblk * kArnThreads;
+  const long long t0 = (long long)blockIdx.x * kArnThreads + threadIdx.x;
+  double acc[NVM];
+  // pass 1: h1 = V^T w
+#pragma unroll
+  for (int i = 0; i < NVM; i++) acc[i] = 0.0;
+  for (long long t = t0; t < n; t += stride) {
+    const double wt = w[t];
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) acc[i] = fma(V[(size_t)i * n + t], wt, acc[i]);
+  }
+  arn_block_store<NVM>(acc, nv, pA + (size_t)blockIdx.x * kMaxV, s_red);
+  grid.sync();
+  arn_grid_reduce(pA, nblk, nv, s_h1);
+  // pass 2: w -= V h1; h2 = V^T w
+#pragma unroll
+  for (int i = 0; i < NVM; i++) acc[i] = 0.0;
+  for (long long t = t0; t < n; t += stride) {
+    double vv[NVM];
+    double wt = w[t];
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        vv[i] = V[(size_t)i * n + t];
+        wt = fma(-s_h1[i], vv[i], wt);
+      }
+    w[t] = wt;
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) acc[i] = fma(vv[i], wt, acc[i]);
+  }
+  arn_block_store<NVM>(acc, nv, pB + (size_t)blockIdx.x * kMaxV, s_red);
+  grid.sync();
+  arn_grid_reduce(pB, nblk, nv, s_h2);
+  // pass 3: w -= V h2; ||w||^2
+  double nacc[1] = {0.0};
+  for (long long t = t0; t < n; t += stride) {
+    double wt = w[t];
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) wt = fma(-s_h2[i], V[(size_t)i * n + t], wt);
+    w[t] = wt;
+    nacc[0] = fma(wt, wt, nacc[0]);
+  }
+  arn_block_store<1>(nacc, 1, pC + (size_t)blockIdx.x * kMaxV, s_red);
+  grid.sync();
+  arn_grid_reduce(pC, nblk, 1, s_n2);
+  // V_nv = w / ||w|| (the elements this thread wrote in pass 3)
+  const double inv = s_n2[0] > 0.0 ? 1.0 / sqrt(s_n2[0]) : 0.0;
+  for (long long t = t0; t < n; t += stride) vnext[t] = w[t] * inv;
+  if (blockIdx.x == 0 && threadIdx.x == 0) gm_update(gs, jj, s_h1, s_h2, s_n2[0]);
+}
+
+// cooperative grid of k_arnoldi<NVM>: one CTA per SM (at most kArnMaxGrid)
+template <int NVM>
+cudaError_t launch_arnoldi(cudaStream_t s, long long n, const double* V, double* w, int nv,
+                           double* vnext, double* part, GmState* gs, int jj) {
+  static int grid[64] = {0};  // per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (grid[dev] == 0) {
+    int sms = 0, per = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_arnoldi<NVM>, kArnThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorLaunchOutOfResources;
+    grid[dev] = std::min(sms, kArnMaxGrid);
+  }
+  const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(grid[dev], (n + kArnThreads - 1) / kArnThreads));
+  void* args[] = {&n, &V, &w, &nv, &vnext, &part, &gs, &jj};
+  return cudaLaunchCooperativeKernel((const void*)k_arnoldi<NVM>, dim3(g), dim3(kArnThreads), args, 0, s);
 }
 
 // ---- field updates -----------------------------------------------------------
@@ -630,10 +763,12 @@ cudaError_t launch_update_e(amps_gpu_ctx* c) {
 // ends when the FP64 residual satisfies ||b - A x|| <= tol ||b||.  The
 // preconditioner is none (precond 0), Jacobi (1, z = D v) or the learned block
 // network (2, z = D v + N(D v); flexible form: the directions z_j are kept).
-// The host does not wait for each step: it queues as many Arnoldi steps as the
-// last cycle took before it first reads the device's convergence flag, then
-// one step per read; steps queued past convergence leave the least-squares
-// state untouched (k_gm_step is frozen), so they cost time but not accuracy.
+// Each Arnoldi step is the operator plus one cooperative kernel (k_arnoldi:
+// CGS2, normalisation and the Givens update).  The host does not wait for each
+// step: it queues as many Arnoldi steps as the last cycle took before it first
+// reads the device's convergence flag, then one step per read; steps queued
+// past convergence leave the least-squares state untouched (gm_update is
+// frozen), so they cost time but not accuracy.
 // Device scratch layout of d_red: [0, kRedBlocks*kMaxV) partials, then h1
 // (kMaxV), h2 (kMaxV), nrm2 (8), y (kMaxV); GmState at kGmOffset.
 amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
@@ -641,9 +776,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   const long long n = 3 * c->nvc;
   const int m = std::min(c->restart, kMaxV);
   double* partial = c->d_red;
-  double* d_h1 = c->d_red + kRedBlocks * kMaxV;
-  double* d_h2 = d_h1 + kMaxV;
-  double* d_n2 = d_h2 + kMaxV;
+  double* d_n2 = c->d_red + kRedBlocks * kMaxV + 2 * kMaxV;
   GmState* gs = reinterpret_cast<GmState*>(c->d_red + kGmOffset);
   const unsigned gr = gridr(n, c->tune_red, c->tune_ept);
   cudaStream_t s = c->stream;
@@ -654,6 +787,8 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     if (e != cudaSuccess) return cuda_check(c, e, #x);          \
   } while (0)
 
+  if (!c->d_arn)
+    CK(cudaMalloc(reinterpret_cast<void**>(&c->d_arn), sizeof(double) * 3 * kArnMaxGrid * kMaxV));
   const double* dinv = nullptr;
   if (precond >= 1) {
     CK(launch_jacobi_diag(c));
@@ -717,18 +852,18 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
         if (precond == 1 && c->pn) CK(precond_harvest_pairs(c, w, vj, 1));
       }
       {
-        TimedLaunch t(c, "gmres_orth", 7);
+        TimedLaunch t(c, "gmres_orth");
         double* vnext = V + (size_t)nv * n;
         if (nv <= 4)
-          arnoldi_orth<4>(s, gr, n, V, w, nv, partial, d_h1, d_h2, d_n2, vnext);
+          e = launch_arnoldi<4>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
         else if (nv <= 8)
-          arnoldi_orth<8>(s, gr, n, V, w, nv, partial, d_h1, d_h2, d_n2, vnext);
+          e = launch_arnoldi<8>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
         else if (nv <= 16)
-          arnoldi_orth<16>(s, gr, n, V, w, nv, partial, d_h1, d_h2, d_n2, vnext);
+          e = launch_arnoldi<16>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
         else
-          arnoldi_orth<32>(s, gr, n, V, w, nv, partial, d_h1, d_h2, d_n2, vnext);
+          e = launch_arnoldi<32>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
+        if (e != cudaSuccess) return cuda_check(c, e, "arnoldi step");
       }
-      k_gm_step<<<1, 32, 0, s>>>(gs, jj, d_h1, d_h2, d_n2);
       CK(cudaGetLastError());
       if (launched >= first_read || launched == m || it + launched >= maxit) {
         CK(cudaMemcpyAsync(c->h_red, &gs->jj, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -1,0 +1,259 @@
+// Species moments on corners: the _PIC_FIELD_SOLVER_SAMPLE_SPECIES_ON_CORNER_
+// sampling of ProcessCell (src/pic/pic_field_solver_ecsim.cpp:2270-2303, flush
+// :2384-2394): per particle of species s and corner c of its cell, with
+// t = m_s W wcorr w_c, the ten sums rho = t, rho u = t v, rho u u = t v v
+// (xx, yy, zz, xy, yz, xz), divided by the cell volume and summed on the
+// corner.  Values are those of the particles after the step (the reference
+// samples inside UpdateJMassMatrix, after the mover).
+//
+//   k_species_cells   one warp per cell, one pass per species present: every
+//                     lane accumulates the 8 x 10 products of its particles
+//                     in registers (FP32), the warp adds its 32 rows through
+//                     shared memory; per-cell partials cellS[cell][s][10][8]
+//   k_species_gather  FP64 corner sums over the cells that have the corner
+//                     (a CSR built once per mesh), times 1 / cell volume;
+//                     component-major out[(10 s + q) * ncorners + corner]
+//
+// Runs after the deposition when sampling is on (amps_gpu_set_species_moments);
+// costs one more read of the particle state.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "deposit_core.cuh"
+
+namespace {
+
+constexpr int kQ = 10;            // quantities per species (Rho_ .. RhoUxUz_)
+constexpr int kV = 8 * kQ;        // values per species per cell
+constexpr int kWarpsS = 4;        // 41.5 KB of static shared memory per CTA
+constexpr int kRow = kV + 1;      // shared row stride (conflict-free columns)
+
+struct SpecArgs {
+  const float* u[3];
+  const float* v[3];
+  const uint8_t* sp;
+  const float* wc;                // may be null
+  const int* base;
+  const int* cnt;
+  long long ncell;
+  int nspec;
+  float mw[AMPS_GPU_MAX_SPECIES]; // m * W per species
+  float* cellS;                   // [ncell][nspec][kQ][8]
+};
+
+__global__ void __launch_bounds__(kWarpsS * 32) k_species_cells(SpecArgs a) {
+  __shared__ float red[kWarpsS][32 * kRow];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float* row = red[wid];
+  const long long nw = (long long)gridDim.x * kWarpsS;
+  for (long long cid = (long long)blockIdx.x * kWarpsS + wid; cid < a.ncell; cid += nw) {
+    const int b0 = a.base[cid], n = a.cnt[cid];
+    const int l = (int)(cid % AMPS_CPB);
+    const float ci[3] = {(float)(l & 7), (float)((l >> 3) & 7), (float)(l >> 6)};
+    unsigned present = 0;
+    for (int q0 = lane; q0 < n; q0 += 32) present |= 1u << a.sp[b0 + q0];
+    present = __reduce_or_sync(0xffffffffu, present);
+    float* out = a.cellS + (size_t)cid * a.nspec * kV;
+    for (int s = 0; s < a.nspec; s++) {
+      if (!((present >> s) & 1u)) {
+        for (int t = lane; t < kV; t += 32) out[s * kV + t] = 0.f;
+        continue;
+      }
+      float acc[kV];
+#pragma unroll
+      for (int t = 0; t < kV; t++) acc[t] = 0.f;
+      for (int q0 = lane; q0 < n; q0 += 32) {
+        const int p = b0 + q0;
+        if (a.sp[p] != s) continue;
+        float f[3], vv[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          f[d] = a.u[d][p] - ci[d];
+          vv[d] = a.v[d][p];
+        }
+        const float m = a.mw[s] * (a.wc ? a.wc[p] : 1.0f);
+        const float val[kQ] = {m,
+                               m * vv[0],
+                               m * vv[1],
+                               m * vv[2],
+                               m * vv[0] * vv[0],
+                               m * vv[1] * vv[1],
+                               m * vv[2] * vv[2],
+                               m * vv[0] * vv[1],
+                               m * vv[1] * vv[2],
+                               m * vv[0] * vv[2]};
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          const float w = ((c & 1) ? f[0] : 1.f - f[0]) * ((c & 2) ? f[1] : 1.f - f[1]) *
+                          ((c & 4) ? f[2] : 1.f - f[2]);
+#pragma unroll
+          for (int q = 0; q < kQ; q++) acc[q * 8 + c] = fmaf(w, val[q], acc[q * 8 + c]);
+        }
+      }
+      // column sums of the warp's 32 rows
+#pragma unroll
+      for (int t = 0; t < kV; t++) row[lane * kRow + t] = acc[t];
+      __syncwarp();
+      for (int t = lane; t < kV; t += 32) {
+        float sum = 0.f;
+        for (int r = 0; r < 32; r++) sum += row[r * kRow + t];
+        out[s * kV + t] = sum;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// out[(10 s + q) * nvc + corner] = sum over entries (cell, c) of the corner of
+// cellS[cell][s][q][c] / V(cell)
+__global__ void __launch_bounds__(256) k_species_gather(long long nvc, int nspec,
+                                                        const int* __restrict__ start,
+                                                        const int* __restrict__ ent,
+                                                        const float* __restrict__ cellS,
+                                                        const double* __restrict__ bdx,
+                                                        double inv_vol, double* __restrict__ out) {
+  const long long total = nvc * nspec * kQ;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long cc = t % nvc;
+    const int k = (int)(t / nvc);  // 10 s + q
+    double sum = 0.0;
+    for (int e = start[cc]; e < start[cc + 1]; e++) {
+      const int en = ent[e];
+      const long long cell = en >> 3;
+      const int c = en & 7;
+      double iv = inv_vol;
+      if (bdx) {
+        const double dx = bdx[cell / AMPS_CPB];
+        iv = 1.0 / (dx * dx * dx);
+      }
+      sum += (double)cellS[(size_t)cell * nspec * kV + (size_t)k * 8 + c] * iv;
+    }
+    out[t] = sum;
+  }
+}
+
+}  // namespace
+
+// Corner -> (cell, corner-of-cell) lists.  Corner (i, j, k) of block b's cell
+// grid (0..8 per axis) is the uniform lattice corner there (periodic), or the
+// AMR mesh's unique corner from the block's corner table.
+amps_gpu_status species_setup(amps_gpu_ctx* c, bool on) {
+  if (!on) {
+    c->spec_on = false;
+    return AMPS_GPU_OK;
+  }
+  if (!c->d_cellS) {
+    const long long nv = c->nvc;
+    std::vector<int> ctab;
+    if (c->amr) {
+      ctab.resize((size_t)c->nb * 729);
+      cudaError_t e = cudaMemcpy(ctab.data(), c->d_ctab, sizeof(int) * ctab.size(), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_check(c, e, "species moments: corner table");
+    }
+    const int nbx = c->cfg.nbx, nby = c->cfg.nby, nbz = c->cfg.nbz;
+    const int NX = 8 * nbx, NY = 8 * nby, NZ = 8 * nbz;
+    auto corner = [&](int b, int ci, int cj, int ck) -> int {
+      if (c->amr) return ctab[(size_t)b * 729 + ci + 9 * (cj + 9 * ck)];
+      const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+      const int I = (8 * bx + ci) % NX, J = (8 * by + cj) % NY, K = (8 * bz + ck) % NZ;
+      return ((I >> 3) + nbx * ((J >> 3) + nby * (K >> 3))) * AMPS_CPB + (I & 7) + 8 * ((J & 7) + 8 * (K & 7));
+    };
+    std::vector<int> count((size_t)nv + 1, 0);
+    for (int b = 0; b < c->nb; b++)
+      for (int l = 0; l < AMPS_CPB; l++)
+        for (int q = 0; q < 8; q++)
+          count[(size_t)corner(b, (l & 7) + (q & 1), ((l >> 3) & 7) + ((q >> 1) & 1), (l >> 6) + (q >> 2)) + 1]++;
+    for (long long i = 0; i < nv; i++) count[(size_t)i + 1] += count[(size_t)i];
+    std::vector<int> ent((size_t)count[(size_t)nv]), fill(count.begin(), count.end() - 1);
+    for (int b = 0; b < c->nb; b++)
+      for (int l = 0; l < AMPS_CPB; l++)
+        for (int q = 0; q < 8; q++) {
+          const int cc = corner(b, (l & 7) + (q & 1), ((l >> 3) & 7) + ((q >> 1) & 1), (l >> 6) + (q >> 2));
+          ent[(size_t)fill[(size_t)cc]++] = (int)(((long long)b * AMPS_CPB + l) * 8 + q);
+        }
+    bool ok = cudaMalloc(reinterpret_cast<void**>(&c->d_cellS),
+                         sizeof(float) * (size_t)c->ncor * c->cfg.nspec * kV) == cudaSuccess &&
+              cudaMalloc(reinterpret_cast<void**>(&c->d_specC),
+                         sizeof(double) * (size_t)nv * c->cfg.nspec * kQ) == cudaSuccess &&
+              cudaMalloc(reinterpret_cast<void**>(&c->d_spec_start), sizeof(int) * count.size()) == cudaSuccess &&
+              cudaMalloc(reinterpret_cast<void**>(&c->d_spec_ent), sizeof(int) * std::max<size_t>(ent.size(), 1)) == cudaSuccess;
+    ok = ok && cudaMemcpy(c->d_spec_start, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(c->d_spec_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(c->d_specC, 0, sizeof(double) * (size_t)nv * c->cfg.nspec * kQ) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      species_free(c);
+      return set_err(c, AMPS_GPU_CUDA_ERROR, "species moments: allocation failed");
+    }
+  }
+  c->spec_on = true;
+  return AMPS_GPU_OK;
+}
+
+void species_free(amps_gpu_ctx* c) {
+  cudaFree(c->d_cellS);
+  cudaFree(c->d_specC);
+  cudaFree(c->d_spec_start);
+  cudaFree(c->d_spec_ent);
+  c->d_cellS = nullptr;
+  c->d_specC = nullptr;
+  c->d_spec_start = c->d_spec_ent = nullptr;
+  c->spec_on = false;
+}
+
+cudaError_t launch_species_moments(amps_gpu_ctx* c) {
+  if (!c->spec_on) return cudaSuccess;
+  SpecArgs a{};
+  for (int d = 0; d < 3; d++) {
+    a.u[d] = c->d_u[c->cur][d];
+    a.v[d] = c->d_v[c->cur][d];
+  }
+  a.sp = c->d_sp[c->cur];
+  a.wc = c->has_wcorr ? c->d_wc[c->cur] : nullptr;
+  a.base = c->d_base;
+  a.cnt = c->d_cnt;
+  a.ncell = c->ncor;
+  a.nspec = c->cfg.nspec;
+  for (int s = 0; s < c->cfg.nspec; s++) a.mw[s] = (float)(c->cfg.mass[s] * c->cfg.weight[s]);
+  a.cellS = c->d_cellS;
+  {
+    TimedLaunch t(c, "species_cells");
+    const long long blocks = std::min<long long>((c->ncor + kWarpsS - 1) / kWarpsS, 152LL * 16);
+    k_species_cells<<<(unsigned)blocks, kWarpsS * 32, 0, c->stream>>>(a);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  {
+    TimedLaunch t(c, "species_gather");
+    const double V = c->cfg.dx[0] * c->cfg.dx[1] * c->cfg.dx[2];
+    const long long total = c->nvc * c->cfg.nspec * kQ;
+    const long long blocks = std::min<long long>((total + 255) / 256, 152LL * 32);
+    k_species_gather<<<(unsigned)blocks, 256, 0, c->stream>>>(
+        c->nvc, c->cfg.nspec, c->d_spec_start, c->d_spec_ent, c->d_cellS,
+        c->amr ? c->d_bdx : nullptr, 1.0 / V, c->d_specC);
+  }
+  return cudaGetLastError();
+}
+
+extern "C" {
+
+amps_gpu_status amps_gpu_set_species_moments(amps_gpu_ctx* c, int on) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  cudaStreamSynchronize(c->stream);
+  return species_setup(c, on != 0);
+}
+
+amps_gpu_status amps_gpu_export_species_moments(amps_gpu_ctx* c, double* out) {
+  if (!c || !out) return set_err(c, AMPS_GPU_INVALID_ARG, "export_species_moments: null output");
+  if (!c->d_specC)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "export_species_moments: sampling was never switched on");
+  cudaSetDevice(c->cfg.device);
+  return layout_download(c, c->d_specC, out, c->nvc, c->cfg.nspec * kQ, false);
+}
+
+}  // extern "C"

@@ -288,6 +288,21 @@ class EcsimContext:
                                                      ptr(M, C.c_double)), "export_moments")
         return J, M
 
+    def set_species_moments(self, on=True):
+        """Sample rho, rho u, rho u u per species on the corners at every deposition."""
+        self._check(self.lib.amps_gpu_set_species_moments(self.h, 1 if on else 0),
+                    "set_species_moments")
+
+    def export_species_moments(self, out=None):
+        """(ncorners, nspec, 10): Rho, RhoUx, RhoUy, RhoUz, RhoUxUx, RhoUyUy,
+        RhoUzUz, RhoUxUy, RhoUyUz, RhoUxUz per species and corner"""
+        ns = self.cfg.nspec
+        if out is None:
+            out = np.empty((self.ncorners, ns, 10))
+        self._check(self.lib.amps_gpu_export_species_moments(self.h, ptr(out, C.c_double)),
+                    "export_species_moments")
+        return out
+
     def export_cell_moments(self, with_m=True, out=None):
         """per-cell ProcessCell partials (cells in block order): cellJ (ncells, 24),
         cellM (ncells, 324) or None; out=(J, M) reuses arrays"""

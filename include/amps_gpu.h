@@ -214,6 +214,17 @@ amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* ctx, double tol, int maxit, i
  * (the reference's first-call branch, pic_field_solver_ecsim.cpp:6209). */
 amps_gpu_status amps_gpu_step(amps_gpu_ctx* ctx, double tol, int maxit, int precond,
                               amps_gpu_step_stats* stats);
+/* Species moments on corners (_PIC_FIELD_SOLVER_SAMPLE_SPECIES_ON_CORNER_,
+ * ProcessCell pic_field_solver_ecsim.cpp:2270-2303): with sampling on, every
+ * deposition (update_j_mass_matrix, push_deposit, step) also forms per corner
+ * and species rho, rho u (3), rho u u (xx, yy, zz, xy, yz, xz) of the
+ * particles after the step, each cell's sums divided by its volume (the
+ * SpecData flush :2384-2394).  Export: out[corner][10*nspec] in the
+ * reference's Rho_ .. RhoUxUz_ order, corners in the fields' corner order (on
+ * AMR meshes hanging corners carry the sums of the fine cells that have them
+ * as a corner). */
+amps_gpu_status amps_gpu_set_species_moments(amps_gpu_ctx* ctx, int on);
+amps_gpu_status amps_gpu_export_species_moments(amps_gpu_ctx* ctx, double* out);
 /* Particle push + re-bin + deposit only (the particle-steps/s hot path). */
 amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* ctx, double* particle_energy);
 /* GMRES inner operator precision: 0 FP32 arithmetic with FP64 refinement at

@@ -427,6 +427,48 @@ double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
   return energy;
 }
 
+/* Species moments on corners (_PIC_FIELD_SOLVER_SAMPLE_SPECIES_ON_CORNER_,
+ * ProcessCell pic_field_solver_ecsim.cpp:2270-2303 and the flush :2384-2394):
+ * per particle and corner t = m W w_c, the ten sums rho, rho u (3),
+ * rho u u (xx, yy, zz, xy, yz, xz) of its species, divided by the cell volume;
+ * out[corner*10*nspec + 10*spec + q] (Rho_ .. RhoUxUz_ order, :138-147). */
+void orc_species_moments(const orc_mesh* g, long n, const double* x, const double* v,
+                         const uint8_t* spec, const double* wcorr, const int32_t* block,
+                         const int32_t* cell, double* out) {
+  const long ncor = (long)NC * NC * NC * g->nbx * g->nby * g->nbz;
+  const int nq = 10 * g->nspec;
+  const double V = g->dx[0] * g->dx[1] * g->dx[2];
+  memset(out, 0, sizeof(double) * ncor * nq);
+  for (long p = 0; p < n; p++) {
+    int bxyz[3], iX[3], nd[8][3];
+    double xmin[3], xI[3], wt[8], wn[8];
+    block_geom(g, block[p], bxyz, xmin);
+    for (int d = 0; d < 3; d++) xI[d] = x[3 * p + d];
+    corner_stencil(xmin, g->dx, xI, wt, wn, nd, iX);
+    (void)cell;
+    const int sp = spec[p];
+    const double mass = g->m[sp] * g->w[sp] * (wcorr ? wcorr[p] : 1.0);
+    const double* u = v + 3 * p;
+    for (int c = 0; c < 8; c++) {
+      const long cor = cidx(g, bxyz[0] * NC + iX[0] + kCornerOff[c][0],
+                            bxyz[1] * NC + iX[1] + kCornerOff[c][1],
+                            bxyz[2] * NC + iX[2] + kCornerOff[c][2]);
+      const double t = mass * wt[c], t0 = t * u[0], t1 = t * u[1], t2 = t * u[2];
+      double* o = out + cor * nq + 10 * sp;
+      o[0] += t / V;
+      o[1] += t0 / V;
+      o[2] += t1 / V;
+      o[3] += t2 / V;
+      o[4] += t0 * u[0] / V;
+      o[5] += t1 * u[1] / V;
+      o[6] += t2 * u[2] / V;
+      o[7] += t0 * u[1] / V;
+      o[8] += t1 * u[2] / V;
+      o[9] += t0 * u[2] / V;
+    }
+  }
+}
+
 /* InterpolateB_C2N (pic_field_solver_ecsim.cpp:5715-5775) */
 void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor) {
   const int NX = NC * g->nbx, NY = NC * g->nby, NZ = NC * g->nbz;

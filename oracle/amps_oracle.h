@@ -64,6 +64,10 @@ void orc_locate(const orc_mesh* g, long n, const double* x, int32_t* block, int3
 
 /* ---- field solve ---- */
 void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor);
+/* species moments on corners (ProcessCell :2270-2303): out[corner][10*nspec] */
+void orc_species_moments(const orc_mesh* g, long n, const double* x, const double* v,
+                         const uint8_t* spec, const double* wcorr, const int32_t* block,
+                         const int32_t* cell, double* out);
 void orc_rhs(const orc_mesh* g, const double* E_n, const double* Bcen, const double* J,
              const double* M, double* rhs);
 void orc_matvec(const orc_mesh* g, const double* M, const double* x, double* y);

@@ -211,6 +211,41 @@ double orc_amr_deposit(const orc_amr* g, long n, const double* x, const double* 
   return energy;
 }
 
+/* Species moments on corners (ProcessCell pic_field_solver_ecsim.cpp:2270-2303,
+ * flush :2384-2394) with each cell's own volume, summed on the unique corners
+ * of the cell (a hanging corner collects the cells of the fine blocks that
+ * have it as a corner): out[corner*10*nspec + 10*spec + q]. */
+void orc_amr_species_moments(const orc_amr* g, long n, const double* x, const double* v,
+                             const uint8_t* spec, const double* wcorr, const int32_t* block,
+                             double* out) {
+  const int nq = 10 * g->nspec;
+  memset(out, 0, sizeof(double) * (size_t)g->ncorners * nq);
+  for (long p = 0; p < n; p++) {
+    double w[8];
+    int cid[8];
+    const int b = block[p];
+    stencil(g, b, x + 3 * p, w, cid);
+    const double dx = bdx(g, b), V = dx * dx * dx;
+    const int s = spec[p];
+    const double mass = g->m[s] * g->w[s] * (wcorr ? wcorr[p] : 1.0);
+    const double* u = v + 3 * p;
+    for (int c = 0; c < 8; c++) {
+      const double t = mass * w[c], t0 = t * u[0], t1 = t * u[1], t2 = t * u[2];
+      double* o = out + (size_t)cid[c] * nq + 10 * s;
+      o[0] += t / V;
+      o[1] += t0 / V;
+      o[2] += t1 / V;
+      o[3] += t2 / V;
+      o[4] += t0 * u[0] / V;
+      o[5] += t1 * u[1] / V;
+      o[6] += t2 * u[2] / V;
+      o[7] += t0 * u[1] / V;
+      o[8] += t1 * u[2] / V;
+      o[9] += t0 * u[2] / V;
+    }
+  }
+}
+
 /* curl of the cell from its 8 corner values (table order): C x */
 static void cell_curl(const double e[8][3], double dx, double out[3]) {
   double dEz_dy = 0, dEy_dz = 0, dEx_dz = 0, dEz_dx = 0, dEy_dx = 0, dEx_dy = 0;

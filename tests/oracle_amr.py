@@ -33,6 +33,7 @@ def lib():
             "orc_amr_deposit": (C.c_double, [C.POINTER(Amr), C.c_long, D, D, U8, D, I32, I32, D,
                                              D, D]),
             "orc_amr_apply": (None, [C.POINTER(Amr), D, D, D, C.c_int, C.c_int, C.c_int]),
+            "orc_amr_species_moments": (None, [C.POINTER(Amr), C.c_long, D, D, U8, D, I32, D]),
             "orc_amr_rhs": (None, [C.POINTER(Amr), D, D, D, D, D]),
             "orc_amr_gmres": (C.c_int, [C.POINTER(Amr), D, D, D, C.c_double, C.c_int, C.c_int, D]),
             "orc_amr_update_b": (None, [C.POINTER(Amr), D, D, D]),
@@ -103,6 +104,14 @@ class AmrOracle:
                                       p(self.spec, C.c_uint8), p(self.wcorr),
                                       p(self.block, C.c_int32), p(self.cell, C.c_int32),
                                       p(self.Bcur), p(self.cellJ), p(self.cellM))
+
+    def species_moments(self):
+        """(ncorners, nspec, 10) corner species moments of the current particles"""
+        out = np.zeros((self.mesh.ncorners, self.g.nspec, 10))
+        self.L.orc_amr_species_moments(C.byref(self.g), len(self.spec), p(self.x), p(self.v),
+                                       p(self.spec, C.c_uint8), p(self.wcorr),
+                                       p(self.block, C.c_int32), p(out))
+        return out
 
     def push(self):
         return self.L.orc_amr_push(C.byref(self.g), len(self.spec), p(self.x), p(self.v),

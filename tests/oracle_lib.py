@@ -45,6 +45,7 @@ def load():
                                     C.c_double, C.c_double]),
         "orc_deposit": (C.c_double, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D]),
         "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
+        "orc_species_moments": (None, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D]),
         "orc_center_to_corner": (None, [C.POINTER(Mesh), D, D]),
         "orc_rhs": (None, [C.POINTER(Mesh), D, D, D, D, D]),
         "orc_matvec": (None, [C.POINTER(Mesh), D, D, D]),
@@ -111,6 +112,15 @@ class OracleState:
         self.Bcur = np.ascontiguousarray(fields["B_corner_cur"], np.float64).copy()
         self.J = np.zeros((nc, 3))
         self.M = np.zeros((nc, 243))
+
+    def species_moments(self):
+        """(ncorners, nspec, 10) corner species moments of the current particles"""
+        ns = self.m.nspec
+        out = np.zeros((self.wl.mesh.ncells, ns, 10))
+        self.lib.orc_species_moments(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
+                                     p(self.spec, C.c_uint8), p(self.wcorr),
+                                     p(self.block, C.c_int32), p(self.cell, C.c_int32), p(out))
+        return out
 
     def relboris(self, dt_total, c_light=1.0):
         """Mover::Relativistic::Boris on E^n and the corner B cur slot"""
