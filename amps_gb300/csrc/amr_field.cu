@@ -98,12 +98,35 @@ __device__ __forceinline__ void cell_curl_t(const T y[3], T s, T out[8][3]) {
   }
 }
 
+// out[k] += component p of s C^T y on the 8 corners
 template <typename T>
-__device__ __forceinline__ T from_f32(float v);
-template <>
-__device__ __forceinline__ double from_f32<double>(float v) { return widen(v); }
-template <>
-__device__ __forceinline__ float from_f32<float>(float v) { return v; }
+__device__ __forceinline__ void cell_curl_t_row(const T y[3], T s, int p, T out[8]) {
+  const T a0 = s * y[0], a1 = s * y[1], a2 = s * y[2];
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    const bool px = k == 1 || k == 2 || k == 5 || k == 6;
+    const bool py = k == 2 || k == 3 || k == 6 || k == 7;
+    const bool pz = k >= 4;
+    if (p == 0) out[k] += (pz ? a1 : -a1) - (py ? a2 : -a2);
+    else if (p == 1) out[k] += (px ? a2 : -a2) - (pz ? a0 : -a0);
+    else out[k] += (py ? a0 : -a0) - (px ? a1 : -a1);
+  }
+}
+
+// scatter component p of out[8] to the cell's corners with P^T
+template <typename T>
+__device__ __forceinline__ void scatter_row(T* __restrict__ y, long long nvc, const int cid[8], int p,
+                                            const T out[8], const Hang& h) {
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int cc = cid[c], s = h.hs[cc], e = h.hs[cc + 1];
+    if (s == e) {
+      atomicAdd(y + p * nvc + cc, out[c]);
+    } else {
+      for (int t = s; t < e; t++) atomicAdd(y + p * nvc + h.hp[t], (T)h.hw[t] * out[c]);
+    }
+  }
+}
 
 struct ApplyArgs {
   long long ncell, nvc;
@@ -116,74 +139,143 @@ struct ApplyArgs {
   const double* dinv;  // optional right preconditioner
   const double* Bcen;  // RHS: centre B (component-major over cells)
   double th2dt2, f, thdt;
-  int with_identity, with_curl, with_mass, rhs_mode;
+  unsigned long long* flags;  // [2]: bounded-wait timeouts
 };
 
-// y += cell contributions in precision T (FP64: outer residuals and RHS;
-// FP32: inner GMRES operator).  rhs_mode: y = -(curl-curl + M) x
-// + theta dt C^T B - f J.
-template <typename T>
-__global__ void __launch_bounds__(256) k_amr_cell_op(ApplyArgs a, T* __restrict__ y) {
-  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= a.ncell) return;
+// ---------------------------------------------------------------------------
+// The operator per cell (weak form, see above), y += its contributions.  A CTA
+// serves 32 cells with 3 threads each (one per output component p; warp p
+// takes the 32 cells): the cells' run of partials (31,104 contiguous bytes) is
+// brought into shared memory by one bulk copy while the threads gather the
+// corner values (each value once, shared through shared memory), and each
+// thread reads the rows 3p..3p+2 of its cell's 27 monomial blocks from there
+// (stride 243 words between a warp's cells: conflict-free).
+//   ACC 0: FP32 inner operator (curl-curl + mass; identity added in FP64 by
+//          k_amr_finish32), FP32 atomics;
+//   ACC 1: the full operator to FP64 accuracy (outer residuals);
+//   ACC 2: the RHS to FP64 accuracy.
+// ACC 1/2 keep the identity and curl terms in FP64 and evaluate the mass term
+// (most of the arithmetic) in FP32 pairs (FF, common.cuh).
+constexpr int kTileCells = 32;
+constexpr int kTileThreads = 3 * kTileCells;
+constexpr uint32_t kTileBytes = kTileCells * AMPS_CELLM * 4;  // 31,104
+
+template <int ACC>
+__global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, float* __restrict__ y32,
+                                                               double* __restrict__ y64) {
+  extern __shared__ __align__(16) float s_m[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ int s_cid[kTileCells][8];
+  __shared__ double s_e[kTileCells][24];  // 8 corners x 3
+  const int tid = threadIdx.x, p = tid / kTileCells, lc = tid % kTileCells;
+  const long long cell0 = (long long)blockIdx.x * kTileCells;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bar, kTileBytes);
+    bulk_copy_g2s(s_m, a.cellM + cell0 * AMPS_CELLM, kTileBytes, &bar);
+  }
+  const long long cell = cell0 + lc;
   const int b = (int)(cell >> 9), l = (int)(cell & 511);
   const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
-  const double dxd = a.bdx[b];
-  const T dx = (T)dxd, V = (T)(dxd * dxd * dxd);
+  const double dxd = a.bdx[b], Vd = dxd * dxd * dxd;
+  // the cell's corners and their values, each gathered once by one of its 3
+  // threads (thread p: corner ids c = p, p+3, p+6; values of component p)
+  for (int c = p; c < 8; c += 3)
+    s_cid[lc][c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+  __syncthreads();
   int cid[8];
-  T e[8][3], out[8][3];
 #pragma unroll
   for (int c = 0; c < 8; c++) {
-    cid[c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+    cid[c] = s_cid[lc][c];
+    s_e[lc][3 * c + p] = cval(a.x, a.dinv, a.nvc, cid[c], p, a.h);
+  }
+  const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
+  __syncthreads();
+  if (!ok) {
+    atomicAdd(a.flags + 2, 1ull);
+    mbar_wait_bounded(&bar, 0, kWaitLimit);  // let the copy land before exiting
+    return;
+  }
+  double e[8][3];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      e[c][d] = (T)cval(a.x, a.dinv, a.nvc, cid[c], d, a.h);
-      out[c][d] = (T)0;
+  for (int c = 0; c < 8; c++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) e[c][d] = s_e[lc][3 * c + d];
+  const float* mm = s_m + lc * AMPS_CELLM + 3 * p;  // row p of every monomial block
+  if (ACC == 0) {
+    const float dx = (float)dxd, V = (float)Vd;
+    float ef[8][3], out[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      out[c] = 0.f;
+#pragma unroll
+      for (int d = 0; d < 3; d++) ef[c][d] = (float)e[c][d];
     }
-  }
-  const T sg = a.rhs_mode ? (T)-1 : (T)1;
-  if (a.with_identity) {
-    const T v8 = (T)0.125 * V;
-#pragma unroll
-    for (int c = 0; c < 8; c++)
-#pragma unroll
-      for (int d = 0; d < 3; d++) out[c][d] += v8 * e[c][d];
-  }
-  if (a.with_curl) {
-    T cu[3];
-    cell_curl<T>(e, (T)0.25 / dx, cu);
-    cell_curl_t<T>(cu, sg * (T)a.th2dt2 * V * (T)0.25 / dx, out);
-  }
-  if (a.with_mass) {
-    // pair (c1, c2) uses the cell's partial of its weight monomial
-    const float* mm = a.cellM + cell * AMPS_CELLM;
-    const T fv = sg * (T)a.f * V;
+    float cu[3];
+    cell_curl<float>(ef, 0.25f / dx, cu);
+    cell_curl_t_row<float>(cu, (float)a.th2dt2 * V * 0.25f / dx, p, out);
+    const float fv = (float)a.f * V;
 #pragma unroll
     for (int c1 = 0; c1 < 8; c1++)
 #pragma unroll
       for (int c2 = 0; c2 <= c1; c2++) {
-        const int mo = pair_monomial(c1, c2);
-        T m9[9];
+        const float* m3 = mm + pair_monomial(c1, c2) * 9;
+        const float m0 = fv * m3[0], m1 = fv * m3[1], m2 = fv * m3[2];
+        out[c1] += m0 * ef[c2][0] + m1 * ef[c2][1] + m2 * ef[c2][2];
+        if (c1 != c2) out[c2] += m0 * ef[c1][0] + m1 * ef[c1][1] + m2 * ef[c1][2];
+      }
+    scatter_row<float>(y32, a.nvc, cid, p, out, a.h);
+  } else {
+    const double sg = ACC == 2 ? -1.0 : 1.0;
+    double out[8];
 #pragma unroll
-        for (int t = 0; t < 9; t++) m9[t] = fv * from_f32<T>(mm[mo * 9 + t]);
+    for (int c = 0; c < 8; c++) {
+      const double ep = p == 0 ? e[c][0] : (p == 1 ? e[c][1] : e[c][2]);  // no dynamic register index
+      out[c] = ACC == 1 ? 0.125 * Vd * ep : 0.0;
+    }
+    double cu[3];
+    cell_curl<double>(e, 0.25 / dxd, cu);
+    cell_curl_t_row<double>(cu, sg * a.th2dt2 * Vd * 0.25 / dxd, p, out);
+    // mass term: sum over pairs of m (FP32 partial) x e, in FP32 pairs
+    float eh[8][3], el[8][3];
+    FF acc[8];
 #pragma unroll
-        for (int p = 0; p < 3; p++) {
-          out[c1][p] += m9[3 * p] * e[c2][0] + m9[3 * p + 1] * e[c2][1] + m9[3 * p + 2] * e[c2][2];
-          if (c1 != c2)
-            out[c2][p] += m9[3 * p] * e[c1][0] + m9[3 * p + 1] * e[c1][1] + m9[3 * p + 2] * e[c1][2];
+    for (int c = 0; c < 8; c++) {
+      acc[c] = FF{0.f, 0.f};
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        eh[c][d] = (float)e[c][d];
+        el[c][d] = (float)(e[c][d] - (double)eh[c][d]);
+      }
+    }
+#pragma unroll
+    for (int c1 = 0; c1 < 8; c1++)
+#pragma unroll
+      for (int c2 = 0; c2 <= c1; c2++) {
+        const float* m3 = mm + pair_monomial(c1, c2) * 9;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const float m = m3[q];
+          ff_add(acc[c1], m, eh[c2][q], el[c2][q]);
+          if (c1 != c2) ff_add(acc[c2], m, eh[c1][q], el[c1][q]);
         }
       }
-  }
-  if (a.rhs_mode) {
-    const T B[3] = {(T)a.Bcen[cell], (T)a.Bcen[a.ncell + cell], (T)a.Bcen[2 * a.ncell + cell]};
-    cell_curl_t<T>(B, (T)a.thdt * V * (T)0.25 / dx, out);
-    const float* jj = a.cellJ + cell * 24;
+    const double fv = sg * a.f * Vd;
 #pragma unroll
-    for (int c = 0; c < 8; c++)
+    for (int c = 0; c < 8; c++) out[c] += fv * ff_value(acc[c]);
+    if (ACC == 2) {
+      const double B[3] = {a.Bcen[cell], a.Bcen[a.ncell + cell], a.Bcen[2 * a.ncell + cell]};
+      cell_curl_t_row<double>(B, a.thdt * Vd * 0.25 / dxd, p, out);
+      const float* jj = a.cellJ + cell * 24;
 #pragma unroll
-      for (int d = 0; d < 3; d++) out[c][d] -= (T)a.f * from_f32<T>(jj[3 * c + d]);
+      for (int c = 0; c < 8; c++) out[c] -= a.f * widen(jj[3 * c + p]);
+    }
+    scatter_row<double>(y64, a.nvc, cid, p, out, a.h);
   }
-  scatter<T>(y, a.nvc, cid, out, a.h);
 }
 
 // Free rows: the identity part S (D x) in FP64 (S = P^T diag(sum of V/8) P,
@@ -435,7 +527,25 @@ static ApplyArgs apply_args(amps_gpu_ctx* c) {
   a.th2dt2 = th * th * dt * dt;
   a.f = 4.0 * kPi * dt * th;
   a.thdt = th * dt;
+  a.flags = c->d_flags;
   return a;
+}
+
+template <int ACC>
+static cudaError_t launch_tile(amps_gpu_ctx* c, const ApplyArgs& a, float* y32, double* y64) {
+  static unsigned long long attr_set = 0;  // per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!((attr_set >> dev) & 1ull)) {
+    cudaError_t e = cudaFuncSetAttribute(k_amr_cell_tile<ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kTileBytes);
+    if (e != cudaSuccess) return e;
+    attr_set |= 1ull << dev;
+  }
+  // AMR meshes hold whole 512-cell blocks: ncell is a multiple of the tile
+  k_amr_cell_tile<ACC><<<(unsigned)(c->ncor / kTileCells), kTileThreads, kTileBytes, c->stream>>>(a, y32,
+                                                                                                 y64);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y) {
@@ -444,11 +554,8 @@ cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* di
   ApplyArgs a = apply_args(c);
   a.x = x;
   a.dinv = dinv;
-  a.with_identity = a.with_curl = a.with_mass = 1;
-  a.rhs_mode = 0;
   TimedLaunch t(c, "matvec", 2);
-  k_amr_cell_op<double><<<(unsigned)((c->ncor + c->tune_tb - 1) / c->tune_tb), c->tune_tb, 0,
-                          c->stream>>>(a, y);
+  if ((e = launch_tile<1>(c, a, nullptr, y)) != cudaSuccess) return e;
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, x, dinv, y, 0);
   return cudaGetLastError();
 }
@@ -460,12 +567,9 @@ cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* 
   ApplyArgs a = apply_args(c);
   a.x = x;
   a.dinv = dinv;
-  a.with_identity = 0;  // the identity part is applied in FP64 by k_amr_finish32
-  a.with_curl = a.with_mass = 1;
-  a.rhs_mode = 0;
+  // the identity part is applied in FP64 by k_amr_finish32
   TimedLaunch t(c, "matvec32", 2);
-  k_amr_cell_op<float><<<(unsigned)((c->ncor + c->tune_tb - 1) / c->tune_tb), c->tune_tb, 0,
-                         c->stream>>>(a, c->d_y32);
+  if ((e = launch_tile<0>(c, a, c->d_y32, nullptr)) != cudaSuccess) return e;
   k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_sv,
                                                      c->d_y32, x, dinv, y);
   return cudaGetLastError();
@@ -478,11 +582,8 @@ cudaError_t launch_amr_rhs(amps_gpu_ctx* c) {
   a.x = c->d_En;
   a.dinv = nullptr;
   a.Bcen = c->d_Bc;
-  a.with_identity = 0;
-  a.with_curl = a.with_mass = 1;
-  a.rhs_mode = 1;
   TimedLaunch t(c, "rhs", 2);
-  k_amr_cell_op<double><<<g1(c->ncor), 256, 0, c->stream>>>(a, c->d_rhs);
+  if ((e = launch_tile<2>(c, a, nullptr, c->d_rhs)) != cudaSuccess) return e;
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, nullptr, nullptr, c->d_rhs, 1);
   return cudaGetLastError();
 }

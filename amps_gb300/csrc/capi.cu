@@ -642,7 +642,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   cudaFree(c->d_hstage);
   c->d_hstage = nullptr;
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
-                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red, c->d_arn,
+                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red, c->d_arn, c->d_xs,
                   c->d_Z, c->d_y32,
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
@@ -918,12 +918,14 @@ amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* c, double tol, int maxit, int
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s;
   amps_gpu_solve_stats st{};
-  if (precond == 2 && (s = reset_flags(c))) return s;
+  // the tensor-core preconditioner and the AMR operator's staged copies
+  // report bounded-wait timeouts in the flags
+  const bool watch = precond == 2 || c->amr;
+  if (watch && (s = reset_flags(c))) return s;
   if ((s = cuda_check(c, launch_rhs(c), "rhs"))) return s;
   amps_gpu_status gs = gmres_solve(c, tol, maxit, precond, &st);
   if (gs != AMPS_GPU_OK && gs != AMPS_GPU_GMRES_NOT_CONVERGED) return gs;
-  // the tensor-core preconditioner reports bounded-wait timeouts in the flags
-  if (precond == 2 && (s = check_flags(c, nullptr, nullptr, nullptr))) return s;
+  if (watch && (s = check_flags(c, nullptr, nullptr, nullptr))) return s;
   // ProcessFinalSolution: E^{n+theta} = E^n + dE
   if ((s = cuda_check(c, launch_add(c, c->d_En, c->d_x, c->d_Eh, 3 * c->nvc), "E_half"))) return s;
   if ((s = cuda_check(c, launch_update_b(c), "update_b"))) return s;

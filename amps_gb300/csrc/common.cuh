@@ -134,6 +134,7 @@ struct amps_gpu_ctx {
   std::vector<StepGraph> graphs;
   double* d_red = nullptr;      // partial reductions
   double* d_arn = nullptr;      // per-CTA partial sums of the cooperative Arnoldi step
+  float* d_xs = nullptr;        // FP32 pair split (hi, lo) of an operator input, 2 x 3*nvc
   double* h_red = nullptr;      // pinned
   int restart = 30;
   int gm_guess[3] = {0, 0, 0};  // per preconditioner: Arnoldi steps of the last first cycle
@@ -265,6 +266,37 @@ cudaError_t launch_amr_fix_hanging(amps_gpu_ctx* c, double* F);
 __host__ __device__ inline int nbr_slot(int ox, int oy, int oz) {
   return (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1);
 }
+
+// FP64-accurate sums of products at FP32 throughput (GB300 issues FP32 FMAs at
+// 64x its FP64 rate): x = xh + xl split into FP32 (xh = fp32(x)); a product
+// with an FP32 coefficient m is m xh exactly (its rounding error recovered by
+// an FMA) plus m xl.  The leading parts are summed with an error-free TwoSum
+// per step (Knuth), whose exact errors go with the small parts into a second
+// FP32 sum (the cascaded summation of Ogita, Rump and Oishi); the two are
+// combined in FP64.  Error ~1e-14 of the sum of |terms| for 81 terms.  The
+// arithmetic uses the _rn intrinsics, which the compiler never contracts into
+// FMAs (a contraction would break the error-free transformations).
+struct FF {
+  float s, q;
+};
+__device__ __forceinline__ void ff_acc(FF& a, float ph, float pl) {
+  const float t = __fadd_rn(a.s, ph);
+  const float bp = __fsub_rn(t, a.s);
+  const float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(ph, bp));
+  a.s = t;
+  a.q = __fadd_rn(a.q, __fadd_rn(err, pl));
+}
+// a += m (xh + xl), m exact in FP32
+__device__ __forceinline__ void ff_add(FF& a, float m, float xh, float xl) {
+  const float ph = __fmul_rn(m, xh);
+  ff_acc(a, ph, fmaf(m, xl, fmaf(m, xh, -ph)));
+}
+// a += (kh + kl)(xh + xl), an FP64 coefficient split into FP32 pairs
+__device__ __forceinline__ void ff_add2(FF& a, float kh, float kl, float xh, float xl) {
+  const float ph = __fmul_rn(kh, xh);
+  ff_acc(a, ph, fmaf(kh, xl, fmaf(kl, xh, fmaf(kh, xh, -ph))));
+}
+__device__ __forceinline__ double ff_value(const FF& a) { return (double)a.s + (double)a.q; }
 
 // Input of the learned preconditioner at one entry e of its region map: D v at
 // a free corner (e >= 0), nothing (e == -1: no corner of the block's lattice

@@ -35,7 +35,7 @@ constexpr double kPi = 3.14159265358979323846264338327950288;
 constexpr int kMaxV = 32;
 constexpr int kRedBlocks = 304;  // 2 x 152 SMs
 constexpr int kGmOffset = 10240;  // doubles into d_red (12288 doubles)
-constexpr int kArnMaxGrid = 160;  // CTAs of the cooperative Arnoldi step (>= SMs)
+constexpr int kArnMaxGrid = 1024;  // CTAs of the cooperative Arnoldi step (at most)
 
 struct Taps {
   double K[3][3][27];  // operator taps without the mass matrix
@@ -97,19 +97,45 @@ __device__ __forceinline__ void corner_ijk(long long c, int& b, int& i, int& j, 
   k = l >> 6;
 }
 
-// y = A (dinv .* x)   (dinv may be null); one thread per (component p, corner)
-__global__ void __launch_bounds__(256) k_matvec(long long ncor, const int* __restrict__ nbr,
-                                                const float* __restrict__ M,
-                                                const double* __restrict__ x,
-                                                const double* __restrict__ dinv,
-                                                double* __restrict__ y, Taps T) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 3 * ncor) return;
-  const int p = (int)(t / ncor);
-  const long long c = t - (long long)p * ncor;
-  int b, i, j, k;
-  corner_ijk(c, b, i, j, k);
-  double acc = 0.0;
+// The operator taps split into FP32 pairs (K = Kh + Kl) for the FP64-accurate
+// evaluations below.
+struct TapsFF {
+  float Kh[3][3][27], Kl[3][3][27];
+  double f;
+};
+
+TapsFF taps_ff(const Taps& T) {
+  TapsFF t;
+  for (int p = 0; p < 3; p++)
+    for (int q = 0; q < 3; q++)
+      for (int s = 0; s < 27; s++) {
+        t.Kh[p][q][s] = (float)T.K[p][q][s];
+        t.Kl[p][q][s] = (float)(T.K[p][q][s] - (double)t.Kh[p][q][s]);
+      }
+  t.f = T.f;
+  return t;
+}
+
+// xh + xl = dinv .* x (dinv may be null), split into FP32 pairs
+__global__ void __launch_bounds__(256) k_split(long long n, const double* __restrict__ x,
+                                               const double* __restrict__ dinv,
+                                               float* __restrict__ xh, float* __restrict__ xl) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double v = dinv ? dinv[t] * x[t] : x[t];
+    const float h = (float)v;
+    xh[t] = h;
+    xl[t] = (float)(v - (double)h);
+  }
+}
+
+// Row (p, corner c) of (K + f M) x to FP64 accuracy: the 27-point taps and
+// the corner's 243 FP32 mass-matrix coefficients against the split input.
+__device__ __forceinline__ double row_ff(long long ncor, const int* __restrict__ nbr,
+                                         const float* __restrict__ M, const float* __restrict__ xh,
+                                         const float* __restrict__ xl, const TapsFF& T, int p,
+                                         long long c, int b, int i, int j, int k) {
+  FF sk{0.f, 0.f}, sm{0.f, 0.f};
 #pragma unroll 3
   for (int s = 0; s < 27; s++) {
     const int dig[3] = {s % 3, (s / 3) % 3, s / 9};
@@ -120,15 +146,30 @@ __global__ void __launch_bounds__(256) k_matvec(long long ncor, const int* __res
     const float* Ms = M + (size_t)(9 * s + 3 * p) * ncor + c;
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-      double xv = x[q * ncor + nb];
-      if (dinv) xv *= dinv[q * ncor + nb];
-      acc += (T.K[p][q][s] + T.f * widen(Ms[(size_t)q * ncor])) * xv;
+      const float h = xh[q * ncor + nb], lo = xl[q * ncor + nb];
+      ff_add2(sk, T.Kh[p][q][s], T.Kl[p][q][s], h, lo);
+      ff_add(sm, Ms[(size_t)q * ncor], h, lo);
     }
   }
-  y[t] = acc;
+  return ff_value(sk) + T.f * ff_value(sm);
 }
 
-// FP32 taps of the operator (inner GMRES iterations)
+// y = A (dinv .* x) to FP64 accuracy from the split input (outer residuals);
+// one thread per (component p, corner)
+__global__ void __launch_bounds__(256) k_matvec(long long ncor, const int* __restrict__ nbr,
+                                                const float* __restrict__ M,
+                                                const float* __restrict__ xh,
+                                                const float* __restrict__ xl,
+                                                double* __restrict__ y, TapsFF T) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * ncor) return;
+  const int p = (int)(t / ncor);
+  const long long c = t - (long long)p * ncor;
+  int b, i, j, k;
+  corner_ijk(c, b, i, j, k);
+  y[t] = row_ff(ncor, nbr, M, xh, xl, T, p, c, b, i, j, k);
+}
+
 struct TapsF {
   float K[3][3][27];
   float f;
@@ -178,12 +219,15 @@ __global__ void __launch_bounds__(256) k_matvec32(long long ncor, const int* __r
   y[t] = xi + (double)acc;
 }
 
+// RHS: theta c dt curl B^n - f J - (curl-curl + f M) E^n, the last term to
+// FP64 accuracy from the split E^n (taps without the identity)
 __global__ void __launch_bounds__(256) k_rhs(long long ncor, const int* __restrict__ nbr,
                                              const float* __restrict__ M,
-                                             const double* __restrict__ En,
+                                             const float* __restrict__ Eh,
+                                             const float* __restrict__ El,
                                              const double* __restrict__ Bc,
                                              const double* __restrict__ J,
-                                             double* __restrict__ rhs, Taps T, double c4x,
+                                             double* __restrict__ rhs, TapsFF T, double c4x,
                                              double c4y, double c4z) {
   // one thread per (component p, corner)
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -192,19 +236,7 @@ __global__ void __launch_bounds__(256) k_rhs(long long ncor, const int* __restri
   const long long c = t - (long long)p * ncor;
   int b, i, j, k;
   corner_ijk(c, b, i, j, k);
-  double r = 0.0;
-#pragma unroll 3
-  for (int s = 0; s < 27; s++) {
-    const int dig[3] = {s % 3, (s / 3) % 3, s / 9};
-    const int di = dig[0] == 0 ? 0 : (dig[0] == 1 ? -1 : 1);
-    const int dj = dig[1] == 0 ? 0 : (dig[1] == 1 ? -1 : 1);
-    const int dk = dig[2] == 0 ? 0 : (dig[2] == 1 ? -1 : 1);
-    const int nb = local_id(nbr, b, i + di, j + dj, k + dk);
-    const float* Ms = M + (size_t)(9 * s + 3 * p) * ncor + c;
-#pragma unroll
-    for (int q = 0; q < 3; q++)
-      r -= (T.K[p][q][s] + T.f * widen(Ms[(size_t)q * ncor])) * En[q * ncor + nb];
-  }
+  double r = -row_ff(ncor, nbr, M, Eh, El, T, p, c, b, i, j, k);
   r -= T.f * J[t];
   // curl B^n from the 2x2 face averages of the 8 cells around the corner
   auto Bv = [&](int ii, int jj, int kk, int comp) {
@@ -495,7 +527,7 @@ __device__ __forceinline__ void arn_block_store(const double (&acc)[NVM], int nv
 }
 
 template <int NVM>
-__global__ void __launch_bounds__(kArnThreads, 1) k_arnoldi(long long n, const double* __restrict__ V,
+__global__ void __launch_bounds__(kArnThreads) k_arnoldi(long long n, const double* __restrict__ V,
                                                           double* __restrict__ w, int nv,
                                                           double* __restrict__ vnext,
                                                           double* __restrict__ part, GmState* gs,
@@ -561,11 +593,12 @@ __global__ void __launch_bounds__(kArnThreads, 1) k_arnoldi(long long n, const d
   if (blockIdx.x == 0 && threadIdx.x == 0) gm_update(gs, jj, s_h1, s_h2, s_n2[0]);
 }
 
-// cooperative grid of k_arnoldi<NVM>: one CTA per SM (at most kArnMaxGrid)
+// cooperative grid of k_arnoldi<NVM>: as many co-resident CTAs as the
+// registers allow (at most kArnMaxGrid), and no more than the vector needs
 template <int NVM>
 cudaError_t launch_arnoldi(cudaStream_t s, long long n, const double* V, double* w, int nv,
                            double* vnext, double* part, GmState* gs, int jj) {
-  static int grid[64] = {0};  // per device
+  static int grid[64] = {0};  // per device: co-resident CTAs
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
@@ -576,9 +609,10 @@ cudaError_t launch_arnoldi(cudaStream_t s, long long n, const double* V, double*
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_arnoldi<NVM>, kArnThreads, 0);
     if (e != cudaSuccess) return e;
     if (per < 1) return cudaErrorLaunchOutOfResources;
-    grid[dev] = std::min(sms, kArnMaxGrid);
+    grid[dev] = std::min(sms * per, kArnMaxGrid);
   }
-  const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(grid[dev], (n + kArnThreads - 1) / kArnThreads));
+  const long long want = (n + kArnThreads - 1) / kArnThreads;
+  const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(grid[dev], want));
   void* args[] = {&n, &V, &w, &nv, &vnext, &part, &gs, &jj};
   return cudaLaunchCooperativeKernel((const void*)k_arnoldi<NVM>, dim3(g), dim3(kArnThreads), args, 0, s);
 }
@@ -689,12 +723,26 @@ unsigned gridr(long long n, int cap = kRedBlocks, int ept = 4) {
 }  // namespace
 
 // ============================================================================
+// FP32 pair split of an operator input into the context's scratch
+static cudaError_t split_input(amps_gpu_ctx* c, const double* x, const double* dinv) {
+  const long long n = 3 * c->nvc;
+  if (!c->d_xs) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n);
+    if (e != cudaSuccess) return e;
+  }
+  k_split<<<gridr(n), 256, 0, c->stream>>>(n, x, dinv, c->d_xs, c->d_xs + n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y) {
   if (c->amr) return launch_amr_matvec(c, x, dinv, y);
-  Taps T = make_taps(c->cfg, true);
-  TimedLaunch t(c, "matvec");
-  k_matvec<<<gridt(3 * c->ncor, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M,
-                                                                          x, dinv, y, T);
+  const TapsFF T = taps_ff(make_taps(c->cfg, true));
+  TimedLaunch t(c, "matvec", 2);
+  cudaError_t e = split_input(c, x, dinv);
+  if (e != cudaSuccess) return e;
+  const long long n = 3 * c->ncor;
+  k_matvec<<<gridt(n, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M,
+                                                               c->d_xs, c->d_xs + n, y, T);
   return cudaGetLastError();
 }
 
@@ -709,12 +757,15 @@ cudaError_t launch_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv
 
 cudaError_t launch_rhs(amps_gpu_ctx* c) {
   if (c->amr) return launch_amr_rhs(c);
-  Taps T = make_taps(c->cfg, false);
+  const TapsFF T = taps_ff(make_taps(c->cfg, false));
   double c4[3];
   for (int d = 0; d < 3; d++) c4[d] = 0.25 * (c->cfg.dt / c->cfg.dx[d] * c->cfg.theta);
-  TimedLaunch t(c, "rhs");
-  k_rhs<<<grid1(3 * c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, c->d_En, c->d_Bc,
-                                                c->d_J, c->d_rhs, T, c4[0], c4[1], c4[2]);
+  TimedLaunch t(c, "rhs", 2);
+  cudaError_t e = split_input(c, c->d_En, nullptr);
+  if (e != cudaSuccess) return e;
+  const long long n = 3 * c->ncor;
+  k_rhs<<<grid1(n), 256, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, c->d_xs, c->d_xs + n, c->d_Bc,
+                                         c->d_J, c->d_rhs, T, c4[0], c4[1], c4[2]);
   return cudaGetLastError();
 }
 

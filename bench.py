@@ -200,6 +200,13 @@ def kernel_bytes(n, ncell, nb, name):
     return None
 
 
+# FP32 operations of one push + deposit of a particle (the fused kernel's
+# algorithm): trilinear weights 16 + E/B gather 96 + Lapenta2017 ~40 + position
+# 6; deposit weights 16 + alpha ~30 + alpha v 18 + J 48 + 27 weight monomials 54
+# + mass matrix 27 x 9 FMA 486 + kinetic energy 6
+FLOP_PER_PARTICLE = 816
+
+
 def cpu_replica_rate(wl_name, steps, seconds_budget, threads):
     """FP64 oracle (Lapenta2017 + ProcessCell + re-binning) on per-thread
     single-block periodic replicas of the workload's plasma.  Returns
@@ -691,6 +698,17 @@ def run_gpu(args):
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
                 "avg_launch_ms": round(ms_top / nl, 4)}
+        if top == "push_deposit":
+            # the deposition is FP32-issue bound: its FP32 pipe rate beside the HBM one
+            nsm = C.c_int()
+            ev.rt.cudaDeviceGetAttribute(C.byref(nsm), 16, local)  # cudaDevAttrMultiProcessorCount
+            mhz = (clocks or {}).get("sm_mhz") or 2070.0
+            fp32_peak = nsm.value * 128 * 2 * mhz * 1e6 / 1e12
+            tflops = npart * FLOP_PER_PARTICLE / (ms_top / nl / 1e3) / 1e12
+            roof["fp32"] = {"achieved_tflops": round(tflops, 2), "peak_tflops": round(fp32_peak, 1),
+                            "frac": round(tflops / fp32_peak, 4),
+                            "flop_per_particle": FLOP_PER_PARTICLE,
+                            "peak_source": "SMs x 128 FP32 lanes x 2 x median SM clock"}
     shares = {k: round(v[0] / sum(x[0] for x in per.values()), 4) for k, v in per.items()}
     # kernels per step (from the event-timed pass) x timed steps
     gpu_launches = int(round(sum(v[1] for v in per.values()) / n_kt * args.steps))
