@@ -84,6 +84,8 @@ SIGNATURES = {
     "amps_gpu_import_particles_local": (C.c_int, [P, C.c_longlong, F, F, U8, I32]),
     "amps_gpu_import_particles_local_weighted": (C.c_int, [P, C.c_longlong, F, F, U8, I32, F]),
     "amps_gpu_set_species_moments": (C.c_int, [P, C.c_int]),
+    "amps_gpu_set_open_axes": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+    "amps_gpu_deleted_particles": (C.c_int, [P, LL]),
     "amps_gpu_export_species_moments": (C.c_int, [P, D]),
     "amps_gpu_export_particles": (C.c_int, [P, D, D, U8, I32, I32, U32, LL]),
     "amps_gpu_num_particles": (C.c_int, [P, LL]),

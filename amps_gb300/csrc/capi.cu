@@ -180,18 +180,18 @@ amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long*
 }
 
 amps_gpu_status reset_flags(amps_gpu_ctx* c) {
-  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 5 * sizeof(unsigned long long), c->stream),
+  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 6 * sizeof(unsigned long long), c->stream),
                     "reset flags");
 }
 
 // The launch sequence of one particle step: flag reset, stencil pack, push
 // (+ deposit), arrivals (+ assembly), flag read-back.
 cudaError_t enqueue_particle_step(amps_gpu_ctx* c, bool deposit) {
-  cudaError_t e = cudaMemsetAsync(c->d_flags, 0, 5 * sizeof(unsigned long long), c->stream);
+  cudaError_t e = cudaMemsetAsync(c->d_flags, 0, 6 * sizeof(unsigned long long), c->stream);
   if (e == cudaSuccess) e = launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur);
   if (e == cudaSuccess) e = launch_push_step(c, deposit);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(c->h_flags, c->d_flags, 4 * sizeof(unsigned long long),
+    e = cudaMemcpyAsync(c->h_flags, c->d_flags, 6 * sizeof(unsigned long long),
                         cudaMemcpyDeviceToHost, c->stream);
   return e;
 }
@@ -234,6 +234,9 @@ amps_gpu_status read_step_flags(amps_gpu_ctx* c, long long* out_of_block, long l
   if (out_of_block) *out_of_block = (long long)c->h_flags[0];
   if (ulp) *ulp = (long long)c->h_flags[1];
   if (overflow) *overflow = (long long)c->h_flags[3];
+  // particles that left through open faces are gone from the layout
+  c->np -= (long long)c->h_flags[5];
+  c->deleted_total += (long long)c->h_flags[5];
   if (c->h_flags[2])
     return set_err(c, AMPS_GPU_DEVICE_TIMEOUT,
                    "device reported " + std::to_string(c->h_flags[2]) +
@@ -963,6 +966,23 @@ amps_gpu_status amps_gpu_step(amps_gpu_ctx* c, double tol, int maxit, int precon
   c->have_moments = true;
   if (stats) *stats = st;
   return fs;
+}
+
+amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* c, int open_x, int open_y, int open_z) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  cudaStreamSynchronize(c->stream);
+  c->open_axes = (open_x ? 1 : 0) | (open_y ? 2 : 0) | (open_z ? 4 : 0);
+  // captured particle steps carry the old setting in their kernel arguments
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_deleted_particles(amps_gpu_ctx* c, long long* total) {
+  if (!c || !total) return AMPS_GPU_INVALID_ARG;
+  *total = c->deleted_total;
+  return AMPS_GPU_OK;
 }
 
 amps_gpu_status amps_gpu_set_graphs(amps_gpu_ctx* c, int on) {

@@ -155,6 +155,8 @@ struct amps_gpu_ctx {
   uint32_t* d_id[2] = {nullptr, nullptr};
   int cur = 0;
   bool has_wcorr = false;
+  int open_axes = 0;            // bit d: particles leaving through a face of axis d are deleted
+  long long deleted_total = 0;  // particles deleted at open faces since creation
   int32_t* d_base = nullptr;    // ncor+1 slot offsets
   int32_t* d_cnt = nullptr;     // ncor occupancy
   int32_t* d_arr = nullptr;     // ncor arrivals in the current step
@@ -164,7 +166,8 @@ struct amps_gpu_ctx {
   int32_t* d_rank = nullptr;    // slots: rank inside the destination cell (rebuild)
   int32_t* d_count = nullptr;   // ncor+1 histogram (rebuild)
   int32_t* d_scan_part = nullptr;
-  // [0] moved > 1 block, [1] near a cell face, [2] device error, [3] overflow, [4] list tail
+  // [0] moved > 1 block, [1] near a cell face, [2] device error, [3] overflow, [4] list tail,
+  // [5] deleted at open faces
   unsigned long long* d_flags = nullptr;
   unsigned long long* h_flags = nullptr;  // pinned
 

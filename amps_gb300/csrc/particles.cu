@@ -83,14 +83,16 @@ __device__ __forceinline__ float clamp_below8(float u) {
 // offset un (cell units of b) -> position on the finest lattice (exact: the
 // scale is a power of two), leaf block from the fine map, offset in that
 // block's cell units (one rounding).  Periodic wrap moves the lattice position
-// by whole domain lengths, which enter as integers.
-__device__ __forceinline__ int amr_dest(const AmrDev& m, int b, float un[3], int ic[3]) {
+// by whole domain lengths, which enter as integers.  Returns -1 when the
+// particle left the domain through a face of an open axis (bit d of open).
+__device__ __forceinline__ int amr_dest(const AmrDev& m, int b, float un[3], int ic[3], int open) {
   const float fs = (float)__ldg(m.bscale + b);
   int F[3], shift[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const int g = __ldg(m.borg + 3 * b + d) + (int)floorf(un[d] * fs);
     const int n = m.nfine[d];
+    if (((open >> d) & 1) && (g < 0 || g >= n)) return -1;
     int w = g % n;
     if (w < 0) w += n;
     F[d] = w;
@@ -163,7 +165,20 @@ struct StepArgs {
   long long ovf_cap;
   SpeciesTab st;
   AmrDev amr;     // fine_map == nullptr on uniform meshes
+  int open;       // bit d: axis d is open (particles leaving the domain are deleted)
+  int nbk[3];     // blocks per axis (uniform meshes)
 };
+
+// A uniform-mesh particle of block b whose destination lies o (in -1..1 per
+// axis) blocks away leaves the domain through a face of an open axis.
+__device__ __forceinline__ bool leaves_open_face(const StepArgs& a, int b, const int o[3]) {
+  const int bc[3] = {b % a.nbk[0], (b / a.nbk[0]) % a.nbk[1], b / (a.nbk[0] * a.nbk[1])};
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (((a.open >> d) & 1) && ((o[d] < 0 && bc[d] == 0) || (o[d] > 0 && bc[d] == a.nbk[d] - 1)))
+      return true;
+  return false;
+}
 
 // 1/dx^3 of block b
 __device__ __forceinline__ float block_inv_vol(const StepArgs& a, int b) {
@@ -204,7 +219,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   int offA, offB;
   lane_offsets(lane, offA, offB);
   double en = 0.0;
-  unsigned long long n_far = 0, n_near = 0;
+  unsigned long long n_far = 0, n_near = 0, n_del = 0;
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
   const float bdtdx = AMR ? __ldg(a.amr.bdtdx + b) : 0.0f;
@@ -287,7 +302,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
             if (!(u[d] >= 0.0f && u[d] < 8.0f)) out = true;
             ic[d] = min((int)u[d], AMPS_NC - 1);
           }
-          if (out) nbk = amr_dest(a.amr, b, u, ic);
+          if (out) nbk = amr_dest(a.amr, b, u, ic, a.open);
 #pragma unroll
           for (int d = 0; d < 3; d++)
             if (fabsf(u[d] - rintf(u[d])) < 4.76837158203125e-7f) nearf = true;
@@ -306,11 +321,16 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
             ic[d] = min((int)un, AMPS_NC - 1);
             if (fabsf(un - rintf(un)) < 4.76837158203125e-7f) nearf = true;
           }
-          if (o[0] | o[1] | o[2]) nbk = __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2]));
+          if (o[0] | o[1] | o[2])
+            nbk = (a.open && leaves_open_face(a, b, o)) ? -1
+                                                        : __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2]));
         }
         if (far) n_far++;
         if (nearf) n_near++;
-        key = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+        // nbk < 0: the particle left the domain through an open face and is
+        // deleted (no slot, no deposit)
+        if (nbk >= 0) key = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+        else n_del++;
       }
       const bool stays = act && key == (int)cid;
       const unsigned smask = __ballot_sync(0xffffffffu, stays);
@@ -330,7 +350,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
                              i, j, k, a.st, inv_vol);
       }
       // movers: slack of the destination cell, else the overflow list
-      const bool mover = act && !stays;
+      const bool mover = act && !stays && key >= 0;
       const int slot = warp_reserve(mover, mover ? key : 0, a.arr);
       if (mover) {
         const int cb = a.base[key], ccap = a.base[key + 1] - cb, cn = a.cnt[key];
@@ -373,6 +393,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   }
   if (n_far) atomicAdd(a.flags + 0, n_far);
   if (n_near) atomicAdd(a.flags + 1, n_near);
+  if (n_del) atomicAdd(a.flags + 5, n_del);
   if (DEP) reduce_energy(en, s_en, a.energy);
 }
 
@@ -1103,6 +1124,10 @@ StepArgs step_args(amps_gpu_ctx* c) {
   a.ovf_cap = c->slots;
   a.st = make_species(c->cfg);
   a.amr = c->amrdev;
+  a.open = c->open_axes;
+  a.nbk[0] = c->cfg.nbx;
+  a.nbk[1] = c->cfg.nby;
+  a.nbk[2] = c->cfg.nbz;
   return a;
 }
 

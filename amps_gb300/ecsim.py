@@ -288,6 +288,16 @@ class EcsimContext:
                                                      ptr(M, C.c_double)), "export_moments")
         return J, M
 
+    def set_open_axes(self, x=False, y=False, z=False):
+        """Delete particles leaving the domain through the faces of these axes."""
+        self._check(self.lib.amps_gpu_set_open_axes(self.h, int(bool(x)), int(bool(y)), int(bool(z))),
+                    "set_open_axes")
+
+    def deleted_particles(self):
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_deleted_particles(self.h, C.byref(n)), "deleted_particles")
+        return n.value
+
     def set_species_moments(self, on=True):
         """Sample rho, rho u, rho u u per species on the corners at every deposition."""
         self._check(self.lib.amps_gpu_set_species_moments(self.h, 1 if on else 0),

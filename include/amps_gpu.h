@@ -214,6 +214,15 @@ amps_gpu_status amps_gpu_field_solve(amps_gpu_ctx* ctx, double tol, int maxit, i
  * (the reference's first-call branch, pic_field_solver_ecsim.cpp:6209). */
 amps_gpu_status amps_gpu_step(amps_gpu_ctx* ctx, double tol, int maxit, int precond,
                               amps_gpu_step_stats* stats);
+/* Particle domain boundaries: an open axis deletes the particles whose move
+ * leaves the domain through one of its faces (the mover's
+ * _PIC_PARTICLE_DOMAIN_BOUNDARY_INTERSECTION_PROCESSING_MODE__DELETE_ branch,
+ * pic_mover_boris.cpp:1159-1170 and :1251-1254, taken when findTreeNode finds
+ * no block); the other axes stay periodic (default: all periodic).  The field
+ * solve stays periodic on every axis.  deleted_particles: the number deleted
+ * since creation (amps_gpu_num_particles drops by as many). */
+amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* ctx, int open_x, int open_y, int open_z);
+amps_gpu_status amps_gpu_deleted_particles(amps_gpu_ctx* ctx, long long* total);
 /* Species moments on corners (_PIC_FIELD_SOLVER_SAMPLE_SPECIES_ON_CORNER_,
  * ProcessCell pic_field_solver_ecsim.cpp:2270-2303): with sampling on, every
  * deposition (update_j_mass_matrix, push_deposit, step) also forms per corner

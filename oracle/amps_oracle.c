@@ -25,6 +25,13 @@
 
 static int wrap(int i, int n) { i %= n; return i < 0 ? i + n : i; }
 
+/* Open axes (bit d): a particle whose move leaves the domain through a face
+ * of such an axis is deleted (the mover's DELETE processing when findTreeNode
+ * finds no block, pic_mover_boris.cpp:1159-1170, 1251-1254); block and cell
+ * become -1 and every later stage skips it.  Other axes are periodic. */
+int orc_open_axes = 0;
+void orc_set_open_axes(int mask) { orc_open_axes = mask; }
+
 static long cidx(const orc_mesh* g, int I, int J, int K) {
   const int NX = NC * g->nbx, NY = NC * g->nby, NZ = NC * g->nbz;
   return (long)wrap(I, NX) + (long)NX * ((long)wrap(J, NY) + (long)NY * wrap(K, NZ));
@@ -229,6 +236,7 @@ long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* sp
               int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev) {
   long nbad = 0;
   for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue;  /* deleted at an open face */
     int bxyz[3], iX[3], nd[8][3];
     double xmin[3], xI[3], vI[3], wt[8], wn[8];
     block_geom(g, block[p], bxyz, xmin);
@@ -255,7 +263,17 @@ long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* sp
       vF[i] = 2.0 * vp - vI[i];
     }
     for (int d = 0; d < 3; d++) xF[d] = xI[d] + dtT * vF[d];
-    locate_one(g, xF, block + p, cell + p);
+    const int nbd[3] = {g->nbx, g->nby, g->nbz};
+    int gone = 0;
+    for (int d = 0; d < 3; d++)
+      if (((orc_open_axes >> d) & 1) &&
+          (xF[d] < g->x0[d] || xF[d] >= g->x0[d] + nbd[d] * NC * g->dx[d]))
+        gone = 1;
+    if (gone) {
+      block[p] = cell[p] = -1;
+    } else {
+      locate_one(g, xF, block + p, cell + p);
+    }
     for (int d = 0; d < 3; d++) { x[3 * p + d] = xF[d]; v[3 * p + d] = vF[d]; }
   }
   return nbad;
@@ -350,6 +368,7 @@ double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
   double V = g->dx[0] * g->dx[1] * g->dx[2];
   double energy = 0.0;
   for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue;
     int bxyz[3], iX[3], nd[8][3];
     double xmin[3], xI[3], vI[3], wt[8], wn[8];
     block_geom(g, block[p], bxyz, xmin);
@@ -440,6 +459,7 @@ void orc_species_moments(const orc_mesh* g, long n, const double* x, const doubl
   const double V = g->dx[0] * g->dx[1] * g->dx[2];
   memset(out, 0, sizeof(double) * ncor * nq);
   for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue;
     int bxyz[3], iX[3], nd[8][3];
     double xmin[3], xI[3], wt[8], wn[8];
     block_geom(g, block[p], bxyz, xmin);

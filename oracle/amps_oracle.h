@@ -64,6 +64,9 @@ void orc_locate(const orc_mesh* g, long n, const double* x, int32_t* block, int3
 
 /* ---- field solve ---- */
 void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor);
+/* open axes (bit d): particles leaving the domain through their faces are
+ * deleted by the pushes (block = cell = -1), on uniform and AMR meshes */
+void orc_set_open_axes(int mask);
 /* species moments on corners (ProcessCell :2270-2303): out[corner][10*nspec] */
 void orc_species_moments(const orc_mesh* g, long n, const double* x, const double* v,
                          const uint8_t* spec, const double* wcorr, const int32_t* block,

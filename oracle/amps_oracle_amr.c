@@ -25,6 +25,8 @@
 #include <string.h>
 
 #define PI_D 3.14159265358979323846264338327950288
+
+extern int orc_open_axes; /* amps_oracle.c */
 #define NSPEC_MAX 8
 
 typedef struct {
@@ -142,7 +144,9 @@ static void stencil(const orc_amr* g, int b, const double x[3], double w[8], int
 
 long orc_amr_push(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
                   int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev) {
+  const double dxf = g->dx0 / (double)(1 << g->lmax);
   for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue; /* deleted at an open face */
     double w[8], E[3] = {0, 0, 0}, B[3] = {0, 0, 0}, val[3];
     int cid[8];
     stencil(g, block[p], x + 3 * p, w, cid);
@@ -161,11 +165,18 @@ long orc_amr_push(const orc_amr* g, long n, double* x, double* v, const uint8_t*
       for (int j = 0; j < 3; j++) vp += al[3 * i + j] * (v[3 * p + j] + h * E[j]);
       vn[i] = 2.0 * vp - v[3 * p + i];
     }
+    int gone = 0;
     for (int d = 0; d < 3; d++) {
       v[3 * p + d] = vn[d];
       x[3 * p + d] += g->dt * vn[d];
+      if (((orc_open_axes >> d) & 1) &&
+          (x[3 * p + d] < g->x0[d] || x[3 * p + d] >= g->x0[d] + g->nfine[d] * dxf))
+        gone = 1;
     }
-    locate_one(g, x + 3 * p, block + p, cell + p);
+    if (gone)
+      block[p] = cell[p] = -1;
+    else
+      locate_one(g, x + 3 * p, block + p, cell + p);
   }
   return 0;
 }
@@ -180,6 +191,7 @@ double orc_amr_deposit(const orc_amr* g, long n, const double* x, const double* 
   memset(cellM, 0, sizeof(double) * ncell * 324);
   double energy = 0.0;
   for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue;
     double w[8], B[3] = {0, 0, 0}, val[3];
     int cid[8];
     const int b = block[p];
@@ -221,6 +233,7 @@ void orc_amr_species_moments(const orc_amr* g, long n, const double* x, const do
   const int nq = 10 * g->nspec;
   memset(out, 0, sizeof(double) * (size_t)g->ncorners * nq);
   for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue;
     double w[8];
     int cid[8];
     const int b = block[p];

@@ -46,6 +46,7 @@ def load():
         "orc_deposit": (C.c_double, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D]),
         "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
         "orc_species_moments": (None, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D]),
+        "orc_set_open_axes": (None, [C.c_int]),
         "orc_center_to_corner": (None, [C.POINTER(Mesh), D, D]),
         "orc_rhs": (None, [C.POINTER(Mesh), D, D, D, D, D]),
         "orc_matvec": (None, [C.POINTER(Mesh), D, D, D]),
