@@ -86,6 +86,10 @@ SIGNATURES = {
     "amps_gpu_set_species_moments": (C.c_int, [P, C.c_int]),
     "amps_gpu_set_open_axes": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
     "amps_gpu_deleted_particles": (C.c_int, [P, LL]),
+    "amps_gpu_add_injection": (C.c_int, [P, C.c_int, C.c_int, C.c_double, D, C.c_double]),
+    "amps_gpu_clear_injection": (C.c_int, [P]),
+    "amps_gpu_set_injection_seed": (C.c_int, [P, C.c_ulonglong]),
+    "amps_gpu_injected_particles": (C.c_int, [P, LL]),
     "amps_gpu_export_species_moments": (C.c_int, [P, D]),
     "amps_gpu_export_particles": (C.c_int, [P, D, D, U8, I32, I32, U32, LL]),
     "amps_gpu_num_particles": (C.c_int, [P, LL]),

@@ -14,6 +14,8 @@
 // scatter to the (up to 8) cells sharing a corner.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "deposit_core.cuh"
 
@@ -40,6 +42,16 @@ __device__ __forceinline__ double cval(const double* __restrict__ F, const doubl
     const int p = h.hp[t];
     v += h.hw[t] * (dinv ? dinv[d * nvc + p] * F[d * nvc + p] : F[d * nvc + p]);
   }
+  return v;
+}
+
+// FP32 value of corner c, component d (xf already scaled), P applied
+__device__ __forceinline__ float cval_f(const float* __restrict__ xf, long long nvc, int c, int d,
+                                        const Hang& h) {
+  const int s = h.hs[c], e = h.hs[c + 1];
+  if (s == e) return xf[d * nvc + c];
+  float v = 0.f;
+  for (int t = s; t < e; t++) v = fmaf((float)h.hw[t], xf[d * nvc + h.hp[t]], v);
   return v;
 }
 
@@ -136,6 +148,7 @@ struct ApplyArgs {
   const float* cellM;
   const float* cellJ;
   const double* x;     // input field (component-major)
+  const float* xf;     // the same times dinv, in FP32 (the FP32 inner operator)
   const double* dinv;  // optional right preconditioner
   const double* Bcen;  // RHS: centre B (component-major over cells)
   double th2dt2, f, thdt;
@@ -166,7 +179,11 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
   extern __shared__ __align__(16) float s_m[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_cid[kTileCells][8];
-  __shared__ double s_e[kTileCells][24];  // 8 corners x 3
+  // corner values (8 corners x 3): FP32 for ACC 0; FP64 and its FP32 pair split for ACC 1/2
+  __shared__ float s_eh[kTileCells][24];
+  __shared__ float s_el[ACC == 0 ? 1 : kTileCells][24];
+  __shared__ double s_e[ACC == 0 ? 1 : kTileCells][24];
+  __shared__ double s_cu[ACC == 0 ? 1 : kTileCells][3];
   const int tid = threadIdx.x, p = tid / kTileCells, lc = tid % kTileCells;
   const long long cell0 = (long long)blockIdx.x * kTileCells;
   if (tid == 0) {
@@ -191,20 +208,23 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     cid[c] = s_cid[lc][c];
-    s_e[lc][3 * c + p] = cval(a.x, a.dinv, a.nvc, cid[c], p, a.h);
+    if (ACC == 0) {
+      s_eh[lc][3 * c + p] = cval_f(a.xf, a.nvc, cid[c], p, a.h);
+    } else {
+      const double v = cval(a.x, a.dinv, a.nvc, cid[c], p, a.h);
+      const float vh = (float)v;
+      s_e[lc][3 * c + p] = v;
+      s_eh[lc][3 * c + p] = vh;
+      s_el[lc][3 * c + p] = (float)(v - (double)vh);
+    }
   }
-  const bool ok = mbar_wait_bounded(&bar, 0, kWaitLimit);
-  __syncthreads();
+  // CTA-uniform: every thread leaves together on a timeout (later barriers)
+  const bool ok = __syncthreads_and(mbar_wait_bounded(&bar, 0, kWaitLimit)) != 0;
   if (!ok) {
-    atomicAdd(a.flags + 2, 1ull);
+    if (tid == 0) atomicAdd(a.flags + 2, 1ull);
     mbar_wait_bounded(&bar, 0, kWaitLimit);  // let the copy land before exiting
     return;
   }
-  double e[8][3];
-#pragma unroll
-  for (int c = 0; c < 8; c++)
-#pragma unroll
-    for (int d = 0; d < 3; d++) e[c][d] = s_e[lc][3 * c + d];
   const float* mm = s_m + lc * AMPS_CELLM + 3 * p;  // row p of every monomial block
   if (ACC == 0) {
     const float dx = (float)dxd, V = (float)Vd;
@@ -213,7 +233,7 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
     for (int c = 0; c < 8; c++) {
       out[c] = 0.f;
 #pragma unroll
-      for (int d = 0; d < 3; d++) ef[c][d] = (float)e[c][d];
+      for (int d = 0; d < 3; d++) ef[c][d] = s_eh[lc][3 * c + d];
     }
     float cu[3];
     cell_curl<float>(ef, 0.25f / dx, cu);
@@ -233,12 +253,27 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
     const double sg = ACC == 2 ? -1.0 : 1.0;
     double out[8];
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const double ep = p == 0 ? e[c][0] : (p == 1 ? e[c][1] : e[c][2]);  // no dynamic register index
-      out[c] = ACC == 1 ? 0.125 * Vd * ep : 0.0;
+    for (int c = 0; c < 8; c++) out[c] = ACC == 1 ? 0.125 * Vd * s_e[lc][3 * c + p] : 0.0;
+    // curl of the cell: component p by thread p, shared
+    {
+      double sa = 0.0, sb = 0.0;
+      const int qa = p == 0 ? 2 : (p == 1 ? 0 : 1), qb = p == 0 ? 1 : (p == 1 ? 2 : 0);
+#pragma unroll
+      for (int k2 = 0; k2 < 8; k2++) {
+        const bool px = k2 == 1 || k2 == 2 || k2 == 5 || k2 == 6;
+        const bool py = k2 == 2 || k2 == 3 || k2 == 6 || k2 == 7;
+        const bool pz = k2 >= 4;
+        // cu0 = (dEz/dy - dEy/dz), cu1 = (dEx/dz - dEz/dx), cu2 = (dEy/dx - dEx/dy)
+        const bool sga = p == 0 ? py : (p == 1 ? pz : px);
+        const bool sgb = p == 0 ? pz : (p == 1 ? px : py);
+        const double va = s_e[lc][3 * k2 + qa], vb = s_e[lc][3 * k2 + qb];
+        sa += sga ? va : -va;
+        sb += sgb ? vb : -vb;
+      }
+      s_cu[lc][p] = 0.25 / dxd * (sa - sb);
     }
-    double cu[3];
-    cell_curl<double>(e, 0.25 / dxd, cu);
+    __syncthreads();
+    const double cu[3] = {s_cu[lc][0], s_cu[lc][1], s_cu[lc][2]};
     cell_curl_t_row<double>(cu, sg * a.th2dt2 * Vd * 0.25 / dxd, p, out);
     // mass term: sum over pairs of m (FP32 partial) x e, in FP32 pairs
     float eh[8][3], el[8][3];
@@ -248,8 +283,8 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
       acc[c] = FF{0.f, 0.f};
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        eh[c][d] = (float)e[c][d];
-        el[c][d] = (float)(e[c][d] - (double)eh[c][d]);
+        eh[c][d] = s_eh[lc][3 * c + d];
+        el[c][d] = s_el[lc][3 * c + d];
       }
     }
 #pragma unroll
@@ -276,6 +311,15 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
     }
     scatter_row<double>(y64, a.nvc, cid, p, out, a.h);
   }
+}
+
+// xf = fp32(dinv .* x), the FP32 inner operator's input
+__global__ void __launch_bounds__(256) k_amr_to_f32(long long n, const double* __restrict__ x,
+                                                    const double* __restrict__ dinv,
+                                                    float* __restrict__ xf) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    xf[t] = (float)(dinv ? dinv[t] * x[t] : x[t]);
 }
 
 // Free rows: the identity part S (D x) in FP64 (S = P^T diag(sum of V/8) P,
@@ -568,7 +612,13 @@ cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* 
   a.x = x;
   a.dinv = dinv;
   // the identity part is applied in FP64 by k_amr_finish32
-  TimedLaunch t(c, "matvec32", 2);
+  const long long n = 3 * c->nvc;
+  if (!c->d_xs && (e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n)) != cudaSuccess)
+    return e;
+  a.xf = c->d_xs;
+  TimedLaunch t(c, "matvec32", 3);
+  k_amr_to_f32<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, c->stream>>>(n, x, dinv,
+                                                                                                 c->d_xs);
   if ((e = launch_tile<0>(c, a, c->d_y32, nullptr)) != cudaSuccess) return e;
   k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_sv,
                                                      c->d_y32, x, dinv, y);

@@ -180,18 +180,18 @@ amps_gpu_status check_flags(amps_gpu_ctx* c, long long* out_of_block, long long*
 }
 
 amps_gpu_status reset_flags(amps_gpu_ctx* c) {
-  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 6 * sizeof(unsigned long long), c->stream),
+  return cuda_check(c, cudaMemsetAsync(c->d_flags, 0, 7 * sizeof(unsigned long long), c->stream),
                     "reset flags");
 }
 
 // The launch sequence of one particle step: flag reset, stencil pack, push
 // (+ deposit), arrivals (+ assembly), flag read-back.
 cudaError_t enqueue_particle_step(amps_gpu_ctx* c, bool deposit) {
-  cudaError_t e = cudaMemsetAsync(c->d_flags, 0, 6 * sizeof(unsigned long long), c->stream);
+  cudaError_t e = cudaMemsetAsync(c->d_flags, 0, 7 * sizeof(unsigned long long), c->stream);
   if (e == cudaSuccess) e = launch_pack_stencils(c, c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur);
   if (e == cudaSuccess) e = launch_push_step(c, deposit);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(c->h_flags, c->d_flags, 6 * sizeof(unsigned long long),
+    e = cudaMemcpyAsync(c->h_flags, c->d_flags, 7 * sizeof(unsigned long long),
                         cudaMemcpyDeviceToHost, c->stream);
   return e;
 }
@@ -234,9 +234,12 @@ amps_gpu_status read_step_flags(amps_gpu_ctx* c, long long* out_of_block, long l
   if (out_of_block) *out_of_block = (long long)c->h_flags[0];
   if (ulp) *ulp = (long long)c->h_flags[1];
   if (overflow) *overflow = (long long)c->h_flags[3];
-  // particles that left through open faces are gone from the layout
-  c->np -= (long long)c->h_flags[5];
+  // particles that left through open faces are gone from the layout, the
+  // injected ones are in it
+  c->np += (long long)c->h_flags[6] - (long long)c->h_flags[5];
   c->deleted_total += (long long)c->h_flags[5];
+  c->injected_total += (long long)c->h_flags[6];
+  c->next_id += (uint32_t)c->h_flags[6];
   if (c->h_flags[2])
     return set_err(c, AMPS_GPU_DEVICE_TIMEOUT,
                    "device reported " + std::to_string(c->h_flags[2]) +
@@ -645,7 +648,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   cudaFree(c->d_hstage);
   c->d_hstage = nullptr;
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
-                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red, c->d_arn, c->d_xs,
+                  c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red, c->d_arn, c->d_xs, c->d_step,
                   c->d_Z, c->d_y32,
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
@@ -976,6 +979,60 @@ amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* c, int open_x, int open_y, 
   // captured particle steps carry the old setting in their kernel arguments
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   c->graphs.clear();
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_add_injection(amps_gpu_ctx* c, int face, int spec, double density,
+                                       const double* drift, double vth) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  if (c->amr) return set_err(c, AMPS_GPU_INVALID_ARG, "add_injection: uniform meshes only");
+  if (face < 0 || face > 5 || !((c->open_axes >> (face >> 1)) & 1))
+    return set_err(c, AMPS_GPU_INVALID_ARG, "add_injection: the face must belong to an open axis");
+  if (spec < 0 || spec >= c->cfg.nspec || !(vth > 0.0) || !(density >= 0.0) || c->inj.size() >= 8)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "add_injection: bad species, density, vth or too many sources");
+  cudaSetDevice(c->cfg.device);
+  cudaStreamSynchronize(c->stream);
+  if (!c->d_step) {
+    unsigned long long init[2] = {0ull, (unsigned long long)c->next_id};
+    if (cudaMalloc(reinterpret_cast<void**>(&c->d_step), sizeof(init)) != cudaSuccess ||
+        cudaMemcpy(c->d_step, init, sizeof(init), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      return set_err(c, AMPS_GPU_CUDA_ERROR, "add_injection: allocation failed");
+    }
+  }
+  amps_gpu_ctx::InjSource s;
+  s.face = face;
+  s.spec = spec;
+  s.density = density;
+  for (int d = 0; d < 3; d++) s.drift[d] = drift ? drift[d] : 0.0;
+  s.vth = vth;
+  c->inj.push_back(s);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_clear_injection(amps_gpu_ctx* c) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  cudaSetDevice(c->cfg.device);
+  cudaStreamSynchronize(c->stream);
+  c->inj.clear();
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_set_injection_seed(amps_gpu_ctx* c, unsigned long long seed) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  c->inj_seed = seed;
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_injected_particles(amps_gpu_ctx* c, long long* total) {
+  if (!c || !total) return AMPS_GPU_INVALID_ARG;
+  *total = c->injected_total;
   return AMPS_GPU_OK;
 }
 

@@ -157,6 +157,16 @@ struct amps_gpu_ctx {
   bool has_wcorr = false;
   int open_axes = 0;            // bit d: particles leaving through a face of axis d are deleted
   long long deleted_total = 0;  // particles deleted at open faces since creation
+  // injection through open faces (particles.cu: k_inject)
+  struct InjSource {
+    int face, spec;
+    double density, drift[3], vth;
+  };
+  std::vector<InjSource> inj;
+  unsigned long long inj_seed = 1;
+  unsigned long long* d_step = nullptr;  // device step counter of the injection random streams
+  long long injected_total = 0;
+  uint32_t next_id = 0;         // id of the next injected particle (import ids are 0..n-1)
   int32_t* d_base = nullptr;    // ncor+1 slot offsets
   int32_t* d_cnt = nullptr;     // ncor occupancy
   int32_t* d_arr = nullptr;     // ncor arrivals in the current step
@@ -167,7 +177,7 @@ struct amps_gpu_ctx {
   int32_t* d_count = nullptr;   // ncor+1 histogram (rebuild)
   int32_t* d_scan_part = nullptr;
   // [0] moved > 1 block, [1] near a cell face, [2] device error, [3] overflow, [4] list tail,
-  // [5] deleted at open faces
+  // [5] deleted at open faces, [6] injected
   unsigned long long* d_flags = nullptr;
   unsigned long long* h_flags = nullptr;  // pinned
 
@@ -224,6 +234,7 @@ amps_gpu_status layout_cell_moments(amps_gpu_ctx* c, double* hJ, double* hM);
 cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
                             double c_light, long long max_sub);
 cudaError_t launch_deposit(amps_gpu_ctx* c);
+void set_next_id(amps_gpu_ctx* c, long long n);
 // species moments on corners (species.cu)
 amps_gpu_status species_setup(amps_gpu_ctx* c, bool on);
 void species_free(amps_gpu_ctx* c);

@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 #include "common.cuh"
@@ -395,6 +396,209 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   if (n_near) atomicAdd(a.flags + 1, n_near);
   if (n_del) atomicAdd(a.flags + 5, n_del);
   if (DEP) reduce_energy(en, s_en, a.energy);
+}
+
+// ---------------------------------------------------------------------------
+// Injection through open faces: the OpenFlow boundary of the reference
+// (PIC::BC::ExternalBoundary::OpenFlow, src/pic/pic_bc.cpp:330-420) on every
+// boundary cell face of an injection source: a Poisson process in time at the
+// rate CalculateInjectionRate_MaxwellianDistribution (pic_bc.cpp:215) x face
+// area / macro-particle weight; each particle at a uniform point of the face
+// with the velocity of InjectMaxwellianDistribution
+// (src/pic/pic_vel_distribution.cpp:49-161), then moved by the Lapenta2017
+// mover for the rest of the step, and placed in its destination cell like a
+// mover (k_arrivals deposits it).  Random numbers: a counter-based stream per
+// (seed, step, source, face cell), inj_uniform below; the FP64 oracle restates
+// the same stream.  One thread per (source, boundary cell face).
+constexpr int kMaxInj = 8;
+struct InjDev {
+  int face, spec, ncell, first;  // first: index of the source's first thread
+  double rate;                   // particles per unit face area per unit time (/weight)
+  double drift[3], beta;         // bulk velocity; beta = 1 / (sqrt(2) vth)
+};
+struct InjArgs {
+  InjDev src[kMaxInj];
+  int nsrc, nthreads;
+  double dt, dx[3];
+  int nbk[3];
+  unsigned long long seed;
+  const unsigned long long* step;  // [0] step counter, [1] next particle id
+};
+
+__device__ __forceinline__ unsigned long long inj_mix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+// uniform in (0, 1) from draw d of the stream key
+__device__ __forceinline__ double inj_uniform(unsigned long long key, unsigned& d) {
+  return ((double)(inj_mix(key + (d++)) >> 11) + 0.5) * 0x1.0p-53;
+}
+
+__global__ void __launch_bounds__(128) k_inject(StepArgs a, InjArgs g) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= g.nthreads) return;
+  int s = 0;
+  while (s + 1 < g.nsrc && t >= g.src[s + 1].first) s++;
+  const InjDev S = g.src[s];
+  const int c = t - S.first;
+  const int ax = S.face >> 1, hi = S.face & 1, ta = (ax + 1) % 3, tb = (ax + 2) % 3;
+  const int NT = 8 * g.nbk[ta];
+  const int it = c % NT, ib = c / NT;  // tangential cell coordinates
+  const double area = g.dx[ta] * g.dx[tb];
+  const double R = S.rate * area;
+  if (!(R > 0.0)) return;
+  double nrm[3] = {0.0, 0.0, 0.0};
+  nrm[ax] = hi ? 1.0 : -1.0;  // outward normal
+  const unsigned long long key =
+      inj_mix(inj_mix(inj_mix(g.seed) ^ *g.step) ^ (((unsigned long long)s << 40) | (unsigned long long)c));
+  unsigned d = 0;
+  double tt = 0.0;
+  for (int k = 0; k < 4096; k++) {
+    tt += -log(inj_uniform(key, d)) / R;
+    if (tt >= g.dt) break;
+    const double c0 = inj_uniform(key, d), c1 = inj_uniform(key, d);
+    // velocity: InjectMaxwellianDistribution (3D branch)
+    double v[3] = {0.0, 0.0, 0.0};
+    bool ok = false;
+    for (int outer = 0; outer < 64 && !ok; outer++) {
+      const double dot = S.drift[0] * nrm[0] + S.drift[1] * nrm[1] + S.drift[2] * nrm[2];
+      const double sc = S.beta * fabs(dot);
+      double u = 0.0, acc = 0.0;
+      bool got = false;
+      for (int tries = 0; tries < 4096 && !got; tries++) {
+        if (dot <= 0.0) {
+          int q = 0;
+          do u = -10.0 + 20.0 * inj_uniform(key, d); while (u + sc <= 0.0 && ++q < 4096);
+          const double cc = sqrt(2.0 + sc * sc);
+          acc = 2.0 * (u + sc) / (sc + cc) * exp(0.5 + 0.5 * sc * (sc - cc) - u * u);
+        } else {
+          int q = 0;
+          do u = -10.0 + 20.0 * inj_uniform(key, d); while (u + sc >= 0.0 && ++q < 4096);
+          const double cc = 0.5 * (-sqrt(sc * sc + 2.0) - sc);
+          acc = (u + sc) * exp(-u * u) / (cc + sc) / exp(-cc * cc);
+        }
+        got = !(acc < inj_uniform(key, d));
+      }
+      if (!got) break;
+      double v1[3], v2[3], v3[3];
+      for (int q = 0; q < 3; q++) v3[q] = -(fabs(u + sc) / S.beta) * nrm[q];
+      if (fabs(nrm[0]) > 1.0e-3) {
+        v2[0] = nrm[1]; v2[1] = -nrm[0]; v2[2] = 0.0;
+      } else {
+        v2[0] = 0.0; v2[1] = nrm[2]; v2[2] = -nrm[1];
+      }
+      double l2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+      for (int q = 0; q < 3; q++) v2[q] /= l2;
+      v1[0] = v2[1] * nrm[2] - v2[2] * nrm[1];
+      v1[1] = -(v2[0] * nrm[2] - v2[2] * nrm[0]);
+      v1[2] = v2[0] * nrm[1] - v2[1] * nrm[0];
+      double l1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+      for (int q = 0; q < 3; q++) v1[q] /= l1;
+      const double cm = sqrt(-log(inj_uniform(key, d))) / S.beta, cp = inj_uniform(key, d);
+      const double d1 = S.drift[0] * v1[0] + S.drift[1] * v1[1] + S.drift[2] * v1[2];
+      const double d2 = S.drift[0] * v2[0] + S.drift[1] * v2[1] + S.drift[2] * v2[2];
+      const double kPi2 = 6.283185307179586476925286766559;
+      for (int q = 0; q < 3; q++)
+        v[q] = (cm * sin(kPi2 * cp) + d1) * v1[q] + (cm * cos(kPi2 * cp) + d2) * v2[q] + v3[q];
+      ok = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2] < 0.0;
+    }
+    if (!ok) {
+      atomicAdd(a.flags + 2, 1ull);  // sampling did not finish within its bounds
+      return;
+    }
+    // position on the face, in the block-local cell units of the boundary cell's block
+    int bc[3];
+    float u[3];
+    bc[ax] = hi ? g.nbk[ax] - 1 : 0;
+    u[ax] = hi ? 8.0f : 0.0f;
+    const double pt = (it + c0), pb = (ib + c1);
+    bc[ta] = (int)(pt / 8.0);
+    u[ta] = (float)(pt - 8.0 * bc[ta]);
+    bc[tb] = (int)(pb / 8.0);
+    u[tb] = (float)(pb - 8.0 * bc[tb]);
+    const int b = bc[0] + g.nbk[0] * (bc[1] + g.nbk[1] * bc[2]);
+    // Lapenta2017 for the rest of the step, fields from the block's packed stencil
+    const float frac = (float)((g.dt - tt) / g.dt);
+    float vf[3] = {(float)v[0], (float)v[1], (float)v[2]};
+    {
+      int ic[3];
+      float f[3];
+      for (int q = 0; q < 3; q++) {
+        ic[q] = min(max((int)u[q], 0), AMPS_NC - 1);
+        f[q] = u[q] - (float)ic[q];
+      }
+      float E[3] = {0.f, 0.f, 0.f}, B[3] = {0.f, 0.f, 0.f};
+      for (int cc = 0; cc < 8; cc++) {
+        const int ox = cc & 1, oy = (cc >> 1) & 1, oz = cc >> 2;
+        const float w = (ox ? f[0] : 1.f - f[0]) * (oy ? f[1] : 1.f - f[1]) * (oz ? f[2] : 1.f - f[2]);
+        const float* st = a.st_push + ((size_t)b * AMPS_SC + (ic[0] + ox) + 9 * ((ic[1] + oy) + 9 * (ic[2] + oz))) *
+                                          AMPS_PUSH_STRIDE;
+        E[0] = fmaf(w, st[0], E[0]);
+        E[1] = fmaf(w, st[1], E[1]);
+        E[2] = fmaf(w, st[2], E[2]);
+        B[0] = fmaf(w, st[3], B[0]);
+        B[1] = fmaf(w, st[4], B[1]);
+        B[2] = fmaf(w, st[5], B[2]);
+      }
+      lapenta(a.st.qdt2m[S.spec] * frac, E, B, vf);
+    }
+    // move and locate (periodic wrap, deletion through open faces)
+    int o[3], ic[3];
+    bool far = false;
+    for (int q = 0; q < 3; q++) {
+      float un = fmaf(vf[q], a.dtdx[q] * frac, u[q]);
+      int od = (int)floorf(un * 0.125f);
+      if (od > 1 || od < -1) far = true;
+      od = max(-1, min(1, od));
+      un -= 8.0f * (float)od;
+      un = clamp_below8(fmaxf(un, 0.0f));
+      o[q] = od;
+      u[q] = un;
+      ic[q] = min((int)un, AMPS_NC - 1);
+    }
+    if (far) atomicAdd(a.flags + 0, 1ull);
+    int nbk = b;
+    if (o[0] | o[1] | o[2]) {
+      if (a.open && leaves_open_face(a, b, o)) continue;  // left again at once
+      nbk = __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2]));
+    }
+    const int key2 = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+    const uint32_t idv = (uint32_t)g.step[1] + (uint32_t)atomicAdd(a.flags + 6, 1ull);
+    const int slot = atomicAdd(a.arr + key2, 1);
+    const int cb = a.base[key2], ccap = a.base[key2 + 1] - cb, cn = a.cnt[key2];
+    if (slot < ccap - cn) {
+      const long long dd = (long long)cb + ccap - 1 - slot;
+      for (int q = 0; q < 3; q++) { a.p.u[q][dd] = u[q]; a.p.v[q][dd] = vf[q]; }
+      a.p.sp[dd] = (uint8_t)S.spec;
+      if (a.p.wc) a.p.wc[dd] = 1.0f;
+      if (a.p.id) a.p.id[dd] = idv;
+    } else {
+      const unsigned long long ov = atomicAdd(a.flags + 3, 1ull);
+      if ((long long)ov < a.ovf_cap) {
+        for (int q = 0; q < 3; q++) { a.ovf.u[q][ov] = u[q]; a.ovf.v[q][ov] = vf[q]; }
+        a.ovf.sp[ov] = (uint8_t)S.spec;
+        if (a.ovf.wc) a.ovf.wc[ov] = 1.0f;
+        if (a.ovf.id) a.ovf.id[ov] = idv;
+        a.ovf_key[ov] = key2;
+      } else {
+        atomicAdd(a.flags + 2, 1ull);
+      }
+    }
+  }
+}
+
+__global__ void k_set_next_id(unsigned long long* step, unsigned long long n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) step[1] = n;
+}
+
+// after the injection: next step, ids past the injected ones
+__global__ void k_step_bump(unsigned long long* step, const unsigned long long* flags) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    step[0] += 1ull;
+    step[1] += flags[6];
+  }
 }
 
 // Arrivals: deposit (DEP), move behind the stayers, update the occupancy.
@@ -1243,6 +1447,72 @@ cudaError_t launch_deposit(amps_gpu_ctx* c) {
 
 // Push (+ deposit) of one step: k_push_deposit, k_arrivals (+ assemble).
 // Overflow recovery is done by the caller (particles_recover).
+// ids of injected particles continue after the imported ones (0..n-1)
+void set_next_id(amps_gpu_ctx* c, long long n) {
+  c->next_id = (uint32_t)n;
+  if (c->d_step) k_set_next_id<<<1, 32, 0, c->stream>>>(c->d_step, (unsigned long long)n);
+}
+
+// CalculateInjectionRate_MaxwellianDistribution (src/pic/pic_bc.cpp:215-242):
+// number flux through a face of outward normal n of a Maxwellian with number
+// density, bulk velocity and beta = 1 / (sqrt(2) vth)
+static double maxwellian_flux(double density, const double drift[3], double beta, const double n[3]) {
+  const double kSqrtPi = 1.7724538509055160273;
+  double vv = 0.0, vnorm = 0.0;
+  for (int d = 0; d < 3; d++) {
+    vv += drift[d] * drift[d];
+    vnorm += drift[d] * n[d];
+  }
+  vv = std::sqrt(vv);
+  const double sc = vv * beta;
+  if (sc > 10.0 && vnorm < 0.0) return std::fabs(vnorm) * density;
+  if (sc > 10.0 && vnorm > 0.0) return 0.0;
+  double aa;
+  if (vv > 1.0e-6) {
+    const double cc = -vnorm / vv;
+    aa = (std::exp(-sc * sc * cc * cc) + kSqrtPi * sc * cc * (1.0 + std::erf(sc * cc))) / (2.0 * kSqrtPi);
+  } else {
+    aa = 1.0 / (2.0 * kSqrtPi);
+  }
+  return std::fabs(aa) * density / beta;
+}
+
+cudaError_t launch_inject(amps_gpu_ctx* c, const StepArgs& a) {
+  InjArgs g{};
+  g.nsrc = (int)std::min<size_t>(c->inj.size(), kMaxInj);
+  const int nbk[3] = {c->cfg.nbx, c->cfg.nby, c->cfg.nbz};
+  int first = 0;
+  for (int s = 0; s < g.nsrc; s++) {
+    const amps_gpu_ctx::InjSource& S = c->inj[(size_t)s];
+    InjDev& D = g.src[s];
+    const int ax = S.face >> 1, ta = (ax + 1) % 3, tb = (ax + 2) % 3;
+    D.face = S.face;
+    D.spec = S.spec;
+    D.ncell = 64 * nbk[ta] * nbk[tb];
+    D.first = first;
+    first += D.ncell;
+    D.beta = 1.0 / (std::sqrt(2.0) * S.vth);
+    for (int d = 0; d < 3; d++) D.drift[d] = S.drift[d];
+    double n[3] = {0.0, 0.0, 0.0};
+    n[ax] = (S.face & 1) ? 1.0 : -1.0;
+    D.rate = maxwellian_flux(S.density, S.drift, D.beta, n) / c->cfg.weight[S.spec];
+  }
+  g.nthreads = first;
+  g.dt = c->cfg.dt;
+  for (int d = 0; d < 3; d++) {
+    g.dx[d] = c->cfg.dx[d];
+    g.nbk[d] = nbk[d];
+  }
+  g.seed = c->inj_seed;
+  g.step = c->d_step;
+  {
+    TimedLaunch t(c, "inject", 2);
+    k_inject<<<(unsigned)((g.nthreads + 127) / 128), 128, 0, c->stream>>>(a, g);
+    k_step_bump<<<1, 32, 0, c->stream>>>(c->d_step, c->d_flags);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
   set_smem_attrs();
   cudaError_t e;
@@ -1268,6 +1538,9 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  if (!c->inj.empty()) {
+    if ((e = launch_inject(c, a)) != cudaSuccess) return e;
+  }
   {
     TimedLaunch t(c, "arrivals");
     if (deposit)
@@ -1362,6 +1635,7 @@ cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double*
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     c->np = n;
+    set_next_id(c, n);
     return rebuild_from_list(c, n);
   }
   ImportArgs a;
@@ -1380,6 +1654,7 @@ cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double*
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   c->np = n;
+  set_next_id(c, n);
   return rebuild_from_list(c, n);
 }
 
@@ -1395,6 +1670,7 @@ cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* 
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   c->np = n;
+  set_next_id(c, n);
   return rebuild_from_list(c, n);
 }
 

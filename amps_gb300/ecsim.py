@@ -293,6 +293,23 @@ class EcsimContext:
         self._check(self.lib.amps_gpu_set_open_axes(self.h, int(bool(x)), int(bool(y)), int(bool(z))),
                     "set_open_axes")
 
+    def add_injection(self, face, spec, density, vth, drift=(0.0, 0.0, 0.0)):
+        """Maxwellian flux injection through an open face (0 -x .. 5 +z)."""
+        d = np.ascontiguousarray(drift, np.float64)
+        self._check(self.lib.amps_gpu_add_injection(self.h, int(face), int(spec), float(density),
+                                                    ptr(d, C.c_double), float(vth)), "add_injection")
+
+    def clear_injection(self):
+        self._check(self.lib.amps_gpu_clear_injection(self.h), "clear_injection")
+
+    def set_injection_seed(self, seed):
+        self._check(self.lib.amps_gpu_set_injection_seed(self.h, int(seed)), "set_injection_seed")
+
+    def injected_particles(self):
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_injected_particles(self.h, C.byref(n)), "injected_particles")
+        return n.value
+
     def deleted_particles(self):
         n = C.c_longlong()
         self._check(self.lib.amps_gpu_deleted_particles(self.h, C.byref(n)), "deleted_particles")

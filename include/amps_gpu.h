@@ -223,6 +223,23 @@ amps_gpu_status amps_gpu_step(amps_gpu_ctx* ctx, double tol, int maxit, int prec
  * since creation (amps_gpu_num_particles drops by as many). */
 amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* ctx, int open_x, int open_y, int open_z);
 amps_gpu_status amps_gpu_deleted_particles(amps_gpu_ctx* ctx, long long* total);
+/* Injection through an open face (the OpenFlow boundary, pic_bc.cpp:330-420),
+ * uniform meshes: every particle step injects on each boundary cell face of
+ * `face` (0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z; its axis must be open) the
+ * particles of species `spec` that a Maxwellian of number density `density`,
+ * bulk velocity drift[3] (NULL: 0) and thermal speed vth = sqrt(kT/m) sends
+ * through it in dt (CalculateInjectionRate_MaxwellianDistribution,
+ * pic_bc.cpp:215, / the species weight): Poisson arrivals in time, uniform on
+ * the face, velocity from InjectMaxwellianDistribution
+ * (pic_vel_distribution.cpp:49), moved by the mover for the rest of the step
+ * and deposited with the others.  Up to 8 sources.  Random numbers come from
+ * counter-based streams keyed by the seed, the step, the source and the face
+ * cell; injected particles get ids after the imported ones. */
+amps_gpu_status amps_gpu_add_injection(amps_gpu_ctx* ctx, int face, int spec, double density,
+                                       const double* drift, double vth);
+amps_gpu_status amps_gpu_clear_injection(amps_gpu_ctx* ctx);
+amps_gpu_status amps_gpu_set_injection_seed(amps_gpu_ctx* ctx, unsigned long long seed);
+amps_gpu_status amps_gpu_injected_particles(amps_gpu_ctx* ctx, long long* total);
 /* Species moments on corners (_PIC_FIELD_SOLVER_SAMPLE_SPECIES_ON_CORNER_,
  * ProcessCell pic_field_solver_ecsim.cpp:2270-2303): with sampling on, every
  * deposition (update_j_mass_matrix, push_deposit, step) also forms per corner

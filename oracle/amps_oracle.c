@@ -279,6 +279,155 @@ long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* sp
   return nbad;
 }
 
+/* OpenFlow injection (PIC::BC::ExternalBoundary::OpenFlow, src/pic/pic_bc.cpp:
+ * 330-420) through one face of an open axis: per boundary cell face a Poisson
+ * process in time at CalculateInjectionRate_MaxwellianDistribution (:215) x
+ * area / weight, a uniform point on the face, the velocity of
+ * InjectMaxwellianDistribution (src/pic/pic_vel_distribution.cpp:49-161),
+ * then the Lapenta2017 push for the rest of the step (fields E_half, Bc_prev)
+ * and the location (periodic wrap; gone again through an open face -> not
+ * kept).  Random numbers: the counter-based stream the device uses (a
+ * splitmix64 finaliser over (seed, step, source, face cell, draw)).  Writes up
+ * to cap particles (x, v, block, cell); returns how many were kept. */
+static unsigned long long inj_mix(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static double inj_uniform(unsigned long long key, unsigned* d) {
+  return ((double)(inj_mix(key + ((*d)++)) >> 11) + 0.5) * 1.1102230246251565e-16;
+}
+
+long orc_inject(const orc_mesh* g, int face, int spec, double density, const double drift[3],
+                double vth, unsigned long long seed, unsigned long long step, int src,
+                const double* E_half, const double* Bc_prev, long cap, double* xo, double* vo,
+                int32_t* blk, int32_t* cel) {
+  const int nb[3] = {g->nbx, g->nby, g->nbz};
+  const int ax = face >> 1, hi = face & 1, ta = (ax + 1) % 3, tb = (ax + 2) % 3;
+  const double beta = 1.0 / (sqrt(2.0) * vth);
+  double nrm[3] = {0, 0, 0};
+  nrm[ax] = hi ? 1.0 : -1.0;
+  /* CalculateInjectionRate_MaxwellianDistribution */
+  double vv = 0.0, vnorm = 0.0, flux;
+  for (int d = 0; d < 3; d++) { vv += drift[d] * drift[d]; vnorm += drift[d] * nrm[d]; }
+  vv = sqrt(vv);
+  {
+    const double sq = 1.7724538509055160273, sc = vv * beta;
+    if (sc > 10.0 && vnorm < 0.0) flux = fabs(vnorm) * density;
+    else if (sc > 10.0 && vnorm > 0.0) flux = 0.0;
+    else {
+      double aa;
+      if (vv > 1.0e-6) {
+        const double cc = -vnorm / vv;
+        aa = (exp(-sc * sc * cc * cc) + sq * sc * cc * (1.0 + erf(sc * cc))) / (2.0 * sq);
+      } else {
+        aa = 1.0 / (2.0 * sq);
+      }
+      flux = fabs(aa) * density / beta;
+    }
+  }
+  const double R = (flux / g->w[spec]) * (g->dx[ta] * g->dx[tb]);  /* the device's order */
+  const int NT = NC * nb[ta], ncell = NT * NC * nb[tb];
+  long kept = 0;
+  if (!(R > 0.0)) return 0;
+  for (int c = 0; c < ncell; c++) {
+    const int it = c % NT, ib = c / NT;
+    const unsigned long long key =
+        inj_mix(inj_mix(inj_mix(seed) ^ step) ^ (((unsigned long long)src << 40) | (unsigned long long)c));
+    unsigned d = 0;
+    double tt = 0.0;
+    for (int k = 0; k < 4096; k++) {
+      tt += -log(inj_uniform(key, &d)) / R;
+      if (tt >= g->dt) break;
+      const double c0 = inj_uniform(key, &d), c1 = inj_uniform(key, &d);
+      double v[3] = {0, 0, 0};
+      int ok = 0;
+      for (int outer = 0; outer < 64 && !ok; outer++) {
+        const double dot = drift[0] * nrm[0] + drift[1] * nrm[1] + drift[2] * nrm[2];
+        const double sc = beta * fabs(dot);
+        double u = 0.0, acc = 0.0;
+        int got = 0;
+        for (int tries = 0; tries < 4096 && !got; tries++) {
+          if (dot <= 0.0) {
+            int q = 0;
+            do u = -10.0 + 20.0 * inj_uniform(key, &d); while (u + sc <= 0.0 && ++q < 4096);
+            const double cc = sqrt(2.0 + sc * sc);
+            acc = 2.0 * (u + sc) / (sc + cc) * exp(0.5 + 0.5 * sc * (sc - cc) - u * u);
+          } else {
+            int q = 0;
+            do u = -10.0 + 20.0 * inj_uniform(key, &d); while (u + sc >= 0.0 && ++q < 4096);
+            const double cc = 0.5 * (-sqrt(sc * sc + 2.0) - sc);
+            acc = (u + sc) * exp(-u * u) / (cc + sc) / exp(-cc * cc);
+          }
+          got = !(acc < inj_uniform(key, &d));
+        }
+        if (!got) break;
+        double v1[3], v2[3], v3[3];
+        for (int q = 0; q < 3; q++) v3[q] = -(fabs(u + sc) / beta) * nrm[q];
+        if (fabs(nrm[0]) > 1.0e-3) { v2[0] = nrm[1]; v2[1] = -nrm[0]; v2[2] = 0.0; }
+        else { v2[0] = 0.0; v2[1] = nrm[2]; v2[2] = -nrm[1]; }
+        double l2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+        for (int q = 0; q < 3; q++) v2[q] /= l2;
+        v1[0] = v2[1] * nrm[2] - v2[2] * nrm[1];
+        v1[1] = -(v2[0] * nrm[2] - v2[2] * nrm[0]);
+        v1[2] = v2[0] * nrm[1] - v2[1] * nrm[0];
+        double l1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+        for (int q = 0; q < 3; q++) v1[q] /= l1;
+        const double cm = sqrt(-log(inj_uniform(key, &d))) / beta, cp = inj_uniform(key, &d);
+        const double d1 = drift[0] * v1[0] + drift[1] * v1[1] + drift[2] * v1[2];
+        const double d2 = drift[0] * v2[0] + drift[1] * v2[1] + drift[2] * v2[2];
+        for (int q = 0; q < 3; q++)
+          v[q] = (cm * sin(2.0 * PI_D * cp) + d1) * v1[q] + (cm * cos(2.0 * PI_D * cp) + d2) * v2[q] + v3[q];
+        ok = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2] < 0.0;
+      }
+      if (!ok) return -1;
+      /* the face point, then the push for the rest of the step */
+      double x[3];
+      x[ax] = g->x0[ax] + (hi ? nb[ax] * NC * g->dx[ax] : 0.0);
+      x[ta] = g->x0[ta] + (it + c0) * g->dx[ta];
+      x[tb] = g->x0[tb] + (ib + c1) * g->dx[tb];
+      int bxyz[3], iX[3], nd[8][3];
+      double xmin[3], wt[8], wn[8], xs[3] = {x[0], x[1], x[2]};
+      int bb[3];
+      for (int q = 0; q < 3; q++) {
+        bb[q] = (int)floor((x[q] - g->x0[q]) / (NC * g->dx[q]));
+        if (bb[q] >= nb[q]) bb[q] = nb[q] - 1;
+        if (bb[q] < 0) bb[q] = 0;
+      }
+      block_geom(g, bb[0] + g->nbx * (bb[1] + g->nby * bb[2]), bxyz, xmin);
+      corner_stencil(xmin, g->dx, xs, wt, wn, nd, iX);
+      double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+      for (int s = 0; s < 8; s++) {
+        long ci = cidx(g, bxyz[0] * NC + iX[0] + nd[s][0], bxyz[1] * NC + iX[1] + nd[s][1],
+                       bxyz[2] * NC + iX[2] + nd[s][2]);
+        for (int q = 0; q < 3; q++) { E[q] += wn[s] * E_half[3 * ci + q]; B[q] += wn[s] * Bc_prev[3 * ci + q]; }
+      }
+      const double drem = g->dt - tt;
+      const double h = 0.5 * g->q[spec] * drem / g->m[spec];
+      double alpha[9], vF[3];
+      alpha_matrix(h, B, alpha);
+      for (int i = 0; i < 3; i++) {
+        double vp = 0.0;
+        for (int j = 0; j < 3; j++) vp += alpha[3 * i + j] * (v[j] + h * E[j]);
+        vF[i] = 2.0 * vp - v[i];
+      }
+      for (int q = 0; q < 3; q++) x[q] += drem * vF[q];
+      int gone = 0;
+      for (int q = 0; q < 3; q++)
+        if (((orc_open_axes >> q) & 1) && (x[q] < g->x0[q] || x[q] >= g->x0[q] + nb[q] * NC * g->dx[q]))
+          gone = 1;
+      if (gone) continue;
+      if (kept < cap) {
+        locate_one(g, x, blk + kept, cel + kept);
+        for (int q = 0; q < 3; q++) { xo[3 * kept + q] = x[q]; vo[3 * kept + q] = vF[q]; }
+      }
+      kept++;
+    }
+  }
+  return kept;
+}
+
 /* Mover::Relativistic::Boris (src/pic/pic_mover_relativistic_boris.cpp:16-583,
  * scalar path :119-175) on the mesh fields: sub-steps of dt = min(1/f_g,
  * remaining) with f_g = |q||B|/(2 pi m gamma) (specfunc.h:1290), fields at the

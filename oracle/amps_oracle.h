@@ -67,6 +67,12 @@ void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor);
 /* open axes (bit d): particles leaving the domain through their faces are
  * deleted by the pushes (block = cell = -1), on uniform and AMR meshes */
 void orc_set_open_axes(int mask);
+/* OpenFlow injection through one face (see amps_oracle.c): up to cap new
+ * particles; returns the number kept, -1 if the velocity sampling ran out */
+long orc_inject(const orc_mesh* g, int face, int spec, double density, const double drift[3],
+                double vth, unsigned long long seed, unsigned long long step, int src,
+                const double* E_half, const double* Bc_prev, long cap, double* xo, double* vo,
+                int32_t* blk, int32_t* cel);
 /* species moments on corners (ProcessCell :2270-2303): out[corner][10*nspec] */
 void orc_species_moments(const orc_mesh* g, long n, const double* x, const double* v,
                          const uint8_t* spec, const double* wcorr, const int32_t* block,

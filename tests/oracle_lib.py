@@ -47,6 +47,9 @@ def load():
         "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
         "orc_species_moments": (None, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D]),
         "orc_set_open_axes": (None, [C.c_int]),
+        "orc_inject": (C.c_long, [C.POINTER(Mesh), C.c_int, C.c_int, C.c_double, D, C.c_double,
+                                  C.c_ulonglong, C.c_ulonglong, C.c_int, D, D, C.c_long, D, D, I32,
+                                  I32]),
         "orc_center_to_corner": (None, [C.POINTER(Mesh), D, D]),
         "orc_rhs": (None, [C.POINTER(Mesh), D, D, D, D, D]),
         "orc_matvec": (None, [C.POINTER(Mesh), D, D, D]),
