@@ -43,6 +43,18 @@ class Config(C.Structure):
     ]
 
 
+class RecordLayout(C.Structure):
+    """amps_gpu_record_layout: the caller's particle record (ParticleDataLength
+    and the offsets of velocity, position, species, weight correction or -1)"""
+    _fields_ = [("record_length", C.c_int), ("off_velocity", C.c_int), ("off_position", C.c_int),
+                ("off_species", C.c_int), ("off_weight", C.c_int)]
+
+    @classmethod
+    def basic(cls, weight_correction=False):
+        """picParticleBasicOffset.cpp: next, prev, v, x, species [, weight correction]"""
+        return cls(80, 16, 40, 64, 72) if weight_correction else cls(65, 16, 40, 64, -1)
+
+
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("converged", C.c_int),
                 ("rel_residual", C.c_double), ("wave_energy", C.c_double)]
@@ -91,6 +103,13 @@ SIGNATURES = {
     "amps_gpu_set_injection_seed": (C.c_int, [P, C.c_ulonglong]),
     "amps_gpu_injected_particles": (C.c_int, [P, LL]),
     "amps_gpu_export_species_moments": (C.c_int, [P, D]),
+    "amps_gpu_restart_particle_bytes": (C.c_int, [P, C.POINTER(RecordLayout), C.c_int, LL]),
+    "amps_gpu_write_restart_particles": (C.c_int, [P, C.POINTER(RecordLayout), I32, P, C.c_int, P,
+                                                   C.c_longlong, LL]),
+    "amps_gpu_read_restart_particles": (C.c_int, [P, C.POINTER(RecordLayout), P, C.c_longlong, P,
+                                                  C.c_int, LL]),
+    "amps_gpu_particle_checksum": (C.c_int, [P, C.POINTER(RecordLayout), I32,
+                                             C.POINTER(C.c_ulonglong)]),
     "amps_gpu_export_particles": (C.c_int, [P, D, D, U8, I32, I32, U32, LL]),
     "amps_gpu_num_particles": (C.c_int, [P, LL]),
     "amps_gpu_import_fields": (C.c_int, [P, D, D, D, D, D]),

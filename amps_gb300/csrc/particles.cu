@@ -1362,6 +1362,8 @@ cudaError_t scan_ints(amps_gpu_ctx* c, const int* in, int* out, long long n) {
   return cudaGetLastError();
 }
 
+}  // namespace
+
 // Counting sort of the list buffer (cur^1, keys in d_key) with n particles into
 // the slotted layout of buffer cur.
 cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
@@ -1373,6 +1375,17 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
     TimedLaunch t(c, "rebuild");
     k_rb_rank<<<grid_for(n, 256), 256, 0, s>>>(n, c->d_key, c->d_rank, c->d_count);
   }
+  return place_ranked(c, n);
+}
+
+// Second half of the counting sort: d_count holds the per-cell counts and
+// d_key/d_rank each list entry's cell and rank in it; lays out buffer cur with
+// slack and scatters the list buffer (cur^1) into it.  The restart reader
+// fills the ranks itself, so that each cell keeps the list order of the file.
+cudaError_t place_ranked(amps_gpu_ctx* c, long long n) {
+  cudaStream_t s = c->stream;
+  const long long nc = c->ncor;
+  cudaError_t e;
   // slack scaled so that sum(cap) <= slots: sum(cap) <= n + n/4 + AMPS_SLACK_MIN nc
   const long long worst = n + n / 4 + (long long)AMPS_SLACK_MIN * nc;
   int num = 1, den = 1;
@@ -1397,8 +1410,6 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
   if (e != cudaSuccess) return e;
   return cudaMemsetAsync(c->d_arr, 0, sizeof(int) * nc, s);
 }
-
-}  // namespace
 
 // ===========================================================================
 // launchers

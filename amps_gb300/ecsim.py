@@ -330,6 +330,63 @@ class EcsimContext:
                     "export_species_moments")
         return out
 
+    # ---- restart particle section (pic_restart.cpp) -------------------------
+    def _restart_args(self, layout, block_order, node_ids):
+        layout = layout if layout is not None else _capi.RecordLayout.basic(False)
+        bo = None
+        if block_order is not None:
+            bo = np.ascontiguousarray(block_order, np.int32)
+            if bo.shape != (self.nblocks,):
+                raise ValueError("block_order must hold every block once")
+        if node_ids is None:  # the block index as a 64-bit node id
+            node_ids = np.arange(self.nblocks, dtype=np.int64).view(np.uint8).reshape(self.nblocks, 8)
+        node_ids = np.ascontiguousarray(node_ids, np.uint8)
+        if node_ids.ndim != 2 or node_ids.shape[0] != self.nblocks:
+            raise ValueError("node_ids must be (nblocks, id_length) bytes")
+        return layout, bo, node_ids
+
+    def restart_particle_bytes(self, layout=None, id_length=8):
+        layout = layout if layout is not None else _capi.RecordLayout.basic(False)
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_restart_particle_bytes(self.h, C.byref(layout), id_length,
+                                                             C.byref(n)), "restart_particle_bytes")
+        return n.value
+
+    def write_restart_particles(self, layout=None, block_order=None, node_ids=None):
+        """The particle section of a restart file (SaveParticleData) as uint8 bytes;
+        node_ids (nblocks, id_length) uint8 are the blocks' cAMRnodeID bytes"""
+        layout, bo, ids = self._restart_args(layout, block_order, node_ids)
+        out = np.empty(self.restart_particle_bytes(layout, ids.shape[1]), np.uint8)
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_write_restart_particles(
+            self.h, C.byref(layout), ptr(bo, C.c_int32), ids.ctypes.data_as(C.c_void_p), ids.shape[1],
+            out.ctypes.data_as(C.c_void_p), out.size, C.byref(n)), "write_restart_particles")
+        return out[:n.value]
+
+    def read_restart_particles(self, data, layout=None, node_ids=None):
+        """Replace the particles by those of a particle section (ReadParticleData)."""
+        layout, _, ids = self._restart_args(layout, None, node_ids)
+        data = np.ascontiguousarray(np.frombuffer(data, np.uint8) if isinstance(data, (bytes, bytearray))
+                                    else data, np.uint8)
+        n = C.c_longlong()
+        self._check(self.lib.amps_gpu_read_restart_particles(
+            self.h, C.byref(layout), data.ctypes.data_as(C.c_void_p), data.size,
+            ids.ctypes.data_as(C.c_void_p), ids.shape[1], C.byref(n)), "read_restart_particles")
+        # the species weights come from the section (GlobalParticleWeight)
+        w = data[51:51 + 8 * self.cfg.nspec].view(np.float64)
+        for i in range(self.cfg.nspec):
+            self.cfg.weight[i] = float(w[i])
+        return n.value
+
+    def particle_checksum(self, layout=None, block_order=None):
+        """GetParticleDataCheckSum: the reference's CRC32 (64-bit accumulator) over
+        the records with zeroed links, blocks in block_order, cells i, j, k"""
+        layout, bo, _ = self._restart_args(layout, block_order, None)
+        v = C.c_ulonglong()
+        self._check(self.lib.amps_gpu_particle_checksum(self.h, C.byref(layout), ptr(bo, C.c_int32),
+                                                        C.byref(v)), "particle_checksum")
+        return v.value
+
     def export_cell_moments(self, with_m=True, out=None):
         """per-cell ProcessCell partials (cells in block order): cellJ (ncells, 24),
         cellM (ncells, 324) or None; out=(J, M) reuses arrays"""

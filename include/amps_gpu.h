@@ -251,6 +251,55 @@ amps_gpu_status amps_gpu_injected_particles(amps_gpu_ctx* ctx, long long* total)
  * as a corner). */
 amps_gpu_status amps_gpu_set_species_moments(amps_gpu_ctx* ctx, int on);
 amps_gpu_status amps_gpu_export_species_moments(amps_gpu_ctx* ctx, double* out);
+
+/* Particle record of the caller's build (picParticleBasicOffset.cpp:160-200):
+ * its length (ParticleDataLength) and the byte offsets of the velocity
+ * (3 double), position (3 double), species (unsigned char) and weight
+ * correction (double; -1 when the build has none).  The first 16 bytes are the
+ * next/prev list links.  Basic build: {65, 16, 40, 64, -1}; with the weight
+ * correction {80, 16, 40, 64, 72} (8-byte alignment of the offset). */
+typedef struct {
+  int record_length;
+  int off_velocity;
+  int off_position;
+  int off_species;
+  int off_weight;
+} amps_gpu_record_layout;
+/* Particle section of a restart file (PIC::Restart::SaveParticleData,
+ * pic_restart.cpp:248-310, SaveParticleDataBlock :312-382): the end-of-user-
+ * data marker, ParticleDataLength (long int), the species weights, then for
+ * each block holding particles, in block_order (NULL: block index order; the
+ * reference's tree order is the caller's), its node id (id_length bytes taken
+ * from node_ids[block*id_length], the caller's cAMRnodeID), the count, the
+ * ParticleNumberTable[i][j][k] and the records of cells i, j, k in reverse
+ * list order.  List links are written as zero; fields the device does not
+ * hold are zero.  Records are packed on the device; out is host memory of at
+ * least restart_particle_bytes(). */
+amps_gpu_status amps_gpu_restart_particle_bytes(amps_gpu_ctx* ctx, const amps_gpu_record_layout* layout,
+                                                int id_length, long long* bytes);
+amps_gpu_status amps_gpu_write_restart_particles(amps_gpu_ctx* ctx, const amps_gpu_record_layout* layout,
+                                                 const int32_t* block_order, const void* node_ids,
+                                                 int id_length, void* out, long long capacity,
+                                                 long long* written);
+/* PIC::Restart::ReadParticleData (pic_restart.cpp:515-575,
+ * ReadParticleDataBlock :430-512): replaces the particles by those of a
+ * particle section (node ids mapped to blocks through node_ids), each cell in
+ * the list order it had when saved; the species weights are taken from the
+ * section.  Unpacked on the device.  A record whose position lies outside the
+ * cell of its table entry, or whose species is out of range, is counted and
+ * reported as AMPS_GPU_INVALID_ARG after loading (position clamped into the
+ * cell, species 0). */
+amps_gpu_status amps_gpu_read_restart_particles(amps_gpu_ctx* ctx, const amps_gpu_record_layout* layout,
+                                                const void* data, long long size, const void* node_ids,
+                                                int id_length, long long* nread);
+/* PIC::Restart::GetParticleDataCheckSum (pic_restart.cpp:578-660): the CRC32
+ * class of specfunc.h:438-505 (polynomial 0x04C11DB7, initial value 0, its
+ * 64-bit accumulator) over every particle record with zeroed links
+ * (GetParticleSignature, pic_pbuffer.cpp:1109-1123), blocks in block_order,
+ * cells i, j, k, list order.  Per-record CRCs are formed on the device and
+ * combined with the CRC append operator. */
+amps_gpu_status amps_gpu_particle_checksum(amps_gpu_ctx* ctx, const amps_gpu_record_layout* layout,
+                                           const int32_t* block_order, unsigned long long* checksum);
 /* Particle push + re-bin + deposit only (the particle-steps/s hot path). */
 amps_gpu_status amps_gpu_push_deposit(amps_gpu_ctx* ctx, double* particle_energy);
 /* GMRES inner operator precision: 0 FP32 arithmetic with FP64 refinement at

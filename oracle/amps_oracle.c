@@ -993,3 +993,144 @@ long orc_trace(long n, double* x, double* p, int32_t* status, int64_t* steps, do
   }
   return total;
 }
+
+/* ===========================================================================
+ * Restart particle section and its checksum
+ * ======================================================================== */
+
+/* CRC32::generare_crc_table (specfunc.h:449-459): the remainder of each byte
+ * value placed in bits 24..31, in a 64-bit word that keeps the bits the eight
+ * shifts move above bit 31. */
+void orc_crc32_table(uint64_t t[256]) {
+  for (int i = 0; i < 256; i++) {
+    uint64_t a = (uint64_t)i << 24;
+    for (int j = 0; j < 8; j++) a = (a & 0x80000000ull) ? (a << 1) ^ 0x04c11db7ull : a << 1;
+    t[i] = a;
+  }
+}
+
+/* CRC32::add (specfunc.h:471-480): index = bits 24..31 of the accumulator xor
+ * the byte; accumulator = (accumulator << 8) xor table[index], all 64 bits. */
+uint64_t orc_crc32_add(uint64_t acc, const uint8_t* p, long n) {
+  uint64_t t[256];
+  orc_crc32_table(t);
+  for (long q = 0; q < n; q++) acc = (acc << 8) ^ t[((acc >> 24) ^ p[q]) & 0xffu];
+  return acc;
+}
+
+/* one record: links (bytes 0..15) and every field the path does not hold are
+ * zero (GetParticleSignature with IncludeListInfo=false clones the particle
+ * into a zeroed buffer keeping its zero links, pic_pbuffer.cpp:1109-1123) */
+static void orc_record(const orc_record_layout* L, const double* x, const double* v, uint8_t sp,
+                       double w, uint8_t* rec) {
+  memset(rec, 0, (size_t)L->len);
+  memcpy(rec + L->off_v, v, 24);
+  memcpy(rec + L->off_x, x, 24);
+  rec[L->off_sp] = sp;
+  if (L->off_w >= 0) memcpy(rec + L->off_w, &w, 8);
+}
+
+/* particles grouped by block (in file order) and reference cell order
+ * (i slowest, i.e. ParticleNumberTable[i][j][k]); stable, so each cell keeps
+ * its list order.  Returns the permutation; start[] gets the group offsets of
+ * the nb*512 (block position, i, j, k) groups. */
+static long* orc_group(int nb, const int32_t* block_order, long n, const int32_t* block,
+                       const int32_t* cell, long** start_out) {
+  int* pos = (int*)malloc(sizeof(int) * (size_t)nb);
+  for (int q = 0; q < nb; q++) pos[block_order ? block_order[q] : q] = q;
+  const long ng = (long)nb * 512;
+  long* start = (long*)calloc((size_t)ng + 1, sizeof(long));
+  long* key = (long*)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
+  for (long p = 0; p < n; p++) {
+    const int l = cell[p], i = l % 8, j = (l / 8) % 8, k = l / 64;
+    key[p] = (long)pos[block[p]] * 512 + i * 64 + j * 8 + k;
+    start[key[p] + 1]++;
+  }
+  for (long g = 0; g < ng; g++) start[g + 1] += start[g];
+  long* fill = (long*)malloc(sizeof(long) * (size_t)ng);
+  memcpy(fill, start, sizeof(long) * (size_t)ng);
+  long* perm = (long*)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
+  for (long p = 0; p < n; p++) perm[fill[key[p]]++] = p;
+  free(fill);
+  free(key);
+  free(pos);
+  *start_out = start;
+  return perm;
+}
+
+/* PIC::Restart::SaveParticleData / SaveParticleDataBlock (pic_restart.cpp:
+ * 248-382): marker, ParticleDataLength, GlobalParticleWeight; per block with
+ * particles its node id, count and ParticleNumberTable, then the records of
+ * each cell from the list tail to its head (:352-371). */
+long long orc_restart_pack(const orc_record_layout* L, int nb, const int32_t* block_order,
+                           const uint8_t* node_ids, int id_len, int nspec, const double* weight,
+                           long n, const double* x, const double* v, const uint8_t* spec,
+                           const double* wcorr, const int32_t* block, const int32_t* cell,
+                           uint8_t* out, long long cap) {
+  static const char marker[43] = "PARTICLE-RESTART-FILE--END-USER-ADDITIONAL";
+  long* start;
+  long* perm = orc_group(nb, block_order, n, block, cell, &start);
+  long long size = 43 + 8 + 8LL * nspec;
+  for (int q = 0; q < nb; q++) {
+    const long tot = start[(long)(q + 1) * 512] - start[(long)q * 512];
+    if (tot) size += id_len + 4 + 4 * 512 + tot * (long long)L->len;
+  }
+  if (out && cap < size) {
+    free(perm);
+    free(start);
+    return -1;
+  }
+  if (out) {
+    long long o = 0;
+    const long long len = L->len;
+    memcpy(out, marker, 43);
+    memcpy(out + 43, &len, 8);
+    memcpy(out + 51, weight, 8 * (size_t)nspec);
+    o = 51 + 8LL * nspec;
+    for (int q = 0; q < nb; q++) {
+      const long g0 = (long)q * 512;
+      const int tot = (int)(start[g0 + 512] - start[g0]);
+      if (!tot) continue;
+      const int b = block_order ? block_order[q] : q;
+      if (id_len) memcpy(out + o, node_ids + (size_t)b * id_len, (size_t)id_len);
+      o += id_len;
+      memcpy(out + o, &tot, 4);
+      o += 4;
+      for (int t = 0; t < 512; t++) {
+        const int c = (int)(start[g0 + t + 1] - start[g0 + t]);
+        memcpy(out + o + 4 * t, &c, 4);
+      }
+      o += 4 * 512;
+      for (int t = 0; t < 512; t++)
+        for (long r = start[g0 + t + 1] - 1; r >= start[g0 + t]; r--) {
+          const long p = perm[r];
+          orc_record(L, x + 3 * p, v + 3 * p, spec[p], wcorr ? wcorr[p] : 1.0, out + o);
+          o += L->len;
+        }
+    }
+  }
+  free(perm);
+  free(start);
+  return size;
+}
+
+/* PIC::Restart::GetParticleDataCheckSum (pic_restart.cpp:578-660): one CRC32
+ * object over the blocks in tree order, cells i, j, k, each list head to tail */
+uint64_t orc_particle_checksum(const orc_record_layout* L, int nb, const int32_t* block_order, long n,
+                               const double* x, const double* v, const uint8_t* spec,
+                               const double* wcorr, const int32_t* block, const int32_t* cell) {
+  long* start;
+  long* perm = orc_group(nb, block_order, n, block, cell, &start);
+  uint64_t t[256];
+  orc_crc32_table(t);
+  uint8_t rec[512];
+  uint64_t acc = 0;
+  for (long r = 0; r < n; r++) {
+    const long p = perm[r];
+    orc_record(L, x + 3 * p, v + 3 * p, spec[p], wcorr ? wcorr[p] : 1.0, rec);
+    for (int q = 0; q < L->len; q++) acc = (acc << 8) ^ t[((acc >> 24) ^ rec[q]) & 0xffu];
+  }
+  free(perm);
+  free(start);
+  return acc;
+}

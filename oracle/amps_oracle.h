@@ -96,6 +96,32 @@ int orc_ecsim_step(const orc_mesh* g, long n, double* x, double* v, const uint8_
                    double* E_half, double* Bcen, double* Bcor_prev, double* Bcor_cur,
                    double* J, double* M, double tol, int maxit, int precond, double* diag);
 
+/* ---- restart particle section and checksum (src/pic/pic_restart.cpp) ----
+ * The CRC32 class of src/general/specfunc.h:438-505 in its 64-bit accumulator
+ * (the reference's `unsigned long`).  The class cannot be compiled from the
+ * reference here (specfunc.h needs MPI), so its low half is pinned by the
+ * published check value of the MSB-first 0x04C11DB7 CRC with initial value 0
+ * (CRC-32/POSIX before its final xor) and the high half by the recurrence. */
+void orc_crc32_table(uint64_t t[256]);
+uint64_t orc_crc32_add(uint64_t acc, const uint8_t* p, long n);
+
+typedef struct {
+  int len, off_v, off_x, off_sp, off_w;   /* off_w < 0: no weight correction */
+} orc_record_layout;
+
+/* Particles in any order in which each (block, cell) keeps its list order;
+ * cell = i + 8 (j + 8 k).  blocks in block_order (NULL: 0..nb-1).  Returns the
+ * section's size (bytes written when out != NULL, -1 when cap is too small). */
+long long orc_restart_pack(const orc_record_layout* L, int nb, const int32_t* block_order,
+                           const uint8_t* node_ids, int id_len, int nspec, const double* weight,
+                           long n, const double* x, const double* v, const uint8_t* spec,
+                           const double* wcorr, const int32_t* block, const int32_t* cell,
+                           uint8_t* out, long long cap);
+/* GetParticleDataCheckSum over the same particles (links zeroed) */
+uint64_t orc_particle_checksum(const orc_record_layout* L, int nb, const int32_t* block_order, long n,
+                               const double* x, const double* v, const uint8_t* spec,
+                               const double* wcorr, const int32_t* block, const int32_t* cell);
+
 /* ---- relativistic Boris, gridless form (srcEarth/gridless/GridlessParticleMovers.cpp:781) ---- */
 void orc_dipole_b(const double x[3], double b_eq, double r_e, const double b_ext[3], double B[3]);
 long orc_trace(long n, double* x, double* p, int32_t* status, int64_t* steps, double q, double m0,

@@ -21,6 +21,11 @@ class Mesh(C.Structure):
                 ("dt", C.c_double), ("theta", C.c_double)]
 
 
+class RecordLayout(C.Structure):
+    _fields_ = [("len", C.c_int), ("off_v", C.c_int), ("off_x", C.c_int), ("off_sp", C.c_int),
+                ("off_w", C.c_int)]
+
+
 D = C.POINTER(C.c_double)
 I32 = C.POINTER(C.c_int32)
 U8 = C.POINTER(C.c_uint8)
@@ -59,6 +64,11 @@ def load():
         "orc_update_e": (C.c_double, [C.POINTER(Mesh), D, D, D]),
         "orc_ecsim_step": (C.c_int, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D, D,
                                      D, D, D, C.c_double, C.c_int, C.c_int, D]),
+        "orc_crc32_add": (C.c_uint64, [C.c_uint64, U8, C.c_long]),
+        "orc_restart_pack": (C.c_longlong, [C.POINTER(RecordLayout), C.c_int, I32, U8, C.c_int, C.c_int,
+                                            D, C.c_long, D, D, U8, D, I32, I32, U8, C.c_longlong]),
+        "orc_particle_checksum": (C.c_uint64, [C.POINTER(RecordLayout), C.c_int, I32, C.c_long, D, D,
+                                               U8, D, I32, I32]),
         "orc_dipole_b": (None, [D, C.c_double, C.c_double, D, D]),
         "orc_trace": (C.c_long, [C.c_long, D, D, I32, I64, C.c_double, C.c_double, C.c_double,
                                  C.c_double, D, C.c_double, C.c_double, C.c_long, C.c_double,
@@ -177,3 +187,49 @@ def trace(x, pm, q, m0, b_eq, r_e, b_ext, r_in, r_out, max_steps, dphi, dt_max):
     tot = lib.orc_trace(n, p(x), p(pm), p(st, C.c_int32), p(steps, C.c_int64), q, m0, b_eq, r_e,
                         p(ext), r_in, r_out, max_steps, dphi, dt_max, 0)
     return x, pm, st, steps, tot
+
+
+def crc32_add(acc, data):
+    """the reference's CRC32::add over bytes, from accumulator acc (64-bit)"""
+    b = np.ascontiguousarray(np.frombuffer(bytes(data), np.uint8))
+    return int(load().orc_crc32_add(acc, p(b, C.c_uint8), b.size))
+
+
+def _layout(layout):
+    return RecordLayout(layout.record_length, layout.off_velocity, layout.off_position,
+                        layout.off_species, layout.off_weight)
+
+
+def restart_pack(layout, nb, x, v, spec, block, cell, weight, wcorr=None, block_order=None,
+                 node_ids=None):
+    """particle section bytes; particles in an order that keeps each cell's list order"""
+    lib = load()
+    L = _layout(layout)
+    x = np.ascontiguousarray(x, np.float64); v = np.ascontiguousarray(v, np.float64)
+    spec = np.ascontiguousarray(spec, np.uint8)
+    block = np.ascontiguousarray(block, np.int32); cell = np.ascontiguousarray(cell, np.int32)
+    wc = None if wcorr is None else np.ascontiguousarray(wcorr, np.float64)
+    bo = None if block_order is None else np.ascontiguousarray(block_order, np.int32)
+    if node_ids is None:
+        node_ids = np.arange(nb, dtype=np.int64).view(np.uint8).reshape(nb, 8)
+    ids = np.ascontiguousarray(node_ids, np.uint8)
+    w = np.ascontiguousarray(weight, np.float64)
+    args = (C.byref(L), nb, p(bo, C.c_int32), p(ids, C.c_uint8), ids.shape[1], w.size, p(w),
+            x.shape[0], p(x), p(v), p(spec, C.c_uint8), p(wc), p(block, C.c_int32), p(cell, C.c_int32))
+    size = lib.orc_restart_pack(*args, None, 0)
+    out = np.zeros(size, np.uint8)
+    assert lib.orc_restart_pack(*args, p(out, C.c_uint8), size) == size
+    return out
+
+
+def particle_checksum(layout, nb, x, v, spec, block, cell, wcorr=None, block_order=None):
+    lib = load()
+    L = _layout(layout)
+    x = np.ascontiguousarray(x, np.float64); v = np.ascontiguousarray(v, np.float64)
+    spec = np.ascontiguousarray(spec, np.uint8)
+    block = np.ascontiguousarray(block, np.int32); cell = np.ascontiguousarray(cell, np.int32)
+    wc = None if wcorr is None else np.ascontiguousarray(wcorr, np.float64)
+    bo = None if block_order is None else np.ascontiguousarray(block_order, np.int32)
+    return int(lib.orc_particle_checksum(C.byref(L), nb, p(bo, C.c_int32), x.shape[0], p(x), p(v),
+                                         p(spec, C.c_uint8), p(wc), p(block, C.c_int32),
+                                         p(cell, C.c_int32)))
