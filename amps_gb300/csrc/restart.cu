@@ -129,44 +129,68 @@ struct PackArgs {
   uint32_t* crc;             // per-record CRC in list order (may be null)
 };
 
-// one warp per cell, one lane per particle
-__global__ void __launch_bounds__(256) k_pack(PackArgs a) {
+// One warp per cell, 32 particles at a time: each lane builds its record in
+// the warp's shared staging area, placed so that the staged bytes are the
+// file's bytes for these records (reverse list order); the warp then stores
+// them as aligned 32-bit words (bytes at the ragged ends), so one store
+// instruction writes 128 contiguous bytes.  Each lane forms its record's CRC
+// from the staged bytes.
+constexpr int kPackThreads = 128;
+
+__global__ void __launch_bounds__(kPackThreads) k_pack(PackArgs a) {
+  extern __shared__ uint8_t s_dyn[];
   __shared__ uint32_t s_tab[256];
-  const uint32_t* tab = nullptr;
   if (a.crc) {
     for (int q = threadIdx.x; q < 256; q += blockDim.x) {
       uint32_t t = (uint32_t)q << 24;
       for (int j = 0; j < 8; j++) t = (t & 0x80000000u) ? (t << 1) ^ 0x04c11db7u : t << 1;
       s_tab[q] = t;
     }
-    tab = s_tab;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const int len = a.L.len;
+  uint8_t* wrec = s_dyn + (threadIdx.x >> 5) * 32 * len;
   const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
-  uint8_t rec[kMaxRecord];
   for (long long cid = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cid < a.ncell;
        cid += nw) {
     const int b = (int)(cid / AMPS_CPB);
     const int b0 = a.base[cid], n = a.cnt[cid];
-    for (int r = lane; r < n; r += 32) {
-      const long long p = b0 + r;
-      double x[3];
-      float v[3];
-      for (int d = 0; d < 3; d++) {
-        x[d] = a.origin[3 * b + d] + (double)a.u[d][p] * a.bdx[3 * b + d];
-        v[d] = a.v[d][p];
+    for (int r0 = 0; r0 < n; r0 += 32) {
+      const int m = min(32, n - r0);
+      if (lane < m) {
+        const long long p = b0 + r0 + lane;
+        double x[3];
+        float v[3];
+        for (int d = 0; d < 3; d++) {
+          x[d] = a.origin[3 * b + d] + (double)a.u[d][p] * a.bdx[3 * b + d];
+          v[d] = a.v[d][p];
+        }
+        uint8_t* rec = wrec + (m - 1 - lane) * len;
+        make_record(rec, a.L, x, v, a.sp[p], a.wc ? (double)a.wc[p] : 1.0);
+        if (a.crc) {
+          uint32_t c = 0;
+          for (int q = 0; q < len; q++) c = (c << 8) ^ s_tab[((c >> 24) ^ rec[q]) & 0xffu];
+          a.crc[a.cell_rec[cid] + r0 + lane] = c;
+        }
       }
-      make_record(rec, a.L, x, v, a.sp[p], a.wc ? (double)a.wc[p] : 1.0);
+      __syncwarp();
       if (a.out) {
-        uint8_t* dst = a.out + a.cell_byte[cid] + (long long)(n - 1 - r) * a.L.len;
-        for (int q = 0; q < a.L.len; q++) dst[q] = rec[q];
+        // file records n-r0-m .. n-r0-1 hold list positions r0+m-1 .. r0
+        uint8_t* dst = a.out + a.cell_byte[cid] + (long long)(n - r0 - m) * len;
+        const int nbytes = m * len;
+        const int head = min(nbytes, (int)((4 - ((uintptr_t)dst & 3u)) & 3u));
+        const int nword = (nbytes - head) >> 2;
+        const int tail0 = head + 4 * nword;
+        if (lane < head) dst[lane] = wrec[lane];
+        if (lane < nbytes - tail0) dst[tail0 + lane] = wrec[tail0 + lane];
+        uint32_t* dw = reinterpret_cast<uint32_t*>(dst + head);
+        for (int w = lane; w < nword; w += 32) {
+          const uint8_t* q = wrec + head + 4 * w;
+          dw[w] = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) | ((uint32_t)q[3] << 24);
+        }
       }
-      if (a.crc) {
-        uint32_t c = 0;
-        for (int q = 0; q < a.L.len; q++) c = (c << 8) ^ tab[((c >> 24) ^ rec[q]) & 0xffu];
-        a.crc[a.cell_rec[cid] + r] = c;
-      }
+      __syncwarp();
     }
   }
 }
@@ -220,10 +244,17 @@ __device__ __forceinline__ double get_f64(const uint8_t* p) {
   return __longlong_as_double((long long)b);
 }
 
-// one warp per cell: the cell's records (reverse list order in the file) into
-// the list buffer in list order, with key = cell and rank = list position
-__global__ void __launch_bounds__(256) k_unpack(UnpackArgs a) {
+// One warp per cell, 32 records at a time: the warp loads the records' bytes
+// (contiguous in the file, reverse list order) into its shared staging area
+// as aligned 32-bit words, then each lane parses one record into the list
+// buffer in list order, with key = cell and rank = list position.
+constexpr int kUnpackThreads = 128;
+
+__global__ void __launch_bounds__(kUnpackThreads) k_unpack(UnpackArgs a) {
+  extern __shared__ uint8_t s_dyn[];
   const int lane = threadIdx.x & 31;
+  const int len = a.L.len;
+  uint8_t* wrec = s_dyn + (threadIdx.x >> 5) * 32 * len;
   const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long cid = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cid < a.ncell;
        cid += nw) {
@@ -231,32 +262,54 @@ __global__ void __launch_bounds__(256) k_unpack(UnpackArgs a) {
     if (n == 0) continue;
     const int b = (int)(cid / AMPS_CPB), l = (int)(cid % AMPS_CPB);
     const int ci[3] = {l % AMPS_NC, (l / AMPS_NC) % AMPS_NC, l / (AMPS_NC * AMPS_NC)};
-    for (int r = lane; r < n; r += 32) {
-      const uint8_t* rec = a.in + a.cell_byte[cid] + (long long)(n - 1 - r) * a.L.len;
-      const long long q = a.cell_rec[cid] + r;
-      bool outside = false;
-      for (int d = 0; d < 3; d++) {
-        const double ud = (get_f64(rec + a.L.off_x + 8 * d) - a.origin[3 * b + d]) / a.bdx[3 * b + d];
-        float uf = (float)ud;
-        const float lo = (float)ci[d], hi = (float)(ci[d] + 1);
-        if (!(ud >= lo && ud < hi)) outside = true;
-        // keep the slot invariant (the offset lies in the cell's range)
-        if (!(uf >= lo)) uf = lo;
-        if (uf >= hi) uf = __int_as_float(__float_as_int(hi) - 1);
-        a.u[d][q] = uf;
-        a.v[d][q] = (float)get_f64(rec + a.L.off_v + 8 * d);
+    for (int r0 = 0; r0 < n; r0 += 32) {
+      const int m = min(32, n - r0);
+      const uint8_t* src = a.in + a.cell_byte[cid] + (long long)(n - r0 - m) * len;
+      const int nbytes = m * len;
+      const int head = min(nbytes, (int)((4 - ((uintptr_t)src & 3u)) & 3u));
+      const int nword = (nbytes - head) >> 2;
+      const int tail0 = head + 4 * nword;
+      if (lane < head) wrec[lane] = src[lane];
+      if (lane < nbytes - tail0) wrec[tail0 + lane] = src[tail0 + lane];
+      const uint32_t* sw = reinterpret_cast<const uint32_t*>(src + head);
+      for (int w = lane; w < nword; w += 32) {
+        const uint32_t v = sw[w];
+        uint8_t* q = wrec + head + 4 * w;
+        q[0] = (uint8_t)v;
+        q[1] = (uint8_t)(v >> 8);
+        q[2] = (uint8_t)(v >> 16);
+        q[3] = (uint8_t)(v >> 24);
       }
-      uint8_t s = rec[a.L.off_sp];
-      if (s >= a.nspec) {
-        atomicAdd(&a.bad[1], 1ull);
-        s = 0;
+      __syncwarp();
+      if (lane < m) {
+        const int r = r0 + lane;
+        const uint8_t* rec = wrec + (m - 1 - lane) * len;
+        const long long q = a.cell_rec[cid] + r;
+        bool outside = false;
+        for (int d = 0; d < 3; d++) {
+          const double ud = (get_f64(rec + a.L.off_x + 8 * d) - a.origin[3 * b + d]) / a.bdx[3 * b + d];
+          float uf = (float)ud;
+          const float lo = (float)ci[d], hi = (float)(ci[d] + 1);
+          if (!(ud >= lo && ud < hi)) outside = true;
+          // keep the slot invariant (the offset lies in the cell's range)
+          if (!(uf >= lo)) uf = lo;
+          if (uf >= hi) uf = __int_as_float(__float_as_int(hi) - 1);
+          a.u[d][q] = uf;
+          a.v[d][q] = (float)get_f64(rec + a.L.off_v + 8 * d);
+        }
+        uint8_t sp = rec[a.L.off_sp];
+        if (sp >= a.nspec) {
+          atomicAdd(&a.bad[1], 1ull);
+          sp = 0;
+        }
+        if (outside) atomicAdd(&a.bad[0], 1ull);
+        a.sp[q] = sp;
+        if (a.wc) a.wc[q] = (float)get_f64(rec + a.L.off_w);
+        if (a.id) a.id[q] = (uint32_t)q;
+        a.key[q] = (int)cid;
+        a.rank[q] = r;
       }
-      if (outside) atomicAdd(&a.bad[0], 1ull);
-      a.sp[q] = s;
-      if (a.wc) a.wc[q] = (float)get_f64(rec + a.L.off_w);
-      if (a.id) a.id[q] = (uint32_t)q;
-      a.key[q] = (int)cid;
-      a.rank[q] = r;
+      __syncwarp();
     }
   }
 }
@@ -359,6 +412,16 @@ void block_geometry(amps_gpu_ctx* c, std::vector<double>& origin, std::vector<do
   }
 }
 
+// device address of page-locked host memory, or null for pageable memory
+void* mapped_ptr(const void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 template <class T>
 T* dev_upload(const std::vector<T>& h, cudaError_t& e) {
   T* d = nullptr;
@@ -396,8 +459,9 @@ amps_gpu_status run_pack(amps_gpu_ctx* c, const Layout& L, const Plan& P, uint8_
     a.L = L;
     a.out = out_dev;
     a.crc = crc_dev;
-    const long long blocks = std::min<long long>((c->ncor + 7) / 8, 152LL * 16);
-    k_pack<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    const int wpb = kPackThreads / 32;
+    const long long blocks = std::max<long long>(1, std::min<long long>((c->ncor + wpb - 1) / wpb, 152LL * 32));
+    k_pack<<<(unsigned)blocks, kPackThreads, (size_t)wpb * 32 * L.len, c->stream>>>(a);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   }
@@ -437,19 +501,22 @@ amps_gpu_status amps_gpu_write_restart_particles(amps_gpu_ctx* c, const amps_gpu
   amps_gpu_status s = make_plan(c, L, block_order, id_length, P);
   if (s) return s;
   if (capacity < P.total_bytes) return set_err(c, AMPS_GPU_INVALID_ARG, "restart: output buffer too small");
-  uint8_t* d_out = nullptr;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&d_out), (size_t)std::max<long long>(P.total_bytes, 1));
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, (size_t)P.total_bytes, c->stream);
-  if (e != cudaSuccess) {
-    cudaFree(d_out);
-    return cuda_check(c, e, "restart: staging");
+  // records are packed straight into page-locked output, else into device
+  // staging copied out in one transfer; every record byte is written by the
+  // device, the headers by the host afterwards
+  uint8_t* direct = static_cast<uint8_t*>(mapped_ptr(out));
+  uint8_t* d_out = direct;
+  cudaError_t e = cudaSuccess;
+  if (!direct) {
+    e = cudaMalloc(reinterpret_cast<void**>(&d_out), (size_t)std::max<long long>(P.total_bytes, 1));
+    if (e != cudaSuccess) return cuda_check(c, e, "restart: staging");
   }
   s = run_pack(c, L, P, d_out, nullptr);
-  if (!s) {
+  if (!s && !direct) {
     e = cudaMemcpy(out, d_out, (size_t)P.total_bytes, cudaMemcpyDeviceToHost);
     s = cuda_check(c, e, "restart: copy out");
   }
-  cudaFree(d_out);
+  if (!direct) cudaFree(d_out);
   if (s) return s;
   // header and block headers
   uint8_t* o = static_cast<uint8_t*>(out);
@@ -642,10 +709,14 @@ amps_gpu_status amps_gpu_read_restart_particles(amps_gpu_ctx* c, const amps_gpu_
   block_geometry(c, origin, bdx);
   const bool wc = L.off_w >= 0;
   cudaError_t e = cudaSuccess;
+  // page-locked input is read in place by the device, else copied in one transfer
+  const uint8_t* direct = static_cast<const uint8_t*>(mapped_ptr(in));
   uint8_t* d_in = nullptr;
   unsigned long long* d_bad = nullptr;
-  e = cudaMalloc(reinterpret_cast<void**>(&d_in), (size_t)std::max<long long>(size, 1));
-  if (e == cudaSuccess) e = cudaMemcpy(d_in, in, (size_t)size, cudaMemcpyHostToDevice);
+  if (!direct) {
+    e = cudaMalloc(reinterpret_cast<void**>(&d_in), (size_t)std::max<long long>(size, 1));
+    if (e == cudaSuccess) e = cudaMemcpy(d_in, in, (size_t)size, cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_bad), 2 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, 2 * sizeof(unsigned long long), c->stream);
   double* d_origin = dev_upload(origin, e);
@@ -658,7 +729,7 @@ amps_gpu_status amps_gpu_read_restart_particles(amps_gpu_ctx* c, const amps_gpu_
     c->has_wcorr = wc;
     const int o = c->cur ^ 1;
     UnpackArgs a{};
-    a.in = d_in;
+    a.in = direct ? direct : d_in;
     a.cnt = c->d_count;
     a.cell_byte = d_byte;
     a.cell_rec = d_rec;
@@ -677,8 +748,9 @@ amps_gpu_status amps_gpu_read_restart_particles(amps_gpu_ctx* c, const amps_gpu_
     a.key = c->d_key;
     a.rank = c->d_rank;
     a.bad = d_bad;
-    const long long blocks = std::max<long long>(1, std::min<long long>((ncell + 7) / 8, 152LL * 16));
-    k_unpack<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+    const int wpb = kUnpackThreads / 32;
+    const long long blocks = std::max<long long>(1, std::min<long long>((ncell + wpb - 1) / wpb, 152LL * 32));
+    k_unpack<<<(unsigned)blocks, kUnpackThreads, (size_t)wpb * 32 * L.len, c->stream>>>(a);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = place_ranked(c, rec);
     if (e == cudaSuccess) e = cudaMemcpyAsync(bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, c->stream);

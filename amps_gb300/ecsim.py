@@ -352,11 +352,17 @@ class EcsimContext:
                                                              C.byref(n)), "restart_particle_bytes")
         return n.value
 
-    def write_restart_particles(self, layout=None, block_order=None, node_ids=None):
+    def write_restart_particles(self, layout=None, block_order=None, node_ids=None, out=None):
         """The particle section of a restart file (SaveParticleData) as uint8 bytes;
-        node_ids (nblocks, id_length) uint8 are the blocks' cAMRnodeID bytes"""
+        node_ids (nblocks, id_length) uint8 are the blocks' cAMRnodeID bytes; out:
+        a uint8 array of at least restart_particle_bytes() (page-locked: the
+        device writes the records into it directly)"""
         layout, bo, ids = self._restart_args(layout, block_order, node_ids)
-        out = np.empty(self.restart_particle_bytes(layout, ids.shape[1]), np.uint8)
+        need = self.restart_particle_bytes(layout, ids.shape[1])
+        if out is None:
+            out = np.empty(need, np.uint8)
+        elif out.dtype != np.uint8 or not out.flags.c_contiguous or out.size < need:
+            raise ValueError("out must be a contiguous uint8 array of at least %d bytes" % need)
         n = C.c_longlong()
         self._check(self.lib.amps_gpu_write_restart_particles(
             self.h, C.byref(layout), ptr(bo, C.c_int32), ids.ctypes.data_as(C.c_void_p), ids.shape[1],

@@ -448,6 +448,60 @@ def tracer_line(n32, n64, device):
             "status": "0 step budget, 1 r < 1 R_E, 2 r > 10 R_E"}
 
 
+def restart_line(ctx):
+    """Restart particle section of the bench state (SaveParticleData layout,
+    basic 65-byte records) and the reference's particle CRC32 checksum, each
+    through the C ABI with host buffers (wall clock); the section read back
+    must give the same checksum."""
+    from amps_gb300._capi import RecordLayout
+    from amps_gb300.ecsim import PinnedArrays
+    lay = RecordLayout.basic(False)
+    ctx.particle_checksum(lay)
+    t0 = time.perf_counter()
+    ck = ctx.particle_checksum(lay)
+    t1 = time.perf_counter()
+    sec = ctx.write_restart_particles(lay)
+    t2 = time.perf_counter()
+    n = ctx.read_restart_particles(sec, lay)
+    t3 = time.perf_counter()
+    ck2 = ctx.particle_checksum(lay)
+    gb = sec.size / 1e9
+    out = {"particles": int(n), "section_bytes": int(sec.size), "checksum": "0x%x" % ck,
+           "checksum_after_read_back_equal": ck == ck2,
+           "checksum_ms": round((t1 - t0) * 1e3, 2), "checksum_records_per_s": n / (t1 - t0),
+           "pageable": {"write_ms": round((t2 - t1) * 1e3, 2), "read_ms": round((t3 - t2) * 1e3, 2),
+                        "write_gb_per_s": gb / (t2 - t1), "read_gb_per_s": gb / (t3 - t2)},
+           "timing": "wall clock, host buffers, C ABI"}
+    pin = PinnedArrays()
+    try:
+        buf = pin.empty(sec.size, np.uint8)
+        ctx.write_restart_particles(lay, out=buf)
+        t4 = time.perf_counter()
+        ctx.write_restart_particles(lay, out=buf)
+        t5 = time.perf_counter()
+        ctx.read_restart_particles(buf, lay)
+        t6 = time.perf_counter()
+        out["page_locked"] = {"write_ms": round((t5 - t4) * 1e3, 2), "read_ms": round((t6 - t5) * 1e3, 2),
+                              "write_gb_per_s": gb / (t5 - t4), "read_gb_per_s": gb / (t6 - t5),
+                              "bytes_equal": bool(np.array_equal(buf, sec))}
+    finally:
+        pin.free()
+    # the same CRC walk on one host core (the oracle's sequential restatement of
+    # GetParticleDataCheckSum) over a 2M-record sample of synthetic particles
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from tests import oracle_lib as O
+    m = 2_000_000
+    rng = np.random.default_rng(0)
+    xs, vs = rng.uniform(0, 64, (m, 3)), rng.standard_normal((m, 3))
+    sp, blk, cel = np.zeros(m, np.uint8), np.zeros(m, np.int32), rng.integers(0, 512, m).astype(np.int32)
+    t7 = time.perf_counter()
+    O.particle_checksum(lay, 1, xs, vs, sp, blk, cel)
+    t8 = time.perf_counter()
+    out["cpu_baseline"] = {"checksum_records_per_s": m / (t8 - t7), "cores": 1, "kind": "port",
+                           "sample": "oracle CRC32 walk over 2,000,000 synthetic 65-byte records"}
+    return out
+
+
 def oracle_check(workload, device):
     """One full ECSIM step of the workload on the GPU and on the FP64 AMR oracle
     from the same initial state (the oracle starts from the device's FP32 particle
@@ -727,6 +781,7 @@ def run_gpu(args):
     trc = None
     if rank == 0 and args.tracer > 0:
         trc = tracer_line(args.tracer, max(1, args.tracer // 256), local)
+    rst = restart_line(ctx) if (rank == 0 and args.restart) else None
     pab = None
     if rank == 0 and args.precond_ab:
         pab = {"config": precond_ab("ecsim_32c_64ppc", local)}
@@ -746,7 +801,7 @@ def run_gpu(args):
                 "cuda_graphs": args.graphs > 0, "autotune": tuning}),
             "e2e": e2e, "e2e_particle_roundtrip": e2e_particles,
             "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
-            "precond_ab": pab, "tracer": trc, "energy": energy,
+            "precond_ab": pab, "tracer": trc, "energy": energy, "restart": rst,
             "clocks": clocks, "gpu_launches": gpu_launches,
         }
         print(json.dumps(line), flush=True)
@@ -816,6 +871,8 @@ def main():
     ap.add_argument("--tracer", type=int, default=0,
                     help="also run the cutoff tracing workload with this many particles (FP32; "
                          "FP64 on 1/256 of them)")
+    ap.add_argument("--restart", type=int, default=1,
+                    help="also time the restart particle section write/read and checksum")
     ap.add_argument("--precond-kernel", type=int, default=0,
                     help="time only the tensor-core inference kernel on this many blocks")
     ap.add_argument("--traffic", type=float, default=None,

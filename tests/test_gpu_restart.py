@@ -189,3 +189,28 @@ def test_checksum_at_size_matches_oracle():
         x1, v1, sp, blk, cel, _ = _oracle_inputs(exp)
         assert x1.shape[0] > 10 ** 6
         assert ctx.particle_checksum(layout) == O.particle_checksum(layout, ctx.nblocks, x1, v1, sp, blk, cel)
+
+
+def test_page_locked_buffers_give_the_same_section():
+    """page-locked output is written and page-locked input read by the device in
+    place; the bytes and the restored state equal those of pageable buffers"""
+    ctx, wl, _ = _stepped_uniform(seed=73)
+    layout = RecordLayout.basic(False)
+    pin = A.PinnedArrays()
+    try:
+        with ctx:
+            sec = ctx.write_restart_particles(layout)
+            buf = pin.empty(sec.size + 100, np.uint8)
+            buf[:] = 0xAB
+            got = ctx.write_restart_particles(layout, out=buf)
+            np.testing.assert_array_equal(got, sec)
+            assert (buf[sec.size:] == 0xAB).all()
+            c0 = ctx.particle_checksum(layout)
+            exp = ctx.export_particles(ids=False)
+            ctx.read_restart_particles(buf[:sec.size], layout)
+            assert ctx.particle_checksum(layout) == c0
+            e2 = ctx.export_particles(ids=False)
+            for k in ("x", "v", "spec", "block", "cell"):
+                np.testing.assert_array_equal(e2[k], exp[k])
+    finally:
+        pin.free()
