@@ -29,6 +29,8 @@ struct Hang {
   const int* hs;
   const int* hp;
   const double* hw;
+  const float* hwh;  // hw as FP32 pairs
+  const float* hwl;
 };
 
 // value of corner c of a component-major field (component d), P applied,
@@ -51,8 +53,21 @@ __device__ __forceinline__ float cval_f(const float* __restrict__ xf, long long 
   const int s = h.hs[c], e = h.hs[c + 1];
   if (s == e) return xf[d * nvc + c];
   float v = 0.f;
-  for (int t = s; t < e; t++) v = fmaf((float)h.hw[t], xf[d * nvc + h.hp[t]], v);
+  for (int t = s; t < e; t++) v = fmaf(h.hwh[t], xf[d * nvc + h.hp[t]], v);
   return v;
+}
+
+// corner c, component d of a field given as FP32 pairs (xh + xl), P applied in pairs
+__device__ __forceinline__ FF cval_ff(const float* __restrict__ xh, const float* __restrict__ xl,
+                                     long long nvc, int c, int d, const Hang& h) {
+  const int s = h.hs[c], e = h.hs[c + 1];
+  if (s == e) return FF{xh[d * nvc + c], xl[d * nvc + c]};
+  FF v{0.f, 0.f};
+  for (int t = s; t < e; t++) {
+    const long long q = d * nvc + h.hp[t];
+    ff_add2(v, h.hwh[t], h.hwl[t], xh[q], xl[q]);
+  }
+  return ff_norm(v);
 }
 
 // scatter out[8][3] to the cell's corners with P^T
@@ -140,10 +155,23 @@ __device__ __forceinline__ void scatter_row(T* __restrict__ y, long long nvc, co
   }
 }
 
+// per cell size (index log2 of the block's cell size in finest cells): the
+// operator's scale factors, FP32 for the inner operator and as FP32 pairs
+struct LevelK {
+  float dx, V;                       // FP32 inner operator
+  float curl[2], cc[2], id[2], m[2], bb[2];  // 0.25/dx, th2dt2 V 0.25/dx, V/8, f V, thdt V 0.25/dx
+};
+constexpr int kMaxScale = 8;
+
 struct ApplyArgs {
   long long ncell, nvc;
   const int* ctab;
   Hang h;
+  const int* bscale;
+  LevelK lk[kMaxScale];
+  float fj[2];          // f as a pair (the current term of the RHS)
+  const float* xh;      // ACC 1/2 input as FP32 pairs (dinv applied)
+  const float* xl;
   const double* bdx;
   const float* cellM;
   const float* cellJ;
@@ -167,8 +195,8 @@ struct ApplyArgs {
 //          k_amr_finish32), FP32 atomics;
 //   ACC 1: the full operator to FP64 accuracy (outer residuals);
 //   ACC 2: the RHS to FP64 accuracy.
-// ACC 1/2 keep the identity and curl terms in FP64 and evaluate the mass term
-// (most of the arithmetic) in FP32 pairs (FF, common.cuh).
+// ACC 1/2 run in FP32 pairs (FF, common.cuh): FP64 arithmetic is a small
+// fraction of the FP32 rate on this part; the pairs carry FP64 accuracy.
 constexpr int kTileCells = 32;
 constexpr int kTileThreads = 3 * kTileCells;
 constexpr uint32_t kTileBytes = kTileCells * AMPS_CELLM * 4;  // 31,104
@@ -179,11 +207,18 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
   extern __shared__ __align__(16) float s_m[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_cid[kTileCells][8];
-  // corner values (8 corners x 3): FP32 for ACC 0; FP64 and its FP32 pair split for ACC 1/2
+  // corner values (8 corners x 3): FP32 for ACC 0, FP32 pairs for ACC 1/2
   __shared__ float s_eh[kTileCells][24];
   __shared__ float s_el[ACC == 0 ? 1 : kTileCells][24];
-  __shared__ double s_e[ACC == 0 ? 1 : kTileCells][24];
-  __shared__ double s_cu[ACC == 0 ? 1 : kTileCells][3];
+  // the cell's curl (and for the RHS its centre B) as pairs, one component per thread
+  __shared__ float s_cu[ACC == 0 ? 1 : kTileCells][3][2];
+  __shared__ float s_b[ACC == 2 ? kTileCells : 1][3][2];
+  // ACC 0: the tile's 32 cells (an 8 x 4 x 1 slab of a block) share 9 x 5 x 2
+  // corners; their contributions are summed in shared memory first, so each
+  // corner gets one global atomic per component instead of up to 8
+  constexpr int kTC = 90;
+  __shared__ float s_acc[ACC == 0 ? 3 * kTC : 1];
+  __shared__ int s_tcid[ACC == 0 ? kTC : 1];
   const int tid = threadIdx.x, p = tid / kTileCells, lc = tid % kTileCells;
   const long long cell0 = (long long)blockIdx.x * kTileCells;
   if (tid == 0) {
@@ -198,11 +233,26 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
   const long long cell = cell0 + lc;
   const int b = (int)(cell >> 9), l = (int)(cell & 511);
   const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
-  const double dxd = a.bdx[b], Vd = dxd * dxd * dxd;
+  const LevelK& K = a.lk[min(__ffs(a.bscale[b]) - 1, kMaxScale - 1)];
   // the cell's corners and their values, each gathered once by one of its 3
   // threads (thread p: corner ids c = p, p+3, p+6; values of component p)
-  for (int c = p; c < 8; c += 3)
-    s_cid[lc][c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+  // tile-local corner of (cell lc, corner c): the slab's cells are i = 0..7,
+  // j = 4 (lc / 8 - ...) rows, one k
+  auto tcorner = [&](int c) { return (lc % 8 + c_off[c][0]) + 9 * ((lc / 8 + c_off[c][1]) + 5 * c_off[c][2]); };
+  for (int c = p; c < 8; c += 3) {
+    const int id = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+    s_cid[lc][c] = id;
+    if (ACC == 0) s_tcid[tcorner(c)] = id;  // the same id from every cell sharing the corner
+  }
+  if (ACC == 0)
+    for (int q = tid; q < 3 * kTC; q += kTileThreads) s_acc[q] = 0.f;
+  if (ACC == 2) {
+    // centre B, component p, split into a pair (the only FP64 arithmetic besides the scatter)
+    const double Bv = a.Bcen[p * a.ncell + cell];
+    const float bh = (float)Bv;
+    s_b[lc][p][0] = bh;
+    s_b[lc][p][1] = (float)(Bv - (double)bh);
+  }
   __syncthreads();
   int cid[8];
 #pragma unroll
@@ -211,11 +261,9 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
     if (ACC == 0) {
       s_eh[lc][3 * c + p] = cval_f(a.xf, a.nvc, cid[c], p, a.h);
     } else {
-      const double v = cval(a.x, a.dinv, a.nvc, cid[c], p, a.h);
-      const float vh = (float)v;
-      s_e[lc][3 * c + p] = v;
-      s_eh[lc][3 * c + p] = vh;
-      s_el[lc][3 * c + p] = (float)(v - (double)vh);
+      const FF v = cval_ff(a.xh, a.xl, a.nvc, cid[c], p, a.h);
+      s_eh[lc][3 * c + p] = v.s;
+      s_el[lc][3 * c + p] = v.q;
     }
   }
   // CTA-uniform: every thread leaves together on a timeout (later barriers)
@@ -227,7 +275,7 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
   }
   const float* mm = s_m + lc * AMPS_CELLM + 3 * p;  // row p of every monomial block
   if (ACC == 0) {
-    const float dx = (float)dxd, V = (float)Vd;
+    const float dx = K.dx, V = K.V;
     float ef[8][3], out[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) {
@@ -248,16 +296,30 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
         out[c1] += m0 * ef[c2][0] + m1 * ef[c2][1] + m2 * ef[c2][2];
         if (c1 != c2) out[c2] += m0 * ef[c1][0] + m1 * ef[c1][1] + m2 * ef[c1][2];
       }
-    scatter_row<float>(y32, a.nvc, cid, p, out, a.h);
-  } else {
-    const double sg = ACC == 2 ? -1.0 : 1.0;
-    double out[8];
 #pragma unroll
-    for (int c = 0; c < 8; c++) out[c] = ACC == 1 ? 0.125 * Vd * s_e[lc][3 * c + p] : 0.0;
-    // curl of the cell: component p by thread p, shared
+    for (int c = 0; c < 8; c++) atomicAdd(&s_acc[3 * tcorner(c) + p], out[c]);
+    __syncthreads();
+    // one global atomic per tile corner and component (P^T for hanging corners)
+    for (int q = tid; q < 3 * kTC; q += kTileThreads) {
+      const int tc = q / 3, pp = q % 3, cc = s_tcid[tc];
+      const float v = s_acc[q];
+      const int hs0 = a.h.hs[cc], hs1 = a.h.hs[cc + 1];
+      if (hs0 == hs1) {
+        atomicAdd(y32 + pp * a.nvc + cc, v);
+      } else {
+        for (int t = hs0; t < hs1; t++) atomicAdd(y32 + pp * a.nvc + a.h.hp[t], a.h.hwh[t] * v);
+      }
+    }
+  } else {
+    const float sg = ACC == 2 ? -1.f : 1.f;
+    FF out[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      out[c] = ACC == 1 ? ff_mul(s_eh[lc][3 * c + p], s_el[lc][3 * c + p], K.id[0], K.id[1]) : FF{0.f, 0.f};
+    // the curl's component p: cu_p = 0.25/dx (sum +-E_qa - sum +-E_qb)
+    const int qa = p == 0 ? 2 : (p == 1 ? 0 : 1), qb = p == 0 ? 1 : (p == 1 ? 2 : 0);
     {
-      double sa = 0.0, sb = 0.0;
-      const int qa = p == 0 ? 2 : (p == 1 ? 0 : 1), qb = p == 0 ? 1 : (p == 1 ? 2 : 0);
+      FF d{0.f, 0.f};
 #pragma unroll
       for (int k2 = 0; k2 < 8; k2++) {
         const bool px = k2 == 1 || k2 == 2 || k2 == 5 || k2 == 6;
@@ -266,15 +328,41 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
         // cu0 = (dEz/dy - dEy/dz), cu1 = (dEx/dz - dEz/dx), cu2 = (dEy/dx - dEx/dy)
         const bool sga = p == 0 ? py : (p == 1 ? pz : px);
         const bool sgb = p == 0 ? pz : (p == 1 ? px : py);
-        const double va = s_e[lc][3 * k2 + qa], vb = s_e[lc][3 * k2 + qb];
-        sa += sga ? va : -va;
-        sb += sgb ? vb : -vb;
+        const float ha = s_eh[lc][3 * k2 + qa], la = s_el[lc][3 * k2 + qa];
+        const float hb = s_eh[lc][3 * k2 + qb], lb = s_el[lc][3 * k2 + qb];
+        ff_acc(d, sga ? ha : -ha, sga ? la : -la);
+        ff_acc(d, sgb ? -hb : hb, sgb ? -lb : lb);
       }
-      s_cu[lc][p] = 0.25 / dxd * (sa - sb);
+      d = ff_norm(d);
+      const FF cu = ff_norm(ff_mul(d.s, d.q, K.curl[0], K.curl[1]));
+      s_cu[lc][p][0] = cu.s;
+      s_cu[lc][p][1] = cu.q;
     }
     __syncthreads();
-    const double cu[3] = {s_cu[lc][0], s_cu[lc][1], s_cu[lc][2]};
-    cell_curl_t_row<double>(cu, sg * a.th2dt2 * Vd * 0.25 / dxd, p, out);
+    // out[k] += s (sig1 y[q1] - sig2 y[q2]) for y = the curl (s = sg th2dt2 V 0.25/dx)
+    // and, for the RHS, y = centre B (s = thdt V 0.25/dx): C^T y, component p
+    const int q1 = p == 0 ? 1 : (p == 1 ? 2 : 0), q2 = p == 0 ? 2 : (p == 1 ? 0 : 1);
+    auto curl_t = [&](float (*y)[2], float sh, float sl) {
+      FF tpp{y[q1][0], y[q1][1]}, tpm{y[q1][0], y[q1][1]};
+      ff_acc(tpp, -y[q2][0], -y[q2][1]);  // y1 - y2
+      ff_acc(tpm, y[q2][0], y[q2][1]);    // y1 + y2
+      tpp = ff_norm(tpp);
+      tpm = ff_norm(tpm);
+      const FF upp = ff_mul(tpp.s, tpp.q, sh, sl), upm = ff_mul(tpm.s, tpm.q, sh, sl);
+#pragma unroll
+      for (int k2 = 0; k2 < 8; k2++) {
+        const bool px = k2 == 1 || k2 == 2 || k2 == 5 || k2 == 6;
+        const bool py = k2 == 2 || k2 == 3 || k2 == 6 || k2 == 7;
+        const bool pz = k2 >= 4;
+        const bool s1 = p == 0 ? pz : (p == 1 ? px : py);
+        const bool s2 = p == 0 ? py : (p == 1 ? pz : px);
+        // s1 y1 - s2 y2: (+,+) y1 - y2, (+,-) y1 + y2, (-,+) -(y1 + y2), (-,-) -(y1 - y2)
+        const FF& u = (s1 == s2) ? upp : upm;
+        const float sgn = s1 ? 1.f : -1.f;
+        ff_acc(out[k2], sgn * u.s, sgn * u.q);
+      }
+    };
+    curl_t(s_cu[lc], sg * K.cc[0], sg * K.cc[1]);
     // mass term: sum over pairs of m (FP32 partial) x e, in FP32 pairs
     float eh[8][3], el[8][3];
     FF acc[8];
@@ -299,17 +387,43 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
           if (c1 != c2) ff_add(acc[c2], m, eh[c1][q], el[c1][q]);
         }
       }
-    const double fv = sg * a.f * Vd;
 #pragma unroll
-    for (int c = 0; c < 8; c++) out[c] += fv * ff_value(acc[c]);
+    for (int c = 0; c < 8; c++) {
+      const FF t = ff_norm(acc[c]);
+      const FF u = ff_mul(t.s, t.q, sg * K.m[0], sg * K.m[1]);
+      ff_acc(out[c], u.s, u.q);
+    }
     if (ACC == 2) {
-      const double B[3] = {a.Bcen[cell], a.Bcen[a.ncell + cell], a.Bcen[2 * a.ncell + cell]};
-      cell_curl_t_row<double>(B, a.thdt * Vd * 0.25 / dxd, p, out);
+      curl_t(s_b[lc], K.bb[0], K.bb[1]);
       const float* jj = a.cellJ + cell * 24;
 #pragma unroll
-      for (int c = 0; c < 8; c++) out[c] -= a.f * widen(jj[3 * c + p]);
+      for (int c = 0; c < 8; c++) ff_add2(out[c], -a.fj[0], -a.fj[1], jj[3 * c + p], 0.f);
     }
-    scatter_row<double>(y64, a.nvc, cid, p, out, a.h);
+    // scatter with P^T: FP64 atomics of the pairs' values
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      const int cc = cid[c], hs0 = a.h.hs[cc], hs1 = a.h.hs[cc + 1];
+      if (hs0 == hs1) {
+        atomicAdd(y64 + p * a.nvc + cc, ff_value(out[c]));
+      } else {
+        const FF o = ff_norm(out[c]);
+        for (int t = hs0; t < hs1; t++)
+          atomicAdd(y64 + p * a.nvc + a.h.hp[t], ff_value(ff_mul(o.s, o.q, a.h.hwh[t], a.h.hwl[t])));
+      }
+    }
+  }
+}
+
+// x (times dinv) as FP32 pairs: the input of the pair-arithmetic operator
+__global__ void __launch_bounds__(256) k_amr_split(long long n, const double* __restrict__ x,
+                                                   const double* __restrict__ dinv,
+                                                   float* __restrict__ xh, float* __restrict__ xl) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double v = dinv ? dinv[t] * x[t] : x[t];
+    const float h = (float)v;
+    xh[t] = h;
+    xl[t] = (float)(v - (double)h);
   }
 }
 
@@ -544,7 +658,7 @@ __global__ void k_amr_pack(long long nvc, const int* ctab, Hang h, const double*
   }
 }
 
-Hang hang_of(const amps_gpu_ctx* c) { return Hang{c->d_hs, c->d_hp, c->d_hw}; }
+Hang hang_of(const amps_gpu_ctx* c) { return Hang{c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl}; }
 unsigned g1(long long n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
@@ -572,7 +686,38 @@ static ApplyArgs apply_args(amps_gpu_ctx* c) {
   a.f = 4.0 * kPi * dt * th;
   a.thdt = th * dt;
   a.flags = c->d_flags;
+  a.bscale = c->d_bscale;
+  auto split = [](double v, float* o) {
+    o[0] = (float)v;
+    o[1] = (float)(v - (double)o[0]);
+  };
+  for (int sc = 0; sc < kMaxScale; sc++) {
+    const double dx = c->dxf * (double)(1 << sc), V = dx * dx * dx;
+    LevelK& K = a.lk[sc];
+    K.dx = (float)dx;
+    K.V = (float)V;
+    split(0.25 / dx, K.curl);
+    split(a.th2dt2 * V * 0.25 / dx, K.cc);
+    split(0.125 * V, K.id);
+    split(a.f * V, K.m);
+    split(a.thdt * V * 0.25 / dx, K.bb);
+  }
+  split(a.f, a.fj);
   return a;
+}
+
+// x (times dinv) as FP32 pairs in the context's scratch (2 x 3 nvc floats)
+static cudaError_t split_input(amps_gpu_ctx* c, const double* x, const double* dinv, ApplyArgs& a) {
+  const long long n = 3 * c->nvc;
+  cudaError_t e = cudaSuccess;
+  if (!c->d_xs && (e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n)) != cudaSuccess)
+    return e;
+  a.xh = c->d_xs;
+  a.xl = c->d_xs + n;
+  k_amr_split<<<(unsigned)std::min<long long>((n + 255) / 256, 152LL * 16), 256, 0, c->stream>>>(n, x, dinv,
+                                                                                                c->d_xs,
+                                                                                                c->d_xs + n);
+  return cudaGetLastError();
 }
 
 template <int ACC>
@@ -598,7 +743,8 @@ cudaError_t launch_amr_matvec(amps_gpu_ctx* c, const double* x, const double* di
   ApplyArgs a = apply_args(c);
   a.x = x;
   a.dinv = dinv;
-  TimedLaunch t(c, "matvec", 2);
+  TimedLaunch t(c, "matvec", 3);
+  if ((e = split_input(c, x, dinv, a)) != cudaSuccess) return e;
   if ((e = launch_tile<1>(c, a, nullptr, y)) != cudaSuccess) return e;
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, x, dinv, y, 0);
   return cudaGetLastError();
@@ -632,7 +778,8 @@ cudaError_t launch_amr_rhs(amps_gpu_ctx* c) {
   a.x = c->d_En;
   a.dinv = nullptr;
   a.Bcen = c->d_Bc;
-  TimedLaunch t(c, "rhs", 2);
+  TimedLaunch t(c, "rhs", 3);
+  if ((e = split_input(c, c->d_En, nullptr, a)) != cudaSuccess) return e;
   if ((e = launch_tile<2>(c, a, nullptr, c->d_rhs)) != cudaSuccess) return e;
   k_amr_constraint<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, nullptr, nullptr, c->d_rhs, 1);
   return cudaGetLastError();

@@ -547,6 +547,12 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
   std::vector<int> borg((size_t)nbl * 3), bscale((size_t)nbl);
   std::vector<double> bdx((size_t)nbl);
   std::vector<float> bdtdx((size_t)nbl), binvvol((size_t)nbl);
+  // hanging weights split into FP32 pairs for the pair-arithmetic kernels
+  std::vector<float> hw_hi(m->hang_weight.size()), hw_lo(m->hang_weight.size());
+  for (size_t t = 0; t < hw_hi.size(); t++) {
+    hw_hi[t] = (float)m->hang_weight[t];
+    hw_lo[t] = (float)(m->hang_weight[t] - (double)hw_hi[t]);
+  }
   for (long long b = 0; b < nbl; b++) {
     const amps_block_desc& d = m->blocks[(size_t)b];
     borg[(size_t)(3 * b)] = d.ix;
@@ -559,6 +565,7 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
   }
   ok = ok && upload(&c->d_ctab, m->corner_tab) && upload(&c->d_hs, m->hang_start) &&
        upload(&c->d_hp, m->hang_parent) && upload(&c->d_hw, m->hang_weight) &&
+       upload(&c->d_hwh, hw_hi) && upload(&c->d_hwl, hw_lo) &&
        upload(&c->d_fine_map, m->fine_map) && upload(&c->d_borg, borg) &&
        upload(&c->d_bscale, bscale) && upload(&c->d_bdx, bdx) && upload(&c->d_bdtdx, bdtdx) &&
        upload(&c->d_binvvol, binvvol) && build_pc_maps_amr(c, m);
@@ -652,7 +659,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_Z, c->d_y32,
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
-                  c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw,
+                  c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl,
                   c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol,
                   c->d_ss, c->d_sc, c->d_sv, c->d_pc_in, c->d_pc_out_v[0], c->d_pc_out_v[1],
                   c->d_pc_set, c->d_pc_jac_v[0], c->d_pc_jac_v[1]};

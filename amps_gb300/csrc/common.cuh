@@ -67,6 +67,8 @@ struct amps_gpu_ctx {
   int* d_hs = nullptr;      // [nvc+1] hanging CSR start (AMR)
   int* d_hp = nullptr;      // hanging parents
   double* d_hw = nullptr;   // hanging weights
+  float* d_hwh = nullptr;   // the hanging weights as FP32 pairs (hi, lo)
+  float* d_hwl = nullptr;
   int* d_fine_map = nullptr;
   int* d_borg = nullptr;      // nb*3 origins, finest-cell units
   int* d_bscale = nullptr;    // nb finest cells per cell
@@ -315,6 +317,16 @@ __device__ __forceinline__ void ff_add2(FF& a, float kh, float kl, float xh, flo
   ff_acc(a, ph, fmaf(kh, xl, fmaf(kl, xh, fmaf(kh, xh, -ph))));
 }
 __device__ __forceinline__ double ff_value(const FF& a) { return (double)a.s + (double)a.q; }
+// (s, q) renormalised so that q is below half an ulp of s (fast two-sum)
+__device__ __forceinline__ FF ff_norm(const FF& a) {
+  const float t = __fadd_rn(a.s, a.q);
+  return FF{t, __fsub_rn(a.q, __fsub_rn(t, a.s))};
+}
+// (xh + xl)(kh + kl) as a pair
+__device__ __forceinline__ FF ff_mul(float xh, float xl, float kh, float kl) {
+  const float ph = __fmul_rn(xh, kh);
+  return FF{ph, fmaf(xh, kl, fmaf(xl, kh, fmaf(xh, kh, -ph)))};
+}
 
 // Input of the learned preconditioner at one entry e of its region map: D v at
 // a free corner (e >= 0), nothing (e == -1: no corner of the block's lattice

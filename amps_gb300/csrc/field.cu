@@ -116,7 +116,8 @@ TapsFF taps_ff(const Taps& T) {
   return t;
 }
 
-// xh + xl = dinv .* x (dinv may be null), split into FP32 pairs
+// xh + xl = dinv .* x (dinv may be null), split into FP32 pairs (xl null: the
+// FP32 rounding only, the input of the FP32 inner operator)
 __global__ void __launch_bounds__(256) k_split(long long n, const double* __restrict__ x,
                                                const double* __restrict__ dinv,
                                                float* __restrict__ xh, float* __restrict__ xl) {
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(256) k_split(long long n, const double* __rest
     const double v = dinv ? dinv[t] * x[t] : x[t];
     const float h = (float)v;
     xh[t] = h;
-    xl[t] = (float)(v - (double)h);
+    if (xl) xl[t] = (float)(v - (double)h);
   }
 }
 
@@ -190,6 +191,7 @@ TapsF taps_f32(const Taps& T) {
 // convergence.  One thread per (component p, corner).
 __global__ void __launch_bounds__(256) k_matvec32(long long ncor, const int* __restrict__ nbr,
                                                   const float* __restrict__ M,
+                                                  const float* __restrict__ xf,
                                                   const double* __restrict__ x,
                                                   const double* __restrict__ dinv,
                                                   double* __restrict__ y, TapsF T) {
@@ -209,11 +211,8 @@ __global__ void __launch_bounds__(256) k_matvec32(long long ncor, const int* __r
     const int nb = local_id(nbr, b, i + di, j + dj, k + dk);
     const float* Ms = M + (size_t)(9 * s + 3 * p) * ncor + c;
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      double v = x[q * ncor + nb];
-      if (dinv) v *= dinv[q * ncor + nb];
-      acc = fmaf(fmaf(T.f, Ms[(size_t)q * ncor], T.K[p][q][s]), (float)v, acc);
-    }
+    for (int q = 0; q < 3; q++)
+      acc = fmaf(fmaf(T.f, Ms[(size_t)q * ncor], T.K[p][q][s]), xf[q * ncor + nb], acc);
   }
   const double xi = dinv ? dinv[t] * x[t] : x[t];
   y[t] = xi + (double)acc;
@@ -723,14 +722,16 @@ unsigned gridr(long long n, int cap = kRedBlocks, int ept = 4) {
 }  // namespace
 
 // ============================================================================
-// FP32 pair split of an operator input into the context's scratch
-static cudaError_t split_input(amps_gpu_ctx* c, const double* x, const double* dinv) {
+// FP32 pair split of an operator input into the context's scratch (hi_only:
+// the FP32 rounding alone)
+static cudaError_t split_input(amps_gpu_ctx* c, const double* x, const double* dinv,
+                               bool hi_only = false) {
   const long long n = 3 * c->nvc;
   if (!c->d_xs) {
     cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n);
     if (e != cudaSuccess) return e;
   }
-  k_split<<<gridr(n), 256, 0, c->stream>>>(n, x, dinv, c->d_xs, c->d_xs + n);
+  k_split<<<gridr(n), 256, 0, c->stream>>>(n, x, dinv, c->d_xs, hi_only ? nullptr : c->d_xs + n);
   return cudaGetLastError();
 }
 
@@ -749,9 +750,11 @@ cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, 
 cudaError_t launch_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv, double* y) {
   if (c->amr) return launch_amr_matvec32(c, x, dinv, y);
   const TapsF T = taps_f32(make_taps(c->cfg, false));
-  TimedLaunch t(c, "matvec32");
+  TimedLaunch t(c, "matvec32", 2);
+  cudaError_t e = split_input(c, x, dinv, true);
+  if (e != cudaSuccess) return e;
   k_matvec32<<<gridt(3 * c->ncor, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr,
-                                                                            c->d_M, x, dinv, y, T);
+                                                                            c->d_M, c->d_xs, x, dinv, y, T);
   return cudaGetLastError();
 }
 
