@@ -436,6 +436,40 @@ __global__ void __launch_bounds__(256) k_amr_to_f32(long long n, const double* _
     xf[t] = (float)(dinv ? dinv[t] * x[t] : x[t]);
 }
 
+// The same with the input and output as FP32 pairs (Krylov vectors): free
+// rows S (D v) + y32 in pairs, hanging rows (D v)_h - (P D v)_h.
+__global__ void __launch_bounds__(256) k_amr_finish_ff(long long nvc, Hang h,
+                                                       const int* __restrict__ ss,
+                                                       const int* __restrict__ sc,
+                                                       const float* __restrict__ svh,
+                                                       const float* __restrict__ svl,
+                                                       const float* __restrict__ y32, OpIn in,
+                                                       float* __restrict__ wh, float* __restrict__ wl) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nvc) return;
+  const int s = h.hs[c], e = h.hs[c + 1];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    FF acc;
+    if (s == e) {
+      acc = FF{y32[d * nvc + c], 0.f};
+      for (int q = ss[c]; q < ss[c + 1]; q++) {
+        const FF v = opin_value(in, d * nvc + sc[q]);
+        ff_add2(acc, svh[q], svl[q], v.s, v.q);
+      }
+    } else {
+      acc = opin_value(in, d * nvc + c);
+      for (int t = s; t < e; t++) {
+        const FF v = opin_value(in, d * nvc + h.hp[t]);
+        ff_add2(acc, -h.hwh[t], -h.hwl[t], v.s, v.q);
+      }
+    }
+    acc = ff_norm(acc);
+    wh[d * nvc + c] = acc.s;
+    wl[d * nvc + c] = acc.q;
+  }
+}
+
 // Free rows: the identity part S (D x) in FP64 (S = P^T diag(sum of V/8) P,
 // mostly diagonal, CSR) plus the FP32 accumulation of the other terms.
 // Hanging rows: the constraint x_h - (P x)_h in FP64.
@@ -768,6 +802,22 @@ cudaError_t launch_amr_matvec32(amps_gpu_ctx* c, const double* x, const double* 
   if ((e = launch_tile<0>(c, a, c->d_y32, nullptr)) != cudaSuccess) return e;
   k_amr_finish32<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_sv,
                                                      c->d_y32, x, dinv, y);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_amr_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, float* wl) {
+  cudaError_t e = cudaMemsetAsync(c->d_y32, 0, sizeof(float) * 3 * c->nvc, c->stream);
+  if (e != cudaSuccess) return e;
+  ApplyArgs a = apply_args(c);
+  const long long n = 3 * c->nvc;
+  if (!c->d_xs && (e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n)) != cudaSuccess)
+    return e;
+  a.xf = c->d_xs;
+  TimedLaunch t(c, "matvec32", 3);
+  if ((e = launch_in_f32(c, in, c->d_xs)) != cudaSuccess) return e;
+  if ((e = launch_tile<0>(c, a, c->d_y32, nullptr)) != cudaSuccess) return e;
+  k_amr_finish_ff<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_svh, c->d_svl,
+                                                      c->d_y32, in, wh, wl);
   return cudaGetLastError();
 }
 

@@ -615,7 +615,13 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
       }
     }
     ss[(size_t)nv] = (int)sc.size();
-    ok = ok && upload(&c->d_ss, ss) && upload(&c->d_sc, sc) && upload(&c->d_sv, sv);
+    std::vector<float> svh(sv.size()), svl(sv.size());
+    for (size_t q = 0; q < sv.size(); q++) {
+      svh[q] = (float)sv[q];
+      svl[q] = (float)(sv[q] - (double)svh[q]);
+    }
+    ok = ok && upload(&c->d_ss, ss) && upload(&c->d_sc, sc) && upload(&c->d_sv, sv) &&
+         upload(&c->d_svh, svh) && upload(&c->d_svl, svl);
   }
   if (!ok) {
     cudaGetLastError();
@@ -661,7 +667,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl,
                   c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol,
-                  c->d_ss, c->d_sc, c->d_sv, c->d_pc_in, c->d_pc_out_v[0], c->d_pc_out_v[1],
+                  c->d_ss, c->d_sc, c->d_sv, c->d_svh, c->d_svl, c->d_dff, c->d_tmpv, c->d_pc_in, c->d_pc_out_v[0], c->d_pc_out_v[1],
                   c->d_pc_set, c->d_pc_jac_v[0], c->d_pc_jac_v[1]};
   for (void* p : ptrs) cudaFree(p);
   for (int b = 0; b < 2; b++) {

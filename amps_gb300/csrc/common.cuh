@@ -78,6 +78,8 @@ struct amps_gpu_ctx {
   int* d_ss = nullptr;        // identity part of the AMR operator, CSR rows (nvc+1)
   int* d_sc = nullptr;        //   columns
   double* d_sv = nullptr;     //   values
+  float* d_svh = nullptr;     //   values as FP32 pairs
+  float* d_svl = nullptr;
 
   // fields (FP64, component-major)
   double* d_En = nullptr;
@@ -97,6 +99,9 @@ struct amps_gpu_ctx {
   double* d_w = nullptr;
   double* d_dinv = nullptr;
   double* d_Z = nullptr;        // (restart+1) * n preconditioned directions (learned)
+  float* d_dff = nullptr;       // 2n: the Jacobi scaling as FP32 pairs (hi n, lo n)
+  double* d_tmpv = nullptr;     // 2n doubles: FP64 copies of Krylov vectors for the
+                                // learned network, its sample harvest and the FP64 inner operator
   float* d_y32 = nullptr;       // 3*nvc FP32 accumulation of the inner AMR operator
   bool inner_fp32 = true;       // GMRES inner operator in FP32 (iterative refinement)
   PrecondState* pn = nullptr;   // learned preconditioner (precond.cu)
@@ -259,6 +264,22 @@ cudaError_t launch_rhs(amps_gpu_ctx* c);
 cudaError_t launch_matvec(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
 // the same operator evaluated in FP32 arithmetic (inner GMRES iterations)
 cudaError_t launch_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv, double* y);
+// Input of the inner operator on a Krylov vector: v as FP32 pairs (vh, vl) or,
+// for the flexible directions, as doubles (vd); the scaling D as FP32 pairs
+// (dh, dl) or none.  The operator computes w = A (D v) and writes it as FP32
+// pairs; FP32 pair vectors of length n hold hi in [0, n) and lo in [n, 2n) of
+// the same bytes a double vector of length n would take.
+struct OpIn {
+  const double* vd;
+  const float* vh;
+  const float* vl;
+  const float* dh;
+  const float* dl;
+};
+cudaError_t launch_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, float* wl);
+// xf = fp32(D v), the FP32 operator's input
+cudaError_t launch_in_f32(amps_gpu_ctx* c, const OpIn& in, float* xf);
+cudaError_t launch_amr_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, float* wl);
 cudaError_t launch_jacobi_diag(amps_gpu_ctx* c);
 cudaError_t launch_update_b(amps_gpu_ctx* c);
 cudaError_t launch_c2n(amps_gpu_ctx* c, const double* Bcen, double* Bcor);
@@ -326,6 +347,16 @@ __device__ __forceinline__ FF ff_norm(const FF& a) {
 __device__ __forceinline__ FF ff_mul(float xh, float xl, float kh, float kl) {
   const float ph = __fmul_rn(xh, kh);
   return FF{ph, fmaf(xh, kl, fmaf(xl, kh, fmaf(xh, kh, -ph)))};
+}
+// D v as a pair at element t (FP64 input split, FP32 pair input scaled in pairs)
+__device__ __forceinline__ FF opin_value(const OpIn& in, long long t) {
+  if (in.vd) {
+    const double v = in.vd[t];
+    const float h = (float)v;
+    return FF{h, (float)(v - (double)h)};
+  }
+  if (!in.dh) return FF{in.vh[t], in.vl[t]};
+  return ff_mul(in.vh[t], in.vl[t], in.dh[t], in.dl[t]);
 }
 
 // Input of the learned preconditioner at one entry e of its region map: D v at

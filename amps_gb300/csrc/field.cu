@@ -616,6 +616,370 @@ cudaError_t launch_arnoldi(cudaStream_t s, long long n, const double* V, double*
   return cudaLaunchCooperativeKernel((const void*)k_arnoldi<NVM>, dim3(g), dim3(kArnThreads), args, 0, s);
 }
 
+// ---- Krylov vectors in FP32 pairs ----------------------------------------------
+// The Arnoldi basis and the operator output are stored as FP32 pairs (hi, lo:
+// 48 significant bits, the bytes of a double vector): FP64 arithmetic runs at
+// ~1/70 of the FP32 rate on this part, and CGS2 is 4 nv n multiply-adds per
+// step, so the sweeps run in pair arithmetic and only per-block sums touch FP64.
+
+// a += (xh + xl)(yh + yl)
+__device__ __forceinline__ void ff_dot_acc(FF& a, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  ff_acc(a, p, fmaf(xh, yl, fmaf(xl, yh, fmaf(xh, yh, -p))));
+}
+__device__ __forceinline__ FF ff_shfl_xor(const FF& a, int o) {
+  return FF{__shfl_xor_sync(0xffffffffu, a.s, o), __shfl_xor_sync(0xffffffffu, a.q, o)};
+}
+__device__ __forceinline__ FF ff_warp_sum(FF a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const FF b = ff_shfl_xor(a, o);
+    ff_acc(a, b.s, b.q);
+  }
+  return a;
+}
+
+// Reduce acc[0..nv) over the block into row[2i], row[2i+1] (a pair per entry).
+template <int NVM>
+__device__ __forceinline__ void arn_block_store_ff(const FF (&acc)[NVM], int nv, float* __restrict__ row,
+                                                   float* __restrict__ s_red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NVM; i++) {
+    if (i < nv) {
+      const FF v = ff_warp_sum(acc[i]);
+      if (lane == 0) {
+        s_red[2 * (wid * kMaxV + i)] = v.s;
+        s_red[2 * (wid * kMaxV + i) + 1] = v.q;
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    FF t{0.f, 0.f};
+    for (int w = 0; w < kArnThreads / 32; w++)
+      ff_acc(t, s_red[2 * (w * kMaxV + threadIdx.x)], s_red[2 * (w * kMaxV + threadIdx.x) + 1]);
+    t = ff_norm(t);
+    row[2 * threadIdx.x] = t.s;
+    row[2 * threadIdx.x + 1] = t.q;
+  }
+  __syncthreads();
+}
+
+// Sum of the blocks' pairs: s_out[i] (FP64) and s_outf[i] (the pair, renormalised)
+__device__ __forceinline__ void arn_grid_reduce_ff(const float* __restrict__ part, int nblk, int nv,
+                                                   double* __restrict__ s_out, float (*s_outf)[2]) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = wid; i < nv; i += kArnThreads / 32) {
+    FF t{0.f, 0.f};
+    for (int b = lane; b < nblk; b += 32)
+      ff_acc(t, __ldcg(part + 2 * ((size_t)b * kMaxV + i)), __ldcg(part + 2 * ((size_t)b * kMaxV + i) + 1));
+    t = ff_norm(ff_warp_sum(t));
+    if (lane == 0) {
+      s_out[i] = (double)t.s + (double)t.q;
+      s_outf[i][0] = t.s;
+      s_outf[i][1] = t.q;
+    }
+  }
+  __syncthreads();
+}
+
+// One Arnoldi step on pair vectors: CGS2 of w against V_0..V_{nv-1},
+// V_nv = w / ||w||, and the Givens update of the least-squares state.  The
+// sweeps are latency-bound at the occupancy the accumulators allow, so each
+// thread moves L consecutive elements per load (L = 4: 16-byte loads of every
+// hi and lo stream, when n is a multiple of 4; else L = 1).
+template <int L>
+__device__ __forceinline__ void ldv(const float* __restrict__ p, long long t, float (&o)[L]) {
+  if constexpr (L == 4) {
+    const float4 q = reinterpret_cast<const float4*>(p)[t];
+    o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w;
+  } else {
+    o[0] = p[t];
+  }
+}
+template <int L>
+__device__ __forceinline__ void stv(float* __restrict__ p, long long t, const float (&o)[L]) {
+  if constexpr (L == 4) {
+    reinterpret_cast<float4*>(p)[t] = make_float4(o[0], o[1], o[2], o[3]);
+  } else {
+    p[t] = o[0];
+  }
+}
+
+template <int NVM, int L>
+__global__ void __launch_bounds__(kArnThreads) k_arnoldi_ff(long long n, const float* __restrict__ V,
+                                                             float* __restrict__ w, int nv,
+                                                             float* __restrict__ vnext,
+                                                             float* __restrict__ part, GmState* gs,
+                                                             int jj) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ float s_red[2 * (kArnThreads / 32) * kMaxV];
+  __shared__ double s_h1[kMaxV], s_h2[kMaxV], s_n2[1];
+  __shared__ float s_f1[kMaxV][2], s_f2[kMaxV][2], s_fn[1][2];
+  const int nblk = gridDim.x;
+  float* pA = part;
+  float* pB = part + 2 * (size_t)nblk * kMaxV;
+  float* pC = pB + 2 * (size_t)nblk * kMaxV;
+  const long long nl = n / L;
+  const long long stride = (long long)nblk * kArnThreads;
+  const long long t0 = (long long)blockIdx.x * kArnThreads + threadIdx.x;
+  float* wl = w + n;
+  auto vh = [&](int i) { return V + 2 * (size_t)i * n; };
+  FF acc[NVM];
+  // pass 1: h1 = V^T w
+#pragma unroll
+  for (int i = 0; i < NVM; i++) acc[i] = FF{0.f, 0.f};
+  for (long long t = t0; t < nl; t += stride) {
+    float a[L], b[L];
+    ldv<L>(w, t, a);
+    ldv<L>(wl, t, b);
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        float x[L], y[L];
+        ldv<L>(vh(i), t, x);
+        ldv<L>(vh(i) + n, t, y);
+#pragma unroll
+        for (int k = 0; k < L; k++) ff_dot_acc(acc[i], x[k], y[k], a[k], b[k]);
+      }
+  }
+  arn_block_store_ff<NVM>(acc, nv, pA + 2 * (size_t)blockIdx.x * kMaxV, s_red);
+  grid.sync();
+  arn_grid_reduce_ff(pA, nblk, nv, s_h1, s_f1);
+  // pass 2: w -= V h1; h2 = V^T w
+#pragma unroll
+  for (int i = 0; i < NVM; i++) acc[i] = FF{0.f, 0.f};
+  for (long long t = t0; t < nl; t += stride) {
+    float a[L], b[L];
+    ldv<L>(w, t, a);
+    ldv<L>(wl, t, b);
+    FF wt[L];
+#pragma unroll
+    for (int k = 0; k < L; k++) wt[k] = FF{a[k], b[k]};
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        float x[L], y[L];
+        ldv<L>(vh(i), t, x);
+        ldv<L>(vh(i) + n, t, y);
+#pragma unroll
+        for (int k = 0; k < L; k++) {
+          const FF u = ff_mul(x[k], y[k], s_f1[i][0], s_f1[i][1]);
+          ff_acc(wt[k], -u.s, -u.q);
+        }
+      }
+#pragma unroll
+    for (int k = 0; k < L; k++) {
+      wt[k] = ff_norm(wt[k]);
+      a[k] = wt[k].s;
+      b[k] = wt[k].q;
+    }
+    stv<L>(w, t, a);
+    stv<L>(wl, t, b);
+    // the V loads again (cache hits) rather than 2 L more registers per vector
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        float x[L], y[L];
+        ldv<L>(vh(i), t, x);
+        ldv<L>(vh(i) + n, t, y);
+#pragma unroll
+        for (int k = 0; k < L; k++) ff_dot_acc(acc[i], x[k], y[k], a[k], b[k]);
+      }
+  }
+  arn_block_store_ff<NVM>(acc, nv, pB + 2 * (size_t)blockIdx.x * kMaxV, s_red);
+  grid.sync();
+  arn_grid_reduce_ff(pB, nblk, nv, s_h2, s_f2);
+  // pass 3: w -= V h2; ||w||^2
+  FF nacc[1] = {FF{0.f, 0.f}};
+  for (long long t = t0; t < nl; t += stride) {
+    float a[L], b[L];
+    ldv<L>(w, t, a);
+    ldv<L>(wl, t, b);
+    FF wt[L];
+#pragma unroll
+    for (int k = 0; k < L; k++) wt[k] = FF{a[k], b[k]};
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        float x[L], y[L];
+        ldv<L>(vh(i), t, x);
+        ldv<L>(vh(i) + n, t, y);
+#pragma unroll
+        for (int k = 0; k < L; k++) {
+          const FF u = ff_mul(x[k], y[k], s_f2[i][0], s_f2[i][1]);
+          ff_acc(wt[k], -u.s, -u.q);
+        }
+      }
+#pragma unroll
+    for (int k = 0; k < L; k++) {
+      wt[k] = ff_norm(wt[k]);
+      a[k] = wt[k].s;
+      b[k] = wt[k].q;
+      ff_dot_acc(nacc[0], a[k], b[k], a[k], b[k]);
+    }
+    stv<L>(w, t, a);
+    stv<L>(wl, t, b);
+  }
+  arn_block_store_ff<1>(nacc, 1, pC + 2 * (size_t)blockIdx.x * kMaxV, s_red);
+  grid.sync();
+  arn_grid_reduce_ff(pC, nblk, 1, s_n2, s_fn);
+  // V_nv = w / ||w|| (the elements this thread wrote in pass 3)
+  const double inv = s_n2[0] > 0.0 ? 1.0 / sqrt(s_n2[0]) : 0.0;
+  const float ih = (float)inv, il = (float)(inv - (double)ih);
+  for (long long t = t0; t < nl; t += stride) {
+    float a[L], b[L];
+    ldv<L>(w, t, a);
+    ldv<L>(wl, t, b);
+#pragma unroll
+    for (int k = 0; k < L; k++) {
+      const FF u = ff_norm(ff_mul(a[k], b[k], ih, il));
+      a[k] = u.s;
+      b[k] = u.q;
+    }
+    stv<L>(vnext, t, a);
+    stv<L>(vnext + n, t, b);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) gm_update(gs, jj, s_h1, s_h2, s_n2[0]);
+}
+
+template <int NVM, int L>
+cudaError_t launch_arnoldi_ff_l(cudaStream_t s, long long n, const float* V, float* w, int nv,
+                                float* vnext, float* part, GmState* gs, int jj) {
+  static int grid[64] = {0};  // per device: co-resident CTAs
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (grid[dev] == 0) {
+    int sms = 0, per = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_arnoldi_ff<NVM, L>, kArnThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorLaunchOutOfResources;
+    grid[dev] = std::min(sms * per, kArnMaxGrid);
+  }
+  const long long want = (n / L + kArnThreads - 1) / kArnThreads;
+  const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(grid[dev], want));
+  void* args[] = {&n, &V, &w, &nv, &vnext, &part, &gs, &jj};
+  return cudaLaunchCooperativeKernel((const void*)k_arnoldi_ff<NVM, L>, dim3(g), dim3(kArnThreads), args, 0, s);
+}
+
+// 16-byte streams when every pair vector's hi and lo start 16-byte aligned
+template <int NVM>
+cudaError_t launch_arnoldi_ff(cudaStream_t s, long long n, const float* V, float* w, int nv,
+                              float* vnext, float* part, GmState* gs, int jj) {
+  if (n % 4 == 0) return launch_arnoldi_ff_l<NVM, 4>(s, n, V, w, nv, vnext, part, gs, jj);
+  return launch_arnoldi_ff_l<NVM, 1>(s, n, V, w, nv, vnext, part, gs, jj);
+}
+
+// V0 = r / ||r|| as a pair vector (nrm2: ||r||^2)
+__global__ void __launch_bounds__(256) k_start_ff(long long n, const double* __restrict__ r,
+                                                  const double* __restrict__ nrm2, float* __restrict__ v) {
+  const double sc = *nrm2 > 0.0 ? 1.0 / sqrt(*nrm2) : 0.0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double x = r[t] * sc;
+    const float h = (float)x;
+    v[t] = h;
+    v[n + t] = (float)(x - (double)h);
+  }
+}
+
+// double vector <-> pair vector
+__global__ void __launch_bounds__(256) k_to_ff(long long n, const double* __restrict__ x, float* __restrict__ v) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double a = x[t];
+    const float h = (float)a;
+    v[t] = h;
+    v[n + t] = (float)(a - (double)h);
+  }
+}
+__global__ void __launch_bounds__(256) k_from_ff(long long n, const float* __restrict__ v, double* __restrict__ x) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    x[t] = (double)v[t] + (double)v[n + t];
+}
+
+// x += D sum_i y_i V_i, V pair vectors, D as pairs (or none); nv from *d_nv
+__global__ void __launch_bounds__(256) k_combine_ff(long long n, const float* __restrict__ V,
+                                                    const double* __restrict__ y,
+                                                    const int* __restrict__ d_nv,
+                                                    const float* __restrict__ dff,
+                                                    double* __restrict__ x) {
+  __shared__ float s_y[kMaxV][2];
+  const int nv = *d_nv;
+  if (threadIdx.x < kMaxV) {
+    const double v = threadIdx.x < nv ? y[threadIdx.x] : 0.0;
+    s_y[threadIdx.x][0] = (float)v;
+    s_y[threadIdx.x][1] = (float)(v - (double)s_y[threadIdx.x][0]);
+  }
+  __syncthreads();
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    FF a{0.f, 0.f};
+    for (int i = 0; i < nv; i++) {
+      const FF u = ff_mul(V[2 * (size_t)i * n + t], V[2 * (size_t)i * n + n + t], s_y[i][0], s_y[i][1]);
+      ff_acc(a, u.s, u.q);
+    }
+    a = ff_norm(a);
+    if (dff) a = ff_mul(a.s, a.q, dff[t], dff[n + t]);
+    x[t] += ff_value(a);
+  }
+}
+
+// the Jacobi scaling D as pairs
+__global__ void __launch_bounds__(256) k_dff(long long n, const double* __restrict__ d, float* __restrict__ v) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const float h = (float)d[t];
+    v[t] = h;
+    v[n + t] = (float)(d[t] - (double)h);
+  }
+}
+
+// xf = fp32(D v)
+__global__ void __launch_bounds__(256) k_in_f32(long long n, OpIn in, float* __restrict__ xf) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    xf[t] = in.vd ? (float)in.vd[t] : (in.dh ? in.vh[t] * in.dh[t] : in.vh[t]);
+}
+
+// w = A (D v) with the identity part in pairs and the rest in FP32 (the FP32
+// inner operator of k_matvec32 with pair input and output)
+__global__ void __launch_bounds__(256) k_matvec32_ff(long long ncor, const int* __restrict__ nbr,
+                                                     const float* __restrict__ M,
+                                                     const float* __restrict__ xf, OpIn in,
+                                                     float* __restrict__ wh, float* __restrict__ wl,
+                                                     TapsF T) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * ncor) return;
+  const int p = (int)(t / ncor);
+  const long long c = t - (long long)p * ncor;
+  int b, i, j, k;
+  corner_ijk(c, b, i, j, k);
+  float acc = 0.f;
+#pragma unroll 3
+  for (int s = 0; s < 27; s++) {
+    const int dig[3] = {s % 3, (s / 3) % 3, s / 9};
+    const int di = dig[0] == 0 ? 0 : (dig[0] == 1 ? -1 : 1);
+    const int dj = dig[1] == 0 ? 0 : (dig[1] == 1 ? -1 : 1);
+    const int dk = dig[2] == 0 ? 0 : (dig[2] == 1 ? -1 : 1);
+    const int nb = local_id(nbr, b, i + di, j + dj, k + dk);
+    const float* Ms = M + (size_t)(9 * s + 3 * p) * ncor + c;
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+      acc = fmaf(fmaf(T.f, Ms[(size_t)q * ncor], T.K[p][q][s]), xf[q * ncor + nb], acc);
+  }
+  FF y = opin_value(in, t);
+  ff_acc(y, acc, 0.f);
+  y = ff_norm(y);
+  wh[t] = y.s;
+  wl[t] = y.q;
+}
+
 // ---- field updates -----------------------------------------------------------
 __global__ void __launch_bounds__(256) k_update_b(long long ncor, const int* __restrict__ nbr,
                                                   const double* __restrict__ Eh,
@@ -758,6 +1122,28 @@ cudaError_t launch_matvec32(amps_gpu_ctx* c, const double* x, const double* dinv
   return cudaGetLastError();
 }
 
+cudaError_t launch_in_f32(amps_gpu_ctx* c, const OpIn& in, float* xf) {
+  const long long n = 3 * c->nvc;
+  k_in_f32<<<gridr(n), 256, 0, c->stream>>>(n, in, xf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, float* wl) {
+  if (c->amr) return launch_amr_matvec32_ff(c, in, wh, wl);
+  const long long n = 3 * c->ncor;
+  if (!c->d_xs) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n);
+    if (e != cudaSuccess) return e;
+  }
+  const TapsF T = taps_f32(make_taps(c->cfg, false));
+  TimedLaunch t(c, "matvec32", 2);
+  cudaError_t e = launch_in_f32(c, in, c->d_xs);
+  if (e != cudaSuccess) return e;
+  k_matvec32_ff<<<gridt(n, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, c->d_xs, in,
+                                                                     wh, wl, T);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_rhs(amps_gpu_ctx* c) {
   if (c->amr) return launch_amr_rhs(c);
   const TapsFF T = taps_ff(make_taps(c->cfg, false));
@@ -851,8 +1237,46 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   const bool flexible = precond == 2;
   if (flexible && !c->d_Z)
     return set_err(c, AMPS_GPU_INVALID_ARG, "learned preconditioner: no network loaded");
-  auto inner_matvec = [&](const double* x, const double* d, double* y) {
-    return c->inner_fp32 ? launch_matvec32(c, x, d, y) : launch_matvec(c, x, d, y);
+  // Krylov vectors V_j and the operator output w are FP32 pair vectors (the
+  // bytes of d_V / d_w); the Jacobi scaling is used as pairs
+  float* Vf = reinterpret_cast<float*>(c->d_V);
+  float* wf = reinterpret_cast<float*>(c->d_w);
+  auto vf = [&](int j) { return Vf + 2 * (size_t)j * n; };
+  const float* dh = nullptr;
+  const float* dl = nullptr;
+  if (dinv) {
+    if (!c->d_dff) CK(cudaMalloc(reinterpret_cast<void**>(&c->d_dff), sizeof(float) * 2 * n));
+    k_dff<<<gr, 256, 0, s>>>(n, dinv, c->d_dff);
+    dh = c->d_dff;
+    dl = c->d_dff + n;
+  }
+  const bool harvest = precond == 1 && c->pn;
+  if ((flexible || harvest || !c->inner_fp32) && !c->d_tmpv)
+    CK(cudaMalloc(reinterpret_cast<void**>(&c->d_tmpv), sizeof(double) * 2 * n));
+  // w = A (D v_j), or A z_j for the flexible directions, as pairs
+  auto inner_matvec = [&](int jj, const double* zj) -> cudaError_t {
+    if (c->inner_fp32) {
+      OpIn in{};
+      if (zj) {
+        in.vd = zj;
+      } else {
+        in.vh = vf(jj);
+        in.vl = vf(jj) + n;
+        in.dh = dh;
+        in.dl = dl;
+      }
+      return launch_matvec32_ff(c, in, wf, wf + n);
+    }
+    // FP64 inner operator, through FP64 copies
+    const double* x = zj;
+    if (!zj) {
+      k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv);
+      x = c->d_tmpv;
+    }
+    cudaError_t ee = launch_matvec(c, x, zj ? nullptr : dinv, c->d_tmpv + n);
+    if (ee != cudaSuccess) return ee;
+    k_to_ff<<<gr, 256, 0, s>>>(n, c->d_tmpv + n, wf);
+    return cudaGetLastError();
   };
   auto read_norm = [&](const double* v, double* out) -> cudaError_t {
     k_norm2<<<gr, 256, 0, s>>>(n, v, partial);
@@ -869,8 +1293,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   int it = 0, cycles = 0;
   bool conv = false;
   double rel = 0.0;
-  double* V = c->d_V;
-  double* w = c->d_w;
+  double* w = c->d_w;  // between cycles: the FP64 residual
   // cycle-start residual: r = b for x = 0
   CK(cudaMemcpyAsync(w, c->d_rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   double beta = bnorm;
@@ -882,40 +1305,45 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     }
     if (it >= maxit) break;
     cycles++;
-    // the FP32 operators keep the identity part in FP64 (their noise is ~1e-7
-    // of the off-identity terms), so a cycle runs to the tolerance; a later
-    // cycle only corrects what that noise left
+    // the FP32 operators keep the identity part in FP64 accuracy (their noise
+    // is ~1e-7 of the off-identity terms), so a cycle runs to the tolerance; a
+    // later cycle only corrects what that noise left
     const double target = tol * bnorm;
     // V0 = r / ||r|| (d_n2 holds ||r||^2 from read_norm)
     k_gm_start<<<1, 32, 0, s>>>(gs, d_n2, target);
-    k_scale<<<gr, 256, 0, s>>>(n, w, V, d_n2);
+    k_start_ff<<<gr, 256, 0, s>>>(n, w, d_n2, vf(0));
     int launched = 0, used = 0;
     bool done = false;
     const int first_read = cycles == 1 ? std::max(1, std::min(c->gm_guess[precond], m)) : 1;
     while (!done && launched < m && it + launched < maxit) {
       const int jj = launched++;
       const int nv = jj + 1;
-      double* vj = V + (size_t)jj * n;
       if (flexible) {
         double* zj = c->d_Z + (size_t)jj * n;
-        CK(launch_precond_net(c, vj, zj));
-        CK(inner_matvec(zj, nullptr, w));
+        k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv);  // v_j in FP64 for the network
+        CK(launch_precond_net(c, c->d_tmpv, zj));
+        CK(inner_matvec(jj, zj));
       } else {
-        CK(inner_matvec(vj, dinv, w));
+        CK(inner_matvec(jj, nullptr));
         // training pairs for the learned preconditioner: (A D v_j, D v_j)
-        if (precond == 1 && c->pn) CK(precond_harvest_pairs(c, w, vj, 1));
+        if (harvest) {
+          k_from_ff<<<gr, 256, 0, s>>>(n, wf, c->d_tmpv);
+          k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv + n);
+          CK(precond_harvest_pairs(c, c->d_tmpv, c->d_tmpv + n, 1));
+        }
       }
       {
         TimedLaunch t(c, "gmres_orth");
-        double* vnext = V + (size_t)nv * n;
+        float* part = reinterpret_cast<float*>(c->d_arn);
+        float* vnext = vf(nv);
         if (nv <= 4)
-          e = launch_arnoldi<4>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
+          e = launch_arnoldi_ff<4>(s, n, Vf, wf, nv, vnext, part, gs, jj);
         else if (nv <= 8)
-          e = launch_arnoldi<8>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
+          e = launch_arnoldi_ff<8>(s, n, Vf, wf, nv, vnext, part, gs, jj);
         else if (nv <= 16)
-          e = launch_arnoldi<16>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
+          e = launch_arnoldi_ff<16>(s, n, Vf, wf, nv, vnext, part, gs, jj);
         else
-          e = launch_arnoldi<32>(s, n, V, w, nv, vnext, c->d_arn, gs, jj);
+          e = launch_arnoldi_ff<32>(s, n, Vf, wf, nv, vnext, part, gs, jj);
         if (e != cudaSuccess) return cuda_check(c, e, "arnoldi step");
       }
       CK(cudaGetLastError());
@@ -933,7 +1361,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     if (flexible)
       k_combine<<<gr, 256, 0, s>>>(n, c->d_Z, gs->y, kMaxV, &gs->jj, nullptr, c->d_x);
     else
-      k_combine<<<gr, 256, 0, s>>>(n, V, gs->y, kMaxV, &gs->jj, dinv, c->d_x);
+      k_combine_ff<<<gr, 256, 0, s>>>(n, Vf, gs->y, &gs->jj, dinv ? c->d_dff : nullptr, c->d_x);
     CK(cudaGetLastError());
     // true residual in FP64
     CK(launch_matvec(c, c->d_x, nullptr, w));
