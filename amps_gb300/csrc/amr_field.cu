@@ -50,8 +50,10 @@ __device__ __forceinline__ double cval(const double* __restrict__ F, const doubl
 // FP32 value of corner c, component d (xf already scaled), P applied
 __device__ __forceinline__ float cval_f(const float* __restrict__ xf, long long nvc, int c, int d,
                                         const Hang& h) {
+  // the value is loaded alongside the hanging test (one dependent load fewer)
+  const float v0 = xf[d * nvc + c];
   const int s = h.hs[c], e = h.hs[c + 1];
-  if (s == e) return xf[d * nvc + c];
+  if (s == e) return v0;
   float v = 0.f;
   for (int t = s; t < e; t++) v = fmaf(h.hwh[t], xf[d * nvc + h.hp[t]], v);
   return v;
@@ -60,8 +62,9 @@ __device__ __forceinline__ float cval_f(const float* __restrict__ xf, long long 
 // corner c, component d of a field given as FP32 pairs (xh + xl), P applied in pairs
 __device__ __forceinline__ FF cval_ff(const float* __restrict__ xh, const float* __restrict__ xl,
                                      long long nvc, int c, int d, const Hang& h) {
+  const FF v0{xh[d * nvc + c], xl[d * nvc + c]};
   const int s = h.hs[c], e = h.hs[c + 1];
-  if (s == e) return FF{xh[d * nvc + c], xl[d * nvc + c]};
+  if (s == e) return v0;
   FF v{0.f, 0.f};
   for (int t = s; t < e; t++) {
     const long long q = d * nvc + h.hp[t];
@@ -206,7 +209,6 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
                                                                double* __restrict__ y64) {
   extern __shared__ __align__(16) float s_m[];
   __shared__ __align__(8) uint64_t bar;
-  __shared__ int s_cid[kTileCells][8];
   // corner values (8 corners x 3): FP32 for ACC 0, FP32 pairs for ACC 1/2
   __shared__ float s_eh[kTileCells][24];
   __shared__ float s_el[ACC == 0 ? 1 : kTileCells][24];
@@ -237,12 +239,15 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
   // the cell's corners and their values, each gathered once by one of its 3
   // threads (thread p: corner ids c = p, p+3, p+6; values of component p)
   // tile-local corner of (cell lc, corner c): the slab's cells are i = 0..7,
-  // j = 4 (lc / 8 - ...) rows, one k
+  // 4 rows j, one k
   auto tcorner = [&](int c) { return (lc % 8 + c_off[c][0]) + 9 * ((lc / 8 + c_off[c][1]) + 5 * c_off[c][2]); };
-  for (int c = p; c < 8; c += 3) {
-    const int id = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
-    s_cid[lc][c] = id;
-    if (ACC == 0) s_tcid[tcorner(c)] = id;  // the same id from every cell sharing the corner
+  // every thread loads its cell's 8 corner ids (cached table), so the value
+  // gathers below wait on one load, not on a barrier
+  int cid[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    cid[c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
+    if (ACC == 0 && c % 3 == p) s_tcid[tcorner(c)] = cid[c];  // the same id from every cell sharing it
   }
   if (ACC == 0)
     for (int q = tid; q < 3 * kTC; q += kTileThreads) s_acc[q] = 0.f;
@@ -253,11 +258,8 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
     s_b[lc][p][0] = bh;
     s_b[lc][p][1] = (float)(Bv - (double)bh);
   }
-  __syncthreads();
-  int cid[8];
 #pragma unroll
   for (int c = 0; c < 8; c++) {
-    cid[c] = s_cid[lc][c];
     if (ACC == 0) {
       s_eh[lc][3 * c + p] = cval_f(a.xf, a.nvc, cid[c], p, a.h);
     } else {
@@ -529,24 +531,30 @@ __global__ void __launch_bounds__(256) k_amr_constraint(long long nvc, Hang h,
 }
 
 // Jacobi diagonal (free corners: sum over their cells of the cell diagonal)
+// Jacobi diagonal (a preconditioner: FP32 arithmetic is enough; per cell size
+// s: base[s] = V (1/8 + th2dt2 / (8 dx^2)), fv[s] = f V)
+struct DiagK {
+  float base[kMaxScale], fv[kMaxScale];
+};
 __global__ void __launch_bounds__(256) k_amr_diag(long long ncell, long long nvc, const int* ctab,
-                                                  Hang h, const double* bdx, const float* cellM,
-                                                  double th2dt2, double f, double* diag) {
+                                                  Hang h, const int* bscale, const float* cellM, DiagK K,
+                                                  double* diag) {
   const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= ncell) return;
   const int b = (int)(cell >> 9), l = (int)(cell & 511);
   const int i = l & 7, j = (l >> 3) & 7, k = l >> 6;
-  const double dx = bdx[b], V = dx * dx * dx;
+  const int sc = min(__ffs(bscale[b]) - 1, kMaxScale - 1);
+  const float base = K.base[sc], fv = K.fv[sc];
   const float* mm = cellM + cell * AMPS_CELLM;
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     const int cc = ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
-    if (h.hs[cc + 1] > h.hs[cc]) continue;
     const float* blk = mm + pair_monomial(c, c) * 9;
-#pragma unroll
-    for (int d = 0; d < 3; d++)
-      atomicAdd(diag + d * nvc + cc,
-                V * (0.125 + th2dt2 / (8.0 * dx * dx) + f * widen(blk[4 * d])));
+    const float m0 = blk[0], m1 = blk[4], m2 = blk[8];
+    if (h.hs[cc + 1] > h.hs[cc]) continue;
+    atomicAdd(diag + cc, (double)fmaf(fv, m0, base));
+    atomicAdd(diag + nvc + cc, (double)fmaf(fv, m1, base));
+    atomicAdd(diag + 2 * nvc + cc, (double)fmaf(fv, m2, base));
   }
 }
 
@@ -556,8 +564,8 @@ __global__ void __launch_bounds__(256) k_amr_invert_diag(long long nvc, Hang h, 
   const bool hang = h.hs[c + 1] > h.hs[c];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    const double v = diag[d * nvc + c];
-    diag[d * nvc + c] = (hang || v == 0.0) ? 1.0 : 1.0 / v;
+    const float v = (float)diag[d * nvc + c];  // a preconditioner: FP32 reciprocal
+    diag[d * nvc + c] = (hang || v == 0.f) ? 1.0 : (double)(1.0f / v);
   }
 }
 
@@ -840,8 +848,14 @@ cudaError_t launch_amr_jacobi(amps_gpu_ctx* c) {
   if (e != cudaSuccess) return e;
   ApplyArgs a = apply_args(c);
   TimedLaunch t(c, "jacobi", 2);
-  k_amr_diag<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, a.h, c->d_bdx,
-                                                  c->d_cellM, a.th2dt2, a.f, c->d_dinv);
+  DiagK K{};
+  for (int sc = 0; sc < kMaxScale; sc++) {
+    const double dx = c->dxf * (double)(1 << sc), V = dx * dx * dx;
+    K.base[sc] = (float)(V * (0.125 + a.th2dt2 / (8.0 * dx * dx)));
+    K.fv[sc] = (float)(a.f * V);
+  }
+  k_amr_diag<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, a.h, c->d_bscale,
+                                                  c->d_cellM, K, c->d_dinv);
   k_amr_invert_diag<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_dinv);
   return cudaGetLastError();
 }

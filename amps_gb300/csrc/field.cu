@@ -263,9 +263,10 @@ __global__ void __launch_bounds__(256) k_jacobi(long long ncor, const float* __r
                                                 double k22, double f) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncor) return;
-  dinv[c] = 1.0 / (k00 + f * widen(M[(size_t)0 * ncor + c]));
-  dinv[ncor + c] = 1.0 / (k11 + f * widen(M[(size_t)4 * ncor + c]));
-  dinv[2 * ncor + c] = 1.0 / (k22 + f * widen(M[(size_t)8 * ncor + c]));
+  // a preconditioner: FP32 arithmetic (FP64 division is slow on this part)
+  dinv[c] = (double)(1.0f / fmaf((float)f, M[(size_t)0 * ncor + c], (float)k00));
+  dinv[ncor + c] = (double)(1.0f / fmaf((float)f, M[(size_t)4 * ncor + c], (float)k11));
+  dinv[2 * ncor + c] = (double)(1.0f / fmaf((float)f, M[(size_t)8 * ncor + c], (float)k22));
 }
 
 // ---- reductions ------------------------------------------------------------
