@@ -220,7 +220,11 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
   // corner gets one global atomic per component instead of up to 8
   constexpr int kTC = 90;
   __shared__ float s_acc[ACC == 0 ? 3 * kTC : 1];
-  __shared__ int s_tcid[ACC == 0 ? kTC : 1];
+  __shared__ int s_tcid[kTC];
+  // ACC 1/2: the same per-corner sums as pairs, accumulated without atomics:
+  // warp p owns component p, and in round c the 32 cells' corner c are 32
+  // distinct tile corners
+  __shared__ float s_ffacc[ACC == 0 ? 1 : 3][ACC == 0 ? 1 : kTC][2];
   const int tid = threadIdx.x, p = tid / kTileCells, lc = tid % kTileCells;
   const long long cell0 = (long long)blockIdx.x * kTileCells;
   if (tid == 0) {
@@ -247,10 +251,16 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     cid[c] = a.ctab[b * 729 + (i + c_off[c][0]) + 9 * ((j + c_off[c][1]) + 9 * (k + c_off[c][2]))];
-    if (ACC == 0 && c % 3 == p) s_tcid[tcorner(c)] = cid[c];  // the same id from every cell sharing it
+    if (c % 3 == p) s_tcid[tcorner(c)] = cid[c];  // the same id from every cell sharing it
   }
-  if (ACC == 0)
+  if (ACC == 0) {
     for (int q = tid; q < 3 * kTC; q += kTileThreads) s_acc[q] = 0.f;
+  } else {
+    for (int q = tid; q < 3 * kTC; q += kTileThreads) {
+      s_ffacc[q / kTC][q % kTC][0] = 0.f;
+      s_ffacc[q / kTC][q % kTC][1] = 0.f;
+    }
+  }
   if (ACC == 2) {
     // centre B, component p, split into a pair (the only FP64 arithmetic besides the scatter)
     const double Bv = a.Bcen[p * a.ncell + cell];
@@ -401,16 +411,27 @@ __global__ void __launch_bounds__(kTileThreads) k_amr_cell_tile(ApplyArgs a, flo
 #pragma unroll
       for (int c = 0; c < 8; c++) ff_add2(out[c], -a.fj[0], -a.fj[1], jj[3 * c + p], 0.f);
     }
-    // scatter with P^T: FP64 atomics of the pairs' values
+    // sum over the tile's cells per corner, in pairs (round c: corner c of every cell)
 #pragma unroll
     for (int c = 0; c < 8; c++) {
-      const int cc = cid[c], hs0 = a.h.hs[cc], hs1 = a.h.hs[cc + 1];
+      float* slot = s_ffacc[p][tcorner(c)];
+      FF v{slot[0], slot[1]};
+      ff_acc(v, out[c].s, out[c].q);
+      slot[0] = v.s;
+      slot[1] = v.q;
+      __syncwarp();
+    }
+    __syncthreads();
+    // scatter with P^T: one FP64 atomic per tile corner and component
+    for (int q = tid; q < 3 * kTC; q += kTileThreads) {
+      const int pp = q / kTC, tc = q % kTC, cc = s_tcid[tc];
+      const FF o = ff_norm(FF{s_ffacc[pp][tc][0], s_ffacc[pp][tc][1]});
+      const int hs0 = a.h.hs[cc], hs1 = a.h.hs[cc + 1];
       if (hs0 == hs1) {
-        atomicAdd(y64 + p * a.nvc + cc, ff_value(out[c]));
+        atomicAdd(y64 + pp * a.nvc + cc, ff_value(o));
       } else {
-        const FF o = ff_norm(out[c]);
         for (int t = hs0; t < hs1; t++)
-          atomicAdd(y64 + p * a.nvc + a.h.hp[t], ff_value(ff_mul(o.s, o.q, a.h.hwh[t], a.h.hwl[t])));
+          atomicAdd(y64 + pp * a.nvc + a.h.hp[t], ff_value(ff_mul(o.s, o.q, a.h.hwh[t], a.h.hwl[t])));
       }
     }
   }

@@ -296,60 +296,6 @@ __device__ __forceinline__ void block_store_partials(double* acc, int nv, double
   }
 }
 
-// partial dots V_i . w for i < nv (NVM >= nv, compile-time register budget)
-template <int NVM>
-__global__ void __launch_bounds__(256) k_dots(long long n, const double* __restrict__ V,
-                                              const double* __restrict__ w, int nv,
-                                              double* __restrict__ partial) {
-  double acc[NVM];
-#pragma unroll
-  for (int i = 0; i < NVM; i++) acc[i] = 0.0;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const double wt = w[t];
-#pragma unroll
-    for (int i = 0; i < NVM; i++)
-      if (i < nv) acc[i] += V[(size_t)i * n + t] * wt;
-  }
-  block_store_partials<NVM>(acc, nv, partial);
-}
-
-// w -= sum_i h_i V_i; then partial dots of the new w with V_i (MODE 0) or its
-// squared norm (MODE 1)
-template <int NVM, int MODE>
-__global__ void __launch_bounds__(256) k_orth(long long n, const double* __restrict__ V,
-                                              double* __restrict__ w, const double* __restrict__ h,
-                                              int nv, double* __restrict__ partial) {
-  __shared__ double s_h[NVM];
-  if (threadIdx.x < NVM) s_h[threadIdx.x] = threadIdx.x < nv ? h[threadIdx.x] : 0.0;
-  __syncthreads();
-  double acc[MODE == 0 ? NVM : 1];
-#pragma unroll
-  for (int i = 0; i < (MODE == 0 ? NVM : 1); i++) acc[i] = 0.0;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    double wt = w[t];
-    double vv[NVM];
-#pragma unroll
-    for (int i = 0; i < NVM; i++)
-      if (i < nv) {
-        vv[i] = V[(size_t)i * n + t];
-        wt -= s_h[i] * vv[i];
-      }
-    w[t] = wt;
-    if (MODE == 0) {
-#pragma unroll
-      for (int i = 0; i < NVM; i++)
-        if (i < nv) acc[i] += vv[i] * wt;
-    } else {
-      acc[0] += wt * wt;
-    }
-  }
-  block_store_partials<(MODE == 0 ? NVM : 1)>(acc, MODE == 0 ? nv : 1, partial);
-}
-
-// out[i] = sum of partials (+ add[i] when add != null); warp i reduces vector i
-// (launch with 32 * nv threads)
 __global__ void k_reduce_partials(const double* __restrict__ partial, int nblk, int nv,
                                   double* __restrict__ out, const double* __restrict__ add) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -358,16 +304,6 @@ __global__ void k_reduce_partials(const double* __restrict__ partial, int nblk, 
   for (int bk = lane; bk < nblk; bk += 32) t += partial[bk * kMaxV + w];
   t = warp_sum(t);
   if (lane == 0) out[w] = t + (add ? add[w] : 0.0);
-}
-
-// dst = src * (1/sqrt(*nrm2)) or src * (1/ *scal) depending on mode
-__global__ void __launch_bounds__(256) k_scale(long long n, const double* __restrict__ src,
-                                               double* __restrict__ dst,
-                                               const double* __restrict__ nrm2) {
-  const double s = *nrm2 > 0.0 ? 1.0 / sqrt(*nrm2) : 0.0;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x)
-    dst[t] = src[t] * s;
 }
 
 // r = b - r (in place on r)
@@ -474,150 +410,14 @@ __global__ void k_gm_solve(GmState* __restrict__ S) {
 }
 
 // one CGS2 Arnoldi orthogonalisation with a register budget fitted to nv
-template <int NVM>
-void arnoldi_orth(cudaStream_t s, unsigned gr, long long n, const double* V, double* w, int nv,
-                  double* partial, double* d_h1, double* d_h2, double* d_n2, double* vnext) {
-  k_dots<NVM><<<gr, 256, 0, s>>>(n, V, w, nv, partial);
-  k_reduce_partials<<<1, 32 * nv, 0, s>>>(partial, gr, nv, d_h1, nullptr);
-  k_orth<NVM, 0><<<gr, 256, 0, s>>>(n, V, w, d_h1, nv, partial);
-  k_reduce_partials<<<1, 32 * nv, 0, s>>>(partial, gr, nv, d_h2, nullptr);
-  k_orth<NVM, 1><<<gr, 256, 0, s>>>(n, V, w, d_h2, nv, partial);
-  k_reduce_partials<<<1, 32, 0, s>>>(partial, gr, 1, d_n2, nullptr);
-  k_scale<<<gr, 256, 0, s>>>(n, w, vnext, d_n2);
-}
-
-// One whole Arnoldi step after the operator, in one cooperative launch (one
-// CTA per SM, grid-wide barriers between the phases): CGS2 against V_0..V_nv-1
-// (h1 = V^T w, w -= V h1, h2 = V^T w, w -= V h2), ||w||, V_nv = w / ||w||,
-// and the Givens update of the least-squares state.  Every CTA reduces the
-// per-CTA partial sums of a phase itself (152 rows), so the phases need no
-// further launches; each phase writes its own partial buffer.
-constexpr int kArnThreads = 256;
-
-__device__ __forceinline__ void arn_grid_reduce(const double* __restrict__ part, int nblk, int nv,
-                                                double* __restrict__ s_out) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int i = wid; i < nv; i += kArnThreads / 32) {
-    double t = 0.0;
-    for (int b = lane; b < nblk; b += 32) t += __ldcg(part + (size_t)b * kMaxV + i);
-    t = warp_sum(t);
-    if (lane == 0) s_out[i] = t;
-  }
-  __syncthreads();
-}
-
-template <int NVM>
-__device__ __forceinline__ void arn_block_store(const double (&acc)[NVM], int nv, double* __restrict__ row,
-                                                double* __restrict__ s_red) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < NVM; i++) {
-    if (i < nv) {
-      const double v = warp_sum(acc[i]);
-      if (lane == 0) s_red[wid * kMaxV + i] = v;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < nv) {
-    double t = 0.0;
-    for (int w = 0; w < kArnThreads / 32; w++) t += s_red[w * kMaxV + threadIdx.x];
-    row[threadIdx.x] = t;
-  }
-  __syncthreads();
-}
-
-template <int NVM>
-__global__ void __launch_bounds__(kArnThreads) k_arnoldi(long long n, const double* __restrict__ V,
-                                                          double* __restrict__ w, int nv,
-                                                          double* __restrict__ vnext,
-                                                          double* __restrict__ part, GmState* gs,
-                                                          int jj) {
-  cg::grid_group grid = cg::this_grid();
-  __shared__ double s_red[(kArnThreads / 32) * kMaxV];
-  __shared__ double s_h1[kMaxV], s_h2[kMaxV], s_n2[1];
-  const int nblk = gridDim.x;
-  double* pA = part;
-  double* pB = part + (size_t)nblk * kMaxV;
-  double* pC = pB + (size_t)nblk * kMaxV;
-  const long long stride = (long long)nblk * kArnThreads;
-  const long long t0 = (long long)blockIdx.x * kArnThreads + threadIdx.x;
-  double acc[NVM];
-  // pass 1: h1 = V^T w
-#pragma unroll
-  for (int i = 0; i < NVM; i++) acc[i] = 0.0;
-  for (long long t = t0; t < n; t += stride) {
-    const double wt = w[t];
-#pragma unroll
-    for (int i = 0; i < NVM; i++)
-      if (i < nv) acc[i] = fma(V[(size_t)i * n + t], wt, acc[i]);
-  }
-  arn_block_store<NVM>(acc, nv, pA + (size_t)blockIdx.x * kMaxV, s_red);
-  grid.sync();
-  arn_grid_reduce(pA, nblk, nv, s_h1);
-  // pass 2: w -= V h1; h2 = V^T w
-#pragma unroll
-  for (int i = 0; i < NVM; i++) acc[i] = 0.0;
-  for (long long t = t0; t < n; t += stride) {
-    double vv[NVM];
-    double wt = w[t];
-#pragma unroll
-    for (int i = 0; i < NVM; i++)
-      if (i < nv) {
-        vv[i] = V[(size_t)i * n + t];
-        wt = fma(-s_h1[i], vv[i], wt);
-      }
-    w[t] = wt;
-#pragma unroll
-    for (int i = 0; i < NVM; i++)
-      if (i < nv) acc[i] = fma(vv[i], wt, acc[i]);
-  }
-  arn_block_store<NVM>(acc, nv, pB + (size_t)blockIdx.x * kMaxV, s_red);
-  grid.sync();
-  arn_grid_reduce(pB, nblk, nv, s_h2);
-  // pass 3: w -= V h2; ||w||^2
-  double nacc[1] = {0.0};
-  for (long long t = t0; t < n; t += stride) {
-    double wt = w[t];
-#pragma unroll
-    for (int i = 0; i < NVM; i++)
-      if (i < nv) wt = fma(-s_h2[i], V[(size_t)i * n + t], wt);
-    w[t] = wt;
-    nacc[0] = fma(wt, wt, nacc[0]);
-  }
-  arn_block_store<1>(nacc, 1, pC + (size_t)blockIdx.x * kMaxV, s_red);
-  grid.sync();
-  arn_grid_reduce(pC, nblk, 1, s_n2);
-  // V_nv = w / ||w|| (the elements this thread wrote in pass 3)
-  const double inv = s_n2[0] > 0.0 ? 1.0 / sqrt(s_n2[0]) : 0.0;
-  for (long long t = t0; t < n; t += stride) vnext[t] = w[t] * inv;
-  if (blockIdx.x == 0 && threadIdx.x == 0) gm_update(gs, jj, s_h1, s_h2, s_n2[0]);
-}
-
-// cooperative grid of k_arnoldi<NVM>: as many co-resident CTAs as the
-// registers allow (at most kArnMaxGrid), and no more than the vector needs
-template <int NVM>
-cudaError_t launch_arnoldi(cudaStream_t s, long long n, const double* V, double* w, int nv,
-                           double* vnext, double* part, GmState* gs, int jj) {
-  static int grid[64] = {0};  // per device: co-resident CTAs
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  if (grid[dev] == 0) {
-    int sms = 0, per = 0;
-    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_arnoldi<NVM>, kArnThreads, 0);
-    if (e != cudaSuccess) return e;
-    if (per < 1) return cudaErrorLaunchOutOfResources;
-    grid[dev] = std::min(sms * per, kArnMaxGrid);
-  }
-  const long long want = (n + kArnThreads - 1) / kArnThreads;
-  const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(grid[dev], want));
-  void* args[] = {&n, &V, &w, &nv, &vnext, &part, &gs, &jj};
-  return cudaLaunchCooperativeKernel((const void*)k_arnoldi<NVM>, dim3(g), dim3(kArnThreads), args, 0, s);
-}
-
 // ---- Krylov vectors in FP32 pairs ----------------------------------------------
+// One whole Arnoldi step after the operator runs in one cooperative launch
+// (co-resident CTAs, grid-wide barriers between the phases): CGS2 against
+// V_0..V_nv-1 (h1 = V^T w, w -= V h1, h2 = V^T w, w -= V h2), ||w||,
+// V_nv = w / ||w||, and the Givens update of the least-squares state.  Every
+// CTA reduces the per-CTA partial sums of a phase itself, so the phases need
+// no further launches; each phase writes its own partial buffer.
+constexpr int kArnThreads = 256;
 // The Arnoldi basis and the operator output are stored as FP32 pairs (hi, lo:
 // 48 significant bits, the bytes of a double vector): FP64 arithmetic runs at
 // ~1/70 of the FP32 rate on this part, and CGS2 is 4 nv n multiply-adds per
@@ -695,6 +495,9 @@ __device__ __forceinline__ void ldv(const float* __restrict__ p, long long t, fl
   if constexpr (L == 4) {
     const float4 q = reinterpret_cast<const float4*>(p)[t];
     o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w;
+  } else if constexpr (L == 2) {
+    const float2 q = reinterpret_cast<const float2*>(p)[t];
+    o[0] = q.x; o[1] = q.y;
   } else {
     o[0] = p[t];
   }
@@ -703,6 +506,8 @@ template <int L>
 __device__ __forceinline__ void stv(float* __restrict__ p, long long t, const float (&o)[L]) {
   if constexpr (L == 4) {
     reinterpret_cast<float4*>(p)[t] = make_float4(o[0], o[1], o[2], o[3]);
+  } else if constexpr (L == 2) {
+    reinterpret_cast<float2*>(p)[t] = make_float2(o[0], o[1]);
   } else {
     p[t] = o[0];
   }
@@ -867,11 +672,12 @@ cudaError_t launch_arnoldi_ff_l(cudaStream_t s, long long n, const float* V, flo
   return cudaLaunchCooperativeKernel((const void*)k_arnoldi_ff<NVM, L>, dim3(g), dim3(kArnThreads), args, 0, s);
 }
 
-// 16-byte streams when every pair vector's hi and lo start 16-byte aligned
+// the widest streams at which every pair vector's hi and lo start aligned
 template <int NVM>
 cudaError_t launch_arnoldi_ff(cudaStream_t s, long long n, const float* V, float* w, int nv,
                               float* vnext, float* part, GmState* gs, int jj) {
   if (n % 4 == 0) return launch_arnoldi_ff_l<NVM, 4>(s, n, V, w, nv, vnext, part, gs, jj);
+  if (n % 2 == 0) return launch_arnoldi_ff_l<NVM, 2>(s, n, V, w, nv, vnext, part, gs, jj);
   return launch_arnoldi_ff_l<NVM, 1>(s, n, V, w, nv, vnext, part, gs, jj);
 }
 
@@ -1383,7 +1189,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
 // Autotuner: candidate launch shapes timed with CUDA events on the context
 // stream, on scratch vectors (the operator and the sweeps have no side effects
 // outside them).  ms[0..2]: operator with 64/128/256 threads per CTA;
-// ms[3..5]: one 8-vector CGS2 sweep with 76/152/304 CTAs (4 elements per thread).
+// ms[3..5]: one 8-vector combination sweep with 76/152/304 CTAs (4 elements per thread).
 amps_gpu_status field_autotune(amps_gpu_ctx* c, double* ms) {
   const long long n = 3 * c->nvc;
   cudaStream_t s = c->stream;
@@ -1421,18 +1227,21 @@ amps_gpu_status field_autotune(amps_gpu_ctx* c, double* ms) {
   }
   c->tune_tb = best_tb;
   const int caps[3] = {76, 152, 304};
-  double* partial = c->d_red;
-  double* d_h1 = c->d_red + kRedBlocks * kMaxV;
-  double* d_h2 = d_h1 + kMaxV;
-  double* d_n2 = d_h2 + kMaxV;
+  // the sweep: x += sum of 8 pair vectors times coefficients (k_combine_ff),
+  // the shape of the solve's grid-stride vector passes
+  GmState* gs = reinterpret_cast<GmState*>(c->d_red + kGmOffset);
+  const int eight = 8;
+  if ((e = cudaMemcpyAsync(&gs->jj, &eight, sizeof(int), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    fail(e, "autotune");
+  if ((e = cudaMemsetAsync(gs->y, 0, sizeof(gs->y), s)) != cudaSuccess) fail(e, "autotune");
+  const float* Vf = reinterpret_cast<const float*>(c->d_V);
   best = 1e30;
   int best_cap = c->tune_red;
   for (int q = 0; q < 3 && !st; q++) {
     const unsigned gr = gridr(n, caps[q], 4);
-    arnoldi_orth<8>(s, gr, n, c->d_V, y, 8, partial, d_h1, d_h2, d_n2, c->d_V + 8 * n);
+    k_combine_ff<<<gr, 256, 0, s>>>(n, Vf, gs->y, &gs->jj, nullptr, x);
     cudaEventRecord(a, s);
-    for (int r = 0; r < 5; r++)
-      arnoldi_orth<8>(s, gr, n, c->d_V, y, 8, partial, d_h1, d_h2, d_n2, c->d_V + 8 * n);
+    for (int r = 0; r < 5; r++) k_combine_ff<<<gr, 256, 0, s>>>(n, Vf, gs->y, &gs->jj, nullptr, x);
     cudaEventRecord(b, s);
     if ((e = cudaEventSynchronize(b)) != cudaSuccess) fail(e, "autotune sweep");
     float t = 0.f;
