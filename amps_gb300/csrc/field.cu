@@ -711,13 +711,15 @@ __global__ void __launch_bounds__(256) k_from_ff(long long n, const float* __res
 }
 
 // x += D sum_i y_i V_i, V pair vectors, D as pairs (or none); nv from *d_nv
+// (at most NVM: the loads of all vectors are issued before the pair sums)
+template <int NVM>
 __global__ void __launch_bounds__(256) k_combine_ff(long long n, const float* __restrict__ V,
                                                     const double* __restrict__ y,
                                                     const int* __restrict__ d_nv,
                                                     const float* __restrict__ dff,
                                                     double* __restrict__ x) {
   __shared__ float s_y[kMaxV][2];
-  const int nv = *d_nv;
+  const int nv = min(*d_nv, NVM);
   if (threadIdx.x < kMaxV) {
     const double v = threadIdx.x < nv ? y[threadIdx.x] : 0.0;
     s_y[threadIdx.x][0] = (float)v;
@@ -726,15 +728,36 @@ __global__ void __launch_bounds__(256) k_combine_ff(long long n, const float* __
   __syncthreads();
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x) {
+    float vh[NVM], vl[NVM];
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        vh[i] = V[2 * (size_t)i * n + t];
+        vl[i] = V[2 * (size_t)i * n + n + t];
+      }
     FF a{0.f, 0.f};
-    for (int i = 0; i < nv; i++) {
-      const FF u = ff_mul(V[2 * (size_t)i * n + t], V[2 * (size_t)i * n + n + t], s_y[i][0], s_y[i][1]);
-      ff_acc(a, u.s, u.q);
-    }
+#pragma unroll
+    for (int i = 0; i < NVM; i++)
+      if (i < nv) {
+        const FF u = ff_mul(vh[i], vl[i], s_y[i][0], s_y[i][1]);
+        ff_acc(a, u.s, u.q);
+      }
     a = ff_norm(a);
     if (dff) a = ff_mul(a.s, a.q, dff[t], dff[n + t]);
     x[t] += ff_value(a);
   }
+}
+
+void launch_combine_ff(cudaStream_t s, unsigned gr, long long n, const float* V, const double* y,
+                       const int* d_nv, int nv_host, const float* dff, double* x) {
+  if (nv_host <= 4)
+    k_combine_ff<4><<<gr, 256, 0, s>>>(n, V, y, d_nv, dff, x);
+  else if (nv_host <= 8)
+    k_combine_ff<8><<<gr, 256, 0, s>>>(n, V, y, d_nv, dff, x);
+  else if (nv_host <= 16)
+    k_combine_ff<16><<<gr, 256, 0, s>>>(n, V, y, d_nv, dff, x);
+  else
+    k_combine_ff<32><<<gr, 256, 0, s>>>(n, V, y, d_nv, dff, x);
 }
 
 // the Jacobi scaling D as pairs
@@ -1168,7 +1191,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     if (flexible)
       k_combine<<<gr, 256, 0, s>>>(n, c->d_Z, gs->y, kMaxV, &gs->jj, nullptr, c->d_x);
     else
-      k_combine_ff<<<gr, 256, 0, s>>>(n, Vf, gs->y, &gs->jj, dinv ? c->d_dff : nullptr, c->d_x);
+      launch_combine_ff(s, gr, n, Vf, gs->y, &gs->jj, used, dinv ? c->d_dff : nullptr, c->d_x);
     CK(cudaGetLastError());
     // true residual in FP64
     CK(launch_matvec(c, c->d_x, nullptr, w));
@@ -1239,9 +1262,9 @@ amps_gpu_status field_autotune(amps_gpu_ctx* c, double* ms) {
   int best_cap = c->tune_red;
   for (int q = 0; q < 3 && !st; q++) {
     const unsigned gr = gridr(n, caps[q], 4);
-    k_combine_ff<<<gr, 256, 0, s>>>(n, Vf, gs->y, &gs->jj, nullptr, x);
+    launch_combine_ff(s, gr, n, Vf, gs->y, &gs->jj, 8, nullptr, x);
     cudaEventRecord(a, s);
-    for (int r = 0; r < 5; r++) k_combine_ff<<<gr, 256, 0, s>>>(n, Vf, gs->y, &gs->jj, nullptr, x);
+    for (int r = 0; r < 5; r++) launch_combine_ff(s, gr, n, Vf, gs->y, &gs->jj, 8, nullptr, x);
     cudaEventRecord(b, s);
     if ((e = cudaEventSynchronize(b)) != cudaSuccess) fail(e, "autotune sweep");
     float t = 0.f;
