@@ -31,7 +31,11 @@ def nested_leaves(nb0, lmax, mode, frac):
 
 
 class AmrMesh:
-    def __init__(self, nb0, lmax, leaves, dx0=1.0, x0=(0.0, 0.0, 0.0)):
+    """open_axes: per axis, non-periodic (the domain faces carry the field
+    boundary condition field_bc: 0 Dirichlet, 1 Neumann, and delete particles)"""
+
+    def __init__(self, nb0, lmax, leaves, dx0=1.0, x0=(0.0, 0.0, 0.0), open_axes=(False, False, False),
+                 field_bc=0):
         self.lib = _capi.load()
         self.nb0 = tuple(int(v) for v in nb0)
         self.lmax = int(lmax)
@@ -42,9 +46,12 @@ class AmrMesh:
         descs = (BlockDesc * len(leaves))(*[BlockDesc(*map(int, r)) for r in leaves])
         h = C.c_void_p()
         x0a = np.array(self.x0, np.float64)
-        st = self.lib.amps_amr_build(self.nb0[0], self.nb0[1], self.nb0[2], self.lmax,
-                                     ptr(x0a, C.c_double), self.dx0, C.cast(descs, C.c_void_p), len(leaves),
-                                     C.byref(h))
+        self.open_axes = tuple(bool(v) for v in open_axes)
+        self.field_bc = int(field_bc)
+        op = (C.c_int * 3)(*[1 if v else 0 for v in self.open_axes])
+        st = self.lib.amps_amr_build_open(self.nb0[0], self.nb0[1], self.nb0[2], self.lmax,
+                                          ptr(x0a, C.c_double), self.dx0, C.cast(descs, C.c_void_p),
+                                          len(leaves), op, self.field_bc, C.byref(h))
         if st != 0:
             raise AmpsGpuError(st, "amps_amr_build")
         self.h = h
@@ -65,6 +72,15 @@ class AmrMesh:
                                  ptr(self.hang_weight, C.c_double), ptr(self.fine_map, C.c_int32))
         self.level = np.ascontiguousarray(leaves[:, 0])
         self.origin = np.ascontiguousarray(leaves[:, 1:4])
+        ne = C.c_int()
+        self.lib.amps_amr_boundary_tables(h, C.byref(ne), None, None, None, None)
+        self.bnd_flag = np.zeros(self.ncorners, np.int32)
+        self.bnd_start = np.zeros(self.ncorners + 1, np.int32)
+        self.bnd_col = np.zeros(max(ne.value, 1), np.int32)
+        self.bnd_weight = np.zeros(max(ne.value, 1), np.float64)
+        self.lib.amps_amr_boundary_tables(h, C.byref(ne), ptr(self.bnd_flag, C.c_int32),
+                                          ptr(self.bnd_start, C.c_int32), ptr(self.bnd_col, C.c_int32),
+                                          ptr(self.bnd_weight, C.c_double))
 
     @property
     def ncells(self):

@@ -43,11 +43,23 @@ extern "C" amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax
                                           const double* x0, double dx0,
                                           const amps_block_desc* blocks, int nblocks,
                                           amps_amr_mesh** out) {
+  return amps_amr_build_open(nbx0, nby0, nbz0, lmax, x0, dx0, blocks, nblocks, nullptr, 0, out);
+}
+
+extern "C" amps_gpu_status amps_amr_build_open(int nbx0, int nby0, int nbz0, int lmax,
+                                               const double* x0, double dx0,
+                                               const amps_block_desc* blocks, int nblocks,
+                                               const int* open_axes, int field_bc,
+                                               amps_amr_mesh** out) {
   if (!out || !blocks || nblocks <= 0 || nbx0 <= 0 || nby0 <= 0 || nbz0 <= 0 || lmax < 0 ||
-      lmax > 6 || dx0 <= 0.0)
+      lmax > 6 || dx0 <= 0.0 || field_bc < 0 || field_bc > 1)
     return AMPS_GPU_INVALID_ARG;
   *out = nullptr;
   amps_amr_mesh* m = new amps_amr_mesh();
+  for (int d = 0; d < 3; d++) m->open[d] = open_axes && open_axes[d] ? 1 : 0;
+  m->field_bc = field_bc;
+  // periodic axes wrap lattice positions; open axes keep them (corners 0..nfine)
+  auto wrap = [&](int d, int v) { return m->open[d] ? v : wrapi(v, m->nfine[d]); };
   m->nb0[0] = nbx0; m->nb0[1] = nby0; m->nb0[2] = nbz0;
   m->lmax = lmax;
   for (int d = 0; d < 3; d++) m->x0[d] = x0 ? x0[d] : 0.0;
@@ -76,9 +88,10 @@ extern "C" amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax
   }
   for (int32_t v : m->fine_map)
     if (v < 0) { delete m; return AMPS_GPU_INVALID_ARG; }  // gap
-  auto block_at = [&](int X, int Y, int Z) {  // leaf block covering finest cell (X,Y,Z)
-    X = wrapi(X, m->nfine[0]); Y = wrapi(Y, m->nfine[1]); Z = wrapi(Z, m->nfine[2]);
-    return m->fine_map[(size_t)(X / 8) + (size_t)nfb[0] * ((Y / 8) + (size_t)nfb[1] * (Z / 8))];
+  auto block_at = [&](int X, int Y, int Z) {  // leaf block covering finest cell (X,Y,Z), -1 outside
+    X = wrap(0, X); Y = wrap(1, Y); Z = wrap(2, Z);
+    if (X < 0 || X >= m->nfine[0] || Y < 0 || Y >= m->nfine[1] || Z < 0 || Z >= m->nfine[2]) return -1;
+    return (int)m->fine_map[(size_t)(X / 8) + (size_t)nfb[0] * ((Y / 8) + (size_t)nfb[1] * (Z / 8))];
   };
   // 2:1 balance across faces, edges and vertices
   for (int b = 0; b < nblocks; b++) {
@@ -91,7 +104,7 @@ extern "C" amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax
           const int Y = B.iy + (oy < 0 ? -1 : (oy > 0 ? size : 0));
           const int Z = B.iz + (oz < 0 ? -1 : (oz > 0 ? size : 0));
           const int nbk = block_at(X, Y, Z);
-          if (std::abs(blocks[nbk].level - B.level) > 1) { delete m; return AMPS_GPU_INVALID_ARG; }
+          if (nbk >= 0 && std::abs(blocks[nbk].level - B.level) > 1) { delete m; return AMPS_GPU_INVALID_ARG; }
         }
   }
   // unique corners
@@ -104,9 +117,9 @@ extern "C" amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax
     for (int k = 0; k <= 8; k++)
       for (int j = 0; j <= 8; j++)
         for (int i = 0; i <= 8; i++) {
-          const int X = wrapi(B.ix + i * st, m->nfine[0]);
-          const int Y = wrapi(B.iy + j * st, m->nfine[1]);
-          const int Z = wrapi(B.iz + k * st, m->nfine[2]);
+          const int X = wrap(0, B.ix + i * st);
+          const int Y = wrap(1, B.iy + j * st);
+          const int Z = wrap(2, B.iz + k * st);
           const uint64_t kk = key3(X, Y, Z);
           auto it = id.find(kk);
           int32_t c;
@@ -135,13 +148,14 @@ extern "C" amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax
       for (int dy = -1; dy <= 0; dy++)
         for (int dx = -1; dx <= 0; dx++) {
           const int b = block_at(X + dx, Y + dy, Z + dz);
-          if (blocks[b].level < best_level) { best_level = blocks[b].level; best = b; }
+          if (b >= 0 && blocks[b].level < best_level) { best_level = blocks[b].level; best = b; }
         }
     const amps_block_desc& B = blocks[best];
     const int st = 1 << (lmax - B.level);
-    // position relative to the coarsest touching block (periodic)
-    const int rel[3] = {wrapi(X - B.ix, m->nfine[0]), wrapi(Y - B.iy, m->nfine[1]),
-                        wrapi(Z - B.iz, m->nfine[2])};
+    // position relative to the coarsest touching block (periodic axes wrap)
+    const int rel[3] = {m->open[0] ? X - B.ix : wrapi(X - B.ix, m->nfine[0]),
+                        m->open[1] ? Y - B.iy : wrapi(Y - B.iy, m->nfine[1]),
+                        m->open[2] ? Z - B.iz : wrapi(Z - B.iz, m->nfine[2])};
     bool off = false;
     for (int d = 0; d < 3; d++) off |= (rel[d] % st) != 0;
     if (!off) continue;
@@ -192,7 +206,70 @@ extern "C" amps_gpu_status amps_amr_build(int nbx0, int nby0, int nbz0, int lmax
         m->hang_weight.push_back(pw.second);
       }
   }
+  // boundary rows: free corners on a domain face of an open axis
+  // (CollectAndMarkDomainBoundary*CornerNodesOnFaces, GetStencil's
+  // boundary_short_circuit, src/pic/ecsim/get_stencil.cpp:440-620): Dirichlet
+  // dE_b = 0; Neumann dE_b = mean of one donor per touching face, the corner
+  // one step of the finest touching block inward along that face's normal
+  m->bnd_flag.assign((size_t)nc, 0);
+  m->bnd_start.assign((size_t)nc + 1, 0);
+  for (int c = 0; c < nc; c++) {
+    m->bnd_start[(size_t)c + 1] = m->bnd_start[(size_t)c];
+    if (hanging[c]) continue;
+    const int P[3] = {m->corner_xyz[3 * c], m->corner_xyz[3 * c + 1], m->corner_xyz[3 * c + 2]};
+    int side[3] = {0, 0, 0}, nface = 0;
+    for (int d = 0; d < 3; d++) {
+      if (!m->open[d]) continue;
+      if (P[d] == 0) side[d] = -1;
+      else if (P[d] == m->nfine[d]) side[d] = 1;
+      nface += side[d] != 0;
+    }
+    if (!nface) continue;
+    m->bnd_flag[(size_t)c] = 1;
+    if (field_bc == 0) continue;
+    int stf = 1 << 30;  // lattice step of the finest block touching the corner
+    for (int dz = -1; dz <= 0; dz++)
+      for (int dy = -1; dy <= 0; dy++)
+        for (int dx = -1; dx <= 0; dx++) {
+          const int b = block_at(P[0] + dx, P[1] + dy, P[2] + dz);
+          if (b >= 0) stf = std::min(stf, 1 << (lmax - blocks[b].level));
+        }
+    std::map<int32_t, double> acc;
+    for (int d = 0; d < 3; d++) {
+      if (!side[d]) continue;
+      int Q[3] = {P[0], P[1], P[2]};
+      Q[d] -= side[d] * stf;
+      auto it = id.find(key3(wrap(0, Q[0]), wrap(1, Q[1]), wrap(2, Q[2])));
+      if (it == id.end()) { delete m; return AMPS_GPU_INVALID_ARG; }
+      const int32_t q = it->second;
+      const double w = 1.0 / nface;
+      if (hanging[q]) {
+        for (auto& pw : par[(size_t)q]) acc[pw.first] += w * pw.second;
+      } else {
+        acc[q] += w;
+      }
+    }
+    for (auto& cw : acc) {
+      m->bnd_col.push_back(cw.first);
+      m->bnd_weight.push_back(cw.second);
+    }
+    m->bnd_start[(size_t)c + 1] = (int32_t)m->bnd_col.size();
+  }
   *out = m;
+  return AMPS_GPU_OK;
+}
+
+extern "C" amps_gpu_status amps_amr_boundary_tables(const amps_amr_mesh* m, int* nentries, int32_t* flag,
+                                                    int32_t* start, int32_t* col, double* weight) {
+  if (!m) return AMPS_GPU_INVALID_ARG;
+  if (nentries) *nentries = (int)m->bnd_col.size();
+  auto cp = [](auto* dst, const auto& v) {
+    if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
+  };
+  cp(flag, m->bnd_flag);
+  cp(start, m->bnd_start);
+  cp(col, m->bnd_col);
+  cp(weight, m->bnd_weight);
   return AMPS_GPU_OK;
 }
 

@@ -31,7 +31,16 @@ struct Hang {
   const double* hw;
   const float* hwh;  // hw as FP32 pairs
   const float* hwl;
+  // boundary rows of meshes with open axes (bflag null: none): row b reads
+  // x_b - sum_{t in [bs[b], bs[b+1])} bw[t] x_{bc[t]}
+  const int* bflag;
+  const int* bs;
+  const int* bc;
+  const double* bw;
+  const float* bwh;
+  const float* bwl;
 };
+__device__ __forceinline__ bool is_bnd(const Hang& h, long long c) { return h.bflag && h.bflag[c]; }
 
 // value of corner c of a component-major field (component d), P applied,
 // optionally scaled by a diagonal (right preconditioner)
@@ -470,21 +479,33 @@ __global__ void __launch_bounds__(256) k_amr_finish_ff(long long nvc, Hang h,
                                                        float* __restrict__ wh, float* __restrict__ wl) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nvc) return;
-  const int s = h.hs[c], e = h.hs[c + 1];
+  int s = h.hs[c], e = h.hs[c + 1];
+  const int* col = h.hp;
+  const float* cwh = h.hwh;
+  const float* cwl = h.hwl;
+  const bool bnd = s == e && is_bnd(h, c);
+  if (bnd) {
+    s = h.bs[c];
+    e = h.bs[c + 1];
+    col = h.bc;
+    cwh = h.bwh;
+    cwl = h.bwl;
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     FF acc;
-    if (s == e) {
+    if (s == e && !bnd) {
       acc = FF{y32[d * nvc + c], 0.f};
       for (int q = ss[c]; q < ss[c + 1]; q++) {
         const FF v = opin_value(in, d * nvc + sc[q]);
         ff_add2(acc, svh[q], svl[q], v.s, v.q);
       }
     } else {
+      // constraint rows: hanging (parents) or boundary (donors)
       acc = opin_value(in, d * nvc + c);
       for (int t = s; t < e; t++) {
-        const FF v = opin_value(in, d * nvc + h.hp[t]);
-        ff_add2(acc, -h.hwh[t], -h.hwl[t], v.s, v.q);
+        const FF v = opin_value(in, d * nvc + col[t]);
+        ff_add2(acc, -cwh[t], -cwl[t], v.s, v.q);
       }
     }
     acc = ff_norm(acc);
@@ -506,21 +527,31 @@ __global__ void __launch_bounds__(256) k_amr_finish32(long long nvc, Hang h,
                                                       double* __restrict__ y) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nvc) return;
-  const int s = h.hs[c], e = h.hs[c + 1];
+  int s = h.hs[c], e = h.hs[c + 1];
+  const int* col = h.hp;
+  const double* w = h.hw;
+  const bool bnd = s == e && is_bnd(h, c);
+  if (bnd) {
+    s = h.bs[c];
+    e = h.bs[c + 1];
+    col = h.bc;
+    w = h.bw;
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    if (s == e) {
+    if (s == e && !bnd) {
       double acc = (double)y32[d * nvc + c];
       for (int q = ss[c]; q < ss[c + 1]; q++) {
-        const int col = sc[q];
-        acc += sv[q] * (dinv ? dinv[d * nvc + col] : 1.0) * x[d * nvc + col];
+        const int cl = sc[q];
+        acc += sv[q] * (dinv ? dinv[d * nvc + cl] : 1.0) * x[d * nvc + cl];
       }
       y[d * nvc + c] = acc;
     } else {
+      // constraint rows: hanging (parents) or boundary (donors)
       double pv = 0.0;
       for (int t = s; t < e; t++) {
-        const int p = h.hp[t];
-        pv += h.hw[t] * (dinv ? dinv[d * nvc + p] : 1.0) * x[d * nvc + p];
+        const int p = col[t];
+        pv += w[t] * (dinv ? dinv[d * nvc + p] : 1.0) * x[d * nvc + p];
       }
       y[d * nvc + c] = (dinv ? dinv[d * nvc + c] : 1.0) * x[d * nvc + c] - pv;
     }
@@ -534,8 +565,17 @@ __global__ void __launch_bounds__(256) k_amr_constraint(long long nvc, Hang h,
                                                         double* __restrict__ y, int rhs_mode) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nvc) return;
-  const int s = h.hs[c], e = h.hs[c + 1];
-  if (s == e) return;
+  int s = h.hs[c], e = h.hs[c + 1];
+  const int* col = h.hp;
+  const double* w = h.hw;
+  if (s == e) {
+    // boundary rows (open axes): the same form with the donor list
+    if (!is_bnd(h, c)) return;
+    s = h.bs[c];
+    e = h.bs[c + 1];
+    col = h.bc;
+    w = h.bw;
+  }
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     if (rhs_mode) {
@@ -543,8 +583,8 @@ __global__ void __launch_bounds__(256) k_amr_constraint(long long nvc, Hang h,
     } else {
       double pv = 0.0;
       for (int t = s; t < e; t++) {
-        const int p = h.hp[t];
-        pv += h.hw[t] * (dinv ? dinv[d * nvc + p] : 1.0) * x[d * nvc + p];
+        const int p = col[t];
+        pv += w[t] * (dinv ? dinv[d * nvc + p] : 1.0) * x[d * nvc + p];
       }
       y[d * nvc + c] = (dinv ? dinv[d * nvc + c] : 1.0) * x[d * nvc + c] - pv;
     }
@@ -582,7 +622,7 @@ __global__ void __launch_bounds__(256) k_amr_diag(long long ncell, long long nvc
 __global__ void __launch_bounds__(256) k_amr_invert_diag(long long nvc, Hang h, double* diag) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nvc) return;
-  const bool hang = h.hs[c + 1] > h.hs[c];
+  const bool hang = h.hs[c + 1] > h.hs[c] || is_bnd(h, c);  // constraint rows: scaling 1
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const float v = (float)diag[d * nvc + c];  // a preconditioner: FP32 reciprocal
@@ -609,6 +649,52 @@ __global__ void __launch_bounds__(256) k_amr_update_b(long long ncell, long long
   cell_curl<double>(e, 0.25 / bdx[b], cu);
 #pragma unroll
   for (int d = 0; d < 3; d++) Bnew[d * ncell + cell] = Bn[d * ncell + cell] - dt * cu[d];
+}
+
+// UpdateB's boundary branch on meshes with open axes
+// (pic_field_solver_ecsim.cpp:5274-5600): a cell with a face on an open domain
+// face keeps B^n (Dirichlet, pass 0) or takes the mean of B^{n+1} of its
+// face-normal inward neighbours, one per such face, in the same block
+// (Neumann, pass p = number of such faces: faces, then edges, then corners, so
+// every donor is final when read).
+__global__ void __launch_bounds__(256) k_amr_bnd_b(long long ncell, const int* __restrict__ borg,
+                                                   const int* __restrict__ bscale, int nf0, int nf1, int nf2,
+                                                   int open, int bc, int pass, const double* __restrict__ Bn,
+                                                   double* __restrict__ Bnew) {
+  const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncell) return;
+  const int b = (int)(cell >> 9), l = (int)(cell & 511);
+  const int idx[3] = {l & 7, (l >> 3) & 7, l >> 6};
+  const int st = bscale[b], nf[3] = {nf0, nf1, nf2};
+  int side[3] = {0, 0, 0}, nface = 0;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (!((open >> d) & 1)) continue;
+    const int lo = borg[3 * b + d] + idx[d] * st;
+    if (lo == 0) side[d] = -1;
+    else if (lo + st == nf[d]) side[d] = 1;
+    nface += side[d] != 0;
+  }
+  if (!nface) return;
+  if (bc == 0) {
+    if (pass == 0)
+#pragma unroll
+      for (int q = 0; q < 3; q++) Bnew[q * ncell + cell] = Bn[q * ncell + cell];
+    return;
+  }
+  if (nface != pass) return;
+  double acc[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (!side[d]) continue;
+    int j[3] = {idx[0], idx[1], idx[2]};
+    j[d] -= side[d];
+    const long long dn = (long long)b * 512 + j[0] + 8 * (j[1] + 8 * j[2]);
+#pragma unroll
+    for (int q = 0; q < 3; q++) acc[q] += Bnew[q * ncell + dn];
+  }
+#pragma unroll
+  for (int q = 0; q < 3; q++) Bnew[q * ncell + cell] = acc[q] / nface;
 }
 
 // C2N: accumulate V*B and V on the corners (P^T for hanging is not used: their
@@ -721,7 +807,10 @@ __global__ void k_amr_pack(long long nvc, const int* ctab, Hang h, const double*
   }
 }
 
-Hang hang_of(const amps_gpu_ctx* c) { return Hang{c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl}; }
+Hang hang_of(const amps_gpu_ctx* c) {
+  return Hang{c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl,
+              c->d_bflag, c->d_bs, c->d_bc, c->d_bw, c->d_bwh, c->d_bwl};
+}
 unsigned g1(long long n) { return (unsigned)((n + 255) / 256); }
 
 }  // namespace
@@ -886,6 +975,12 @@ cudaError_t launch_amr_update_b(amps_gpu_ctx* c) {
   k_amr_update_b<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->nvc, c->d_ctab, hang_of(c),
                                                       c->d_bdx, c->d_Eh, c->d_Bc, c->d_Bc2,
                                                       c->cfg.dt);
+  if (c->mesh_open) {
+    const int* nf = c->amrdev.nfine;
+    for (int pass = (c->field_bc == 0 ? 0 : 1); pass <= (c->field_bc == 0 ? 0 : 3); pass++)
+      k_amr_bnd_b<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_borg, c->d_bscale, nf[0], nf[1], nf[2],
+                                                       c->mesh_open, c->field_bc, pass, c->d_Bc, c->d_Bc2);
+  }
   return cudaGetLastError();
 }
 

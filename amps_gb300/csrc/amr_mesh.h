@@ -22,5 +22,15 @@ struct amps_amr_mesh {
   std::vector<int32_t> hang_start;     // ncorners + 1 (CSR of parents; empty range = free)
   std::vector<int32_t> hang_parent;
   std::vector<double> hang_weight;
+  // non-periodic (open) axes: the corners on their domain faces carry the field
+  // boundary condition as constraint rows b: x_b - sum_k w_k x_col_k = 0
+  // (Dirichlet: no entries; Neumann: the inward face-normal donors, averaged,
+  // hanging donors expanded to their parents)
+  int open[3] = {0, 0, 0};
+  int field_bc = 0;                    // 0 Dirichlet, 1 Neumann
+  std::vector<int32_t> bnd_flag;       // ncorners: 1 on a constraint row
+  std::vector<int32_t> bnd_start;      // ncorners + 1
+  std::vector<int32_t> bnd_col;
+  std::vector<double> bnd_weight;
   std::string err;
 };

@@ -424,11 +424,21 @@ bool build_pc_maps_uniform(amps_gpu_ctx* c) {
 bool build_pc_maps_amr(amps_gpu_ctx* c, const amps_amr_mesh* m) {
   const long long nbl = (long long)m->blocks.size(), nv = c->nvc;
   const long long FX = m->nfine[0], FY = m->nfine[1], FZ = m->nfine[2];
-  auto key = [&](long long x, long long y, long long z) {
-    x = ((x % FX) + FX) % FX;
-    y = ((y % FY) + FY) % FY;
-    z = ((z % FZ) + FZ) % FZ;
-    return x + FX * (y + FY * z);
+  // periodic axes wrap; on open axes positions beyond the faces have no corner
+  // (key -1, never stored); corners of open axes run 0..F, hence F + 1 per axis
+  const long long SX = FX + 1, SY = FY + 1;
+  auto key = [&](long long x, long long y, long long z) -> long long {
+    const long long p[3] = {x, y, z}, F[3] = {FX, FY, FZ};
+    long long q[3];
+    for (int d = 0; d < 3; d++) {
+      if (m->open[d]) {
+        if (p[d] < 0 || p[d] > F[d]) return -1;
+        q[d] = p[d];
+      } else {
+        q[d] = ((p[d] % F[d]) + F[d]) % F[d];
+      }
+    }
+    return q[0] + SX * (q[1] + SY * q[2]);
   };
   std::unordered_map<long long, int> at;
   at.reserve((size_t)nv * 2);
@@ -628,6 +638,24 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
     amps_gpu_destroy(c);
     return AMPS_GPU_CUDA_ERROR;
   }
+  // field boundary rows (open axes)
+  c->mesh_open = (m->open[0] ? 1 : 0) | (m->open[1] ? 2 : 0) | (m->open[2] ? 4 : 0);
+  c->field_bc = m->field_bc;
+  c->open_axes = c->mesh_open;  // particles leave through the open faces
+  if (c->mesh_open) {
+    std::vector<float> bh(m->bnd_weight.size()), bl(m->bnd_weight.size());
+    for (size_t q = 0; q < bh.size(); q++) {
+      bh[q] = (float)m->bnd_weight[q];
+      bl[q] = (float)(m->bnd_weight[q] - (double)bh[q]);
+    }
+    ok = upload(&c->d_bflag, m->bnd_flag) && upload(&c->d_bs, m->bnd_start) && upload(&c->d_bc, m->bnd_col) &&
+         upload(&c->d_bw, m->bnd_weight) && upload(&c->d_bwh, bh) && upload(&c->d_bwl, bl);
+    if (!ok) {
+      cudaGetLastError();
+      amps_gpu_destroy(c);
+      return AMPS_GPU_CUDA_ERROR;
+    }
+  }
   for (int d = 0; d < 3; d++) c->amrdev.nfine[d] = m->nfine[d];
   c->amrdev.fine_map = c->d_fine_map;
   c->amrdev.borg = c->d_borg;
@@ -666,6 +694,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
                   c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl,
+                  c->d_bflag, c->d_bs, c->d_bc, c->d_bw, c->d_bwh, c->d_bwl,
                   c->d_fine_map, c->d_borg, c->d_bscale, c->d_bdx, c->d_bdtdx, c->d_binvvol,
                   c->d_ss, c->d_sc, c->d_sv, c->d_svh, c->d_svl, c->d_dff, c->d_tmpv, c->d_pc_in, c->d_pc_out_v[0], c->d_pc_out_v[1],
                   c->d_pc_set, c->d_pc_jac_v[0], c->d_pc_jac_v[1]};
@@ -988,7 +1017,11 @@ amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* c, int open_x, int open_y, 
   if (!c) return AMPS_GPU_INVALID_ARG;
   cudaSetDevice(c->cfg.device);
   cudaStreamSynchronize(c->stream);
-  c->open_axes = (open_x ? 1 : 0) | (open_y ? 2 : 0) | (open_z ? 4 : 0);
+  const int want = (open_x ? 1 : 0) | (open_y ? 2 : 0) | (open_z ? 4 : 0);
+  // an AMR mesh without periodic wrap on an axis has no particle wrap there either
+  if (c->amr && c->mesh_open && want != c->mesh_open)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "set_open_axes: the mesh fixes the open axes");
+  c->open_axes = want;
   // captured particle steps carry the old setting in their kernel arguments
   for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
   c->graphs.clear();

@@ -69,6 +69,15 @@ struct amps_gpu_ctx {
   double* d_hw = nullptr;   // hanging weights
   float* d_hwh = nullptr;   // the hanging weights as FP32 pairs (hi, lo)
   float* d_hwl = nullptr;
+  // field boundary rows of AMR meshes with open axes (null: fully periodic)
+  int* d_bflag = nullptr;   // nvc: 1 on a boundary constraint row
+  int* d_bs = nullptr;      // nvc+1 CSR of the donor lists
+  int* d_bc = nullptr;
+  double* d_bw = nullptr;
+  float* d_bwh = nullptr;
+  float* d_bwl = nullptr;
+  int mesh_open = 0;        // bit d: axis d of the AMR mesh is not periodic
+  int field_bc = 0;         // 0 Dirichlet, 1 Neumann on the open faces
   int* d_fine_map = nullptr;
   int* d_borg = nullptr;      // nb*3 origins, finest-cell units
   int* d_bscale = nullptr;    // nb finest cells per cell

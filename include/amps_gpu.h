@@ -114,6 +114,27 @@ amps_gpu_status amps_amr_tables(const amps_amr_mesh* m, int32_t* corner_tab, int
                                 int32_t* hang_start, int32_t* hang_parent, double* hang_weight,
                                 int32_t* fine_map);
 amps_gpu_status amps_amr_destroy(amps_amr_mesh* m);
+/* A mesh with non-periodic axes (open_axes[d] != 0; the reference's
+ * _PIC_BC__PERIODIC_MODE_OFF_ with the field boundary policy of
+ * src/pic/ecsim/domain_bc.cpp applied to every domain face): corners keep
+ * their positions 0..nfine on open axes, and the free corners on those
+ * domain faces become constraint rows of the field solve (GetStencil's
+ * boundary_short_circuit, src/pic/ecsim/get_stencil.cpp:440-620):
+ * field_bc 0 Dirichlet (dE = 0, the corner keeps E^n), 1 Neumann (dE equals
+ * the mean of the inward face-normal donor corners).  The cells on those
+ * faces take UpdateB's boundary branch (pic_field_solver_ecsim.cpp:
+ * 5274-5600): Dirichlet B^{n+1} = B^n, Neumann B^{n+1} = mean of the inward
+ * face-normal donor cells, faces before edges before corners.  Particles
+ * leaving through those faces are deleted (amps_gpu_set_open_axes is implied
+ * by the mesh). */
+amps_gpu_status amps_amr_build_open(int nbx0, int nby0, int nbz0, int lmax, const double* x0,
+                                    double dx0, const amps_block_desc* blocks, int nblocks,
+                                    const int* open_axes, int field_bc, amps_amr_mesh** out);
+/* Constraint rows of the boundary corners: flag[ncorners] (1: boundary row),
+ * CSR start[ncorners+1], col/weight[nentries]: row b reads
+ * x_b - sum weight x_col = 0.  Any pointer may be NULL. */
+amps_gpu_status amps_amr_boundary_tables(const amps_amr_mesh* m, int* nentries, int32_t* flag,
+                                         int32_t* start, int32_t* col, double* weight);
 /* Leaves of a nested refinement: mode 0 refines a central box of relative
  * half-width frac/2 (halved per level), mode 1 a central sphere of relative
  * radius frac (halved per level); 2:1 balance enforced.  Returns the leaf

@@ -43,6 +43,14 @@ typedef struct {
   int nspec;
   double q[NSPEC_MAX], m[NSPEC_MAX], w[NSPEC_MAX];
   double dt, theta;
+  /* open (non-periodic) axes: boundary constraint rows of the field solve and
+   * UpdateB's boundary branch (NULL flag: fully periodic) */
+  const int32_t* bnd_flag;    /* ncorners */
+  const int32_t* bnd_start;   /* ncorners+1 */
+  const int32_t* bnd_col;
+  const double* bnd_weight;
+  int open_mask;              /* bit d: axis d open */
+  int field_bc;               /* 0 Dirichlet, 1 Neumann */
 } orc_amr;
 
 static const int kOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
@@ -347,6 +355,19 @@ void orc_amr_apply(const orc_amr* g, const double* cellM, const double* x, doubl
     corner_val(g, x, c, pv);
     for (int d = 0; d < 3; d++) y[3 * c + d] = x[3 * c + d] - pv[d];
   }
+  /* boundary rows of open axes (GetStencil's boundary_short_circuit,
+   * get_stencil.cpp:440-620): Dirichlet dE_b = 0, Neumann dE_b = mean of the
+   * inward face-normal donors */
+  if (g->bnd_flag)
+    for (int c = 0; c < nc; c++) {
+      if (!g->bnd_flag[c]) continue;
+      for (int d = 0; d < 3; d++) {
+        double v = x[3 * c + d];
+        for (int t = g->bnd_start[c]; t < g->bnd_start[c + 1]; t++)
+          v -= g->bnd_weight[t] * x[3 * g->bnd_col[t] + d];
+        y[3 * c + d] = v;
+      }
+    }
 }
 
 /* RHS in weak form: sum_cells V [theta c dt C^T B - (theta c dt)^2 C^T C E^n - f M E^n] - f J_weak,
@@ -381,7 +402,7 @@ void orc_amr_rhs(const orc_amr* g, const double* E_n, const double* Bcen, const 
     }
   }
   for (int c = 0; c < nc; c++)
-    if (g->hang_start[c + 1] > g->hang_start[c])
+    if (g->hang_start[c + 1] > g->hang_start[c] || (g->bnd_flag && g->bnd_flag[c]))
       for (int d = 0; d < 3; d++) rhs[3 * c + d] = 0.0;
   free(tmp);
 }
@@ -481,6 +502,42 @@ void orc_amr_update_b(const orc_amr* g, const double* E_half, const double* Bn, 
       for (int d = 0; d < 3; d++) Bnp1[3 * cl + d] = Bn[3 * cl + d] - g->dt * cu[d];
     }
   }
+  if (!g->open_mask) return;
+  /* UpdateB's boundary branch (pic_field_solver_ecsim.cpp:5274-5600) on the
+   * cells with a face on an open domain face: Dirichlet keeps B^n; Neumann
+   * takes the mean of B^{n+1} of the face-normal inward neighbours (one per
+   * such face, same block), faces before edges before corners */
+  for (int pass = (g->field_bc == 0 ? 0 : 1); pass <= (g->field_bc == 0 ? 0 : 3); pass++)
+    for (int b = 0; b < g->nblocks; b++) {
+      const int st = 1 << (g->lmax - g->level[b]);
+      for (int l = 0; l < 512; l++) {
+        const int idx[3] = {l & 7, (l >> 3) & 7, l >> 6};
+        int side[3] = {0, 0, 0}, nface = 0;
+        for (int d = 0; d < 3; d++) {
+          if (!((g->open_mask >> d) & 1)) continue;
+          const int lo = g->origin[3 * b + d] + idx[d] * st;
+          if (lo == 0) side[d] = -1;
+          else if (lo + st == g->nfine[d]) side[d] = 1;
+          nface += side[d] != 0;
+        }
+        if (!nface) continue;
+        const long cl = (long)b * 512 + l;
+        if (g->field_bc == 0) {
+          for (int q = 0; q < 3; q++) Bnp1[3 * cl + q] = Bn[3 * cl + q];
+          continue;
+        }
+        if (nface != pass) continue;
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < 3; d++) {
+          if (!side[d]) continue;
+          int j[3] = {idx[0], idx[1], idx[2]};
+          j[d] -= side[d];
+          const long dn = (long)b * 512 + j[0] + 8 * (j[1] + 8 * j[2]);
+          for (int q = 0; q < 3; q++) acc[q] += Bnp1[3 * dn + q];
+        }
+        for (int q = 0; q < 3; q++) Bnp1[3 * cl + q] = acc[q] / nface;
+      }
+    }
 }
 
 /* corner B: volume-weighted mean of the touching cells; hanging corners interpolated */

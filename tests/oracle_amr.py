@@ -17,7 +17,9 @@ class Amr(C.Structure):
                 ("level", I32), ("origin", I32), ("corner_tab", I32), ("hang_start", I32),
                 ("hang_parent", I32), ("hang_weight", D), ("fine_map", I32),
                 ("nspec", C.c_int), ("q", C.c_double * 8), ("m", C.c_double * 8),
-                ("w", C.c_double * 8), ("dt", C.c_double), ("theta", C.c_double)]
+                ("w", C.c_double * 8), ("dt", C.c_double), ("theta", C.c_double),
+                ("bnd_flag", I32), ("bnd_start", I32), ("bnd_col", I32), ("bnd_weight", D),
+                ("open_mask", C.c_int), ("field_bc", C.c_int)]
 
 
 _bound = False
@@ -80,6 +82,15 @@ class AmrOracle:
         for i, s in enumerate(species):
             g.q[i], g.m[i], g.w[i] = s.charge, s.mass, s.weight
         g.dt, g.theta = dt, theta
+        # open axes: boundary rows and UpdateB's boundary branch
+        mask = sum(1 << d for d in range(3) if getattr(mesh, "open_axes", (False,) * 3)[d])
+        g.open_mask = mask
+        g.field_bc = getattr(mesh, "field_bc", 0)
+        if mask:
+            g.bnd_flag = p(mesh.bnd_flag, C.c_int32)
+            g.bnd_start = p(mesh.bnd_start, C.c_int32)
+            g.bnd_col = p(mesh.bnd_col, C.c_int32)
+            g.bnd_weight = p(mesh.bnd_weight)
         self.g = g
         n = len(spec)
         self.x = np.ascontiguousarray(x, np.float64).copy()

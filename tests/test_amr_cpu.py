@@ -145,3 +145,72 @@ def test_every_free_corner_is_one_cells_low_corner(recipe):
     count = np.bincount(low[~hanging[low]], minlength=m.ncorners)
     free = ~hanging
     assert np.all(count[free] == 1), (np.sum(count[free] == 0), np.sum(count[free] > 1))
+
+
+def test_open_axis_mesh_boundary_rows():
+    """open axes: corners 0..nfine on those axes, the free corners on their
+    domain faces are boundary rows (Dirichlet: no donors; Neumann: one inward
+    donor per touching face, weights summing to 1)"""
+    from amps_gb300 import amr as AM
+    leaves = [(0, i * 8, j * 8, k * 8) for k in range(2) for j in range(2) for i in range(3)]
+    per = AM.AmrMesh((3, 2, 2), 0, leaves)
+    assert per.ncorners == 24 * 16 * 16 and per.bnd_flag.sum() == 0
+    for bc in (0, 1):
+        m = AM.AmrMesh((3, 2, 2), 0, leaves, open_axes=(True, False, True), field_bc=bc)
+        assert m.ncorners == 25 * 16 * 17
+        xyz = m.corner_xyz.reshape(-1, 3)
+        on = (xyz[:, 0] == 0) | (xyz[:, 0] == 24) | (xyz[:, 2] == 0) | (xyz[:, 2] == 16)
+        np.testing.assert_array_equal(m.bnd_flag.astype(bool), on)
+        nent = np.diff(m.bnd_start)
+        if bc == 0:
+            assert nent.sum() == 0
+            continue
+        for c in np.flatnonzero(on):
+            s, e = m.bnd_start[c], m.bnd_start[c + 1]
+            faces = int(xyz[c, 0] in (0, 24)) + int(xyz[c, 2] in (0, 16))
+            assert e - s == faces and abs(m.bnd_weight[s:e].sum() - 1.0) < 1e-15
+            for q in m.bnd_col[s:e]:
+                assert np.abs(xyz[q] - xyz[c]).sum() == 1   # one lattice step inward
+    # two levels: hanging donors expand to their parents, the rows stay normalised
+    base = AM.central_refined_mesh((4, 4, 4), lmax=1, frac=0.5)
+    m2 = AM.AmrMesh((4, 4, 4), 1, base.leaves, open_axes=(True, True, False), field_bc=1)
+    assert m2.nhanging == base.nhanging
+    rows = np.flatnonzero(m2.bnd_flag)
+    sums = np.add.reduceat(m2.bnd_weight, m2.bnd_start[rows]) if len(rows) else []
+    assert np.allclose(sums, 1.0)
+
+
+def test_oracle_open_boundary_rows_and_update_b():
+    """the oracle's operator rows and UpdateB boundary branch on an open mesh"""
+    from amps_gb300 import amr as AM
+    from tests.oracle_amr import AmrOracle
+    import amps_gb300 as A
+    leaves = [(0, i * 8, j * 8, k * 8) for k in range(2) for j in range(2) for i in range(2)]
+    wl = A.electron_proton_plasma("o", 1, 1, 1, 2, 2)
+    for bc in (0, 1):
+        m = AM.AmrMesh((2, 2, 2), 0, leaves, open_axes=(False, True, False), field_bc=bc)
+        x = np.zeros((0, 3))
+        ao = AmrOracle(m, wl.species, wl.dt, wl.theta, x, np.zeros((0, 3)), np.zeros(0, np.uint8))
+        rng = np.random.default_rng(bc)
+        v = rng.standard_normal((m.ncorners, 3))
+        y = ao.apply(v)
+        for c in np.flatnonzero(m.bnd_flag)[:50]:
+            s, e = m.bnd_start[c], m.bnd_start[c + 1]
+            want = v[c] - (m.bnd_weight[s:e, None] * v[m.bnd_col[s:e]]).sum(axis=0)
+            np.testing.assert_allclose(y[c], want, rtol=0, atol=1e-15)
+        ao.Bcen[:] = rng.standard_normal(ao.Bcen.shape)
+        ao.E_half[:] = 1e-3 * rng.standard_normal(ao.E_half.shape)
+        import ctypes as C
+        from tests.oracle_amr import p
+        bnew = np.zeros_like(ao.Bcen)
+        ao.L.orc_amr_update_b(C.byref(ao.g), p(ao.E_half), p(ao.Bcen), p(bnew))
+        # cells with j = 0 in the blocks at y = 0 (first layer)
+        l = np.arange(m.ncells) % 512
+        blk = np.arange(m.ncells) // 512
+        jy = (l >> 3) & 7
+        at0 = (m.origin[blk, 1] == 0) & (jy == 0)
+        if bc == 0:
+            np.testing.assert_array_equal(bnew[at0], ao.Bcen[at0])
+        else:
+            inward = np.flatnonzero(at0) + 8                   # j + 1, same block
+            np.testing.assert_allclose(bnew[at0], bnew[inward], rtol=0, atol=0)
