@@ -602,8 +602,13 @@ __global__ void k_step_bump(unsigned long long* step, const unsigned long long* 
 }
 
 // Arrivals: deposit (DEP), move behind the stayers, update the occupancy.
+// Arrivals are few per cell (a few % of its particles), so records are staged
+// in chunks of kArrChunk lanes: a smaller record buffer and a register cap let
+// 3 CTAs share an SM, which hides more of the per-cell load latency.
+constexpr int kArrChunk = 16;
+
 template <bool DEP>
-__global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
+__global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
   float4* s_dep = s_dyn;
   float* s_rec = reinterpret_cast<float*>(s_dyn + AMPS_SC);
@@ -616,7 +621,7 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
                         AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0, a.flags))
       return;
   }
-  float* rec = s_rec + wid * 32 * kRec;
+  float* rec = s_rec + wid * kArrChunk * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
   double en = 0.0;
@@ -644,8 +649,8 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
       float old[9];
       if (DEP) tile.preload(lane, a.cellM, a.cellJ, cid, old);
       const int src0 = b0 + cap - na, dst0 = b0 + nst;
-      for (int q0 = 0; q0 < na; q0 += 32) {
-        const bool act = q0 + lane < na;
+      for (int q0 = 0; q0 < na; q0 += kArrChunk) {
+        const bool act = lane < kArrChunk && q0 + lane < na;
         const long long ps = src0 + q0 + lane, pd = dst0 + q0 + lane;
         float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
         int s = 0;
@@ -671,7 +676,7 @@ __global__ void __launch_bounds__(256) k_arrivals(StepArgs a) {
         }
         if (DEP) {
           __syncwarp();
-          const int cnt = min(32, na - q0);
+          const int cnt = min(kArrChunk, na - q0);
           if (lane < kTileLanes) tile.accumulate(rec, cnt, offA, offB);
           __syncwarp();
         }
@@ -1339,6 +1344,7 @@ size_t smem_push(bool dep) {
   return (size_t)AMPS_SC * (2 + 1) * sizeof(float4) + (dep ? kWarps * 32 * kRec * sizeof(float) : 0);
 }
 size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * 32 * kRec * sizeof(float); }
+size_t smem_arr() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * kArrChunk * kRec * sizeof(float); }
 
 void set_smem_attrs() {
   static bool done = false;
@@ -1347,8 +1353,8 @@ void set_smem_attrs() {
   cudaFuncSetAttribute(k_push_deposit<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
   cudaFuncSetAttribute(k_push_deposit<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(true));
   cudaFuncSetAttribute(k_push_deposit<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
-  cudaFuncSetAttribute(k_arrivals<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
-  cudaFuncSetAttribute(k_arrivals<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
+  cudaFuncSetAttribute(k_arrivals<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr());
+  cudaFuncSetAttribute(k_arrivals<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr());
   cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
   done = true;
 }
@@ -1555,9 +1561,9 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
   {
     TimedLaunch t(c, "arrivals");
     if (deposit)
-      k_arrivals<true><<<grid, kWarps * 32, smem_dep(), c->stream>>>(a);
+      k_arrivals<true><<<grid, kWarps * 32, smem_arr(), c->stream>>>(a);
     else
-      k_arrivals<false><<<grid, kWarps * 32, smem_dep(), c->stream>>>(a);
+      k_arrivals<false><<<grid, kWarps * 32, smem_arr(), c->stream>>>(a);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
