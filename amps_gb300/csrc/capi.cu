@@ -1031,7 +1031,6 @@ amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* c, int open_x, int open_y, 
 amps_gpu_status amps_gpu_add_injection(amps_gpu_ctx* c, int face, int spec, double density,
                                        const double* drift, double vth) {
   if (!c) return AMPS_GPU_INVALID_ARG;
-  if (c->amr) return set_err(c, AMPS_GPU_INVALID_ARG, "add_injection: uniform meshes only");
   if (face < 0 || face > 5 || !((c->open_axes >> (face >> 1)) & 1))
     return set_err(c, AMPS_GPU_INVALID_ARG, "add_injection: the face must belong to an open axis");
   if (spec < 0 || spec >= c->cfg.nspec || !(vth > 0.0) || !(density >= 0.0) || c->inj.size() >= 8)

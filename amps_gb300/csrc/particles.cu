@@ -444,7 +444,9 @@ __global__ void __launch_bounds__(128) k_inject(StepArgs a, InjArgs g) {
   const InjDev S = g.src[s];
   const int c = t - S.first;
   const int ax = S.face >> 1, hi = S.face & 1, ta = (ax + 1) % 3, tb = (ax + 2) % 3;
-  const int NT = 8 * g.nbk[ta];
+  const bool amr = a.amr.fine_map != nullptr;
+  // face cells (uniform) or finest-lattice face patches (AMR), each its own stream
+  const int NT = amr ? a.amr.nfine[ta] : 8 * g.nbk[ta];
   const int it = c % NT, ib = c / NT;  // tangential cell coordinates
   const double area = g.dx[ta] * g.dx[tb];
   const double R = S.rate * area;
@@ -509,16 +511,29 @@ __global__ void __launch_bounds__(128) k_inject(StepArgs a, InjArgs g) {
       return;
     }
     // position on the face, in the block-local cell units of the boundary cell's block
-    int bc[3];
+    int b;
     float u[3];
-    bc[ax] = hi ? g.nbk[ax] - 1 : 0;
     u[ax] = hi ? 8.0f : 0.0f;
     const double pt = (it + c0), pb = (ib + c1);
-    bc[ta] = (int)(pt / 8.0);
-    u[ta] = (float)(pt - 8.0 * bc[ta]);
-    bc[tb] = (int)(pb / 8.0);
-    u[tb] = (float)(pb - 8.0 * bc[tb]);
-    const int b = bc[0] + g.nbk[0] * (bc[1] + g.nbk[1] * bc[2]);
+    if (amr) {
+      // the leaf block owning the patch's boundary cell (finest lattice)
+      int F[3];
+      F[ax] = hi ? a.amr.nfine[ax] - 1 : 0;
+      F[ta] = it;
+      F[tb] = ib;
+      b = __ldg(a.amr.fine_map + (F[0] >> 3) + (a.amr.nfine[0] >> 3) * ((F[1] >> 3) + (a.amr.nfine[1] >> 3) * (F[2] >> 3)));
+      const double sc = (double)__ldg(a.amr.bscale + b);
+      u[ta] = (float)((pt - (double)__ldg(a.amr.borg + 3 * b + ta)) / sc);
+      u[tb] = (float)((pb - (double)__ldg(a.amr.borg + 3 * b + tb)) / sc);
+    } else {
+      int bc[3];
+      bc[ax] = hi ? g.nbk[ax] - 1 : 0;
+      bc[ta] = (int)(pt / 8.0);
+      u[ta] = (float)(pt - 8.0 * bc[ta]);
+      bc[tb] = (int)(pb / 8.0);
+      u[tb] = (float)(pb - 8.0 * bc[tb]);
+      b = bc[0] + g.nbk[0] * (bc[1] + g.nbk[1] * bc[2]);
+    }
     // Lapenta2017 for the rest of the step, fields from the block's packed stencil
     const float frac = (float)((g.dt - tt) / g.dt);
     float vf[3] = {(float)v[0], (float)v[1], (float)v[2]};
@@ -547,6 +562,13 @@ __global__ void __launch_bounds__(128) k_inject(StepArgs a, InjArgs g) {
     // move and locate (periodic wrap, deletion through open faces)
     int o[3], ic[3];
     bool far = false;
+    int nbk = b;
+    if (amr) {
+      const float dtdx = __ldg(a.amr.bdtdx + b) * frac;
+      for (int q = 0; q < 3; q++) u[q] = fmaf(vf[q], dtdx, u[q]);
+      nbk = amr_dest(a.amr, b, u, ic, a.open);
+      if (nbk < 0) continue;  // left the domain again at once
+    } else {
     for (int q = 0; q < 3; q++) {
       float un = fmaf(vf[q], a.dtdx[q] * frac, u[q]);
       int od = (int)floorf(un * 0.125f);
@@ -559,10 +581,10 @@ __global__ void __launch_bounds__(128) k_inject(StepArgs a, InjArgs g) {
       ic[q] = min((int)un, AMPS_NC - 1);
     }
     if (far) atomicAdd(a.flags + 0, 1ull);
-    int nbk = b;
     if (o[0] | o[1] | o[2]) {
       if (a.open && leaves_open_face(a, b, o)) continue;  // left again at once
       nbk = __ldg(a.nbr + b * 27 + nbr_slot(o[0], o[1], o[2]));
+    }
     }
     const int key2 = nbk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
     const uint32_t idv = (uint32_t)g.step[1] + (uint32_t)atomicAdd(a.flags + 6, 1ull);
@@ -1505,7 +1527,8 @@ cudaError_t launch_inject(amps_gpu_ctx* c, const StepArgs& a) {
     const int ax = S.face >> 1, ta = (ax + 1) % 3, tb = (ax + 2) % 3;
     D.face = S.face;
     D.spec = S.spec;
-    D.ncell = 64 * nbk[ta] * nbk[tb];
+    // face cells (uniform) or finest-lattice face patches (AMR)
+    D.ncell = c->amr ? c->amrdev.nfine[ta] * c->amrdev.nfine[tb] : 64 * nbk[ta] * nbk[tb];
     D.first = first;
     first += D.ncell;
     D.beta = 1.0 / (std::sqrt(2.0) * S.vth);
@@ -1517,7 +1540,7 @@ cudaError_t launch_inject(amps_gpu_ctx* c, const StepArgs& a) {
   g.nthreads = first;
   g.dt = c->cfg.dt;
   for (int d = 0; d < 3; d++) {
-    g.dx[d] = c->cfg.dx[d];
+    g.dx[d] = c->amr ? c->dxf : c->cfg.dx[d];
     g.nbk[d] = nbk[d];
   }
   g.seed = c->inj_seed;

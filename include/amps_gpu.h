@@ -244,8 +244,8 @@ amps_gpu_status amps_gpu_step(amps_gpu_ctx* ctx, double tol, int maxit, int prec
  * since creation (amps_gpu_num_particles drops by as many). */
 amps_gpu_status amps_gpu_set_open_axes(amps_gpu_ctx* ctx, int open_x, int open_y, int open_z);
 amps_gpu_status amps_gpu_deleted_particles(amps_gpu_ctx* ctx, long long* total);
-/* Injection through an open face (the OpenFlow boundary, pic_bc.cpp:330-420),
- * uniform meshes: every particle step injects on each boundary cell face of
+/* Injection through an open face (the OpenFlow boundary, pic_bc.cpp:270-440),
+ * uniform and AMR meshes: every particle step injects on each boundary cell face of
  * `face` (0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z; its axis must be open) the
  * particles of species `spec` that a Maxwellian of number density `density`,
  * bulk velocity drift[3] (NULL: 0) and thermal speed vth = sqrt(kT/m) sends
@@ -255,7 +255,8 @@ amps_gpu_status amps_gpu_deleted_particles(amps_gpu_ctx* ctx, long long* total);
  * (pic_vel_distribution.cpp:49), moved by the mover for the rest of the step
  * and deposited with the others.  Up to 8 sources.  Random numbers come from
  * counter-based streams keyed by the seed, the step, the source and the face
- * cell; injected particles get ids after the imported ones. */
+ * cell (AMR meshes: the finest-lattice face patch); injected particles get
+ * ids after the imported ones. */
 amps_gpu_status amps_gpu_add_injection(amps_gpu_ctx* ctx, int face, int spec, double density,
                                        const double* drift, double vth);
 amps_gpu_status amps_gpu_clear_injection(amps_gpu_ctx* ctx);

@@ -289,14 +289,86 @@ long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* sp
  * kept).  Random numbers: the counter-based stream the device uses (a
  * splitmix64 finaliser over (seed, step, source, face cell, draw)).  Writes up
  * to cap particles (x, v, block, cell); returns how many were kept. */
-static unsigned long long inj_mix(unsigned long long z) {
+unsigned long long orc_inj_mix(unsigned long long z) {
   z += 0x9E3779B97F4A7C15ull;
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
 }
-static double inj_uniform(unsigned long long key, unsigned* d) {
-  return ((double)(inj_mix(key + ((*d)++)) >> 11) + 0.5) * 1.1102230246251565e-16;
+double orc_inj_uniform(unsigned long long key, unsigned* d) {
+  return ((double)(orc_inj_mix(key + ((*d)++)) >> 11) + 0.5) * 1.1102230246251565e-16;
+}
+/* the stream of face cell (or finest face patch) c of source src at step */
+unsigned long long orc_inj_key(unsigned long long seed, unsigned long long step, int src, long c) {
+  return orc_inj_mix(orc_inj_mix(orc_inj_mix(seed) ^ step) ^ (((unsigned long long)src << 40) | (unsigned long long)c));
+}
+
+/* CalculateInjectionRate_MaxwellianDistribution (pic_bc.cpp:215): particles
+ * per unit area and time through a face of outward normal nrm */
+double orc_inj_flux(double density, const double drift[3], double vth, const double nrm[3]) {
+  const double beta = 1.0 / (sqrt(2.0) * vth);
+  double vv = 0.0, vnorm = 0.0;
+  for (int d = 0; d < 3; d++) { vv += drift[d] * drift[d]; vnorm += drift[d] * nrm[d]; }
+  vv = sqrt(vv);
+  const double sq = 1.7724538509055160273, sc = vv * beta;
+  if (sc > 10.0 && vnorm < 0.0) return fabs(vnorm) * density;
+  if (sc > 10.0 && vnorm > 0.0) return 0.0;
+  double aa;
+  if (vv > 1.0e-6) {
+    const double cc = -vnorm / vv;
+    aa = (exp(-sc * sc * cc * cc) + sq * sc * cc * (1.0 + erf(sc * cc))) / (2.0 * sq);
+  } else {
+    aa = 1.0 / (2.0 * sq);
+  }
+  return fabs(aa) * density / beta;
+}
+
+/* InjectMaxwellianDistribution (pic_vel_distribution.cpp:49, 3D branch):
+ * an inward velocity drawn from stream key (draw counter d); 0 when the
+ * bounded rejection loops did not finish */
+int orc_inj_velocity(unsigned long long key, unsigned* d, const double drift[3], const double nrm[3],
+                     double beta, double v[3]) {
+  int ok = 0;
+  v[0] = v[1] = v[2] = 0.0;
+  for (int outer = 0; outer < 64 && !ok; outer++) {
+    const double dot = drift[0] * nrm[0] + drift[1] * nrm[1] + drift[2] * nrm[2];
+    const double sc = beta * fabs(dot);
+    double u = 0.0, acc = 0.0;
+    int got = 0;
+    for (int tries = 0; tries < 4096 && !got; tries++) {
+      if (dot <= 0.0) {
+        int q = 0;
+        do u = -10.0 + 20.0 * orc_inj_uniform(key, d); while (u + sc <= 0.0 && ++q < 4096);
+        const double cc = sqrt(2.0 + sc * sc);
+        acc = 2.0 * (u + sc) / (sc + cc) * exp(0.5 + 0.5 * sc * (sc - cc) - u * u);
+      } else {
+        int q = 0;
+        do u = -10.0 + 20.0 * orc_inj_uniform(key, d); while (u + sc >= 0.0 && ++q < 4096);
+        const double cc = 0.5 * (-sqrt(sc * sc + 2.0) - sc);
+        acc = (u + sc) * exp(-u * u) / (cc + sc) / exp(-cc * cc);
+      }
+      got = !(acc < orc_inj_uniform(key, d));
+    }
+    if (!got) break;
+    double v1[3], v2[3], v3[3];
+    for (int q = 0; q < 3; q++) v3[q] = -(fabs(u + sc) / beta) * nrm[q];
+    if (fabs(nrm[0]) > 1.0e-3) { v2[0] = nrm[1]; v2[1] = -nrm[0]; v2[2] = 0.0; }
+    else { v2[0] = 0.0; v2[1] = nrm[2]; v2[2] = -nrm[1]; }
+    double l2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
+    for (int q = 0; q < 3; q++) v2[q] /= l2;
+    v1[0] = v2[1] * nrm[2] - v2[2] * nrm[1];
+    v1[1] = -(v2[0] * nrm[2] - v2[2] * nrm[0]);
+    v1[2] = v2[0] * nrm[1] - v2[1] * nrm[0];
+    double l1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+    for (int q = 0; q < 3; q++) v1[q] /= l1;
+    const double cm = sqrt(-log(orc_inj_uniform(key, d))) / beta, cp = orc_inj_uniform(key, d);
+    const double d1 = drift[0] * v1[0] + drift[1] * v1[1] + drift[2] * v1[2];
+    const double d2 = drift[0] * v2[0] + drift[1] * v2[1] + drift[2] * v2[2];
+    for (int q = 0; q < 3; q++)
+      v[q] = (cm * sin(2.0 * PI_D * cp) + d1) * v1[q] + (cm * cos(2.0 * PI_D * cp) + d2) * v2[q] + v3[q];
+    ok = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2] < 0.0;
+  }
+  return ok;
 }
 
 long orc_inject(const orc_mesh* g, int face, int spec, double density, const double drift[3],
@@ -308,80 +380,22 @@ long orc_inject(const orc_mesh* g, int face, int spec, double density, const dou
   const double beta = 1.0 / (sqrt(2.0) * vth);
   double nrm[3] = {0, 0, 0};
   nrm[ax] = hi ? 1.0 : -1.0;
-  /* CalculateInjectionRate_MaxwellianDistribution */
-  double vv = 0.0, vnorm = 0.0, flux;
-  for (int d = 0; d < 3; d++) { vv += drift[d] * drift[d]; vnorm += drift[d] * nrm[d]; }
-  vv = sqrt(vv);
-  {
-    const double sq = 1.7724538509055160273, sc = vv * beta;
-    if (sc > 10.0 && vnorm < 0.0) flux = fabs(vnorm) * density;
-    else if (sc > 10.0 && vnorm > 0.0) flux = 0.0;
-    else {
-      double aa;
-      if (vv > 1.0e-6) {
-        const double cc = -vnorm / vv;
-        aa = (exp(-sc * sc * cc * cc) + sq * sc * cc * (1.0 + erf(sc * cc))) / (2.0 * sq);
-      } else {
-        aa = 1.0 / (2.0 * sq);
-      }
-      flux = fabs(aa) * density / beta;
-    }
-  }
+  const double flux = orc_inj_flux(density, drift, vth, nrm);
   const double R = (flux / g->w[spec]) * (g->dx[ta] * g->dx[tb]);  /* the device's order */
   const int NT = NC * nb[ta], ncell = NT * NC * nb[tb];
   long kept = 0;
   if (!(R > 0.0)) return 0;
   for (int c = 0; c < ncell; c++) {
     const int it = c % NT, ib = c / NT;
-    const unsigned long long key =
-        inj_mix(inj_mix(inj_mix(seed) ^ step) ^ (((unsigned long long)src << 40) | (unsigned long long)c));
+    const unsigned long long key = orc_inj_key(seed, step, src, c);
     unsigned d = 0;
     double tt = 0.0;
     for (int k = 0; k < 4096; k++) {
-      tt += -log(inj_uniform(key, &d)) / R;
+      tt += -log(orc_inj_uniform(key, &d)) / R;
       if (tt >= g->dt) break;
-      const double c0 = inj_uniform(key, &d), c1 = inj_uniform(key, &d);
-      double v[3] = {0, 0, 0};
-      int ok = 0;
-      for (int outer = 0; outer < 64 && !ok; outer++) {
-        const double dot = drift[0] * nrm[0] + drift[1] * nrm[1] + drift[2] * nrm[2];
-        const double sc = beta * fabs(dot);
-        double u = 0.0, acc = 0.0;
-        int got = 0;
-        for (int tries = 0; tries < 4096 && !got; tries++) {
-          if (dot <= 0.0) {
-            int q = 0;
-            do u = -10.0 + 20.0 * inj_uniform(key, &d); while (u + sc <= 0.0 && ++q < 4096);
-            const double cc = sqrt(2.0 + sc * sc);
-            acc = 2.0 * (u + sc) / (sc + cc) * exp(0.5 + 0.5 * sc * (sc - cc) - u * u);
-          } else {
-            int q = 0;
-            do u = -10.0 + 20.0 * inj_uniform(key, &d); while (u + sc >= 0.0 && ++q < 4096);
-            const double cc = 0.5 * (-sqrt(sc * sc + 2.0) - sc);
-            acc = (u + sc) * exp(-u * u) / (cc + sc) / exp(-cc * cc);
-          }
-          got = !(acc < inj_uniform(key, &d));
-        }
-        if (!got) break;
-        double v1[3], v2[3], v3[3];
-        for (int q = 0; q < 3; q++) v3[q] = -(fabs(u + sc) / beta) * nrm[q];
-        if (fabs(nrm[0]) > 1.0e-3) { v2[0] = nrm[1]; v2[1] = -nrm[0]; v2[2] = 0.0; }
-        else { v2[0] = 0.0; v2[1] = nrm[2]; v2[2] = -nrm[1]; }
-        double l2 = sqrt(v2[0] * v2[0] + v2[1] * v2[1] + v2[2] * v2[2]);
-        for (int q = 0; q < 3; q++) v2[q] /= l2;
-        v1[0] = v2[1] * nrm[2] - v2[2] * nrm[1];
-        v1[1] = -(v2[0] * nrm[2] - v2[2] * nrm[0]);
-        v1[2] = v2[0] * nrm[1] - v2[1] * nrm[0];
-        double l1 = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
-        for (int q = 0; q < 3; q++) v1[q] /= l1;
-        const double cm = sqrt(-log(inj_uniform(key, &d))) / beta, cp = inj_uniform(key, &d);
-        const double d1 = drift[0] * v1[0] + drift[1] * v1[1] + drift[2] * v1[2];
-        const double d2 = drift[0] * v2[0] + drift[1] * v2[1] + drift[2] * v2[2];
-        for (int q = 0; q < 3; q++)
-          v[q] = (cm * sin(2.0 * PI_D * cp) + d1) * v1[q] + (cm * cos(2.0 * PI_D * cp) + d2) * v2[q] + v3[q];
-        ok = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2] < 0.0;
-      }
-      if (!ok) return -1;
+      const double c0 = orc_inj_uniform(key, &d), c1 = orc_inj_uniform(key, &d);
+      double v[3];
+      if (!orc_inj_velocity(key, &d, drift, nrm, beta, v)) return -1;
       /* the face point, then the push for the rest of the step */
       double x[3];
       x[ax] = g->x0[ax] + (hi ? nb[ax] * NC * g->dx[ax] : 0.0);

@@ -27,6 +27,12 @@
 #define PI_D 3.14159265358979323846264338327950288
 
 extern int orc_open_axes; /* amps_oracle.c */
+/* injection helpers (amps_oracle.c) */
+unsigned long long orc_inj_key(unsigned long long seed, unsigned long long step, int src, long c);
+double orc_inj_uniform(unsigned long long key, unsigned* d);
+double orc_inj_flux(double density, const double drift[3], double vth, const double nrm[3]);
+int orc_inj_velocity(unsigned long long key, unsigned* d, const double drift[3], const double nrm[3],
+                     double beta, double v[3]);
 #define NSPEC_MAX 8
 
 typedef struct {
@@ -187,6 +193,84 @@ long orc_amr_push(const orc_amr* g, long n, double* x, double* v, const uint8_t*
       locate_one(g, x + 3 * p, block + p, cell + p);
   }
   return 0;
+}
+
+/* OpenFlow injection through face `face` of an open axis on the AMR mesh
+ * (pic_bc.cpp:270-440 with CalculateInjectionRate_MaxwellianDistribution :215
+ * and InjectMaxwellianDistribution, pic_vel_distribution.cpp:49): the face is
+ * cut into finest-lattice patches (patch c = it + nfine[ta] ib), each with its
+ * own Poisson stream (the device's key); an arrival at time tt is placed
+ * uniformly on its patch, pushed with Lapenta2017 for dt - tt with the fields
+ * of the leaf block owning the patch's boundary cell, and kept when it stays
+ * in the domain.  Returns the kept count (-1: sampling bound hit). */
+long orc_amr_inject(const orc_amr* g, int face, int spec, double density, const double drift[3],
+                    double vth, unsigned long long seed, unsigned long long step, int src,
+                    const double* E_half, const double* Bc_prev, long cap, double* xo, double* vo,
+                    int32_t* blk, int32_t* cel) {
+  const int ax = face >> 1, hi = face & 1, ta = (ax + 1) % 3, tb = (ax + 2) % 3;
+  const double dxf = g->dx0 / (double)(1 << g->lmax);
+  const double beta = 1.0 / (sqrt(2.0) * vth);
+  double nrm[3] = {0, 0, 0};
+  nrm[ax] = hi ? 1.0 : -1.0;
+  const double flux = orc_inj_flux(density, drift, vth, nrm);
+  const double R = (flux / g->w[spec]) * (dxf * dxf);  /* the device's order */
+  const int NT = g->nfine[ta], np = NT * g->nfine[tb];
+  long kept = 0;
+  if (!(R > 0.0)) return 0;
+  for (int c = 0; c < np; c++) {
+    const int it = c % NT, ib = c / NT;
+    const unsigned long long key = orc_inj_key(seed, step, src, c);
+    unsigned d = 0;
+    double tt = 0.0;
+    for (int k = 0; k < 4096; k++) {
+      tt += -log(orc_inj_uniform(key, &d)) / R;
+      if (tt >= g->dt) break;
+      const double c0 = orc_inj_uniform(key, &d), c1 = orc_inj_uniform(key, &d);
+      double v[3];
+      if (!orc_inj_velocity(key, &d, drift, nrm, beta, v)) return -1;
+      /* the face point and the leaf block owning the patch's boundary cell */
+      int F[3];
+      F[ax] = hi ? g->nfine[ax] - 1 : 0;
+      F[ta] = it;
+      F[tb] = ib;
+      const int nfb0 = g->nfine[0] / 8, nfb1 = g->nfine[1] / 8;
+      const int b = g->fine_map[F[0] / 8 + nfb0 * (F[1] / 8 + nfb1 * (F[2] / 8))];
+      double x[3];
+      x[ax] = g->x0[ax] + (hi ? g->nfine[ax] * dxf : 0.0);
+      x[ta] = g->x0[ta] + (it + c0) * dxf;
+      x[tb] = g->x0[tb] + (ib + c1) * dxf;
+      double w[8], E[3] = {0, 0, 0}, B[3] = {0, 0, 0}, val[3], xs[3] = {x[0], x[1], x[2]};
+      int cid[8];
+      stencil(g, b, xs, w, cid);
+      for (int q = 0; q < 8; q++) {
+        corner_val(g, E_half, cid[q], val);
+        for (int e = 0; e < 3; e++) E[e] += w[q] * val[e];
+        corner_val(g, Bc_prev, cid[q], val);
+        for (int e = 0; e < 3; e++) B[e] += w[q] * val[e];
+      }
+      const double drem = g->dt - tt;
+      const double h = 0.5 * g->q[spec] * drem / g->m[spec];
+      double al[9], vF[3];
+      alpha_matrix(h, B, al);
+      for (int i = 0; i < 3; i++) {
+        double vp = 0.0;
+        for (int j = 0; j < 3; j++) vp += al[3 * i + j] * (v[j] + h * E[j]);
+        vF[i] = 2.0 * vp - v[i];
+      }
+      int gone = 0;
+      for (int q = 0; q < 3; q++) {
+        x[q] += drem * vF[q];
+        if (((orc_open_axes >> q) & 1) && (x[q] < g->x0[q] || x[q] >= g->x0[q] + g->nfine[q] * dxf)) gone = 1;
+      }
+      if (gone) continue;
+      if (kept < cap) {
+        locate_one(g, x, blk + kept, cel + kept);
+        for (int q = 0; q < 3; q++) { xo[3 * kept + q] = x[q]; vo[3 * kept + q] = vF[q]; }
+      }
+      kept++;
+    }
+  }
+  return kept;
 }
 
 /* per-cell partials (cellJ[ncell*24] = sum q W w_c alpha v; cellM[ncell*324] =

@@ -43,6 +43,9 @@ def lib():
             "orc_amr_update_e": (C.c_double, [C.POINTER(Amr), D, D, D]),
             "orc_amr_step": (C.c_int, [C.POINTER(Amr), C.c_long, D, D, U8, D, I32, I32, D, D, D,
                                        D, D, D, D, C.c_double, C.c_int, D]),
+            "orc_amr_inject": (C.c_long, [C.POINTER(Amr), C.c_int, C.c_int, C.c_double, D, C.c_double,
+                                          C.c_ulonglong, C.c_ulonglong, C.c_int, D, D, C.c_long, D, D,
+                                          I32, I32]),
         }
         for k, (r, a) in sig.items():
             f = getattr(L, k)

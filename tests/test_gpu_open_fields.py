@@ -132,3 +132,47 @@ def test_open_mesh_fixes_particle_open_axes():
         ctx.set_open_axes(True, False, False)
         with pytest.raises(A.AmpsGpuError):
             ctx.set_open_axes(False, False, False)
+
+
+def test_amr_injection_matches_oracle(open_oracle):
+    """OpenFlow injection on a two-level mesh with open x: the same finest-patch
+    streams on the device and in the oracle give the same injected particles
+    (count, positions after the partial push, velocities)"""
+    from tests.test_gpu_injection import match
+    import ctypes as C
+    from tests.oracle_amr import p as pa
+    mesh, wl, ic, x, f = open_case((4, 4, 4), 1, (True, False, False), 1, seed=85)
+    open_oracle.orc_set_open_axes(1)
+    e, i = wl.species
+    srcs = [(0, 0, 400.0 * e.weight, e.vth, (0.02, 0.0, 0.0)),
+            (1, 1, 400.0 * i.weight, i.vth, (-0.004, 0.001, 0.0))]
+    ao = oracle_for(mesh, wl, ic, x, f)
+    with gpu_for(mesh, wl, ic, x, f) as ctx:
+        ctx.set_injection_seed(91)
+        for face, spec, dens, vth, drift in srcs:
+            ctx.add_injection(face, spec, dens, vth, drift)
+        n0 = ctx.num_particles()
+        ctx.push_deposit()
+        ao.push()
+        xs, vs = [], []
+        for s, (face, spec, dens, vth, drift) in enumerate(srcs):
+            cap = 400000
+            xo, vo = np.zeros((cap, 3)), np.zeros((cap, 3))
+            blk, cel = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+            k = ao.L.orc_amr_inject(C.byref(ao.g), face, spec, dens, pa(np.array(drift, np.float64)), vth, 91, 0,
+                                    s, pa(ao.E_half), pa(ao.Bprev), cap, pa(xo), pa(vo), pa(blk, C.c_int32),
+                                    pa(cel, C.c_int32))
+            assert 50 < k <= cap
+            xs.append(xo[:k]); vs.append(vo[:k])
+        xi, vi = np.concatenate(xs), np.concatenate(vs)
+        ninj = ctx.injected_particles()
+        assert ninj == len(xi)
+        alive = ao.block >= 0
+        assert ctx.num_particles() == n0 - (~alive).sum() + ninj
+        g = ctx.export_particles()
+        order = np.argsort(g["id"])
+        g = {k: v[order] for k, v in g.items()}
+        new = g["id"] >= n0
+        m = match(g["x"][new], xi)
+        assert np.abs(g["x"][new] - xi[m]).max() <= 1e-5 * mesh.dx0
+        assert np.abs(g["v"][new] - vi[m]).max() <= 2e-5 * np.abs(vi).max()
