@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   float* rec = s_rec + wid * 32 * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
-  double en = 0.0;
+  float en_row = 0.f;  // FP32 across the row's cells, FP64 in the CTA reduction
   unsigned long long n_far = 0, n_near = 0, n_del = 0;
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
@@ -389,13 +389,13 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
     if (lane == 0) a.stay[cid] = nst;
     if (DEP) {
       tile.flush(lane, a.cellM, a.cellJ, cid, false);
-      en += (double)en_cell;
+      en_row += en_cell;
     }
   }
   if (n_far) atomicAdd(a.flags + 0, n_far);
   if (n_near) atomicAdd(a.flags + 1, n_near);
   if (n_del) atomicAdd(a.flags + 5, n_del);
-  if (DEP) reduce_energy(en, s_en, a.energy);
+  if (DEP) reduce_energy((double)en_row, s_en, a.energy);
 }
 
 // ---------------------------------------------------------------------------
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   float* rec = s_rec + wid * kArrChunk * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
-  double en = 0.0;
+  float en_row = 0.f;  // the row's arrivals: a few per cell, FP32 is enough before the FP64 reduction
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
   // the row's 8 cells: lane i < 8 loads cell i's slot range, occupancy, stayers
@@ -668,6 +668,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     if (na > 0) {
       Tile tile;
       tile.zero();
+      float en_cell = 0.f;  // FP32 per cell, FP64 across cells (FP64 issues slowly here)
       float old[9];
       if (DEP) tile.preload(lane, a.cellM, a.cellJ, cid, old);
       const int src0 = b0 + cap - na, dst0 = b0 + nst;
@@ -693,8 +694,8 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
           if (a.p.wc) a.p.wc[pd] = wcv;
           if (a.p.id) a.p.id[pd] = idv;
           if (DEP)
-            en += stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
-                               wcv, i, j, k, a.st, inv_vol);
+            en_cell += stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+                                    wcv, i, j, k, a.st, inv_vol);
         }
         if (DEP) {
           __syncwarp();
@@ -710,6 +711,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
         if (slot >= dst0 + na) a.p.sp[slot] = kHole;
       }
       if (DEP) tile.flush_onto(lane, a.cellM, a.cellJ, cid, old);
+      en_row += en_cell;
     }
   }
   if (lane < AMPS_NC) {
@@ -717,7 +719,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     a.cnt[cl] = mst + max(0, min(marr, mcap - mn0));
     a.arr[cl] = 0;
   }
-  if (DEP) reduce_energy(en, s_en, a.energy);
+  if (DEP) reduce_energy((double)en_row, s_en, a.energy);
 }
 
 // Full deposition over the compact layout.
