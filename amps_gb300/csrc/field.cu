@@ -187,7 +187,7 @@ TapsF taps_f32(const Taps& T) {
 
 // y = A (dinv .* x) with the identity part in FP64 and the rest (curl-curl
 // and mass-matrix terms, a small fraction of A on ECSIM time steps) in FP32
-// arithmetic: the inner operator of the refined GMRES, never the judge of
+// arithmetic: the inner operator of the refined GMRES, which never decides
 // convergence.  One thread per (component p, corner).
 __global__ void __launch_bounds__(256) k_matvec32(long long ncor, const int* __restrict__ nbr,
                                                   const float* __restrict__ M,
