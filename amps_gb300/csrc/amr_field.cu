@@ -931,8 +931,8 @@ cudaError_t launch_amr_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, f
   if (!c->d_xs && (e = cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n)) != cudaSuccess)
     return e;
   a.xf = c->d_xs;
-  TimedLaunch t(c, "matvec32", 3);
-  if ((e = launch_in_f32(c, in, c->d_xs)) != cudaSuccess) return e;
+  TimedLaunch t(c, "matvec32", in.xf_ready ? 2 : 3);
+  if (!in.xf_ready && (e = launch_in_f32(c, in, c->d_xs)) != cudaSuccess) return e;
   if ((e = launch_tile<0>(c, a, c->d_y32, nullptr)) != cudaSuccess) return e;
   k_amr_finish_ff<<<g1(c->nvc), 256, 0, c->stream>>>(c->nvc, a.h, c->d_ss, c->d_sc, c->d_svh, c->d_svl,
                                                       c->d_y32, in, wh, wl);

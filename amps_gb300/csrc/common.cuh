@@ -284,6 +284,7 @@ struct OpIn {
   const float* vl;
   const float* dh;
   const float* dl;
+  bool xf_ready;  // fp32(D v) already in the context's scratch (written by the Arnoldi step)
 };
 cudaError_t launch_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, float* wl);
 // xf = fp32(D v), the FP32 operator's input

@@ -518,7 +518,8 @@ __global__ void __launch_bounds__(kArnThreads) k_arnoldi_ff(long long n, const f
                                                              float* __restrict__ w, int nv,
                                                              float* __restrict__ vnext,
                                                              float* __restrict__ part, GmState* gs,
-                                                             int jj) {
+                                                             int jj, float* __restrict__ xf,
+                                                             const float* __restrict__ dh) {
   cg::grid_group grid = cg::this_grid();
   __shared__ float s_red[2 * (kArnThreads / 32) * kMaxV];
   __shared__ double s_h1[kMaxV], s_h2[kMaxV], s_n2[1];
@@ -646,13 +647,23 @@ __global__ void __launch_bounds__(kArnThreads) k_arnoldi_ff(long long n, const f
     }
     stv<L>(vnext, t, a);
     stv<L>(vnext + n, t, b);
+    if (xf) {
+      // the next operator's FP32 input fp32(D V_nv), written while it is in registers
+      if (dh) {
+        float dd[L];
+        ldv<L>(dh, t, dd);
+#pragma unroll
+        for (int k = 0; k < L; k++) a[k] *= dd[k];
+      }
+      stv<L>(xf, t, a);
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) gm_update(gs, jj, s_h1, s_h2, s_n2[0]);
 }
 
 template <int NVM, int L>
 cudaError_t launch_arnoldi_ff_l(cudaStream_t s, long long n, const float* V, float* w, int nv,
-                                float* vnext, float* part, GmState* gs, int jj) {
+                                float* vnext, float* part, GmState* gs, int jj, float* xf, const float* dh) {
   static int grid[64] = {0};  // per device: co-resident CTAs
   int dev = 0;
   cudaGetDevice(&dev);
@@ -668,22 +679,23 @@ cudaError_t launch_arnoldi_ff_l(cudaStream_t s, long long n, const float* V, flo
   }
   const long long want = (n / L + kArnThreads - 1) / kArnThreads;
   const unsigned g = (unsigned)std::max<long long>(1, std::min<long long>(grid[dev], want));
-  void* args[] = {&n, &V, &w, &nv, &vnext, &part, &gs, &jj};
+  void* args[] = {&n, &V, &w, &nv, &vnext, &part, &gs, &jj, &xf, &dh};
   return cudaLaunchCooperativeKernel((const void*)k_arnoldi_ff<NVM, L>, dim3(g), dim3(kArnThreads), args, 0, s);
 }
 
 // the widest streams at which every pair vector's hi and lo start aligned
 template <int NVM>
 cudaError_t launch_arnoldi_ff(cudaStream_t s, long long n, const float* V, float* w, int nv,
-                              float* vnext, float* part, GmState* gs, int jj) {
-  if (n % 4 == 0) return launch_arnoldi_ff_l<NVM, 4>(s, n, V, w, nv, vnext, part, gs, jj);
-  if (n % 2 == 0) return launch_arnoldi_ff_l<NVM, 2>(s, n, V, w, nv, vnext, part, gs, jj);
-  return launch_arnoldi_ff_l<NVM, 1>(s, n, V, w, nv, vnext, part, gs, jj);
+                              float* vnext, float* part, GmState* gs, int jj, float* xf, const float* dh) {
+  if (n % 4 == 0) return launch_arnoldi_ff_l<NVM, 4>(s, n, V, w, nv, vnext, part, gs, jj, xf, dh);
+  if (n % 2 == 0) return launch_arnoldi_ff_l<NVM, 2>(s, n, V, w, nv, vnext, part, gs, jj, xf, dh);
+  return launch_arnoldi_ff_l<NVM, 1>(s, n, V, w, nv, vnext, part, gs, jj, xf, dh);
 }
 
 // V0 = r / ||r|| as a pair vector (nrm2: ||r||^2)
 __global__ void __launch_bounds__(256) k_start_ff(long long n, const double* __restrict__ r,
-                                                  const double* __restrict__ nrm2, float* __restrict__ v) {
+                                                  const double* __restrict__ nrm2, float* __restrict__ v,
+                                                  float* __restrict__ xf, const float* __restrict__ dh) {
   const double sc = *nrm2 > 0.0 ? 1.0 / sqrt(*nrm2) : 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
        t += (long long)gridDim.x * blockDim.x) {
@@ -691,6 +703,7 @@ __global__ void __launch_bounds__(256) k_start_ff(long long n, const double* __r
     const float h = (float)x;
     v[t] = h;
     v[n + t] = (float)(x - (double)h);
+    if (xf) xf[t] = dh ? h * dh[t] : h;  // the first operator's FP32 input
   }
 }
 
@@ -966,8 +979,8 @@ cudaError_t launch_matvec32_ff(amps_gpu_ctx* c, const OpIn& in, float* wh, float
     if (e != cudaSuccess) return e;
   }
   const TapsF T = taps_f32(make_taps(c->cfg, false));
-  TimedLaunch t(c, "matvec32", 2);
-  cudaError_t e = launch_in_f32(c, in, c->d_xs);
+  TimedLaunch t(c, "matvec32", in.xf_ready ? 1 : 2);
+  cudaError_t e = in.xf_ready ? cudaSuccess : launch_in_f32(c, in, c->d_xs);
   if (e != cudaSuccess) return e;
   k_matvec32_ff<<<gridt(n, c->tune_tb), c->tune_tb, 0, c->stream>>>(c->ncor, c->d_nbr, c->d_M, c->d_xs, in,
                                                                      wh, wl, T);
@@ -1084,6 +1097,12 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   if ((flexible || harvest || !c->inner_fp32) && !c->d_tmpv)
     CK(cudaMalloc(reinterpret_cast<void**>(&c->d_tmpv), sizeof(double) * 2 * n));
   // w = A (D v_j), or A z_j for the flexible directions, as pairs
+  // the FP32 operator input of the next Krylov vector is written by the step
+  // that makes the vector (k_start_ff, k_arnoldi_ff) when the operator takes V
+  // directly (no learned directions, FP32 inner operator)
+  const bool pre_xf = !flexible && c->inner_fp32;
+  if (pre_xf && !c->d_xs) CK(cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n));
+  float* xf_next = pre_xf ? c->d_xs : nullptr;
   auto inner_matvec = [&](int jj, const double* zj) -> cudaError_t {
     if (c->inner_fp32) {
       OpIn in{};
@@ -1094,6 +1113,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
         in.vl = vf(jj) + n;
         in.dh = dh;
         in.dl = dl;
+        in.xf_ready = pre_xf;
       }
       return launch_matvec32_ff(c, in, wf, wf + n);
     }
@@ -1141,7 +1161,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     const double target = tol * bnorm;
     // V0 = r / ||r|| (d_n2 holds ||r||^2 from read_norm)
     k_gm_start<<<1, 32, 0, s>>>(gs, d_n2, target);
-    k_start_ff<<<gr, 256, 0, s>>>(n, w, d_n2, vf(0));
+    k_start_ff<<<gr, 256, 0, s>>>(n, w, d_n2, vf(0), xf_next, dh);
     int launched = 0, used = 0;
     bool done = false;
     const int first_read = cycles == 1 ? std::max(1, std::min(c->gm_guess[precond], m)) : 1;
@@ -1167,13 +1187,13 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
         float* part = reinterpret_cast<float*>(c->d_arn);
         float* vnext = vf(nv);
         if (nv <= 4)
-          e = launch_arnoldi_ff<4>(s, n, Vf, wf, nv, vnext, part, gs, jj);
+          e = launch_arnoldi_ff<4>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
         else if (nv <= 8)
-          e = launch_arnoldi_ff<8>(s, n, Vf, wf, nv, vnext, part, gs, jj);
+          e = launch_arnoldi_ff<8>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
         else if (nv <= 16)
-          e = launch_arnoldi_ff<16>(s, n, Vf, wf, nv, vnext, part, gs, jj);
+          e = launch_arnoldi_ff<16>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
         else
-          e = launch_arnoldi_ff<32>(s, n, Vf, wf, nv, vnext, part, gs, jj);
+          e = launch_arnoldi_ff<32>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
         if (e != cudaSuccess) return cuda_check(c, e, "arnoldi step");
       }
       CK(cudaGetLastError());
