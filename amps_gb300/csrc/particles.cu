@@ -1293,6 +1293,151 @@ __global__ void __launch_bounds__(256) k_relboris(RelBorisArgs a) {
   if (my_sub) atomicAdd(a.nsub, my_sub);
 }
 
+// The same mover on a periodic AMR mesh (block tree of AmrDev): at the start
+// of every sub-step the particle is re-located (periodic wrap, finest-block
+// map: k_import_amr's rules) and E, B are interpolated from that leaf block's
+// 8 cell corners (FP64 component-major corner arrays over the unique corners;
+// a hanging corner takes its constraint P, CSR hs/hp/hw).  The sub-step rule
+// and the update are k_relboris's.
+struct AmrRelBorisArgs {
+  PBuf d;
+  int* key;
+  long long n;
+  AmrDev m;
+  const int* ctab;
+  const int* hs;
+  const int* hp;
+  const double* hw;
+  long long nvc;
+  const double* E;
+  const double* B;
+  double x0[3], dxf;
+  double qm[AMPS_GPU_MAX_SPECIES];
+  double qabs_over_m[AMPS_GPU_MAX_SPECIES];
+  double dt_total, c_light;
+  long long max_sub;
+  unsigned long long* flags;
+  unsigned long long* nsub;
+};
+
+__device__ __forceinline__ int amr_rb_locate(const AmrRelBorisArgs& a, double x[3]) {
+  int F[3];
+  for (int d = 0; d < 3; d++) {
+    const double L = a.m.nfine[d] * a.dxf;
+    // a sub-step can carry a fast particle more than one period
+    const double k = floor((x[d] - a.x0[d]) / L);
+    if (k != 0.0) x[d] -= k * L;
+    if (x[d] < a.x0[d]) x[d] += L;
+    if (x[d] >= a.x0[d] + L) x[d] -= L;
+    if (x[d] >= a.x0[d] + L) x[d] = a.x0[d] + L - 1e-10 * a.dxf;
+    if (x[d] < a.x0[d]) x[d] = a.x0[d];
+    F[d] = min(max((int)floor((x[d] - a.x0[d]) / a.dxf), 0), a.m.nfine[d] - 1);
+  }
+  const int nb0 = a.m.nfine[0] >> 3, nb1 = a.m.nfine[1] >> 3;
+  return a.m.fine_map[(F[0] >> 3) + nb0 * ((F[1] >> 3) + nb1 * (F[2] >> 3))];
+}
+
+__global__ void __launch_bounds__(256) k_amr_relboris(AmrRelBorisArgs a) {
+  unsigned long long my_sub = 0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int blk = a.key[p] / AMPS_CPB;
+    const int sp = a.d.sp[p];
+    double x[3], v[3];
+    for (int d = 0; d < 3; d++) {
+      x[d] = a.x0[d] + a.m.borg[3 * blk + d] * a.dxf + (double)a.d.u[d][p] * (a.m.bscale[blk] * a.dxf);
+      v[d] = a.d.v[d][p];
+    }
+    const double cc2 = a.c_light * a.c_light;
+    double rem = a.dt_total;
+    long long ns = 0;
+    while (rem > 0.0) {
+      if (ns >= a.max_sub) {
+        atomicAdd(a.flags + 2, 1ull);
+        break;
+      }
+      blk = amr_rb_locate(a, x);
+      const double dx = a.m.bscale[blk] * a.dxf;
+      int ic[3];
+      double f[3];
+      for (int d = 0; d < 3; d++) {
+        const double u = (x[d] - (a.x0[d] + a.m.borg[3 * blk + d] * a.dxf)) / dx;
+        ic[d] = min(max((int)u, 0), AMPS_NC - 1);
+        f[d] = u - ic[d];
+      }
+      double Ef[3] = {0, 0, 0}, Bf[3] = {0, 0, 0};
+#pragma unroll 1
+      for (int q = 0; q < 8; q++) {
+        // table order (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1) (1,1,1) (0,1,1)
+        const int ox = ((q + 1) >> 1) & 1, oy = (q >> 1) & 1, oz = q >> 2;
+        const double w = 1.0 * (ox ? f[0] : 1.0 - f[0]) * (oy ? f[1] : 1.0 - f[1]) * (oz ? f[2] : 1.0 - f[2]);
+        const int cc = a.ctab[blk * 729 + (ic[0] + ox) + 9 * ((ic[1] + oy) + 9 * (ic[2] + oz))];
+        const int hs0 = a.hs[cc], hs1 = a.hs[cc + 1];
+        for (int d = 0; d < 3; d++) {
+          double e, b;
+          if (hs0 == hs1) {
+            e = a.E[d * a.nvc + cc];
+            b = a.B[d * a.nvc + cc];
+          } else {
+            e = 0.0;
+            b = 0.0;
+            for (int t = hs0; t < hs1; t++) {
+              e += a.hw[t] * a.E[d * a.nvc + a.hp[t]];
+              b += a.hw[t] * a.B[d * a.nvc + a.hp[t]];
+            }
+          }
+          Ef[d] += w * e;
+          Bf[d] += w * b;
+        }
+      }
+      double gam = 1.0 / sqrt(1.0 - (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / cc2);
+      const double bmag = sqrt(Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
+      double dt = rem;
+      if (bmag > 1.0e-25) {
+        const double dtmax = 1.0 / (a.qabs_over_m[sp] * bmag / (2.0 * 3.14159265358979323846 * gam));
+        if (dtmax < rem) dt = dtmax;
+      }
+      rem -= dt;
+      const double h = 0.5 * a.qm[sp] * dt;
+      double um[3], t[3], up[3], sv[3], upl[3], uf[3], l = 0.0;
+      for (int d = 0; d < 3; d++) um[d] = gam * v[d] + h * Ef[d];
+      gam = sqrt(1.0 + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]) / cc2);
+      for (int d = 0; d < 3; d++) { t[d] = h / gam * Bf[d]; l += t[d] * t[d]; }
+      up[0] = um[0] + (um[1] * t[2] - um[2] * t[1]);
+      up[1] = um[1] + (um[2] * t[0] - um[0] * t[2]);
+      up[2] = um[2] + (um[0] * t[1] - um[1] * t[0]);
+      for (int d = 0; d < 3; d++) sv[d] = 2.0 * t[d] / (1.0 + l);
+      upl[0] = um[0] + (up[1] * sv[2] - up[2] * sv[1]);
+      upl[1] = um[1] + (up[2] * sv[0] - up[0] * sv[2]);
+      upl[2] = um[2] + (up[0] * sv[1] - up[1] * sv[0]);
+      for (int d = 0; d < 3; d++) uf[d] = upl[d] + h * Ef[d];
+      gam = sqrt(1.0 + (uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2]) / cc2);
+      for (int d = 0; d < 3; d++) {
+        v[d] = uf[d] / gam;
+        x[d] += v[d] * dt;
+      }
+      ns++;
+    }
+    my_sub += (unsigned long long)ns;
+    // final leaf block, cell and FP32 offset (k_import_amr's rules)
+    blk = amr_rb_locate(a, x);
+    const double dx = a.m.bscale[blk] * a.dxf;
+    int ic[3];
+    for (int d = 0; d < 3; d++) {
+      const double ud = (x[d] - (a.x0[d] + a.m.borg[3 * blk + d] * a.dxf)) / dx;
+      const int ci = min(max((int)ud, 0), AMPS_NC - 1);
+      float u = (float)ud;
+      if (u < (float)ci) u = (float)ci;
+      if (u >= (float)(ci + 1)) u = nextafterf((float)(ci + 1), 0.0f);
+      ic[d] = ci;
+      a.d.u[d][p] = u;
+      a.d.v[d][p] = (float)v[d];
+    }
+    a.key[p] = blk * AMPS_CPB + ic[0] + AMPS_NC * (ic[1] + AMPS_NC * ic[2]);
+  }
+  if (my_sub) atomicAdd(a.nsub, my_sub);
+}
+
 int grid_for(long long n, int threads) {
   long long g = (n + threads - 1) / threads;
   if (g > 152LL * 64) g = 152LL * 64;
@@ -1628,6 +1773,38 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
     k_gather_valid<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
         c->ncor, c->d_base, c->d_cnt, pbuf(c, c->cur), pbuf(c, c->cur ^ 1), c->d_key,
         c->d_flags + 4);
+  }
+  if (c->amr) {
+    AmrRelBorisArgs a;
+    a.d = pbuf(c, c->cur ^ 1);
+    a.key = c->d_key;
+    a.n = c->np;
+    a.m = c->amrdev;
+    a.ctab = c->d_ctab;
+    a.hs = c->d_hs;
+    a.hp = c->d_hp;
+    a.hw = c->d_hw;
+    a.nvc = c->nvc;
+    a.E = E;
+    a.B = B;
+    for (int d = 0; d < 3; d++) a.x0[d] = c->cfg.x0[d];
+    a.dxf = c->dxf;
+    for (int sp = 0; sp < AMPS_GPU_MAX_SPECIES; sp++) {
+      a.qm[sp] = sp < c->cfg.nspec ? c->cfg.charge[sp] / c->cfg.mass[sp] : 0.0;
+      a.qabs_over_m[sp] = sp < c->cfg.nspec ? fabs(c->cfg.charge[sp]) / c->cfg.mass[sp] : 0.0;
+    }
+    a.dt_total = dt_total;
+    a.c_light = c_light;
+    a.max_sub = max_sub;
+    a.flags = c->d_flags;
+    a.nsub = c->d_flags + 5;
+    {
+      TimedLaunch t(c, "relboris");
+      k_amr_relboris<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return rebuild_from_list(c, c->np);
   }
   RelBorisArgs a;
   a.d = pbuf(c, c->cur ^ 1);

@@ -195,6 +195,85 @@ long orc_amr_push(const orc_amr* g, long n, double* x, double* v, const uint8_t*
   return 0;
 }
 
+/* Mover::Relativistic::Boris (src/pic/pic_mover_relativistic_boris.cpp:16-583,
+ * scalar path :119-175) on a periodic AMR mesh: the sub-step rule and the
+ * two-rotation update of the uniform-mesh restatement (orc_relboris); at the
+ * start of every sub-step the particle is re-located in the block tree
+ * (findTreeNode: periodic wrap and the finest-block map) and E, B are the
+ * trilinear interpolation from that leaf block's 8 cell corners, hanging
+ * corners through their constraint.  E = E^n, B = the corner B of the "cur"
+ * slot (interleaved x, y, z per corner).  Returns the number of sub-steps. */
+/* a sub-step can carry a fast particle more than one period: shift by whole
+ * periods first (the uniform mesh's block-periodic shift), then locate_one */
+static void wrap_far(const orc_amr* g, double x[3]) {
+  const double dxf = g->dx0 / (double)(1 << g->lmax);
+  for (int d = 0; d < 3; d++) {
+    const double L = g->nfine[d] * dxf;
+    const double k = floor((x[d] - g->x0[d]) / L);
+    if (k != 0.0) x[d] -= k * L;
+  }
+}
+
+long orc_amr_relboris(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
+                      int32_t* block, int32_t* cell, const double* E, const double* B,
+                      double dt_total, double c_light) {
+  const double cc2 = c_light * c_light;
+  long nsub = 0;
+  for (long p = 0; p < n; p++) {
+    double* xp = x + 3 * p;
+    double* vp = v + 3 * p;
+    const int sp = spec[p];
+    const double q = g->q[sp], m = g->m[sp];
+    double rem = dt_total;
+    while (rem > 0.0) {
+      double w[8], Ef[3] = {0, 0, 0}, Bf[3] = {0, 0, 0}, val[3];
+      int cid[8];
+      wrap_far(g, xp);
+      locate_one(g, xp, block + p, cell + p);
+      stencil(g, block[p], xp, w, cid);
+      for (int c = 0; c < 8; c++) {
+        corner_val(g, E, cid[c], val);
+        for (int d = 0; d < 3; d++) Ef[d] += w[c] * val[d];
+        corner_val(g, B, cid[c], val);
+        for (int d = 0; d < 3; d++) Bf[d] += w[c] * val[d];
+      }
+      double gam = 1.0 / sqrt(1.0 - (vp[0] * vp[0] + vp[1] * vp[1] + vp[2] * vp[2]) / cc2);
+      const double bmag = sqrt(Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
+      double dt = rem;
+      if (bmag > 1.0e-25) {
+        const double dtmax = 1.0 / (fabs(q) * bmag / (2.0 * PI_D * m * gam));
+        if (dtmax < rem) dt = dtmax;
+      }
+      rem -= dt;
+      const double h = q * dt / (2.0 * m);
+      double um[3], t[3], up[3], s[3], upl[3], uf[3], l = 0.0;
+      for (int d = 0; d < 3; d++) um[d] = gam * vp[d] + h * Ef[d];
+      gam = sqrt(1.0 + (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]) / cc2);
+      for (int d = 0; d < 3; d++) {
+        t[d] = h / gam * Bf[d];
+        l += t[d] * t[d];
+      }
+      up[0] = um[0] + (um[1] * t[2] - um[2] * t[1]);
+      up[1] = um[1] + (um[2] * t[0] - um[0] * t[2]);
+      up[2] = um[2] + (um[0] * t[1] - um[1] * t[0]);
+      for (int d = 0; d < 3; d++) s[d] = 2.0 * t[d] / (1.0 + l);
+      upl[0] = um[0] + (up[1] * s[2] - up[2] * s[1]);
+      upl[1] = um[1] + (up[2] * s[0] - up[0] * s[2]);
+      upl[2] = um[2] + (up[0] * s[1] - up[1] * s[0]);
+      for (int d = 0; d < 3; d++) uf[d] = upl[d] + h * Ef[d];
+      gam = sqrt(1.0 + (uf[0] * uf[0] + uf[1] * uf[1] + uf[2] * uf[2]) / cc2);
+      for (int d = 0; d < 3; d++) {
+        vp[d] = uf[d] / gam;
+        xp[d] += vp[d] * dt;
+      }
+      nsub++;
+    }
+    wrap_far(g, xp);
+    locate_one(g, xp, block + p, cell + p);
+  }
+  return nsub;
+}
+
 /* OpenFlow injection through face `face` of an open axis on the AMR mesh
  * (pic_bc.cpp:270-440 with CalculateInjectionRate_MaxwellianDistribution :215
  * and InjectMaxwellianDistribution, pic_vel_distribution.cpp:49): the face is

@@ -214,3 +214,24 @@ def test_oracle_open_boundary_rows_and_update_b():
         else:
             inward = np.flatnonzero(at0) + 8                   # j + 1, same block
             np.testing.assert_allclose(bnew[at0], bnew[inward], rtol=0, atol=0)
+
+
+def test_amr_relboris_equals_uniform_relboris():
+    """the AMR restatement of Mover::Relativistic::Boris on a single-level mesh
+    takes the uniform-mesh restatement's sub-steps, positions and velocities"""
+    wl, st, ao, gidx, rng = uniform_pair((2, 1, 1), ppc=2, seed=9)
+    st.E_n[:] = 2e-2 * rng.standard_normal(st.E_n.shape)
+    ao.E_n[:] = st.E_n[gidx]
+    v = st.v * 6.0
+    sp = np.linalg.norm(v, axis=1)
+    v = np.where(sp[:, None] >= 0.95, v * (0.95 / sp)[:, None], v)
+    st.v[:] = v
+    ao.v[:] = v
+    n_u = st.relboris(30.0, 1.0)
+    n_a = ao.relboris(30.0, 1.0)
+    assert n_a == n_u and n_a > len(v)
+    L = np.array(wl.mesh.shape, float) * wl.mesh.dx
+    d = ao.x - st.x
+    d -= L * np.rint(d / L)
+    assert np.abs(d).max() < 1e-9 * wl.mesh.dx
+    np.testing.assert_allclose(ao.v, st.v, rtol=0, atol=1e-10)
