@@ -907,8 +907,8 @@ amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* c, double dt_
                                                      double light_speed, long long* substeps) {
   if (!c || !(dt_total >= 0.0) || !(light_speed > 0.0))
     return set_err(c, AMPS_GPU_INVALID_ARG, "move_particles_relativistic: bad arguments");
-  if (c->amr && c->mesh_open)
-    return set_err(c, AMPS_GPU_INVALID_ARG, "move_particles_relativistic: periodic meshes only");
+  if (c->open_axes)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "move_particles_relativistic: periodic axes only");
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s;
   if ((s = reset_flags(c))) return s;

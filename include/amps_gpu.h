@@ -215,10 +215,11 @@ amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* ctx, long long* out_of_blo
  * at most one gyro period (1/f_g, f_g = |q||B|/(2 pi m gamma)), with E = the
  * corner E^n slot and B = the corner B "cur" slot interpolated at each
  * sub-step's start, then re-binned.  light_speed in the context's units.
- * Uniform meshes and periodic AMR meshes (on AMR meshes each sub-step
- * re-locates the particle in the block tree and interpolates from its leaf
- * block's corners, hanging corners through their constraint).  substeps
- * (optional) receives the total sub-steps. */
+ * Uniform and AMR meshes (on AMR meshes each sub-step re-locates the
+ * particle in the block tree and interpolates from its leaf block's corners,
+ * hanging corners through their constraint); every axis periodic
+ * (INVALID_ARG after amps_gpu_set_open_axes or on a mesh with open axes).
+ * substeps (optional) receives the total sub-steps. */
 amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* ctx, double dt_total,
                                                      double light_speed, long long* substeps);
 /* ECSIM::UpdateJMassMatrix (pic_field_solver_ecsim.cpp:3244): J and the

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import amps_gb300 as A
-from tests.gpu_cases import rel_err
+from tests.gpu_cases import make_case, rel_err
 from tests.test_gpu_amr import amr_case, by_id, face_dist, gpu_for, oracle_for
 from tests.test_gpu_open_fields import open_case
 
@@ -44,8 +44,16 @@ def test_amr_relboris_matches_oracle(dt_total, vscale):
     assert np.any(lv[e["block"]] != lv[e0["block"]])
 
 
-def test_amr_relboris_refuses_open_mesh():
+def test_relboris_refuses_open_axes():
     mesh, wl, ic, x, f = open_case((3, 2, 2), 0, (True, False, False), 0)
     with gpu_for(mesh, wl, ic, x, f) as ctx:
+        with pytest.raises(A.AmpsGpuError):
+            ctx.MoveParticlesRelativistic(1.0, 1.0)
+    # uniform mesh with particle open axes
+    wl, ic, x, f = make_case(nb=(2, 1, 1), ppc=2, seed=63)
+    with A.EcsimContext(wl, capacity=len(x) + 1024) as ctx:
+        ctx.import_particles(x, ic["v"].astype(np.float64), ic["spec"])
+        ctx.import_fields(**f)
+        ctx.set_open_axes(False, False, True)
         with pytest.raises(A.AmpsGpuError):
             ctx.MoveParticlesRelativistic(1.0, 1.0)
