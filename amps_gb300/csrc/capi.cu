@@ -907,19 +907,20 @@ amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* c, double dt_
                                                      double light_speed, long long* substeps) {
   if (!c || !(dt_total >= 0.0) || !(light_speed > 0.0))
     return set_err(c, AMPS_GPU_INVALID_ARG, "move_particles_relativistic: bad arguments");
-  if (c->open_axes)
-    return set_err(c, AMPS_GPU_INVALID_ARG, "move_particles_relativistic: periodic axes only");
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s;
   if ((s = reset_flags(c))) return s;
   if ((s = cuda_check(c, launch_relboris(c, c->d_En, c->d_Bcor_cur, dt_total, light_speed, 100000000LL),
                       "relativistic Boris")))
     return s;
-  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_flags, c->d_flags, 6 * sizeof(unsigned long long),
+  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_flags, c->d_flags, 7 * sizeof(unsigned long long),
                                          cudaMemcpyDeviceToHost, c->stream), "flags")))
     return s;
   if ((s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync"))) return s;
   if (substeps) *substeps = (long long)c->h_flags[5];
+  // particles that left through an open face were not placed
+  c->np -= (long long)c->h_flags[6];
+  c->deleted_total += (long long)c->h_flags[6];
   if (c->h_flags[2])
     return set_err(c, AMPS_GPU_DEVICE_TIMEOUT, "relativistic Boris: sub-step cap reached");
   c->have_moments = false;

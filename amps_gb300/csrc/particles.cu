@@ -903,8 +903,10 @@ __global__ void __launch_bounds__(256) k_rb_rank(long long n, const int* __restr
   for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
        base += (long long)gridDim.x * blockDim.x) {
     const long long p = base + threadIdx.x;
-    const bool act = p < n;
-    const int r = warp_reserve(act, act ? key[p] : 0, count);
+    // key < 0: deleted by the mover (open face), not placed
+    const int k = p < n ? key[p] : -1;
+    const bool act = k >= 0;
+    const int r = warp_reserve(act, act ? k : 0, count);
     if (act) rank[p] = r;
   }
 }
@@ -929,7 +931,9 @@ __global__ void __launch_bounds__(256) k_rb_scatter(long long n, const int* __re
                                                     const int* __restrict__ base, PBuf s, PBuf d) {
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
-    const long long q = (long long)base[key[p]] + rank[p];
+    const int k = key[p];
+    if (k < 0) continue;  // deleted by the mover
+    const long long q = (long long)base[k] + rank[p];
     copy_particle(s, p, d, q);
   }
 }
@@ -1168,8 +1172,9 @@ struct RelBorisArgs {
   double qabs_over_m[AMPS_GPU_MAX_SPECIES];
   double dt_total, c_light;
   long long max_sub;
-  unsigned long long* flags;   // [2] sub-step cap reached
+  unsigned long long* flags;   // [2] sub-step cap reached, [6] deleted at an open face
   unsigned long long* nsub;    // total sub-steps
+  int open;                    // bit d: axis d open (a particle past its faces is deleted)
 };
 
 // block and in-block coordinate of x (periodic; same rules as k_import)
@@ -1270,10 +1275,17 @@ __global__ void __launch_bounds__(256) k_relboris(RelBorisArgs a) {
       for (int d = 0; d < 3; d++) {
         v[d] = uf[d] / gam;
         x[d] += v[d] * dt;
+        if (((a.open >> d) & 1) && (x[d] < a.x0[d] || x[d] >= a.x0[d] + a.nbk[d] * AMPS_NC * a.dx[d]))
+          rem = -1.0;
       }
       ns++;
     }
     my_sub += (unsigned long long)ns;
+    if (rem < 0.0) {  // left the domain through an open face
+      a.key[p] = -1;
+      atomicAdd(a.flags + 6, 1ull);
+      continue;
+    }
     // final block, cell and FP32 offset
     rb_locate(a, x, bx, xmin);
     int ic[3];
@@ -1318,6 +1330,7 @@ struct AmrRelBorisArgs {
   long long max_sub;
   unsigned long long* flags;
   unsigned long long* nsub;
+  int open;
 };
 
 __device__ __forceinline__ int amr_rb_locate(const AmrRelBorisArgs& a, double x[3]) {
@@ -1415,10 +1428,17 @@ __global__ void __launch_bounds__(256) k_amr_relboris(AmrRelBorisArgs a) {
       for (int d = 0; d < 3; d++) {
         v[d] = uf[d] / gam;
         x[d] += v[d] * dt;
+        if (((a.open >> d) & 1) && (x[d] < a.x0[d] || x[d] >= a.x0[d] + a.m.nfine[d] * a.dxf))
+          rem = -1.0;
       }
       ns++;
     }
     my_sub += (unsigned long long)ns;
+    if (rem < 0.0) {  // left the domain through an open face
+      a.key[p] = -1;
+      atomicAdd(a.flags + 6, 1ull);
+      continue;
+    }
     // final leaf block, cell and FP32 offset (k_import_amr's rules)
     blk = amr_rb_locate(a, x);
     const double dx = a.m.bscale[blk] * a.dxf;
@@ -1798,6 +1818,7 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
     a.max_sub = max_sub;
     a.flags = c->d_flags;
     a.nsub = c->d_flags + 5;
+    a.open = c->open_axes;
     {
       TimedLaunch t(c, "relboris");
       k_amr_relboris<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
@@ -1825,6 +1846,7 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
   a.max_sub = max_sub;
   a.flags = c->d_flags;
   a.nsub = c->d_flags + 5;
+  a.open = c->open_axes;
   {
     TimedLaunch t(c, "relboris");
     k_relboris<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);

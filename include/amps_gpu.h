@@ -217,8 +217,8 @@ amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* ctx, long long* out_of_blo
  * sub-step's start, then re-binned.  light_speed in the context's units.
  * Uniform and AMR meshes (on AMR meshes each sub-step re-locates the
  * particle in the block tree and interpolates from its leaf block's corners,
- * hanging corners through their constraint); every axis periodic
- * (INVALID_ARG after amps_gpu_set_open_axes or on a mesh with open axes).
+ * hanging corners through their constraint).  A particle past a face of an
+ * open axis after a sub-step is deleted (findTreeNode finds no block there).
  * substeps (optional) receives the total sub-steps. */
 amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* ctx, double dt_total,
                                                      double light_speed, long long* substeps);

@@ -505,9 +505,20 @@ long orc_relboris(const orc_mesh* g, long n, double* x, double* v, const uint8_t
         xI[d] += vI[d] * dt;
       }
       nsub++;
+      /* findTreeNode finds no block past an open face: the particle is deleted */
+      const int nbd[3] = {g->nbx, g->nby, g->nbz};
+      for (int d = 0; d < 3; d++)
+        if (((orc_open_axes >> d) & 1) &&
+            (xI[d] < g->x0[d] || xI[d] >= g->x0[d] + nbd[d] * NC * g->dx[d]))
+          rem = -1.0;
+    }
+    for (int d = 0; d < 3; d++) { x[3 * p + d] = xI[d]; v[3 * p + d] = vI[d]; }
+    if (rem < 0.0) {
+      block[p] = cell[p] = -1;
+      continue;
     }
     locate_one(g, xI, block + p, cell + p);
-    for (int d = 0; d < 3; d++) { x[3 * p + d] = xI[d]; v[3 * p + d] = vI[d]; }
+    for (int d = 0; d < 3; d++) x[3 * p + d] = xI[d];
   }
   return nsub;
 }

@@ -267,6 +267,15 @@ long orc_amr_relboris(const orc_amr* g, long n, double* x, double* v, const uint
         xp[d] += vp[d] * dt;
       }
       nsub++;
+      /* findTreeNode finds no block past an open face: the particle is deleted */
+      for (int d = 0; d < 3; d++)
+        if (((orc_open_axes >> d) & 1) &&
+            (xp[d] < g->x0[d] || xp[d] >= g->x0[d] + g->nfine[d] * (g->dx0 / (double)(1 << g->lmax))))
+          rem = -1.0;
+    }
+    if (rem < 0.0) {
+      block[p] = cell[p] = -1;
+      continue;
     }
     wrap_far(g, xp);
     locate_one(g, xp, block + p, cell + p);

@@ -44,16 +44,37 @@ def test_amr_relboris_matches_oracle(dt_total, vscale):
     assert np.any(lv[e["block"]] != lv[e0["block"]])
 
 
-def test_relboris_refuses_open_axes():
-    mesh, wl, ic, x, f = open_case((3, 2, 2), 0, (True, False, False), 0)
+@pytest.fixture
+def open_oracle():
+    from tests import oracle_lib as O
+    lib = O.load()
+    yield lib
+    lib.orc_set_open_axes(0)
+
+
+@pytest.mark.parametrize("nb0,lmax,open_axes", [((3, 2, 2), 0, (True, False, True)),
+                                                 ((4, 4, 4), 1, (True, True, False))])
+def test_relboris_open_faces_delete_like_oracle(open_oracle, nb0, lmax, open_axes):
+    """fast particles on a mesh with open axes: the set deleted at the open
+    faces is the oracle's, the survivors follow it"""
+    mesh, wl, ic, x, f = open_case(nb0, lmax, open_axes, 1, seed=87, vscale=6.0)
+    v = ic["v"].astype(np.float64)
+    sp = np.linalg.norm(v, axis=1)
+    ic["v"] = np.where(sp[:, None] >= 0.95, v * (0.95 / sp)[:, None], v)
+    open_oracle.orc_set_open_axes(sum(1 << d for d in range(3) if open_axes[d]))
     with gpu_for(mesh, wl, ic, x, f) as ctx:
-        with pytest.raises(A.AmpsGpuError):
-            ctx.MoveParticlesRelativistic(1.0, 1.0)
-    # uniform mesh with particle open axes
-    wl, ic, x, f = make_case(nb=(2, 1, 1), ppc=2, seed=63)
-    with A.EcsimContext(wl, capacity=len(x) + 1024) as ctx:
-        ctx.import_particles(x, ic["v"].astype(np.float64), ic["spec"])
-        ctx.import_fields(**f)
-        ctx.set_open_axes(False, False, True)
-        with pytest.raises(A.AmpsGpuError):
-            ctx.MoveParticlesRelativistic(1.0, 1.0)
+        e0 = by_id(ctx.export_particles())
+        ctx.MoveParticlesRelativistic(8.0, 1.0)
+        e = by_id(ctx.export_particles())
+        n_left = ctx.num_particles()
+    ao = oracle_for(mesh, wl, {"v": e0["v"], "spec": e0["spec"]}, e0["x"], f)
+    ao.relboris(8.0, 1.0)
+    alive = ao.block >= 0
+    assert (~alive).sum() > 50 and alive.sum() > 50
+    assert n_left == alive.sum()
+    np.testing.assert_array_equal(e["id"], e0["id"][alive])
+    assert rel_err(e["v"], ao.v[alive]) < 2e-6
+    L = np.array(mesh.nfine, float) * mesh.dx0 / (1 << mesh.lmax)
+    d = e["x"] - ao.x[alive]
+    d -= L * np.rint(d / L)
+    assert np.max(np.abs(d)) < 2e-6 * mesh.dx0
