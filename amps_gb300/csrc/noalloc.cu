@@ -1,12 +1,12 @@
 // ECSIM current / mass-matrix deposition that allocates no device memory.
 //
-// Who needs it: callers that own every device allocation themselves and may
-// not let a library call cudaMalloc/cudaFree -- a host code that runs inside
-// a memory-pool-managed framework, or one that records its step into a CUDA
-// graph and cannot have allocations happen inside the recorded region.  They
-// pass their own device buffers for the inputs and outputs; the per-block
-// field stencils and per-cell partial sums that the deposition needs in
-// between live in one file-scope __device__ array instead.
+// Who needs it: host codes that may not call cudaMalloc or cudaFree through a
+// library -- one whose device memory is owned by its framework's pool
+// allocator, or one that must not stall its other streams in the middle of a
+// step (cudaFree synchronises the whole device).  They pass their own device
+// buffers for the inputs and outputs; the per-block field stencils and
+// per-cell partial sums that the deposition needs in between live in one
+// file-scope __device__ array instead.
 //
 // Limits and sharing:
 //   * the scratch array holds a mesh of at most kMaxBlocks = 16 blocks of 8^3
@@ -15,10 +15,12 @@
 //     until the process exits;
 //   * every call uses the same array: two calls that overlap on the GPU (on
 //     different streams, or from different host threads without ordering)
-//     race on it.  Each call overwrites all scratch it reads, so no state
-//     leaks from one call into the next;
+//     race on it.  Each call writes all scratch it reads before reading it
+//     (a block whose stencil copy timed out fills its cells' partials with
+//     NaN), so no state leaks from one call into the next;
 //   * the first call on a device resolves the array's device address with
 //     cudaGetSymbolAddress; make that first call before any stream capture.
+//   * the caller's current device is restored before the call returns.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -125,7 +127,14 @@ __global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
   if (!stage_stencils(&bar, s_dep, a.stencil + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE,
                       AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0,
                       g_na_flags)) {
-    // the staging copy never completed: mark the energy output NaN
+    // the staging copy never completed: this CTA's cells get NaN partials
+    // (so J and M are NaN where they contribute, never a previous call's
+    // values) and the energy output is NaN
+    const float qnan = __int_as_float(0x7fc00000);
+    const long long c0 = (long long)b * AMPS_CPB + (long long)AMPS_NC * AMPS_NC * k;
+    for (int t = threadIdx.x; t < AMPS_NC * AMPS_NC * AMPS_CELLM; t += blockDim.x)
+      a.cellM[c0 * AMPS_CELLM + t] = qnan;
+    for (int t = threadIdx.x; t < AMPS_NC * AMPS_NC * 24; t += blockDim.x) a.cellJ[c0 * 24 + t] = qnan;
     if (threadIdx.x == 0) *a.energy = __longlong_as_double(0x7ff8000000000000LL);
     return;
   }
@@ -220,10 +229,12 @@ cudaError_t setup_device(int dev, unsigned char** out) {
 
 }  // namespace
 
-extern "C" amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(
-    const amps_gpu_config* cfg, long long n, const int32_t* d_cell_start, const float* d_u,
-    const float* d_v, const uint8_t* d_spec, const double* d_B_corner, double* d_J, double* d_M,
-    double* d_energy, void* stream) {
+namespace {
+
+amps_gpu_status deposit_noalloc(const amps_gpu_config* cfg, long long n, const int32_t* d_cell_start,
+                                const float* d_u, const float* d_v, const uint8_t* d_spec,
+                                const double* d_B_corner, double* d_J, double* d_M,
+                                double* d_energy, void* stream) {
   if (!cfg || n < 0 || !d_cell_start || !d_B_corner || !d_J || !d_M || !d_energy ||
       (n > 0 && (!d_u || !d_v || !d_spec)))
     return AMPS_GPU_INVALID_ARG;
@@ -273,4 +284,23 @@ extern "C" amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(
   k_na_assemble<<<(unsigned)((ncor + 255) / 256), 256, 0, s>>>(m, ncor, cellM, cellJ, inv_vol,
                                                                d_M, d_J);
   return cudaGetLastError() == cudaSuccess ? AMPS_GPU_OK : AMPS_GPU_CUDA_ERROR;
+}
+
+}  // namespace
+
+extern "C" amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(
+    const amps_gpu_config* cfg, long long n, const int32_t* d_cell_start, const float* d_u,
+    const float* d_v, const uint8_t* d_spec, const double* d_B_corner, double* d_J, double* d_M,
+    double* d_energy, void* stream) {
+  // the call selects cfg->device; the host thread's current device is the
+  // caller's, so it is put back on every return path
+  int prev = -1;
+  const bool had = cudaGetDevice(&prev) == cudaSuccess;
+  const amps_gpu_status st = deposit_noalloc(cfg, n, d_cell_start, d_u, d_v, d_spec, d_B_corner,
+                                             d_J, d_M, d_energy, stream);
+  if (had) {
+    int now = -1;
+    if (cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+  }
+  return st;
 }

@@ -25,11 +25,12 @@
 //   rebuild              counting sort of an unsorted list into the slotted
 //                        layout: import, and recovery when slack overflows
 //
-// Deposition arithmetic: per particle the 36 corner-pair weight products,
-// k*alpha (9), the 8 weights and q*alpha*v are staged in shared memory; each
-// lane then owns a 4 x 3 tile of the 36x9 mass-matrix block (27 lanes) or of
-// the 8x3 current block (2 lanes) and accumulates it in registers over chunks
-// of 32 particles, adding chunk sums with Kahan compensation.
+// Deposition arithmetic: per particle the 27 distinct trilinear weight
+// monomials, k*alpha (9), the 8 corner weights and q*alpha*v are staged in
+// shared memory; 27 lanes each own a 3 x 3 tile of the 27x9 monomial block of
+// the mass matrix and 3 lanes a 3 x 3 tile of the 8x3 current block, and
+// accumulate it in registers over chunks of 32 particles, adding chunk sums
+// with Kahan compensation (deposit_core.cuh).
 #include <cuda_runtime.h>
 
 #include <algorithm>

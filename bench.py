@@ -38,9 +38,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s (push+deposit)"
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the
-# one-pass ncu capture summarised in profiles/dram_traffic_amr_64c_128ppc.md
-MEASURED_TRAFFIC = {"amr_64c_128ppc": {"push_deposit": 4.66e9, "arrivals": 1.09e9}}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# particle-step kernels on the default workload, from a one-pass ncu capture
+# of this bench command; "version" names the kernel revision it was taken on
+MEASURED_TRAFFIC = {"amr_64c_128ppc": {"version": "push_deposit 27-monomial 3x3 tiles",
+                                       "push_deposit": 4.66e9, "arrivals": 1.09e9}}
 UNIT = "particle-steps/s"
 
 
@@ -879,7 +881,7 @@ def main():
                     help="time only the tensor-core inference kernel on this many blocks")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the top kernel from an ncu capture "
-                         "(default: the capture in profiles/ for the default workload)")
+                         "(default: the committed capture of the default workload)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

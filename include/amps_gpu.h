@@ -392,24 +392,28 @@ amps_gpu_status amps_gpu_precond_forward(amps_gpu_ctx* ctx, long long count, con
 
 /* ---- deposition for callers that may not allocate device memory ----
  * No counterpart in the reference: a variant of UpdateJMassMatrix for a host
- * code that owns all device memory itself (a pool-managed framework, or a step
- * recorded into a CUDA graph) and so cannot let a library call cudaMalloc or
- * cudaFree.  It allocates nothing: the caller passes device buffers for every
- * input and output, and the block stencils and per-cell partial sums in between
- * live in one static device array of 11.1 MiB that every GPU loading the
- * library keeps until exit.  That array limits the mesh to 16 blocks (8192
- * cells); larger meshes return AMPS_GPU_INVALID_ARG.  All calls share it, so
- * calls that overlap on the GPU race; each call rewrites the scratch it reads,
- * so nothing carries over between calls.  The first call on a device looks up
- * the array's address (cudaGetSymbolAddress); make it before any stream capture.
+ * code that may not call cudaMalloc or cudaFree through a library -- its
+ * device memory belongs to its framework's pool allocator, or it must not
+ * stall its other streams in mid-step (cudaFree synchronises the device).  It
+ * allocates nothing: the caller passes device buffers for every input and
+ * output, and the block stencils and per-cell partial sums in between live in
+ * one static device array of 11.1 MiB that every GPU loading the library keeps
+ * until exit.  That array limits the mesh to 16 blocks (8192 cells); larger
+ * meshes return AMPS_GPU_INVALID_ARG.  All calls share it, so calls that
+ * overlap on the GPU race; each call writes the scratch it reads before
+ * reading it, so nothing carries over between calls.  The first call on a
+ * device looks up the array's address (cudaGetSymbolAddress); make it before
+ * any stream capture.  The caller's current device is restored on return.
  * Inputs (device pointers, asynchronous on `stream`): particles sorted by cell
  * key block*512 + (i + 8*(j + 8*k)), d_cell_start[ncell+1] their offsets; d_u,
  * d_v structure-of-arrays of length 3n (x[n], y[n], z[n]) with u the FP32
  * block-local offset in cell units; d_spec species bytes; d_B_corner the corner
  * B "cur" slot, 3 per corner in the global layout.  Outputs: d_J (3 per corner),
- * d_M (243 per corner) in the global layout, d_energy[1] the kinetic energy
- * (NaN if the device reported a bounded-wait timeout).  cfg->device selects the
- * GPU; particle_capacity and track_ids are ignored. */
+ * d_M (243 per corner) in the global layout, d_energy[1] the kinetic energy.
+ * If the device hit a bounded-wait timeout, *d_energy is NaN and the J and M
+ * entries the affected blocks contribute to are NaN: treat J and M as invalid
+ * whenever *d_energy is NaN.  cfg->device selects the GPU; particle_capacity
+ * and track_ids are ignored. */
 amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(const amps_gpu_config* cfg, long long n,
                                                       const int32_t* d_cell_start,
                                                       const float* d_u, const float* d_v,

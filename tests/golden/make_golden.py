@@ -26,7 +26,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("AMPS_REFERENCE", "/root/reference")
 REFBIN = os.path.join(ROOT, "oracle", "_ref")
 
 

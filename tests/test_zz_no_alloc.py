@@ -1,9 +1,9 @@
 """The no-allocation deposition entry point against the context path.
 
 amps_gpu_update_j_mass_matrix_noalloc serves callers that cannot let a library
-allocate device memory (they own every device buffer, for example inside a
-pool-managed framework or a step recorded into a CUDA graph).  This test plays
-such a caller: it allocates the input and output buffers itself, calls the
+call cudaMalloc or cudaFree (their device memory belongs to their framework's
+pool allocator, or they must not stall other streams in mid-step, which
+cudaFree does).  This test plays such a caller: it allocates the input and output buffers itself, calls the
 entry point twice in a row through the C ABI and checks both results against
 amps_gpu_update_j_mass_matrix on the same particles and fields, within the
 deposit tolerance used elsewhere (relative 1e-5 for J and M, 1e-6 for the
