@@ -620,6 +620,38 @@ double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
   return energy;
 }
 
+/* Per-species maximum over cells of ProcessCell's cflCell
+ * (pic_field_solver_ecsim.cpp:2236 sums |v| dt per species, :2356-2359 divides
+ * by the count times the cell diagonal; UpdateJMassMatrix keeps the maximum,
+ * :3352 and :3972-3977).  A cell without particles of a species gives 0/0 in
+ * the reference, which its > test never keeps, so such cells do not count.
+ * cfl_max[g->nspec]. */
+void orc_cfl(const orc_mesh* g, long n, const double* v, const uint8_t* spec,
+             const int32_t* block, const int32_t* cell, double* cfl_max) {
+  const long ncell = (long)NC * NC * NC * g->nbx * g->nby * g->nbz;
+  const int ns = g->nspec;
+  double* sum = (double*)calloc((size_t)ncell * ns, sizeof(double));
+  long* cnt = (long*)calloc((size_t)ncell * ns, sizeof(long));
+  for (long p = 0; p < n; p++) {
+    if (block[p] < 0) continue;
+    const long cl = (long)block[p] * 512 + cell[p];
+    const double* vp = v + 3 * p;
+    const double vsqr = vp[0] * vp[0] + vp[1] * vp[1] + vp[2] * vp[2];
+    sum[cl * ns + spec[p]] += sqrt(vsqr) * g->dt;
+    cnt[cl * ns + spec[p]] += 1;
+  }
+  const double diag = sqrt(g->dx[0] * g->dx[0] + g->dx[1] * g->dx[1] + g->dx[2] * g->dx[2]);
+  for (int s2 = 0; s2 < ns; s2++) cfl_max[s2] = 0.0;
+  for (long c = 0; c < ncell; c++)
+    for (int s2 = 0; s2 < ns; s2++)
+      if (cnt[c * ns + s2] > 0) {
+        const double cf = sum[c * ns + s2] / ((double)cnt[c * ns + s2] * diag);
+        if (cf > cfl_max[s2]) cfl_max[s2] = cf;
+      }
+  free(sum);
+  free(cnt);
+}
+
 /* Species moments on corners (_PIC_FIELD_SOLVER_SAMPLE_SPECIES_ON_CORNER_,
  * ProcessCell pic_field_solver_ecsim.cpp:2270-2303 and the flush :2384-2394):
  * per particle and corner t = m W w_c, the ten sums rho, rho u (3),

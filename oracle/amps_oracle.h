@@ -61,6 +61,8 @@ double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
                    const uint8_t* spec, const double* wcorr, const int32_t* block,
                    const int32_t* cell, const double* Bc_cur, double* J, double* M);
 void orc_locate(const orc_mesh* g, long n, const double* x, int32_t* block, int32_t* cell);
+void orc_cfl(const orc_mesh* g, long n, const double* v, const uint8_t* spec,
+             const int32_t* block, const int32_t* cell, double* cfl_max);
 
 /* ---- field solve ---- */
 void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor);

@@ -1,0 +1,22 @@
+// Hand-written build configuration of the reference sources compiled by
+// oracle/pins/ecsim_pin.cpp, in place of what the reference's configuration
+// script would generate for its fast-wave test input
+// (input/test/fast-wave.input): electromagnetic ECSIM field solver with the
+// corner-based magnetic field, normalised units, one global time step,
+// species-dependent global particle weights with individual weight
+// corrections.  pic.h fixes PIC::nTotalSpecies at 1 (the configuration script
+// rewrites that line), so the harness runs one species at a time.
+//
+// src/pic/pic.h includes src/pic/picGlobal.dfn (the defaults) and then the
+// coupler header FluidPicInterface.h, whose stand-in includes this file, so
+// these definitions replace the defaults.
+#pragma once
+#undef _PIC_FIELD_SOLVER_MODE_
+#define _PIC_FIELD_SOLVER_MODE_ _PIC_FIELD_SOLVER_MODE__ELECTROMAGNETIC__ECSIM_
+#undef _PIC_FIELD_SOLVER_B_MODE_
+#define _PIC_FIELD_SOLVER_B_MODE_ _PIC_FIELD_SOLVER_B_CORNER_BASED_
+#undef _PIC_FIELD_SOLVER_INPUT_UNIT_
+#define _PIC_FIELD_SOLVER_INPUT_UNIT_ _PIC_FIELD_SOLVER_INPUT_UNIT_NORM_
+#undef _SIMULATION_TIME_STEP_MODE_
+#define _SIMULATION_TIME_STEP_MODE_ _SINGLE_GLOBAL_TIME_STEP_
+#define _TOTAL_SPECIES_NUMBER_ 1

@@ -13,6 +13,11 @@ Run here (the reference sources are only present in the build container):
 * index_matrix.json      ProcessCell's IndexMatrix table
                          (src/pic/pic_field_solver_ecsim.cpp:1889-1891), read from
                          the reference source as text
+* ecsim_ref.json         ProcessCell (per-cell J, M, energy, cflCell) and Lapenta2017
+                         (x', v', cell) of the reference, compiled from
+                         src/pic/pic_field_solver_ecsim.cpp, pic_mover_boris.cpp and
+                         pic_interpolation_routines.cpp with the hand-written
+                         configuration of oracle/pins/refcfg/ (oracle/_ref/ecsim_pin)
 * stormer_c1.csv         copied from srcEarth/test/C1/reference_C1_stormer.csv
 """
 import ctypes as C
@@ -93,6 +98,19 @@ def gridless():
         json.dump(data, f)
 
 
+def ecsim_ref():
+    """ProcessCell and Lapenta2017 of the reference, compiled from its sources
+    by oracle/Makefile (target ref) and run by oracle/pins/ecsim_pin.cpp"""
+    out = subprocess.run([os.path.join(REFBIN, "ecsim_pin")], capture_output=True, text=True,
+                         check=True).stdout
+    data = json.loads(out)
+    data["source"] = ("src/pic/pic_field_solver_ecsim.cpp:1882-2438 ProcessCell, "
+                      "src/pic/pic_mover_boris.cpp:876-1380 Lapenta2017, "
+                      "src/pic/pic_interpolation_routines.cpp:1074-1194 CornerBased::InitStencil")
+    with open(os.path.join(HERE, "ecsim_ref.json"), "w") as f:
+        json.dump(data, f)
+
+
 def stormer():
     shutil.copy(os.path.join(REF, "srcEarth/test/C1/reference_C1_stormer.csv"),
                 os.path.join(HERE, "stormer_c1.csv"))
@@ -102,5 +120,6 @@ if __name__ == "__main__":
     stencil()
     index_matrix()
     gridless()
+    ecsim_ref()
     stormer()
     print("golden fixtures written to", HERE)

@@ -50,6 +50,7 @@ def load():
                                     C.c_double, C.c_double]),
         "orc_deposit": (C.c_double, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D]),
         "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
+        "orc_cfl": (None, [C.POINTER(Mesh), C.c_long, D, U8, I32, I32, D]),
         "orc_species_moments": (None, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D]),
         "orc_set_open_axes": (None, [C.c_int]),
         "orc_inject": (C.c_long, [C.POINTER(Mesh), C.c_int, C.c_int, C.c_double, D, C.c_double,
@@ -153,6 +154,13 @@ class OracleState:
                                     p(self.spec, C.c_uint8), p(self.wcorr),
                                     p(self.block, C.c_int32), p(self.cell, C.c_int32),
                                     p(self.Bcur), p(self.J), p(self.M))
+
+    def cfl(self):
+        """per-species maximum over cells of ProcessCell's cflCell"""
+        out = np.zeros(self.m.nspec)
+        self.lib.orc_cfl(C.byref(self.m), len(self.spec), p(self.v), p(self.spec, C.c_uint8),
+                         p(self.block, C.c_int32), p(self.cell, C.c_int32), p(out))
+        return out
 
     def step(self, tol=1e-8, maxit=200, precond=0):
         diag = np.zeros(3)

@@ -158,3 +158,102 @@ def test_gmres_meets_stop_rule():
         assert it > 0
         r = b - st.matvec(xs.reshape(-1, 3)).ravel()
         assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(b)
+
+
+# ---- ProcessCell and Lapenta2017 of the reference, compiled from its sources
+# (golden ecsim_ref.json, oracle/pins/ecsim_pin.cpp): the oracle on the same
+# particles, fields and plasma in a periodic 8^3-cell block (the reference runs
+# in its default 5^3-cell block; the golden particles and their corners lie in
+# cells 0..4, where the two blocks coincide).
+CORNER_OFF = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+
+
+def ref_golden():
+    return json.load(open(os.path.join(GOLD, "ecsim_ref.json")))
+
+
+def ref_mesh(g, species):
+    m = O.Mesh()
+    m.nbx = m.nby = m.nbz = 1
+    for d in range(3):
+        m.x0[d] = 0.0
+        m.dx[d] = g["dx"]
+    m.nspec = 1
+    m.q[0], m.m[0], m.w[0] = g["charge"][species], g["mass"][species], g["weight"]
+    m.dt, m.theta = g["dt"], 0.5
+    return m
+
+
+def ref_fields(g):
+    """E^{n+theta} and B on the 8^3 block's corners from the golden corner values"""
+    n1 = g["block_cells"] + 1
+    E, B = np.zeros((512, 3)), np.zeros((512, 3))
+    cf = np.array(g["corner_fields"])
+    for t in range(len(cf)):
+        i, j, k = t % n1, (t // n1) % n1, t // (n1 * n1)
+        E[i + 8 * (j + 8 * k)] = cf[t, :3]
+        B[i + 8 * (j + 8 * k)] = cf[t, 3:]
+    return E, B
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(b)))
+
+
+def test_process_cell_matches_reference_build():
+    g = ref_golden()
+    lib = O.load()
+    _, Bc = ref_fields(g)
+    for rec in g["process_cell"]:
+        m = ref_mesh(g, rec["species"])
+        ps = rec["particles"]
+        n = len(ps)
+        x = np.ascontiguousarray([p["x"] for p in ps], np.float64)
+        v = np.ascontiguousarray([p["v"] for p in ps], np.float64)
+        wc = np.ascontiguousarray([p["wcorr"] for p in ps], np.float64)
+        sp = np.zeros(n, np.uint8)
+        blk, cel = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        lib.orc_locate(O.C.byref(m), n, O.p(x), O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32))
+        ci, cj, ck = rec["cell"]
+        assert np.all(cel == ci + 8 * (cj + 8 * ck))
+        J, M = np.zeros((512, 3)), np.zeros((512, 243))
+        e = lib.orc_deposit(O.C.byref(m), n, O.p(x), O.p(v), O.p(sp, O.C.c_uint8), O.p(wc),
+                            O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32), O.p(Bc), O.p(J), O.p(M))
+        cor = [(ci + o[0]) + 8 * ((cj + o[1]) + 8 * (ck + o[2])) for o in CORNER_OFF]
+        gJ = np.array(rec["J"]).reshape(8, 3)
+        gM = np.array(rec["M"]).reshape(8, 243)
+        assert rel(J[cor], gJ) < 1e-13, rel(J[cor], gJ)
+        assert rel(M[cor], gM) < 1e-13, rel(M[cor], gM)
+        # nothing else was deposited
+        others = np.setdiff1d(np.arange(512), cor)
+        assert not J[others].any() and not M[others].any()
+        assert e == pytest.approx(rec["energy"], rel=1e-13)
+        cfl = np.zeros(1)
+        lib.orc_cfl(O.C.byref(m), n, O.p(v), O.p(sp, O.C.c_uint8), O.p(blk, O.C.c_int32),
+                    O.p(cel, O.C.c_int32), O.p(cfl))
+        assert cfl[0] == pytest.approx(rec["cfl"], rel=1e-13)
+
+
+def test_lapenta2017_matches_reference_build():
+    g = ref_golden()
+    lib = O.load()
+    E, B = ref_fields(g)
+    for species in (0, 1):
+        recs = [r for r in g["lapenta"] if r["species"] == species]
+        m = ref_mesh(g, species)
+        n = len(recs)
+        x = np.ascontiguousarray([r["in"]["x"] for r in recs], np.float64)
+        v = np.ascontiguousarray([r["in"]["v"] for r in recs], np.float64)
+        sp = np.zeros(n, np.uint8)
+        blk, cel = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        lib.orc_locate(O.C.byref(m), n, O.p(x), O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32))
+        out = lib.orc_push(O.C.byref(m), n, O.p(x), O.p(v), O.p(sp, O.C.c_uint8),
+                           O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32), O.p(E), O.p(B))
+        assert out == 0
+        gx = np.array([r["x"] for r in recs])
+        gv = np.array([r["v"] for r in recs])
+        assert np.max(np.abs(x - gx)) < 1e-13 * g["dx"], np.max(np.abs(x - gx))
+        assert rel(v, gv) < 1e-13, rel(v, gv)
+        assert all(r["code"] == 3 for r in recs)   # _PARTICLE_MOTION_FINISHED_
+        gc = np.array([r["cell"][0] + 8 * (r["cell"][1] + 8 * r["cell"][2]) for r in recs])
+        np.testing.assert_array_equal(cel, gc)
