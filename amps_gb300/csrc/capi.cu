@@ -927,6 +927,26 @@ amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* c, double dt_
   return AMPS_GPU_OK;
 }
 
+amps_gpu_status amps_gpu_move_particles_boris(amps_gpu_ctx* c, double dt_total) {
+  if (!c || !(dt_total >= 0.0))
+    return set_err(c, AMPS_GPU_INVALID_ARG, "move_particles_boris: bad arguments");
+  cudaSetDevice(c->cfg.device);
+  amps_gpu_status s;
+  if ((s = reset_flags(c))) return s;
+  if ((s = cuda_check(c, launch_relboris(c, c->d_En, c->d_Bcor_cur, dt_total, 1.0, 1, false),
+                      "Boris")))
+    return s;
+  if ((s = cuda_check(c, cudaMemcpyAsync(c->h_flags, c->d_flags, 7 * sizeof(unsigned long long),
+                                         cudaMemcpyDeviceToHost, c->stream), "flags")))
+    return s;
+  if ((s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync"))) return s;
+  // particles that left through an open face were not placed
+  c->np -= (long long)c->h_flags[6];
+  c->deleted_total += (long long)c->h_flags[6];
+  c->have_moments = false;
+  return AMPS_GPU_OK;
+}
+
 amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* c, double* particle_energy) {
   if (!c) return AMPS_GPU_INVALID_ARG;
   cudaSetDevice(c->cfg.device);

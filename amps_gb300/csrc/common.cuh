@@ -248,7 +248,7 @@ amps_gpu_status layout_download(amps_gpu_ctx* c, const void* dev, double* host, 
                                 int ncomp, bool dev_f32);
 amps_gpu_status layout_cell_moments(amps_gpu_ctx* c, double* hJ, double* hM);
 cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
-                            double c_light, long long max_sub);
+                            double c_light, long long max_sub, bool rel = true);
 cudaError_t launch_deposit(amps_gpu_ctx* c);
 void set_next_id(amps_gpu_ctx* c, long long n);
 // counting sort of the list buffer into the slotted layout (keys in d_key)

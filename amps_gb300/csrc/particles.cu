@@ -1201,6 +1201,32 @@ __device__ __forceinline__ void rb_locate(const RelBorisArgs& a, double x[3], in
   }
 }
 
+// Mover::Boris (src/pic/pic_mover_boris.cpp:126-553, scalar path :264-290)
+// with BorisSplitAcceleration_default's Lorentz force (:104-112): one step of
+// dt_total, u = v + dt/2 (q/m) E, h = dt/2 (q/m) B, U = ((1-h^2) u + 2 (u x h
+// + (u.h) h)) / (1+h^2), v' = U + dt/2 (q/m) E, x' = x + dt v'.
+__device__ __forceinline__ void boris_plain(double qm, double dt, const double Ef[3],
+                                            const double Bf[3], double v[3]) {
+  const double dt2 = dt / 2.0;
+  double accl[3], u[3], h[3];
+  for (int d = 0; d < 3; d++) {
+    accl[d] = qm * Ef[d];
+    u[d] = v[d] + dt2 * accl[d];
+    h[d] = -dt2 * (-(qm * Bf[d]));
+  }
+  const double h2 = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
+  const double uh = u[0] * h[0] + u[1] * h[1] + u[2] * h[2];
+  const double U0 = ((1 - h2) * u[0] + 2 * (u[1] * h[2] - h[1] * u[2] + uh * h[0])) / (1 + h2);
+  const double U1 = ((1 - h2) * u[1] + 2 * (u[2] * h[0] - h[2] * u[0] + uh * h[1])) / (1 + h2);
+  const double U2 = ((1 - h2) * u[2] + 2 * (u[0] * h[1] - h[0] * u[1] + uh * h[2])) / (1 + h2);
+  v[0] = U0 + dt2 * accl[0];
+  v[1] = U1 + dt2 * accl[1];
+  v[2] = U2 + dt2 * accl[2];
+}
+
+// REL: Mover::Relativistic::Boris with gyro-period sub-steps; !REL: one plain
+// Boris step of dt_total (fields and re-location as above).
+template <bool REL>
 __global__ void __launch_bounds__(256) k_relboris(RelBorisArgs a) {
   unsigned long long my_sub = 0;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
@@ -1248,6 +1274,18 @@ __global__ void __launch_bounds__(256) k_relboris(RelBorisArgs a) {
           Ef[d] += wq * a.E[d * a.ncor + id];
           Bf[d] += wq * a.B[d * a.ncor + id];
         }
+      }
+      if (!REL) {
+        const double dt = rem;
+        rem = 0.0;
+        boris_plain(a.qm[sp], dt, Ef, Bf, v);
+        for (int d = 0; d < 3; d++) {
+          x[d] += dt * v[d];
+          if (((a.open >> d) & 1) && (x[d] < a.x0[d] || x[d] >= a.x0[d] + a.nbk[d] * AMPS_NC * a.dx[d]))
+            rem = -1.0;
+        }
+        ns++;
+        continue;
       }
       const double cc2 = a.c_light * a.c_light;
       double gam = 1.0 / sqrt(1.0 - (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / cc2);
@@ -1351,6 +1389,7 @@ __device__ __forceinline__ int amr_rb_locate(const AmrRelBorisArgs& a, double x[
   return a.m.fine_map[(F[0] >> 3) + nb0 * ((F[1] >> 3) + nb1 * (F[2] >> 3))];
 }
 
+template <bool REL>
 __global__ void __launch_bounds__(256) k_amr_relboris(AmrRelBorisArgs a) {
   unsigned long long my_sub = 0;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < a.n;
@@ -1403,6 +1442,18 @@ __global__ void __launch_bounds__(256) k_amr_relboris(AmrRelBorisArgs a) {
           Ef[d] += w * e;
           Bf[d] += w * b;
         }
+      }
+      if (!REL) {
+        const double dt = rem;
+        rem = 0.0;
+        boris_plain(a.qm[sp], dt, Ef, Bf, v);
+        for (int d = 0; d < 3; d++) {
+          x[d] += dt * v[d];
+          if (((a.open >> d) & 1) && (x[d] < a.x0[d] || x[d] >= a.x0[d] + a.m.nfine[d] * a.dxf))
+            rem = -1.0;
+        }
+        ns++;
+        continue;
       }
       double gam = 1.0 / sqrt(1.0 - (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]) / cc2);
       const double bmag = sqrt(Bf[0] * Bf[0] + Bf[1] * Bf[1] + Bf[2] * Bf[2]);
@@ -1785,7 +1836,7 @@ cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow) {
 // sub-stepped move with new keys, counting-sort rebuild.  Sub-step total in
 // flags[4] (read back by the caller).
 cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
-                            double c_light, long long max_sub) {
+                            double c_light, long long max_sub, bool rel) {
   cudaError_t e = cudaMemsetAsync(c->d_flags + 4, 0, 2 * sizeof(unsigned long long), c->stream);
   if (e != cudaSuccess) return e;
   {
@@ -1821,8 +1872,11 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
     a.nsub = c->d_flags + 5;
     a.open = c->open_axes;
     {
-      TimedLaunch t(c, "relboris");
-      k_amr_relboris<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
+      TimedLaunch t(c, rel ? "relboris" : "boris");
+      if (rel)
+        k_amr_relboris<true><<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
+      else
+        k_amr_relboris<false><<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -1849,8 +1903,11 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
   a.nsub = c->d_flags + 5;
   a.open = c->open_axes;
   {
-    TimedLaunch t(c, "relboris");
-    k_relboris<<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
+    TimedLaunch t(c, rel ? "relboris" : "boris");
+    if (rel)
+      k_relboris<true><<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
+    else
+      k_relboris<false><<<grid_for(c->np, 256), 256, 0, c->stream>>>(a);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;

@@ -421,6 +421,11 @@ class EcsimContext:
                     "Mover::Relativistic::Boris")
         return n.value
 
+    def MoveParticlesBoris(self, dt_total):
+        """Mover::Boris (non-relativistic test-particle push) on the mesh
+        fields (E^n, corner B cur): one step of dt_total, then re-binning."""
+        self._check(self.lib.amps_gpu_move_particles_boris(self.h, dt_total), "Mover::Boris")
+
     def UpdateJMassMatrix(self):
         e = C.c_double()
         self._check(self.lib.amps_gpu_update_j_mass_matrix(self.h, C.byref(e)),

@@ -222,6 +222,14 @@ amps_gpu_status amps_gpu_move_particles(amps_gpu_ctx* ctx, long long* out_of_blo
  * substeps (optional) receives the total sub-steps. */
 amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* ctx, double dt_total,
                                                      double light_speed, long long* substeps);
+/* PIC::Mover::Boris (src/pic/pic_mover_boris.cpp:126-553, scalar path
+ * :264-290), the non-relativistic test-particle mover, with the Lorentz force
+ * of BorisSplitAcceleration_default (:104-112): one FP64 step of dt_total per
+ * particle, E = the corner E^n slot and B = the corner B "cur" slot
+ * interpolated at the particle's start position (CornerBased::InitStencil
+ * weights), then re-binning.  Uniform and AMR meshes; a particle past a face
+ * of an open axis is deleted (:352-427, the DELETE processing mode). */
+amps_gpu_status amps_gpu_move_particles_boris(amps_gpu_ctx* ctx, double dt_total);
 /* ECSIM::UpdateJMassMatrix (pic_field_solver_ecsim.cpp:3244): J and the
  * 243-term mass matrix on all corners from the corner B "cur" slot. */
 amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* ctx, double* particle_energy);

@@ -523,6 +523,53 @@ long orc_relboris(const orc_mesh* g, long n, double* x, double* v, const uint8_t
   return nsub;
 }
 
+/* Mover::Boris (pic_mover_boris.cpp:126-553): one step of dt per particle
+ * with E, B interpolated at the start position (CornerBased::InitStencil
+ * weights) from the corner arrays (interleaved x, y, z), x' = x + dt v'
+ * (:288-290), then findTreeNode/FindCellIndex (periodic wrap; past a face of
+ * an open axis the particle is deleted: block = cell = -1).  Returns the
+ * number of deleted particles. */
+long orc_boris(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
+               int32_t* block, int32_t* cell, const double* E, const double* B, double dt) {
+  long ndel = 0;
+  const int nbd[3] = {g->nbx, g->nby, g->nbz};
+  for (long p = 0; p < n; p++) {
+    double xs[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+    int bxyz[3], iX[3], nd[8][3];
+    double xmin[3], wt[8], wn[8];
+    locate_one(g, xs, block + p, cell + p);
+    block_geom(g, block[p], bxyz, xmin);
+    corner_stencil(xmin, g->dx, xs, wt, wn, nd, iX);
+    double Ef[3] = {0, 0, 0}, Bf[3] = {0, 0, 0};
+    for (int s2 = 0; s2 < 8; s2++) {
+      long c = cidx(g, bxyz[0] * NC + iX[0] + nd[s2][0], bxyz[1] * NC + iX[1] + nd[s2][1],
+                    bxyz[2] * NC + iX[2] + nd[s2][2]);
+      for (int d = 0; d < 3; d++) {
+        Ef[d] += wn[s2] * E[3 * c + d];
+        Bf[d] += wn[s2] * B[3 * c + d];
+      }
+    }
+    double* vp = v + 3 * p;
+    orc_boris_velocity(g->q[spec[p]] / g->m[spec[p]], dt, Ef, Bf, vp);
+    int gone = 0;
+    for (int d = 0; d < 3; d++) {
+      xs[d] = xs[d] + dt * vp[d];
+      if (((orc_open_axes >> d) & 1) &&
+          (xs[d] < g->x0[d] || xs[d] >= g->x0[d] + nbd[d] * NC * g->dx[d]))
+        gone = 1;
+    }
+    for (int d = 0; d < 3; d++) x[3 * p + d] = xs[d];
+    if (gone) {
+      block[p] = cell[p] = -1;
+      ndel++;
+      continue;
+    }
+    locate_one(g, xs, block + p, cell + p);
+    for (int d = 0; d < 3; d++) x[3 * p + d] = xs[d];
+  }
+  return ndel;
+}
+
 /* IndexMatrix[c1][c2] of ProcessCell (pic_field_solver_ecsim.cpp:1889-1891):
  * neighbour slot of corner c2 as seen from corner c1. */
 static int index_matrix(int c1, int c2) {

@@ -12,11 +12,14 @@
  *
  * Parity: the 81-point operator coefficients are pinned against the
  * reference's own stencil library (src/general/stencil.h) through
- * oracle/pins/stencil_pin.cpp.  The Lapenta2017 push, ProcessCell deposition
- * and the field update are restated line by line but cannot be compiled from
- * the reference (they need its generated build headers), so they are pinned
- * by the conservation law ECSIM is built on (theta = 0.5 conserves total
- * energy to the linear-solver tolerance) rather than by golden vectors.
+ * oracle/pins/stencil_pin.cpp.  ProcessCell (J, M, particle energy, cflCell),
+ * Lapenta2017 and Boris are pinned against the reference's own
+ * pic_field_solver_ecsim.cpp, pic_mover_boris.cpp and
+ * pic_interpolation_routines.cpp, compiled with a hand-written configuration
+ * by oracle/pins/ecsim_pin.cpp (golden tests/golden/ecsim_ref.json; equal to
+ * 1e-13, bit-identical on x86).  The field update is pinned by the
+ * conservation law ECSIM is built on (theta = 0.5 conserves total energy to
+ * the linear-solver tolerance).
  * The GMRES is absent from the reference (SWMF share/Library), so its
  * parity is unpinned: the stop rule is stated explicitly instead.
  */
@@ -61,8 +64,34 @@ double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
                    const uint8_t* spec, const double* wcorr, const int32_t* block,
                    const int32_t* cell, const double* Bc_cur, double* J, double* M);
 void orc_locate(const orc_mesh* g, long n, const double* x, int32_t* block, int32_t* cell);
+long orc_boris(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
+               int32_t* block, int32_t* cell, const double* E, const double* B, double dt);
 void orc_cfl(const orc_mesh* g, long n, const double* v, const uint8_t* spec,
              const int32_t* block, const int32_t* cell, double* cfl_max);
+
+/* Mover::Boris (src/pic/pic_mover_boris.cpp:126-553, scalar path :264-290)
+ * with the Lorentz force of BorisSplitAcceleration_default (:104-112):
+ * accl = (q/m) E, rotation = -(q/m) B, u = v + dt/2 accl, h = -dt/2 rotation,
+ * U = ((1-h^2) u + 2 (u x h + (u.h) h)) / (1+h^2), v' = U + dt/2 accl. */
+static inline void orc_boris_velocity(double qm, double dt, const double E[3], const double B[3],
+                                      double v[3]) {
+  double accl[3], rot[3], u[3], h[3], U[3];
+  const double dt2 = dt / 2.0;
+  for (int d = 0; d < 3; d++) {
+    accl[d] = 0.0 + qm * E[d];
+    rot[d] = 0.0 - qm * B[d];
+  }
+  for (int d = 0; d < 3; d++) {
+    u[d] = v[d] + dt2 * accl[d];
+    h[d] = -dt2 * rot[d];
+  }
+  const double h2 = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
+  const double uh = u[0] * h[0] + u[1] * h[1] + u[2] * h[2];
+  U[0] = ((1 - h2) * u[0] + 2 * (u[1] * h[2] - h[1] * u[2] + uh * h[0])) / (1 + h2);
+  U[1] = ((1 - h2) * u[1] + 2 * (u[2] * h[0] - h[2] * u[0] + uh * h[1])) / (1 + h2);
+  U[2] = ((1 - h2) * u[2] + 2 * (u[0] * h[1] - h[0] * u[1] + uh * h[2])) / (1 + h2);
+  for (int d = 0; d < 3; d++) v[d] = U[d] + dt2 * accl[d];
+}
 
 /* ---- field solve ---- */
 void orc_center_to_corner(const orc_mesh* g, const double* Bcen, double* Bcor);

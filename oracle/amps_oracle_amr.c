@@ -24,6 +24,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "amps_oracle.h"
+
 #define PI_D 3.14159265358979323846264338327950288
 
 extern int orc_open_axes; /* amps_oracle.c */
@@ -281,6 +283,48 @@ long orc_amr_relboris(const orc_amr* g, long n, double* x, double* v, const uint
     locate_one(g, xp, block + p, cell + p);
   }
   return nsub;
+}
+
+/* Mover::Boris (src/pic/pic_mover_boris.cpp:126-553) on a periodic AMR mesh:
+ * one step of dt with E, B interpolated at the start position from its leaf
+ * block's 8 cell corners (hanging corners through their constraint), the
+ * velocity update of orc_boris_velocity, x' = x + dt v', then re-location in
+ * the block tree (past a face of an open axis: deleted, block = cell = -1).
+ * Returns the number of deleted particles. */
+long orc_amr_boris(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
+                   int32_t* block, int32_t* cell, const double* E, const double* B, double dt) {
+  long ndel = 0;
+  const double dxf = g->dx0 / (double)(1 << g->lmax);
+  for (long p = 0; p < n; p++) {
+    double* xp = x + 3 * p;
+    double* vp = v + 3 * p;
+    double w[8], Ef[3] = {0, 0, 0}, Bf[3] = {0, 0, 0}, val[3];
+    int cid[8];
+    wrap_far(g, xp);
+    locate_one(g, xp, block + p, cell + p);
+    stencil(g, block[p], xp, w, cid);
+    for (int c = 0; c < 8; c++) {
+      corner_val(g, E, cid[c], val);
+      for (int d = 0; d < 3; d++) Ef[d] += w[c] * val[d];
+      corner_val(g, B, cid[c], val);
+      for (int d = 0; d < 3; d++) Bf[d] += w[c] * val[d];
+    }
+    orc_boris_velocity(g->q[spec[p]] / g->m[spec[p]], dt, Ef, Bf, vp);
+    int gone = 0;
+    for (int d = 0; d < 3; d++) {
+      xp[d] = xp[d] + dt * vp[d];
+      if (((orc_open_axes >> d) & 1) && (xp[d] < g->x0[d] || xp[d] >= g->x0[d] + g->nfine[d] * dxf))
+        gone = 1;
+    }
+    if (gone) {
+      block[p] = cell[p] = -1;
+      ndel++;
+      continue;
+    }
+    wrap_far(g, xp);
+    locate_one(g, xp, block + p, cell + p);
+  }
+  return ndel;
 }
 
 /* OpenFlow injection through face `face` of an open axis on the AMR mesh

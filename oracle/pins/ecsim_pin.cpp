@@ -26,6 +26,11 @@
 //     ParticleEnergy and cflCell;
 //   lapenta: particles with corner fields E^{n+theta}, B, and x', v' after
 //     Lapenta2017;
+//   boris: the same for Mover::Boris, whose force hook
+//     (_PIC_PARTICLE_MOVER__BORIS_SPLIT_ACCELERATION_) is set to
+//     pin_boris_split_acceleration: E and B of the corner fields at x with the
+//     reference's CornerBased::InitStencil weights, accl = (q/m) E,
+//     rotation = -(q/m) B, as BorisSplitAcceleration_default (:104-112);
 //   fields, corner_fields: the corner field function and its values at the
 //     corners of the block's cells, used for both.
 #include "pic.h"
@@ -33,6 +38,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <new>
 #include <vector>
 
 // ---- globals the compiled functions read, defined elsewhere in AMPS ----
@@ -63,6 +69,29 @@ void exit(long int line, const char* file, const char* msg) {
 
 PIC::ParticleBuffer::byte* PIC::ParticleBuffer::GetParticleDataPointer(long int ptr) {
   return ParticleDataBuffer + ptr * ParticleDataLength;
+}
+
+namespace {
+const double* g_hook_E = nullptr;  // corner fields the Boris force hook reads
+const double* g_hook_B = nullptr;
+}  // namespace
+
+void pin_boris_split_acceleration(double* accl, double* rotation, int spec, long int, double* x,
+                                  double*, void* startNode) {
+  PIC::InterpolationRoutines::CornerBased::cStencil st;
+  PIC::InterpolationRoutines::CornerBased::InitStencil(
+      x, static_cast<cTreeNodeAMR<PIC::Mesh::cDataBlockAMR>*>(startNode), st);
+  double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+  for (int t = 0; t < st.Length; t++)
+    for (int d = 0; d < 3; d++) {
+      E[d] += st.Weight[t] * g_hook_E[3 * st.LocalCellID[t] + d];
+      B[d] += st.Weight[t] * g_hook_B[3 * st.LocalCellID[t] + d];
+    }
+  const double qm = PIC::MolecularData::GetElectricCharge(spec) / PIC::MolecularData::GetMass(spec);
+  for (int d = 0; d < 3; d++) {
+    accl[d] = 0.0 + qm * E[d];
+    rotation[d] = 0.0 - qm * B[d];
+  }
 }
 
 namespace {
@@ -122,6 +151,10 @@ Block make_block(double dx, const FieldFn& f) {
     m->dx_max_refinment[d] = dx;
     m->dxRootBlock[d] = NX * dx;
   }
+  // the one non-trivial member the pinned functions touch (Boris walks the
+  // internal-boundary list): construct it in place, empty
+  using BoundaryList = decltype(m->InternalBoundaryList);
+  new (&m->InternalBoundaryList) BoundaryList();
   PIC::Mesh::mesh = m;
   b.node = static_cast<Node*>(calloc(1, sizeof(Node)));
   b.block = static_cast<PIC::Mesh::cDataBlockAMR*>(calloc(1, sizeof(PIC::Mesh::cDataBlockAMR)));
@@ -336,6 +369,37 @@ int main() {
     int i, j, k;
     PIC::Mesh::mesh->FindCellIndex(r.x, i, j, k, blk.node, false);
     printf("%s{\"species\":%d,\"in\":", n ? "," : "", species);
+    print_particle(q);
+    printf(",\"x\":[%.17g,%.17g,%.17g],\"v\":[%.17g,%.17g,%.17g],\"code\":%d,\"cell\":[%d,%d,%d]}",
+           r.x[0], r.x[1], r.x[2], r.v[0], r.v[1], r.v[2], code, i, j, k);
+  }
+  printf("],");
+
+  // ---- Boris on particles of the block interior (E = E^{n+theta} slot
+  // values, B = corner B: the same corner arrays) ----
+  PIC::Mesh::mesh->rootTree = blk.node;
+  g_hook_E = blk.E.data();
+  g_hook_B = blk.B.data();
+  printf("\"boris\":[");
+  for (int n = 0; n < 200; n++) {
+    Particle q;
+    for (int d = 0; d < 3; d++) q.x[d] = (0.5 + (NX - 1.0) * rng.next()) * dx;
+    const int species = n % 2;
+    use_species(species);
+    q.s = 0;
+    const double vt = species ? 0.01 : 0.05;
+    for (int d = 0; d < 3; d++) q.v[d] = vt * (2.0 * rng.next() - 1.0) * 1.7;
+    q.w = 1.0;
+    const long ptr = next_free++;
+    PIC::ParticleBuffer::byte* pp = buf.data() + ptr * L;
+    put(pp, q, -1, -1);
+    const int code = PIC::Mover::Boris(ptr, 2.5 * dt, blk.node);
+    Particle r = q;
+    PIC::ParticleBuffer::GetX(r.x, pp);
+    PIC::ParticleBuffer::GetV(r.v, pp);
+    int i, j, k;
+    PIC::Mesh::mesh->FindCellIndex(r.x, i, j, k, blk.node, false);
+    printf("%s{\"species\":%d,\"dt\":%.17g,\"in\":", n ? "," : "", species, 2.5 * dt);
     print_particle(q);
     printf(",\"x\":[%.17g,%.17g,%.17g],\"v\":[%.17g,%.17g,%.17g],\"code\":%d,\"cell\":[%d,%d,%d]}",
            r.x[0], r.x[1], r.x[2], r.v[0], r.v[1], r.v[2], code, i, j, k);

@@ -4,7 +4,11 @@
 // (input/test/fast-wave.input): electromagnetic ECSIM field solver with the
 // corner-based magnetic field, normalised units, one global time step,
 // species-dependent global particle weights with individual weight
-// corrections.  pic.h fixes PIC::nTotalSpecies at 1 (the configuration script
+// corrections.  Mover::Boris takes its force through the reference's hook
+// _PIC_PARTICLE_MOVER__BORIS_SPLIT_ACCELERATION_ (picGlobal.dfn:125), which
+// a model overrides with its own field source; here it is the harness's
+// pin_boris_split_acceleration (the Lorentz part of
+// BorisSplitAcceleration_default on the harness's corner fields).  pic.h fixes PIC::nTotalSpecies at 1 (the configuration script
 // rewrites that line), so the harness runs one species at a time.
 //
 // src/pic/pic.h includes src/pic/picGlobal.dfn (the defaults) and then the
@@ -20,3 +24,8 @@
 #undef _SIMULATION_TIME_STEP_MODE_
 #define _SIMULATION_TIME_STEP_MODE_ _SINGLE_GLOBAL_TIME_STEP_
 #define _TOTAL_SPECIES_NUMBER_ 1
+#undef _PIC_PARTICLE_MOVER__BORIS_SPLIT_ACCELERATION_
+#define _PIC_PARTICLE_MOVER__BORIS_SPLIT_ACCELERATION_(accl, rotation, spec, ptr, x, v, startNode) \
+  pin_boris_split_acceleration(accl, rotation, spec, ptr, x, v, startNode);
+void pin_boris_split_acceleration(double* accl, double* rotation, int spec, long int ptr, double* x,
+                                  double* v, void* startNode);

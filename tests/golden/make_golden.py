@@ -13,8 +13,8 @@ Run here (the reference sources are only present in the build container):
 * index_matrix.json      ProcessCell's IndexMatrix table
                          (src/pic/pic_field_solver_ecsim.cpp:1889-1891), read from
                          the reference source as text
-* ecsim_ref.json         ProcessCell (per-cell J, M, energy, cflCell) and Lapenta2017
-                         (x', v', cell) of the reference, compiled from
+* ecsim_ref.json         ProcessCell (per-cell J, M, energy, cflCell), Lapenta2017 and
+                         Boris (x', v', cell) of the reference, compiled from
                          src/pic/pic_field_solver_ecsim.cpp, pic_mover_boris.cpp and
                          pic_interpolation_routines.cpp with the hand-written
                          configuration of oracle/pins/refcfg/ (oracle/_ref/ecsim_pin)
@@ -105,7 +105,7 @@ def ecsim_ref():
                          check=True).stdout
     data = json.loads(out)
     data["source"] = ("src/pic/pic_field_solver_ecsim.cpp:1882-2438 ProcessCell, "
-                      "src/pic/pic_mover_boris.cpp:876-1380 Lapenta2017, "
+                      "src/pic/pic_mover_boris.cpp:876-1380 Lapenta2017, :126-553 Boris, "
                       "src/pic/pic_interpolation_routines.cpp:1074-1194 CornerBased::InitStencil")
     with open(os.path.join(HERE, "ecsim_ref.json"), "w") as f:
         json.dump(data, f)

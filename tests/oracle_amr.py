@@ -34,6 +34,8 @@ def lib():
             "orc_amr_push": (C.c_long, [C.POINTER(Amr), C.c_long, D, D, U8, I32, I32, D, D]),
             "orc_amr_relboris": (C.c_long, [C.POINTER(Amr), C.c_long, D, D, U8, I32, I32, D, D,
                                             C.c_double, C.c_double]),
+            "orc_amr_boris": (C.c_long, [C.POINTER(Amr), C.c_long, D, D, U8, I32, I32, D, D,
+                                         C.c_double]),
             "orc_amr_deposit": (C.c_double, [C.POINTER(Amr), C.c_long, D, D, U8, D, I32, I32, D,
                                              D, D]),
             "orc_amr_apply": (None, [C.POINTER(Amr), D, D, D, C.c_int, C.c_int, C.c_int]),
@@ -141,6 +143,13 @@ class AmrOracle:
                                        p(self.spec, C.c_uint8), p(self.block, C.c_int32),
                                        p(self.cell, C.c_int32), p(self.E_n), p(self.Bcur),
                                        dt_total, c_light)
+
+    def boris(self, dt):
+        """Mover::Boris with E^n and the corner B "cur" slot; returns the
+        number of particles deleted at open faces"""
+        return self.L.orc_amr_boris(C.byref(self.g), len(self.spec), p(self.x), p(self.v),
+                                    p(self.spec, C.c_uint8), p(self.block, C.c_int32),
+                                    p(self.cell, C.c_int32), p(self.E_n), p(self.Bcur), dt)
 
     def apply(self, x, identity=1, curl=1, mass=1):
         x = np.ascontiguousarray(x, np.float64)

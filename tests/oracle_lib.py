@@ -48,6 +48,7 @@ def load():
         "orc_push": (C.c_long, [C.POINTER(Mesh), C.c_long, D, D, U8, I32, I32, D, D]),
         "orc_relboris": (C.c_long, [C.POINTER(Mesh), C.c_long, D, D, U8, I32, I32, D, D,
                                     C.c_double, C.c_double]),
+        "orc_boris": (C.c_long, [C.POINTER(Mesh), C.c_long, D, D, U8, I32, I32, D, D, C.c_double]),
         "orc_deposit": (C.c_double, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D, D, D]),
         "orc_locate": (None, [C.POINTER(Mesh), C.c_long, D, I32, I32]),
         "orc_cfl": (None, [C.POINTER(Mesh), C.c_long, D, U8, I32, I32, D]),
@@ -143,6 +144,13 @@ class OracleState:
                                      p(self.spec, C.c_uint8), p(self.block, C.c_int32),
                                      p(self.cell, C.c_int32), p(self.E_n), p(self.Bcur),
                                      dt_total, c_light)
+
+    def boris(self, dt):
+        """Mover::Boris on E^n and the corner B cur slot; returns the number of
+        particles deleted at open faces"""
+        return self.lib.orc_boris(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
+                                  p(self.spec, C.c_uint8), p(self.block, C.c_int32),
+                                  p(self.cell, C.c_int32), p(self.E_n), p(self.Bcur), dt)
 
     def push(self):
         return self.lib.orc_push(C.byref(self.m), len(self.spec), p(self.x), p(self.v),

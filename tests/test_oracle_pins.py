@@ -257,3 +257,29 @@ def test_lapenta2017_matches_reference_build():
         assert all(r["code"] == 3 for r in recs)   # _PARTICLE_MOTION_FINISHED_
         gc = np.array([r["cell"][0] + 8 * (r["cell"][1] + 8 * r["cell"][2]) for r in recs])
         np.testing.assert_array_equal(cel, gc)
+
+
+def test_boris_matches_reference_build():
+    g = ref_golden()
+    lib = O.load()
+    E, B = ref_fields(g)
+    for species in (0, 1):
+        recs = [r for r in g["boris"] if r["species"] == species]
+        m = ref_mesh(g, species)
+        n = len(recs)
+        x = np.ascontiguousarray([r["in"]["x"] for r in recs], np.float64)
+        v = np.ascontiguousarray([r["in"]["v"] for r in recs], np.float64)
+        sp = np.zeros(n, np.uint8)
+        blk, cel = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        lib.orc_locate(O.C.byref(m), n, O.p(x), O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32))
+        ndel = lib.orc_boris(O.C.byref(m), n, O.p(x), O.p(v), O.p(sp, O.C.c_uint8),
+                             O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32), O.p(E), O.p(B),
+                             recs[0]["dt"])
+        assert ndel == 0
+        gx = np.array([r["x"] for r in recs])
+        gv = np.array([r["v"] for r in recs])
+        assert np.max(np.abs(x - gx)) < 1e-13 * g["dx"], np.max(np.abs(x - gx))
+        assert rel(v, gv) < 1e-13, rel(v, gv)
+        assert all(r["code"] == 3 for r in recs)   # _PARTICLE_MOTION_FINISHED_
+        gc = np.array([r["cell"][0] + 8 * (r["cell"][1] + 8 * r["cell"][2]) for r in recs])
+        np.testing.assert_array_equal(cel, gc)
