@@ -319,7 +319,7 @@ bool alloc_context(amps_gpu_ctx* c) {
        !dalloc(&c->d_scan_part, (nc + 1) / 1024 + 2) && !dalloc(&c->d_flags, 8);
   ok = ok && cudaMallocHost(&c->h_flags, 8 * sizeof(unsigned long long)) == cudaSuccess;
   ok = ok && !dalloc(&c->d_cellM, (size_t)AMPS_CELLM * nc) && !dalloc(&c->d_cellJ, 24 * nc) &&
-       !dalloc(&c->d_energy, 4);
+       !dalloc(&c->d_energy, 4 + AMPS_GPU_MAX_SPECIES);  // energies, then per-species CFL
   ok = ok && cudaMallocHost(&c->h_energy, 4 * sizeof(double)) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();

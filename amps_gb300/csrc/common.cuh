@@ -200,7 +200,7 @@ struct amps_gpu_ctx {
   // deposition scratch: per-cell partial sums
   float* d_cellM = nullptr;     // ncor * AMPS_CELLM
   float* d_cellJ = nullptr;     // ncor * 24
-  double* d_energy = nullptr;   // [0] particle, [1] wave
+  double* d_energy = nullptr;   // [0] particle, [1] wave, [4 + s] max CFL of species s
   double* h_energy = nullptr;   // pinned
 
   // species moments on corners (species.cu), when sampling is on

@@ -24,7 +24,8 @@ constexpr uint8_t kHole = 0xFF;
 struct SpeciesTab {
   float qdt2m[AMPS_GPU_MAX_SPECIES];  // 0.5*q*dt/m (weight independent)
   float qw[AMPS_GPU_MAX_SPECIES];     // q*w
-  float mw[AMPS_GPU_MAX_SPECIES];     // m*w
+  float keh[AMPS_GPU_MAX_SPECIES];    // 0.5*m*w (FP64) = keh + kel, two floats
+  float kel[AMPS_GPU_MAX_SPECIES];
 };
 
 SpeciesTab make_species(const amps_gpu_config& c) {
@@ -32,9 +33,25 @@ SpeciesTab make_species(const amps_gpu_config& c) {
   for (int s = 0; s < c.nspec; s++) {
     t.qdt2m[s] = (float)(0.5 * (c.charge[s] * c.dt / c.mass[s]));
     t.qw[s] = (float)(c.charge[s] * c.weight[s]);
-    t.mw[s] = (float)(c.mass[s] * c.weight[s]);
+    const double ke = 0.5 * c.mass[s] * c.weight[s];
+    t.keh[s] = (float)ke;
+    t.kel[s] = (float)(ke - (double)t.keh[s]);
   }
   return t;
+}
+
+// en += the kinetic energy 0.5 m W v^2 of one particle (ProcessCell :2238,
+// summed in FP64 by the reference) as a float pair: the squares and the
+// weight-correction product exact by FMA, sums by TwoSum, the FP64 species
+// factor 0.5 m w as two floats (FF, common.cuh).  Error ~1e-14 of the sum.
+__device__ __forceinline__ void kinetic_energy(FF& en, float v0, float v1, float v2, float wcorr,
+                                               int s, const SpeciesTab& st) {
+  const float p0 = __fmul_rn(v0, v0);
+  FF t{p0, fmaf(v0, v0, -p0)};
+  ff_add(t, v1, v1, 0.f);
+  ff_add(t, v2, v2, 0.f);
+  const FF tw = ff_mul(t.s, t.q, wcorr, 0.f);
+  ff_add2(en, st.keh[s], st.kel[s], tw.s, tw.q);
 }
 
 // Stage one bulk copy per stencil into shared memory; returns false on timeout.
@@ -81,12 +98,12 @@ __host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
   return cid * 24 + ce;
 }
 
-// Record of one particle at block-local offset u inside cell (i,j,k); returns
-// its kinetic energy 0.5 m W v^2 (FP32; summed per cell, then in FP64).
-__device__ __forceinline__ float stage_record(float* __restrict__ r, const float4* __restrict__ sB,
-                                               float u0, float u1, float u2, float v0, float v1,
-                                               float v2, int s, float wcorr, int i, int j, int k,
-                                               const SpeciesTab& st, float inv_vol) {
+// Record of one particle at block-local offset u inside cell (i,j,k); adds
+// its kinetic energy to en.
+__device__ __forceinline__ void stage_record(float* __restrict__ r, const float4* __restrict__ sB,
+                                             float u0, float u1, float u2, float v0, float v1,
+                                             float v2, int s, float wcorr, int i, int j, int k,
+                                             const SpeciesTab& st, float inv_vol, FF& en) {
   const float fx = fminf(fmaxf(u0 - (float)i, 0.f), 1.f);
   const float fy = fminf(fmaxf(u1 - (float)j, 0.f), 1.f);
   const float fz = fminf(fmaxf(u2 - (float)k, 0.f), 1.f);
@@ -119,7 +136,6 @@ __device__ __forceinline__ float stage_record(float* __restrict__ r, const float
   al[7] = c0 * (P0 + h2 * B2 * B1);
   al[8] = c0 * (1.f + h2 * B2 * B2);
   const float qW = st.qw[s] * wcorr;
-  const float mW = st.mw[s] * wcorr;
   const float kc = qW * h * inv_vol;
   float4* r4 = reinterpret_cast<float4*>(r);
   {
@@ -150,7 +166,7 @@ __device__ __forceinline__ float stage_record(float* __restrict__ r, const float
   const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
   const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
   r4[15] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
-  return 0.5f * mW * (v0 * v0 + v1 * v1 + v2 * v2);
+  kinetic_energy(en, v0, v1, v2, wcorr, s, st);
 }
 
 // Each of the first kTileLanes lanes owns a 3 x 3 tile: lanes 0..26 the

@@ -141,28 +141,25 @@ __global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
   float* rec = s_rec + wid * 32 * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
-  double en = 0.0;
+  FF en{0.f, 0.f};
   const int j = wid;
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = a.start[cid], n0 = a.start[cid + 1] - b0;
     Tile tile;
     tile.zero();
-    float en_cell = 0.f;
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const long long p = b0 + q0 + lane;
       if (q0 + lane < n0)
-        en_cell += stage_record(rec + lane * kRec, s_dep, a.u[p], a.u[a.n + p], a.u[2 * a.n + p],
-                                a.v[p], a.v[a.n + p], a.v[2 * a.n + p], a.sp[p], 1.0f, i, j, k,
-                                a.st, a.inv_vol);
+        stage_record(rec + lane * kRec, s_dep, a.u[p], a.u[a.n + p], a.u[2 * a.n + p], a.v[p],
+                     a.v[a.n + p], a.v[2 * a.n + p], a.sp[p], 1.0f, i, j, k, a.st, a.inv_vol, en);
       __syncwarp();
       if (lane < kTileLanes) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
-    en += (double)en_cell;
   }
-  reduce_energy(en, s_en, a.energy);
+  reduce_energy(ff_value(en), s_en, a.energy);
 }
 
 __global__ void __launch_bounds__(256) k_na_assemble(NaMesh m, long long ncor,
@@ -276,7 +273,9 @@ amps_gpu_status deposit_noalloc(const amps_gpu_config* cfg, long long n, const i
   for (int q = 0; q < cfg->nspec; q++) {
     a.st.qdt2m[q] = (float)(0.5 * (cfg->charge[q] * cfg->dt / cfg->mass[q]));
     a.st.qw[q] = (float)(cfg->charge[q] * cfg->weight[q]);
-    a.st.mw[q] = (float)(cfg->mass[q] * cfg->weight[q]);
+    const double ke = 0.5 * cfg->mass[q] * cfg->weight[q];
+    a.st.keh[q] = (float)ke;
+    a.st.kel[q] = (float)(ke - (double)a.st.keh[q]);
   }
   const size_t smem = AMPS_SC * sizeof(float4) + kNaWarps * 32 * kRec * sizeof(float);
   k_na_deposit<<<dim3((unsigned)nb, AMPS_NC), kNaWarps * 32, smem, s>>>(a);

@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   float* rec = s_rec + wid * 32 * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
-  float en_row = 0.f;  // FP32 across the row's cells, FP64 in the CTA reduction
+  FF en_row{0.f, 0.f};  // float pair across the row's cells, FP64 in the CTA reduction
   unsigned long long n_far = 0, n_near = 0, n_del = 0;
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
@@ -236,7 +236,6 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = __shfl_sync(0xffffffffu, mb0, i), n0 = __shfl_sync(0xffffffffu, mn0, i);
     Tile tile;
-    float en_cell = 0.f;
     tile.zero();
     int nst = 0;
     // software pipeline: the next chunk's particles are loaded while this one
@@ -348,8 +347,8 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
           if (a.p.id) a.p.id[d] = idv;
         }
         if (DEP)
-          en_cell += stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv,
-                             i, j, k, a.st, inv_vol);
+          stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv, i, j,
+                       k, a.st, inv_vol, en_row);
       }
       // movers: slack of the destination cell, else the overflow list
       const bool mover = act && !stays && key >= 0;
@@ -388,15 +387,12 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
     // vacated slots become holes
     for (int t = nst + lane; t < n0; t += 32) a.p.sp[b0 + t] = kHole;
     if (lane == 0) a.stay[cid] = nst;
-    if (DEP) {
-      tile.flush(lane, a.cellM, a.cellJ, cid, false);
-      en_row += en_cell;
-    }
+    if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid, false);
   }
   if (n_far) atomicAdd(a.flags + 0, n_far);
   if (n_near) atomicAdd(a.flags + 1, n_near);
   if (n_del) atomicAdd(a.flags + 5, n_del);
-  if (DEP) reduce_energy((double)en_row, s_en, a.energy);
+  if (DEP) reduce_energy(ff_value(en_row), s_en, a.energy);
 }
 
 // ---------------------------------------------------------------------------
@@ -647,7 +643,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   float* rec = s_rec + wid * kArrChunk * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
-  float en_row = 0.f;  // the row's arrivals: a few per cell, FP32 is enough before the FP64 reduction
+  FF en_row{0.f, 0.f};  // the row's arrivals, as a float pair before the FP64 reduction
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
   // the row's 8 cells: lane i < 8 loads cell i's slot range, occupancy, stayers
@@ -669,7 +665,6 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     if (na > 0) {
       Tile tile;
       tile.zero();
-      float en_cell = 0.f;  // FP32 per cell, FP64 across cells (FP64 issues slowly here)
       float old[9];
       if (DEP) tile.preload(lane, a.cellM, a.cellJ, cid, old);
       const int src0 = b0 + cap - na, dst0 = b0 + nst;
@@ -695,8 +690,8 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
           if (a.p.wc) a.p.wc[pd] = wcv;
           if (a.p.id) a.p.id[pd] = idv;
           if (DEP)
-            en_cell += stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
-                                    wcv, i, j, k, a.st, inv_vol);
+            stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv, i, j,
+                         k, a.st, inv_vol, en_row);
         }
         if (DEP) {
           __syncwarp();
@@ -712,7 +707,6 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
         if (slot >= dst0 + na) a.p.sp[slot] = kHole;
       }
       if (DEP) tile.flush_onto(lane, a.cellM, a.cellJ, cid, old);
-      en_row += en_cell;
     }
   }
   if (lane < AMPS_NC) {
@@ -720,7 +714,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     a.cnt[cl] = mst + max(0, min(marr, mcap - mn0));
     a.arr[cl] = 0;
   }
-  if (DEP) reduce_energy((double)en_row, s_en, a.energy);
+  if (DEP) reduce_energy(ff_value(en_row), s_en, a.energy);
 }
 
 // Full deposition over the compact layout.
@@ -738,7 +732,7 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
   float* rec = s_rec + wid * 32 * kRec;
   int offA, offB;
   lane_offsets(lane, offA, offB);
-  double en = 0.0;
+  FF en{0.f, 0.f};
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
   for (int i = 0; i < AMPS_NC; i++) {
@@ -746,21 +740,19 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
     const int b0 = a.base[cid], n0 = a.cnt[cid];
     Tile tile;
     tile.zero();
-    float en_cell = 0.f;
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const long long p = b0 + q0 + lane;
       if (q0 + lane < n0)
-        en_cell += stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p],
-                                a.p.v[0][p], a.p.v[1][p], a.p.v[2][p], a.p.sp[p],
-                                a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st, inv_vol);
+        stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p], a.p.v[0][p],
+                     a.p.v[1][p], a.p.v[2][p], a.p.sp[p], a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st,
+                     inv_vol, en);
       __syncwarp();
       if (lane < kTileLanes) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
-    en += (double)en_cell;
   }
-  reduce_energy(en, s_en, a.energy);
+  reduce_energy(ff_value(en), s_en, a.energy);
 }
 
 // ---------------------------------------------------------------------------

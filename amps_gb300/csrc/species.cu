@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "common.cuh"
@@ -239,7 +240,111 @@ cudaError_t launch_species_moments(amps_gpu_ctx* c) {
   return cudaGetLastError();
 }
 
+// Per-species CFL number of UpdateJMassMatrix (ProcessCell,
+// src/pic/pic_field_solver_ecsim.cpp:2236 and :2356-2359; maximum over cells
+// :3352, :3972-3977): per cell and species the mean particle speed times dt
+// over the cell diagonal, maximum over the cells holding that species.  One
+// warp per cell, one pass per species present; |v| as a float pair (exact
+// squares, TwoSum, sqrt with one Newton correction), cell sums as float
+// pairs, the ratio in FP64 by one lane; the maximum by an integer atomicMax on
+// the bits of a non-negative double.
+struct CflArgs {
+  const float* v[3];
+  const uint8_t* sp;
+  const int* base;
+  const int* cnt;
+  long long ncell;
+  int nspec;
+  double dt;
+  double diag;                 // uniform meshes: |(dx, dy, dz)|
+  const double* bdx;           // AMR meshes: cell size per block (diagonal sqrt(3) dx)
+  unsigned long long* cfl;     // [nspec] bits of the FP64 maximum
+};
+
+__device__ __forceinline__ FF speed_ff(float v0, float v1, float v2) {
+  const float p0 = __fmul_rn(v0, v0);
+  FF t{p0, fmaf(v0, v0, -p0)};
+  ff_add(t, v1, v1, 0.f);
+  ff_add(t, v2, v2, 0.f);
+  t = ff_norm(t);
+  const float r = __fsqrt_rn(t.s);
+  if (r == 0.f) return FF{0.f, 0.f};
+  // sqrt(s + q) = r + (s - r^2 + q) / (2 r) to second order; s - r^2 is exact
+  const float e = __fadd_rn(fmaf(-r, r, t.s), t.q);
+  return FF{r, __fdiv_rn(e, __fmul_rn(2.f, r))};
+}
+
+__global__ void __launch_bounds__(256) k_particle_cfl(CflArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long cid = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cid < a.ncell;
+       cid += nw) {
+    const int b0 = a.base[cid], n = a.cnt[cid];
+    unsigned present = 0;
+    for (int q = lane; q < n; q += 32) present |= 1u << a.sp[b0 + q];
+    present = __reduce_or_sync(0xffffffffu, present);
+    for (int s = 0; s < a.nspec; s++) {
+      if (!((present >> s) & 1u)) continue;
+      FF sum{0.f, 0.f};
+      int count = 0;
+      for (int q = lane; q < n; q += 32) {
+        const int p = b0 + q;
+        if (a.sp[p] != s) continue;
+        const FF sv = speed_ff(a.v[0][p], a.v[1][p], a.v[2][p]);
+        ff_acc(sum, sv.s, sv.q);
+        count++;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float hs = __shfl_xor_sync(0xffffffffu, sum.s, o);
+        const float hq = __shfl_xor_sync(0xffffffffu, sum.q, o);
+        ff_acc(sum, hs, hq);
+        count += __shfl_xor_sync(0xffffffffu, count, o);
+      }
+      if (lane == 0 && count > 0) {
+        const double diag = a.bdx ? 1.7320508075688772 * a.bdx[cid / AMPS_CPB] : a.diag;
+        const double cfl = ff_value(sum) * a.dt / ((double)count * diag);
+        atomicMax(a.cfl + s, (unsigned long long)__double_as_longlong(cfl));
+      }
+    }
+  }
+}
+
 extern "C" {
+
+amps_gpu_status amps_gpu_particle_cfl(amps_gpu_ctx* c, double* cfl) {
+  if (!c || !cfl) return set_err(c, AMPS_GPU_INVALID_ARG, "particle_cfl: null output");
+  cudaSetDevice(c->cfg.device);
+  CflArgs a{};
+  for (int d = 0; d < 3; d++) a.v[d] = c->d_v[c->cur][d];
+  a.sp = c->d_sp[c->cur];
+  a.base = c->d_base;
+  a.cnt = c->d_cnt;
+  a.ncell = c->ncor;
+  a.nspec = c->cfg.nspec;
+  a.dt = c->cfg.dt;
+  a.diag = sqrt(c->cfg.dx[0] * c->cfg.dx[0] + c->cfg.dx[1] * c->cfg.dx[1] +
+                c->cfg.dx[2] * c->cfg.dx[2]);
+  a.bdx = c->amr ? c->d_bdx : nullptr;
+  a.cfl = reinterpret_cast<unsigned long long*>(c->d_energy + 4);
+  amps_gpu_status st;
+  if ((st = cuda_check(c, cudaMemsetAsync(a.cfl, 0, AMPS_GPU_MAX_SPECIES * sizeof(double), c->stream),
+                       "cfl reset")))
+    return st;
+  {
+    TimedLaunch t(c, "particle_cfl");
+    const long long blocks = std::min<long long>((c->ncor + 7) / 8, 152LL * 16);
+    if (blocks > 0) k_particle_cfl<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+  }
+  if ((st = cuda_check(c, cudaGetLastError(), "particle_cfl"))) return st;
+  double out[AMPS_GPU_MAX_SPECIES];
+  if ((st = cuda_check(c, cudaMemcpyAsync(out, c->d_energy + 4, c->cfg.nspec * sizeof(double),
+                                          cudaMemcpyDeviceToHost, c->stream), "cfl")))
+    return st;
+  if ((st = cuda_check(c, cudaStreamSynchronize(c->stream), "sync"))) return st;
+  for (int s = 0; s < c->cfg.nspec; s++) cfl[s] = out[s];
+  return AMPS_GPU_OK;
+}
 
 amps_gpu_status amps_gpu_set_species_moments(amps_gpu_ctx* c, int on) {
   if (!c) return AMPS_GPU_INVALID_ARG;

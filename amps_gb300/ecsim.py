@@ -426,6 +426,13 @@ class EcsimContext:
         fields (E^n, corner B cur): one step of dt_total, then re-binning."""
         self._check(self.lib.amps_gpu_move_particles_boris(self.h, dt_total), "Mover::Boris")
 
+    def particle_cfl(self):
+        """per-species maximum CFL number of the current particles (the value
+        UpdateJMassMatrix prints)"""
+        out = np.zeros(len(self.wl.species))
+        self._check(self.lib.amps_gpu_particle_cfl(self.h, ptr(out, C.c_double)), "particle_cfl")
+        return out
+
     def UpdateJMassMatrix(self):
         e = C.c_double()
         self._check(self.lib.amps_gpu_update_j_mass_matrix(self.h, C.byref(e)),

@@ -230,6 +230,13 @@ amps_gpu_status amps_gpu_move_particles_relativistic(amps_gpu_ctx* ctx, double d
  * weights), then re-binning.  Uniform and AMR meshes; a particle past a face
  * of an open axis is deleted (:352-427, the DELETE processing mode). */
 amps_gpu_status amps_gpu_move_particles_boris(amps_gpu_ctx* ctx, double dt_total);
+/* The per-species CFL number UpdateJMassMatrix reports ("max cfl number for
+ * spec", src/pic/pic_field_solver_ecsim.cpp:2236, :2356-2359, :3972-3987): per
+ * cell and species sum(|v| dt) / (count * |cell diagonal|), the maximum over
+ * the cells that hold the species (cells without it do not count).  Computed
+ * on demand from the particles as they are now -- right after a deposition,
+ * the particles ProcessCell saw -- in FP64-accurate arithmetic.  cfl[nspec]. */
+amps_gpu_status amps_gpu_particle_cfl(amps_gpu_ctx* ctx, double* cfl);
 /* ECSIM::UpdateJMassMatrix (pic_field_solver_ecsim.cpp:3244): J and the
  * 243-term mass matrix on all corners from the corner B "cur" slot. */
 amps_gpu_status amps_gpu_update_j_mass_matrix(amps_gpu_ctx* ctx, double* particle_energy);
