@@ -2,12 +2,16 @@
 
 The shared library is the product; this module only binds it.  Importing it
 fails loudly when the library has not been built: there is no CPU fallback.
+The host-side mesh builder and initial condition (amps_amr_*, amps_ic_*) live
+in libamps_host.so, on which libamps_gpu.so depends; load_host() binds that
+library alone, for callers that build meshes and particles without a GPU.
 """
 import ctypes as C
 import os
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libamps_gpu.so")
+HOST_LIB_PATH = os.path.join(_HERE, "libamps_host.so")
 
 MAX_SPECIES = 8
 
@@ -160,6 +164,25 @@ SIGNATURES = {
 }
 
 _lib = None
+_host = None
+
+
+def load_host():
+    """Load and bind libamps_host.so (AMR mesh builder, initial condition)."""
+    global _host
+    if _host is not None:
+        return _host
+    if not os.path.exists(HOST_LIB_PATH):
+        raise ImportError("libamps_host.so is not built (%s); run __graft_entry__.build()"
+                          % HOST_LIB_PATH)
+    lib = C.CDLL(HOST_LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        if name.startswith(("amps_amr_", "amps_ic_")):
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+    _host = lib
+    return lib
 
 
 def load():

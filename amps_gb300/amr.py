@@ -21,7 +21,7 @@ class BlockDesc(C.Structure):
 def nested_leaves(nb0, lmax, mode, frac):
     """Leaves of a nested refinement (mode 0: central box of relative half-width
     frac/2, mode 1: central sphere of relative radius frac; halved per level)."""
-    lib = _capi.load()
+    lib = _capi.load_host()
     n = lib.amps_amr_nested_leaves(nb0[0], nb0[1], nb0[2], lmax, mode, frac, None, 0)
     if n < 0:
         raise AmpsGpuError(-n, "amps_amr_nested_leaves")
@@ -36,7 +36,7 @@ class AmrMesh:
 
     def __init__(self, nb0, lmax, leaves, dx0=1.0, x0=(0.0, 0.0, 0.0), open_axes=(False, False, False),
                  field_bc=0):
-        self.lib = _capi.load()
+        self.lib = _capi.load_host()
         self.nb0 = tuple(int(v) for v in nb0)
         self.lmax = int(lmax)
         self.dx0 = float(dx0)
@@ -138,7 +138,7 @@ def amr_initial_condition(mesh, species, ppc_base, seed=100, nthreads=1, per_cel
     are generated on nthreads host threads (the result does not depend on it)."""
     ns = len(species)
     vth = np.array([s.vth for s in species], np.float64)
-    lib = _capi.load()
+    lib = _capi.load_host()
 
     def block_ppc(b):
         return ppc_base if per_cell else max(1, ppc_base // (8 ** int(mesh.level[b])))

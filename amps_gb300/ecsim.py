@@ -105,7 +105,7 @@ def make_initial_condition(wl: Workload, nthreads: int = 8):
     """Maxwellian particles (FP32-representable) from the reference LCG.
     Returns dict with u (n,3) float32 cell-unit offsets, v (n,3) float32,
     spec (n,) uint8, block (n,) int32 and x (n,3) float64 physical."""
-    lib = _capi.load()
+    lib = _capi.load_host()
     m = wl.mesh
     ns = len(wl.species)
     n = lib.amps_ic_count(m.nbx, m.nby, m.nbz, wl.ppc, ns)

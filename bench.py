@@ -504,14 +504,20 @@ def restart_line(ctx):
     return out
 
 
-def oracle_check(workload, device):
-    """One full ECSIM step of the workload on the GPU and on the FP64 AMR oracle
-    from the same initial state (the oracle starts from the device's FP32 particle
-    offsets): relative errors of fields, per-cell moments and particles."""
+def cpu_leg(workload, device, tol=None):
+    """The CPU baseline leg: one full ECSIM step (UpdateJMassMatrix, field
+    solve, push + re-bin + deposit) of an AMR workload on the GPU and in the
+    FP64 AMR oracle from the same particles (the oracle starts from the GPU's
+    FP32-stored state).  Returns (cpu_baseline, parity): the oracle's push +
+    deposit rate on one core, and the relative errors (max norm over the max
+    entry) of fields, per-cell moments, particles and energies, with the
+    block/cell mismatches checked against the face rule (tests/parity.py)."""
     import amps_gb300 as A
     from amps_gb300 import amr
     from tests import oracle_amr as OA
+    from tests import parity as P
     wl = amr.AMR_WORKLOADS[workload]()
+    tol = tol or wl.tol
     mesh = wl.mesh()
     ic = wl.initial_condition(mesh, seed=100, nthreads=os.cpu_count() or 8)
     n = len(ic["spec"])
@@ -522,11 +528,9 @@ def oracle_check(workload, device):
     e0 = ctx.export_particles()
     order = np.argsort(e0["id"])
     x0 = e0["x"][order]
-    t0 = time.perf_counter()
     ctx.UpdateJMassMatrix()
-    st = ctx.PicTimeStep(tol=wl.tol, maxit=400, precond=1)
-    ctx.synchronize()
-    t_gpu = time.perf_counter() - t0
+    st = ctx.PicTimeStep(tol=tol, maxit=400, precond=1)
+    cfl_gpu = ctx.particle_cfl()
     g = ctx.export_fields()
     gJ, gM = ctx.export_cell_moments()
     e1 = ctx.export_particles()
@@ -538,10 +542,13 @@ def oracle_check(workload, device):
     ao.Bcen[:] = f["B_center"]
     ao.Bprev[:] = f["B_corner_prev"]
     ao.Bcur[:] = f["B_corner_cur"]
-    t0 = time.perf_counter()
     ao.deposit()
-    it, diag = ao.step(tol=wl.tol, maxit=400)
-    t_cpu = time.perf_counter() - t0
+    it, wave = ao.field_solve(tol=tol, maxit=400)
+    t0 = time.perf_counter()
+    ao.push()
+    t1 = time.perf_counter()
+    pe = ao.deposit()
+    t2 = time.perf_counter()
 
     def rel(a, b):
         den = np.max(np.abs(b))
@@ -549,28 +556,53 @@ def oracle_check(workload, device):
     L = np.array(mesh.nfine, float) * mesh.dxf
     d = e1["x"][o1] - ao.x
     d -= L * np.rint(d / L)
-    same = (e1["block"][o1] == ao.block) & (e1["cell"][o1] == ao.cell)
-    # particles within rounding of a cell face may sit in the neighbouring cell
-    # (same corners, same corner moments, but another cell's partials): compare
-    # the per-cell partials on the cells no such particle touches
+    gb, gc = e1["block"][o1], e1["cell"][o1]
+    rep = P.mismatch_report(e1["x"][o1], gb, gc, ao.x, ao.block, ao.cell, mesh.block_origins(),
+                            mesh.block_dx(), L)
+    same = (gb == ao.block) & (gc == ao.cell)
+    # a particle filed in the neighbouring cell moves its contribution between
+    # the two cells' partials (same corners, same corner moments): compare the
+    # per-cell partials of the cells no such particle touches
     touched = np.zeros(mesh.ncells, bool)
-    touched[(e1["block"][o1] * 512 + e1["cell"][o1])[~same]] = True
+    touched[(gb * 512 + gc)[~same]] = True
     touched[(ao.block * 512 + ao.cell)[~same]] = True
     keep = ~touched
-    gJk, oJk = gJ.reshape(-1, 24)[keep], ao.cellJ.reshape(-1, 24)[keep]
-    gMk, oMk = gM.reshape(-1, 324)[keep], ao.cellM.reshape(-1, 324)[keep]
-    return {"workload": workload, "particles": n, "gpu_seconds": round(t_gpu, 3),
-            "oracle_seconds": round(t_cpu, 1),
-            "rel_err_E_n": rel(g["E_n"], ao.E_n), "rel_err_E_half": rel(g["E_half"], ao.E_half),
-            "rel_err_B_center": rel(g["B_center"] - np.array(wl.b0), ao.Bcen - np.array(wl.b0)),
-            "rel_err_cell_J": rel(gJk, oJk), "rel_err_cell_M": rel(gMk, oMk),
-            "cells_excluded_face_particles": int(touched.sum()),
-            "max_position_err_dx0": float(np.max(np.abs(d)) / mesh.dx0),
-            "rel_err_v": rel(e1["v"][o1], ao.v),
-            "block_cell_identical": float(np.mean(same)),
-            "particle_energy_rel": abs(st.particle_energy - diag[0]) / diag[0],
-            "wave_energy_rel": abs(st.solve.wave_energy - diag[1]) / diag[1],
-            "gmres_iterations_gpu_oracle": [st.solve.iterations, int(it)]}
+    b0 = np.array(wl.b0)
+    # the oracle's per-species CFL of the same particles (ProcessCell's cflCell)
+    key = ao.block.astype(np.int64) * 512 + ao.cell
+    cfl_orc = []
+    for s in range(len(wl.species)):
+        m = ao.spec == s
+        u, inv = np.unique(key[m], return_inverse=True)
+        sums = np.bincount(inv, weights=np.sqrt(np.sum(ao.v[m] ** 2, axis=1)) * wl.dt)
+        cnt = np.bincount(inv)
+        diag = np.sqrt(3.0) * mesh.block_dx()[u // 512]
+        cfl_orc.append(float(np.max(sums / (cnt * diag))))
+    parity = {
+        "workload": workload, "particles": n, "tol": tol,
+        "rel_err_E_n": rel(g["E_n"], ao.E_n), "rel_err_E_half": rel(g["E_half"], ao.E_half),
+        "rel_err_B_center": rel(g["B_center"] - b0, ao.Bcen - b0),
+        "rel_err_B_corner": rel(g["B_corner_cur"] - b0, ao.Bcur - b0),
+        "rel_err_cell_J": rel(gJ.reshape(-1, 24)[keep], ao.cellJ.reshape(-1, 24)[keep]),
+        "rel_err_cell_M": rel(gM.reshape(-1, 324)[keep], ao.cellM.reshape(-1, 324)[keep]),
+        "cells_excluded_face_particles": int(touched.sum()),
+        "max_position_err_dx0": float(np.max(np.abs(d)) / mesh.dx0),
+        "rel_err_v": rel(e1["v"][o1], ao.v),
+        "block_cell_mismatches": rep["mismatches"],
+        "mismatch_max_offset_ulps": round(rep["max_offset_ulps"], 3),
+        "face_rule_holds": rep["face_rule_holds"],
+        "particle_energy_rel": abs(st.particle_energy - pe) / pe,
+        "wave_energy_rel": abs(st.solve.wave_energy - wave) / wave,
+        "cfl_rel": float(np.max(np.abs(cfl_gpu - np.array(cfl_orc)) / np.array(cfl_orc))),
+        "gmres_iterations_gpu_oracle": [int(st.solve.iterations), int(it)],
+        "norm": "max |gpu - oracle| / max |oracle| per array",
+    }
+    cpu = {"value": n / (t2 - t0), "unit": UNIT, "cores": 1, "kind": "port",
+           "sample": "FP64 AMR oracle (Lapenta2017 + re-binning across levels + ProcessCell, "
+                     "restated line by line and pinned to the reference's compiled ProcessCell/"
+                     "Lapenta2017) on one core: one push + deposit of %s (%d particles), %.1f s"
+                     % (workload, n, t2 - t0)}
+    return cpu, parity
 
 
 def field_solve_ab(ctx, tol, ev, stream, reps=3):
@@ -745,14 +777,18 @@ def run_gpu(args):
     nl = max(1, launches)
     nbytes = kernel_bytes(npart, ncell, nblk, top)
     traffic = args.traffic
+    traffic_src = "--traffic" if traffic is not None else None
     if traffic is None and top in MEASURED_TRAFFIC.get(args.workload, {}):
         traffic = MEASURED_TRAFFIC[args.workload][top]
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of this command, kernel "
+                       "revision: " + MEASURED_TRAFFIC[args.workload]["version"])
     roof = None
     if nbytes:
         achieved = nbytes / (ms_top / nl / 1e3) / 1e9
         roof = {"kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                "traffic": traffic, "algorithmic_bytes_per_launch": int(nbytes),
+                "traffic": traffic, "traffic_source": traffic_src,
+                "algorithmic_bytes_per_launch": int(nbytes),
                 "avg_launch_ms": round(ms_top / nl, 4)}
         if top == "push_deposit":
             # the deposition is FP32-issue bound: its FP32 pipe rate beside the HBM one
@@ -769,17 +805,15 @@ def run_gpu(args):
     # kernels per step (from the event-timed pass) x timed steps
     gpu_launches = int(round(sum(v[1] for v in per.values()) / n_kt * args.steps))
 
-    cpu = None
-    if rank == 0 and args.cpu_seconds > 0:
+    cpu = parity = None
+    if rank == 0 and ws == 1 and args.cpu_seconds > 0:
         if info["amr"]:
-            rate, ci = cpu_amr_replica_rate(args.cpu_seconds, 1)
-            smp = "FP64 AMR oracle push+re-bin+ProcessCell on one replica (%s; %d particles), " \
-                  "%.1f s" % (ci["replica"], ci["replica_particles"], ci["seconds"])
+            cpu, parity = cpu_leg(args.parity_workload, local)
         else:
             rate, ci = cpu_replica_rate(args.workload, 1, args.cpu_seconds, 1)
             smp = "FP64 oracle Lapenta2017+ProcessCell on a periodic 8^3-cell replica of the " \
                   "same plasma (%d particles), %.1f s" % (ci["replica_particles"], ci["seconds"])
-        cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp}
+            cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": smp}
     trc = None
     if rank == 0 and args.tracer > 0:
         trc = tracer_line(args.tracer, max(1, args.tracer // 256), local)
@@ -802,7 +836,7 @@ def run_gpu(args):
                 "gmres_precond": "jacobi", "first_solve_iterations": solve.iterations,
                 "cuda_graphs": args.graphs > 0, "autotune": tuning}),
             "e2e": e2e, "e2e_particle_roundtrip": e2e_particles,
-            "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu,
+            "roofline": roof, "kernel_shares": shares, "cpu_baseline": cpu, "parity": parity,
             "precond_ab": pab, "tracer": trc, "energy": energy, "restart": rst,
             "clocks": clocks, "gpu_launches": gpu_launches,
         }
@@ -864,7 +898,11 @@ def main():
                     help="also the same A/B at dt = 1/omega_pe")
     ap.add_argument("--graphs", type=int, default=1, help="particle step as a CUDA graph")
     ap.add_argument("--oracle-check", action="store_true",
-                    help="one full ECSIM step on the GPU and the FP64 oracle (AMR workloads)")
+                    help="run only the CPU baseline leg (one full ECSIM step on the GPU and "
+                         "the FP64 oracle, parity errors) on --parity-workload")
+    ap.add_argument("--parity-workload", default="amr_64c_32ppc",
+                    help="AMR workload of the CPU baseline leg: the headline mesh at 32 "
+                         "particles per species per base cell by default (16.8M particles)")
     ap.add_argument("--energy-steps", type=int, default=0,
                     help="also run this many full ECSIM steps and report the energy drift")
     ap.add_argument("--energy-precond", type=int, default=1, choices=(1, 2),
@@ -872,9 +910,9 @@ def main():
                          "(trained first on the run's own Jacobi solves)")
     ap.add_argument("--train-samples", type=int, default=20000,
                     help="block pairs harvested for the in-run training (--energy-precond 2)")
-    ap.add_argument("--tracer", type=int, default=0,
+    ap.add_argument("--tracer", type=int, default=16777216,
                     help="also run the cutoff tracing workload with this many particles (FP32; "
-                         "FP64 on 1/256 of them)")
+                         "FP64 on 1/256 of them); 0 = off")
     ap.add_argument("--restart", type=int, default=1,
                     help="also time the restart particle section write/read and checksum")
     ap.add_argument("--precond-kernel", type=int, default=0,
@@ -886,7 +924,8 @@ def main():
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.oracle_check:
-        print(json.dumps({"oracle_check": oracle_check(args.workload, 0)}), flush=True)
+        cpu, parity = cpu_leg(args.parity_workload, 0)
+        print(json.dumps({"cpu_baseline": cpu, "parity": parity}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args)
