@@ -1,8 +1,8 @@
 // Device code shared by the particle kernels (particles.cu) and the
 // no-allocation deposition entry point (noalloc.cu): species constants, the
-// bulk-copy staging of block stencils, the per-particle deposition record,
-// the register-tile accumulation with Kahan-compensated chunk sums, and
-// FP32 -> FP64 widening.
+// bulk-copy staging of block stencils, the per-particle deposition fields,
+// the register-tile accumulation (packed FP32x2 FMAs) with Kahan-compensated
+// chunk sums, and FP32 -> FP64 widening.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -13,10 +13,19 @@
 
 namespace {
 constexpr uint32_t kWaitLimit = 1u << 24;
-// floats per staged particle record: 64 used; the stride of 68 (272 B) puts the
-// records of 8 consecutive lanes in distinct 16-byte bank groups, so a warp's
-// 16-byte record stores run without bank conflicts
-constexpr int kRec = 68;
+// Staged deposition fields, a structure of arrays per warp: field f of the
+// record at position p is rec[f * FS + p].  A chunk stages one record per
+// lane (position = lane); particles that do not deposit stage zero weight.
+//   0..26  the 27 trilinear weight monomials X_x[a] X_y[b] X_z[c], a + 3b + 9c
+//   27..35 k alpha, row-major 3x3, k = q W h / V
+//   36..43 the 8 corner weights
+//   44     zero (pads the last current lane's third weight)
+//   45..47 q W alpha v
+// FS is the positions per field plus 4, so the 16-byte loads of 4 positions
+// of different fields spread over the banks and the per-lane stores of one
+// field are conflict-free.
+constexpr int kFields = 48;
+constexpr int kFS = 36;       // 32-position chunks (push/deposit, full deposit)
 constexpr int kTileLanes = 30;  // lanes owning a 3 x 3 output tile
 constexpr int kWarps = 8;     // warps per CTA (one row of 8 cells each)
 constexpr uint8_t kHole = 0xFF;
@@ -98,11 +107,15 @@ __host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
   return cid * 24 + ce;
 }
 
-// Record of one particle at block-local offset u inside cell (i,j,k); adds
-// its kinetic energy to en.
-__device__ __forceinline__ void stage_record(float* __restrict__ r, const float4* __restrict__ sB,
-                                             float u0, float u1, float u2, float v0, float v1,
-                                             float v2, int s, float wcorr, int i, int j, int k,
+// The fields of one particle at block-local offset u inside cell (i,j,k), at
+// record position pos; wq = q weight correction of a depositing particle, 0
+// for a lane that deposits nothing (its k alpha and q alpha v, hence all its
+// products, are zero).  Adds its kinetic energy (weighted by wq) to en.
+template <int FS>
+__device__ __forceinline__ void stage_fields(float* __restrict__ rec, int pos,
+                                             const float4* __restrict__ sB, float u0, float u1,
+                                             float u2, float v0, float v1, float v2, int s,
+                                             float wq, int i, int j, int k,
                                              const SpeciesTab& st, float inv_vol, FF& en) {
   const float fx = fminf(fmaxf(u0 - (float)i, 0.f), 1.f);
   const float fy = fminf(fmaxf(u1 - (float)j, 0.f), 1.f);
@@ -135,71 +148,84 @@ __device__ __forceinline__ void stage_record(float* __restrict__ r, const float4
   al[6] = c0 * (-P1 + h2 * B2 * B0);
   al[7] = c0 * (P0 + h2 * B2 * B1);
   al[8] = c0 * (1.f + h2 * B2 * B2);
-  const float qW = st.qw[s] * wcorr;
+  const float qW = st.qw[s] * wq;
   const float kc = qW * h * inv_vol;
-  float4* r4 = reinterpret_cast<float4*>(r);
+  float* r = rec + pos;
   {
-    // 27 weight monomials in groups of 3 (+1 pad): record floats 0..35
     const float X[3] = {gx * gx, gx * fx, fx * fx};
     const float Y[3] = {gy * gy, gy * fy, fy * fy};
     const float Z[3] = {gz * gz, gz * fz, fz * fz};
-    float m[27];
 #pragma unroll
     for (int c = 0; c < 3; c++)
 #pragma unroll
       for (int b = 0; b < 3; b++) {
         const float yz = Y[b] * Z[c];
 #pragma unroll
-        for (int a = 0; a < 3; a++) m[a + 3 * b + 9 * c] = X[a] * yz;
+        for (int a = 0; a < 3; a++) r[(a + 3 * b + 9 * c) * FS] = X[a] * yz;
       }
-#pragma unroll
-    for (int g = 0; g < 9; g++) r4[g] = make_float4(m[3 * g], m[3 * g + 1], m[3 * g + 2], 0.f);
   }
-  // k alpha rows (36..47), corner weights in groups of 3 (48..59), q W alpha v (60..63)
-  r4[9] = make_float4(kc * al[0], kc * al[1], kc * al[2], 0.f);
-  r4[10] = make_float4(kc * al[3], kc * al[4], kc * al[5], 0.f);
-  r4[11] = make_float4(kc * al[6], kc * al[7], kc * al[8], 0.f);
-  r4[12] = make_float4(w[0], w[1], w[2], 0.f);
-  r4[13] = make_float4(w[3], w[4], w[5], 0.f);
-  r4[14] = make_float4(w[6], w[7], 0.f, 0.f);
+#pragma unroll
+  for (int e = 0; e < 9; e++) r[(27 + e) * FS] = kc * al[e];
+#pragma unroll
+  for (int c = 0; c < 8; c++) r[(36 + c) * FS] = w[c];
+  r[44 * FS] = 0.f;
   const float vr0 = al[0] * v0 + al[1] * v1 + al[2] * v2;
   const float vr1 = al[3] * v0 + al[4] * v1 + al[5] * v2;
   const float vr2 = al[6] * v0 + al[7] * v1 + al[8] * v2;
-  r4[15] = make_float4(qW * vr0, qW * vr1, qW * vr2, 0.f);
-  kinetic_energy(en, v0, v1, v2, wcorr, s, st);
+  r[45 * FS] = qW * vr0;
+  r[46 * FS] = qW * vr1;
+  r[47 * FS] = qW * vr2;
+  kinetic_energy(en, v0, v1, v2, wq, s, st);
+}
+
+// d += a * b on packed FP32 pairs (two independent FMAs per instruction)
+__device__ __forceinline__ void ffma2(unsigned long long& d, unsigned long long a,
+                                      unsigned long long b) {
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(d) : "l"(a), "l"(b));
 }
 
 // Each of the first kTileLanes lanes owns a 3 x 3 tile: lanes 0..26 the
 // products (monomials 3g..3g+2) x (k alpha row hh), lanes 27..29 the products
-// (corner weights 3g'..3g'+2) x (q W alpha v).  A record costs every lane two
-// 16-byte shared loads and 9 FMAs.
+// (corner weights 3g'..3g'+2) x (q W alpha v); lanes 30, 31 repeat lane 27's
+// loads and discard the result.  Four records cost every lane six 16-byte
+// shared loads (4 positions of each of its 3 + 3 fields) and 18 packed FMAs,
+// the even and odd positions accumulated in the two halves of each pair.
 struct Tile {
   float sum[9], cmp[9];
   __device__ __forceinline__ void zero() {
 #pragma unroll
     for (int e = 0; e < 9; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
   }
-  // accumulate the cnt staged records of the warp, then compensated add
-  __device__ __forceinline__ void accumulate(const float* __restrict__ rec, int cnt, int offA,
-                                             int offB) {
-    float acc[9];
+  // accumulate the staged positions [0, npos) (npos a multiple of 4), then
+  // compensated add
+  template <int FS>
+  __device__ __forceinline__ void accumulate(const float* __restrict__ rec, int npos, int fA,
+                                             int fB) {
+    unsigned long long acc[9];
 #pragma unroll
-    for (int e = 0; e < 9; e++) acc[e] = 0.f;
-#pragma unroll 4
-    for (int r = 0; r < cnt; r++) {
-      const float4 A = *reinterpret_cast<const float4*>(rec + r * kRec + offA);
-      const float4 B = *reinterpret_cast<const float4*>(rec + r * kRec + offB);
-      const float av[3] = {A.x, A.y, A.z};
+    for (int e = 0; e < 9; e++) acc[e] = 0ull;
+    const float* pa = rec + fA * FS;
+    const float* pb = rec + fB * FS;
+#pragma unroll 2
+    for (int r = 0; r < npos; r += 4) {
+      ulonglong2 A[3], B[3];
 #pragma unroll
       for (int q = 0; q < 3; q++) {
-        acc[3 * q + 0] = fmaf(av[q], B.x, acc[3 * q + 0]);
-        acc[3 * q + 1] = fmaf(av[q], B.y, acc[3 * q + 1]);
-        acc[3 * q + 2] = fmaf(av[q], B.z, acc[3 * q + 2]);
+        A[q] = *reinterpret_cast<const ulonglong2*>(pa + q * FS + r);
+        B[q] = *reinterpret_cast<const ulonglong2*>(pb + q * FS + r);
       }
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+          ffma2(acc[3 * q + e], A[q].x, B[e].x);
+          ffma2(acc[3 * q + e], A[q].y, B[e].y);
+        }
     }
 #pragma unroll
     for (int e = 0; e < 9; e++) {
-      const float y = acc[e] - cmp[e];
+      const float2 a = *reinterpret_cast<const float2*>(&acc[e]);
+      const float y = (a.x + a.y) - cmp[e];
       const float t = sum[e] + y;
       cmp[e] = (t - sum[e]) - y;
       sum[e] = t;
@@ -279,13 +305,14 @@ struct Tile {
   }
 };
 
-__device__ __forceinline__ void lane_offsets(int lane, int& offA, int& offB) {
+// the first A field and the first B field of this lane's tile
+__device__ __forceinline__ void lane_fields(int lane, int& fA, int& fB) {
   if (lane < 27) {
-    offA = 4 * (lane / 3);
-    offB = 36 + 4 * (lane % 3);
+    fA = 3 * (lane / 3);
+    fB = 27 + 3 * (lane % 3);
   } else {
-    offA = lane < kTileLanes ? 48 + 4 * (lane - 27) : 0;
-    offB = 60;
+    fA = 36 + 3 * (lane < kTileLanes ? lane - 27 : 0);
+    fB = 45;
   }
 }
 

@@ -138,9 +138,9 @@ __global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
     if (threadIdx.x == 0) *a.energy = __longlong_as_double(0x7ff8000000000000LL);
     return;
   }
-  float* rec = s_rec + wid * 32 * kRec;
-  int offA, offB;
-  lane_offsets(lane, offA, offB);
+  float* rec = s_rec + wid * kFields * kFS;
+  int fA, fB;
+  lane_fields(lane, fA, fB);
   FF en{0.f, 0.f};
   const int j = wid;
   for (int i = 0; i < AMPS_NC; i++) {
@@ -150,11 +150,19 @@ __global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
     tile.zero();
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const long long p = b0 + q0 + lane;
-      if (q0 + lane < n0)
-        stage_record(rec + lane * kRec, s_dep, a.u[p], a.u[a.n + p], a.u[2 * a.n + p], a.v[p],
-                     a.v[a.n + p], a.v[2 * a.n + p], a.sp[p], 1.0f, i, j, k, a.st, a.inv_vol, en);
+      const bool act = q0 + lane < n0;
+      // positions past the cell's particles stage zero weight at the cell centre
+      float u[3] = {i + 0.5f, j + 0.5f, k + 0.5f}, v[3] = {0.f, 0.f, 0.f};
+      int s = 0;
+      if (act) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) { u[d] = a.u[d * a.n + p]; v[d] = a.v[d * a.n + p]; }
+        s = a.sp[p];
+      }
+      stage_fields<kFS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, act ? 1.0f : 0.f,
+                        i, j, k, a.st, a.inv_vol, en);
       __syncwarp();
-      if (lane < kTileLanes) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
+      tile.accumulate<kFS>(rec, (min(32, n0 - q0) + 3) & ~3, fA, fB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
@@ -215,7 +223,7 @@ cudaError_t setup_device(int dev, unsigned char** out) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_deposit_scratch);
     if (e != cudaSuccess) return e;
-    const int smem = (int)(AMPS_SC * sizeof(float4) + kNaWarps * 32 * kRec * sizeof(float));
+    const int smem = (int)(AMPS_SC * sizeof(float4) + kNaWarps * kFields * kFS * sizeof(float));
     e = cudaFuncSetAttribute(k_na_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = static_cast<unsigned char*>(p);
@@ -277,7 +285,7 @@ amps_gpu_status deposit_noalloc(const amps_gpu_config* cfg, long long n, const i
     a.st.keh[q] = (float)ke;
     a.st.kel[q] = (float)(ke - (double)a.st.keh[q]);
   }
-  const size_t smem = AMPS_SC * sizeof(float4) + kNaWarps * 32 * kRec * sizeof(float);
+  const size_t smem = AMPS_SC * sizeof(float4) + kNaWarps * kFields * kFS * sizeof(float);
   k_na_deposit<<<dim3((unsigned)nb, AMPS_NC), kNaWarps * 32, smem, s>>>(a);
   const double inv_vol = 1.0 / (cfg->dx[0] * cfg->dx[1] * cfg->dx[2]);
   k_na_assemble<<<(unsigned)((ncor + 255) / 256), 256, 0, s>>>(m, ncor, cellM, cellJ, inv_vol,

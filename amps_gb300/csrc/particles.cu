@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
   float4* s_push = s_dyn;                         // 729 x 2 float4
   float4* s_dep = s_dyn + 2 * AMPS_SC;            // 729 float4
-  float* s_rec = reinterpret_cast<float*>(s_dyn + 3 * AMPS_SC);  // kWarps x 32 x kRec
+  float* s_rec = reinterpret_cast<float*>(s_dyn + 3 * AMPS_SC);  // kWarps x kFields x kFS
   __shared__ __align__(8) uint64_t bar;
   __shared__ double s_en[kWarps];
   const int b = blockIdx.x, k = blockIdx.y;
@@ -217,9 +217,9 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   if (!stage_stencils(&bar, s_push, a.st_push + (size_t)b * AMPS_SC * AMPS_PUSH_STRIDE, bp, s_dep,
                       a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE, bd, a.flags))
     return;
-  float* rec = s_rec + wid * 32 * kRec;
-  int offA, offB;
-  lane_offsets(lane, offA, offB);
+  float* rec = s_rec + wid * kFields * kFS;
+  int fA, fB;
+  lane_fields(lane, fA, fB);
   FF en_row{0.f, 0.f};  // float pair across the row's cells, FP64 in the CTA reduction
   unsigned long long n_far = 0, n_near = 0, n_del = 0;
   const int j = wid;
@@ -346,10 +346,12 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
           if (a.p.wc) a.p.wc[d] = wcv;
           if (a.p.id) a.p.id[d] = idv;
         }
-        if (DEP)
-          stage_record(rec + spos * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv, i, j,
-                       k, a.st, inv_vol, en_row);
       }
+      // every lane stages its position; only stayers carry weight (movers are
+      // deposited by k_arrivals in their destination cell)
+      if (DEP)
+        stage_fields<kFS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], act ? s : 0,
+                          stays ? wcv : 0.f, i, j, k, a.st, inv_vol, en_row);
       // movers: slack of the destination cell, else the overflow list
       const bool mover = act && !stays && key >= 0;
       const int slot = warp_reserve(mover, mover ? key : 0, a.arr);
@@ -379,7 +381,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
       const int cst = __popc(smask);
       if (DEP) {
         __syncwarp();
-        if (lane < kTileLanes && cst > 0) tile.accumulate(rec, cst, offA, offB);
+        if (cst > 0) tile.accumulate<kFS>(rec, (min(32, n0 - q0) + 3) & ~3, fA, fB);
         __syncwarp();
       }
       nst += cst;
@@ -625,6 +627,7 @@ __global__ void k_step_bump(unsigned long long* step, const unsigned long long* 
 // in chunks of kArrChunk lanes: a smaller record buffer and a register cap let
 // 3 CTAs share an SM, which hides more of the per-cell load latency.
 constexpr int kArrChunk = 16;
+constexpr int kFSArr = kArrChunk + 4;  // field stride of the arrivals' staged fields
 
 template <bool DEP>
 __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
@@ -640,9 +643,9 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
                         AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0, a.flags))
       return;
   }
-  float* rec = s_rec + wid * kArrChunk * kRec;
-  int offA, offB;
-  lane_offsets(lane, offA, offB);
+  float* rec = s_rec + wid * kFields * kFSArr;
+  int fA, fB;
+  lane_fields(lane, fA, fB);
   FF en_row{0.f, 0.f};  // the row's arrivals, as a float pair before the FP64 reduction
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
@@ -689,14 +692,14 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
           a.p.sp[pd] = (uint8_t)s;
           if (a.p.wc) a.p.wc[pd] = wcv;
           if (a.p.id) a.p.id[pd] = idv;
-          if (DEP)
-            stage_record(rec + lane * kRec, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wcv, i, j,
-                         k, a.st, inv_vol, en_row);
         }
         if (DEP) {
+          // positions past the chunk's arrivals stage zero weight
+          if (lane < kArrChunk)
+            stage_fields<kFSArr>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+                                 act ? wcv : 0.f, i, j, k, a.st, inv_vol, en_row);
           __syncwarp();
-          const int cnt = min(kArrChunk, na - q0);
-          if (lane < kTileLanes) tile.accumulate(rec, cnt, offA, offB);
+          tile.accumulate<kFSArr>(rec, (min(kArrChunk, na - q0) + 3) & ~3, fA, fB);
           __syncwarp();
         }
       }
@@ -729,9 +732,9 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
   if (!stage_stencils(&bar, s_dep, a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE,
                       AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0, a.flags))
     return;
-  float* rec = s_rec + wid * 32 * kRec;
-  int offA, offB;
-  lane_offsets(lane, offA, offB);
+  float* rec = s_rec + wid * kFields * kFS;
+  int fA, fB;
+  lane_fields(lane, fA, fB);
   FF en{0.f, 0.f};
   const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
@@ -742,12 +745,20 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
     tile.zero();
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const long long p = b0 + q0 + lane;
-      if (q0 + lane < n0)
-        stage_record(rec + lane * kRec, s_dep, a.p.u[0][p], a.p.u[1][p], a.p.u[2][p], a.p.v[0][p],
-                     a.p.v[1][p], a.p.v[2][p], a.p.sp[p], a.p.wc ? a.p.wc[p] : 1.0f, i, j, k, a.st,
-                     inv_vol, en);
+      const bool act = q0 + lane < n0;
+      // positions past the cell's particles stage zero weight at the cell centre
+      float u[3] = {i + 0.5f, j + 0.5f, k + 0.5f}, v[3] = {0.f, 0.f, 0.f}, wq = 0.f;
+      int s = 0;
+      if (act) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) { u[d] = a.p.u[d][p]; v[d] = a.p.v[d][p]; }
+        s = a.p.sp[p];
+        wq = a.p.wc ? a.p.wc[p] : 1.0f;
+      }
+      stage_fields<kFS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wq, i, j, k,
+                        a.st, inv_vol, en);
       __syncwarp();
-      if (lane < kTileLanes) tile.accumulate(rec, min(32, n0 - q0), offA, offB);
+      tile.accumulate<kFS>(rec, (min(32, n0 - q0) + 3) & ~3, fA, fB);
       __syncwarp();
     }
     tile.flush(lane, a.cellM, a.cellJ, cid, false);
@@ -1574,10 +1585,10 @@ StepArgs step_args(amps_gpu_ctx* c) {
 }
 
 size_t smem_push(bool dep) {
-  return (size_t)AMPS_SC * (2 + 1) * sizeof(float4) + (dep ? kWarps * 32 * kRec * sizeof(float) : 0);
+  return (size_t)AMPS_SC * (2 + 1) * sizeof(float4) + (dep ? kWarps * kFields * kFS * sizeof(float) : 0);
 }
-size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * 32 * kRec * sizeof(float); }
-size_t smem_arr() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * kArrChunk * kRec * sizeof(float); }
+size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * kFields * kFS * sizeof(float); }
+size_t smem_arr() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * kFields * kFSArr * sizeof(float); }
 
 void set_smem_attrs() {
   static bool done = false;
