@@ -875,12 +875,10 @@ amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* c, const double* J, const 
 
 amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* c, double* J, double* M) {
   if (!c) return AMPS_GPU_INVALID_ARG;
-  if (c->amr)
-    return set_err(c, AMPS_GPU_INVALID_ARG,
-                   "export_moments: AMR contexts keep per-cell moments (export_cell_moments)");
   cudaSetDevice(c->cfg.device);
   amps_gpu_status s = cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
   if (s) return s;
+  if (c->amr) return amr_export_corner_moments(c, J, M);
   s = download_vec3(c, c->d_J, J, c->ncor);
   if (s) return s;
   if ((s = layout_download(c, c->d_M, M, c->ncor, 243, true))) return s;

@@ -207,6 +207,8 @@ struct amps_gpu_ctx {
   bool spec_on = false;
   float* d_cellS = nullptr;     // [ncor][nspec][10][8] per-cell partials
   double* d_specC = nullptr;    // [10*nspec][nvc] corner values
+  double* d_amrJ = nullptr;     // AMR corner-layout moments (export_moments)
+  double* d_amrM = nullptr;
   int* d_spec_start = nullptr;  // corner -> (cell*8 + corner-of-cell) CSR
   int* d_spec_ent = nullptr;
 
@@ -258,6 +260,7 @@ cudaError_t place_ranked(amps_gpu_ctx* c, long long n);
 // species moments on corners (species.cu)
 amps_gpu_status species_setup(amps_gpu_ctx* c, bool on);
 void species_free(amps_gpu_ctx* c);
+amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M);
 cudaError_t launch_species_moments(amps_gpu_ctx* c);
 cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,

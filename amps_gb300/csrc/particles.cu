@@ -214,6 +214,35 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t bp = AMPS_SC * AMPS_PUSH_STRIDE * sizeof(float);
   const uint32_t bd = DEP ? AMPS_SC * AMPS_DEP_STRIDE * sizeof(float) : 0;
+  const int j = wid;
+  // slot range and occupancy of the row's 8 cells, one lane per cell
+  int mb0 = 0, mn0 = 0;
+  if (lane < AMPS_NC) {
+    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
+    mb0 = a.base[cl];
+    mn0 = a.cnt[cl];
+  }
+  // software pipeline over the row's chunks: the next chunk's particles (the
+  // next 32 of this cell, or the first 32 of the next cell) are loaded while
+  // this one is processed; its slots lie above every slot this chunk writes
+  float pu[3] = {0.f, 0.f, 0.f}, pv[3] = {0.f, 0.f, 0.f};
+  int ps = 0;
+  float pwc = 1.0f;
+  uint32_t pid = 0;
+  int pf_cell = 0;  // cell whose chunk the prefetch registers hold
+  auto prefetch = [&](int c, int q) {
+    const int cb = __shfl_sync(0xffffffffu, mb0, c), cn = __shfl_sync(0xffffffffu, mn0, c);
+    pf_cell = c;
+    if (q < cn) {
+      const int pn = cb + q;
+#pragma unroll
+      for (int d = 0; d < 3; d++) { pu[d] = a.p.u[d][pn]; pv[d] = a.p.v[d][pn]; }
+      ps = a.p.sp[pn];
+      pwc = a.p.wc ? a.p.wc[pn] : 1.0f;
+      pid = a.p.id ? a.p.id[pn] : 0u;
+    }
+  };
+  prefetch(0, lane);  // in flight while the stencils are staged
   if (!stage_stencils(&bar, s_push, a.st_push + (size_t)b * AMPS_SC * AMPS_PUSH_STRIDE, bp, s_dep,
                       a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE, bd, a.flags))
     return;
@@ -222,39 +251,15 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   lane_fields(lane, fA, fB);
   FF en_row{0.f, 0.f};  // float pair across the row's cells, FP64 in the CTA reduction
   unsigned long long n_far = 0, n_near = 0, n_del = 0;
-  const int j = wid;
   const float inv_vol = block_inv_vol(a, b);
   const float bdtdx = AMR ? __ldg(a.amr.bdtdx + b) : 0.0f;
-  // slot range and occupancy of the row's 8 cells, one lane per cell
-  int mb0 = 0, mn0 = 0;
-  if (lane < AMPS_NC) {
-    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
-    mb0 = a.base[cl];
-    mn0 = a.cnt[cl];
-  }
   for (int i = 0; i < AMPS_NC; i++) {
     const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
     const int b0 = __shfl_sync(0xffffffffu, mb0, i), n0 = __shfl_sync(0xffffffffu, mn0, i);
     Tile tile;
     tile.zero();
     int nst = 0;
-    // software pipeline: the next chunk's particles are loaded while this one
-    // is processed (its slots lie above every slot this chunk writes)
-    float pu[3] = {0.f, 0.f, 0.f}, pv[3] = {0.f, 0.f, 0.f};
-    int ps = 0;
-    float pwc = 1.0f;
-    uint32_t pid = 0;
-    auto prefetch = [&](int q) {
-      if (q < n0) {
-        const int pn = b0 + q;
-#pragma unroll
-        for (int d = 0; d < 3; d++) { pu[d] = a.p.u[d][pn]; pv[d] = a.p.v[d][pn]; }
-        ps = a.p.sp[pn];
-        pwc = a.p.wc ? a.p.wc[pn] : 1.0f;
-        pid = a.p.id ? a.p.id[pn] : 0u;
-      }
-    };
-    prefetch(lane);
+    if (pf_cell != i) prefetch(i, lane);  // the previous cell was empty
     for (int q0 = 0; q0 < n0; q0 += 32) {
       const int p = b0 + q0 + lane;
       const bool act = q0 + lane < n0;
@@ -262,7 +267,10 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
       int s = ps, key = -1;
       float wcv = pwc;
       uint32_t idv = pid;
-      prefetch(q0 + 32 + lane);
+      if (q0 + 32 < n0)
+        prefetch(i, q0 + 32 + lane);
+      else if (i + 1 < AMPS_NC)
+        prefetch(i + 1, lane);
       if (act) {
         // gather E^{n+theta}, B^n at the old position
         int ic[3];

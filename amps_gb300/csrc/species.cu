@@ -139,52 +139,69 @@ __global__ void __launch_bounds__(256) k_species_gather(long long nvc, int nspec
 
 }  // namespace
 
-// Corner -> (cell, corner-of-cell) lists.  Corner (i, j, k) of block b's cell
-// grid (0..8 per axis) is the uniform lattice corner there (periodic), or the
-// AMR mesh's unique corner from the block's corner table.
+// Corner -> (cell, corner-of-cell) lists, built once per context.  Corner
+// (i, j, k) of block b's cell grid (0..8 per axis) is the uniform lattice
+// corner there (periodic), or the AMR mesh's unique corner from the block's
+// corner table.  Entry = cell * 8 + q, q the corner's binary offset
+// (q & 1, (q >> 1) & 1, q >> 2) in the cell.
+amps_gpu_status corner_csr_setup(amps_gpu_ctx* c) {
+  if (c->d_spec_start) return AMPS_GPU_OK;
+  const long long nv = c->nvc;
+  std::vector<int> ctab;
+  if (c->amr) {
+    ctab.resize((size_t)c->nb * 729);
+    cudaError_t e = cudaMemcpy(ctab.data(), c->d_ctab, sizeof(int) * ctab.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_check(c, e, "corner lists: corner table");
+  }
+  const int nbx = c->cfg.nbx, nby = c->cfg.nby, nbz = c->cfg.nbz;
+  const int NX = 8 * nbx, NY = 8 * nby, NZ = 8 * nbz;
+  auto corner = [&](int b, int ci, int cj, int ck) -> int {
+    if (c->amr) return ctab[(size_t)b * 729 + ci + 9 * (cj + 9 * ck)];
+    const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    const int I = (8 * bx + ci) % NX, J = (8 * by + cj) % NY, K = (8 * bz + ck) % NZ;
+    return ((I >> 3) + nbx * ((J >> 3) + nby * (K >> 3))) * AMPS_CPB + (I & 7) + 8 * ((J & 7) + 8 * (K & 7));
+  };
+  std::vector<int> count((size_t)nv + 1, 0);
+  for (int b = 0; b < c->nb; b++)
+    for (int l = 0; l < AMPS_CPB; l++)
+      for (int q = 0; q < 8; q++)
+        count[(size_t)corner(b, (l & 7) + (q & 1), ((l >> 3) & 7) + ((q >> 1) & 1), (l >> 6) + (q >> 2)) + 1]++;
+  for (long long i = 0; i < nv; i++) count[(size_t)i + 1] += count[(size_t)i];
+  std::vector<int> ent((size_t)count[(size_t)nv]), fill(count.begin(), count.end() - 1);
+  for (int b = 0; b < c->nb; b++)
+    for (int l = 0; l < AMPS_CPB; l++)
+      for (int q = 0; q < 8; q++) {
+        const int cc = corner(b, (l & 7) + (q & 1), ((l >> 3) & 7) + ((q >> 1) & 1), (l >> 6) + (q >> 2));
+        ent[(size_t)fill[(size_t)cc]++] = (int)(((long long)b * AMPS_CPB + l) * 8 + q);
+      }
+  bool ok = cudaMalloc(reinterpret_cast<void**>(&c->d_spec_start), sizeof(int) * count.size()) == cudaSuccess &&
+            cudaMalloc(reinterpret_cast<void**>(&c->d_spec_ent), sizeof(int) * std::max<size_t>(ent.size(), 1)) == cudaSuccess;
+  ok = ok && cudaMemcpy(c->d_spec_start, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+       cudaMemcpy(c->d_spec_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    cudaFree(c->d_spec_start);
+    cudaFree(c->d_spec_ent);
+    c->d_spec_start = c->d_spec_ent = nullptr;
+    return set_err(c, AMPS_GPU_CUDA_ERROR, "corner lists: allocation failed");
+  }
+  return AMPS_GPU_OK;
+}
+
 amps_gpu_status species_setup(amps_gpu_ctx* c, bool on) {
   if (!on) {
     c->spec_on = false;
     return AMPS_GPU_OK;
   }
+  amps_gpu_status st = corner_csr_setup(c);
+  if (st) return st;
   if (!c->d_cellS) {
     const long long nv = c->nvc;
-    std::vector<int> ctab;
-    if (c->amr) {
-      ctab.resize((size_t)c->nb * 729);
-      cudaError_t e = cudaMemcpy(ctab.data(), c->d_ctab, sizeof(int) * ctab.size(), cudaMemcpyDeviceToHost);
-      if (e != cudaSuccess) return cuda_check(c, e, "species moments: corner table");
-    }
-    const int nbx = c->cfg.nbx, nby = c->cfg.nby, nbz = c->cfg.nbz;
-    const int NX = 8 * nbx, NY = 8 * nby, NZ = 8 * nbz;
-    auto corner = [&](int b, int ci, int cj, int ck) -> int {
-      if (c->amr) return ctab[(size_t)b * 729 + ci + 9 * (cj + 9 * ck)];
-      const int bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
-      const int I = (8 * bx + ci) % NX, J = (8 * by + cj) % NY, K = (8 * bz + ck) % NZ;
-      return ((I >> 3) + nbx * ((J >> 3) + nby * (K >> 3))) * AMPS_CPB + (I & 7) + 8 * ((J & 7) + 8 * (K & 7));
-    };
-    std::vector<int> count((size_t)nv + 1, 0);
-    for (int b = 0; b < c->nb; b++)
-      for (int l = 0; l < AMPS_CPB; l++)
-        for (int q = 0; q < 8; q++)
-          count[(size_t)corner(b, (l & 7) + (q & 1), ((l >> 3) & 7) + ((q >> 1) & 1), (l >> 6) + (q >> 2)) + 1]++;
-    for (long long i = 0; i < nv; i++) count[(size_t)i + 1] += count[(size_t)i];
-    std::vector<int> ent((size_t)count[(size_t)nv]), fill(count.begin(), count.end() - 1);
-    for (int b = 0; b < c->nb; b++)
-      for (int l = 0; l < AMPS_CPB; l++)
-        for (int q = 0; q < 8; q++) {
-          const int cc = corner(b, (l & 7) + (q & 1), ((l >> 3) & 7) + ((q >> 1) & 1), (l >> 6) + (q >> 2));
-          ent[(size_t)fill[(size_t)cc]++] = (int)(((long long)b * AMPS_CPB + l) * 8 + q);
-        }
     bool ok = cudaMalloc(reinterpret_cast<void**>(&c->d_cellS),
                          sizeof(float) * (size_t)c->ncor * c->cfg.nspec * kV) == cudaSuccess &&
               cudaMalloc(reinterpret_cast<void**>(&c->d_specC),
-                         sizeof(double) * (size_t)nv * c->cfg.nspec * kQ) == cudaSuccess &&
-              cudaMalloc(reinterpret_cast<void**>(&c->d_spec_start), sizeof(int) * count.size()) == cudaSuccess &&
-              cudaMalloc(reinterpret_cast<void**>(&c->d_spec_ent), sizeof(int) * std::max<size_t>(ent.size(), 1)) == cudaSuccess;
-    ok = ok && cudaMemcpy(c->d_spec_start, count.data(), sizeof(int) * count.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(c->d_spec_ent, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemset(c->d_specC, 0, sizeof(double) * (size_t)nv * c->cfg.nspec * kQ) == cudaSuccess;
+                         sizeof(double) * (size_t)nv * c->cfg.nspec * kQ) == cudaSuccess;
+    ok = ok && cudaMemset(c->d_specC, 0, sizeof(double) * (size_t)nv * c->cfg.nspec * kQ) == cudaSuccess;
     if (!ok) {
       cudaGetLastError();
       species_free(c);
@@ -196,6 +213,9 @@ amps_gpu_status species_setup(amps_gpu_ctx* c, bool on) {
 }
 
 void species_free(amps_gpu_ctx* c) {
+  cudaFree(c->d_amrJ);
+  cudaFree(c->d_amrM);
+  c->d_amrJ = c->d_amrM = nullptr;
   cudaFree(c->d_cellS);
   cudaFree(c->d_specC);
   cudaFree(c->d_spec_start);
@@ -308,6 +328,88 @@ __global__ void __launch_bounds__(256) k_particle_cfl(CflArgs a) {
       }
     }
   }
+}
+
+// AMR moments in the corner layout: what ProcessCell's flush
+// (pic_field_solver_ecsim.cpp:2362-2426) adds into the corner nodes, summed
+// over the cells (of any level) that have the corner -- J[corner][3] =
+// sum cellJ / V(cell), M[corner][27 slots][9] with slot(d) = dig(dx) +
+// 3 dig(dy) + 9 dig(dz), dig(0) = 0, dig(-1) = 1, dig(+1) = 2, d the partner
+// corner's offset in the cell (IndexMatrix, :1889-1891) and the block the
+// cell's partial of the pair's weight monomial (already divided by V).  One
+// thread per (corner, output element); hanging corners get their own sums.
+__global__ void __launch_bounds__(256) k_amr_corner_moments(
+    long long nvc, const int* __restrict__ start, const int* __restrict__ ent,
+    const float* __restrict__ cellM, const float* __restrict__ cellJ, const double* __restrict__ bdx,
+    double* __restrict__ J, double* __restrict__ M) {
+  const long long total = nvc * 246;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long cc = t / 246;
+    const int el = (int)(t % 246);
+    double sum = 0.0;
+    if (el < 243) {
+      const int slot = el / 9, comp = el % 9;
+      const int dg[3] = {slot % 3, (slot / 3) % 3, slot / 9};
+      int d[3];
+#pragma unroll
+      for (int a = 0; a < 3; a++) d[a] = dg[a] == 0 ? 0 : (dg[a] == 1 ? -1 : 1);
+      for (int e = start[cc]; e < start[cc + 1]; e++) {
+        const int en = ent[e];
+        const long long cell = en >> 3;
+        const int q = en & 7;
+        const int o[3] = {(q & 1) + d[0], ((q >> 1) & 1) + d[1], (q >> 2) + d[2]};
+        if (o[0] < 0 || o[0] > 1 || o[1] < 0 || o[1] > 1 || o[2] < 0 || o[2] > 1) continue;
+        const int q2 = o[0] + 2 * o[1] + 4 * o[2];
+        // binary offset -> table order of ProcessCell's corners
+        const int t1 = q ^ ((q >> 1) & 1), t2 = q2 ^ ((q2 >> 1) & 1);
+        sum += (double)cellM[cellM_at(cell, pair_monomial(t1, t2) * 9 + comp)];
+      }
+      M[cc * 243 + el] = sum;
+    } else {
+      const int comp = el - 243;
+      for (int e = start[cc]; e < start[cc + 1]; e++) {
+        const int en = ent[e];
+        const long long cell = en >> 3;
+        const int q = en & 7;
+        const double dx = bdx[cell / AMPS_CPB];
+        sum += (double)cellJ[cellJ_at(cell, (q ^ ((q >> 1) & 1)) * 3 + comp)] / (dx * dx * dx);
+      }
+      J[cc * 3 + comp] = sum;
+    }
+  }
+}
+
+// the corner-layout moments of an AMR context (k_amr_corner_moments) into
+// host J[nvc][3], M[nvc][243] (mesh corner numbering)
+amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M) {
+  amps_gpu_status st = corner_csr_setup(c);
+  if (st) return st;
+  if (!c->d_amrJ) {
+    if (cudaMalloc(reinterpret_cast<void**>(&c->d_amrJ), sizeof(double) * 3 * (size_t)c->nvc) != cudaSuccess ||
+        cudaMalloc(reinterpret_cast<void**>(&c->d_amrM), sizeof(double) * 243 * (size_t)c->nvc) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(c->d_amrJ);
+      c->d_amrJ = nullptr;
+      return set_err(c, AMPS_GPU_CUDA_ERROR, "export_moments: allocation failed");
+    }
+  }
+  {
+    TimedLaunch t(c, "amr_corner_moments");
+    const long long total = c->nvc * 246;
+    const long long blocks = std::min<long long>((total + 255) / 256, 152LL * 64);
+    k_amr_corner_moments<<<(unsigned)blocks, 256, 0, c->stream>>>(
+        c->nvc, c->d_spec_start, c->d_spec_ent, c->d_cellM, c->d_cellJ, c->d_bdx, c->d_amrJ,
+        c->d_amrM);
+  }
+  if ((st = cuda_check(c, cudaGetLastError(), "amr_corner_moments"))) return st;
+  if (J && (st = cuda_check(c, cudaMemcpyAsync(J, c->d_amrJ, sizeof(double) * 3 * (size_t)c->nvc,
+                                               cudaMemcpyDeviceToHost, c->stream), "J")))
+    return st;
+  if (M && (st = cuda_check(c, cudaMemcpyAsync(M, c->d_amrM, sizeof(double) * 243 * (size_t)c->nvc,
+                                               cudaMemcpyDeviceToHost, c->stream), "M")))
+    return st;
+  return cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
 }
 
 extern "C" {

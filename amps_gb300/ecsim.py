@@ -277,8 +277,10 @@ class EcsimContext:
                                                      ptr(M, C.c_double)), "import_moments")
 
     def export_moments(self, with_m=True, out=None):
-        """corner J (ncells, 3) and M (ncells, 243); out=(J, M) reuses arrays"""
-        nc = self.wl.mesh.ncells
+        """corner J (ncorners, 3) and M (ncorners, 243); out=(J, M) reuses arrays.
+        On AMR contexts the mesh's unique corners, each summing ProcessCell's
+        flush over the cells that have it."""
+        nc = self.ncorners
         if out is not None:
             J, M = out
         else:

@@ -193,8 +193,13 @@ amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* ctx, const double* E_n, con
 amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* ctx, double* E_n, double* E_half,
                                        double* B_center, double* B_corner_prev,
                                        double* B_corner_cur);
-/* J: 3 per corner, M: 243 per corner (global layout above).  Uniform meshes
- * only: AMR contexts return AMPS_GPU_INVALID_ARG. */
+/* J: 3 per corner, M: 243 per corner (global layout above).  Import: uniform
+ * meshes only (AMR contexts return AMPS_GPU_INVALID_ARG: their solve reads the
+ * per-cell blocks).  Export on AMR contexts: the same corner layout over the
+ * mesh's unique corners (J[corner][3], M[corner][243]), each corner the sum of
+ * ProcessCell's flush (pic_field_solver_ecsim.cpp:2362-2426) over the cells of
+ * any level that have it -- hanging corners included, with their own sums --
+ * so an AMR run can take J and M back into its corner nodes. */
 amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* ctx, const double* J, const double* M);
 amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* ctx, double* J, double* M);
 /* Per-cell pieces of ProcessCell (pic_field_solver_ecsim.cpp:1882-2438) before

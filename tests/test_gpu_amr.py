@@ -206,9 +206,55 @@ def test_amr_context_on_uniform_mesh_matches_uniform_context():
     assert sa.particle_energy == pytest.approx(su.particle_energy, rel=1e-6)
 
 
-def test_amr_rejects_corner_moments():
-    mesh = amr.uniform_mesh((1, 1, 1))
-    wl = A.electron_proton_plasma("u", 1, 1, 1, 2, 2)
-    with A.EcsimContext(wl, capacity=64, amr_mesh=mesh) as ca:
-        with pytest.raises(A.AmpsGpuError):
-            ca.export_moments()
+TABLE_OFF = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+
+
+def corner_sums(mesh, cellJ, cellM):
+    """ProcessCell's flush (pic_field_solver_ecsim.cpp:2362-2426) of per-cell
+    blocks (cellJ [cell][8 corners x 3], cellM [cell][36 pairs c2 <= c1][9])
+    into the mesh's unique corners, in numpy"""
+    nb = mesh.nblocks
+    ncell = nb * 512
+    l = np.arange(512)
+    ci, cj, ck = l % 8, (l // 8) % 8, l // 64
+    tab = mesh.corner_tab.reshape(nb, 729)
+    cor = np.stack([tab[:, (ci + o[0]) + 9 * ((cj + o[1]) + 9 * (ck + o[2]))].reshape(ncell)
+                    for o in TABLE_OFF], 1)                     # [cell][table corner]
+    inv_v = np.repeat(1.0 / mesh.block_dx() ** 3, 512)
+    J = np.zeros((mesh.ncorners, 3))
+    M = np.zeros((mesh.ncorners, 243))
+    cJ = cellJ.reshape(ncell, 8, 3)
+    cM = cellM.reshape(ncell, 36, 9)
+    dig = lambda d: 0 if d == 0 else (1 if d < 0 else 2)
+    slot = lambda a, b: sum(dig(TABLE_OFF[b][x] - TABLE_OFF[a][x]) * 3 ** x for x in range(3))
+    for c in range(8):
+        np.add.at(J, cor[:, c], cJ[:, c] * inv_v[:, None])
+    pr = 0
+    for c1 in range(8):
+        for c2 in range(c1 + 1):
+            s1 = slot(c1, c2)
+            np.add.at(M, (cor[:, c1][:, None], 9 * s1 + np.arange(9)[None, :]), cM[:, pr])
+            if c1 != c2:
+                s2 = slot(c2, c1)
+                np.add.at(M, (cor[:, c2][:, None], 9 * s2 + np.arange(9)[None, :]), cM[:, pr])
+            pr += 1
+    return J, M
+
+
+def test_amr_corner_moments_match_oracle():
+    """export_moments on an AMR context: the corner layout of the per-cell
+    blocks, against the same flush of the FP64 oracle's blocks"""
+    mesh, wl, ic, x, f = amr_case(ppc=8, seed=31)
+    with gpu_for(mesh, wl, ic, x, f) as ctx:
+        ctx.UpdateJMassMatrix()
+        J, M = ctx.export_moments()
+        gJ, gM = ctx.export_cell_moments()
+    ao = oracle_for(mesh, wl, ic, x, f)
+    ao.deposit()
+    rJ, rM = corner_sums(mesh, ao.cellJ, ao.cellM)
+    assert J.shape == (mesh.ncorners, 3) and M.shape == (mesh.ncorners, 243)
+    assert rel_err(J, rJ) <= 1e-5, rel_err(J, rJ)
+    assert rel_err(M, rM) <= 1e-5, rel_err(M, rM)
+    # the device's own per-cell blocks, flushed the same way, agree to rounding
+    sJ, sM = corner_sums(mesh, gJ, gM)
+    assert rel_err(J, sJ) <= 1e-12 and rel_err(M, sM) <= 1e-12
