@@ -221,11 +221,15 @@ AMR_WORKLOADS = {
     # than L2, small enough for full profiler captures)
     "amr_64c_32ppc": lambda: AmrWorkload("amr_64c_32ppc", (8, 8, 8), 1, 0, 0.5, 32),
     # three levels, 256^3 effective cells: level 2 inside a central sphere of
-    # radius 0.2 box lengths, level 1 inside radius 0.4 (4432 blocks, 2.27M
+    # radius 0.3 box lengths, level 1 inside radius 0.6 (8912 blocks, 4.56M
     # cells); 64 particles per species in every cell, weight corrections 8^-L
-    # (290,455,168 particles)
-    "amr_256e_3lvl": lambda: AmrWorkload("amr_256e_3lvl", (8, 8, 8), 2, 1, 0.4, 64, per_cell=True),
-    # the same mesh at 64 particles per species per base-cell volume (8 per
-    # level-1 cell, 1 per level-2 cell; 33.5M particles)
+    # (584,056,832 particles)
+    "amr_256e_3lvl": lambda: AmrWorkload("amr_256e_3lvl", (8, 8, 8), 2, 1, 0.6, 64, per_cell=True),
+    # level 2 inside radius 0.2, level 1 inside 0.4 (4432 blocks, 2.27M cells,
+    # 290,455,168 particles)
+    "amr_256e_3lvl_r02": lambda: AmrWorkload("amr_256e_3lvl_r02", (8, 8, 8), 2, 1, 0.4, 64,
+                                             per_cell=True),
+    # the radius-0.2 mesh at 64 particles per species per base-cell volume (8
+    # per level-1 cell, 1 per level-2 cell; 33.5M particles)
     "amr_256e_3lvl_sparse": lambda: AmrWorkload("amr_256e_3lvl_sparse", (8, 8, 8), 2, 1, 0.4, 64),
 }

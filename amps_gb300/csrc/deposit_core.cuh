@@ -303,6 +303,30 @@ struct Tile {
       }
     }
   }
+  // add this tile's sums to the cell partials by global reductions: no value
+  // comes back, so the warp does not wait on the read-modify-write, which the
+  // L2 performs
+  __device__ __forceinline__ void flush_red(int lane, float* __restrict__ cellM,
+                                            float* __restrict__ cellJ, long long cid) {
+    if (lane < 27) {
+      const int g = lane / 3, hh = lane % 3;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++)
+          atomicAdd(cellM + cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e), sum[3 * q + e] - cmp[3 * q + e]);
+    } else if (lane < kTileLanes) {
+      const int g = lane - 27;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const int corner = 3 * g + q;
+        if (corner < 8)
+#pragma unroll
+          for (int e = 0; e < 3; e++)
+            atomicAdd(cellJ + cellJ_at(cid, corner * 3 + e), sum[3 * q + e] - cmp[3 * q + e]);
+      }
+    }
+  }
 };
 
 // the first A field and the first B field of this lane's tile

@@ -676,8 +676,6 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     if (na > 0) {
       Tile tile;
       tile.zero();
-      float old[9];
-      if (DEP) tile.preload(lane, a.cellM, a.cellJ, cid, old);
       const int src0 = b0 + cap - na, dst0 = b0 + nst;
       for (int q0 = 0; q0 < na; q0 += kArrChunk) {
         const bool act = lane < kArrChunk && q0 + lane < na;
@@ -717,7 +715,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
         const int slot = src0 + t;
         if (slot >= dst0 + na) a.p.sp[slot] = kHole;
       }
-      if (DEP) tile.flush_onto(lane, a.cellM, a.cellJ, cid, old);
+      if (DEP) tile.flush_red(lane, a.cellM, a.cellJ, cid);
     }
   }
   if (lane < AMPS_NC) {

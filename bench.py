@@ -903,8 +903,9 @@ def main():
     ap.add_argument("--parity-workload", default="amr_64c_32ppc",
                     help="AMR workload of the CPU baseline leg: the headline mesh at 32 "
                          "particles per species per base cell by default (16.8M particles)")
-    ap.add_argument("--energy-steps", type=int, default=0,
-                    help="also run this many full ECSIM steps and report the energy drift")
+    ap.add_argument("--energy-steps", type=int, default=50,
+                    help="also run this many full ECSIM steps and report the energy drift "
+                         "(0 = off)")
     ap.add_argument("--energy-precond", type=int, default=1, choices=(1, 2),
                     help="preconditioner of those steps: 1 Jacobi, 2 the learned network "
                          "(trained first on the run's own Jacobi solves)")
