@@ -17,11 +17,11 @@ barrier and device synchronisation and timed with CUDA events on the library's
 stream; the max over ranks is reported.  N > 1 runs independent replicas (the
 path is not sharded), value = all ranks' particle-steps / max time.
 
---impl reference times the reference CPU path on the host cores: the
-reference's ECSIM sources need its generated build headers and do not compile
-standalone, so the FP64 restatement of Lapenta2017 + ProcessCell (oracle/) is
-timed instead, one replica of the same plasma per host thread (AMR workloads:
-the same mesh recipe at 32^3 base cells).
+--impl reference times the reference CPU path on the host cores: the FP64
+restatement of Lapenta2017 + re-binning + ProcessCell (oracle/, pinned to the
+reference's own ProcessCell and Lapenta2017 compiled from its sources) over
+every particle of the same workload on all host threads (uniform workloads:
+one replica of the plasma per host thread).
 """
 import argparse
 import ctypes as C
@@ -245,52 +245,6 @@ def cpu_replica_rate(wl_name, steps, seconds_budget, threads):
     n = rep.nparticles
     return sum(counts) / dt, {"replica_particles": n, "threads": threads, "seconds": dt,
                               "particle_steps": sum(counts)}
-
-
-def cpu_amr_replica_rate(seconds_budget, threads, ppc_base=32):
-    """FP64 AMR oracle (push with re-binning across levels + ProcessCell per
-    cell) on per-thread replicas of the AMR plasma: the same mesh recipe at
-    32^3 base cells (120 blocks).  Returns particle-steps/s over all threads."""
-    import amps_gb300 as A  # noqa: F401
-    from amps_gb300 import amr
-    from tests import oracle_amr as OA
-    wl = amr.AmrWorkload("cpu_replica", (4, 4, 4), 1, 0, 0.5, ppc_base)
-    mesh = wl.mesh()
-    f = amr.amr_initial_fields(mesh, wl.b0)
-    states = []
-    for t in range(threads):
-        ic = amr.amr_initial_condition(mesh, wl.species, ppc_base, seed=100 + 2 * t + 1)
-        bo, bd = mesh.block_origins(), mesh.block_dx()
-        x = bo[ic["block"]] + ic["u"].astype(np.float64) * bd[ic["block"]][:, None]
-        ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64),
-                          ic["spec"])
-        ao.E_half[:] = f["E_half"]
-        ao.Bprev[:] = f["B_corner_prev"]
-        ao.Bcur[:] = f["B_corner_cur"]
-        states.append(ao)
-    counts = [0] * threads
-    deadline = [None]
-
-    def work(i):
-        st = states[i]
-        while time.time() < deadline[0]:
-            st.push()
-            st.deposit()
-            counts[i] += len(st.spec)
-
-    deadline[0] = time.time() + seconds_budget
-    t0 = time.time()
-    th = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
-    for t in th:
-        t.start()
-    for t in th:
-        t.join()
-    dt = time.time() - t0
-    n = len(states[0].spec)
-    return sum(counts) / dt, {"replica_particles": n, "threads": threads, "seconds": dt,
-                              "particle_steps": sum(counts),
-                              "replica": "AMR mesh, 4^3 level-0 blocks, central 1/8 refined 2x, "
-                                         "%d ppc per species per base cell" % ppc_base}
 
 
 def setup_workload(name, device, track_ids=False):
@@ -846,33 +800,63 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def reference_amr_workload(name, threads, steps, warmup):
+    """The reference CPU path on the GPU arm's own AMR workload: the FP64 AMR
+    oracle (Lapenta2017 + re-binning + ProcessCell, pinned to the reference's
+    compiled ProcessCell/Lapenta2017) over every particle of the workload on
+    `threads` host threads, one push + deposit per step.  Returns the per-step
+    seconds of the timed steps and the particle count."""
+    from amps_gb300 import amr
+    from tests import oracle_amr as OA
+    wl = amr.AMR_WORKLOADS[name]()
+    mesh = wl.mesh()
+    ic = wl.initial_condition(mesh, seed=100, nthreads=threads)
+    x = mesh.block_origins()[ic["block"]] + ic["u"].astype(np.float64) * mesh.block_dx()[ic["block"]][:, None]
+    wc = None if ic["wcorr"] is None else ic["wcorr"].astype(np.float64)
+    ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64), ic["spec"],
+                      wcorr=wc)
+    f = amr.amr_initial_fields(mesh, wl.b0)
+    ao.Bprev[:] = f["B_corner_prev"]
+    ao.Bcur[:] = f["B_corner_cur"]
+    del ic, x
+    for _ in range(warmup):
+        ao.push_deposit_mt(threads)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ao.push_deposit_mt(threads)
+        times.append(time.perf_counter() - t0)
+    return times, len(ao.spec)
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
         return
     from amps_gb300 import amr
     threads = os.cpu_count() or 1
-    rates = []
-    is_amr = args.workload in amr.AMR_WORKLOADS
-    for _ in range(args.steps):
-        if is_amr:
-            r, info = cpu_amr_replica_rate(args.ref_seconds, threads)
-        else:
-            r, info = cpu_replica_rate(args.workload, 1, args.ref_seconds, threads)
-        rates.append(r)
-    value = float(np.mean(rates))
-    if is_amr:
-        sample = ("FP64 AMR oracle port of Lapenta2017 + re-binning across levels + ProcessCell, "
-                  "one replica per host thread (%s; %d threads, %d particles each), %g s per "
-                  "step" % (info["replica"], threads, info["replica_particles"], args.ref_seconds))
+    if args.workload in amr.AMR_WORKLOADS:
+        times, n = reference_amr_workload(args.workload, threads, args.steps, args.warmup)
+        value = n * len(times) / sum(times)
+        sample = ("FP64 AMR oracle (Lapenta2017 + re-binning across levels + ProcessCell, pinned to "
+                  "the reference's compiled ProcessCell/Lapenta2017) over all %d particles of %s "
+                  "on %d host threads (push over particle ranges, deposit over block ranges), "
+                  "%.2f s per step" % (n, args.workload, threads, sum(times) / len(times)))
+        same = True
     else:
+        rates = []
+        for _ in range(args.steps):
+            r, info = cpu_replica_rate(args.workload, 1, args.ref_seconds, threads)
+            rates.append(r)
+        value = float(np.mean(rates))
         sample = ("FP64 oracle port of Lapenta2017 + ProcessCell + re-binning, one periodic "
                   "8^3-cell replica of the same plasma per host thread (%d threads, %d particles "
                   "each), %g s per step" % (threads, info["replica_particles"], args.ref_seconds))
+        same = False
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload},
+            "config": {"workload": args.workload, "same_config": same},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,

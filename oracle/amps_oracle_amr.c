@@ -20,6 +20,7 @@
  * pinned by energy conservation, not by reference output.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -407,6 +408,41 @@ long orc_amr_inject(const orc_amr* g, int face, int spec, double density, const 
 
 /* per-cell partials (cellJ[ncell*24] = sum q W w_c alpha v; cellM[ncell*324] =
  * sum (q W qdt/2m / V) w_c1 w_c2 alpha over pairs c2<=c1).  Returns energy. */
+/* ProcessCell's per-particle terms (pic_field_solver_ecsim.cpp:2186-2342) of
+ * particle p added to its cell's blocks; returns its kinetic energy. */
+static double deposit_one(const orc_amr* g, long p, const double* x, const double* v,
+                          const uint8_t* spec, const double* wcorr, const int32_t* block,
+                          const int32_t* cell, const double* Bc_cur, double* cellJ, double* cellM) {
+  double w[8], B[3] = {0, 0, 0}, val[3];
+  int cid[8];
+  const int b = block[p];
+  stencil(g, b, x + 3 * p, w, cid);
+  for (int c = 0; c < 8; c++) {
+    corner_val(g, Bc_cur, cid[c], val);
+    for (int d = 0; d < 3; d++) B[d] += w[c] * val[d];
+  }
+  const double dx = bdx(g, b), V = dx * dx * dx;
+  const int s = spec[p];
+  const double W = g->w[s] * (wcorr ? wcorr[p] : 1.0);
+  const double qW = g->q[s] * W, mW = g->m[s] * W;
+  const double h = 0.5 * qW * g->dt / mW;
+  double al[9], vr[3] = {0, 0, 0};
+  alpha_matrix(h, B, al);
+  const double* vv = v + 3 * p;
+  const double e = 0.5 * mW * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) vr[i] += al[3 * i + j] * vv[j];
+  const long cl = (long)b * 512 + cell[p];
+  for (int c = 0; c < 8; c++)
+    for (int d = 0; d < 3; d++) cellJ[cl * 24 + 3 * c + d] += qW * w[c] * vr[d];
+  const double mc = qW * h / V;
+  int pr = 0;
+  for (int c1 = 0; c1 < 8; c1++)
+    for (int c2 = 0; c2 <= c1; c2++, pr++)
+      for (int ab = 0; ab < 9; ab++) cellM[cl * 324 + pr * 9 + ab] += mc * w[c1] * w[c2] * al[ab];
+  return e;
+}
+
 double orc_amr_deposit(const orc_amr* g, long n, const double* x, const double* v,
                        const uint8_t* spec, const double* wcorr, const int32_t* block,
                        const int32_t* cell, const double* Bc_cur, double* cellJ, double* cellM) {
@@ -416,35 +452,103 @@ double orc_amr_deposit(const orc_amr* g, long n, const double* x, const double* 
   double energy = 0.0;
   for (long p = 0; p < n; p++) {
     if (block[p] < 0) continue;
-    double w[8], B[3] = {0, 0, 0}, val[3];
-    int cid[8];
-    const int b = block[p];
-    stencil(g, b, x + 3 * p, w, cid);
-    for (int c = 0; c < 8; c++) {
-      corner_val(g, Bc_cur, cid[c], val);
-      for (int d = 0; d < 3; d++) B[d] += w[c] * val[d];
-    }
-    const double dx = bdx(g, b), V = dx * dx * dx;
-    const int s = spec[p];
-    const double W = g->w[s] * (wcorr ? wcorr[p] : 1.0);
-    const double qW = g->q[s] * W, mW = g->m[s] * W;
-    const double h = 0.5 * qW * g->dt / mW;
-    double al[9], vr[3] = {0, 0, 0};
-    alpha_matrix(h, B, al);
-    const double* vv = v + 3 * p;
-    energy += 0.5 * mW * (vv[0] * vv[0] + vv[1] * vv[1] + vv[2] * vv[2]);
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++) vr[i] += al[3 * i + j] * vv[j];
-    const long cl = (long)b * 512 + cell[p];
-    for (int c = 0; c < 8; c++)
-      for (int d = 0; d < 3; d++) cellJ[cl * 24 + 3 * c + d] += qW * w[c] * vr[d];
-    const double mc = qW * h / V;
-    int pr = 0;
-    for (int c1 = 0; c1 < 8; c1++)
-      for (int c2 = 0; c2 <= c1; c2++, pr++)
-        for (int ab = 0; ab < 9; ab++) cellM[cl * 324 + pr * 9 + ab] += mc * w[c1] * w[c2] * al[ab];
+    energy += deposit_one(g, p, x, v, spec, wcorr, block, cell, Bc_cur, cellJ, cellM);
   }
   return energy;
+}
+
+/* The same push + deposit on nthreads host threads (the reference's HYBRID
+ * OpenMP mode runs its mover and UpdateJMassMatrix on all the rank's cores):
+ * the push over contiguous particle ranges; the particles then bucketed by
+ * block (counting sort, the re-binning's relinking); the deposit over
+ * contiguous block ranges of about equal particle counts, so every cell's
+ * blocks are written by one thread, in particle order.  Per-particle results
+ * are those of orc_amr_push / orc_amr_deposit; only the order of the energy
+ * sum differs.  Returns the kinetic energy. */
+typedef struct {
+  const orc_amr* g;
+  long p0, p1;
+  int b0, b1;
+  double* x;
+  double* v;
+  const uint8_t* spec;
+  const double* wcorr;
+  int32_t* block;
+  int32_t* cell;
+  const double *E_half, *Bc_prev, *Bc_cur;
+  double *cellJ, *cellM;
+  const long* start;   /* per block: first index into order */
+  const long* order;   /* particle indices bucketed by block */
+  double energy;
+} mt_task;
+
+static void* mt_push(void* arg) {
+  mt_task* t = (mt_task*)arg;
+  orc_amr_push(t->g, t->p1 - t->p0, t->x + 3 * t->p0, t->v + 3 * t->p0, t->spec + t->p0,
+               t->block + t->p0, t->cell + t->p0, t->E_half, t->Bc_prev);
+  return NULL;
+}
+
+static void* mt_deposit(void* arg) {
+  mt_task* t = (mt_task*)arg;
+  memset(t->cellJ + (long)t->b0 * 512 * 24, 0, sizeof(double) * (size_t)(t->b1 - t->b0) * 512 * 24);
+  memset(t->cellM + (long)t->b0 * 512 * 324, 0, sizeof(double) * (size_t)(t->b1 - t->b0) * 512 * 324);
+  double e = 0.0;
+  for (long k = t->start[t->b0]; k < t->start[t->b1]; k++)
+    e += deposit_one(t->g, t->order[k], t->x, t->v, t->spec, t->wcorr, t->block, t->cell, t->Bc_cur,
+                     t->cellJ, t->cellM);
+  t->energy = e;
+  return NULL;
+}
+
+double orc_amr_push_deposit_mt(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
+                               const double* wcorr, int32_t* block, int32_t* cell,
+                               const double* E_half, const double* Bc_prev, const double* Bc_cur,
+                               double* cellJ, double* cellM, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  mt_task task[256];
+  const int nb = g->nblocks;
+  for (int t = 0; t < nthreads; t++) {
+    mt_task* k = task + t;
+    memset(k, 0, sizeof(*k));
+    k->g = g; k->x = x; k->v = v; k->spec = spec; k->wcorr = wcorr; k->block = block; k->cell = cell;
+    k->E_half = E_half; k->Bc_prev = Bc_prev; k->Bc_cur = Bc_cur; k->cellJ = cellJ; k->cellM = cellM;
+    k->p0 = n * t / nthreads;
+    k->p1 = n * (t + 1) / nthreads;
+  }
+  for (int t = 0; t < nthreads; t++) pthread_create(th + t, NULL, mt_push, task + t);
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  /* bucket by block (deleted particles, block < 0, are left out) */
+  long* start = (long*)calloc((size_t)nb + 1, sizeof(long));
+  long* order = (long*)malloc(sizeof(long) * (size_t)(n > 0 ? n : 1));
+  for (long p = 0; p < n; p++)
+    if (block[p] >= 0) start[block[p] + 1]++;
+  for (int b = 0; b < nb; b++) start[b + 1] += start[b];
+  long* fill = (long*)malloc(sizeof(long) * (size_t)(nb > 0 ? nb : 1));
+  memcpy(fill, start, sizeof(long) * (size_t)nb);
+  for (long p = 0; p < n; p++)
+    if (block[p] >= 0) order[fill[block[p]]++] = p;
+  free(fill);
+  /* block ranges of about equal particle counts */
+  int b = 0;
+  const long tot = start[nb];
+  for (int t = 0; t < nthreads; t++) {
+    task[t].b0 = b;
+    const long target = tot * (t + 1) / nthreads;
+    while (b < nb && (t == nthreads - 1 || start[b + 1] <= target)) b++;
+    task[t].b1 = (t == nthreads - 1) ? nb : b;
+    task[t].start = start;
+    task[t].order = order;
+  }
+  for (int t = 0; t < nthreads; t++) pthread_create(th + t, NULL, mt_deposit, task + t);
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  double e = 0.0;
+  for (int t = 0; t < nthreads; t++) e += task[t].energy;
+  free(start);
+  free(order);
+  return e;
 }
 
 /* Species moments on corners (ProcessCell pic_field_solver_ecsim.cpp:2270-2303,

@@ -235,3 +235,33 @@ def test_amr_relboris_equals_uniform_relboris():
     d -= L * np.rint(d / L)
     assert np.abs(d).max() < 1e-9 * wl.mesh.dx
     np.testing.assert_allclose(ao.v, st.v, rtol=0, atol=1e-10)
+
+
+def test_threaded_push_deposit_equals_serial():
+    """the threaded oracle step of the CPU reference arm (push over particle
+    ranges, deposit over block ranges) gives the serial restatement's
+    particles and per-cell blocks exactly, the energy to its summation order"""
+    mesh = amr.central_refined_mesh((4, 4, 4), lmax=1, frac=0.5)
+    wl = A.electron_proton_plasma("mt", 1, 1, 1, 4, 2)
+    ic = amr.amr_initial_condition(mesh, wl.species, 4, seed=23)
+    x = mesh.block_origins()[ic["block"]] + ic["u"].astype(np.float64) * mesh.block_dx()[ic["block"]][:, None]
+    f = amr.amr_initial_fields(mesh, wl.b0)
+    states = []
+    for _ in range(2):
+        ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64) * 5.0,
+                          ic["spec"])
+        ao.E_half[:] = 1e-2 * np.cos(np.arange(ao.E_half.size)).reshape(ao.E_half.shape)
+        ao.Bprev[:] = f["B_corner_prev"]
+        ao.Bcur[:] = f["B_corner_cur"]
+        states.append(ao)
+    a, b = states
+    a.push()
+    ea = a.deposit()
+    eb = b.push_deposit_mt(5)
+    np.testing.assert_array_equal(a.x, b.x)
+    np.testing.assert_array_equal(a.v, b.v)
+    np.testing.assert_array_equal(a.block, b.block)
+    np.testing.assert_array_equal(a.cellJ, b.cellJ)
+    np.testing.assert_array_equal(a.cellM, b.cellM)
+    assert eb == pytest.approx(ea, rel=1e-13)
+    assert (a.block != mesh.nblocks).all() and len(np.unique(a.block)) > 10
