@@ -127,6 +127,7 @@ SIGNATURES = {
     "amps_gpu_move_particles_relativistic": (C.c_int, [P, C.c_double, C.c_double, LL]),
     "amps_gpu_move_particles_boris": (C.c_int, [P, C.c_double]),
     "amps_gpu_particle_cfl": (C.c_int, [P, C.POINTER(C.c_double)]),
+    "amps_gpu_write_tecplot": (C.c_int, [P, C.c_char_p]),
     "amps_gpu_update_j_mass_matrix": (C.c_int, [P, D]),
     "amps_gpu_field_solve": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(SolveStats)]),
     "amps_gpu_step": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(StepStats)]),

@@ -428,6 +428,11 @@ class EcsimContext:
         fields (E^n, corner B cur): one step of dt_total, then re-binning."""
         self._check(self.lib.amps_gpu_move_particles_boris(self.h, dt_total), "Mover::Boris")
 
+    def write_tecplot(self, path):
+        """Tecplot ASCII file of the corner fields (the reference's mesh-writer
+        layout: FEBRICK zone, corner E, B and E^{n+theta})"""
+        self._check(self.lib.amps_gpu_write_tecplot(self.h, str(path).encode()), "write_tecplot")
+
     def particle_cfl(self):
         """per-species maximum CFL number of the current particles (the value
         UpdateJMassMatrix prints)"""

@@ -202,6 +202,15 @@ amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* ctx, double* E_n, double* E
  * so an AMR run can take J and M back into its corner nodes. */
 amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* ctx, const double* J, const double* M);
 amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* ctx, double* J, double* M);
+/* Tecplot ASCII output of the corner fields in the layout of the reference's
+ * mesh writer (outputMeshDataTECPLOT, src/meshAMR/meshAMRgeneric.h:8845; data
+ * file :7685-7710): VARIABLES "X", "Y", "Z", ECSIM's corner E
+ * ("Ex (corner node)" .., pic_field_solver_ecsim.cpp:6416-6420), the corner B
+ * ("cur" slot) and E^{n+theta}; one ZONE, DATAPACKING=POINT, ZONETYPE=FEBRICK,
+ * one line per corner node (position and values, "%e"), then the 8 node
+ * numbers of every cell.  Periodic far faces and AMR corners get nodes at their
+ * positions (values of the corner they wrap to / the unique corner). */
+amps_gpu_status amps_gpu_write_tecplot(amps_gpu_ctx* ctx, const char* path);
 /* Per-cell pieces of ProcessCell (pic_field_solver_ecsim.cpp:1882-2438) before
  * the corner assembly, cells in block order: cellJ[24] = sum q W w_c (alpha v)
  * for the 8 corners (order (0,0,0),(1,0,0),(1,1,0),(0,1,0), then z+1), and
