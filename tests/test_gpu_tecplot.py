@@ -19,7 +19,8 @@ def parse(path):
     with open(path) as f:
         head = f.readline()
         zone = f.readline()
-        parts = dict(t.split("=") for t in zone.replace("ZONE", "").replace(" ", "").strip().split(","))
+        assert zone.startswith("ZONE ")
+        parts = dict(t.split("=") for t in zone[len("ZONE "):].replace(" ", "").strip().split(","))
         n, e = int(parts["N"]), int(parts["E"])
         nodes = np.array([[float(t) for t in f.readline().split()] for _ in range(n)])
         conn = np.array([[int(t) for t in f.readline().split()] for _ in range(e)]) - 1
