@@ -126,14 +126,16 @@ __device__ __forceinline__ void stage_fields(float* __restrict__ rec, int pos,
   w[4] = gx * gy * fz; w[5] = fx * gy * fz; w[6] = fx * fy * fz; w[7] = gx * fy * fz;
   const int sb = i + 9 * (j + 9 * k);
   const int coff[8] = {0, 1, 10, 9, 81, 82, 91, 90};
-  float B0 = 0.f, B1 = 0.f, B2 = 0.f;
+  // two partial sums per component (corners 0-3, 4-7): six independent chains
+  float Bs[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 #pragma unroll
   for (int c = 0; c < 8; c++) {
     const float4 q = sB[sb + coff[c]];
-    B0 = fmaf(w[c], q.x, B0);
-    B1 = fmaf(w[c], q.y, B1);
-    B2 = fmaf(w[c], q.z, B2);
+    Bs[c >> 2][0] = fmaf(w[c], q.x, Bs[c >> 2][0]);
+    Bs[c >> 2][1] = fmaf(w[c], q.y, Bs[c >> 2][1]);
+    Bs[c >> 2][2] = fmaf(w[c], q.z, Bs[c >> 2][2]);
   }
+  const float B0 = Bs[0][0] + Bs[1][0], B1 = Bs[0][1] + Bs[1][1], B2 = Bs[0][2] + Bs[1][2];
   const float h = st.qdt2m[s];
   const float h2 = h * h;
   const float c0 = 1.0f / (1.0f + h2 * (B0 * B0 + B1 * B1 + B2 * B2));
@@ -214,13 +216,16 @@ struct Tile {
         A[q] = *reinterpret_cast<const ulonglong2*>(pa + q * FS + r);
         B[q] = *reinterpret_cast<const ulonglong2*>(pb + q * FS + r);
       }
+      // the 9 positions-(r, r+1) products first, then the 9 (r+2, r+3) ones:
+      // 9 independent accumulators between dependent packed FMAs
 #pragma unroll
       for (int q = 0; q < 3; q++)
 #pragma unroll
-        for (int e = 0; e < 3; e++) {
-          ffma2(acc[3 * q + e], A[q].x, B[e].x);
-          ffma2(acc[3 * q + e], A[q].y, B[e].y);
-        }
+        for (int e = 0; e < 3; e++) ffma2(acc[3 * q + e], A[q].x, B[e].x);
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++) ffma2(acc[3 * q + e], A[q].y, B[e].y);
     }
 #pragma unroll
     for (int e = 0; e < 9; e++) {

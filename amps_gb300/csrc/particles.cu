@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
         }
         // E and B as three packed pairs (E0 E1) (E2 B0) (B1 B2), the layout of a
         // stencil corner's two float4s, accumulated by packed FMAs
-        unsigned long long eb[3] = {0ull, 0ull, 0ull};
+        unsigned long long eb[2][3] = {{0ull, 0ull, 0ull}, {0ull, 0ull, 0ull}};  // z = 0, 1 layers
 #pragma unroll
         for (int cc = 0; cc < 2; cc++)
 #pragma unroll
@@ -296,14 +296,19 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
               const ulonglong2 q1v = reinterpret_cast<const ulonglong2*>(s_push)[2 * sidx + 1];
               unsigned long long ww;
               asm("mov.b64 %0, {%1, %1};" : "=l"(ww) : "f"(w));
-              ffma2(eb[0], ww, q0v.x);
-              ffma2(eb[1], ww, q0v.y);
-              ffma2(eb[2], ww, q1v.x);
+              ffma2(eb[cc][0], ww, q0v.x);
+              ffma2(eb[cc][1], ww, q0v.y);
+              ffma2(eb[cc][2], ww, q1v.x);
             }
-        const float2 e01 = *reinterpret_cast<const float2*>(&eb[0]);
-        const float2 e2b0 = *reinterpret_cast<const float2*>(&eb[1]);
-        const float2 b12 = *reinterpret_cast<const float2*>(&eb[2]);
-        const float E[3] = {e01.x, e01.y, e2b0.x}, B[3] = {e2b0.y, b12.x, b12.y};
+        float eb_f[6];
+#pragma unroll
+        for (int t = 0; t < 3; t++) {
+          const float2 lo = *reinterpret_cast<const float2*>(&eb[0][t]);
+          const float2 hi = *reinterpret_cast<const float2*>(&eb[1][t]);
+          eb_f[2 * t] = lo.x + hi.x;
+          eb_f[2 * t + 1] = lo.y + hi.y;
+        }
+        const float E[3] = {eb_f[0], eb_f[1], eb_f[2]}, B[3] = {eb_f[3], eb_f[4], eb_f[5]};
         lapenta(a.st.qdt2m[s], E, B, v);
         bool far = false, nearf = false;
         int nbk = b;
