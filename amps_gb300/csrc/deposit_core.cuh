@@ -236,101 +236,59 @@ struct Tile {
       sum[e] = t;
     }
   }
-  // the cell's current partials of this lane's tile, loaded ahead of an add-flush
-  __device__ __forceinline__ void preload(int lane, const float* __restrict__ cellM,
-                                          const float* __restrict__ cellJ, long long cid,
-                                          float old[9]) const {
-#pragma unroll
-    for (int e = 0; e < 9; e++) old[e] = 0.f;
-    if (lane < 27) {
-      const int g = lane / 3, hh = lane % 3;
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++) old[3 * q + e] = cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)];
-    } else if (lane < kTileLanes) {
-      const int g = lane - 27;
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-        if (3 * g + q < 8)
-#pragma unroll
-          for (int e = 0; e < 3; e++) old[3 * q + e] = cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)];
-    }
-  }
-  // write old + this tile's sums
-  __device__ __forceinline__ void flush_onto(int lane, float* __restrict__ cellM,
-                                             float* __restrict__ cellJ, long long cid,
-                                             const float old[9]) {
-    if (lane < 27) {
-      const int g = lane / 3, hh = lane % 3;
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++)
-          cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)] =
-              old[3 * q + e] + (sum[3 * q + e] - cmp[3 * q + e]);
-    } else if (lane < kTileLanes) {
-      const int g = lane - 27;
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-        if (3 * g + q < 8)
-#pragma unroll
-          for (int e = 0; e < 3; e++)
-            cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)] = old[3 * q + e] + (sum[3 * q + e] - cmp[3 * q + e]);
-    }
-  }
-  // write (or add to) the cell partials
+  // write the tile's sums to the cell partials
   __device__ __forceinline__ void flush(int lane, float* __restrict__ cellM,
-                                        float* __restrict__ cellJ, long long cid, bool add) {
-    if (lane < 27) {
-      const int g = lane / 3, hh = lane % 3;
-#pragma unroll
-      for (int q = 0; q < 3; q++)
-#pragma unroll
-        for (int e = 0; e < 3; e++) {
-          const long long o = cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e);
-          const float v = sum[3 * q + e] - cmp[3 * q + e];
-          cellM[o] = add ? cellM[o] + v : v;
-        }
-    } else if (lane < kTileLanes) {
-      const int g = lane - 27;
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const int corner = 3 * g + q;
-        if (corner < 8) {
-#pragma unroll
-          for (int e = 0; e < 3; e++) {
-            const long long o = cellJ_at(cid, corner * 3 + e);
-            const float v = sum[3 * q + e] - cmp[3 * q + e];
-            cellJ[o] = add ? cellJ[o] + v : v;
-          }
-        }
-      }
-    }
-  }
-  // add this tile's sums to the cell partials by global reductions: no value
-  // comes back, so the warp does not wait on the read-modify-write, which the
-  // L2 performs
-  __device__ __forceinline__ void flush_red(int lane, float* __restrict__ cellM,
-                                            float* __restrict__ cellJ, long long cid) {
+                                        float* __restrict__ cellJ, long long cid) const {
     if (lane < 27) {
       const int g = lane / 3, hh = lane % 3;
 #pragma unroll
       for (int q = 0; q < 3; q++)
 #pragma unroll
         for (int e = 0; e < 3; e++)
-          atomicAdd(cellM + cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e), sum[3 * q + e] - cmp[3 * q + e]);
+          cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)] = sum[3 * q + e] - cmp[3 * q + e];
     } else if (lane < kTileLanes) {
       const int g = lane - 27;
 #pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const int corner = 3 * g + q;
-        if (corner < 8)
+      for (int q = 0; q < 3; q++)
+        if (3 * g + q < 8)
 #pragma unroll
           for (int e = 0; e < 3; e++)
-            atomicAdd(cellJ + cellJ_at(cid, corner * 3 + e), sum[3 * q + e] - cmp[3 * q + e]);
-      }
+            cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)] = sum[3 * q + e] - cmp[3 * q + e];
     }
+  }
+  // add the tile's sums to the cell partials by global reductions, which the
+  // L2 performs without a read-back in the warp.  The warp first parks its 267
+  // sums in scr at their partial offsets, so every reduction then covers 32
+  // consecutive partials (4 sectors) instead of one partial in each of ~28
+  // sectors: the L2's sector rate bounds a reduction-heavy pass.  scr is the
+  // warp's staging area; the caller's accumulates are complete (__syncwarp).
+  __device__ __forceinline__ void flush_red(int lane, float* __restrict__ scr,
+                                            float* __restrict__ cellM,
+                                            float* __restrict__ cellJ, long long cid) const {
+    if (lane < 27) {
+      const int g = lane / 3, hh = lane % 3;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int e = 0; e < 3; e++) scr[(3 * g + q) * 9 + 3 * hh + e] = sum[3 * q + e] - cmp[3 * q + e];
+    } else if (lane < kTileLanes) {
+      const int g = lane - 27;
+#pragma unroll
+      for (int q = 0; q < 3; q++)
+        if (3 * g + q < 8)
+#pragma unroll
+          for (int e = 0; e < 3; e++)
+            scr[AMPS_CELLM + (3 * g + q) * 3 + e] = sum[3 * q + e] - cmp[3 * q + e];
+    }
+    __syncwarp();
+    float* m = cellM + cellM_at(cid, 0);
+#pragma unroll
+    for (int r = 0; r < (AMPS_CELLM + 31) / 32; r++) {
+      const int t = lane + 32 * r;
+      if (t < AMPS_CELLM) atomicAdd(m + t, scr[t]);
+    }
+    if (lane < 24) atomicAdd(cellJ + cellJ_at(cid, lane), scr[AMPS_CELLM + lane]);
+    __syncwarp();
   }
 };
 

@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) k_na_deposit(NaArgs a) {
       tile.accumulate<kFS>(rec, (min(32, n0 - q0) + 3) & ~3, fA, fB);
       __syncwarp();
     }
-    tile.flush(lane, a.cellM, a.cellJ, cid, false);
+    tile.flush(lane, a.cellM, a.cellJ, cid);
   }
   reduce_energy(ff_value(en), s_en, a.energy);
 }

@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
     // vacated slots become holes
     for (int t = nst + lane; t < n0; t += 32) a.p.sp[b0 + t] = kHole;
     if (lane == 0) a.stay[cid] = nst;
-    if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid, false);
+    if (DEP) tile.flush(lane, a.cellM, a.cellJ, cid);
   }
   if (n_far) atomicAdd(a.flags + 0, n_far);
   if (n_near) atomicAdd(a.flags + 1, n_near);
@@ -642,95 +642,104 @@ __global__ void k_step_bump(unsigned long long* step, const unsigned long long* 
 }
 
 // Arrivals: deposit (DEP), move behind the stayers, update the occupancy.
-// Arrivals are few per cell (a few % of its particles), so records are staged
-// in chunks of kArrChunk lanes: a smaller record buffer and a register cap let
-// 3 CTAs share an SM, which hides more of the per-cell load latency.
+// A CTA takes the 64 cells of one block layer: one thread per cell loads its
+// slot range and counts and updates the occupancy, the cells with arrivals are
+// listed in shared memory, and the warps take listed cells one at a time from
+// a shared counter, so a few busy cells do not hold idle warps at the CTA's
+// final barrier.  Arrivals are few per cell (a few % of its particles), so
+// records are staged in chunks of kArrChunk lanes: a smaller record buffer and
+// a register cap let 3 CTAs share an SM, which hides more of the per-cell
+// load latency.
 constexpr int kArrChunk = 16;
 constexpr int kFSArr = kArrChunk + 4;  // field stride of the arrivals' staged fields
+constexpr int kLayer = AMPS_NC * AMPS_NC;
 
 template <bool DEP>
 __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
   float* s_rec = reinterpret_cast<float*>(s_dyn);
   __shared__ double s_en[kWarps];
+  __shared__ int4 s_cell[kLayer];  // listed cell: layer index, first arrival slot, destination, count
+  __shared__ int s_nw[2], s_next;
   const int b = blockIdx.x, k = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // the few arrivals read the block's B stencil from global memory (L2-resident:
   // 11.7 KB per block) instead of waiting for a staged copy at CTA start
   const float4* s_dep = reinterpret_cast<const float4*>(a.st_dep) + (size_t)b * AMPS_SC;
+  int4 cv = make_int4(0, 0, 0, 0);
+  bool has = false;
+  if (threadIdx.x < kLayer) {
+    const long long cl = (long long)b * AMPS_CPB + threadIdx.x + kLayer * k;
+    const int b0 = a.base[cl], cap = a.base[cl + 1] - b0, n0 = a.cnt[cl], nst = a.stay[cl];
+    const int na = min(a.arr[cl], cap - n0);
+    a.cnt[cl] = nst + max(0, na);
+    a.arr[cl] = 0;
+    has = na > 0;
+    cv = make_int4(threadIdx.x, b0 + cap - na, b0 + nst, na);
+  }
+  const unsigned hm = __ballot_sync(0xffffffffu, has);
+  if (lane == 0 && wid < 2) s_nw[wid] = __popc(hm);
+  if (threadIdx.x == 0) s_next = 0;
+  __syncthreads();
+  if (has) s_cell[(wid ? s_nw[0] : 0) + __popc(hm & lanemask_lt())] = cv;
+  const int ncell = s_nw[0] + s_nw[1];
+  __syncthreads();
   float* rec = s_rec + wid * kFields * kFSArr;
   int fA, fB;
   lane_fields(lane, fA, fB);
-  FF en_row{0.f, 0.f};  // the row's arrivals, as a float pair before the FP64 reduction
-  const int j = wid;
+  FF en_w{0.f, 0.f};  // the warp's arrivals, as a float pair before the FP64 reduction
   const float inv_vol = block_inv_vol(a, b);
-  // the row's 8 cells: lane i < 8 loads cell i's slot range, occupancy, stayers
-  // and arrivals at once (one round of loads instead of eight dependent ones)
-  int mb0 = 0, mcap = 0, mn0 = 0, mst = 0, marr = 0;
-  if (lane < AMPS_NC) {
-    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
-    mb0 = a.base[cl];
-    mcap = a.base[cl + 1] - mb0;
-    mn0 = a.cnt[cl];
-    mst = a.stay[cl];
-    marr = a.arr[cl];
-  }
-  for (int i = 0; i < AMPS_NC; i++) {
-    const long long cid = (long long)b * AMPS_CPB + i + AMPS_NC * (j + AMPS_NC * k);
-    const int b0 = __shfl_sync(0xffffffffu, mb0, i), cap = __shfl_sync(0xffffffffu, mcap, i);
-    const int n0 = __shfl_sync(0xffffffffu, mn0, i), nst = __shfl_sync(0xffffffffu, mst, i);
-    const int na = min(__shfl_sync(0xffffffffu, marr, i), cap - n0);
-    if (na > 0) {
-      Tile tile;
-      tile.zero();
-      const int src0 = b0 + cap - na, dst0 = b0 + nst;
-      for (int q0 = 0; q0 < na; q0 += kArrChunk) {
-        const bool act = lane < kArrChunk && q0 + lane < na;
-        const long long ps = src0 + q0 + lane, pd = dst0 + q0 + lane;
-        float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
-        int s = 0;
-        float wcv = 1.0f;
-        uint32_t idv = 0;
-        if (act) {
+  for (;;) {
+    int e = 0;
+    if (lane == 0) e = atomicAdd(&s_next, 1);
+    e = __shfl_sync(0xffffffffu, e, 0);
+    if (e >= ncell) break;
+    const int4 c = s_cell[e];
+    const int i = c.x & (AMPS_NC - 1), j = c.x / AMPS_NC;
+    const int src0 = c.y, dst0 = c.z, na = c.w;
+    const long long cid = (long long)b * AMPS_CPB + c.x + kLayer * k;
+    Tile tile;
+    tile.zero();
+    for (int q0 = 0; q0 < na; q0 += kArrChunk) {
+      const bool act = lane < kArrChunk && q0 + lane < na;
+      const long long ps = src0 + q0 + lane, pd = dst0 + q0 + lane;
+      float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
+      int s = 0;
+      float wcv = 1.0f;
+      uint32_t idv = 0;
+      if (act) {
 #pragma unroll
-          for (int d = 0; d < 3; d++) { u[d] = a.p.u[d][ps]; v[d] = a.p.v[d][ps]; }
-          s = a.p.sp[ps];
-          if (a.p.wc) wcv = a.p.wc[ps];
-          if (a.p.id) idv = a.p.id[ps];
-        }
-        __syncwarp();
-        if (act) {
-#pragma unroll
-          for (int d = 0; d < 3; d++) { a.p.u[d][pd] = u[d]; a.p.v[d][pd] = v[d]; }
-          a.p.sp[pd] = (uint8_t)s;
-          if (a.p.wc) a.p.wc[pd] = wcv;
-          if (a.p.id) a.p.id[pd] = idv;
-        }
-        if (DEP) {
-          // positions past the chunk's arrivals stage zero weight
-          if (lane < kArrChunk)
-            stage_fields<kFSArr>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
-                                 act ? wcv : 0.f, i, j, k, a.st, inv_vol, en_row);
-          __syncwarp();
-          tile.accumulate<kFSArr>(rec, (min(kArrChunk, na - q0) + 3) & ~3, fA, fB);
-          __syncwarp();
-        }
+        for (int d = 0; d < 3; d++) { u[d] = a.p.u[d][ps]; v[d] = a.p.v[d][ps]; }
+        s = a.p.sp[ps];
+        if (a.p.wc) wcv = a.p.wc[ps];
+        if (a.p.id) idv = a.p.id[ps];
       }
       __syncwarp();
-      // slots that held arrivals and are now beyond the new occupancy
-      for (int t = lane; t < na; t += 32) {
-        const int slot = src0 + t;
-        if (slot >= dst0 + na) a.p.sp[slot] = kHole;
+      if (act) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) { a.p.u[d][pd] = u[d]; a.p.v[d][pd] = v[d]; }
+        a.p.sp[pd] = (uint8_t)s;
+        if (a.p.wc) a.p.wc[pd] = wcv;
+        if (a.p.id) a.p.id[pd] = idv;
       }
-      if (DEP) tile.flush_red(lane, a.cellM, a.cellJ, cid);
+      if (DEP) {
+        // positions past the chunk's arrivals stage zero weight
+        if (lane < kArrChunk)
+          stage_fields<kFSArr>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+                               act ? wcv : 0.f, i, j, k, a.st, inv_vol, en_w);
+        __syncwarp();
+        tile.accumulate<kFSArr>(rec, (min(kArrChunk, na - q0) + 3) & ~3, fA, fB);
+        __syncwarp();
+      }
     }
+    // slots that held arrivals and are now beyond the new occupancy
+    for (int t = lane; t < na; t += 32) {
+      const int slot = src0 + t;
+      if (slot >= dst0 + na) a.p.sp[slot] = kHole;
+    }
+    if (DEP) tile.flush_red(lane, rec, a.cellM, a.cellJ, cid);
   }
-  if (lane < AMPS_NC) {
-    const long long cl = (long long)b * AMPS_CPB + lane + AMPS_NC * (j + AMPS_NC * k);
-    a.cnt[cl] = mst + max(0, min(marr, mcap - mn0));
-    a.arr[cl] = 0;
-  }
-  if (DEP) reduce_energy(ff_value(en_row), s_en, a.energy);
+  if (DEP) reduce_energy(ff_value(en_w), s_en, a.energy);
 }
 
 // Full deposition over the compact layout.
@@ -774,7 +783,7 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
       tile.accumulate<kFS>(rec, (min(32, n0 - q0) + 3) & ~3, fA, fB);
       __syncwarp();
     }
-    tile.flush(lane, a.cellM, a.cellJ, cid, false);
+    tile.flush(lane, a.cellM, a.cellJ, cid);
   }
   reduce_energy(ff_value(en), s_en, a.energy);
 }
