@@ -41,8 +41,9 @@ METRIC = "particle-steps/s (push+deposit)"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # particle-step kernels on the default workload, from a one-pass ncu capture
 # of this bench command; "version" names the kernel revision it was taken on
-MEASURED_TRAFFIC = {"amr_64c_128ppc": {"version": "push_deposit 27-monomial 3x3 tiles",
-                                       "push_deposit": 4.66e9, "arrivals": 1.09e9}}
+MEASURED_TRAFFIC = {"amr_64c_128ppc": {"version": "push_deposit packed-FMA 3x3 tiles on SoA "
+                                                  "records; arrivals from a per-layer cell list",
+                                       "push_deposit": 4.663e9, "arrivals": 1.016e9}}
 UNIT = "particle-steps/s"
 
 
@@ -800,33 +801,58 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def reference_amr_workload(name, threads, steps, warmup):
+def reference_amr_workload(name, threads, steps, warmup, budget):
     """The reference CPU path on the GPU arm's own AMR workload: the FP64 AMR
     oracle (Lapenta2017 + re-binning + ProcessCell, pinned to the reference's
-    compiled ProcessCell/Lapenta2017) over every particle of the workload on
-    `threads` host threads, one push + deposit per step.  Returns the per-step
-    seconds of the timed steps and the particle count."""
+    compiled ProcessCell/Lapenta2017) on `threads` host threads, one push +
+    deposit per step.  Each step is a bounded sample of the workload: the
+    particles of every m-th block, pushed, and those blocks' ProcessCell, with m
+    the smallest stride at which the warm-up and timed steps take about `budget`
+    seconds (m = 1, every particle, when the whole workload fits).  The sample's
+    particles are put back before every step, outside the timed region, so
+    every step does the same work.  Returns the per-step seconds, the particles
+    per step, the stride and the workload's particle count."""
     from amps_gb300 import amr
     from tests import oracle_amr as OA
     wl = amr.AMR_WORKLOADS[name]()
     mesh = wl.mesh()
     ic = wl.initial_condition(mesh, seed=100, nthreads=threads)
-    x = mesh.block_origins()[ic["block"]] + ic["u"].astype(np.float64) * mesh.block_dx()[ic["block"]][:, None]
-    wc = None if ic["wcorr"] is None else ic["wcorr"].astype(np.float64)
-    ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64), ic["spec"],
-                      wcorr=wc)
+    nb = mesh.nblocks
     f = amr.amr_initial_fields(mesh, wl.b0)
-    ao.Bprev[:] = f["B_corner_prev"]
-    ao.Bcur[:] = f["B_corner_cur"]
-    del ic, x
-    for _ in range(warmup):
-        ao.push_deposit_mt(threads)
+
+    def sample(m):
+        sel = np.arange(nb) % m == 0
+        pick = sel[ic["block"]]
+        blk = ic["block"][pick]
+        x = mesh.block_origins()[blk] + ic["u"][pick].astype(np.float64) * mesh.block_dx()[blk][:, None]
+        wc = None if ic["wcorr"] is None else ic["wcorr"][pick].astype(np.float64)
+        ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"][pick].astype(np.float64),
+                          ic["spec"][pick], wcorr=wc)
+        ao.Bprev[:] = f["B_corner_prev"]
+        ao.Bcur[:] = f["B_corner_cur"]
+        start = [a.copy() for a in (ao.x, ao.v, ao.block, ao.cell)]
+        return ao, sel.astype(np.uint8), start
+
+    # calibration on every 8th block: seconds per step of the whole workload
+    ntot = len(ic["spec"])
+    ao, sel, start = sample(8)
+    t0 = time.perf_counter()
+    ao.push_deposit_mt(threads, sel)
+    full = (time.perf_counter() - t0) * ntot / len(ao.spec)
+    m = max(1, int(np.ceil((steps + warmup) * full / budget)))
+    if m != 8:
+        del ao
+        ao, sel, start = sample(m)
+    del ic
     times = []
-    for _ in range(steps):
+    for it in range(warmup + steps):
+        for a, a0 in zip((ao.x, ao.v, ao.block, ao.cell), start):
+            a[:] = a0
         t0 = time.perf_counter()
-        ao.push_deposit_mt(threads)
-        times.append(time.perf_counter() - t0)
-    return times, len(ao.spec)
+        ao.push_deposit_mt(threads, sel)
+        if it >= warmup:
+            times.append(time.perf_counter() - t0)
+    return times, len(ao.spec), m, ntot
 
 
 def run_reference(args):
@@ -836,12 +862,17 @@ def run_reference(args):
     from amps_gb300 import amr
     threads = os.cpu_count() or 1
     if args.workload in amr.AMR_WORKLOADS:
-        times, n = reference_amr_workload(args.workload, threads, args.steps, args.warmup)
+        times, n, m, ntot = reference_amr_workload(args.workload, threads, args.steps, args.warmup,
+                                             args.ref_budget)
         value = n * len(times) / sum(times)
+        part = ("all %d particles" % n if m == 1 else
+                "the %d particles of one block in %d (%.3g of the workload)"
+                % (n, m, n / ntot))
         sample = ("FP64 AMR oracle (Lapenta2017 + re-binning across levels + ProcessCell, pinned to "
-                  "the reference's compiled ProcessCell/Lapenta2017) over all %d particles of %s "
-                  "on %d host threads (push over particle ranges, deposit over block ranges), "
-                  "%.2f s per step" % (n, args.workload, threads, sum(times) / len(times)))
+                  "the reference's compiled ProcessCell/Lapenta2017) on %d host threads (push over "
+                  "particle ranges, deposit over block ranges): per step %s of %s, pushed, and "
+                  "those blocks' ProcessCell, %.2f s per step" %
+                  (threads, part, args.workload, sum(times) / len(times)))
         same = True
     else:
         rates = []
@@ -876,6 +907,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-budget", type=float, default=90.0,
+                    help="reference arm on an AMR workload: seconds of warm-up + timed steps; "
+                         "each step is a sample of the workload's blocks sized to fit")
     ap.add_argument("--precond-ab", type=int, default=1,
                     help="learned vs plain vs Jacobi GMRES on the 32^3 plasma (1 = on)")
     ap.add_argument("--precond-stiff", type=int, default=1,

@@ -464,7 +464,10 @@ double orc_amr_deposit(const orc_amr* g, long n, const double* x, const double* 
  * contiguous block ranges of about equal particle counts, so every cell's
  * blocks are written by one thread, in particle order.  Per-particle results
  * are those of orc_amr_push / orc_amr_deposit; only the order of the energy
- * sum differs.  Returns the kinetic energy. */
+ * sum differs.  Returns the kinetic energy.  sel (may be NULL: every block)
+ * restricts the deposit to the blocks with sel[b] != 0: the others are
+ * neither cleared nor deposited (a bounded sample of the step: the particles of
+ * some blocks, pushed, and those blocks' ProcessCell). */
 typedef struct {
   const orc_amr* g;
   long p0, p1;
@@ -479,6 +482,7 @@ typedef struct {
   double *cellJ, *cellM;
   const long* start;   /* per block: first index into order */
   const long* order;   /* particle indices bucketed by block */
+  const uint8_t* sel;  /* blocks to deposit, NULL: all */
   double energy;
 } mt_task;
 
@@ -491,12 +495,15 @@ static void* mt_push(void* arg) {
 
 static void* mt_deposit(void* arg) {
   mt_task* t = (mt_task*)arg;
-  memset(t->cellJ + (long)t->b0 * 512 * 24, 0, sizeof(double) * (size_t)(t->b1 - t->b0) * 512 * 24);
-  memset(t->cellM + (long)t->b0 * 512 * 324, 0, sizeof(double) * (size_t)(t->b1 - t->b0) * 512 * 324);
   double e = 0.0;
-  for (long k = t->start[t->b0]; k < t->start[t->b1]; k++)
-    e += deposit_one(t->g, t->order[k], t->x, t->v, t->spec, t->wcorr, t->block, t->cell, t->Bc_cur,
-                     t->cellJ, t->cellM);
+  for (int b = t->b0; b < t->b1; b++) {
+    if (t->sel && !t->sel[b]) continue;
+    memset(t->cellJ + (long)b * 512 * 24, 0, sizeof(double) * 512 * 24);
+    memset(t->cellM + (long)b * 512 * 324, 0, sizeof(double) * 512 * 324);
+    for (long k = t->start[b]; k < t->start[b + 1]; k++)
+      e += deposit_one(t->g, t->order[k], t->x, t->v, t->spec, t->wcorr, t->block, t->cell,
+                       t->Bc_cur, t->cellJ, t->cellM);
+  }
   t->energy = e;
   return NULL;
 }
@@ -504,7 +511,7 @@ static void* mt_deposit(void* arg) {
 double orc_amr_push_deposit_mt(const orc_amr* g, long n, double* x, double* v, const uint8_t* spec,
                                const double* wcorr, int32_t* block, int32_t* cell,
                                const double* E_half, const double* Bc_prev, const double* Bc_cur,
-                               double* cellJ, double* cellM, int nthreads) {
+                               double* cellJ, double* cellM, int nthreads, const uint8_t* sel) {
   if (nthreads < 1) nthreads = 1;
   if (nthreads > 256) nthreads = 256;
   pthread_t th[256];
@@ -541,6 +548,7 @@ double orc_amr_push_deposit_mt(const orc_amr* g, long n, double* x, double* v, c
     task[t].b1 = (t == nthreads - 1) ? nb : b;
     task[t].start = start;
     task[t].order = order;
+    task[t].sel = sel;
   }
   for (int t = 0; t < nthreads; t++) pthread_create(th + t, NULL, mt_deposit, task + t);
   for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);

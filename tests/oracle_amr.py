@@ -37,7 +37,7 @@ def lib():
             "orc_amr_boris": (C.c_long, [C.POINTER(Amr), C.c_long, D, D, U8, I32, I32, D, D,
                                          C.c_double]),
             "orc_amr_push_deposit_mt": (C.c_double, [C.POINTER(Amr), C.c_long, D, D, U8, D, I32,
-                                                     I32, D, D, D, D, D, C.c_int]),
+                                                     I32, D, D, D, D, D, C.c_int, U8]),
             "orc_amr_deposit": (C.c_double, [C.POINTER(Amr), C.c_long, D, D, U8, D, I32, I32, D,
                                              D, D]),
             "orc_amr_apply": (None, [C.POINTER(Amr), D, D, D, C.c_int, C.c_int, C.c_int]),
@@ -125,13 +125,19 @@ class AmrOracle:
                                       p(self.block, C.c_int32), p(self.cell, C.c_int32),
                                       p(self.Bcur), p(self.cellJ), p(self.cellM))
 
-    def push_deposit_mt(self, nthreads):
+    def push_deposit_mt(self, nthreads, sel=None):
         """push then deposit on nthreads host threads (same per-cell results as
-        push() followed by deposit()); returns the kinetic energy"""
+        push() followed by deposit()); sel (uint8 per block, optional): deposit
+        only the blocks with sel != 0, leave the others' partials untouched.
+        Returns the kinetic energy."""
+        if sel is not None:
+            sel = np.ascontiguousarray(sel, np.uint8)
+            assert sel.shape == (self.mesh.nblocks,)
         return self.L.orc_amr_push_deposit_mt(
             C.byref(self.g), len(self.spec), p(self.x), p(self.v), p(self.spec, C.c_uint8),
             p(self.wcorr), p(self.block, C.c_int32), p(self.cell, C.c_int32), p(self.E_half),
-            p(self.Bprev), p(self.Bcur), p(self.cellJ), p(self.cellM), nthreads)
+            p(self.Bprev), p(self.Bcur), p(self.cellJ), p(self.cellM), nthreads,
+            p(sel, C.c_uint8))
 
     def species_moments(self):
         """(ncorners, nspec, 10) corner species moments of the current particles"""

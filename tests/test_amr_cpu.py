@@ -247,14 +247,14 @@ def test_threaded_push_deposit_equals_serial():
     x = mesh.block_origins()[ic["block"]] + ic["u"].astype(np.float64) * mesh.block_dx()[ic["block"]][:, None]
     f = amr.amr_initial_fields(mesh, wl.b0)
     states = []
-    for _ in range(2):
+    for _ in range(3):
         ao = OA.AmrOracle(mesh, wl.species, wl.dt, wl.theta, x, ic["v"].astype(np.float64) * 5.0,
                           ic["spec"])
         ao.E_half[:] = 1e-2 * np.cos(np.arange(ao.E_half.size)).reshape(ao.E_half.shape)
         ao.Bprev[:] = f["B_corner_prev"]
         ao.Bcur[:] = f["B_corner_cur"]
         states.append(ao)
-    a, b = states
+    a, b, c = states
     a.push()
     ea = a.deposit()
     eb = b.push_deposit_mt(5)
@@ -265,3 +265,16 @@ def test_threaded_push_deposit_equals_serial():
     np.testing.assert_array_equal(a.cellM, b.cellM)
     assert eb == pytest.approx(ea, rel=1e-13)
     assert (a.block != mesh.nblocks).all() and len(np.unique(a.block)) > 10
+    # a block selection (the reference arm's bounded sample): the selected
+    # blocks' partials as above, the others untouched
+    sel = (np.arange(mesh.nblocks) % 3 == 0).astype(np.uint8)
+    c.cellJ[:] = 7.0
+    c.cellM[:] = 7.0
+    c.push_deposit_mt(4, sel)
+    np.testing.assert_array_equal(c.x, a.x)
+    cj, cm = c.cellJ.reshape(mesh.nblocks, -1), c.cellM.reshape(mesh.nblocks, -1)
+    aj, am = a.cellJ.reshape(mesh.nblocks, -1), a.cellM.reshape(mesh.nblocks, -1)
+    on = sel.astype(bool)
+    np.testing.assert_array_equal(cj[on], aj[on])
+    np.testing.assert_array_equal(cm[on], am[on])
+    assert (cj[~on] == 7.0).all() and (cm[~on] == 7.0).all()
