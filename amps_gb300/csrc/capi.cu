@@ -258,7 +258,11 @@ amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_b
                       "particle step")))
     return s;
   long long ovf = 0;
-  if ((s = read_step_flags(c, out_of_block, near_face, &ovf))) return s;
+  if ((s = read_step_flags(c, out_of_block, near_face, &ovf))) {
+    // no recovery: drop the overflowed cells' arrival counts it would have used
+    cudaMemsetAsync(c->d_arr, 0, sizeof(int) * c->ncor, c->stream);
+    return s;
+  }
   if (ovf > 0) {
     // rare: some cell ran out of slack.  Re-sort everything (new slack) and
     // redo the deposition from the rebuilt layout.

@@ -254,9 +254,9 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
 cudaError_t launch_deposit(amps_gpu_ctx* c);
 void set_next_id(amps_gpu_ctx* c, long long n);
 // counting sort of the list buffer into the slotted layout (keys in d_key)
-cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n);
+cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n, bool demand = false);
 // its placement half: d_count, d_key and d_rank already filled
-cudaError_t place_ranked(amps_gpu_ctx* c, long long n);
+cudaError_t place_ranked(amps_gpu_ctx* c, long long n, bool demand = false);
 // species moments on corners (species.cu)
 amps_gpu_status species_setup(amps_gpu_ctx* c, bool on);
 void species_free(amps_gpu_ctx* c);

@@ -671,9 +671,11 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   if (threadIdx.x < kLayer) {
     const long long cl = (long long)b * AMPS_CPB + threadIdx.x + kLayer * k;
     const int b0 = a.base[cl], cap = a.base[cl + 1] - b0, n0 = a.cnt[cl], nst = a.stay[cl];
-    const int na = min(a.arr[cl], cap - n0);
+    const int dem = a.arr[cl], na = min(dem, cap - n0);
     a.cnt[cl] = nst + max(0, na);
-    a.arr[cl] = 0;
+    // a cell whose arrivals overflowed its slack keeps their number: the
+    // recovery that follows sizes its new slack by it (and clears it)
+    a.arr[cl] = dem > cap - n0 ? dem : 0;
     has = na > 0;
     cv = make_int4(threadIdx.x, b0 + cap - na, b0 + nst, na);
   }
@@ -942,14 +944,23 @@ __global__ void __launch_bounds__(256) k_rb_rank(long long n, const int* __restr
 // The constant term keeps sparsely filled cells (fine AMR levels) from
 // overflowing: a cell's occupancy random-walks by ~sqrt(2 x crossings) per
 // step, and over 10^5 cells the largest excursion reaches ~4.5 of those.
+// dem (optional): the arrivals of cells that overflowed in the last step; such
+// a cell gets kDemandSlack times that many extra slots.  A steady inflow does
+// this: on meshes whose particle weights scale with the level, light particles
+// stream from a finer level into the coarse cells along the interface at 8x the
+// number rate per level of difference, and those cells keep growing.
+// base = false: the extra slots alone (their total sizes the base slack).
+constexpr int kDemandSlack = 8;
 __global__ void __launch_bounds__(256) k_rb_caps(long long ncell, const int* __restrict__ count,
-                                                 int* __restrict__ cap, int num, int den) {
+                                                 int* __restrict__ cap, int num, int den,
+                                                 const int* __restrict__ dem, bool base) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c > ncell) return;
   if (c == ncell) { cap[c] = 0; return; }
   const int n = count[c];
   const int slack = (n >> 2) + AMPS_SLACK_MIN;
-  cap[c] = n + (int)(((long long)slack * num) / den);
+  cap[c] = (base ? n + (int)(((long long)slack * num) / den) : 0) +
+           (dem ? kDemandSlack * dem[c] : 0);
 }
 
 __global__ void __launch_bounds__(256) k_rb_scatter(long long n, const int* __restrict__ key,
@@ -1638,7 +1649,7 @@ cudaError_t scan_ints(amps_gpu_ctx* c, const int* in, int* out, long long n) {
 
 // Counting sort of the list buffer (cur^1, keys in d_key) with n particles into
 // the slotted layout of buffer cur.
-cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
+cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n, bool demand) {
   cudaStream_t s = c->stream;
   const long long nc = c->ncor;
   cudaError_t e = cudaMemsetAsync(c->d_count, 0, sizeof(int) * (nc + 1), s);
@@ -1647,27 +1658,53 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
     TimedLaunch t(c, "rebuild");
     k_rb_rank<<<grid_for(n, 256), 256, 0, s>>>(n, c->d_key, c->d_rank, c->d_count);
   }
-  return place_ranked(c, n);
+  return place_ranked(c, n, demand);
 }
 
 // Second half of the counting sort: d_count holds the per-cell counts and
 // d_key/d_rank each list entry's cell and rank in it; lays out buffer cur with
 // slack and scatters the list buffer (cur^1) into it.  The restart reader
 // fills the ranks itself, so that each cell keeps the list order of the file.
-cudaError_t place_ranked(amps_gpu_ctx* c, long long n) {
+cudaError_t place_ranked(amps_gpu_ctx* c, long long n, bool demand) {
   cudaStream_t s = c->stream;
   const long long nc = c->ncor;
+  const unsigned grid = (unsigned)((nc + 1 + 255) / 256);
   cudaError_t e;
-  // slack scaled so that sum(cap) <= slots: sum(cap) <= n + n/4 + AMPS_SLACK_MIN nc
+  // base slack scaled so that sum(cap) <= slots: sum(cap) <= n + n/4 + AMPS_SLACK_MIN nc
   const long long worst = n + n / 4 + (long long)AMPS_SLACK_MIN * nc;
-  int num = 1, den = 1;
-  if (worst > c->slots) {
-    num = (int)std::max(0LL, (c->slots - n) / 1024);
-    den = (int)std::max(1LL, (worst - n) / 1024 + 1);
+  auto scale = [&](long long room, int& num, int& den) {
+    num = 1;
+    den = 1;
+    if (worst - n > room) {
+      num = (int)std::max(0LL, room / 1024);
+      den = (int)std::max(1LL, (worst - n) / 1024 + 1);
+    }
+  };
+  int num, den;
+  scale(c->slots - n, num, den);
+  // the overflowed cells' demand (d_arr) as extra slack: its total E is read
+  // back, and the base slack shrinks to the room left (n + base + E <= slots)
+  // while E takes at most half of the room; beyond that it is dropped
+  const int* dem = nullptr;
+  if (demand) {
+    {
+      TimedLaunch t(c, "rebuild");
+      k_rb_caps<<<grid, 256, 0, s>>>(nc, c->d_count, c->d_tmp, 1, 1, c->d_arr, false);
+    }
+    e = scan_ints(c, c->d_tmp, c->d_base, nc + 1);
+    int extra = -1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&extra, c->d_base + nc, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    const long long room = c->slots - n;
+    if (extra >= 0 && 2LL * extra <= room) {
+      dem = c->d_arr;
+      scale(room - extra, num, den);
+    }
   }
   {
     TimedLaunch t(c, "rebuild");
-    k_rb_caps<<<(unsigned)((nc + 1 + 255) / 256), 256, 0, s>>>(nc, c->d_count, c->d_tmp, num, den);
+    k_rb_caps<<<grid, 256, 0, s>>>(nc, c->d_count, c->d_tmp, num, den, dem, true);
   }
   e = scan_ints(c, c->d_tmp, c->d_base, nc + 1);
   if (e != cudaSuccess) return e;
@@ -1854,7 +1891,7 @@ cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow) {
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return rebuild_from_list(c, c->np);
+  return rebuild_from_list(c, c->np, true);
 }
 
 // Relativistic Boris move of every particle: compact layout -> list buffer,

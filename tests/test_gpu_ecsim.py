@@ -251,3 +251,31 @@ def test_many_steps_layout_invariants():
     ctx.UpdateJMassMatrix()
     J2, M2 = ctx.export_moments()
     assert G.rel_err(J1, J2) <= 2e-6 and G.rel_err(M1, M2) <= 2e-6
+
+
+def test_overflowed_cells_get_demand_slack():
+    """At vscale 40 nearly every particle changes cell each step: a cell of 64
+    receives ~64 arrivals, more than the count/4 + 32 slack of a rebuild.  The
+    first step overflows and is recovered; the recovery sizes each overflowed
+    cell's slack by its arrivals, so the next steps fit (one recovery in four
+    steps).  The layout stays valid and the fused moments equal a fresh
+    deposit of it."""
+    wl, ic, x, f = G.make_case(ppc=32, vscale=40.0)
+    n = len(ic["spec"])
+    ctx = G.gpu_ctx(wl, ic, x, f, capacity=10 * n)
+    ctx.set_kernel_timing(True)
+    for _ in range(4):
+        ctx.push_deposit(want_energy=False)
+    rec = ctx.kernel_times().get("recover", (0.0, 0))[1]
+    ctx.set_kernel_timing(False)
+    assert rec == 1, rec
+    g = ctx.export_particles()
+    np.testing.assert_array_equal(np.sort(g["id"]), np.arange(n))
+    org = A.block_origins(wl.mesh, g["block"])
+    ci = np.stack([g["cell"] % 8, (g["cell"] // 8) % 8, g["cell"] // 64], 1)
+    lo = org + ci * wl.mesh.dx
+    assert np.all(g["x"] >= lo - 1e-12) and np.all(g["x"] < lo + wl.mesh.dx + 1e-12)
+    J1, M1 = ctx.export_moments()
+    ctx.UpdateJMassMatrix()
+    J2, M2 = ctx.export_moments()
+    assert G.rel_err(J1, J2) <= 2e-6 and G.rel_err(M1, M2) <= 2e-6
