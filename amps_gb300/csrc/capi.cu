@@ -258,16 +258,15 @@ amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_b
                       "particle step")))
     return s;
   long long ovf = 0;
-  if ((s = read_step_flags(c, out_of_block, near_face, &ovf))) {
-    // no recovery: drop the overflowed cells' arrival counts it would have used
-    cudaMemsetAsync(c->d_arr, 0, sizeof(int) * c->ncor, c->stream);
-    return s;
-  }
+  if ((s = read_step_flags(c, out_of_block, near_face, &ovf))) return s;
   if (ovf > 0) {
-    // rare: some cell ran out of slack.  Re-sort everything (new slack) and
-    // redo the deposition from the rebuilt layout.
-    if ((s = cuda_check(c, particles_recover(c, ovf), "overflow recovery"))) return s;
-    if (deposit && (s = cuda_check(c, launch_deposit(c), "deposit"))) return s;
+    // some cell ran out of slack: the overflowed arrivals are deposited and
+    // go to the slots their cells' movers vacated; when a cell is full the
+    // layout is rebuilt from itself with new slack
+    long long left = 0;
+    if ((s = cuda_check(c, particles_place_overflow(c, ovf, deposit, &left), "overflow placement")))
+      return s;
+    if (left > 0 && (s = cuda_check(c, particles_relayout(c, ovf), "overflow relayout"))) return s;
     if ((s = check_flags(c, nullptr, nullptr, nullptr))) return s;
   }
   if (deposit && (s = cuda_check(c, launch_species_moments(c), "species moments"))) return s;

@@ -254,15 +254,17 @@ cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, d
 cudaError_t launch_deposit(amps_gpu_ctx* c);
 void set_next_id(amps_gpu_ctx* c, long long n);
 // counting sort of the list buffer into the slotted layout (keys in d_key)
-cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n, bool demand = false);
+cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n);
 // its placement half: d_count, d_key and d_rank already filled
-cudaError_t place_ranked(amps_gpu_ctx* c, long long n, bool demand = false);
+cudaError_t place_ranked(amps_gpu_ctx* c, long long n);
 // species moments on corners (species.cu)
 amps_gpu_status species_setup(amps_gpu_ctx* c, bool on);
 void species_free(amps_gpu_ctx* c);
 amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M);
 cudaError_t launch_species_moments(amps_gpu_ctx* c);
-cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow);
+cudaError_t particles_place_overflow(amps_gpu_ctx* c, long long n_overflow, bool deposit,
+                                     long long* left);
+cudaError_t particles_relayout(amps_gpu_ctx* c, long long n_overflow);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
                                const uint8_t* d_spec_in, const double* d_wc, long long n);
 cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* d_v,

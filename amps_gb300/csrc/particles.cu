@@ -671,11 +671,9 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   if (threadIdx.x < kLayer) {
     const long long cl = (long long)b * AMPS_CPB + threadIdx.x + kLayer * k;
     const int b0 = a.base[cl], cap = a.base[cl + 1] - b0, n0 = a.cnt[cl], nst = a.stay[cl];
-    const int dem = a.arr[cl], na = min(dem, cap - n0);
+    const int na = min(a.arr[cl], cap - n0);
     a.cnt[cl] = nst + max(0, na);
-    // a cell whose arrivals overflowed its slack keeps their number: the
-    // recovery that follows sizes its new slack by it (and clears it)
-    a.arr[cl] = dem > cap - n0 ? dem : 0;
+    a.arr[cl] = 0;
     has = na > 0;
     cv = make_int4(threadIdx.x, b0 + cap - na, b0 + nst, na);
   }
@@ -742,6 +740,137 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     if (DEP) tile.flush_red(lane, rec, a.cellM, a.cellJ, cid);
   }
   if (DEP) reduce_energy(ff_value(en_w), s_en, a.energy);
+}
+
+// Overflow entries into the slots their cell's movers vacated.  The push and
+// the arrivals give arrivals only a cell's slack (the slots past its occupancy
+// at the start of the step), so a cell can overflow while the particles that
+// left it freed slots; after the arrivals a cell's first cnt slots hold its
+// particles and the rest of its range is free.  One warp per entry: a free
+// slot is reserved on cnt, the particle written there and the entry's key set
+// to -1.  Entries whose cell is full are counted in *left and stay in the list
+// for the relayout, which files them in the same cell.  Every entry is
+// deposited here like an arrival (DEP).
+template <bool DEP>
+__global__ void __launch_bounds__(256) k_ovf_place(StepArgs a, long long n_ovf,
+                                                   unsigned long long* left) {
+  extern __shared__ __align__(16) float4 s_dyn[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long long e = (long long)blockIdx.x * kWarps + wid;
+  if (e >= n_ovf) return;  // the whole warp: no block-wide barrier follows
+  const int key = a.ovf_key[e];
+  const int b0 = a.base[key], cap = a.base[key + 1] - b0;
+  int slot = 0;
+  if (lane == 0) {
+    slot = atomicAdd(a.cnt + key, 1);
+    if (slot >= cap) atomicSub(a.cnt + key, 1);  // cnt never falls below cap again
+  }
+  slot = __shfl_sync(0xffffffffu, slot, 0);
+  const bool fits = slot < cap;
+  if (!fits && lane == 0) atomicAdd(left, 1ull);
+  float u[3], v[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) { u[d] = a.ovf.u[d][e]; v[d] = a.ovf.v[d][e]; }
+  const int s = a.ovf.sp[e];
+  const float wcv = a.ovf.wc ? a.ovf.wc[e] : 1.0f;
+  if (fits && lane == 0) {
+    const long long d = (long long)b0 + slot;
+#pragma unroll
+    for (int q = 0; q < 3; q++) { a.p.u[q][d] = u[q]; a.p.v[q][d] = v[q]; }
+    a.p.sp[d] = (uint8_t)s;
+    if (a.p.wc) a.p.wc[d] = wcv;
+    if (a.p.id) a.p.id[d] = a.ovf.id[e];
+    a.ovf_key[e] = -1;
+  }
+  if (DEP) {
+    float* rec = reinterpret_cast<float*>(s_dyn) + wid * kFields * kFSArr;
+    int fA, fB;
+    lane_fields(lane, fA, fB);
+    const int b = key / AMPS_CPB, l = key % AMPS_CPB;
+    const float4* s_dep = reinterpret_cast<const float4*>(a.st_dep) + (size_t)b * AMPS_SC;
+    FF en{0.f, 0.f};
+    // the particle at position 0, zero weight at positions 1..3
+    if (lane < 4)
+      stage_fields<kFSArr>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+                           lane == 0 ? wcv : 0.f, l & (AMPS_NC - 1), (l / AMPS_NC) & (AMPS_NC - 1),
+                           l / (AMPS_NC * AMPS_NC), a.st, block_inv_vol(a, b), en);
+    __syncwarp();
+    Tile tile;
+    tile.zero();
+    tile.accumulate<kFSArr>(rec, 4, fA, fB);
+    __syncwarp();
+    tile.flush_red(lane, rec, a.cellM, a.cellJ, key);
+    if (lane == 0) atomicAdd(a.energy, ff_value(en));
+  }
+}
+
+// Relayout kernels (particles_relayout): the unplaced overflow entries (key
+// >= 0) counted per cell; one warp per cell copying its particles to the new
+// offsets (pad + newb[c]); the unplaced entries behind them.
+__global__ void __launch_bounds__(256) k_ovf_count(long long n_ovf, const int* __restrict__ key,
+                                                   int* __restrict__ count) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n_ovf && key[e] >= 0) atomicAdd(count + key[e], 1);
+}
+
+// Each lane loads its kRelayoutRound particles of a round before it stores any
+// (the source and destination buffers are distinct): the copy is bound by the
+// loads in flight, and one particle per lane at a time ran at a third of the
+// rate (1.5 against 4.3 TB/s on 584M particles).
+constexpr int kRelayoutRound = 4;
+__global__ void __launch_bounds__(256) k_relayout_cells(long long ncell, const int* __restrict__ base,
+                                                        const int* __restrict__ cnt,
+                                                        const int* __restrict__ newb, long long pad,
+                                                        PBuf s, PBuf d) {
+  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= ncell) return;
+  const long long ob = base[c], nb = pad + newb[c];
+  const int n = cnt[c];
+  for (int q0 = 0; q0 < n; q0 += 32 * kRelayoutRound) {
+    float u[kRelayoutRound][3], v[kRelayoutRound][3], w[kRelayoutRound];
+    uint32_t id[kRelayoutRound];
+    uint8_t sp[kRelayoutRound];
+#pragma unroll
+    for (int r = 0; r < kRelayoutRound; r++) {
+      const long long q = q0 + 32 * r + lane;
+      if (q < n) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) { u[r][k] = __ldg(s.u[k] + ob + q); v[r][k] = __ldg(s.v[k] + ob + q); }
+        sp[r] = __ldg(s.sp + ob + q);
+        w[r] = s.wc ? __ldg(s.wc + ob + q) : 0.f;
+        id[r] = s.id ? __ldg(s.id + ob + q) : 0u;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kRelayoutRound; r++) {
+      const long long q = q0 + 32 * r + lane;
+      if (q < n) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) { d.u[k][nb + q] = u[r][k]; d.v[k][nb + q] = v[r][k]; }
+        d.sp[nb + q] = sp[r];
+        if (d.wc) d.wc[nb + q] = w[r];
+        if (d.id) d.id[nb + q] = id[r];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_ovf_file(long long n_ovf, const int* __restrict__ key,
+                                                  const int* __restrict__ newb, long long pad,
+                                                  int* __restrict__ fill, PBuf b) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_ovf) return;
+  const int k = key[e];
+  if (k < 0) return;  // placed in a vacated slot
+  const int slot = atomicAdd(fill + k, 1);
+  copy_particle(b, e, b, pad + newb[k] + slot);
+}
+
+__global__ void __launch_bounds__(256) k_offset_copy(long long n, const int* __restrict__ src,
+                                                     long long off, int* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (int)(off + src[i]);
 }
 
 // Full deposition over the compact layout.
@@ -944,23 +1073,14 @@ __global__ void __launch_bounds__(256) k_rb_rank(long long n, const int* __restr
 // The constant term keeps sparsely filled cells (fine AMR levels) from
 // overflowing: a cell's occupancy random-walks by ~sqrt(2 x crossings) per
 // step, and over 10^5 cells the largest excursion reaches ~4.5 of those.
-// dem (optional): the arrivals of cells that overflowed in the last step; such
-// a cell gets kDemandSlack times that many extra slots.  A steady inflow does
-// this: on meshes whose particle weights scale with the level, light particles
-// stream from a finer level into the coarse cells along the interface at 8x the
-// number rate per level of difference, and those cells keep growing.
-// base = false: the extra slots alone (their total sizes the base slack).
-constexpr int kDemandSlack = 8;
 __global__ void __launch_bounds__(256) k_rb_caps(long long ncell, const int* __restrict__ count,
-                                                 int* __restrict__ cap, int num, int den,
-                                                 const int* __restrict__ dem, bool base) {
+                                                 int* __restrict__ cap, int num, int den) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c > ncell) return;
   if (c == ncell) { cap[c] = 0; return; }
   const int n = count[c];
   const int slack = (n >> 2) + AMPS_SLACK_MIN;
-  cap[c] = (base ? n + (int)(((long long)slack * num) / den) : 0) +
-           (dem ? kDemandSlack * dem[c] : 0);
+  cap[c] = n + (int)(((long long)slack * num) / den);
 }
 
 __global__ void __launch_bounds__(256) k_rb_scatter(long long n, const int* __restrict__ key,
@@ -1649,7 +1769,7 @@ cudaError_t scan_ints(amps_gpu_ctx* c, const int* in, int* out, long long n) {
 
 // Counting sort of the list buffer (cur^1, keys in d_key) with n particles into
 // the slotted layout of buffer cur.
-cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n, bool demand) {
+cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n) {
   cudaStream_t s = c->stream;
   const long long nc = c->ncor;
   cudaError_t e = cudaMemsetAsync(c->d_count, 0, sizeof(int) * (nc + 1), s);
@@ -1658,53 +1778,27 @@ cudaError_t rebuild_from_list(amps_gpu_ctx* c, long long n, bool demand) {
     TimedLaunch t(c, "rebuild");
     k_rb_rank<<<grid_for(n, 256), 256, 0, s>>>(n, c->d_key, c->d_rank, c->d_count);
   }
-  return place_ranked(c, n, demand);
+  return place_ranked(c, n);
 }
 
 // Second half of the counting sort: d_count holds the per-cell counts and
 // d_key/d_rank each list entry's cell and rank in it; lays out buffer cur with
 // slack and scatters the list buffer (cur^1) into it.  The restart reader
 // fills the ranks itself, so that each cell keeps the list order of the file.
-cudaError_t place_ranked(amps_gpu_ctx* c, long long n, bool demand) {
+cudaError_t place_ranked(amps_gpu_ctx* c, long long n) {
   cudaStream_t s = c->stream;
   const long long nc = c->ncor;
-  const unsigned grid = (unsigned)((nc + 1 + 255) / 256);
   cudaError_t e;
-  // base slack scaled so that sum(cap) <= slots: sum(cap) <= n + n/4 + AMPS_SLACK_MIN nc
+  // slack scaled so that sum(cap) <= slots: sum(cap) <= n + n/4 + AMPS_SLACK_MIN nc
   const long long worst = n + n / 4 + (long long)AMPS_SLACK_MIN * nc;
-  auto scale = [&](long long room, int& num, int& den) {
-    num = 1;
-    den = 1;
-    if (worst - n > room) {
-      num = (int)std::max(0LL, room / 1024);
-      den = (int)std::max(1LL, (worst - n) / 1024 + 1);
-    }
-  };
-  int num, den;
-  scale(c->slots - n, num, den);
-  // the overflowed cells' demand (d_arr) as extra slack: its total E is read
-  // back, and the base slack shrinks to the room left (n + base + E <= slots)
-  // while E takes at most half of the room; beyond that it is dropped
-  const int* dem = nullptr;
-  if (demand) {
-    {
-      TimedLaunch t(c, "rebuild");
-      k_rb_caps<<<grid, 256, 0, s>>>(nc, c->d_count, c->d_tmp, 1, 1, c->d_arr, false);
-    }
-    e = scan_ints(c, c->d_tmp, c->d_base, nc + 1);
-    int extra = -1;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&extra, c->d_base + nc, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
-    const long long room = c->slots - n;
-    if (extra >= 0 && 2LL * extra <= room) {
-      dem = c->d_arr;
-      scale(room - extra, num, den);
-    }
+  int num = 1, den = 1;
+  if (worst > c->slots) {
+    num = (int)std::max(0LL, (c->slots - n) / 1024);
+    den = (int)std::max(1LL, (worst - n) / 1024 + 1);
   }
   {
     TimedLaunch t(c, "rebuild");
-    k_rb_caps<<<grid, 256, 0, s>>>(nc, c->d_count, c->d_tmp, num, den, dem, true);
+    k_rb_caps<<<(unsigned)((nc + 1 + 255) / 256), 256, 0, s>>>(nc, c->d_count, c->d_tmp, num, den);
   }
   e = scan_ints(c, c->d_tmp, c->d_base, nc + 1);
   if (e != cudaSuccess) return e;
@@ -1766,7 +1860,8 @@ cudaError_t launch_deposit(amps_gpu_ctx* c) {
 }
 
 // Push (+ deposit) of one step: k_push_deposit, k_arrivals (+ assemble).
-// Overflow recovery is done by the caller (particles_recover).
+// Overflow recovery is done by the caller (particles_place_overflow,
+// particles_relayout).
 // ids of injected particles continue after the imported ones (0..n-1)
 void set_next_id(amps_gpu_ctx* c, long long n) {
   c->next_id = (uint32_t)n;
@@ -1875,23 +1970,84 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
   return cudaSuccess;
 }
 
-// After an overflow (n_overflow particles already in the list buffer with
-// their keys): append the compact layout behind them and rebuild.
-cudaError_t particles_recover(amps_gpu_ctx* c, long long n_overflow) {
-  c->h_flags[3] = (unsigned long long)n_overflow;
-  cudaError_t e = cudaMemcpyAsync(c->d_flags + 4, c->h_flags + 3, sizeof(unsigned long long),
-                                  cudaMemcpyHostToDevice, c->stream);
+// Overflow entries into the slots vacated in their cells (k_ovf_place); *left
+// receives the number that found their cell full.  With the deposit, the
+// uniform mesh's corner moments are assembled again.
+cudaError_t particles_place_overflow(amps_gpu_ctx* c, long long n_overflow, bool deposit,
+                                     long long* left) {
+  cudaError_t e = cudaMemsetAsync(c->d_flags + 7, 0, sizeof(unsigned long long), c->stream);
   if (e != cudaSuccess) return e;
   {
-    TimedLaunch t(c, "recover");
-    const long long threads = c->ncor * 32;
-    k_gather_valid<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
-        c->ncor, c->d_base, c->d_cnt, pbuf(c, c->cur), pbuf(c, c->cur ^ 1), c->d_key,
-        c->d_flags + 4);
+    TimedLaunch t(c, "overflow_place");
+    const unsigned grid = (unsigned)((n_overflow + kWarps - 1) / kWarps);
+    if (deposit)
+      k_ovf_place<true><<<grid, kWarps * 32, smem_arr(), c->stream>>>(step_args(c), n_overflow,
+                                                                      c->d_flags + 7);
+    else
+      k_ovf_place<false><<<grid, kWarps * 32, 0, c->stream>>>(step_args(c), n_overflow,
+                                                             c->d_flags + 7);
   }
   e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->h_flags + 7, c->d_flags + 7, sizeof(unsigned long long),
+                        cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return e;
-  return rebuild_from_list(c, c->np, true);
+  *left = (long long)c->h_flags[7];
+  // the step assembled the corner moments before the overflow was deposited
+  return deposit ? launch_assemble(c) : cudaSuccess;
+}
+
+// Relayout after an overflow that the vacated slots did not absorb: every
+// cell's particles are copied from the slotted layout into the other buffer at
+// new offsets (its count plus its unplaced overflow entries, plus slack), the
+// unplaced entries filed behind them, and the buffers swapped.  The overflow
+// list occupies the first n_overflow slots of the other buffer, so the new
+// layout starts past it (pad) and those slots become holes.  Nothing is
+// gathered or re-sorted, and no deposit is redone: k_ovf_place deposited
+// every overflow entry.
+cudaError_t particles_relayout(amps_gpu_ctx* c, long long n_overflow) {
+  cudaStream_t s = c->stream;
+  const long long nc = c->ncor, n = c->np;
+  const long long pad = (n_overflow + 127) & ~127LL;
+  const long long room = c->slots - pad - n;
+  if (room < 0) return cudaErrorMemoryAllocation;
+  const int other = c->cur ^ 1;
+  cudaError_t e = cudaMemcpyAsync(c->d_count, c->d_cnt, sizeof(int) * nc, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return e;
+  // slack scaled so that pad + sum(cap) <= slots
+  const long long worst = n + n / 4 + (long long)AMPS_SLACK_MIN * nc;
+  int num = 1, den = 1;
+  if (worst - n > room) {
+    num = (int)std::max(0LL, room / 1024);
+    den = (int)std::max(1LL, (worst - n) / 1024 + 1);
+  }
+  {
+    TimedLaunch t(c, "relayout_aux", 2);
+    k_ovf_count<<<grid_for(n_overflow, 256), 256, 0, s>>>(n_overflow, c->d_key, c->d_count);
+    k_rb_caps<<<(unsigned)((nc + 1 + 255) / 256), 256, 0, s>>>(nc, c->d_count, c->d_tmp, num, den);
+  }
+  e = scan_ints(c, c->d_tmp, c->d_rank, nc + 1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_sp[other] + pad, 0xFF, (size_t)(c->slots - pad), s);
+  if (e != cudaSuccess) return e;
+  {
+    TimedLaunch t(c, "relayout");
+    const long long threads = nc * 32;
+    k_relayout_cells<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        nc, c->d_base, c->d_cnt, c->d_rank, pad, pbuf(c, c->cur), pbuf(c, other));
+  }
+  {
+    TimedLaunch t(c, "relayout_aux", 2);
+    k_ovf_file<<<grid_for(n_overflow, 256), 256, 0, s>>>(n_overflow, c->d_key, c->d_rank, pad,
+                                                         c->d_cnt, pbuf(c, other));
+    k_offset_copy<<<(unsigned)((nc + 1 + 255) / 256), 256, 0, s>>>(nc + 1, c->d_rank, pad,
+                                                                   c->d_base);
+  }
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_sp[other], 0xFF, (size_t)pad, s);
+  if (e != cudaSuccess) return e;
+  c->cur = other;
+  return cudaSuccess;
 }
 
 // Relativistic Boris move of every particle: compact layout -> list buffer,

@@ -253,22 +253,9 @@ def test_many_steps_layout_invariants():
     assert G.rel_err(J1, J2) <= 2e-6 and G.rel_err(M1, M2) <= 2e-6
 
 
-def test_overflowed_cells_get_demand_slack():
-    """At vscale 40 nearly every particle changes cell each step: a cell of 64
-    receives ~64 arrivals, more than the count/4 + 32 slack of a rebuild.  The
-    first step overflows and is recovered; the recovery sizes each overflowed
-    cell's slack by its arrivals, so the next steps fit (one recovery in four
-    steps).  The layout stays valid and the fused moments equal a fresh
-    deposit of it."""
-    wl, ic, x, f = G.make_case(ppc=32, vscale=40.0)
-    n = len(ic["spec"])
-    ctx = G.gpu_ctx(wl, ic, x, f, capacity=10 * n)
-    ctx.set_kernel_timing(True)
-    for _ in range(4):
-        ctx.push_deposit(want_energy=False)
-    rec = ctx.kernel_times().get("recover", (0.0, 0))[1]
-    ctx.set_kernel_timing(False)
-    assert rec == 1, rec
+def check_layout_and_moments(ctx, wl, n):
+    """every id once, each particle inside the cell it is filed under, fused
+    moments equal to a fresh deposit of the layout"""
     g = ctx.export_particles()
     np.testing.assert_array_equal(np.sort(g["id"]), np.arange(n))
     org = A.block_origins(wl.mesh, g["block"])
@@ -279,3 +266,80 @@ def test_overflowed_cells_get_demand_slack():
     ctx.UpdateJMassMatrix()
     J2, M2 = ctx.export_moments()
     assert G.rel_err(J1, J2) <= 2e-6 and G.rel_err(M1, M2) <= 2e-6
+
+
+def row_case(name, cells, seed=5):
+    """protons placed cell by cell: cells = [(ix, count, vx)] in the row
+    (iy, iz) = (4, 4), offsets in [0.3, 0.7) of a cell, unperturbed fields"""
+    wl = A.electron_proton_plasma(name, 2, 2, 2, 1, 3)
+    rng = np.random.default_rng(seed)
+    dx = wl.mesh.dx
+    xs, vs = [], []
+    for ix, m, vx in cells:
+        off = rng.uniform(0.3, 0.7, (m, 3))
+        xs.append((np.array([ix, 4, 4]) + off) * dx)
+        vs.append(np.tile([vx, 0.0, 0.0], (m, 1)))
+    x = np.concatenate(xs)
+    v = np.concatenate(vs).astype(np.float32)
+    ic = {"v": v, "spec": np.ones(len(x), np.uint8)}
+    return wl, ic, x, A.initial_fields(wl)
+
+
+def steps_match_oracle(ctx, st, steps):
+    for _ in range(steps):
+        ctx.push_deposit(want_energy=False)
+        st.push()
+        st.deposit()
+        compare_particles(ctx, st)
+        J, M = ctx.export_moments()
+        assert G.rel_err(J, st.J) <= 1e-5 and G.rel_err(M, st.M) <= 1e-5
+
+
+def test_overflow_fills_vacated_slots():
+    """A periodic row of 16 cells, each with 30 protons at rest and 100 moving
+    exactly one cell per step along x (the proton gyration is 0.002 rad per
+    step).  Every cell receives 100 arrivals, more than its count/4 + 32 slack,
+    while its own 100 leave: every step overflows, and every overflowed
+    particle goes to a vacated slot and is deposited there (no relayout).
+    Positions, J and M match the oracle after every step; the layout stays
+    valid."""
+    wl, ic, x, f = row_case("row", [(i, 30, 0.0) for i in range(16)] +
+                            [(i, 100, 10.0) for i in range(16)])
+    assert wl.mesh.dx / wl.dt == 10.0
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    st = G.oracle_state(wl, ic, x, f)
+    ctx.set_kernel_timing(True)
+    steps_match_oracle(ctx, st, 4)
+    kt = ctx.kernel_times()
+    ctx.set_kernel_timing(False)
+    assert kt.get("overflow_place", (0.0, 0))[1] == 4, kt
+    assert kt.get("relayout", (0.0, 0))[1] == 0, kt
+    check_layout_and_moments(ctx, wl, len(x))
+
+
+def test_overflow_into_full_cells_rebuilds():
+    """A conveyor: 64 protons at rest in cell (10, 4, 4) and 100 in each of the
+    six cells behind it along x, moving exactly one cell per step (unperturbed
+    fields; the proton gyration is 0.002 rad per step).  Every step the
+    conveyor's front moves 100 particles into a cell with no vacated slots and
+    fewer free slots (count/4 + 32), so the overflow cannot be placed and the
+    layout is rebuilt from itself (particle buffers swapped): four relayouts in
+    four steps.  Positions, J and M match the oracle after every step."""
+    wl, ic, x, f = row_case("conveyor", [(10, 64, 0.0)] + [(10 - k, 100, 10.0) for k in range(1, 7)])
+    dx = wl.mesh.dx
+    n = len(x)
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    st = G.oracle_state(wl, ic, x, f)
+    ctx.set_kernel_timing(True)
+    steps_match_oracle(ctx, st, 4)
+    kt = ctx.kernel_times()
+    ctx.set_kernel_timing(False)
+    assert kt.get("relayout", (0.0, 0))[1] == 4, kt
+    g = ctx.export_particles()
+    ix = np.floor(g["x"][:, 0] / dx).astype(int)
+    # the six moving columns now in cells 8..13, the resting 64 in cell 10
+    expect = np.zeros(16, int)
+    expect[8:14] = 100
+    expect[10] += 64
+    np.testing.assert_array_equal(np.bincount(ix, minlength=16), expect)
+    check_layout_and_moments(ctx, wl, n)
