@@ -865,14 +865,14 @@ def run_reference(args):
         times, n, m, ntot = reference_amr_workload(args.workload, threads, args.steps, args.warmup,
                                              args.ref_budget)
         value = n * len(times) / sum(times)
-        part = ("all %d particles" % n if m == 1 else
-                "the %d particles of one block in %d (%.3g of the workload)"
-                % (n, m, n / ntot))
+        part = ("all %d particles of %s, pushed, and ProcessCell of every block"
+                % (n, args.workload) if m == 1 else
+                "the %d particles of one block in %d of %s (%.3g of the workload), pushed, and "
+                "those blocks' ProcessCell" % (n, m, args.workload, n / ntot))
         sample = ("FP64 AMR oracle (Lapenta2017 + re-binning across levels + ProcessCell, pinned to "
                   "the reference's compiled ProcessCell/Lapenta2017) on %d host threads (push over "
-                  "particle ranges, deposit over block ranges): per step %s of %s, pushed, and "
-                  "those blocks' ProcessCell, %.2f s per step" %
-                  (threads, part, args.workload, sum(times) / len(times)))
+                  "particle ranges, deposit over block ranges): per step %s, %.2f s per step" %
+                  (threads, part, sum(times) / len(times)))
         same = True
     else:
         rates = []
