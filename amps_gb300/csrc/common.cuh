@@ -148,6 +148,14 @@ struct amps_gpu_ctx {
     cudaGraphExec_t exec;
   };
   std::vector<StepGraph> graphs;
+  // the first GMRES cycle of a solve as a graph (gmres_solve), keyed by the
+  // preconditioner, the Arnoldi steps and the launch shapes it was captured with
+  struct SolveGraph {
+    int precond, steps, tb, red, ept;
+    cudaGraphExec_t exec;
+  };
+  std::vector<SolveGraph> solve_graphs;
+  bool solve_graphs_off = false;  // a capture failed: solves stay eager
   double* d_red = nullptr;      // partial reductions
   double* d_arn = nullptr;      // per-CTA partial sums of the cooperative Arnoldi step
   float* d_xs = nullptr;        // FP32 pair split (hi, lo) of an operator input, 2 x 3*nvc

@@ -354,6 +354,7 @@ struct GmState {
   double target;
   int jj;    // columns processed in this cycle
   int done;  // |g[jj]| <= target, or breakdown
+  double bn2, rn2;  // graph cycle (k_gm_first, k_gm_status): ||b||^2, end-of-cycle ||r||^2
 };
 static_assert(kGmOffset * sizeof(double) + sizeof(GmState) <= 12288 * sizeof(double),
               "GmState must fit in d_red");
@@ -367,6 +368,25 @@ __global__ void k_gm_start(GmState* __restrict__ S, const double* __restrict__ n
   S->target = target;
   S->jj = 0;
   S->done = 0;
+}
+
+// start of the first cycle from x0 = 0 (r = b): g = (||b||, 0, ...), target
+// tol ||b|| on the device; keeps ||b||^2 for the host's single read
+__global__ void k_gm_first(GmState* __restrict__ S, const double* __restrict__ n2, double tol) {
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i <= kMaxV; i++) S->g[i] = 0.0;
+  const double b2 = *n2;
+  S->g[0] = sqrt(b2);
+  S->target = tol * sqrt(b2);
+  S->jj = 0;
+  S->done = 0;
+  S->bn2 = b2;
+  S->rn2 = -1.0;
+}
+
+// end of the graph cycle: the true residual's ||r||^2 next to jj, done, ||b||^2
+__global__ void k_gm_status(GmState* __restrict__ S, const double* __restrict__ n2) {
+  if (threadIdx.x == 0) S->rn2 = *n2;
 }
 
 // Arnoldi column jj: h = h1 + h2 (the two CGS passes), h[jj+1] = ||w||; apply
@@ -1072,11 +1092,7 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
 
   if (!c->d_arn)
     CK(cudaMalloc(reinterpret_cast<void**>(&c->d_arn), sizeof(double) * 3 * kArnMaxGrid * kMaxV));
-  const double* dinv = nullptr;
-  if (precond >= 1) {
-    CK(launch_jacobi_diag(c));
-    dinv = c->d_dinv;
-  }
+  const double* dinv = precond >= 1 ? c->d_dinv : nullptr;
   const bool flexible = precond == 2;
   if (flexible && !c->d_Z)
     return set_err(c, AMPS_GPU_INVALID_ARG, "learned preconditioner: no network loaded");
@@ -1089,7 +1105,6 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   const float* dl = nullptr;
   if (dinv) {
     if (!c->d_dff) CK(cudaMalloc(reinterpret_cast<void**>(&c->d_dff), sizeof(float) * 2 * n));
-    k_dff<<<gr, 256, 0, s>>>(n, dinv, c->d_dff);
     dh = c->d_dff;
     dl = c->d_dff + n;
   }
@@ -1128,25 +1143,146 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     k_to_ff<<<gr, 256, 0, s>>>(n, c->d_tmpv + n, wf);
     return cudaGetLastError();
   };
-  auto read_norm = [&](const double* v, double* out) -> cudaError_t {
+  auto norm_to = [&](const double* v) {
     k_norm2<<<gr, 256, 0, s>>>(n, v, partial);
     k_reduce_partials<<<1, 32, 0, s>>>(partial, gr, 1, d_n2, nullptr);
+  };
+  auto read_norm = [&](const double* v, double* out) -> cudaError_t {
+    norm_to(v);
     cudaError_t ee = cudaMemcpyAsync(c->h_red, d_n2, sizeof(double), cudaMemcpyDeviceToHost, s);
     if (ee != cudaSuccess) return ee;
     ee = cudaStreamSynchronize(s);
     *out = std::sqrt(c->h_red[0]);
     return ee;
   };
-  CK(cudaMemsetAsync(c->d_x, 0, sizeof(double) * n, s));
-  double bnorm = 0.0;
-  CK(read_norm(c->d_rhs, &bnorm));
+  // the Jacobi scaling, x0 = 0, r0 = b
+  auto prologue = [&]() -> cudaError_t {
+    if (dinv) {
+      cudaError_t ee = launch_jacobi_diag(c);
+      if (ee != cudaSuccess) return ee;
+      k_dff<<<gr, 256, 0, s>>>(n, dinv, c->d_dff);
+    }
+    cudaError_t ee = cudaMemsetAsync(c->d_x, 0, sizeof(double) * n, s);
+    if (ee == cudaSuccess)
+      ee = cudaMemcpyAsync(c->d_w, c->d_rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    return ee;
+  };
+  // Arnoldi step jj: the operator (after the network for flexible directions),
+  // then the cooperative CGS2 + normalisation + Givens step
+  auto arnoldi_step = [&](int jj) -> cudaError_t {
+    const int nv = jj + 1;
+    cudaError_t ee;
+    if (flexible) {
+      double* zj = c->d_Z + (size_t)jj * n;
+      k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv);  // v_j in FP64 for the network
+      if ((ee = launch_precond_net(c, c->d_tmpv, zj)) != cudaSuccess) return ee;
+      if ((ee = inner_matvec(jj, zj)) != cudaSuccess) return ee;
+    } else {
+      if ((ee = inner_matvec(jj, nullptr)) != cudaSuccess) return ee;
+      // training pairs for the learned preconditioner: (A D v_j, D v_j)
+      if (harvest) {
+        k_from_ff<<<gr, 256, 0, s>>>(n, wf, c->d_tmpv);
+        k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv + n);
+        if ((ee = precond_harvest_pairs(c, c->d_tmpv, c->d_tmpv + n, 1)) != cudaSuccess) return ee;
+      }
+    }
+    TimedLaunch t(c, "gmres_orth");
+    float* part = reinterpret_cast<float*>(c->d_arn);
+    float* vnext = vf(nv);
+    if (nv <= 4) return launch_arnoldi_ff<4>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
+    if (nv <= 8) return launch_arnoldi_ff<8>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
+    if (nv <= 16) return launch_arnoldi_ff<16>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
+    return launch_arnoldi_ff<32>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
+  };
+  // end of a cycle of at most nv_max steps: least squares, x += (D) V y, the
+  // true FP64 residual into w and its squared norm into d_n2
+  double* w = c->d_w;  // between cycles: the FP64 residual
+  auto cycle_end = [&](int nv_max) -> cudaError_t {
+    k_gm_solve<<<1, 32, 0, s>>>(gs);
+    if (flexible)
+      k_combine<<<gr, 256, 0, s>>>(n, c->d_Z, gs->y, kMaxV, &gs->jj, nullptr, c->d_x);
+    else
+      launch_combine_ff(s, gr, n, Vf, gs->y, &gs->jj, nv_max, dinv ? c->d_dff : nullptr, c->d_x);
+    cudaError_t ee = cudaGetLastError();
+    if (ee == cudaSuccess) ee = launch_matvec(c, c->d_x, nullptr, w);
+    if (ee != cudaSuccess) return ee;
+    k_residual<<<gr, 256, 0, s>>>(n, c->d_rhs, w);
+    norm_to(w);
+    return cudaGetLastError();
+  };
+
   int it = 0, cycles = 0;
   bool conv = false;
-  double rel = 0.0;
-  double* w = c->d_w;  // between cycles: the FP64 residual
-  // cycle-start residual: r = b for x = 0
-  CK(cudaMemcpyAsync(w, c->d_rhs, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  double beta = bnorm;
+  double rel = 0.0, bnorm = 0.0, beta = 0.0;
+  // The first cycle as one CUDA graph when the previous solve with this
+  // preconditioner tells how many Arnoldi steps to queue (K): prologue, ||b||
+  // and the cycle start on the device, K steps, the cycle end, one read of
+  // (steps used, converged, ||b||^2, ||r||^2).  Steps past convergence are
+  // frozen; a cycle that needed more than K steps ends as a restart.  Later
+  // cycles run as below.
+  const int K = std::max(1, std::min({c->gm_guess[precond], m, maxit}));
+  const bool graph = c->use_graphs && !c->timing && !flexible && !harvest && c->inner_fp32 &&
+                     c->gm_guess[precond] > 0 && !c->solve_graphs_off;
+  bool graph_done = false;
+  if (graph) {
+    cudaGraphExec_t exec = nullptr;
+    for (auto& g : c->solve_graphs)
+      if (g.precond == precond && g.steps == K && g.tb == c->tune_tb && g.red == c->tune_red &&
+          g.ept == c->tune_ept)
+        exec = g.exec;
+    if (!exec) {
+      cudaGraph_t gr_cap = nullptr;
+      cudaError_t ee = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+      if (ee == cudaSuccess) {
+        cudaError_t e1 = prologue();
+        if (e1 == cudaSuccess) {
+          norm_to(c->d_rhs);
+          k_gm_first<<<1, 32, 0, s>>>(gs, d_n2, tol);
+          k_start_ff<<<gr, 256, 0, s>>>(n, w, d_n2, vf(0), xf_next, dh);
+          for (int jj = 0; jj < K && e1 == cudaSuccess; jj++) e1 = arnoldi_step(jj);
+        }
+        if (e1 == cudaSuccess) e1 = cycle_end(K);
+        if (e1 == cudaSuccess) {
+          k_gm_status<<<1, 32, 0, s>>>(gs, d_n2);
+          e1 = cudaMemcpyAsync(c->h_red, &gs->jj, 2 * sizeof(int) + 2 * sizeof(double),
+                               cudaMemcpyDeviceToHost, s);
+        }
+        ee = cudaStreamEndCapture(s, &gr_cap);
+        if (ee == cudaSuccess && e1 == cudaSuccess)
+          ee = cudaGraphInstantiate(&exec, gr_cap, 0);
+        else if (ee == cudaSuccess)
+          ee = e1;
+        if (gr_cap) cudaGraphDestroy(gr_cap);
+      }
+      if (ee != cudaSuccess || !exec) {
+        // not capturable here: clear the error state of the capture, solve eagerly
+        cudaGetLastError();
+        c->solve_graphs_off = true;
+        exec = nullptr;
+      } else {
+        if (c->solve_graphs.size() >= 8) {
+          cudaGraphExecDestroy(c->solve_graphs.front().exec);
+          c->solve_graphs.erase(c->solve_graphs.begin());
+        }
+        c->solve_graphs.push_back({precond, K, c->tune_tb, c->tune_red, c->tune_ept, exec});
+      }
+    }
+    if (exec) {
+      CK(cudaGraphLaunch(exec, s));
+      CK(cudaStreamSynchronize(s));
+      const int* stat = reinterpret_cast<const int*>(c->h_red);
+      it = stat[0];
+      cycles = 1;
+      bnorm = std::sqrt(c->h_red[1]);
+      beta = std::sqrt(std::max(0.0, c->h_red[2]));
+      graph_done = true;
+    }
+  }
+  if (!graph_done) {
+    CK(prologue());
+    CK(read_norm(c->d_rhs, &bnorm));
+    beta = bnorm;
+  }
   while (true) {
     rel = bnorm > 0.0 ? beta / bnorm : 0.0;
     if (rel <= tol) {
@@ -1159,43 +1295,14 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
     // is ~1e-7 of the off-identity terms), so a cycle runs to the tolerance; a
     // later cycle only corrects what that noise left
     const double target = tol * bnorm;
-    // V0 = r / ||r|| (d_n2 holds ||r||^2 from read_norm)
+    // V0 = r / ||r|| (d_n2 holds ||r||^2)
     k_gm_start<<<1, 32, 0, s>>>(gs, d_n2, target);
     k_start_ff<<<gr, 256, 0, s>>>(n, w, d_n2, vf(0), xf_next, dh);
     int launched = 0, used = 0;
     bool done = false;
     const int first_read = cycles == 1 ? std::max(1, std::min(c->gm_guess[precond], m)) : 1;
     while (!done && launched < m && it + launched < maxit) {
-      const int jj = launched++;
-      const int nv = jj + 1;
-      if (flexible) {
-        double* zj = c->d_Z + (size_t)jj * n;
-        k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv);  // v_j in FP64 for the network
-        CK(launch_precond_net(c, c->d_tmpv, zj));
-        CK(inner_matvec(jj, zj));
-      } else {
-        CK(inner_matvec(jj, nullptr));
-        // training pairs for the learned preconditioner: (A D v_j, D v_j)
-        if (harvest) {
-          k_from_ff<<<gr, 256, 0, s>>>(n, wf, c->d_tmpv);
-          k_from_ff<<<gr, 256, 0, s>>>(n, vf(jj), c->d_tmpv + n);
-          CK(precond_harvest_pairs(c, c->d_tmpv, c->d_tmpv + n, 1));
-        }
-      }
-      {
-        TimedLaunch t(c, "gmres_orth");
-        float* part = reinterpret_cast<float*>(c->d_arn);
-        float* vnext = vf(nv);
-        if (nv <= 4)
-          e = launch_arnoldi_ff<4>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
-        else if (nv <= 8)
-          e = launch_arnoldi_ff<8>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
-        else if (nv <= 16)
-          e = launch_arnoldi_ff<16>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
-        else
-          e = launch_arnoldi_ff<32>(s, n, Vf, wf, nv, vnext, part, gs, jj, xf_next, dh);
-        if (e != cudaSuccess) return cuda_check(c, e, "arnoldi step");
-      }
+      CK(arnoldi_step(launched++));
       CK(cudaGetLastError());
       if (launched >= first_read || launched == m || it + launched >= maxit) {
         CK(cudaMemcpyAsync(c->h_red, &gs->jj, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1206,18 +1313,13 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
       }
     }
     it += used;
-    if (cycles == 1) c->gm_guess[precond] = used;
-    k_gm_solve<<<1, 32, 0, s>>>(gs);
-    if (flexible)
-      k_combine<<<gr, 256, 0, s>>>(n, c->d_Z, gs->y, kMaxV, &gs->jj, nullptr, c->d_x);
-    else
-      launch_combine_ff(s, gr, n, Vf, gs->y, &gs->jj, used, dinv ? c->d_dff : nullptr, c->d_x);
-    CK(cudaGetLastError());
-    // true residual in FP64
-    CK(launch_matvec(c, c->d_x, nullptr, w));
-    k_residual<<<gr, 256, 0, s>>>(n, c->d_rhs, w);
-    CK(read_norm(w, &beta));
+    CK(cycle_end(used));
+    CK(cudaMemcpyAsync(c->h_red, d_n2, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    beta = std::sqrt(c->h_red[0]);
   }
+  // the next solve's first cycle queues as many steps as this solve took
+  if (conv) c->gm_guess[precond] = std::max(1, std::min(it, m));
   // the solve's own pair (b, x)
   if (conv && precond == 1 && c->pn) CK(precond_harvest_pairs(c, c->d_rhs, c->d_x, 0));
 #undef CK

@@ -5,6 +5,7 @@ import pytest
 
 import amps_gb300 as A
 from tests.gpu_cases import by_id, make_case, rel_err
+from tests.test_gpu_amr import amr_case, gpu_for
 
 pytestmark = pytest.mark.gpu
 
@@ -58,3 +59,42 @@ def test_autotune_keeps_solution():
     assert st.converged and st2.converged
     for k in ("E_n", "B_center"):
         assert rel_err(out[1][k], out[0][k]) < 1e-9
+
+
+@pytest.mark.parametrize("amr", [False, True])
+@pytest.mark.parametrize("precond", [0, 1])
+def test_graph_field_solve_equals_stream_solve(amr, precond):
+    """With graphs on, a solve's first GMRES cycle runs as one CUDA graph once
+    an earlier solve told how many Arnoldi steps to queue: the same kernels in
+    the same order as the stream solve.  In one context (one mass matrix),
+    solves of the same system with graphs off and then on take the same
+    iteration counts and give the same fields: bit for bit on the uniform mesh,
+    to 1e-9 of the largest entry on the AMR mesh (its operator sums with FP32
+    atomics, whose order varies from run to run)."""
+    if amr:
+        mesh, wl, ic, x, f = amr_case(seed=29)
+        ctx = gpu_for(mesh, wl, ic, x, f)
+    else:
+        wl, ic, x, f = make_case(nb=(2, 2, 2), ppc=8, seed=47)
+        ctx = A.EcsimContext(wl, capacity=len(x) + 1024)
+        ctx.import_particles(x, ic["v"].astype(np.float64), ic["spec"])
+        ctx.import_fields(**f)
+    out = {}
+    with ctx:
+        ctx.UpdateJMassMatrix()
+        f0 = ctx.export_fields()
+        for graphs in (False, True):
+            ctx.set_graphs(graphs)
+            its = []
+            for _ in range(3):
+                ctx.import_fields(**f0)
+                st = ctx.TimeStep(tol=1e-10, maxit=200, precond=precond)
+                assert st.converged
+                its.append(st.iterations)
+            out[graphs] = (its, ctx.export_fields())
+    assert out[True][0] == out[False][0]
+    for k, v in out[False][1].items():
+        if amr:
+            assert rel_err(out[True][1][k], v) <= 1e-9, k
+        else:
+            np.testing.assert_array_equal(out[True][1][k], v, err_msg=k)
