@@ -69,6 +69,12 @@ class StepStats(C.Structure):
                 ("out_of_block", C.c_longlong), ("ulp_face", C.c_longlong)]
 
 
+class DiveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double),
+                ("gauss_before", C.c_double), ("gauss_after", C.c_double),
+                ("moved", C.c_longlong)]
+
+
 P = C.c_void_p
 D = C.POINTER(C.c_double)
 F = C.POINTER(C.c_float)
@@ -128,6 +134,8 @@ SIGNATURES = {
     "amps_gpu_move_particles_boris": (C.c_int, [P, C.c_double]),
     "amps_gpu_particle_cfl": (C.c_int, [P, C.POINTER(C.c_double)]),
     "amps_gpu_write_tecplot": (C.c_int, [P, C.c_char_p]),
+    "amps_gpu_div_e_correction": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(DiveStats)]),
+    "amps_gpu_export_div_e": (C.c_int, [P, D, D, D, D]),
     "amps_gpu_update_j_mass_matrix": (C.c_int, [P, D]),
     "amps_gpu_field_solve": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(SolveStats)]),
     "amps_gpu_step": (C.c_int, [P, C.c_double, C.c_int, C.c_int, C.POINTER(StepStats)]),

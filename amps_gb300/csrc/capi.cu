@@ -691,6 +691,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   c->graphs.clear();
   for (auto& g : c->solve_graphs) cudaGraphExecDestroy(g.exec);
   c->solve_graphs.clear();
+  cudaFree(c->d_dive);
+  c->d_dive = nullptr;
   cudaFree(c->d_hstage);
   c->d_hstage = nullptr;
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,

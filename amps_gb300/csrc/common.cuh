@@ -156,6 +156,10 @@ struct amps_gpu_ctx {
   };
   std::vector<SolveGraph> solve_graphs;
   bool solve_graphs_off = false;  // a capture failed: solves stay eager
+  // div E correction (dive.cu): per cell rho_new, rho_old, div E, phi, then the
+  // CG vectors f, r, p, Ap and the species-0 corner charge (9 x ncor doubles)
+  double* d_dive = nullptr;
+  bool dive_have_rho = false;
   double* d_red = nullptr;      // partial reductions
   double* d_arn = nullptr;      // per-CTA partial sums of the cooperative Arnoldi step
   float* d_xs = nullptr;        // FP32 pair split (hi, lo) of an operator input, 2 x 3*nvc
@@ -273,6 +277,7 @@ cudaError_t launch_species_moments(amps_gpu_ctx* c);
 cudaError_t particles_place_overflow(amps_gpu_ctx* c, long long n_overflow, bool deposit,
                                      long long* left);
 cudaError_t particles_relayout(amps_gpu_ctx* c, long long n_overflow);
+cudaError_t particles_to_list(amps_gpu_ctx* c);
 cudaError_t launch_import_fp64(amps_gpu_ctx* c, const double* d_x, const double* d_v,
                                const uint8_t* d_spec_in, const double* d_wc, long long n);
 cudaError_t launch_import_local(amps_gpu_ctx* c, const float* d_u, const float* d_v,

@@ -2050,6 +2050,19 @@ cudaError_t particles_relayout(amps_gpu_ctx* c, long long n_overflow) {
   return cudaSuccess;
 }
 
+// Every particle of the slotted layout (buffer cur) into the list buffer
+// (cur^1) with its cell as key, for a pass that moves particles and re-bins
+// them with rebuild_from_list.
+cudaError_t particles_to_list(amps_gpu_ctx* c) {
+  cudaError_t e = cudaMemsetAsync(c->d_flags + 4, 0, sizeof(unsigned long long), c->stream);
+  if (e != cudaSuccess) return e;
+  TimedLaunch t(c, "gather");
+  const long long threads = c->ncor * 32;
+  k_gather_valid<<<(unsigned)((threads + 255) / 256), 256, 0, c->stream>>>(
+      c->ncor, c->d_base, c->d_cnt, pbuf(c, c->cur), pbuf(c, c->cur ^ 1), c->d_key, c->d_flags + 4);
+  return cudaGetLastError();
+}
+
 // Relativistic Boris move of every particle: compact layout -> list buffer,
 // sub-stepped move with new keys, counting-sort rebuild.  Sub-step total in
 // flags[4] (read back by the caller).

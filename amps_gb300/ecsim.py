@@ -433,6 +433,28 @@ class EcsimContext:
         layout: FEBRICK zone, corner E, B and E^{n+theta})"""
         self._check(self.lib.amps_gpu_write_tecplot(self.h, str(path).encode()), "write_tecplot")
 
+    def div_e_correction(self, tol=1e-8, maxit=500, redeposit=True):
+        """ECSIM::divECorrection on periodic uniform meshes: net charge, div E,
+        the Poisson solve, the species-0 position correction and re-binning;
+        redeposit: UpdateJMassMatrix on the corrected particles.  Returns the
+        statistics (CG iterations and residual, the Gauss-law residual before
+        and after, particles corrected)."""
+        st = _capi.DiveStats()
+        self._check(self.lib.amps_gpu_div_e_correction(self.h, tol, maxit, 1 if redeposit else 0,
+                                                       C.byref(st)), "div_e_correction")
+        return {"iterations": st.iterations, "rel_residual": st.rel_residual,
+                "gauss_before": st.gauss_before, "gauss_after": st.gauss_after,
+                "moved": st.moved}
+
+    def export_div_e(self):
+        """per-cell rho_new, rho_old, div E and phi of the last correction"""
+        nc = self.wl.mesh.ncells
+        out = {k: np.zeros(nc) for k in ("rho_new", "rho_old", "div_e", "phi")}
+        self._check(self.lib.amps_gpu_export_div_e(
+            self.h, ptr(out["rho_new"], C.c_double), ptr(out["rho_old"], C.c_double),
+            ptr(out["div_e"], C.c_double), ptr(out["phi"], C.c_double)), "export_div_e")
+        return out
+
     def particle_cfl(self):
         """per-species maximum CFL number of the current particles (the value
         UpdateJMassMatrix prints)"""

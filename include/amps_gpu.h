@@ -211,6 +211,38 @@ amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* ctx, double* J, double* M)
  * numbers of every cell.  Periodic far faces and AMR corners get nodes at their
  * positions (values of the corner they wrap to / the unique corner). */
 amps_gpu_status amps_gpu_write_tecplot(amps_gpu_ctx* ctx, const char* path);
+
+/* div E correction (PIC::FieldSolver::Electromagnetic::ECSIM::divECorrection,
+ * src/pic/pic_field_solver_ecsim.cpp:4341-4364; the reference exits when it is
+ * switched on, :6168-6170), on periodic uniform meshes -- the reference's own
+ * restriction (:4361-4363); other contexts get AMPS_GPU_INVALID_ARG.  After a
+ * step (particles at x^{n+1}, E^n the new E): the previous net charge kept as
+ * rho_old, the net charge rho_new of the particles on the cell centres
+ * (ComputeNetCharge :4690, cell-centred linear weights), div E of the corner E
+ * at the centres (ComputeDivE :1474), the Poisson equation Laplacian(phi) =
+ * (-4 pi (g rho_new + (1-g) rho_old) + div E) / g, g = 0.51 (PoissonGetStencil
+ * :645, PoissonUpdateRhs :6023) solved by CG to ||r|| <= tol ||f|| (the mean
+ * of the right-hand side removed: the periodic null space), the species-0
+ * positions corrected by -0.9 grad phi / (4 pi rho_e) capped at 0.1 dx
+ * (CorrectParticleLocation :4440; rho_e = the species-0 charge density at the
+ * nearest corner, summed from the particles) and re-binned, rho_new again.
+ * redeposit != 0: then UpdateJMassMatrix on the corrected particles (the
+ * reference deposits after the correction).  The densities persist between
+ * calls (the first call takes rho_old = rho_new). */
+typedef struct {
+  int iterations;          /* CG iterations */
+  double rel_residual;     /* ||r|| / ||f|| of the Poisson solve */
+  double gauss_before;     /* ||div E - 4 pi (g rho_new + (1-g) rho_old)||_2 before ... */
+  double gauss_after;      /* ... and after the correction */
+  long long moved;         /* species-0 particles corrected */
+} amps_gpu_dive_stats;
+amps_gpu_status amps_gpu_div_e_correction(amps_gpu_ctx* ctx, double tol, int maxit, int redeposit,
+                                          amps_gpu_dive_stats* stats);
+/* the per-cell rho_new, rho_old, div E and phi of the last correction (each
+ * ncells doubles in the global cell order I + NX (J + NY K) of the field
+ * arrays; any may be NULL) */
+amps_gpu_status amps_gpu_export_div_e(amps_gpu_ctx* ctx, double* rho_new, double* rho_old,
+                                      double* div_e, double* phi);
 /* Per-cell pieces of ProcessCell (pic_field_solver_ecsim.cpp:1882-2438) before
  * the corner assembly, cells in block order: cellJ[24] = sum q W w_c (alpha v)
  * for the 8 corners (order (0,0,0),(1,0,0),(1,1,0),(0,1,0), then z+1), and

@@ -153,6 +153,26 @@ uint64_t orc_particle_checksum(const orc_record_layout* L, int nb, const int32_t
                                const double* x, const double* v, const uint8_t* spec,
                                const double* wcorr, const int32_t* block, const int32_t* cell);
 
+/* ---- div E correction on the periodic uniform mesh (amps_oracle_dive.c;
+ *      ECSIM::divECorrection, pic_field_solver_ecsim.cpp:4341-4364) ---- */
+void orc_net_charge(const orc_mesh* g, long n, const double* x, const uint8_t* spec,
+                    const double* wcorr, const int32_t* block, double* rho);
+void orc_div_e(const orc_mesh* g, const double* E, double* dive);
+void orc_poisson_rhs(const orc_mesh* g, const double* rho_new, const double* rho_old,
+                     const double* dive, double* rhs);
+int orc_poisson_cg(const orc_mesh* g, const double* rhs, double* phi, double tol, int maxit,
+                   double* rel);
+void orc_corner_charge(const orc_mesh* g, long n, const double* x, const uint8_t* spec,
+                       const double* wcorr, const int32_t* block, const int32_t* cell, int s0,
+                       double* cq);
+long orc_dive_correct(const orc_mesh* g, long n, double* x, const uint8_t* spec,
+                      const int32_t* block, const int32_t* cell, const double* phi,
+                      const double* cq);
+void orc_div_e_correction(const orc_mesh* g, long n, double* x, const uint8_t* spec,
+                          const double* wcorr, int32_t* block, int32_t* cell, const double* E,
+                          double* rho_new, double* rho_old, double* dive, double* phi, int first,
+                          double tol, int maxit, double* stats);
+
 /* ---- relativistic Boris, gridless form (srcEarth/gridless/GridlessParticleMovers.cpp:781) ---- */
 void orc_dipole_b(const double x[3], double b_eq, double r_e, const double b_ext[3], double B[3]);
 long orc_trace(long n, double* x, double* p, int32_t* status, int64_t* steps, double q, double m0,

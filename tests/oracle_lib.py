@@ -71,6 +71,14 @@ def load():
                                             D, C.c_long, D, D, U8, D, I32, I32, U8, C.c_longlong]),
         "orc_particle_checksum": (C.c_uint64, [C.POINTER(RecordLayout), C.c_int, I32, C.c_long, D, D,
                                                U8, D, I32, I32]),
+        "orc_net_charge": (None, [C.POINTER(Mesh), C.c_long, D, U8, D, I32, D]),
+        "orc_div_e": (None, [C.POINTER(Mesh), D, D]),
+        "orc_poisson_rhs": (None, [C.POINTER(Mesh), D, D, D, D]),
+        "orc_poisson_cg": (C.c_int, [C.POINTER(Mesh), D, D, C.c_double, C.c_int, D]),
+        "orc_corner_charge": (None, [C.POINTER(Mesh), C.c_long, D, U8, D, I32, I32, C.c_int, D]),
+        "orc_dive_correct": (C.c_long, [C.POINTER(Mesh), C.c_long, D, U8, I32, I32, D, D]),
+        "orc_div_e_correction": (None, [C.POINTER(Mesh), C.c_long, D, U8, D, I32, I32, D, D, D, D,
+                                        D, C.c_int, C.c_double, C.c_int, D]),
         "orc_dipole_b": (None, [D, C.c_double, C.c_double, D, D]),
         "orc_trace": (C.c_long, [C.c_long, D, D, I32, I64, C.c_double, C.c_double, C.c_double,
                                  C.c_double, D, C.c_double, C.c_double, C.c_long, C.c_double,
@@ -162,6 +170,27 @@ class OracleState:
                                     p(self.spec, C.c_uint8), p(self.wcorr),
                                     p(self.block, C.c_int32), p(self.cell, C.c_int32),
                                     p(self.Bcur), p(self.J), p(self.M))
+
+    def div_e_correction(self, tol=1e-8, maxit=500):
+        """ECSIM::divECorrection on the oracle's particles and E^n (its corner
+        E^{n+1} after a step): net charge, div E, the Poisson solve, the
+        species-0 position correction and re-binning.  The densities persist
+        between calls.  Returns the statistics of orc_div_e_correction."""
+        nc = self.wl.mesh.ncells
+        first = not hasattr(self, "rho_new")
+        if first:
+            self.rho_new = np.zeros(nc)
+            self.rho_old = np.zeros(nc)
+            self.div_e = np.zeros(nc)
+            self.phi = np.zeros(nc)
+        st = np.zeros(5)
+        self.lib.orc_div_e_correction(C.byref(self.m), len(self.spec), p(self.x),
+                                      p(self.spec, C.c_uint8), p(self.wcorr),
+                                      p(self.block, C.c_int32), p(self.cell, C.c_int32),
+                                      p(self.E_n), p(self.rho_new), p(self.rho_old), p(self.div_e),
+                                      p(self.phi), 1 if first else 0, tol, maxit, p(st))
+        return {"iterations": int(st[0]), "rel_residual": st[1], "gauss_before": st[2],
+                "gauss_after": st[3], "moved": int(st[4])}
 
     def cfl(self):
         """per-species maximum over cells of ProcessCell's cflCell"""
