@@ -199,8 +199,9 @@ cudaError_t enqueue_particle_step(amps_gpu_ctx* c, bool deposit) {
 // The same sequence as a CUDA graph, captured once per set of buffers it reads
 // (the corner-B slots swap every field solve, so two graphs alternate).
 cudaError_t launch_particle_step_graph(amps_gpu_ctx* c, bool deposit) {
-  const void* key[4] = {c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur,
-                        (const void*)((uintptr_t)c->d_u[c->cur][0] ^ (c->has_wcorr ? 1u : 0u))};
+  const void* key[5] = {c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur,
+                        (const void*)((uintptr_t)c->d_u[c->cur][0] ^ (c->has_wcorr ? 1u : 0u)),
+                        (const void*)(uintptr_t)c->arr_chunk};
   for (auto& g : c->graphs)
     if (g.deposit == deposit && std::memcmp(g.key, key, sizeof(key)) == 0)
       return cudaGraphLaunch(g.exec, c->stream);
@@ -252,13 +253,25 @@ amps_gpu_status read_step_flags(amps_gpu_ctx* c, long long* out_of_block, long l
 amps_gpu_status particle_step(amps_gpu_ctx* c, bool deposit, long long* out_of_block,
                               long long* near_face) {
   amps_gpu_status s;
-  const bool graph = c->use_graphs && !c->timing;
+  // the autotuner's arrivals comparison runs on stream launches
+  const bool graph = c->use_graphs && !c->timing && c->arr_tune_left == 0;
+  c->arr_tune_cur = -1;
   if ((s = cuda_check(c, graph ? launch_particle_step_graph(c, deposit)
                                : enqueue_particle_step(c, deposit),
                       "particle step")))
     return s;
   long long ovf = 0;
   if ((s = read_step_flags(c, out_of_block, near_face, &ovf))) return s;
+  if (c->arr_tune_cur >= 0) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->arr_ev[0], c->arr_ev[1]) == cudaSuccess) {
+      c->arr_tune_ms[c->arr_tune_cur] += ms;
+      c->arr_tune_n[c->arr_tune_cur]++;
+    }
+    if (--c->arr_tune_left == 0 && c->arr_tune_n[0] > 0 && c->arr_tune_n[1] > 0)
+      c->arr_chunk = c->arr_tune_ms[1] / c->arr_tune_n[1] < c->arr_tune_ms[0] / c->arr_tune_n[0] ? 32 : 16;
+    c->arr_tune_cur = -1;
+  }
   if (ovf > 0) {
     // some cell ran out of slack: the overflowed arrivals are deposited and
     // go to the slots their cells' movers vacated; when a cell is full the
@@ -691,6 +704,8 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   c->graphs.clear();
   for (auto& g : c->solve_graphs) cudaGraphExecDestroy(g.exec);
   c->solve_graphs.clear();
+  for (int q = 0; q < 2; q++)
+    if (c->arr_ev[q]) cudaEventDestroy(c->arr_ev[q]);
   cudaFree(c->d_dive);
   c->d_dive = nullptr;
   cudaFree(c->d_hstage);
@@ -1120,10 +1135,35 @@ amps_gpu_status amps_gpu_set_graphs(amps_gpu_ctx* c, int on) {
   return AMPS_GPU_OK;
 }
 
+// the field kernels' launch shapes now, on scratch vectors; the arrivals chunk
+// over the next particle steps (3 with each variant), which do their work as
+// usual
 amps_gpu_status amps_gpu_autotune(amps_gpu_ctx* c, double* ms) {
   if (!c) return AMPS_GPU_INVALID_ARG;
   cudaSetDevice(c->cfg.device);
+  for (int q = 0; q < 2; q++)
+    if (!c->arr_ev[q] && cudaEventCreate(&c->arr_ev[q]) != cudaSuccess)
+      return set_err(c, AMPS_GPU_CUDA_ERROR, "autotune: event creation failed");
+  c->arr_tune_left = 6;
+  c->arr_tune_ms[0] = c->arr_tune_ms[1] = 0.0;
+  c->arr_tune_n[0] = c->arr_tune_n[1] = 0;
   return field_autotune(c, ms);
+}
+
+amps_gpu_status amps_gpu_set_arrivals_chunk(amps_gpu_ctx* c, int chunk) {
+  if (!c || (chunk != 16 && chunk != 32)) return set_err(c, AMPS_GPU_INVALID_ARG, "arrivals chunk: 16 or 32");
+  c->arr_chunk = chunk;
+  c->arr_tune_left = 0;
+  return AMPS_GPU_OK;
+}
+
+amps_gpu_status amps_gpu_get_particle_tuning(amps_gpu_ctx* c, int* arrivals_chunk, int* pending,
+                                             double* ms) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  if (arrivals_chunk) *arrivals_chunk = c->arr_chunk;
+  if (pending) *pending = c->arr_tune_left;
+  for (int q = 0; ms && q < 2; q++) ms[q] = c->arr_tune_n[q] ? c->arr_tune_ms[q] / c->arr_tune_n[q] : 0.0;
+  return AMPS_GPU_OK;
 }
 
 amps_gpu_status amps_gpu_get_tuning(amps_gpu_ctx* c, int* threads_per_cta, int* reduction_ctas) {

@@ -144,7 +144,7 @@ struct amps_gpu_ctx {
   bool use_graphs = false;
   struct StepGraph {
     bool deposit;
-    const void* key[4];
+    const void* key[5];
     cudaGraphExec_t exec;
   };
   std::vector<StepGraph> graphs;
@@ -160,6 +160,15 @@ struct amps_gpu_ctx {
   // CG vectors f, r, p, Ap and the species-0 corner charge (9 x ncor doubles)
   double* d_dive = nullptr;
   bool dive_have_rho = false;
+  // arrivals staged 16 or 32 at a time (k_arrivals<DEP, CHUNK>); the autotuner
+  // alternates them over arr_tune_left steps, timed by arr_ev, then keeps the
+  // faster (arr_tune_ms: summed ms per variant, arr_tune_n: steps)
+  int arr_chunk = 16;
+  int arr_tune_left = 0;
+  int arr_tune_cur = -1;  // variant of the step in flight, -1: none
+  double arr_tune_ms[2] = {0.0, 0.0};
+  int arr_tune_n[2] = {0, 0};
+  cudaEvent_t arr_ev[2] = {nullptr, nullptr};
   double* d_red = nullptr;      // partial reductions
   double* d_arn = nullptr;      // per-CTA partial sums of the cooperative Arnoldi step
   float* d_xs = nullptr;        // FP32 pair split (hi, lo) of an operator input, 2 x 3*nvc

@@ -647,15 +647,17 @@ __global__ void k_step_bump(unsigned long long* step, const unsigned long long* 
 // listed in shared memory, and the warps take listed cells one at a time from
 // a shared counter, so a few busy cells do not hold idle warps at the CTA's
 // final barrier.  Arrivals are few per cell (a few % of its particles), so
-// records are staged in chunks of kArrChunk lanes: a smaller record buffer and
-// a register cap let 3 CTAs share an SM, which hides more of the per-cell
-// load latency.
+// records are staged in chunks of CHUNK lanes: at 16, a smaller record buffer
+// and a register cap let 3 CTAs share an SM, which hides more of the per-cell
+// load latency; 32 (2 CTAs per SM) halves the chunks of cells with many
+// arrivals.  The autotuner picks one on the run's own steps.
 constexpr int kArrChunk = 16;
-constexpr int kFSArr = kArrChunk + 4;  // field stride of the arrivals' staged fields
+constexpr int kFSArr = kArrChunk + 4;  // field stride of staged fields at 16 lanes
 constexpr int kLayer = AMPS_NC * AMPS_NC;
 
-template <bool DEP>
-__global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
+template <bool DEP, int CHUNK>
+__global__ void __launch_bounds__(256, CHUNK == 16 ? 3 : 2) k_arrivals(StepArgs a) {
+  constexpr int FS = CHUNK + 4;  // field stride of the staged fields
   extern __shared__ __align__(16) float4 s_dyn[];
   float* s_rec = reinterpret_cast<float*>(s_dyn);
   __shared__ double s_en[kWarps];
@@ -684,7 +686,7 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
   if (has) s_cell[(wid ? s_nw[0] : 0) + __popc(hm & lanemask_lt())] = cv;
   const int ncell = s_nw[0] + s_nw[1];
   __syncthreads();
-  float* rec = s_rec + wid * kFields * kFSArr;
+  float* rec = s_rec + wid * kFields * FS;
   int fA, fB;
   lane_fields(lane, fA, fB);
   FF en_w{0.f, 0.f};  // the warp's arrivals, as a float pair before the FP64 reduction
@@ -700,8 +702,8 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
     const long long cid = (long long)b * AMPS_CPB + c.x + kLayer * k;
     Tile tile;
     tile.zero();
-    for (int q0 = 0; q0 < na; q0 += kArrChunk) {
-      const bool act = lane < kArrChunk && q0 + lane < na;
+    for (int q0 = 0; q0 < na; q0 += CHUNK) {
+      const bool act = lane < CHUNK && q0 + lane < na;
       const long long ps = src0 + q0 + lane, pd = dst0 + q0 + lane;
       float u[3] = {0.f, 0.f, 0.f}, v[3] = {0.f, 0.f, 0.f};
       int s = 0;
@@ -724,11 +726,11 @@ __global__ void __launch_bounds__(256, 3) k_arrivals(StepArgs a) {
       }
       if (DEP) {
         // positions past the chunk's arrivals stage zero weight
-        if (lane < kArrChunk)
-          stage_fields<kFSArr>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+        if (lane < CHUNK)
+          stage_fields<FS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
                                act ? wcv : 0.f, i, j, k, a.st, inv_vol, en_w);
         __syncwarp();
-        tile.accumulate<kFSArr>(rec, (min(kArrChunk, na - q0) + 3) & ~3, fA, fB);
+        tile.accumulate<FS>(rec, (min(CHUNK, na - q0) + 3) & ~3, fA, fB);
         __syncwarp();
       }
     }
@@ -1741,7 +1743,7 @@ size_t smem_push(bool dep) {
   return (size_t)AMPS_SC * (2 + 1) * sizeof(float4) + (dep ? kWarps * kFields * kFS * sizeof(float) : 0);
 }
 size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * kFields * kFS * sizeof(float); }
-size_t smem_arr() { return (size_t)kWarps * kFields * kFSArr * sizeof(float); }
+size_t smem_arr(int chunk) { return (size_t)kWarps * kFields * (chunk + 4) * sizeof(float); }
 
 void set_smem_attrs() {
   static bool done = false;
@@ -1750,8 +1752,10 @@ void set_smem_attrs() {
   cudaFuncSetAttribute(k_push_deposit<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
   cudaFuncSetAttribute(k_push_deposit<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(true));
   cudaFuncSetAttribute(k_push_deposit<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_push(false));
-  cudaFuncSetAttribute(k_arrivals<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr());
-  cudaFuncSetAttribute(k_arrivals<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr());
+  cudaFuncSetAttribute(k_arrivals<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(16));
+  cudaFuncSetAttribute(k_arrivals<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(16));
+  cudaFuncSetAttribute(k_arrivals<true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(32));
+  cudaFuncSetAttribute(k_arrivals<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(32));
   cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
   done = true;
 }
@@ -1958,11 +1962,27 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
     if ((e = launch_inject(c, a)) != cudaSuccess) return e;
   }
   {
+    // while the autotuner compares the chunk sizes, steps alternate them and
+    // events bracket the launch (read after the step's synchronisation)
+    const bool tune = c->arr_tune_left > 0;
+    const int chunk = tune ? ((c->arr_tune_left & 1) ? 32 : 16) : c->arr_chunk;
+    if (tune) {
+      c->arr_tune_cur = chunk == 32 ? 1 : 0;
+      cudaEventRecord(c->arr_ev[0], c->stream);
+    }
     TimedLaunch t(c, "arrivals");
-    if (deposit)
-      k_arrivals<true><<<grid, kWarps * 32, smem_arr(), c->stream>>>(a);
-    else
-      k_arrivals<false><<<grid, kWarps * 32, smem_arr(), c->stream>>>(a);
+    if (chunk == 32) {
+      if (deposit)
+        k_arrivals<true, 32><<<grid, kWarps * 32, smem_arr(32), c->stream>>>(a);
+      else
+        k_arrivals<false, 32><<<grid, kWarps * 32, smem_arr(32), c->stream>>>(a);
+    } else {
+      if (deposit)
+        k_arrivals<true, 16><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(a);
+      else
+        k_arrivals<false, 16><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(a);
+    }
+    if (tune) cudaEventRecord(c->arr_ev[1], c->stream);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -1981,7 +2001,7 @@ cudaError_t particles_place_overflow(amps_gpu_ctx* c, long long n_overflow, bool
     TimedLaunch t(c, "overflow_place");
     const unsigned grid = (unsigned)((n_overflow + kWarps - 1) / kWarps);
     if (deposit)
-      k_ovf_place<true><<<grid, kWarps * 32, smem_arr(), c->stream>>>(step_args(c), n_overflow,
+      k_ovf_place<true><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(step_args(c), n_overflow,
                                                                       c->d_flags + 7);
     else
       k_ovf_place<false><<<grid, kWarps * 32, 0, c->stream>>>(step_args(c), n_overflow,

@@ -582,9 +582,25 @@ class EcsimContext:
     def set_graphs(self, on=True):
         self._check(self.lib.amps_gpu_set_graphs(self.h, 1 if on else 0), "set_graphs")
 
+    def set_arrivals_chunk(self, chunk):
+        """stage arrivals 16 or 32 at a time (ends an autotuner comparison)"""
+        self._check(self.lib.amps_gpu_set_arrivals_chunk(self.h, int(chunk)), "set_arrivals_chunk")
+
+    def particle_tuning(self):
+        """the arrivals chunk in use, the particle steps the autotuner still
+        compares, and the mean ms per arrivals launch of 16 and 32"""
+        chunk, pending = C.c_int(), C.c_int()
+        ms = np.zeros(2)
+        self._check(self.lib.amps_gpu_get_particle_tuning(self.h, C.byref(chunk), C.byref(pending),
+                                                          ptr(ms, C.c_double)), "particle_tuning")
+        return {"arrivals_chunk": chunk.value, "pending_steps": pending.value,
+                "arrivals_ms_16_32": ms.round(4).tolist()}
+
     def autotune(self):
         """Times candidate launch shapes of the field kernels; returns the
-        candidates' times and the chosen (threads per CTA, reduction CTAs)."""
+        candidates' times and the chosen (threads per CTA, reduction CTAs).
+        Also arms the arrivals comparison of the next 6 particle steps
+        (particle_tuning)."""
         ms = np.zeros(6)
         self._check(self.lib.amps_gpu_autotune(self.h, ptr(ms, C.c_double)), "autotune")
         tb, red = C.c_int(), C.c_int()

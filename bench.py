@@ -595,6 +595,10 @@ def run_gpu(args):
     ctx.UpdateJMassMatrix()
     tuning = ctx.autotune()
     solve = ctx.TimeStep(tol=tol, maxit=200, precond=1)
+    # the autotuner's arrivals comparison runs on the next particle steps
+    while ctx.particle_tuning()["pending_steps"] > 0:
+        ctx.push_deposit(want_energy=False)
+    tuning.update(ctx.particle_tuning())
     stream = ctx.stream()
     ctx.set_graphs(args.graphs > 0)
     for _ in range(args.warmup):

@@ -493,6 +493,15 @@ amps_gpu_status amps_gpu_update_j_mass_matrix_noalloc(const amps_gpu_config* cfg
 amps_gpu_status amps_gpu_set_graphs(amps_gpu_ctx* ctx, int on);
 amps_gpu_status amps_gpu_autotune(amps_gpu_ctx* ctx, double* ms);
 amps_gpu_status amps_gpu_get_tuning(amps_gpu_ctx* ctx, int* threads_per_cta, int* reduction_ctas);
+/* The particle side of the autotuner: amps_gpu_autotune also arms a
+ * comparison of the arrivals kernel staging 16 or 32 arrivals at a time over
+ * the next 6 particle steps (3 each, stream launches timed by events; the
+ * steps do their work as usual), then keeps the faster.  get: the chunk in use,
+ * the steps still to compare, ms[2] mean ms per launch of each (0 until
+ * measured).  set: force one (16 or 32), ending a comparison. */
+amps_gpu_status amps_gpu_set_arrivals_chunk(amps_gpu_ctx* ctx, int chunk);
+amps_gpu_status amps_gpu_get_particle_tuning(amps_gpu_ctx* ctx, int* arrivals_chunk, int* pending,
+                                             double* ms);
 
 /* ---- per-kernel device timing on the context stream (CUDA events) ---- */
 amps_gpu_status amps_gpu_set_kernel_timing(amps_gpu_ctx* ctx, int enable);

@@ -216,6 +216,24 @@ def test_fused_push_deposit_matches_oracle(vscale):
     assert eg == pytest.approx(eo, rel=1e-6)
 
 
+@pytest.mark.parametrize("chunk", [16, 32])
+def test_arrivals_chunk_matches_oracle(chunk):
+    """the arrivals kernel staging 16 or 32 arrivals at a time (the autotuner's
+    two variants) gives the oracle's particles, J and M"""
+    wl, ic, x, f = G.make_case(vscale=8.0)
+    ctx = G.gpu_ctx(wl, ic, x, f)
+    ctx.set_arrivals_chunk(chunk)
+    assert ctx.particle_tuning()["arrivals_chunk"] == chunk
+    st = G.oracle_state(wl, ic, x, f)
+    eg = ctx.push_deposit()
+    st.push()
+    eo = st.deposit()
+    compare_particles(ctx, st)
+    J, M = ctx.export_moments()
+    assert G.rel_err(J, st.J) <= 1e-5 and G.rel_err(M, st.M) <= 1e-5
+    assert eg == pytest.approx(eo, rel=1e-6)
+
+
 def test_fused_and_separate_paths_agree():
     wl, ic, x, f = G.make_case(vscale=4.0)
     a = G.gpu_ctx(wl, ic, x, f)

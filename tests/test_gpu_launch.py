@@ -98,3 +98,31 @@ def test_graph_field_solve_equals_stream_solve(amr, precond):
             assert rel_err(out[True][1][k], v) <= 1e-9, k
         else:
             np.testing.assert_array_equal(out[True][1][k], v, err_msg=k)
+
+
+def test_autotune_compares_arrivals_chunks():
+    """autotune arms a comparison of the two arrivals variants over the next 6
+    particle steps (graphs on: those steps run as stream launches), then keeps
+    the faster; the steps still do their work (layout and moments valid)"""
+    wl, ic, x, f = make_case(nb=(2, 2, 2), ppc=8, seed=53, vscale=4.0)
+    with A.EcsimContext(wl, capacity=len(x) + 4096, track_ids=True) as ctx:
+        ctx.set_graphs(True)
+        ctx.import_particles(x, ic["v"].astype(np.float64), ic["spec"])
+        ctx.import_fields(**f)
+        ctx.UpdateJMassMatrix()
+        ctx.autotune()
+        assert ctx.particle_tuning()["pending_steps"] == 6
+        for _ in range(6):
+            ctx.push_deposit(want_energy=False)
+        t = ctx.particle_tuning()
+        assert t["pending_steps"] == 0 and t["arrivals_chunk"] in (16, 32)
+        assert all(m > 0 for m in t["arrivals_ms_16_32"]), t
+        ms = t["arrivals_ms_16_32"]
+        assert t["arrivals_chunk"] == (32 if ms[1] < ms[0] else 16)
+        ctx.push_deposit(want_energy=False)          # a graph step with the choice
+        e = by_id(ctx.export_particles())
+        np.testing.assert_array_equal(e["id"], np.arange(len(x)))
+        J1, M1 = ctx.export_moments()
+        ctx.UpdateJMassMatrix()
+        J2, M2 = ctx.export_moments()
+        assert rel_err(J1, J2) <= 2e-6 and rel_err(M1, M2) <= 2e-6
