@@ -94,6 +94,9 @@ SIGNATURES = {
     "amps_amr_destroy": (C.c_int, [P]),
     "amps_amr_build_open": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, D, C.c_double, P, C.c_int,
                                       C.POINTER(C.c_int), C.c_int, C.POINTER(P)]),
+    "amps_amr_build_open_faces": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, D, C.c_double, P,
+                                            C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(P)]),
     "amps_amr_boundary_tables": (C.c_int, [P, C.POINTER(C.c_int), I32, I32, I32, D]),
     "amps_amr_nested_leaves": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_double, P, C.c_int]),

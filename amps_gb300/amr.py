@@ -32,7 +32,9 @@ def nested_leaves(nb0, lmax, mode, frac):
 
 class AmrMesh:
     """open_axes: per axis, non-periodic (the domain faces carry the field
-    boundary condition field_bc: 0 Dirichlet, 1 Neumann, and delete particles)"""
+    boundary condition field_bc -- 0 Dirichlet, 1 Neumann, one value for every
+    face or six, one per face in the order -x, +x, -y, +y, -z, +z -- and delete
+    particles)"""
 
     def __init__(self, nb0, lmax, leaves, dx0=1.0, x0=(0.0, 0.0, 0.0), open_axes=(False, False, False),
                  field_bc=0):
@@ -47,11 +49,17 @@ class AmrMesh:
         h = C.c_void_p()
         x0a = np.array(self.x0, np.float64)
         self.open_axes = tuple(bool(v) for v in open_axes)
-        self.field_bc = int(field_bc)
+        faces = [int(field_bc)] * 6 if np.isscalar(field_bc) else [int(v) for v in field_bc]
+        assert len(faces) == 6
+        self.field_bc = field_bc
+        self.face_bc = tuple(faces)
+        self.neumann_mask = sum(1 << f for f in range(6) if self.open_axes[f // 2] and faces[f] == 1)
         op = (C.c_int * 3)(*[1 if v else 0 for v in self.open_axes])
-        st = self.lib.amps_amr_build_open(self.nb0[0], self.nb0[1], self.nb0[2], self.lmax,
-                                          ptr(x0a, C.c_double), self.dx0, C.cast(descs, C.c_void_p),
-                                          len(leaves), op, self.field_bc, C.byref(h))
+        fb = (C.c_int * 6)(*faces)
+        st = self.lib.amps_amr_build_open_faces(self.nb0[0], self.nb0[1], self.nb0[2], self.lmax,
+                                                ptr(x0a, C.c_double), self.dx0,
+                                                C.cast(descs, C.c_void_p), len(leaves), op, fb,
+                                                C.byref(h))
         if st != 0:
             raise AmpsGpuError(st, "amps_amr_build")
         self.h = h

@@ -51,13 +51,28 @@ extern "C" amps_gpu_status amps_amr_build_open(int nbx0, int nby0, int nbz0, int
                                                const amps_block_desc* blocks, int nblocks,
                                                const int* open_axes, int field_bc,
                                                amps_amr_mesh** out) {
+  const int faces[6] = {field_bc, field_bc, field_bc, field_bc, field_bc, field_bc};
+  return amps_amr_build_open_faces(nbx0, nby0, nbz0, lmax, x0, dx0, blocks, nblocks, open_axes,
+                                   faces, out);
+}
+
+extern "C" amps_gpu_status amps_amr_build_open_faces(int nbx0, int nby0, int nbz0, int lmax,
+                                                     const double* x0, double dx0,
+                                                     const amps_block_desc* blocks, int nblocks,
+                                                     const int* open_axes, const int* face_bc,
+                                                     amps_amr_mesh** out) {
   if (!out || !blocks || nblocks <= 0 || nbx0 <= 0 || nby0 <= 0 || nbz0 <= 0 || lmax < 0 ||
-      lmax > 6 || dx0 <= 0.0 || field_bc < 0 || field_bc > 1)
+      lmax > 6 || dx0 <= 0.0 || !face_bc)
     return AMPS_GPU_INVALID_ARG;
+  for (int f = 0; f < 6; f++)
+    if (face_bc[f] < 0 || face_bc[f] > 1) return AMPS_GPU_INVALID_ARG;
   *out = nullptr;
   amps_amr_mesh* m = new amps_amr_mesh();
   for (int d = 0; d < 3; d++) m->open[d] = open_axes && open_axes[d] ? 1 : 0;
-  m->field_bc = field_bc;
+  // the Neumann faces of the open axes (cDomainBC's per-face policy,
+  // src/pic/ecsim/domain_bc.cpp:39-45)
+  for (int f = 0; f < 6; f++)
+    if (m->open[f / 2] && face_bc[f] == 1) m->neumann |= 1 << f;
   // periodic axes wrap lattice positions; open axes keep them (corners 0..nfine)
   auto wrap = [&](int d, int v) { return m->open[d] ? v : wrapi(v, m->nfine[d]); };
   m->nb0[0] = nbx0; m->nb0[1] = nby0; m->nb0[2] = nbz0;
@@ -210,7 +225,10 @@ extern "C" amps_gpu_status amps_amr_build_open(int nbx0, int nby0, int nbz0, int
   // (CollectAndMarkDomainBoundary*CornerNodesOnFaces, GetStencil's
   // boundary_short_circuit, src/pic/ecsim/get_stencil.cpp:440-620): Dirichlet
   // dE_b = 0; Neumann dE_b = mean of one donor per touching face, the corner
-  // one step of the finest touching block inward along that face's normal
+  // one step of the finest touching block inward along that face's normal.  A
+  // corner on faces of both types is Neumann: RecomputeBCType marks the
+  // Dirichlet faces first and the Neumann faces over them
+  // (src/pic/ecsim/domain_bc.cpp:49-63).
   m->bnd_flag.assign((size_t)nc, 0);
   m->bnd_start.assign((size_t)nc + 1, 0);
   for (int c = 0; c < nc; c++) {
@@ -226,7 +244,10 @@ extern "C" amps_gpu_status amps_amr_build_open(int nbx0, int nby0, int nbz0, int
     }
     if (!nface) continue;
     m->bnd_flag[(size_t)c] = 1;
-    if (field_bc == 0) continue;
+    bool neumann = false;
+    for (int d = 0; d < 3; d++)
+      if (side[d]) neumann |= (m->neumann >> (2 * d + (side[d] > 0))) & 1;
+    if (!neumann) continue;
     int stf = 1 << 30;  // lattice step of the finest block touching the corner
     for (int dz = -1; dz <= 0; dz++)
       for (int dy = -1; dy <= 0; dy++)

@@ -656,10 +656,11 @@ __global__ void __launch_bounds__(256) k_amr_update_b(long long ncell, long long
 // face keeps B^n (Dirichlet, pass 0) or takes the mean of B^{n+1} of its
 // face-normal inward neighbours, one per such face, in the same block
 // (Neumann, pass p = number of such faces: faces, then edges, then corners, so
-// every donor is final when read).
+// every donor is final when read).  A cell on a Neumann face (bit 2d + high of
+// neumann) is Neumann, whatever its other faces.
 __global__ void __launch_bounds__(256) k_amr_bnd_b(long long ncell, const int* __restrict__ borg,
                                                    const int* __restrict__ bscale, int nf0, int nf1, int nf2,
-                                                   int open, int bc, int pass, const double* __restrict__ Bn,
+                                                   int open, int neumann, int pass, const double* __restrict__ Bn,
                                                    double* __restrict__ Bnew) {
   const long long cell = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= ncell) return;
@@ -676,7 +677,11 @@ __global__ void __launch_bounds__(256) k_amr_bnd_b(long long ncell, const int* _
     nface += side[d] != 0;
   }
   if (!nface) return;
-  if (bc == 0) {
+  bool neu = false;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    if (side[d]) neu |= (neumann >> (2 * d + (side[d] > 0))) & 1;
+  if (!neu) {
     if (pass == 0)
 #pragma unroll
       for (int q = 0; q < 3; q++) Bnew[q * ncell + cell] = Bn[q * ncell + cell];
@@ -977,9 +982,9 @@ cudaError_t launch_amr_update_b(amps_gpu_ctx* c) {
                                                       c->cfg.dt);
   if (c->mesh_open) {
     const int* nf = c->amrdev.nfine;
-    for (int pass = (c->field_bc == 0 ? 0 : 1); pass <= (c->field_bc == 0 ? 0 : 3); pass++)
+    for (int pass = 0; pass <= (c->neumann ? 3 : 0); pass++)
       k_amr_bnd_b<<<g1(c->ncor), 256, 0, c->stream>>>(c->ncor, c->d_borg, c->d_bscale, nf[0], nf[1], nf[2],
-                                                       c->mesh_open, c->field_bc, pass, c->d_Bc, c->d_Bc2);
+                                                       c->mesh_open, c->neumann, pass, c->d_Bc, c->d_Bc2);
   }
   return cudaGetLastError();
 }

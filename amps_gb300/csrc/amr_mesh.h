@@ -27,7 +27,7 @@ struct amps_amr_mesh {
   // (Dirichlet: no entries; Neumann: the inward face-normal donors, averaged,
   // hanging donors expanded to their parents)
   int open[3] = {0, 0, 0};
-  int field_bc = 0;                    // 0 Dirichlet, 1 Neumann
+  int neumann = 0;                     // bit 2d + high: Neumann face of open axis d (else Dirichlet)
   std::vector<int32_t> bnd_flag;       // ncorners: 1 on a constraint row
   std::vector<int32_t> bnd_start;      // ncorners + 1
   std::vector<int32_t> bnd_col;

@@ -656,7 +656,7 @@ amps_gpu_status amps_gpu_create_amr(const amps_gpu_config* cfg, const amps_amr_m
   }
   // field boundary rows (open axes)
   c->mesh_open = (m->open[0] ? 1 : 0) | (m->open[1] ? 2 : 0) | (m->open[2] ? 4 : 0);
-  c->field_bc = m->field_bc;
+  c->neumann = m->neumann;
   c->open_axes = c->mesh_open;  // particles leave through the open faces
   if (c->mesh_open) {
     std::vector<float> bh(m->bnd_weight.size()), bl(m->bnd_weight.size());

@@ -77,7 +77,7 @@ struct amps_gpu_ctx {
   float* d_bwh = nullptr;
   float* d_bwl = nullptr;
   int mesh_open = 0;        // bit d: axis d of the AMR mesh is not periodic
-  int field_bc = 0;         // 0 Dirichlet, 1 Neumann on the open faces
+  int neumann = 0;          // bit 2d + high: a Neumann open face (else Dirichlet)
   int* d_fine_map = nullptr;
   int* d_borg = nullptr;      // nb*3 origins, finest-cell units
   int* d_bscale = nullptr;    // nb finest cells per cell

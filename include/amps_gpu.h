@@ -130,6 +130,16 @@ amps_gpu_status amps_amr_destroy(amps_amr_mesh* m);
 amps_gpu_status amps_amr_build_open(int nbx0, int nby0, int nbz0, int lmax, const double* x0,
                                     double dx0, const amps_block_desc* blocks, int nblocks,
                                     const int* open_axes, int field_bc, amps_amr_mesh** out);
+/* The same with one field boundary type per domain face (cDomainBC's per-face
+ * policy, src/pic/ecsim/domain_bc.cpp:39-45): face_bc[2 d + high] (faces -x,
+ * +x, -y, +y, -z, +z), 0 Dirichlet or 1 Neumann; faces of periodic axes are
+ * ignored.  A corner or cell on faces of both types is Neumann, its donors
+ * along every open face it touches (RecomputeBCType marks the Neumann faces
+ * after the Dirichlet ones). */
+amps_gpu_status amps_amr_build_open_faces(int nbx0, int nby0, int nbz0, int lmax, const double* x0,
+                                          double dx0, const amps_block_desc* blocks, int nblocks,
+                                          const int* open_axes, const int* face_bc,
+                                          amps_amr_mesh** out);
 /* Constraint rows of the boundary corners: flag[ncorners] (1: boundary row),
  * CSR start[ncorners+1], col/weight[nentries]: row b reads
  * x_b - sum weight x_col = 0.  Any pointer may be NULL. */

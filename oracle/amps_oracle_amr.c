@@ -59,7 +59,7 @@ typedef struct {
   const int32_t* bnd_col;
   const double* bnd_weight;
   int open_mask;              /* bit d: axis d open */
-  int field_bc;               /* 0 Dirichlet, 1 Neumann */
+  int field_bc;               /* bit 2d + high: Neumann face of open axis d (else Dirichlet) */
 } orc_amr;
 
 static const int kOff[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
@@ -834,8 +834,9 @@ void orc_amr_update_b(const orc_amr* g, const double* E_half, const double* Bn, 
   /* UpdateB's boundary branch (pic_field_solver_ecsim.cpp:5274-5600) on the
    * cells with a face on an open domain face: Dirichlet keeps B^n; Neumann
    * takes the mean of B^{n+1} of the face-normal inward neighbours (one per
-   * such face, same block), faces before edges before corners */
-  for (int pass = (g->field_bc == 0 ? 0 : 1); pass <= (g->field_bc == 0 ? 0 : 3); pass++)
+   * such face, same block), faces before edges before corners; a cell on any
+   * Neumann face is Neumann (domain_bc.cpp:49-63 marks those faces last) */
+  for (int pass = 0; pass <= (g->field_bc ? 3 : 0); pass++)
     for (int b = 0; b < g->nblocks; b++) {
       const int st = 1 << (g->lmax - g->level[b]);
       for (int l = 0; l < 512; l++) {
@@ -850,8 +851,12 @@ void orc_amr_update_b(const orc_amr* g, const double* E_half, const double* Bn, 
         }
         if (!nface) continue;
         const long cl = (long)b * 512 + l;
-        if (g->field_bc == 0) {
-          for (int q = 0; q < 3; q++) Bnp1[3 * cl + q] = Bn[3 * cl + q];
+        int neu = 0;
+        for (int d = 0; d < 3; d++)
+          if (side[d]) neu |= (g->field_bc >> (2 * d + (side[d] > 0))) & 1;
+        if (!neu) {
+          if (pass == 0)
+            for (int q = 0; q < 3; q++) Bnp1[3 * cl + q] = Bn[3 * cl + q];
           continue;
         }
         if (nface != pass) continue;

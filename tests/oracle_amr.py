@@ -94,7 +94,7 @@ class AmrOracle:
         # open axes: boundary rows and UpdateB's boundary branch
         mask = sum(1 << d for d in range(3) if getattr(mesh, "open_axes", (False,) * 3)[d])
         g.open_mask = mask
-        g.field_bc = getattr(mesh, "field_bc", 0)
+        g.field_bc = getattr(mesh, "neumann_mask", 0)
         if mask:
             g.bnd_flag = p(mesh.bnd_flag, C.c_int32)
             g.bnd_start = p(mesh.bnd_start, C.c_int32)

@@ -180,6 +180,69 @@ def test_open_axis_mesh_boundary_rows():
     assert np.allclose(sums, 1.0)
 
 
+def test_per_face_boundary_rows():
+    """one field boundary type per face (-x D, +x N, -z N, +z D on open x and z):
+    a corner on a Neumann face has donors (one per open face it touches, also
+    the Dirichlet ones), a corner only on Dirichlet faces has none"""
+    from amps_gb300 import amr as AM
+    leaves = [(0, i * 8, j * 8, k * 8) for k in range(2) for j in range(2) for i in range(3)]
+    m = AM.AmrMesh((3, 2, 2), 0, leaves, open_axes=(True, False, True), field_bc=(0, 1, 0, 0, 1, 0))
+    assert m.neumann_mask == (1 << 1) | (1 << 4)
+    xyz = m.corner_xyz.reshape(-1, 3)
+    xm, xp, zm, zp = xyz[:, 0] == 0, xyz[:, 0] == 24, xyz[:, 2] == 0, xyz[:, 2] == 16
+    np.testing.assert_array_equal(m.bnd_flag.astype(bool), xm | xp | zm | zp)
+    nent = np.diff(m.bnd_start)
+    neumann = xp | zm
+    faces = (xm | xp).astype(int) + (zm | zp).astype(int)
+    np.testing.assert_array_equal(nent[neumann], faces[neumann])
+    assert (nent[~neumann] == 0).all()
+    # the all-Dirichlet and all-Neumann masks of the single-type call
+    assert AM.AmrMesh((3, 2, 2), 0, leaves, open_axes=(True, False, True), field_bc=0).neumann_mask == 0
+    assert AM.AmrMesh((3, 2, 2), 0, leaves, open_axes=(True, False, True),
+                      field_bc=1).neumann_mask == 0b110011
+
+
+def test_oracle_per_face_update_b():
+    """UpdateB's boundary branch with per-face types: cells on a Neumann face
+    average their inward neighbours (over every open face they touch), cells
+    only on Dirichlet faces keep B^n"""
+    import ctypes as C
+    from amps_gb300 import amr as AM
+    from tests import oracle_amr as OA
+    from tests.oracle_amr import AmrOracle
+    import amps_gb300 as A
+    leaves = [(0, i * 8, j * 8, k * 8) for k in range(2) for j in range(2) for i in range(2)]
+    wl = A.electron_proton_plasma("o", 1, 1, 1, 2, 2)
+    m = AM.AmrMesh((2, 2, 2), 0, leaves, open_axes=(True, True, False), field_bc=(1, 0, 0, 1, 0, 0))
+    ao = AmrOracle(m, wl.species, wl.dt, wl.theta, np.zeros((0, 3)), np.zeros((0, 3)),
+                   np.zeros(0, np.uint8))
+    rng = np.random.default_rng(2)
+    ao.E_half[:] = 1e-2 * rng.standard_normal(ao.E_half.shape)
+    ao.Bcen[:] = rng.standard_normal(ao.Bcen.shape)
+    Bn = ao.Bcen.copy()
+    B1 = np.zeros_like(Bn)
+    ao.L.orc_amr_update_b(C.byref(ao.g), OA.p(ao.E_half), OA.p(Bn), OA.p(B1))
+    org = m.origin
+    cells = np.arange(m.nblocks * 512)
+    b, l = cells // 512, cells % 512
+    ijk = np.stack([l % 8, (l // 8) % 8, l // 64], 1) + org[b]
+    side = np.zeros((len(cells), 3), int)
+    for d in range(2):
+        side[ijk[:, d] == 0, d] = -1
+        side[ijk[:, d] == 15, d] = 1
+    neu = (side[:, 0] == -1) | (side[:, 1] == 1)
+    dir_only = (side != 0).any(1) & ~neu
+    np.testing.assert_array_equal(B1[dir_only], Bn[dir_only])
+    for c in np.flatnonzero(neu)[:40]:
+        donors = []
+        for d in range(2):
+            if side[c, d]:
+                j = ijk[c].copy()
+                j[d] -= side[c, d]
+                donors.append(np.flatnonzero((ijk == j).all(1))[0])
+        np.testing.assert_allclose(B1[c], B1[donors].mean(0), rtol=0, atol=1e-14)
+
+
 def test_oracle_open_boundary_rows_and_update_b():
     """the oracle's operator rows and UpdateB boundary branch on an open mesh"""
     from amps_gb300 import amr as AM

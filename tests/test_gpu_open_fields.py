@@ -60,10 +60,14 @@ def boundary_cells(mesh):
     return n.ravel()
 
 
+# field boundary types: one for every open face, or one per face (-x, +x, -y,
+# +y, -z, +z: cDomainBC's per-face policy)
 CASES = [((3, 2, 2), 0, (True, False, False), 0),
          ((3, 2, 2), 0, (True, False, True), 1),
          ((4, 4, 4), 1, (True, True, False), 1),
-         ((4, 4, 4), 1, (False, False, True), 0)]
+         ((4, 4, 4), 1, (False, False, True), 0),
+         ((3, 2, 2), 0, (True, False, True), (0, 1, 0, 0, 1, 0)),
+         ((4, 4, 4), 1, (True, True, False), (1, 0, 0, 1, 0, 0))]
 
 
 @pytest.mark.parametrize("nb0,lmax,open_axes,bc", CASES)
@@ -101,7 +105,7 @@ def test_open_field_solve_matches_oracle(nb0, lmax, open_axes, bc):
         assert np.abs(dE[b] - mean).max() <= 1e-9 * np.abs(dE).max()
 
 
-@pytest.mark.parametrize("nb0,lmax,open_axes,bc", [CASES[1], CASES[2]])
+@pytest.mark.parametrize("nb0,lmax,open_axes,bc", [CASES[1], CASES[2], CASES[5]])
 def test_open_steps_match_oracle(open_oracle, nb0, lmax, open_axes, bc):
     """two full ECSIM steps with fast particles: the set deleted at the open
     faces, the surviving particles and the fields follow the oracle"""
