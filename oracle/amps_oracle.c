@@ -229,6 +229,38 @@ static void alpha_matrix(double qdt2m, const double B[3], double alpha[9]) {
   alpha[8] = c0 * (1.0 + BB[2][2]);
 }
 
+/* Where the magnetic field the particles see lives: 0 the corners
+ * (_PIC_FIELD_SOLVER_B_CORNER_BASED_: the Bc arguments are corner arrays), 1 the
+ * cell centres (_PIC_FIELD_SOLVER_B_CENTER_BASED_, the reference's default: the
+ * same arguments are cell arrays, B^n for the push and B^{n+1} for the
+ * deposit, read by CellCentered::Linear's trilinear stencil). */
+static int orc_b_center = 0;
+void orc_set_b_center(int on) { orc_b_center = on ? 1 : 0; }
+
+/* B at x from the cell centres: GetTriliniarInterpolationStencil
+ * (pic_interpolation_routines.cpp:820-905) -- iLoc in cell units from the
+ * block's low face, i0 = -1 below half a cell else (int)(iLoc - 0.5), weight
+ * iLoc - (i0 + 0.5), the 8 centres in the stencil's order (i, then j, then k
+ * innermost), neighbouring blocks' cells beyond the block (periodic) */
+static void centre_b(const orc_mesh* g, const int bxyz[3], const double xmin[3], const double x[3],
+                     const double* Bc, double B[3]) {
+  int i0[3];
+  double w[3];
+  for (int d = 0; d < 3; d++) {
+    const double loc = (x[d] - xmin[d]) / (NC * g->dx[d]) * NC;
+    i0[d] = loc < 0.5 ? -1 : (int)(loc - 0.50);
+    w[d] = loc - (i0[d] + 0.5);
+  }
+  B[0] = B[1] = B[2] = 0.0;
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++)
+      for (int k = 0; k < 2; k++) {
+        const double W = (i ? w[0] : 1.0 - w[0]) * (j ? w[1] : 1.0 - w[1]) * (k ? w[2] : 1.0 - w[2]);
+        const long c = cidx(g, bxyz[0] * NC + i0[0] + i, bxyz[1] * NC + i0[1] + j, bxyz[2] * NC + i0[2] + k);
+        for (int d = 0; d < 3; d++) B[d] += W * Bc[3 * c + d];
+      }
+}
+
 /* Lapenta2017 (pic_mover_boris.cpp:876-1375) for every particle, followed by
  * the re-binning of the moved particle.  Returns the number of particles that
  * were found outside their block on entry (the reference aborts there). */
@@ -248,9 +280,10 @@ long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* sp
                     bxyz[2] * NC + iX[2] + nd[s][2]);
       for (int d = 0; d < 3; d++) {
         E[d] += wn[s] * E_half[3 * c + d];
-        B[d] += wn[s] * Bc_prev[3 * c + d];
+        if (!orc_b_center) B[d] += wn[s] * Bc_prev[3 * c + d];
       }
     }
+    if (orc_b_center) centre_b(g, bxyz, xmin, xI, Bc_prev, B);
     int sp = spec[p];
     double dtT = g->dt;
     double qdtm = g->q[sp] * dtT / g->m[sp];
@@ -596,10 +629,14 @@ double orc_deposit(const orc_mesh* g, long n, const double* x, const double* v,
     for (int d = 0; d < 3; d++) { xI[d] = x[3 * p + d]; vI[d] = v[3 * p + d]; }
     corner_stencil(xmin, g->dx, xI, wt, wn, nd, iX);
     double B[3] = {0, 0, 0};
-    for (int s = 0; s < 8; s++) {
-      long c = cidx(g, bxyz[0] * NC + iX[0] + nd[s][0], bxyz[1] * NC + iX[1] + nd[s][1],
-                    bxyz[2] * NC + iX[2] + nd[s][2]);
-      for (int d = 0; d < 3; d++) B[d] += wn[s] * Bc_cur[3 * c + d];
+    if (orc_b_center) {
+      centre_b(g, bxyz, xmin, xI, Bc_cur, B);
+    } else {
+      for (int s = 0; s < 8; s++) {
+        long c = cidx(g, bxyz[0] * NC + iX[0] + nd[s][0], bxyz[1] * NC + iX[1] + nd[s][1],
+                      bxyz[2] * NC + iX[2] + nd[s][2]);
+        for (int d = 0; d < 3; d++) B[d] += wn[s] * Bc_cur[3 * c + d];
+      }
     }
     int sp = spec[p];
     double W = g->w[sp] * (wcorr ? wcorr[p] : 1.0);
@@ -1010,15 +1047,22 @@ int orc_ecsim_step(const orc_mesh* g, long n, double* x, double* v, const uint8_
   int it = orc_gmres(g, M, rhs, dE, tol, maxit, 30, precond, &resid);
   for (long i = 0; i < 3 * nc; i++) E_half[i] = E_n[i] + dE[i]; /* ProcessFinalSolution :6311 */
   orc_update_b(g, E_half, Bcen, Bnew);
+  /* centre B: Bnew = B^{n+1}, Bcen still B^n until the copy below */
+  double* Bold = NULL;
+  if (orc_b_center) {
+    Bold = (double*)malloc(sizeof(double) * 3 * nc);
+    memcpy(Bold, Bcen, sizeof(double) * 3 * nc);
+  }
   memcpy(Bcen, Bnew, sizeof(double) * 3 * nc);
   /* corner B: prev <- C2N(B^n) (already there), cur <- C2N(B^{n+1}) */
   memcpy(Bcor_prev, Bcor_cur, sizeof(double) * 3 * nc);
   orc_center_to_corner(g, Bcen, Bcor_cur);
   double wave = orc_update_e(g, E_half, E_n, Bcen);
-  /* Mover::MoveParticles with E^{n+theta} and the corner B of B^n */
-  orc_push(g, n, x, v, spec, block, cell, E_half, Bcor_prev);
-  /* UpdateJMassMatrix with the corner B of B^{n+1} */
-  double pe = orc_deposit(g, n, x, v, spec, wcorr, block, cell, Bcor_cur, J, M);
+  /* Mover::MoveParticles with E^{n+theta} and B^n (corner or centre), then
+   * UpdateJMassMatrix with B^{n+1} */
+  orc_push(g, n, x, v, spec, block, cell, E_half, orc_b_center ? Bold : Bcor_prev);
+  double pe = orc_deposit(g, n, x, v, spec, wcorr, block, cell, orc_b_center ? Bcen : Bcor_cur, J, M);
+  free(Bold);
   if (diag) { diag[0] = pe; diag[1] = wave; diag[2] = resid; }
   free(rhs); free(dE); free(Bnew);
   return it;

@@ -52,6 +52,10 @@ void orc_laplacian_table(int axis, double out[27]);
 void orc_graddiv_table(int p, int q, double out[27]);
 
 /* ---- interpolation / push / deposition ---- */
+/* 1: the B arguments of orc_push / orc_deposit (and the ECSIM step's) are cell
+ * arrays interpolated from the cell centres (_PIC_FIELD_SOLVER_B_CENTER_BASED_);
+ * 0 (default): corner arrays */
+void orc_set_b_center(int on);
 void orc_corner_weights(const double xloc[3], double w_table[8]);
 long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
               int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev);

@@ -20,6 +20,17 @@
 // electron (q -1, m 1) or the proton (q +1, m 25) in species slot 0; the
 // "species" field of each record says which.
 //
+// Built with PIN_B_CENTER (oracle/_ref/ecsim_pin_cb), the configuration puts
+// the magnetic field on the cell centres (_PIC_FIELD_SOLVER_B_CENTER_BASED_,
+// the reference's default) with the cell-centred linear interpolation: the
+// block then also gets its centre nodes (ghost layers included) carrying B in
+// the current and previous slots, Lapenta2017's B_C scratch holds the centre
+// values, and the record adds "b_mode": "center" and "center_fields" (B at the
+// centres of cells 0..4).  CellCentered::Linear::InitStencil reads the global
+// StencilTable[0].Length to decide whether to renormalise its weights
+// (pic_interpolation_routines.cpp:900): it is set to 8, a full stencil, so the
+// weights are used as computed.
+//
 // Output (JSON on stdout):
 //   process_cell: cells with particles (x, v, species, weight correction) and
 //     the 8 corners' J[3] and M[243] of ProcessCell's CellData plus the cell's
@@ -101,6 +112,12 @@ namespace EC = PIC::FieldSolver::Electromagnetic::ECSIM;
 
 constexpr int NX = _BLOCK_CELLS_X_;
 constexpr int NG = _GHOST_CELLS_X_;
+#if _PIC_FIELD_SOLVER_B_MODE_ == _PIC_FIELD_SOLVER_B_CENTER_BASED_
+constexpr bool kCenterB = true;
+#else
+constexpr bool kCenterB = false;
+#endif
+constexpr int NCEN = _TOTAL_BLOCK_CELLS_X_ * _TOTAL_BLOCK_CELLS_Y_ * _TOTAL_BLOCK_CELLS_Z_;
 constexpr int NCOR = (1 + _TOTAL_BLOCK_CELLS_X_) * (1 + _TOTAL_BLOCK_CELLS_Y_) * (1 + _TOTAL_BLOCK_CELLS_Z_);
 // corner associated data: E^n[3] E^{n+theta}[3] J[3] M[243] | B cur[3] B prev[3]
 constexpr int kRecDoubles = 258;
@@ -131,6 +148,8 @@ struct Block {
   std::vector<PIC::Mesh::cDataCornerNode*> corners;
   std::vector<double> assoc;   // kRecDoubles per corner
   std::vector<double> E, B;    // 3 per corner local number (Lapenta2017 scratch)
+  std::vector<double> cassoc;  // centre B: current[3] previous[3] per centre node
+  std::vector<double> Bcen;    // 3 per centre local number (Lapenta2017 scratch, centre B)
   double dx;
 };
 
@@ -191,6 +210,25 @@ Block make_block(double dx, const FieldFn& f) {
       r[255 + q] = b.B[3 * nd + q];    // corner B, previous slot
     }
   }
+  if (kCenterB) {
+    b.cassoc.assign((size_t)NCEN * 6, 0.0);
+    b.Bcen.assign((size_t)NCEN * 3, 0.0);
+    for (int k = -NG; k < NX + NG; k++)
+      for (int j = -NG; j < NX + NG; j++)
+        for (int i = -NG; i < NX + NG; i++) {
+          const int nd = _getCenterNodeLocalNumber(i, j, k);
+          auto* cn = static_cast<PIC::Mesh::cDataCenterNode*>(calloc(1, sizeof(PIC::Mesh::cDataCenterNode)));
+          cn->associatedDataPointer = reinterpret_cast<char*>(&b.cassoc[(size_t)nd * 6]);
+          b.block->GetCenterNodeBuffer()[nd] = cn;
+          const double x[3] = {(i + 0.5) * dx, (j + 0.5) * dx, (k + 0.5) * dx};
+          for (int q = 0; q < 3; q++) {
+            const double v = f.at(3 + q, x);
+            b.cassoc[(size_t)nd * 6 + q] = v;      // CurrentBOffset 0
+            b.cassoc[(size_t)nd * 6 + 3 + q] = v;  // PrevBOffset 3 doubles
+            b.Bcen[(size_t)nd * 3 + q] = v;
+          }
+        }
+  }
   return b;
 }
 
@@ -250,6 +288,9 @@ int main() {
   }
   f.a[5] += 0.5;  // B0 along z
   Block blk = make_block(dx, f);
+  static PIC::InterpolationRoutines::CellCentered::cStencil stencil_table[1];
+  stencil_table[0].Length = 8;
+  PIC::InterpolationRoutines::CellCentered::StencilTable = stencil_table;
 
   const int L = _PIC_PARTICLE_DATA__BASIC_DATA_LENGTH_;
   PIC::ParticleBuffer::ParticleDataLength = L;
@@ -278,6 +319,18 @@ int main() {
                blk.E[3 * nd + 1], blk.E[3 * nd + 2], blk.B[3 * nd], blk.B[3 * nd + 1], blk.B[3 * nd + 2]);
       }
   printf("],");
+  if (kCenterB) {
+    // B at the centres of cells 0..NX-1 (i fastest)
+    printf("\"b_mode\":\"center\",\"center_fields\":[");
+    for (int k = 0; k < NX; k++)
+      for (int j = 0; j < NX; j++)
+        for (int i = 0; i < NX; i++) {
+          const int nd = _getCenterNodeLocalNumber(i, j, k);
+          printf("%s[%.17g,%.17g,%.17g]", (i || j || k) ? "," : "", blk.Bcen[3 * nd], blk.Bcen[3 * nd + 1],
+                 blk.Bcen[3 * nd + 2]);
+        }
+    printf("],");
+  }
 
   // ---- ProcessCell on three cells of the block interior ----
   const int cells[4][3] = {{1, 2, 3}, {2, 2, 2}, {3, 1, 2}, {2, 3, 1}};
@@ -341,7 +394,7 @@ int main() {
   // ---- Lapenta2017 on particles of the block interior ----
   PIC::Mover::cLapentaInputData data;
   data.E_Corner = blk.E.data();
-  data.B_C = blk.B.data();
+  data.B_C = kCenterB ? blk.Bcen.data() : blk.B.data();
   data.MolMass = PIC::MolecularData::MolMass;
   data.ElectricChargeTable = PIC::MolecularData::ElectricChargeTable;
   data.TimeStepTable = PIC::ParticleWeightTimeStep::GlobalTimeStep;

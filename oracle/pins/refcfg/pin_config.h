@@ -18,7 +18,19 @@
 #undef _PIC_FIELD_SOLVER_MODE_
 #define _PIC_FIELD_SOLVER_MODE_ _PIC_FIELD_SOLVER_MODE__ELECTROMAGNETIC__ECSIM_
 #undef _PIC_FIELD_SOLVER_B_MODE_
+#ifdef PIN_B_CENTER
+// the reference's default magnetic-field placement (picGlobal.dfn), with the
+// cell-centred linear interpolation its ECSIM test inputs select
+// (cell_centered_linear_interpolation_mode=amps, input/test/fast-wave.input:90,
+// which ampsConfig.pl:2927-2931 turns into these two macros)
+#define _PIC_FIELD_SOLVER_B_MODE_ _PIC_FIELD_SOLVER_B_CENTER_BASED_
+#undef _PIC_COUPLER__INTERPOLATION_MODE_
+#define _PIC_COUPLER__INTERPOLATION_MODE_ _PIC_COUPLER__INTERPOLATION_MODE__CELL_CENTERED_LINEAR_
+#undef _PIC_CELL_CENTERED_LINEAR_INTERPOLATION_ROUTINE_
+#define _PIC_CELL_CENTERED_LINEAR_INTERPOLATION_ROUTINE_ _PIC_CELL_CENTERED_LINEAR_INTERPOLATION_ROUTINE__AMPS_
+#else
 #define _PIC_FIELD_SOLVER_B_MODE_ _PIC_FIELD_SOLVER_B_CORNER_BASED_
+#endif
 #undef _PIC_FIELD_SOLVER_INPUT_UNIT_
 #define _PIC_FIELD_SOLVER_INPUT_UNIT_ _PIC_FIELD_SOLVER_INPUT_UNIT_NORM_
 #undef _SIMULATION_TIME_STEP_MODE_

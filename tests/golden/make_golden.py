@@ -18,6 +18,10 @@ Run here (the reference sources are only present in the build container):
                          src/pic/pic_field_solver_ecsim.cpp, pic_mover_boris.cpp and
                          pic_interpolation_routines.cpp with the hand-written
                          configuration of oracle/pins/refcfg/ (oracle/_ref/ecsim_pin)
+* ecsim_ref_cb.json      the same with the magnetic field on the cell centres (the
+                         reference's default, _PIC_FIELD_SOLVER_B_CENTER_BASED_, with
+                         the cell-centred linear interpolation of its ECSIM test
+                         inputs; oracle/_ref/ecsim_pin_cb)
 * stormer_c1.csv         copied from srcEarth/test/C1/reference_C1_stormer.csv
 """
 import ctypes as C
@@ -111,6 +115,21 @@ def ecsim_ref():
         json.dump(data, f)
 
 
+def ecsim_ref_cb():
+    """the same routines configured with the magnetic field on the cell centres
+    (oracle/_ref/ecsim_pin_cb)"""
+    out = subprocess.run([os.path.join(REFBIN, "ecsim_pin_cb")], capture_output=True, text=True,
+                         check=True).stdout
+    data = json.loads(out)
+    data["source"] = ("src/pic/pic_field_solver_ecsim.cpp:1882-2438 ProcessCell, "
+                      "src/pic/pic_mover_boris.cpp:876-1380 Lapenta2017, "
+                      "src/pic/pic_interpolation_routines.cpp:224-905 CellCentered::Linear, "
+                      "_PIC_FIELD_SOLVER_B_CENTER_BASED_")
+    data.pop("boris", None)   # the Boris force hook reads the corner fields: ecsim_ref.json has it
+    with open(os.path.join(HERE, "ecsim_ref_cb.json"), "w") as f:
+        json.dump(data, f)
+
+
 def stormer():
     shutil.copy(os.path.join(REF, "srcEarth/test/C1/reference_C1_stormer.csv"),
                 os.path.join(HERE, "stormer_c1.csv"))
@@ -121,5 +140,6 @@ if __name__ == "__main__":
     index_matrix()
     gridless()
     ecsim_ref()
+    ecsim_ref_cb()
     stormer()
     print("golden fixtures written to", HERE)

@@ -54,6 +54,7 @@ def load():
         "orc_cfl": (None, [C.POINTER(Mesh), C.c_long, D, U8, I32, I32, D]),
         "orc_species_moments": (None, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D]),
         "orc_set_open_axes": (None, [C.c_int]),
+        "orc_set_b_center": (None, [C.c_int]),
         "orc_inject": (C.c_long, [C.POINTER(Mesh), C.c_int, C.c_int, C.c_double, D, C.c_double,
                                   C.c_ulonglong, C.c_ulonglong, C.c_int, D, D, C.c_long, D, D, I32,
                                   I32]),
@@ -115,8 +116,13 @@ def mesh_of(wl):
 class OracleState:
     """FP64 oracle state for one workload (global periodic corner layout)."""
 
-    def __init__(self, wl, x, v, spec, fields, wcorr=None):
+    def __init__(self, wl, x, v, spec, fields, wcorr=None, b_center=False):
+        """b_center: the particles see B interpolated from the cell centres
+        (_PIC_FIELD_SOLVER_B_CENTER_BASED_): the push reads Bcen_prev (B^n),
+        the deposit Bcen (B^{n+1} after a step; both the imported B_center at
+        first)"""
         self.lib = load()
+        self.b_center = bool(b_center)
         self.wl = wl
         self.m = mesh_of(wl)
         n = len(spec)
@@ -134,6 +140,7 @@ class OracleState:
         self.Bcen = np.ascontiguousarray(fields["B_center"], np.float64).copy()
         self.Bprev = np.ascontiguousarray(fields["B_corner_prev"], np.float64).copy()
         self.Bcur = np.ascontiguousarray(fields["B_corner_cur"], np.float64).copy()
+        self.Bcen_prev = self.Bcen.copy()
         self.J = np.zeros((nc, 3))
         self.M = np.zeros((nc, 243))
 
@@ -160,16 +167,25 @@ class OracleState:
                                   p(self.spec, C.c_uint8), p(self.block, C.c_int32),
                                   p(self.cell, C.c_int32), p(self.E_n), p(self.Bcur), dt)
 
+    def _with_b_mode(self, call):
+        self.lib.orc_set_b_center(1 if self.b_center else 0)
+        try:
+            return call()
+        finally:
+            self.lib.orc_set_b_center(0)
+
     def push(self):
-        return self.lib.orc_push(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
-                                 p(self.spec, C.c_uint8), p(self.block, C.c_int32),
-                                 p(self.cell, C.c_int32), p(self.E_half), p(self.Bprev))
+        B = self.Bcen_prev if self.b_center else self.Bprev
+        return self._with_b_mode(lambda: self.lib.orc_push(
+            C.byref(self.m), len(self.spec), p(self.x), p(self.v), p(self.spec, C.c_uint8),
+            p(self.block, C.c_int32), p(self.cell, C.c_int32), p(self.E_half), p(B)))
 
     def deposit(self):
-        return self.lib.orc_deposit(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
-                                    p(self.spec, C.c_uint8), p(self.wcorr),
-                                    p(self.block, C.c_int32), p(self.cell, C.c_int32),
-                                    p(self.Bcur), p(self.J), p(self.M))
+        B = self.Bcen if self.b_center else self.Bcur
+        return self._with_b_mode(lambda: self.lib.orc_deposit(
+            C.byref(self.m), len(self.spec), p(self.x), p(self.v), p(self.spec, C.c_uint8),
+            p(self.wcorr), p(self.block, C.c_int32), p(self.cell, C.c_int32), p(B), p(self.J),
+            p(self.M)))
 
     def div_e_correction(self, tol=1e-8, maxit=500):
         """ECSIM::divECorrection on the oracle's particles and E^n (its corner
@@ -201,12 +217,13 @@ class OracleState:
 
     def step(self, tol=1e-8, maxit=200, precond=0):
         diag = np.zeros(3)
-        it = self.lib.orc_ecsim_step(C.byref(self.m), len(self.spec), p(self.x), p(self.v),
-                                     p(self.spec, C.c_uint8), p(self.wcorr),
-                                     p(self.block, C.c_int32), p(self.cell, C.c_int32),
-                                     p(self.E_n), p(self.E_half), p(self.Bcen), p(self.Bprev),
-                                     p(self.Bcur), p(self.J), p(self.M), tol, maxit, precond,
-                                     p(diag))
+        prev = self.Bcen.copy()
+        it = self._with_b_mode(lambda: self.lib.orc_ecsim_step(
+            C.byref(self.m), len(self.spec), p(self.x), p(self.v), p(self.spec, C.c_uint8),
+            p(self.wcorr), p(self.block, C.c_int32), p(self.cell, C.c_int32), p(self.E_n),
+            p(self.E_half), p(self.Bcen), p(self.Bprev), p(self.Bcur), p(self.J), p(self.M), tol,
+            maxit, precond, p(diag)))
+        self.Bcen_prev = prev
         return it, diag
 
     def rhs(self):

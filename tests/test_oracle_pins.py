@@ -283,3 +283,75 @@ def test_boris_matches_reference_build():
         assert all(r["code"] == 3 for r in recs)   # _PARTICLE_MOTION_FINISHED_
         gc = np.array([r["cell"][0] + 8 * (r["cell"][1] + 8 * r["cell"][2]) for r in recs])
         np.testing.assert_array_equal(cel, gc)
+
+
+# ---- the same routines configured with the magnetic field on the cell centres
+# (the reference's default, golden ecsim_ref_cb.json, oracle/_ref/ecsim_pin_cb):
+# ProcessCell and Lapenta2017 read B from the centres with CellCentered::
+# Linear's stencil (pic_interpolation_routines.cpp:820-905)
+def ref_golden_cb():
+    return json.load(open(os.path.join(GOLD, "ecsim_ref_cb.json")))
+
+
+def ref_center_b(g):
+    """B on the 8^3 block's cells from the golden centre values of cells 0..4"""
+    n = g["block_cells"]
+    B = np.zeros((512, 3))
+    cf = np.array(g["center_fields"])
+    for t in range(len(cf)):
+        i, j, k = t % n, (t // n) % n, t // (n * n)
+        B[i + 8 * (j + 8 * k)] = cf[t]
+    return B
+
+
+def test_process_cell_center_b_matches_reference_build():
+    g = ref_golden_cb()
+    assert g["b_mode"] == "center"
+    lib = O.load()
+    Bc = ref_center_b(g)
+    lib.orc_set_b_center(1)
+    try:
+        for rec in g["process_cell"]:
+            m = ref_mesh(g, rec["species"])
+            ps = rec["particles"]
+            n = len(ps)
+            x = np.ascontiguousarray([p["x"] for p in ps], np.float64)
+            v = np.ascontiguousarray([p["v"] for p in ps], np.float64)
+            wc = np.ascontiguousarray([p["wcorr"] for p in ps], np.float64)
+            sp = np.zeros(n, np.uint8)
+            blk, cel = np.zeros(n, np.int32), np.zeros(n, np.int32)
+            lib.orc_locate(O.C.byref(m), n, O.p(x), O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32))
+            ci, cj, ck = rec["cell"]
+            J, M = np.zeros((512, 3)), np.zeros((512, 243))
+            e = lib.orc_deposit(O.C.byref(m), n, O.p(x), O.p(v), O.p(sp, O.C.c_uint8), O.p(wc),
+                                O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32), O.p(Bc), O.p(J), O.p(M))
+            cor = [(ci + o[0]) + 8 * ((cj + o[1]) + 8 * (ck + o[2])) for o in CORNER_OFF]
+            assert rel(J[cor], np.array(rec["J"]).reshape(8, 3)) < 1e-13
+            assert rel(M[cor], np.array(rec["M"]).reshape(8, 243)) < 1e-13
+            assert e == pytest.approx(rec["energy"], rel=1e-13)
+    finally:
+        lib.orc_set_b_center(0)
+
+
+def test_lapenta2017_center_b_matches_reference_build():
+    g = ref_golden_cb()
+    lib = O.load()
+    E, _ = ref_fields(g)
+    Bc = ref_center_b(g)
+    lib.orc_set_b_center(1)
+    try:
+        for species in (0, 1):
+            recs = [r for r in g["lapenta"] if r["species"] == species]
+            m = ref_mesh(g, species)
+            n = len(recs)
+            x = np.ascontiguousarray([r["in"]["x"] for r in recs], np.float64)
+            v = np.ascontiguousarray([r["in"]["v"] for r in recs], np.float64)
+            sp = np.zeros(n, np.uint8)
+            blk, cel = np.zeros(n, np.int32), np.zeros(n, np.int32)
+            lib.orc_locate(O.C.byref(m), n, O.p(x), O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32))
+            assert lib.orc_push(O.C.byref(m), n, O.p(x), O.p(v), O.p(sp, O.C.c_uint8),
+                                O.p(blk, O.C.c_int32), O.p(cel, O.C.c_int32), O.p(E), O.p(Bc)) == 0
+            assert np.max(np.abs(x - np.array([r["x"] for r in recs]))) < 1e-13 * g["dx"]
+            assert rel(v, np.array([r["v"] for r in recs])) < 1e-13
+    finally:
+        lib.orc_set_b_center(0)
