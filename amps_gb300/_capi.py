@@ -163,6 +163,7 @@ SIGNATURES = {
     "amps_gpu_autotune": (C.c_int, [P, D]),
     "amps_gpu_get_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "amps_gpu_set_arrivals_chunk": (C.c_int, [P, C.c_int]),
+    "amps_gpu_set_b_center": (C.c_int, [P, C.c_int]),
     "amps_gpu_get_particle_tuning": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), D]),
     "amps_gpu_set_kernel_timing": (C.c_int, [P, C.c_int]),
     "amps_gpu_get_kernel_times": (C.c_int, [P, C.POINTER(C.c_char_p), D, LL, C.c_int,

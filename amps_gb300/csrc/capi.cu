@@ -199,9 +199,10 @@ cudaError_t enqueue_particle_step(amps_gpu_ctx* c, bool deposit) {
 // The same sequence as a CUDA graph, captured once per set of buffers it reads
 // (the corner-B slots swap every field solve, so two graphs alternate).
 cudaError_t launch_particle_step_graph(amps_gpu_ctx* c, bool deposit) {
-  const void* key[5] = {c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur,
+  const void* key[7] = {c->d_Eh, c->d_Bcor_prev, c->d_Bcor_cur,
                         (const void*)((uintptr_t)c->d_u[c->cur][0] ^ (c->has_wcorr ? 1u : 0u)),
-                        (const void*)(uintptr_t)c->arr_chunk};
+                        (const void*)(uintptr_t)c->arr_chunk, c->b_center ? c->d_Bc : nullptr,
+                        c->b_center ? c->d_Bc2 : nullptr};
   for (auto& g : c->graphs)
     if (g.deposit == deposit && std::memcmp(g.key, key, sizeof(key)) == 0)
       return cudaGraphLaunch(g.exec, c->stream);
@@ -713,7 +714,7 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   void* ptrs[] = {c->d_nbr, c->d_En, c->d_Eh, c->d_Bc, c->d_Bc2, c->d_Bcor_prev, c->d_Bcor_cur,
                   c->d_J, c->d_M, c->d_rhs, c->d_x, c->d_V, c->d_w, c->d_dinv, c->d_red, c->d_arn, c->d_xs, c->d_step,
                   c->d_Z, c->d_y32,
-                  c->d_stencil_push, c->d_stencil_dep, c->d_key, c->d_rank, c->d_base, c->d_cnt,
+                  c->d_stencil_push, c->d_stencil_dep, c->d_stencil_cprev, c->d_stencil_ccur, c->d_key, c->d_rank, c->d_base, c->d_cnt,
                   c->d_arr, c->d_stay, c->d_tmp, c->d_count, c->d_scan_part, c->d_flags,
                   c->d_cellM, c->d_cellJ, c->d_energy, c->d_ctab, c->d_hs, c->d_hp, c->d_hw, c->d_hwh, c->d_hwl,
                   c->d_bflag, c->d_bs, c->d_bc, c->d_bw, c->d_bwh, c->d_bwl,
@@ -862,7 +863,9 @@ amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* c, const double* E_n, const
       (s = upload_vec3(c, B_corner_prev, c->d_Bcor_prev, nv)) ||
       (s = upload_vec3(c, B_corner_cur, c->d_Bcor_cur, nv)))
     return s;
-  return AMPS_GPU_OK;
+  // the centre B^n a centre-B push reads before the first field solve
+  return cuda_check(c, cudaMemcpyAsync(c->d_Bc2, c->d_Bc, sizeof(double) * 3 * nc,
+                                       cudaMemcpyDeviceToDevice, c->stream), "B centre copy");
 }
 
 amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* c, double* E_n, double* E_half,
@@ -1148,6 +1151,20 @@ amps_gpu_status amps_gpu_autotune(amps_gpu_ctx* c, double* ms) {
   c->arr_tune_ms[0] = c->arr_tune_ms[1] = 0.0;
   c->arr_tune_n[0] = c->arr_tune_n[1] = 0;
   return field_autotune(c, ms);
+}
+
+amps_gpu_status amps_gpu_set_b_center(amps_gpu_ctx* c, int on) {
+  if (!c) return AMPS_GPU_INVALID_ARG;
+  if (on && c->amr)
+    return set_err(c, AMPS_GPU_INVALID_ARG, "set_b_center: centre B is built for uniform meshes");
+  cudaSetDevice(c->cfg.device);
+  if (on && !c->d_stencil_cprev) {
+    const size_t n = (size_t)c->nb * AMPS_CSC * 4;
+    if (dalloc(&c->d_stencil_cprev, n) || dalloc(&c->d_stencil_ccur, n))
+      return set_err(c, AMPS_GPU_CUDA_ERROR, "set_b_center: centre stencils");
+  }
+  c->b_center = on != 0;
+  return AMPS_GPU_OK;
 }
 
 amps_gpu_status amps_gpu_set_arrivals_chunk(amps_gpu_ctx* c, int chunk) {

@@ -25,6 +25,7 @@
 #define AMPS_SC 729         // stencil corners per block (9^3)
 #define AMPS_PUSH_STRIDE 8  // floats per stencil corner for the push: E3 B3 pad2
 #define AMPS_DEP_STRIDE 4   // floats per stencil corner for the deposit: B3 pad1
+#define AMPS_CSC 1000       // centre stencil per block (10^3 cell centres incl. the +-1 halo)
 #define AMPS_SLACK_MIN 32   // slack slots per cell on top of count/4 (rebuild)
 #define AMPS_CELLM 243      // per-cell mass-matrix partials: 27 weight monomials x 9
 
@@ -144,7 +145,7 @@ struct amps_gpu_ctx {
   bool use_graphs = false;
   struct StepGraph {
     bool deposit;
-    const void* key[5];
+    const void* key[7];
     cudaGraphExec_t exec;
   };
   std::vector<StepGraph> graphs;
@@ -163,6 +164,13 @@ struct amps_gpu_ctx {
   // arrivals staged 16 or 32 at a time (k_arrivals<DEP, CHUNK>); the autotuner
   // alternates them over arr_tune_left steps, timed by arr_ev, then keeps the
   // faster (arr_tune_ms: summed ms per variant, arr_tune_n: steps)
+  // magnetic field the particles see: false corners (the corner B slots),
+  // true cell centres (_PIC_FIELD_SOLVER_B_CENTER_BASED_: centre B^n for the
+  // push, B^{n+1} for the deposit, uniform meshes), staged per block as 10^3
+  // float4 (B3 pad) in d_stencil_cprev / d_stencil_ccur
+  bool b_center = false;
+  float* d_stencil_cprev = nullptr;
+  float* d_stencil_ccur = nullptr;
   int arr_chunk = 16;
   int arr_tune_left = 0;
   int arr_tune_cur = -1;  // variant of the step in flight, -1: none

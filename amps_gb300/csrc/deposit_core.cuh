@@ -66,16 +66,18 @@ __device__ __forceinline__ void kinetic_energy(FF& en, float v0, float v1, float
 // Stage one bulk copy per stencil into shared memory; returns false on timeout.
 __device__ bool stage_stencils(uint64_t* bar, void* dst0, const void* src0, uint32_t bytes0,
                                void* dst1, const void* src1, uint32_t bytes1,
-                               unsigned long long* flags) {
+                               unsigned long long* flags, void* dst2 = nullptr,
+                               const void* src2 = nullptr, uint32_t bytes2 = 0) {
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_arrive_expect_tx(bar, bytes0 + bytes1);
+    mbar_arrive_expect_tx(bar, bytes0 + bytes1 + bytes2);
     if (bytes0) bulk_copy_g2s(dst0, src0, bytes0, bar);
     if (bytes1) bulk_copy_g2s(dst1, src1, bytes1, bar);
+    if (bytes2) bulk_copy_g2s(dst2, src2, bytes2, bar);
   }
   if (!mbar_wait_bounded(bar, 0, kWaitLimit)) {
     if (threadIdx.x == 0) atomicAdd(flags + 2, 1ull);
@@ -107,11 +109,45 @@ __host__ __device__ __forceinline__ long long cellJ_at(long long cid, int ce) {
   return cid * 24 + ce;
 }
 
+// B at block-local offset u from a centre stencil (10^3 cell centres of the
+// block incl. the +-1 halo): CellCentered::Linear's trilinear weights
+// (pic_interpolation_routines.cpp:820-905: i0 = -1 below half a cell, else
+// (int)(u - 0.5), weight u - (i0 + 0.5))
+__device__ __forceinline__ void centre_b(const float4* __restrict__ sC, float u0, float u1, float u2,
+                                         float B[3]) {
+  const float u[3] = {u0, u1, u2};
+  int o[3];
+  float w[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    o[d] = u[d] < 0.5f ? -1 : (int)(u[d] - 0.5f);
+    w[d] = u[d] - ((float)o[d] + 0.5f);
+  }
+  const int s0 = (o[0] + 1) + 10 * ((o[1] + 1) + 10 * (o[2] + 1));
+  float Bs[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+  for (int c = 0; c < 2; c++)
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        const float W = (a ? w[0] : 1.f - w[0]) * (b ? w[1] : 1.f - w[1]) * (c ? w[2] : 1.f - w[2]);
+        const float4 q = sC[s0 + a + 10 * b + 100 * c];
+        Bs[c][0] = fmaf(W, q.x, Bs[c][0]);
+        Bs[c][1] = fmaf(W, q.y, Bs[c][1]);
+        Bs[c][2] = fmaf(W, q.z, Bs[c][2]);
+      }
+  B[0] = Bs[0][0] + Bs[1][0];
+  B[1] = Bs[0][1] + Bs[1][1];
+  B[2] = Bs[0][2] + Bs[1][2];
+}
+
 // The fields of one particle at block-local offset u inside cell (i,j,k), at
 // record position pos; wq = q weight correction of a depositing particle, 0
 // for a lane that deposits nothing (its k alpha and q alpha v, hence all its
-// products, are zero).  Adds its kinetic energy (weighted by wq) to en.
-template <int FS>
+// products, are zero).  Adds its kinetic energy (weighted by wq) to en.  sB:
+// the corner B stencil, or (CB) the centre B stencil.
+template <int FS, bool CB = false>
 __device__ __forceinline__ void stage_fields(float* __restrict__ rec, int pos,
                                              const float4* __restrict__ sB, float u0, float u1,
                                              float u2, float v0, float v1, float v2, int s,
@@ -124,18 +160,29 @@ __device__ __forceinline__ void stage_fields(float* __restrict__ rec, int pos,
   float w[8];
   w[0] = gx * gy * gz; w[1] = fx * gy * gz; w[2] = fx * fy * gz; w[3] = gx * fy * gz;
   w[4] = gx * gy * fz; w[5] = fx * gy * fz; w[6] = fx * fy * fz; w[7] = gx * fy * fz;
-  const int sb = i + 9 * (j + 9 * k);
-  const int coff[8] = {0, 1, 10, 9, 81, 82, 91, 90};
-  // two partial sums per component (corners 0-3, 4-7): six independent chains
-  float Bs[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+  float B0, B1, B2;
+  if (CB) {
+    float Bc[3];
+    centre_b(sB, u0, u1, u2, Bc);
+    B0 = Bc[0];
+    B1 = Bc[1];
+    B2 = Bc[2];
+  } else {
+    const int sb = i + 9 * (j + 9 * k);
+    const int coff[8] = {0, 1, 10, 9, 81, 82, 91, 90};
+    // two partial sums per component (corners 0-3, 4-7): six independent chains
+    float Bs[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
 #pragma unroll
-  for (int c = 0; c < 8; c++) {
-    const float4 q = sB[sb + coff[c]];
-    Bs[c >> 2][0] = fmaf(w[c], q.x, Bs[c >> 2][0]);
-    Bs[c >> 2][1] = fmaf(w[c], q.y, Bs[c >> 2][1]);
-    Bs[c >> 2][2] = fmaf(w[c], q.z, Bs[c >> 2][2]);
+    for (int c = 0; c < 8; c++) {
+      const float4 q = sB[sb + coff[c]];
+      Bs[c >> 2][0] = fmaf(w[c], q.x, Bs[c >> 2][0]);
+      Bs[c >> 2][1] = fmaf(w[c], q.y, Bs[c >> 2][1]);
+      Bs[c >> 2][2] = fmaf(w[c], q.z, Bs[c >> 2][2]);
+    }
+    B0 = Bs[0][0] + Bs[1][0];
+    B1 = Bs[0][1] + Bs[1][1];
+    B2 = Bs[0][2] + Bs[1][2];
   }
-  const float B0 = Bs[0][0] + Bs[1][0], B1 = Bs[0][1] + Bs[1][1], B2 = Bs[0][2] + Bs[1][2];
   const float h = st.qdt2m[s];
   const float h2 = h * h;
   const float c0 = 1.0f / (1.0f + h2 * (B0 * B0 + B1 * B1 + B2 * B2));

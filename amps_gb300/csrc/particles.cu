@@ -130,11 +130,26 @@ __device__ __forceinline__ int warp_reserve(bool active, int key, int* __restric
 }
 
 // ---------------------------------------------------------------------------
+// Per block: the corner stencils (push: E^{n+theta}, corner B^n; deposit:
+// corner B^{n+1}) and, with centre B (cp != nullptr), the centre stencils of
+// B^n (Bcp) and B^{n+1} (Bcc) over the block's cells and the +-1 halo, centre
+// (i, j, k) in -1..8 at (i+1) + 10 ((j+1) + 10 (k+1)).
 __global__ void k_pack_stencils(int nb, long long ncor, const int* __restrict__ nbr,
                                 const double* __restrict__ Eh, const double* __restrict__ Bprev,
                                 const double* __restrict__ Bcur, float* __restrict__ sp,
-                                float* __restrict__ sd) {
+                                float* __restrict__ sd, const double* __restrict__ Bcp,
+                                const double* __restrict__ Bcc, float4* __restrict__ cp,
+                                float4* __restrict__ cc) {
   const int b = blockIdx.x;
+  if (cp) {
+    for (int s = threadIdx.x; s < AMPS_CSC; s += blockDim.x) {
+      const int cid = local_id(nbr, b, s % 10 - 1, (s / 10) % 10 - 1, s / 100 - 1);
+      cp[(size_t)b * AMPS_CSC + s] =
+          make_float4((float)Bcp[cid], (float)Bcp[ncor + cid], (float)Bcp[2 * ncor + cid], 0.f);
+      cc[(size_t)b * AMPS_CSC + s] =
+          make_float4((float)Bcc[cid], (float)Bcc[ncor + cid], (float)Bcc[2 * ncor + cid], 0.f);
+    }
+  }
   for (int s = threadIdx.x; s < AMPS_SC; s += blockDim.x) {
     const int i = s % 9, j = (s / 9) % 9, k = s / 81;
     const int cid = local_id(nbr, b, i, j, k);
@@ -156,6 +171,8 @@ struct StepArgs {
   int* stay;
   const float* st_push;
   const float* st_dep;
+  const float4* st_cprev;  // centre B stencils (centre-B runs), else nullptr
+  const float4* st_ccur;
   PBuf p;         // current slots
   PBuf ovf;       // overflow list (the other buffer)
   int* ovf_key;
@@ -202,18 +219,23 @@ __device__ __forceinline__ void lapenta(float h, const float E[3], const float B
   v[2] = 2.f * a2 - v[2];
 }
 
-template <bool DEP, bool AMR>
+// CB: the particles see B interpolated from the cell centres (B^n from the
+// centre stencil for the push, B^{n+1} for the deposit); E from the corners.
+template <bool DEP, bool AMR, bool CB = false>
 __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
+  constexpr int kDepSC = CB ? AMPS_CSC : AMPS_SC;
   float4* s_push = s_dyn;                         // 729 x 2 float4
-  float4* s_dep = s_dyn + 2 * AMPS_SC;            // 729 float4
-  float* s_rec = reinterpret_cast<float*>(s_dyn + 3 * AMPS_SC);  // kWarps x kFields x kFS
+  float4* s_dep = s_dyn + 2 * AMPS_SC;            // 729 float4 corners, or 1000 centres (CB)
+  float4* s_cprev = s_dep + kDepSC;               // 1000 float4 centres of B^n (CB)
+  float* s_rec = reinterpret_cast<float*>(s_cprev + (CB ? AMPS_CSC : 0));  // kWarps x kFields x kFS
   __shared__ __align__(8) uint64_t bar;
   __shared__ double s_en[kWarps];
   const int b = blockIdx.x, k = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t bp = AMPS_SC * AMPS_PUSH_STRIDE * sizeof(float);
-  const uint32_t bd = DEP ? AMPS_SC * AMPS_DEP_STRIDE * sizeof(float) : 0;
+  const uint32_t bd = DEP ? kDepSC * 4 * sizeof(float) : 0;
+  const uint32_t bc = CB ? AMPS_CSC * sizeof(float4) : 0;
   const int j = wid;
   // slot range and occupancy of the row's 8 cells, one lane per cell
   int mb0 = 0, mn0 = 0;
@@ -243,8 +265,11 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
     }
   };
   prefetch(0, lane);  // in flight while the stencils are staged
+  const void* dep_src = CB ? (const void*)(a.st_ccur + (size_t)b * AMPS_CSC)
+                           : (const void*)(a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE);
   if (!stage_stencils(&bar, s_push, a.st_push + (size_t)b * AMPS_SC * AMPS_PUSH_STRIDE, bp, s_dep,
-                      a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE, bd, a.flags))
+                      dep_src, bd, a.flags, s_cprev, CB ? a.st_cprev + (size_t)b * AMPS_CSC : nullptr,
+                      bc))
     return;
   float* rec = s_rec + wid * kFields * kFS;
   int fA, fB;
@@ -293,12 +318,14 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
                               (cc ? f[2] : 1.f - f[2]);
               const int sidx = (ic[0] + aa) + 9 * (ic[1] + bb) + 81 * (ic[2] + cc);
               const ulonglong2 q0v = reinterpret_cast<const ulonglong2*>(s_push)[2 * sidx];
-              const ulonglong2 q1v = reinterpret_cast<const ulonglong2*>(s_push)[2 * sidx + 1];
               unsigned long long ww;
               asm("mov.b64 %0, {%1, %1};" : "=l"(ww) : "f"(w));
               ffma2(eb[cc][0], ww, q0v.x);
               ffma2(eb[cc][1], ww, q0v.y);
-              ffma2(eb[cc][2], ww, q1v.x);
+              if (!CB) {
+                const ulonglong2 q1v = reinterpret_cast<const ulonglong2*>(s_push)[2 * sidx + 1];
+                ffma2(eb[cc][2], ww, q1v.x);
+              }
             }
         float eb_f[6];
 #pragma unroll
@@ -308,7 +335,9 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
           eb_f[2 * t] = lo.x + hi.x;
           eb_f[2 * t + 1] = lo.y + hi.y;
         }
-        const float E[3] = {eb_f[0], eb_f[1], eb_f[2]}, B[3] = {eb_f[3], eb_f[4], eb_f[5]};
+        const float E[3] = {eb_f[0], eb_f[1], eb_f[2]};
+        float B[3] = {eb_f[3], eb_f[4], eb_f[5]};
+        if (CB) centre_b(s_cprev, u[0], u[1], u[2], B);
         lapenta(a.st.qdt2m[s], E, B, v);
         bool far = false, nearf = false;
         int nbk = b;
@@ -369,7 +398,7 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
       // every lane stages its position; only stayers carry weight (movers are
       // deposited by k_arrivals in their destination cell)
       if (DEP)
-        stage_fields<kFS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], act ? s : 0,
+        stage_fields<kFS, CB>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], act ? s : 0,
                           stays ? wcv : 0.f, i, j, k, a.st, inv_vol, en_row);
       // movers: slack of the destination cell, else the overflow list
       const bool mover = act && !stays && key >= 0;
@@ -655,7 +684,7 @@ constexpr int kArrChunk = 16;
 constexpr int kFSArr = kArrChunk + 4;  // field stride of staged fields at 16 lanes
 constexpr int kLayer = AMPS_NC * AMPS_NC;
 
-template <bool DEP, int CHUNK>
+template <bool DEP, int CHUNK, bool CB = false>
 __global__ void __launch_bounds__(256, CHUNK == 16 ? 3 : 2) k_arrivals(StepArgs a) {
   constexpr int FS = CHUNK + 4;  // field stride of the staged fields
   extern __shared__ __align__(16) float4 s_dyn[];
@@ -666,8 +695,10 @@ __global__ void __launch_bounds__(256, CHUNK == 16 ? 3 : 2) k_arrivals(StepArgs 
   const int b = blockIdx.x, k = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   // the few arrivals read the block's B stencil from global memory (L2-resident:
-  // 11.7 KB per block) instead of waiting for a staged copy at CTA start
-  const float4* s_dep = reinterpret_cast<const float4*>(a.st_dep) + (size_t)b * AMPS_SC;
+  // 11.7 KB per block, 16 KB of centres) instead of waiting for a staged copy
+  // at CTA start
+  const float4* s_dep = CB ? a.st_ccur + (size_t)b * AMPS_CSC
+                           : reinterpret_cast<const float4*>(a.st_dep) + (size_t)b * AMPS_SC;
   int4 cv = make_int4(0, 0, 0, 0);
   bool has = false;
   if (threadIdx.x < kLayer) {
@@ -727,7 +758,7 @@ __global__ void __launch_bounds__(256, CHUNK == 16 ? 3 : 2) k_arrivals(StepArgs 
       if (DEP) {
         // positions past the chunk's arrivals stage zero weight
         if (lane < CHUNK)
-          stage_fields<FS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+          stage_fields<FS, CB>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
                                act ? wcv : 0.f, i, j, k, a.st, inv_vol, en_w);
         __syncwarp();
         tile.accumulate<FS>(rec, (min(CHUNK, na - q0) + 3) & ~3, fA, fB);
@@ -753,7 +784,7 @@ __global__ void __launch_bounds__(256, CHUNK == 16 ? 3 : 2) k_arrivals(StepArgs 
 // to -1.  Entries whose cell is full are counted in *left and stay in the list
 // for the relayout, which files them in the same cell.  Every entry is
 // deposited here like an arrival (DEP).
-template <bool DEP>
+template <bool DEP, bool CB = false>
 __global__ void __launch_bounds__(256) k_ovf_place(StepArgs a, long long n_ovf,
                                                    unsigned long long* left) {
   extern __shared__ __align__(16) float4 s_dyn[];
@@ -789,11 +820,12 @@ __global__ void __launch_bounds__(256) k_ovf_place(StepArgs a, long long n_ovf,
     int fA, fB;
     lane_fields(lane, fA, fB);
     const int b = key / AMPS_CPB, l = key % AMPS_CPB;
-    const float4* s_dep = reinterpret_cast<const float4*>(a.st_dep) + (size_t)b * AMPS_SC;
+    const float4* s_dep = CB ? a.st_ccur + (size_t)b * AMPS_CSC
+                             : reinterpret_cast<const float4*>(a.st_dep) + (size_t)b * AMPS_SC;
     FF en{0.f, 0.f};
     // the particle at position 0, zero weight at positions 1..3
     if (lane < 4)
-      stage_fields<kFSArr>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
+      stage_fields<kFSArr, CB>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s,
                            lane == 0 ? wcv : 0.f, l & (AMPS_NC - 1), (l / AMPS_NC) & (AMPS_NC - 1),
                            l / (AMPS_NC * AMPS_NC), a.st, block_inv_vol(a, b), en);
     __syncwarp();
@@ -875,17 +907,20 @@ __global__ void __launch_bounds__(256) k_offset_copy(long long n, const int* __r
   if (i < n) dst[i] = (int)(off + src[i]);
 }
 
-// Full deposition over the compact layout.
+// Full deposition over the compact layout (CB: B^{n+1} from the centre stencil).
+template <bool CB = false>
 __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
   extern __shared__ __align__(16) float4 s_dyn[];
+  constexpr int kDepSC = CB ? AMPS_CSC : AMPS_SC;
   float4* s_dep = s_dyn;
-  float* s_rec = reinterpret_cast<float*>(s_dyn + AMPS_SC);
+  float* s_rec = reinterpret_cast<float*>(s_dyn + kDepSC);
   __shared__ __align__(8) uint64_t bar;
   __shared__ double s_en[kWarps];
   const int b = blockIdx.x, k = blockIdx.y;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (!stage_stencils(&bar, s_dep, a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE,
-                      AMPS_SC * AMPS_DEP_STRIDE * sizeof(float), nullptr, nullptr, 0, a.flags))
+  const void* src = CB ? (const void*)(a.st_ccur + (size_t)b * AMPS_CSC)
+                       : (const void*)(a.st_dep + (size_t)b * AMPS_SC * AMPS_DEP_STRIDE);
+  if (!stage_stencils(&bar, s_dep, src, kDepSC * 4 * sizeof(float), nullptr, nullptr, 0, a.flags))
     return;
   float* rec = s_rec + wid * kFields * kFS;
   int fA, fB;
@@ -910,8 +945,8 @@ __global__ void __launch_bounds__(256) k_deposit(StepArgs a) {
         s = a.p.sp[p];
         wq = a.p.wc ? a.p.wc[p] : 1.0f;
       }
-      stage_fields<kFS>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wq, i, j, k,
-                        a.st, inv_vol, en);
+      stage_fields<kFS, CB>(rec, lane, s_dep, u[0], u[1], u[2], v[0], v[1], v[2], s, wq, i, j, k,
+                            a.st, inv_vol, en);
       __syncwarp();
       tile.accumulate<kFS>(rec, (min(32, n0 - q0) + 3) & ~3, fA, fB);
       __syncwarp();
@@ -1720,6 +1755,8 @@ StepArgs step_args(amps_gpu_ctx* c) {
   a.stay = c->d_stay;
   a.st_push = c->d_stencil_push;
   a.st_dep = c->d_stencil_dep;
+  a.st_cprev = c->b_center ? reinterpret_cast<const float4*>(c->d_stencil_cprev) : nullptr;
+  a.st_ccur = c->b_center ? reinterpret_cast<const float4*>(c->d_stencil_ccur) : nullptr;
   a.p = pbuf(c, c->cur);
   a.ovf = pbuf(c, c->cur ^ 1);
   a.ovf_key = c->d_key;
@@ -1739,10 +1776,13 @@ StepArgs step_args(amps_gpu_ctx* c) {
   return a;
 }
 
-size_t smem_push(bool dep) {
-  return (size_t)AMPS_SC * (2 + 1) * sizeof(float4) + (dep ? kWarps * kFields * kFS * sizeof(float) : 0);
+size_t smem_push(bool dep, bool cb = false) {
+  return (size_t)(2 * AMPS_SC + (cb ? 2 * AMPS_CSC : AMPS_SC)) * sizeof(float4) +
+         (dep ? kWarps * kFields * kFS * sizeof(float) : 0);
 }
-size_t smem_dep() { return (size_t)AMPS_SC * sizeof(float4) + kWarps * kFields * kFS * sizeof(float); }
+size_t smem_dep(bool cb = false) {
+  return (size_t)(cb ? AMPS_CSC : AMPS_SC) * sizeof(float4) + kWarps * kFields * kFS * sizeof(float);
+}
 size_t smem_arr(int chunk) { return (size_t)kWarps * kFields * (chunk + 4) * sizeof(float); }
 
 void set_smem_attrs() {
@@ -1756,7 +1796,16 @@ void set_smem_attrs() {
   cudaFuncSetAttribute(k_arrivals<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(16));
   cudaFuncSetAttribute(k_arrivals<true, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(32));
   cudaFuncSetAttribute(k_arrivals<false, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(32));
-  cudaFuncSetAttribute(k_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep());
+  cudaFuncSetAttribute(k_deposit<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep(false));
+  cudaFuncSetAttribute(k_deposit<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_dep(true));
+  cudaFuncSetAttribute(k_push_deposit<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_push(true, true));
+  cudaFuncSetAttribute(k_push_deposit<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_push(false, true));
+  cudaFuncSetAttribute(k_arrivals<true, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(16));
+  cudaFuncSetAttribute(k_arrivals<false, 16, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(16));
+  cudaFuncSetAttribute(k_arrivals<true, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(32));
+  cudaFuncSetAttribute(k_arrivals<false, 32, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_arr(32));
   done = true;
 }
 
@@ -1832,8 +1881,14 @@ cudaError_t launch_pack_stencils(amps_gpu_ctx* c, const double* Eh, const double
                                  const double* Bcur) {
   if (c->amr) return launch_amr_pack(c, Eh, Bprev, Bcur);
   TimedLaunch t(c, "pack_stencils");
-  k_pack_stencils<<<c->nb, 256, 0, c->stream>>>(c->nb, c->ncor, c->d_nbr, Eh, Bprev, Bcur,
-                                                 c->d_stencil_push, c->d_stencil_dep);
+  // centre B: B^n in the scratch slot d_Bc2 (the field solve swaps it there;
+  // the field import copies the imported centres into it), B^{n+1} in d_Bc
+  const bool cb = c->b_center;
+  k_pack_stencils<<<c->nb, 256, 0, c->stream>>>(
+      c->nb, c->ncor, c->d_nbr, Eh, Bprev, Bcur, c->d_stencil_push, c->d_stencil_dep,
+      cb ? c->d_Bc2 : nullptr, cb ? c->d_Bc : nullptr,
+      cb ? reinterpret_cast<float4*>(c->d_stencil_cprev) : nullptr,
+      cb ? reinterpret_cast<float4*>(c->d_stencil_ccur) : nullptr);
   return cudaGetLastError();
 }
 
@@ -1856,7 +1911,10 @@ cudaError_t launch_deposit(amps_gpu_ctx* c) {
   StepArgs a = step_args(c);
   {
     TimedLaunch t(c, "deposit");
-    k_deposit<<<dim3(c->nb, AMPS_NC), kWarps * 32, smem_dep(), c->stream>>>(a);
+    if (c->b_center)
+      k_deposit<true><<<dim3(c->nb, AMPS_NC), kWarps * 32, smem_dep(true), c->stream>>>(a);
+    else
+      k_deposit<false><<<dim3(c->nb, AMPS_NC), kWarps * 32, smem_dep(false), c->stream>>>(a);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -1949,6 +2007,11 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
         k_push_deposit<true, true><<<grid, kWarps * 32, smem_push(true), c->stream>>>(a);
       else
         k_push_deposit<false, true><<<grid, kWarps * 32, smem_push(false), c->stream>>>(a);
+    } else if (c->b_center) {
+      if (deposit)
+        k_push_deposit<true, false, true><<<grid, kWarps * 32, smem_push(true, true), c->stream>>>(a);
+      else
+        k_push_deposit<false, false, true><<<grid, kWarps * 32, smem_push(false, true), c->stream>>>(a);
     } else {
       if (deposit)
         k_push_deposit<true, false><<<grid, kWarps * 32, smem_push(true), c->stream>>>(a);
@@ -1971,16 +2034,17 @@ cudaError_t launch_push_step(amps_gpu_ctx* c, bool deposit) {
       cudaEventRecord(c->arr_ev[0], c->stream);
     }
     TimedLaunch t(c, "arrivals");
-    if (chunk == 32) {
-      if (deposit)
-        k_arrivals<true, 32><<<grid, kWarps * 32, smem_arr(32), c->stream>>>(a);
-      else
-        k_arrivals<false, 32><<<grid, kWarps * 32, smem_arr(32), c->stream>>>(a);
-    } else {
-      if (deposit)
-        k_arrivals<true, 16><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(a);
-      else
-        k_arrivals<false, 16><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(a);
+    const size_t sm = smem_arr(chunk);
+    const int v = (chunk == 32 ? 1 : 0) | (deposit ? 2 : 0) | (c->b_center ? 4 : 0);
+    switch (v) {
+      case 0: k_arrivals<false, 16><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      case 1: k_arrivals<false, 32><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      case 2: k_arrivals<true, 16><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      case 3: k_arrivals<true, 32><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      case 4: k_arrivals<false, 16, true><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      case 5: k_arrivals<false, 32, true><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      case 6: k_arrivals<true, 16, true><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
+      default: k_arrivals<true, 32, true><<<grid, kWarps * 32, sm, c->stream>>>(a); break;
     }
     if (tune) cudaEventRecord(c->arr_ev[1], c->stream);
   }
@@ -2000,7 +2064,10 @@ cudaError_t particles_place_overflow(amps_gpu_ctx* c, long long n_overflow, bool
   {
     TimedLaunch t(c, "overflow_place");
     const unsigned grid = (unsigned)((n_overflow + kWarps - 1) / kWarps);
-    if (deposit)
+    if (deposit && c->b_center)
+      k_ovf_place<true, true><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(step_args(c), n_overflow,
+                                                                            c->d_flags + 7);
+    else if (deposit)
       k_ovf_place<true><<<grid, kWarps * 32, smem_arr(16), c->stream>>>(step_args(c), n_overflow,
                                                                       c->d_flags + 7);
     else

@@ -257,6 +257,14 @@ class EcsimContext:
         self._check(self.lib.amps_gpu_import_fields(self.h, *[ptr(a, C.c_double) for a in arrs]),
                     "import_fields")
 
+    def set_b_center(self, on=True):
+        """True: the particles see B interpolated from the cell centres
+        (_PIC_FIELD_SOLVER_B_CENTER_BASED_, the reference's default build;
+        CellCentered::Linear, pic_interpolation_routines.cpp:820-905): the push
+        reads centre B^n, the deposit centre B^{n+1}; E stays at the corners.
+        False (default): the corner B slots.  Uniform meshes only."""
+        self._check(self.lib.amps_gpu_set_b_center(self.h, 1 if on else 0), "set_b_center")
+
     def export_fields(self, out=None):
         """corner E^n, E^{n+theta}, B prev/cur and centre B; out: dict of
         arrays to fill (e.g. page-locked ones)"""

@@ -200,6 +200,16 @@ amps_gpu_status amps_gpu_num_particles(amps_gpu_ctx* ctx, long long* n);
 amps_gpu_status amps_gpu_import_fields(amps_gpu_ctx* ctx, const double* E_n, const double* E_half,
                                        const double* B_center, const double* B_corner_prev,
                                        const double* B_corner_cur);
+/* Where the magnetic field the particles see is interpolated from.  on = 0
+ * (default): the corner B slots (_PIC_FIELD_SOLVER_B_CORNER_BASED_).  on = 1:
+ * the cell centres (_PIC_FIELD_SOLVER_B_CENTER_BASED_, the reference's default
+ * build: Lapenta2017 pic_mover_boris.cpp:979, ProcessCell
+ * pic_field_solver_ecsim.cpp:2050-2117, CellCentered::Linear
+ * pic_interpolation_routines.cpp:820-905): the push reads B^n, the deposit B^{n+1} (after a
+ * field solve; both the imported B_center before the first), E stays at the
+ * corners.  Uniform meshes only (INVALID_ARG on AMR).  The no-alloc entry
+ * point always reads corner B. */
+amps_gpu_status amps_gpu_set_b_center(amps_gpu_ctx* ctx, int on);
 amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* ctx, double* E_n, double* E_half,
                                        double* B_center, double* B_corner_prev,
                                        double* B_corner_cur);
