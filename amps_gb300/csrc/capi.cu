@@ -735,6 +735,9 @@ amps_gpu_status amps_gpu_destroy(amps_gpu_ctx* c) {
   if (c->h_flags) cudaFreeHost(c->h_flags);
   if (c->h_energy) cudaFreeHost(c->h_energy);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
+  for (auto& e : c->copy_ev)
+    if (e) cudaEventDestroy(e);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return AMPS_GPU_OK;

@@ -56,6 +56,10 @@ struct amps_gpu_ctx {
   long long ncor = 0;       // cells (= owned corners on a uniform mesh)
   long long nvc = 0;        // corners carrying unknowns (= ncor uniform, unique corners on AMR)
   cudaStream_t stream = nullptr;
+  // device-to-host copies that overlap the producing kernels (created on
+  // first use) and the events that order them, one per chunk
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev[9] = {nullptr};
   std::string err;
 
   // mesh
@@ -278,6 +282,9 @@ amps_gpu_status layout_upload(amps_gpu_ctx* c, const double* host, void* dev, lo
 amps_gpu_status layout_download(amps_gpu_ctx* c, const void* dev, double* host, long long n,
                                 int ncomp, bool dev_f32);
 amps_gpu_status layout_cell_moments(amps_gpu_ctx* c, double* hJ, double* hM);
+// device address of a page-locked host array (kernels write it across the host
+// link directly), or null for pageable memory
+double* host_mapped(double* host);
 cudaError_t launch_relboris(amps_gpu_ctx* c, const double* E, const double* B, double dt_total,
                             double c_light, long long max_sub, bool rel = true);
 cudaError_t launch_deposit(amps_gpu_ctx* c);

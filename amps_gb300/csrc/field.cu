@@ -950,7 +950,10 @@ unsigned gridr(long long n, int cap = kRedBlocks, int ept = 4) {
 
 // ============================================================================
 // FP32 pair split of an operator input into the context's scratch (hi_only:
-// the FP32 rounding alone)
+// the FP32 rounding alone).  d_xs is also where k_start_ff / k_arnoldi_ff
+// leave the FP32 input of the next Krylov vector's operator application: this
+// split, k_rhs and the AMR operators overwrite it, so none of them may run
+// between an Arnoldi step and the operator application that follows it.
 static cudaError_t split_input(amps_gpu_ctx* c, const double* x, const double* dinv,
                                bool hi_only = false) {
   const long long n = 3 * c->nvc;
@@ -1115,6 +1118,8 @@ amps_gpu_status gmres_solve(amps_gpu_ctx* c, double tol, int maxit, int precond,
   // the FP32 operator input of the next Krylov vector is written by the step
   // that makes the vector (k_start_ff, k_arnoldi_ff) when the operator takes V
   // directly (no learned directions, FP32 inner operator)
+  // (nothing that writes d_xs -- split_input, k_rhs, the AMR operators -- runs
+  // between a step that writes it and the inner_matvec that reads it)
   const bool pre_xf = !flexible && c->inner_fp32;
   if (pre_xf && !c->d_xs) CK(cudaMalloc(reinterpret_cast<void**>(&c->d_xs), sizeof(float) * 2 * n));
   float* xf_next = pre_xf ? c->d_xs : nullptr;

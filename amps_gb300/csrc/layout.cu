@@ -29,30 +29,39 @@ __device__ __forceinline__ long long dev_index(const Perm& p, long long h) {
   return (long long)b * AMPS_CPB + (I & 7) + 8 * ((J & 7) + 8 * (K & 7));
 }
 
-// dev[comp*n + dev(h)] = host[h*ncomp + comp]   (T = double or float on device)
+// dev[comp*n + dev(h)] = host[h*ncomp + comp]   (T = double or float on device).
+// One thread per host element, in host order: a warp reads 256 consecutive
+// host bytes (whole lines across the host link for a page-locked array); the
+// scattered device writes stay in HBM / L2.
 template <class T>
 __global__ void __launch_bounds__(256) k_to_device(long long n, int ncomp, Perm p,
                                                    const double* __restrict__ host,
                                                    T* __restrict__ dev) {
-  for (long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x; h < n;
-       h += (long long)gridDim.x * blockDim.x) {
-    const long long d = dev_index(p, h);
-    for (int cc = 0; cc < ncomp; cc++) dev[(size_t)cc * n + d] = (T)host[(size_t)h * ncomp + cc];
+  const long long total = n * ncomp;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long h = t / ncomp;
+    const int cc = (int)(t - h * ncomp);
+    dev[(size_t)cc * n + dev_index(p, h)] = (T)host[t];
   }
 }
 
 __device__ __forceinline__ double to_f64(double v) { return v; }
 __device__ __forceinline__ double to_f64(float v) { return widen(v); }
 
-// host[h*ncomp + comp] = dev[comp*n + dev(h)]
+// host[h*ncomp + comp] = dev[comp*n + dev(h)], one thread per host element in
+// host order (coalesced writes across the host link; the link, ~190 GB/s
+// device to host, bounds a page-locked download)
 template <class T>
 __global__ void __launch_bounds__(256) k_to_host(long long n, int ncomp, Perm p,
                                                  const T* __restrict__ dev,
                                                  double* __restrict__ host) {
-  for (long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x; h < n;
-       h += (long long)gridDim.x * blockDim.x) {
-    const long long d = dev_index(p, h);
-    for (int cc = 0; cc < ncomp; cc++) host[(size_t)h * ncomp + cc] = to_f64(dev[(size_t)cc * n + d]);
+  const long long total = n * ncomp;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long h = t / ncomp;
+    const int cc = (int)(t - h * ncomp);
+    host[t] = to_f64(dev[(size_t)cc * n + dev_index(p, h)]);
   }
 }
 
@@ -85,7 +94,20 @@ unsigned grid_of(long long n) {
 
 Perm perm_of(const amps_gpu_ctx* c) { return Perm{c->cfg.nbx, c->cfg.nby, c->amr}; }
 
+}  // namespace
+
 // device address of a page-locked host array, or null for pageable memory
+double* host_mapped(double* host) {
+  cudaPointerAttributes at;
+  if (!host || cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? static_cast<double*>(at.devicePointer) : nullptr;
+}
+
+namespace {
+
 template <class T>
 T* mapped(T* host) {
   cudaPointerAttributes at;
@@ -126,11 +148,11 @@ amps_gpu_status layout_upload(amps_gpu_ctx* c, const double* host, void* dev, lo
   }
   if (e == cudaSuccess) {
     if (dev_f32)
-      k_to_device<float><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c), st,
-                                                           static_cast<float*>(dev));
+      k_to_device<float><<<grid_of(n * ncomp), 256, 0, c->stream>>>(n, ncomp, perm_of(c), st,
+                                                                   static_cast<float*>(dev));
     else
-      k_to_device<double><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c), st,
-                                                            static_cast<double*>(dev));
+      k_to_device<double><<<grid_of(n * ncomp), 256, 0, c->stream>>>(n, ncomp, perm_of(c), st,
+                                                                    static_cast<double*>(dev));
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -145,11 +167,11 @@ amps_gpu_status layout_download(amps_gpu_ctx* c, const void* dev, double* host, 
   double* st = direct ? direct : host_stage(c, bytes);
   if (!st) return set_err(c, AMPS_GPU_CUDA_ERROR, "layout staging allocation failed");
   if (dev_f32)
-    k_to_host<float><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c),
-                                                       static_cast<const float*>(dev), st);
+    k_to_host<float><<<grid_of(n * ncomp), 256, 0, c->stream>>>(n, ncomp, perm_of(c),
+                                                               static_cast<const float*>(dev), st);
   else
-    k_to_host<double><<<grid_of(n), 256, 0, c->stream>>>(n, ncomp, perm_of(c),
-                                                        static_cast<const double*>(dev), st);
+    k_to_host<double><<<grid_of(n * ncomp), 256, 0, c->stream>>>(n, ncomp, perm_of(c),
+                                                                static_cast<const double*>(dev), st);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !direct) e = cudaMemcpyAsync(host, st, bytes, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);

@@ -337,54 +337,62 @@ __global__ void __launch_bounds__(256) k_particle_cfl(CflArgs a) {
 // 3 dig(dy) + 9 dig(dz), dig(0) = 0, dig(-1) = 1, dig(+1) = 2, d the partner
 // corner's offset in the cell (IndexMatrix, :1889-1891) and the block the
 // cell's partial of the pair's weight monomial (already divided by V).  One
-// thread per (corner, output element); hanging corners get their own sums.
-__global__ void __launch_bounds__(256) k_amr_corner_moments(
-    long long nvc, const int* __restrict__ start, const int* __restrict__ ent,
+// warp per corner: for each of the corner's cells (in CSR order) its 8 partner
+// corners x 9 components (distinct slots) are added to the corner's 243 + 3
+// FP64 sums in shared memory, which the warp then writes as one contiguous
+// run (whole lines across the host link for a page-locked destination).
+// Hanging corners get their own sums.  Corners [c0, c1); J or M may be null.
+constexpr int kCmWarps = 8;
+__device__ __forceinline__ int slot_digit(int d) { return d == 0 ? 0 : (d < 0 ? 1 : 2); }
+__global__ void __launch_bounds__(kCmWarps * 32) k_amr_corner_moments(
+    long long c0, long long c1, const int* __restrict__ start, const int* __restrict__ ent,
     const float* __restrict__ cellM, const float* __restrict__ cellJ, const double* __restrict__ bdx,
     double* __restrict__ J, double* __restrict__ M) {
-  const long long total = nvc * 246;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long cc = t / 246;
-    const int el = (int)(t % 246);
-    double sum = 0.0;
-    if (el < 243) {
-      const int slot = el / 9, comp = el % 9;
-      const int dg[3] = {slot % 3, (slot / 3) % 3, slot / 9};
-      int d[3];
-#pragma unroll
-      for (int a = 0; a < 3; a++) d[a] = dg[a] == 0 ? 0 : (dg[a] == 1 ? -1 : 1);
-      for (int e = start[cc]; e < start[cc + 1]; e++) {
-        const int en = ent[e];
-        const long long cell = en >> 3;
-        const int q = en & 7;
-        const int o[3] = {(q & 1) + d[0], ((q >> 1) & 1) + d[1], (q >> 2) + d[2]};
-        if (o[0] < 0 || o[0] > 1 || o[1] < 0 || o[1] > 1 || o[2] < 0 || o[2] > 1) continue;
-        const int q2 = o[0] + 2 * o[1] + 4 * o[2];
-        // binary offset -> table order of ProcessCell's corners
-        const int t1 = q ^ ((q >> 1) & 1), t2 = q2 ^ ((q2 >> 1) & 1);
-        sum += (double)cellM[cellM_at(cell, pair_monomial(t1, t2) * 9 + comp)];
+  __shared__ double s_acc[kCmWarps][246];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* acc = s_acc[wid];
+  for (long long cc = c0 + (long long)blockIdx.x * kCmWarps + wid; cc < c1;
+       cc += (long long)gridDim.x * kCmWarps) {
+    for (int t = lane; t < 246; t += 32) acc[t] = 0.0;
+    __syncwarp();
+    const int e1 = start[cc + 1];
+    for (int e = start[cc]; e < e1; e++) {
+      const int en = ent[e];
+      const long long cell = en >> 3;
+      const int q = en & 7;  // the corner's offset bits in the cell (x, y, z)
+      if (M) {
+        for (int k = lane; k < 72; k += 32) {
+          const int q2 = k / 9, comp = k - 9 * q2;
+          const int ax = (q & 1) + (q2 & 1), ay = ((q >> 1) & 1) + ((q2 >> 1) & 1),
+                    az = (q >> 2) + (q2 >> 2);
+          const int slot = slot_digit((q2 & 1) - (q & 1)) + 3 * slot_digit(((q2 >> 1) & 1) - ((q >> 1) & 1)) +
+                           9 * slot_digit((q2 >> 2) - (q >> 2));
+          acc[slot * 9 + comp] += (double)cellM[cellM_at(cell, (ax + 3 * ay + 9 * az) * 9 + comp)];
+        }
       }
-      M[cc * 243 + el] = sum;
-    } else {
-      const int comp = el - 243;
-      for (int e = start[cc]; e < start[cc + 1]; e++) {
-        const int en = ent[e];
-        const long long cell = en >> 3;
-        const int q = en & 7;
+      if (J && lane < 3) {
         const double dx = bdx[cell / AMPS_CPB];
-        sum += (double)cellJ[cellJ_at(cell, (q ^ ((q >> 1) & 1)) * 3 + comp)] / (dx * dx * dx);
+        acc[243 + lane] += (double)cellJ[cellJ_at(cell, (q ^ ((q >> 1) & 1)) * 3 + lane)] / (dx * dx * dx);
       }
-      J[cc * 3 + comp] = sum;
+      __syncwarp();
     }
+    if (M)
+      for (int t = lane; t < 243; t += 32) M[cc * 243 + t] = acc[t];
+    if (J && lane < 3) J[cc * 3 + lane] = acc[243 + lane];
+    __syncwarp();
   }
 }
 
 // the corner-layout moments of an AMR context (k_amr_corner_moments) into
-// host J[nvc][3], M[nvc][243] (mesh corner numbering)
+// host J[nvc][3], M[nvc][243] (mesh corner numbering).  The kernel writes a
+// device buffer in kCmChunks corner ranges; each range's copy to the host
+// runs on the copy stream while the kernel produces the next, so a
+// page-locked destination fills at the host link's rate.
+constexpr int kCmChunks = 8;
 amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M) {
   amps_gpu_status st = corner_csr_setup(c);
   if (st) return st;
+  if (!J && !M) return AMPS_GPU_OK;
   if (!c->d_amrJ) {
     if (cudaMalloc(reinterpret_cast<void**>(&c->d_amrJ), sizeof(double) * 3 * (size_t)c->nvc) != cudaSuccess ||
         cudaMalloc(reinterpret_cast<void**>(&c->d_amrM), sizeof(double) * 243 * (size_t)c->nvc) != cudaSuccess) {
@@ -394,22 +402,41 @@ amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M)
       return set_err(c, AMPS_GPU_CUDA_ERROR, "export_moments: allocation failed");
     }
   }
-  {
-    TimedLaunch t(c, "amr_corner_moments");
-    const long long total = c->nvc * 246;
-    const long long blocks = std::min<long long>((total + 255) / 256, 152LL * 64);
-    k_amr_corner_moments<<<(unsigned)blocks, 256, 0, c->stream>>>(
-        c->nvc, c->d_spec_start, c->d_spec_ent, c->d_cellM, c->d_cellJ, c->d_bdx, c->d_amrJ,
-        c->d_amrM);
+  if (!c->copy_stream) {
+    if ((st = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking),
+                         "copy stream")))
+      return st;
+    for (auto& e : c->copy_ev)
+      if ((st = cuda_check(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event")))
+        return st;
   }
-  if ((st = cuda_check(c, cudaGetLastError(), "amr_corner_moments"))) return st;
-  if (J && (st = cuda_check(c, cudaMemcpyAsync(J, c->d_amrJ, sizeof(double) * 3 * (size_t)c->nvc,
-                                               cudaMemcpyDeviceToHost, c->stream), "J")))
-    return st;
-  if (M && (st = cuda_check(c, cudaMemcpyAsync(M, c->d_amrM, sizeof(double) * 243 * (size_t)c->nvc,
-                                               cudaMemcpyDeviceToHost, c->stream), "M")))
-    return st;
-  return cuda_check(c, cudaStreamSynchronize(c->stream), "sync");
+  const long long per = (c->nvc + kCmChunks - 1) / kCmChunks;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < kCmChunks && e == cudaSuccess; k++) {
+    const long long a = std::min<long long>(c->nvc, k * per), b = std::min<long long>(c->nvc, a + per);
+    if (a >= b) break;
+    {
+      TimedLaunch t(c, "amr_corner_moments");
+      const long long blocks = std::min<long long>((b - a + kCmWarps - 1) / kCmWarps, 152LL * 8);
+      k_amr_corner_moments<<<(unsigned)blocks, kCmWarps * 32, 0, c->stream>>>(
+          a, b, c->d_spec_start, c->d_spec_ent, c->d_cellM, c->d_cellJ, c->d_bdx,
+          J ? c->d_amrJ : nullptr, M ? c->d_amrM : nullptr);
+    }
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(c->copy_ev[k], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->copy_ev[k], 0);
+    if (e == cudaSuccess && M)
+      e = cudaMemcpyAsync(M + a * 243, c->d_amrM + a * 243, sizeof(double) * 243 * (size_t)(b - a),
+                          cudaMemcpyDeviceToHost, c->copy_stream);
+    if (e == cudaSuccess && J)
+      e = cudaMemcpyAsync(J + a * 3, c->d_amrJ + a * 3, sizeof(double) * 3 * (size_t)(b - a),
+                          cudaMemcpyDeviceToHost, c->copy_stream);
+  }
+  // the context's stream resumes after the last copy
+  if (e == cudaSuccess) e = cudaEventRecord(c->copy_ev[kCmChunks], c->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->copy_ev[kCmChunks], 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_check(c, e, "export corner moments");
 }
 
 extern "C" {

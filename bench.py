@@ -591,6 +591,10 @@ def run_gpu(args):
     ctx, info = setup_workload(args.workload, local)
     npart, ncell, nblk = info["particles"], info["cells"], info["blocks"]
     tol = info["tol"]
+    if args.b_center:
+        # the reference's default build: B seen by the particles from the cell centres
+        ctx.set_b_center(True)
+    info["b_field"] = "cell centres" if args.b_center else "corners"
     # one field solve so the push sees a self-consistent E^{n+theta}
     ctx.UpdateJMassMatrix()
     tuning = ctx.autotune()
@@ -675,8 +679,10 @@ def run_gpu(args):
     # end to end through the reference-facing C ABI with host FP64 buffers in
     # page-locked memory: per step the host hands in the fields the push and
     # the deposit read (E^{n+theta}, corner B prev/cur) and reads back the
-    # moments the field solve needs (J and the mass matrix; per-cell partials
-    # on AMR meshes) -- the drop-in for MoveParticles + UpdateJMassMatrix with
+    # moments the field solve needs: corner J and the 243-term corner mass
+    # matrix, the node data UpdateJMassMatrix leaves at JxOffsetIndex /
+    # MassMatrixOffsetIndex (on AMR meshes summed over the cells of every
+    # unique corner) -- the drop-in for MoveParticles + UpdateJMassMatrix with
     # the particles resident on the device
     e2e = None
     e2e_particles = None
@@ -687,19 +693,13 @@ def run_gpu(args):
         hf = {k: pin.empty(f0[k].shape) for k in ("E_half", "B_corner_prev", "B_corner_cur")}
         for k in hf:
             hf[k][:] = f0[k]
-        if info["amr"]:
-            hJ, hM = pin.empty((ncell, 24)), pin.empty((ncell, 324))
-        else:
-            hJ, hM = pin.empty((ncell, 3)), pin.empty((ncell, 243))
+        hJ, hM = pin.empty((ctx.ncorners, 3)), pin.empty((ctx.ncorners, 243))
         ctx.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             ctx.import_fields(**hf)
             ctx.push_deposit(want_energy=False)
-            if info["amr"]:
-                ctx.export_cell_moments(out=(hJ, hM))
-            else:
-                ctx.export_moments(out=(hJ, hM))
+            ctx.export_moments(out=(hJ, hM))
         ctx.synchronize()
         e2e_s = time.perf_counter() - t0
         bi = int(sum(a.nbytes for a in hf.values()))
@@ -707,9 +707,8 @@ def run_gpu(args):
         e2e = {"value": npart * args.e2e_steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "steps": args.e2e_steps,
                "host_memory": "page-locked (cudaHostAlloc)",
-               "api": "amps_gpu_import_fields (E_half, B corner prev/cur) + amps_gpu_push_deposit + " +
-                      ("amps_gpu_export_cell_moments (J, M)" if info["amr"]
-                       else "amps_gpu_export_moments (J, M)")}
+               "api": "amps_gpu_import_fields (E_half, B corner prev/cur) + amps_gpu_push_deposit + "
+                      "amps_gpu_export_moments (corner J, M)"}
         pin.free()
         # the heavier round trip: every particle in and out through the FP64 AoS-style API
         exp = ctx.export_particles(ids=False)
@@ -919,6 +918,9 @@ def main():
     ap.add_argument("--precond-stiff", type=int, default=1,
                     help="also the same A/B at dt = 1/omega_pe")
     ap.add_argument("--graphs", type=int, default=1, help="particle step as a CUDA graph")
+    ap.add_argument("--b-center", type=int, default=0,
+                    help="1: the particles see B from the cell centres "
+                         "(_PIC_FIELD_SOLVER_B_CENTER_BASED_; uniform workloads)")
     ap.add_argument("--oracle-check", action="store_true",
                     help="run only the CPU baseline leg (one full ECSIM step on the GPU and "
                          "the FP64 oracle, parity errors) on --parity-workload")

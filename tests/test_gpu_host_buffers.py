@@ -56,3 +56,22 @@ def test_amr_cell_moments_pinned_equal_pageable():
         ctx.export_cell_moments(out=(qJ, qM))
         assert np.array_equal(J, qJ) and np.array_equal(M, qM)
     pin.free()
+
+
+def test_amr_corner_moments_pinned_equal_pageable():
+    """the corner-layout export written across the host link into page-locked
+    arrays equals the one copied through a device buffer, also mixed"""
+    mesh, wl, ic, x, f = amr_case(ppc=8)
+    pin = A.PinnedArrays()
+    with gpu_for(mesh, wl, ic, x, f) as ctx:
+        ctx.UpdateJMassMatrix()
+        J, M = ctx.export_moments()
+        pJ, pM = pin.empty(J.shape), pin.empty(M.shape)
+        ctx.export_moments(out=(pJ, pM))
+        assert np.array_equal(J, pJ) and np.array_equal(M, pM)
+        qJ, qM = np.empty(J.shape), pin.empty(M.shape)
+        ctx.export_moments(out=(qJ, qM))
+        assert np.array_equal(J, qJ) and np.array_equal(M, qM)
+        J1, _ = ctx.export_moments(with_m=False)
+        assert np.array_equal(J, J1)
+    pin.free()
