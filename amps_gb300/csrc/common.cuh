@@ -240,6 +240,7 @@ struct amps_gpu_ctx {
   bool spec_on = false;
   float* d_cellS = nullptr;     // [ncor][nspec][10][8] per-cell partials
   double* d_specC = nullptr;    // [10*nspec][nvc] corner values
+  float* d_bivh = nullptr;      // AMR: 1/dx^3 per block as an FP32 pair (hi nb, lo nb)
   double* d_amrJ = nullptr;     // AMR corner-layout moments (export_moments)
   double* d_amrM = nullptr;
   int* d_spec_start = nullptr;  // corner -> (cell*8 + corner-of-cell) CSR

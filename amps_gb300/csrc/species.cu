@@ -213,6 +213,8 @@ amps_gpu_status species_setup(amps_gpu_ctx* c, bool on) {
 }
 
 void species_free(amps_gpu_ctx* c) {
+  cudaFree(c->d_bivh);
+  c->d_bivh = nullptr;
   cudaFree(c->d_amrJ);
   cudaFree(c->d_amrM);
   c->d_amrJ = c->d_amrM = nullptr;
@@ -337,49 +339,65 @@ __global__ void __launch_bounds__(256) k_particle_cfl(CflArgs a) {
 // 3 dig(dy) + 9 dig(dz), dig(0) = 0, dig(-1) = 1, dig(+1) = 2, d the partner
 // corner's offset in the cell (IndexMatrix, :1889-1891) and the block the
 // cell's partial of the pair's weight monomial (already divided by V).  One
-// warp per corner: for each of the corner's cells (in CSR order) its 8 partner
-// corners x 9 components (distinct slots) are added to the corner's 243 + 3
-// FP64 sums in shared memory, which the warp then writes as one contiguous
-// run (whole lines across the host link for a page-locked destination).
-// Hanging corners get their own sums.  Corners [c0, c1); J or M may be null.
-constexpr int kCmWarps = 8;
-__device__ __forceinline__ int slot_digit(int d) { return d == 0 ? 0 : (d < 0 ? 1 : 2); }
-__global__ void __launch_bounds__(kCmWarps * 32) k_amr_corner_moments(
+// CTA per corner: thread t < 243 sums M element t over the corner's cells (in
+// CSR order, the cells whose pair lies inside them), threads 243..245 the J
+// components; the cells' entries are staged in shared memory first, so the
+// loads of the partials of all the corner's cells are independent.  The sums
+// are FP32 pairs (error-free TwoSum; J's 1/V an FP32 pair per block, ivh/ivl)
+// widened once: a warp-wide FP64 instruction occupies GB300's narrow FP64
+// pipe ~64x longer than an FP32 one, and FP64 adds and divides made this
+// kernel 8.6 ms per export of config 2.  Hanging corners get their own sums.
+// Corners [c0, c1); J or M may be null.
+constexpr int kCmThreads = 256;
+constexpr int kCmEnt = 32;  // entries staged per corner (more are read from global memory)
+__global__ void __launch_bounds__(kCmThreads) k_amr_corner_moments(
     long long c0, long long c1, const int* __restrict__ start, const int* __restrict__ ent,
-    const float* __restrict__ cellM, const float* __restrict__ cellJ, const double* __restrict__ bdx,
-    double* __restrict__ J, double* __restrict__ M) {
-  __shared__ double s_acc[kCmWarps][246];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* acc = s_acc[wid];
-  for (long long cc = c0 + (long long)blockIdx.x * kCmWarps + wid; cc < c1;
-       cc += (long long)gridDim.x * kCmWarps) {
-    for (int t = lane; t < 246; t += 32) acc[t] = 0.0;
-    __syncwarp();
-    const int e1 = start[cc + 1];
-    for (int e = start[cc]; e < e1; e++) {
-      const int en = ent[e];
-      const long long cell = en >> 3;
-      const int q = en & 7;  // the corner's offset bits in the cell (x, y, z)
-      if (M) {
-        for (int k = lane; k < 72; k += 32) {
-          const int q2 = k / 9, comp = k - 9 * q2;
-          const int ax = (q & 1) + (q2 & 1), ay = ((q >> 1) & 1) + ((q2 >> 1) & 1),
-                    az = (q >> 2) + (q2 >> 2);
-          const int slot = slot_digit((q2 & 1) - (q & 1)) + 3 * slot_digit(((q2 >> 1) & 1) - ((q >> 1) & 1)) +
-                           9 * slot_digit((q2 >> 2) - (q >> 2));
-          acc[slot * 9 + comp] += (double)cellM[cellM_at(cell, (ax + 3 * ay + 9 * az) * 9 + comp)];
-        }
-      }
-      if (J && lane < 3) {
-        const double dx = bdx[cell / AMPS_CPB];
-        acc[243 + lane] += (double)cellJ[cellJ_at(cell, (q ^ ((q >> 1) & 1)) * 3 + lane)] / (dx * dx * dx);
-      }
-      __syncwarp();
+    const float* __restrict__ cellM, const float* __restrict__ cellJ, const float* __restrict__ ivh,
+    const float* __restrict__ ivl, double* __restrict__ J, double* __restrict__ M) {
+  __shared__ int s_ent[kCmEnt];
+  __shared__ int s_rng[2];
+  const int t = threadIdx.x;
+  // this thread's M element: slot t / 9 (digits 0, 1, 2 = offsets 0, -1, +1), component t % 9
+  const int slot = t / 9, comp = t - 9 * slot;
+  const int dg[3] = {slot % 3, (slot / 3) % 3, slot / 9};
+  int d[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) d[a] = dg[a] == 0 ? 0 : (dg[a] == 1 ? -1 : 1);
+  for (long long cc = c0 + blockIdx.x; cc < c1; cc += gridDim.x) {
+    if (t == 0) {
+      s_rng[0] = start[cc];
+      s_rng[1] = start[cc + 1];
     }
-    if (M)
-      for (int t = lane; t < 243; t += 32) M[cc * 243 + t] = acc[t];
-    if (J && lane < 3) J[cc * 3 + lane] = acc[243 + lane];
-    __syncwarp();
+    __syncthreads();
+    const int e0 = s_rng[0], ne = s_rng[1] - s_rng[0];
+    if (t < ne && t < kCmEnt) s_ent[t] = ent[e0 + t];
+    __syncthreads();
+    FF sum{0.f, 0.f};
+    if (t < 243) {
+      if (M) {
+#pragma unroll 4
+        for (int e = 0; e < ne; e++) {
+          const int en = e < kCmEnt ? s_ent[e] : ent[e0 + e];
+          const int q = en & 7;  // the corner's offset bits in the cell (x, y, z)
+          const int o0 = (q & 1) + d[0], o1 = ((q >> 1) & 1) + d[1], o2 = (q >> 2) + d[2];
+          if ((unsigned)o0 > 1u || (unsigned)o1 > 1u || (unsigned)o2 > 1u) continue;
+          const int mono = ((q & 1) + o0) + 3 * (((q >> 1) & 1) + o1) + 9 * ((q >> 2) + o2);
+          ff_acc(sum, cellM[cellM_at(en >> 3, mono * 9 + comp)], 0.f);
+        }
+        M[cc * 243 + t] = widen(sum.s) + widen(sum.q);
+      }
+    } else if (t < 246 && J) {
+      const int jc = t - 243;
+      for (int e = 0; e < ne; e++) {
+        const int en = e < kCmEnt ? s_ent[e] : ent[e0 + e];
+        const long long cell = en >> 3;
+        const int q = en & 7, b = (int)(cell / AMPS_CPB);
+        const FF p = ff_mul(cellJ[cellJ_at(cell, (q ^ ((q >> 1) & 1)) * 3 + jc)], 0.f, ivh[b], ivl[b]);
+        ff_acc(sum, p.s, p.q);
+      }
+      J[cc * 3 + jc] = widen(sum.s) + widen(sum.q);
+    }
+    __syncthreads();  // s_rng and s_ent are rewritten for the next corner
   }
 }
 
@@ -402,6 +420,27 @@ amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M)
       return set_err(c, AMPS_GPU_CUDA_ERROR, "export_moments: allocation failed");
     }
   }
+  if (!c->d_bivh) {
+    // 1/dx^3 per block as an FP32 pair
+    std::vector<double> bdx((size_t)c->nb);
+    if ((st = cuda_check(c, cudaMemcpy(bdx.data(), c->d_bdx, sizeof(double) * bdx.size(),
+                                       cudaMemcpyDeviceToHost), "block sizes")))
+      return st;
+    std::vector<float> iv(2 * bdx.size());
+    for (size_t b = 0; b < bdx.size(); b++) {
+      const double v = 1.0 / (bdx[b] * bdx[b] * bdx[b]);
+      iv[b] = (float)v;
+      iv[bdx.size() + b] = (float)(v - (double)iv[b]);
+    }
+    if (cudaMalloc(reinterpret_cast<void**>(&c->d_bivh), sizeof(float) * iv.size()) != cudaSuccess) {
+      cudaGetLastError();
+      c->d_bivh = nullptr;
+      return set_err(c, AMPS_GPU_CUDA_ERROR, "export_moments: allocation failed");
+    }
+    if ((st = cuda_check(c, cudaMemcpy(c->d_bivh, iv.data(), sizeof(float) * iv.size(),
+                                       cudaMemcpyHostToDevice), "block volumes")))
+      return st;
+  }
   if (!c->copy_stream) {
     if ((st = cuda_check(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking),
                          "copy stream")))
@@ -417,9 +456,9 @@ amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M)
     if (a >= b) break;
     {
       TimedLaunch t(c, "amr_corner_moments");
-      const long long blocks = std::min<long long>((b - a + kCmWarps - 1) / kCmWarps, 152LL * 8);
-      k_amr_corner_moments<<<(unsigned)blocks, kCmWarps * 32, 0, c->stream>>>(
-          a, b, c->d_spec_start, c->d_spec_ent, c->d_cellM, c->d_cellJ, c->d_bdx,
+      const long long blocks = std::min<long long>(b - a, 152LL * 8);
+      k_amr_corner_moments<<<(unsigned)blocks, kCmThreads, 0, c->stream>>>(
+          a, b, c->d_spec_start, c->d_spec_ent, c->d_cellM, c->d_cellJ, c->d_bivh, c->d_bivh + c->nb,
           J ? c->d_amrJ : nullptr, M ? c->d_amrM : nullptr);
     }
     e = cudaGetLastError();
