@@ -90,6 +90,13 @@ def sum_over_ranks(dist, val):
     return float(t.item())
 
 
+def replica_throughput(dist, units, ms):
+    """Whole-job throughput of N independent replicas: the units all ranks
+    processed over the slowest rank's time.  Returns (units/s, max ms)."""
+    ms_max = max_over_ranks(dist, ms)
+    return sum_over_ranks(dist, units) / (ms_max / 1e3), ms_max
+
+
 # ---------------------------------------------------------------------------
 class CudaEvents:
     """CUDA events on an external stream through the runtime library."""
@@ -629,9 +636,7 @@ def run_gpu(args):
         ctx.push_deposit(want_energy=False)
     ktimes = ctx.kernel_times()
     ctx.set_kernel_timing(False)
-    ms_max = max_over_ranks(dist, ms)
-    total_ps = sum_over_ranks(dist, float(npart) * args.steps)
-    value = total_ps / (ms_max / 1e3)
+    value, ms_max = replica_throughput(dist, float(npart) * args.steps, ms)
 
     # full ECSIM step (field solve + push + deposit), Jacobi GMRES
     t_step = []
