@@ -700,17 +700,23 @@ def run_gpu(args):
             hf[k][:] = f0[k]
         hJ, hM = pin.empty((ctx.ncorners, 3)), pin.empty((ctx.ncorners, 243))
         ctx.synchronize()
+        t_exp = 0.0  # the export calls alone (each returns with its copies complete)
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             ctx.import_fields(**hf)
             ctx.push_deposit(want_energy=False)
+            t1 = time.perf_counter()
             ctx.export_moments(out=(hJ, hM))
+            t_exp += time.perf_counter() - t1
         ctx.synchronize()
         e2e_s = time.perf_counter() - t0
         bi = int(sum(a.nbytes for a in hf.values()))
         bo = int(hJ.nbytes + hM.nbytes)
         e2e = {"value": npart * args.e2e_steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "steps": args.e2e_steps,
+               "ms_per_step": round(e2e_s / args.e2e_steps * 1e3, 3),
+               "export_ms": round(t_exp / args.e2e_steps * 1e3, 3),
+               "export_gbs": round(bo * args.e2e_steps / t_exp / 1e9, 1),
                "host_memory": "page-locked (cudaHostAlloc)",
                "api": "amps_gpu_import_fields (E_half, B corner prev/cur) + amps_gpu_push_deposit + "
                       "amps_gpu_export_moments (corner J, M)"}
