@@ -59,7 +59,7 @@ struct amps_gpu_ctx {
   // device-to-host copies that overlap the producing kernels (created on
   // first use) and the events that order them, one per chunk
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t copy_ev[9] = {nullptr};
+  cudaEvent_t copy_ev[17] = {nullptr};
   std::string err;
 
   // mesh

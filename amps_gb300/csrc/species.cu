@@ -406,7 +406,9 @@ __global__ void __launch_bounds__(kCmThreads) k_amr_corner_moments(
 // device buffer in kCmChunks corner ranges; each range's copy to the host
 // runs on the copy stream while the kernel produces the next, so a
 // page-locked destination fills at the host link's rate.
-constexpr int kCmChunks = 8;
+constexpr int kCmChunks = 16;
+static_assert(sizeof(amps_gpu_ctx::copy_ev) / sizeof(cudaEvent_t) >= kCmChunks + 1,
+              "one event per export chunk and one for the end");
 amps_gpu_status amr_export_corner_moments(amps_gpu_ctx* c, double* J, double* M) {
   amps_gpu_status st = corner_csr_setup(c);
   if (st) return st;
