@@ -123,3 +123,32 @@ def test_center_b_rejected_on_amr():
     with pytest.raises(A.AmpsGpuError):
         ctx.set_b_center(True)
     ctx.set_b_center(False)
+
+
+def test_center_b_open_axes_and_graphs():
+    """open x and z (fast particles leave and are deleted) with centre B, the
+    step as a CUDA graph: the surviving set, states and moments match the
+    centre-B oracle over two steps"""
+    lib = O.load()
+    lib.orc_set_open_axes(1 | 4)
+    try:
+        wl, ic, x, f, ctx, st = centre_case(vscale=40.0)
+        ctx.set_open_axes(True, False, True)
+        ctx.set_graphs(True)
+        for step in range(2):
+            eg = ctx.push_deposit()
+            st.push()
+            eo = st.deposit()
+            alive = st.block >= 0
+            assert ctx.num_particles() == int(alive.sum())
+            g = G.by_id(ctx.export_particles())
+            np.testing.assert_array_equal(g["id"], np.flatnonzero(alive))
+            L = np.array(wl.mesh.shape) * wl.mesh.dx
+            d = np.abs(g["x"] - st.x[alive])
+            d = np.minimum(d, np.abs(d - L))
+            assert d.max() <= 4e-6 * (step + 1)
+            assert np.abs(g["v"] - st.v[alive]).max() <= 2e-5 * np.abs(st.v).max()
+            check_moments(ctx, st, eg, eo)
+        assert (st.block < 0).sum() > 100
+    finally:
+        lib.orc_set_open_axes(0)

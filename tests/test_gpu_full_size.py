@@ -26,7 +26,10 @@ from tests import parity as P
 pytestmark = pytest.mark.gpu
 
 
-def test_uniform_plasma_two_steps_full_size():
+@pytest.mark.parametrize("b_center", [False, True], ids=["corner_B", "centre_B"])
+def test_uniform_plasma_two_steps_full_size(b_center):
+    """b_center: the particles see B from the cell centres (the reference's
+    default configuration) on the GPU and in the oracle"""
     wl = A.WORKLOADS["ecsim_32c_64ppc"]()
     ic = A.make_initial_condition(wl, nthreads=os.cpu_count() or 4)
     x = A.physical_positions(wl.mesh, ic["u"], ic["block"])
@@ -38,7 +41,8 @@ def test_uniform_plasma_two_steps_full_size():
     try:
         ctx.import_particles(x, v, ic["spec"])
         ctx.import_fields(**f)
-        st = O.OracleState(wl, x, v, ic["spec"], f)
+        ctx.set_b_center(b_center)
+        st = O.OracleState(wl, x, v, ic["spec"], f, b_center=b_center)
         eg = ctx.UpdateJMassMatrix()
         eo = st.deposit()
         assert eg == pytest.approx(eo, rel=1e-6)
