@@ -186,16 +186,16 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------
-def kernel_bytes(n, ncell, nb, name):
+def kernel_bytes(n, ncell, nb, name, b_center=False):
     """Algorithmic bytes per launch of each particle-step kernel: what the
     kernel must read and write given the slotted cell layout (n particles,
-    ncell cells, nb blocks)."""
+    ncell cells, nb blocks; b_center: B from the cell centres)."""
     ctas = nb * 8
     if name == "push_deposit":
         # particles: read u,v (24) + species (1), write u,v (24); per cell: base, cnt
         # (8), stay (4), partials 267 floats (27 monomials x 9 + 8 corners x 3);
-        # stencils 23.3 + 11.7 KB per CTA
-        return n * 49 + ncell * (12 + 267 * 4) + ctas * (23328 + 11664)
+        # stencils 23.3 + 11.7 KB per CTA (centre B: 23.3 + 2 x 16 KB)
+        return n * 49 + ncell * (12 + 267 * 4) + ctas * (23328 + (32000 if b_center else 11664))
     if name == "arrivals":
         # per cell: base, base+1, cnt, stay, arr (20) and cnt/arr writes (8); the
         # ~1% arrivals and their partial read-modify-write; stencil per CTA
@@ -749,7 +749,7 @@ def run_gpu(args):
     top = max(per, key=lambda k: per[k][0])
     ms_top, launches = per[top]
     nl = max(1, launches)
-    nbytes = kernel_bytes(npart, ncell, nblk, top)
+    nbytes = kernel_bytes(npart, ncell, nblk, top, bool(args.b_center))
     traffic = args.traffic
     traffic_src = "--traffic" if traffic is not None else None
     if traffic is None and top in MEASURED_TRAFFIC.get(args.workload, {}):
