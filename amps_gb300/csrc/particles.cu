@@ -5,25 +5,36 @@
 // (species byte 0xFF marks an empty slot).  Almost every particle stays in its
 // cell during a step, so the step never re-sorts the whole population:
 //
-//   k_push_deposit<DEP>  one warp per cell: Lapenta2017 push of the cell's
+//   k_push_deposit<DEP,AMR,CB>
+//                        one warp per cell: Lapenta2017 push of the cell's
 //                        particles (src/pic/pic_mover_boris.cpp:876-1120) with
 //                        E^{n+theta} and corner B^n gathered from a per-block
-//                        stencil staged by one bulk (TMA) copy; particles that
-//                        stay are compacted in place and, when DEP, deposited
-//                        right away with ProcessCell's terms
+//                        stencil staged by one bulk (TMA) copy (CB: B^n from a
+//                        staged stencil of the block's cell centres,
+//                        CellCentered::Linear); particles that stay are
+//                        compacted in place and, when DEP, deposited right away
+//                        with ProcessCell's terms
 //                        (pic_field_solver_ecsim.cpp:1882-2438); particles that
 //                        leave are written into the slack of their destination
 //                        cell (findTreeNode/FindCellIndex rules,
 //                        meshAMRgeneric.h:2256-2320,2852-2883, periodic wrap of
 //                        pic_bc_periodic.cpp:86-178), or to an overflow list
-//   k_arrivals<DEP>      one warp per cell: deposits the particles that arrived,
-//                        moves them behind the stayers, updates cnt
-//   k_deposit            full ProcessCell pass over the compact layout
+//   k_arrivals<DEP,CHUNK,CB>
+//                        one CTA per block layer: the cells with arrivals are
+//                        listed, warps take them from a shared counter, deposit
+//                        the arrivals, move them behind the stayers, update cnt
+//   k_ovf_place, k_relayout_cells
+//                        slack overflow: overflowed arrivals into the slots
+//                        their cells' movers vacated (deposited there); when a
+//                        cell is full, every cell copied to new offsets in the
+//                        other buffer
+//   k_deposit<CB>        full ProcessCell pass over the compact layout
 //                        (UpdateJMassMatrix without a preceding push)
 //   k_assemble           per-cell partial sums -> 243-term corner mass matrix
 //                        and corner J in FP64 (:2362-2426, shared corners summed)
 //   rebuild              counting sort of an unsorted list into the slotted
-//                        layout: import, and recovery when slack overflows
+//                        layout: import, and the positions the div E
+//                        correction moves
 //
 // Deposition arithmetic: per particle the 27 distinct trilinear weight
 // monomials, k*alpha (9), the 8 corner weights and q*alpha*v are staged in
