@@ -219,7 +219,10 @@ amps_gpu_status amps_gpu_export_fields(amps_gpu_ctx* ctx, double* E_n, double* E
  * mesh's unique corners (J[corner][3], M[corner][243]), each corner the sum of
  * ProcessCell's flush (pic_field_solver_ecsim.cpp:2362-2426) over the cells of
  * any level that have it -- hanging corners included, with their own sums --
- * so an AMR run can take J and M back into its corner nodes. */
+ * so an AMR run can take J and M back into its corner nodes.  Either pointer
+ * may be NULL.  Page-locked host arrays (cudaHostAlloc / cudaHostRegister)
+ * fill at the host link's rate: the AMR corner sums are made in corner ranges
+ * whose copies overlap the next range's kernel. */
 amps_gpu_status amps_gpu_import_moments(amps_gpu_ctx* ctx, const double* J, const double* M);
 amps_gpu_status amps_gpu_export_moments(amps_gpu_ctx* ctx, double* J, double* M);
 /* Tecplot ASCII output of the corner fields in the layout of the reference's
