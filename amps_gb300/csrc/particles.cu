@@ -688,15 +688,17 @@ __global__ void k_step_bump(unsigned long long* step, const unsigned long long* 
 // a shared counter, so a few busy cells do not hold idle warps at the CTA's
 // final barrier.  Arrivals are few per cell (a few % of its particles), so
 // records are staged in chunks of CHUNK lanes: at 16, a smaller record buffer
-// and a register cap let 3 CTAs share an SM, which hides more of the per-cell
-// load latency; 32 (2 CTAs per SM) halves the chunks of cells with many
-// arrivals.  The autotuner picks one on the run's own steps.
+// and a 64-register cap (56 bytes of spills) let 4 CTAs share an SM, which
+// hides more of the per-cell load latency (0.29 against 0.32 ms per launch
+// with 3 CTAs on the 67.1M-particle AMR plasma); 32 (2 CTAs per SM) halves the
+// chunks of cells with many arrivals.  The autotuner picks one on the run's
+// own steps.
 constexpr int kArrChunk = 16;
 constexpr int kFSArr = kArrChunk + 4;  // field stride of staged fields at 16 lanes
 constexpr int kLayer = AMPS_NC * AMPS_NC;
 
 template <bool DEP, int CHUNK, bool CB = false>
-__global__ void __launch_bounds__(256, CHUNK == 16 ? 3 : 2) k_arrivals(StepArgs a) {
+__global__ void __launch_bounds__(256, CHUNK == 16 ? 4 : 2) k_arrivals(StepArgs a) {
   constexpr int FS = CHUNK + 4;  // field stride of the staged fields
   extern __shared__ __align__(16) float4 s_dyn[];
   float* s_rec = reinterpret_cast<float*>(s_dyn);
