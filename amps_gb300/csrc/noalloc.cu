@@ -19,7 +19,8 @@
 //     (a block whose stencil copy timed out fills its cells' partials with
 //     NaN), so no state leaks from one call into the next;
 //   * the first call on a device resolves the array's device address with
-//     cudaGetSymbolAddress; make that first call before any stream capture.
+//     cudaGetSymbolAddress, which must not run while a stream of that device
+//     is being captured.
 //   * the caller's current device is restored before the call returns.
 #include <cuda_runtime.h>
 

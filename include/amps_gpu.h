@@ -486,8 +486,9 @@ amps_gpu_status amps_gpu_precond_forward(amps_gpu_ctx* ctx, long long count, con
  * meshes return AMPS_GPU_INVALID_ARG.  All calls share it, so calls that
  * overlap on the GPU race; each call writes the scratch it reads before
  * reading it, so nothing carries over between calls.  The first call on a
- * device looks up the array's address (cudaGetSymbolAddress); make it before
- * any stream capture.  The caller's current device is restored on return.
+ * device looks up the array's address (cudaGetSymbolAddress), which must not
+ * run while a stream of that device is being captured.  The caller's current
+ * device is restored on return.
  * Inputs (device pointers, asynchronous on `stream`): particles sorted by cell
  * key block*512 + (i + 8*(j + 8*k)), d_cell_start[ncell+1] their offsets; d_u,
  * d_v structure-of-arrays of length 3n (x[n], y[n], z[n]) with u the FP32
