@@ -1,8 +1,8 @@
 // Device code shared by the particle kernels (particles.cu) and the
 // no-allocation deposition entry point (noalloc.cu): species constants, the
 // bulk-copy staging of block stencils, the per-particle deposition fields,
-// the register-tile accumulation (packed FP32x2 FMAs) with Kahan-compensated
-// chunk sums, and FP32 -> FP64 widening.
+// the register-tile accumulation (packed FP32x2 FMAs) with FP32 chunk sums,
+// and FP32 -> FP64 widening.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -240,13 +240,16 @@ __device__ __forceinline__ void ffma2(unsigned long long& d, unsigned long long 
 // shared loads (4 positions of each of its 3 + 3 fields) and 18 packed FMAs,
 // the even and odd positions accumulated in the two halves of each pair.
 struct Tile {
-  float sum[9], cmp[9];
+  float sum[9];
   __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int e = 0; e < 9; e++) { sum[e] = 0.f; cmp[e] = 0.f; }
+    for (int e = 0; e < 9; e++) sum[e] = 0.f;
   }
-  // accumulate the staged positions [0, npos) (npos a multiple of 4), then
-  // compensated add
+  // accumulate the staged positions [0, npos) (npos a multiple of 4) and add
+  // the chunk's sums.  A Kahan-compensated add here changed the full-size
+  // per-cell J and M errors against the FP64 oracle in no printed digit
+  // (4.6e-7, 1.0e-6 at 128 particles per cell; the FP32 positions dominate)
+  // and cost 4 % of the push/deposit kernel's time.
   template <int FS>
   __device__ __forceinline__ void accumulate(const float* __restrict__ rec, int npos, int fA,
                                              int fB) {
@@ -277,10 +280,7 @@ struct Tile {
 #pragma unroll
     for (int e = 0; e < 9; e++) {
       const float2 a = *reinterpret_cast<const float2*>(&acc[e]);
-      const float y = (a.x + a.y) - cmp[e];
-      const float t = sum[e] + y;
-      cmp[e] = (t - sum[e]) - y;
-      sum[e] = t;
+      sum[e] += a.x + a.y;
     }
   }
   // write the tile's sums to the cell partials
@@ -292,7 +292,7 @@ struct Tile {
       for (int q = 0; q < 3; q++)
 #pragma unroll
         for (int e = 0; e < 3; e++)
-          cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)] = sum[3 * q + e] - cmp[3 * q + e];
+          cellM[cellM_at(cid, (3 * g + q) * 9 + 3 * hh + e)] = sum[3 * q + e];
     } else if (lane < kTileLanes) {
       const int g = lane - 27;
 #pragma unroll
@@ -300,7 +300,7 @@ struct Tile {
         if (3 * g + q < 8)
 #pragma unroll
           for (int e = 0; e < 3; e++)
-            cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)] = sum[3 * q + e] - cmp[3 * q + e];
+            cellJ[cellJ_at(cid, (3 * g + q) * 3 + e)] = sum[3 * q + e];
     }
   }
   // add the tile's sums to the cell partials by global reductions, which the
@@ -317,7 +317,7 @@ struct Tile {
 #pragma unroll
       for (int q = 0; q < 3; q++)
 #pragma unroll
-        for (int e = 0; e < 3; e++) scr[(3 * g + q) * 9 + 3 * hh + e] = sum[3 * q + e] - cmp[3 * q + e];
+        for (int e = 0; e < 3; e++) scr[(3 * g + q) * 9 + 3 * hh + e] = sum[3 * q + e];
     } else if (lane < kTileLanes) {
       const int g = lane - 27;
 #pragma unroll
@@ -325,7 +325,7 @@ struct Tile {
         if (3 * g + q < 8)
 #pragma unroll
           for (int e = 0; e < 3; e++)
-            scr[AMPS_CELLM + (3 * g + q) * 3 + e] = sum[3 * q + e] - cmp[3 * q + e];
+            scr[AMPS_CELLM + (3 * g + q) * 3 + e] = sum[3 * q + e];
     }
     __syncwarp();
     float* m = cellM + cellM_at(cid, 0);

@@ -40,8 +40,7 @@
 // monomials, k*alpha (9), the 8 corner weights and q*alpha*v are staged in
 // shared memory; 27 lanes each own a 3 x 3 tile of the 27x9 monomial block of
 // the mass matrix and 3 lanes a 3 x 3 tile of the 8x3 current block, and
-// accumulate it in registers over chunks of 32 particles, adding chunk sums
-// with Kahan compensation (deposit_core.cuh).
+// accumulate it in registers over chunks of 32 particles (deposit_core.cuh).
 #include <cuda_runtime.h>
 
 #include <algorithm>
