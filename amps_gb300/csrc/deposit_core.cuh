@@ -258,16 +258,16 @@ struct Tile {
     for (int e = 0; e < 9; e++) acc[e] = 0ull;
     const float* pa = rec + fA * FS;
     const float* pb = rec + fB * FS;
-#pragma unroll 2
-    for (int r = 0; r < npos; r += 4) {
+    // four staged positions: six 16-byte loads, 18 packed FMAs -- the 9
+    // positions-(r, r+1) products first, then the 9 (r+2, r+3) ones: 9
+    // independent accumulators between dependent packed FMAs
+    auto four = [&](int r) {
       ulonglong2 A[3], B[3];
 #pragma unroll
       for (int q = 0; q < 3; q++) {
         A[q] = *reinterpret_cast<const ulonglong2*>(pa + q * FS + r);
         B[q] = *reinterpret_cast<const ulonglong2*>(pb + q * FS + r);
       }
-      // the 9 positions-(r, r+1) products first, then the 9 (r+2, r+3) ones:
-      // 9 independent accumulators between dependent packed FMAs
 #pragma unroll
       for (int q = 0; q < 3; q++)
 #pragma unroll
@@ -276,6 +276,14 @@ struct Tile {
       for (int q = 0; q < 3; q++)
 #pragma unroll
         for (int e = 0; e < 3; e++) ffma2(acc[3 * q + e], A[q].y, B[e].y);
+    };
+    if (npos == FS - 4) {
+      // a full chunk: no loop control
+#pragma unroll
+      for (int r = 0; r < FS - 4; r += 4) four(r);
+    } else {
+#pragma unroll 2
+      for (int r = 0; r < npos; r += 4) four(r);
     }
 #pragma unroll
     for (int e = 0; e < 9; e++) {

@@ -42,7 +42,8 @@ METRIC = "particle-steps/s (push+deposit)"
 # particle-step kernels on the default workload, from a one-pass ncu capture
 # of this bench command; "version" names the kernel revision it was taken on
 MEASURED_TRAFFIC = {"amr_64c_128ppc": {"version": "push_deposit packed-FMA 3x3 tiles on SoA "
-                                                  "records, FP32 chunk sums; arrivals from a "
+                                                  "records, FP32 chunk sums, unrolled full chunks; "
+                                                  "arrivals from a "
                                                   "per-layer cell list",
                                        "push_deposit": 4.663e9, "arrivals": 1.015e9}}
 UNIT = "particle-steps/s"
