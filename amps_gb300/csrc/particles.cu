@@ -412,7 +412,8 @@ __global__ void __launch_bounds__(256, 2) k_push_deposit(StepArgs a) {
                           stays ? wcv : 0.f, i, j, k, a.st, inv_vol, en_row);
       // movers: slack of the destination cell, else the overflow list
       const bool mover = act && !stays && key >= 0;
-      const int slot = warp_reserve(mover, mover ? key : 0, a.arr);
+      // one reservation per mover (a chunk has a few): no warp-wide key match
+      const int slot = mover ? atomicAdd(a.arr + key, 1) : 0;
       if (mover) {
         const int cb = a.base[key], ccap = a.base[key + 1] - cb, cn = a.cnt[key];
         if (slot < ccap - cn) {
