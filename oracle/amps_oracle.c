@@ -261,6 +261,18 @@ static void centre_b(const orc_mesh* g, const int bxyz[3], const double xmin[3],
       }
 }
 
+/* B at each of n points x[3n] (located in block[n]) from the cell-centred
+ * field Bc, by the stencil above (a check of the centre-B restatement) */
+void orc_centre_b_at(const orc_mesh* g, long n, const double* x, const int32_t* block,
+                     const double* Bc, double* B) {
+  for (long p = 0; p < n; p++) {
+    int bxyz[3];
+    double xmin[3];
+    block_geom(g, block[p], bxyz, xmin);
+    centre_b(g, bxyz, xmin, x + 3 * p, Bc, B + 3 * p);
+  }
+}
+
 /* Lapenta2017 (pic_mover_boris.cpp:876-1375) for every particle, followed by
  * the re-binning of the moved particle.  Returns the number of particles that
  * were found outside their block on entry (the reference aborts there). */

@@ -56,6 +56,9 @@ void orc_graddiv_table(int p, int q, double out[27]);
  * arrays interpolated from the cell centres (_PIC_FIELD_SOLVER_B_CENTER_BASED_);
  * 0 (default): corner arrays */
 void orc_set_b_center(int on);
+/* B at n located points from a cell-centred field (the centre-B stencil) */
+void orc_centre_b_at(const orc_mesh* g, long n, const double* x, const int32_t* block,
+                     const double* Bc, double* B);
 void orc_corner_weights(const double xloc[3], double w_table[8]);
 long orc_push(const orc_mesh* g, long n, double* x, double* v, const uint8_t* spec,
               int32_t* block, int32_t* cell, const double* E_half, const double* Bc_prev);

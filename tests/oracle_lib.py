@@ -55,6 +55,7 @@ def load():
         "orc_species_moments": (None, [C.POINTER(Mesh), C.c_long, D, D, U8, D, I32, I32, D]),
         "orc_set_open_axes": (None, [C.c_int]),
         "orc_set_b_center": (None, [C.c_int]),
+        "orc_centre_b_at": (None, [C.POINTER(Mesh), C.c_long, D, C.POINTER(C.c_int32), D, D]),
         "orc_inject": (C.c_long, [C.POINTER(Mesh), C.c_int, C.c_int, C.c_double, D, C.c_double,
                                   C.c_ulonglong, C.c_ulonglong, C.c_int, D, D, C.c_long, D, D, I32,
                                   I32]),

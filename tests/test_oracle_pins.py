@@ -355,3 +355,40 @@ def test_lapenta2017_center_b_matches_reference_build():
             assert rel(v, np.array([r["v"] for r in recs])) < 1e-13
     finally:
         lib.orc_set_b_center(0)
+
+
+def test_oracle_centre_b_stencil_exact_for_linear_fields():
+    """CellCentered::Linear's trilinear stencil over cell centres reproduces a
+    field linear in position wherever the stencil does not wrap (points at
+    least 1.5 cells from the domain faces, across block boundaries too), and a
+    constant field everywhere, the periodic wrap included (its weights sum to 1)"""
+    import amps_gb300 as A
+    wl = A.electron_proton_plasma("centre-b", 2, 2, 2, 1, 3)
+    lib = O.load()
+    m = O.mesh_of(wl)
+    shp = wl.mesh.shape  # cells per axis
+    dx, x0 = wl.mesh.dx, np.array(wl.mesh.x0, float)
+    I, J, K = np.meshgrid(np.arange(shp[0]), np.arange(shp[1]), np.arange(shp[2]), indexing="ij")
+    # cell-centre coordinates in the oracle's order I + NX (J + NY K)
+    xc = np.stack([(I.ravel(order="F") + 0.5), (J.ravel(order="F") + 0.5),
+                   (K.ravel(order="F") + 0.5)], axis=1) * dx + x0
+    rng = np.random.default_rng(7)
+    a = rng.standard_normal(3)
+    G = rng.standard_normal((3, 3))
+    Bc = np.ascontiguousarray(a + xc @ G.T)
+    L = np.array(shp, float) * dx
+    n = 4000
+    x = x0 + 1.5 * dx + rng.random((n, 3)) * (L - 3.0 * dx)
+    x = np.ascontiguousarray(x)
+    block = np.zeros(n, np.int32)
+    cell = np.zeros(n, np.int32)
+    lib.orc_locate(O.C.byref(m), n, O.p(x), O.p(block, O.C.c_int32), O.p(cell, O.C.c_int32))
+    B = np.zeros((n, 3))
+    lib.orc_centre_b_at(O.C.byref(m), n, O.p(x), O.p(block, O.C.c_int32), O.p(Bc), O.p(B))
+    np.testing.assert_allclose(B, a + x @ G.T, rtol=0, atol=1e-12 * np.abs(Bc).max())
+    # a constant field, points anywhere (stencils that wrap the periodic faces)
+    xa = np.ascontiguousarray(x0 + rng.random((n, 3)) * L)
+    lib.orc_locate(O.C.byref(m), n, O.p(xa), O.p(block, O.C.c_int32), O.p(cell, O.C.c_int32))
+    Bk = np.ascontiguousarray(np.broadcast_to(a, Bc.shape))
+    lib.orc_centre_b_at(O.C.byref(m), n, O.p(xa), O.p(block, O.C.c_int32), O.p(Bk), O.p(B))
+    np.testing.assert_allclose(B, np.broadcast_to(a, B.shape), rtol=0, atol=1e-14)
