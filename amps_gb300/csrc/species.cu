@@ -16,6 +16,14 @@
 //
 // Runs after the deposition when sampling is on (amps_gpu_set_species_moments);
 // costs one more read of the particle state.
+//
+// Also here, on the same corner CSR:
+//   k_amr_corner_moments  AMR contexts' J and M in the corner layout
+//                     (amps_gpu_export_moments): one CTA per corner, FP32-pair
+//                     sums of the cells' partials, written in corner ranges
+//                     whose host copies overlap the next range's kernel
+//   k_particle_cfl    the per-species maximum of ProcessCell's cflCell
+//                     (amps_gpu_particle_cfl)
 #include <cuda_runtime.h>
 
 #include <algorithm>
